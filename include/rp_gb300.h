@@ -1,0 +1,329 @@
+/*
+ * rp_gb300.h -- C ABI of the GB300 (sm_103a) non-sequential ray-tracing hot path.
+ *
+ * This library replaces raypier's Cython hot path
+ *   raypier/core/ctracer.pyx:2062-2118   trace_segment_c
+ *   raypier/core/ctracer.pyx:2173-2182   trace_segment (Python entry)
+ *   raypier/core/tracer.py:9-47          trace_rays (generation driver)
+ * and the per-face / per-material plugin calls it dispatches to
+ *   raypier/core/ctracer.pxd:231-235     Face.intersect_c / compute_normal_c / compute_tangent_c
+ *   raypier/core/ctracer.pxd:189-193     InterfaceMaterial.eval_child_ray_c
+ *   raypier/core/ctracer.pxd:212-213     Shape.point_inside_c
+ *   raypier/core/ctracer.pxd:207-209     Distortion.z_offset_and_gradient_c / z_offset_c
+ * The reference dispatches through Cython virtual methods; here a scene is a set
+ * of plain tables (faces, face lists, materials, shapes, distortions, dispersion
+ * curves) and each face/material/shape/distortion is selected by a type tag.
+ *
+ * Conventions: every entry point returns an int status (RP_OK == 0, negative on
+ * error); no C++ exception crosses this boundary.  The context owns all device
+ * memory; the caller owns every host buffer it passes.  A context is bound to one
+ * CUDA device and one stream and is not thread-safe.
+ */
+#ifndef RP_GB300_H
+#define RP_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RP_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+#define RP_OK               0
+#define RP_ERR_INVALID     -1   /* bad argument or malformed scene            */
+#define RP_ERR_CAPACITY    -2   /* an output buffer is too small              */
+#define RP_ERR_BUDGET      -3   /* the context's device-memory budget is hit  */
+#define RP_ERR_TIMEOUT     -4   /* a bounded device-side wait gave up         */
+#define RP_ERR_CUDA        -5   /* a CUDA runtime call failed                 */
+#define RP_ERR_UNSUPPORTED -6   /* face/material/shape type not implemented   */
+#define RP_ERR_NOMEM       -7   /* host allocation failed                     */
+
+/* ---- ray record --------------------------------------------------------- */
+/* Byte-identical to ctracer.ray_t / ctracer.ray_dtype: 188 bytes, packed
+ * (raypier/core/ctracer.pxd:40-48, raypier/core/ctracer.pyx:45-60). */
+#pragma pack(push, 1)
+typedef struct rp_ray {
+    double origin[3], direction[3], normal[3], E_vector[3];
+    double refractive_index[2], E1_amp[2], E2_amp[2];   /* complex: re, im */
+    double length, phase, accumulated_path;
+    uint32_t wavelength_idx, parent_idx, end_face_idx, ray_ident, ray_type_id;
+} rp_ray;
+#pragma pack(pop)
+
+#define RP_RAY_BYTES 188
+#define RP_REFL_RAY  1u          /* ctracer.pyx:19 REFL_RAY */
+#define RP_NO_FACE   0xFFFFFFFFu /* end_face_idx of a ray that hit nothing */
+
+/* ---- scene tables ------------------------------------------------------- */
+/* Affine map: out = m * p + t, m row-major (ctracer.pxd:62-64 transform_t). */
+typedef struct rp_transform {
+    double m[9];
+    double t[3];
+} rp_transform;
+
+/* A FaceList: faces [first_face, first_face + n_faces) share one transform
+ * (ctracer.pxd:238-251). */
+typedef struct rp_facelist {
+    rp_transform trans;       /* local -> global */
+    rp_transform inv_trans;   /* global -> local */
+    int32_t first_face;
+    int32_t n_faces;
+} rp_facelist;
+
+/* Face types (raypier/core/cfaces.pyx). */
+enum rp_face_type {
+    RP_FACE_NONE = 0,          /* base Face: never hit (ctracer.pyx:1747-1757) */
+    RP_FACE_CIRCULAR = 1,      /* CircularFace          cfaces.pyx:140-191  p: diameter, offset, z_plane */
+    RP_FACE_RECTANGULAR = 2,   /* RectangularFace       cfaces.pyx:354-407  p: length, width, offset, z_plane */
+    RP_FACE_SHAPED_PLANAR = 3, /* ShapedPlanarFace      cfaces.pyx:194-242  p: z_height */
+    RP_FACE_SPHERICAL = 4,     /* SphericalFace         cfaces.pyx:410-498  p: diameter, curvature, z_height */
+    RP_FACE_SHAPED_SPHERICAL = 5, /* ShapedSphericalFace cfaces.pyx:501-608 p: curvature, z_height */
+    RP_FACE_CONIC = 6,         /* ConicRevolutionFace   cfaces.pyx:1751-1837 p: curvature, z_height, conic_const */
+    RP_FACE_ASPHERIC = 7,      /* AsphericFace          cfaces.pyx:1840-2025 p: curvature, z_height, conic_const, A4..A16, atol */
+    RP_FACE_EXTPOLY = 8,       /* ExtendedPolynomialFace cfaces.pyx:2028-2320 p: R, beta, norm_radius, z_height, atol; aux: coefs[n_aux0][n_aux1] */
+    RP_FACE_DISTORTION = 9,    /* DistortionFace        cfaces.pyx:2323-2438 p: accuracy; base, distortion */
+    RP_FACE_ORIENTED_POLYGON = 10, /* OrientedPolygonFace cfaces.pyx:1121-1222 p: origin[3], normal[3], x_axis[3], y_axis[3]; aux: xy[n_aux0][2] */
+    RP_FACE_POLYGON = 11,      /* PolygonFace           cfaces.pyx:1077-1118 p: z_plane; aux: xy[n_aux0][2] */
+    RP_FACE_ELLIPTICAL_PLANE = 12 /* ElipticalPlaneFace cfaces.pyx:313-351  p: g_x, g_y, diameter */
+};
+
+#define RP_FACE_NPARAM 16
+typedef struct rp_face {
+    int32_t type;            /* rp_face_type */
+    int32_t idx;             /* Face.idx: the value written to end_face_idx */
+    int32_t material;        /* index into the material table, -1 for sub-faces */
+    int32_t invert_normal;   /* Face.invert_normal (ctracer.pxd:228) */
+    int32_t invert_normals;  /* CircularFace / ShapedFace .invert_normals (cfaces.pyx:53,136) */
+    int32_t shape;           /* first op of this face's shape program, -1: no shape */
+    int32_t aux;             /* offset into the aux double table */
+    int32_t n_aux0, n_aux1;  /* aux extents (see face type) */
+    int32_t base;            /* DistortionFace: record index of the base face */
+    int32_t distortion;      /* DistortionFace: index into the distortion table */
+    int32_t reserved;
+    double tolerance;        /* Face.tolerance */
+    double p[RP_FACE_NPARAM];
+} rp_face;
+
+/* Shapes (raypier/core/cshapes.pyx) as a postfix program of boolean ops,
+ * terminated by RP_SHAPE_END. */
+enum rp_shape_op_type {
+    RP_SHAPE_END = 0,
+    RP_SHAPE_TRUE = 1,     /* base Shape: always inside (ctracer.pyx:1653-1655) */
+    RP_SHAPE_CIRCLE = 2,   /* CircleShape    cshapes.pyx:102-116  a,b = centre, c = radius */
+    RP_SHAPE_RECT = 3,     /* RectangleShape cshapes.pyx:119-136  a,b = centre, c = width, d = height */
+    RP_SHAPE_POLYGON = 4,  /* PolygonShape   cshapes.pyx:139-168  aux: xy[n][2] */
+    RP_SHAPE_AND = 5,      /* BooleanAND     cshapes.pyx:48-50 */
+    RP_SHAPE_OR = 6,       /* BooleanOR      cshapes.pyx:53-55 */
+    RP_SHAPE_XOR = 7,      /* BooleanXOR     cshapes.pyx:58-60 */
+    RP_SHAPE_NOT = 8       /* InvertShape    cshapes.pyx:30-36 */
+};
+typedef struct rp_shape_op {
+    int32_t op;
+    int32_t aux;
+    int32_t n;
+    int32_t reserved;
+    double a, b, c, d;
+} rp_shape_op;
+
+/* Distortions (raypier/core/cdistortions.pyx). */
+enum rp_distortion_type {
+    RP_DIST_ZERNIKE = 1,     /* ZernikeDistortion   cdistortions.pyx:323-514; aux: n_coefs x (j,n,m,k,value) */
+    RP_DIST_SIMPLE_J7 = 2    /* SimpleTestZernikeJ7 cdistortions.pyx:39-81  */
+};
+typedef struct rp_distortion {
+    int32_t type;
+    int32_t n_coefs;
+    int32_t k_max;
+    int32_t aux;
+    double unit_radius;
+    double amplitude;
+} rp_distortion;
+
+/* Materials (raypier/core/cmaterials.pyx). */
+enum rp_material_type {
+    RP_MAT_NONE = 0,                 /* base InterfaceMaterial: no child (ctracer.pyx:1580-1586) */
+    RP_MAT_OPAQUE = 1,               /* OpaqueMaterial            cmaterials.pyx:242-251 */
+    RP_MAT_TRANSPARENT = 2,          /* TransparentMaterial       cmaterials.pyx:254-278 */
+    RP_MAT_PEC = 3,                  /* PECMaterial               cmaterials.pyx:281-319 */
+    RP_MAT_PARTIAL = 4,              /* PartiallyReflectiveMaterial cmaterials.pyx:322-397  p0 = reflectivity */
+    RP_MAT_LINEAR_POLARISING = 5,    /* LinearPolarisingMaterial  cmaterials.pyx:400-455 */
+    RP_MAT_WAVEPLATE = 6,            /* WaveplateMaterial         cmaterials.pyx:458-551  p0,p1 = retardance (re,im), p2..p4 = fast axis */
+    RP_MAT_DIELECTRIC = 7,           /* DielectricMaterial        cmaterials.pyx:554-680 */
+    RP_MAT_FULL_DIELECTRIC = 8,      /* FullDielectricMaterial    cmaterials.pyx:727-872 */
+    RP_MAT_FULL_DIELECTRIC_DISPERSIVE = 9, /* FullDielectricDispersiveMaterial cmaterials.pyx:875-1013 */
+    RP_MAT_CIRCULAR_APERTURE = 10,   /* CircularApertureMaterial  cmaterials.pyx:1602-1662
+                                        p: outer_radius, radius, edge_width, invert, origin[3] */
+    RP_MAT_RECT_APERTURE = 11        /* RectangularApertureMaterial cmaterials.pyx:1665-1763
+                                        p: outer_width, outer_height, width, height, edge_width, invert, origin[3] */
+};
+typedef struct rp_material {
+    int32_t type;
+    int32_t curve_inside;    /* dispersive: index into the dispersion table */
+    int32_t curve_outside;
+    int32_t reserved;
+    double n_inside[2];      /* complex (re, im) */
+    double n_outside[2];
+    double reflection_threshold;
+    double transmission_threshold;
+    double p[10];
+} rp_material;
+
+/* Dispersion curves: BaseDispersionCurve (cmaterials.pyx:152-239). */
+typedef struct rp_dispersion {
+    int32_t formula_id;      /* 0, 1, 2 or 3 (formula 5 has no return value in the reference) */
+    int32_t n_coefs;
+    int32_t aux;             /* offset of the coefficients in the aux table */
+    int32_t reserved;
+    double absorption;       /* cm^-1 */
+    double wavelength_min, wavelength_max;
+} rp_dispersion;
+
+/* A whole scene.  faces[0 .. n_faces) are the traced faces in FaceList order
+ * (the reference's all_faces order); records after n_faces are sub-faces
+ * (DistortionFace base faces) that are only reached through rp_face.base. */
+typedef struct rp_scene_desc {
+    int32_t n_lists;
+    int32_t n_faces;
+    int32_t n_face_records;
+    int32_t n_materials;
+    int32_t n_shape_ops;
+    int32_t n_distortions;
+    int32_t n_dispersions;
+    int32_t n_aux;
+    const rp_facelist *lists;
+    const rp_face *faces;
+    const rp_material *materials;
+    const rp_shape_op *shape_ops;
+    const rp_distortion *distortions;
+    const rp_dispersion *dispersions;
+    const double *aux;
+} rp_scene_desc;
+
+/* Per-call statistics. */
+typedef struct rp_stats {
+    uint64_t rays_in;        /* rays traced (segments) */
+    uint64_t rays_out;       /* children kept */
+    uint64_t hits;           /* rays that hit a face */
+    uint64_t terminated;     /* children dropped by the |E|^2 rule */
+    double   device_ms;      /* device time of the traced generations */
+} rp_stats;
+
+/* Trace flags. */
+#define RP_TRACE_PLAIN_FP64  0u  /* all-FP64 path, bit-parity with the reference */
+#define RP_TRACE_MIXED       1u  /* FP32 bulk, FP64 roots / last Newton step / OPL */
+
+typedef struct rp_ctx rp_ctx;
+typedef struct rp_scene rp_scene;
+typedef struct rp_rays rp_rays;
+
+/* ---- library ------------------------------------------------------------ */
+int rp_version(void);
+const char *rp_status_string(int status);
+/* Last CUDA error text seen by this thread (empty if none). */
+const char *rp_last_error(void);
+
+/* ---- context ------------------------------------------------------------ */
+/* Bind to `device`; hbm_budget 0 = no limit.  Replaces nothing in the
+ * reference (which has no device); owns the stream and scratch arenas. */
+int rp_ctx_create(int device, uint64_t hbm_budget, rp_ctx **out);
+int rp_ctx_destroy(rp_ctx *ctx);
+int rp_ctx_synchronize(rp_ctx *ctx);
+/* Bytes of device memory the context holds. */
+int rp_ctx_memory(rp_ctx *ctx, uint64_t *bytes_in_use);
+
+/* ---- scenes ------------------------------------------------------------- */
+/* Upload a scene.  `wavelengths` is the RayCollection.wavelengths array that
+ * the reference pushes into each material (core/tracer.py:28-34,
+ * ctracer.pyx:1647-1650); dispersion tables are evaluated once here, as the
+ * reference's on_set_wavelengths does (cmaterials.pyx:883-887).  Returns
+ * RP_ERR_INVALID when a wavelength lies outside a curve's range
+ * (cmaterials.pyx:220-224 raises ValueError there). */
+int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *desc,
+                    const double *wavelengths, int64_t n_wavelengths,
+                    rp_scene **out);
+int rp_scene_destroy(rp_scene *scene);
+/* Per-face hit counters accumulated since the last reset (Face.count,
+ * ctracer.pyx:2108). counts has n_faces entries. */
+int rp_scene_face_counts(rp_scene *scene, uint32_t *counts, int32_t n_faces, int reset);
+
+/* ---- device ray buffers (structure-of-arrays) ---------------------------- */
+int rp_rays_alloc(rp_ctx *ctx, uint64_t capacity, rp_rays **out);
+int rp_rays_free(rp_rays *rays);
+int rp_rays_count(const rp_rays *rays, uint64_t *n);
+int rp_rays_capacity(const rp_rays *rays, uint64_t *cap);
+/* Copy n packed 188-byte records in (RayCollection.from_array, ctracer.pyx:1142-1154)
+ * or out (RayCollection.copy_as_array, ctracer.pyx:1048-1054). */
+int rp_rays_upload_aos(rp_rays *rays, const void *records, uint64_t n);
+int rp_rays_download_aos(const rp_rays *rays, void *records, uint64_t n);
+/* Device pointer of one SoA field (for zero-copy consumers); field names follow
+ * ray_dtype: "origin_x", ..., "E1_amp" (double2), "wavelength_idx", ... */
+int rp_rays_field(const rp_rays *rays, const char *name, void **dev_ptr);
+
+/* ---- tracing ------------------------------------------------------------ */
+/* One generation: replaces trace_segment_c (ctracer.pyx:2062-2118).
+ * `in` is mutated as in the reference (length, end_face_idx); children are
+ * written to `out` in the reference's append order (parent ascending,
+ * reflected before transmitted).  When e2_terminate > 0 a child with
+ * |E1|^2 + |E2|^2 < e2_terminate is dropped (stable).  `max_length` is a C
+ * float as in the reference (ctracer.pxd:261).  Returns RP_ERR_CAPACITY if
+ * `out` cannot hold the children (out is then left with count 0). */
+int rp_trace_segment(rp_ctx *ctx, rp_scene *scene, rp_rays *in, rp_rays *out,
+                     float max_length, uint32_t flags, double e2_terminate,
+                     rp_stats *stats);
+
+/* Sequential variant: only face `face_idx` of face list `list_idx` is tested
+ * (trace_one_face_segment_c, ctracer.pyx:2121-2170). */
+int rp_trace_one_face_segment(rp_ctx *ctx, rp_scene *scene, rp_rays *in, rp_rays *out,
+                              int32_t list_idx, int32_t face_idx, float max_length,
+                              uint32_t flags, double e2_terminate, rp_stats *stats);
+
+/* Whole non-sequential trace (trace_rays, core/tracer.py:9-47): generation g+1
+ * is traced from generation g while it is non-empty and g < recursion_limit.
+ * gens[0] must hold the input rays; gens[1..max_gens) are allocated by the
+ * library as needed (free them with rp_rays_free).  *n_gens receives the
+ * number of traced generations (the reference's len(traced_rays)). */
+int rp_trace_rays(rp_ctx *ctx, rp_scene *scene, rp_rays **gens, int32_t max_gens,
+                  int32_t recursion_limit, float max_length, uint32_t flags,
+                  double e2_terminate, int32_t *n_gens, rp_stats *stats);
+
+/* Host-buffer convenience: upload `n` input records, trace all generations,
+ * download them into `out_records` (capacity `out_cap` records, generations
+ * concatenated) with `gen_offsets[0..n_gens]` the start of each generation.
+ * Reference counterpart: trace_rays + RayCollection.copy_as_array. */
+int rp_trace_rays_host(rp_ctx *ctx, rp_scene *scene, const void *in_records, uint64_t n,
+                       int32_t recursion_limit, float max_length, uint32_t flags,
+                       double e2_terminate, void *out_records, uint64_t out_cap,
+                       uint64_t *gen_offsets, int32_t max_gens, int32_t *n_gens,
+                       rp_stats *stats);
+
+/* ---- single-plugin calls (batches of independent inputs, host buffers) ---- */
+/* Face.intersect (ctracer.pyx:1769-1777): distance along p1->p2 (local
+ * coordinates, 3 doubles per point) to face record `rec`, -1 for a miss. */
+int rp_face_intersect(rp_scene *scene, int32_t rec, const double *p1, const double *p2, uint64_t n,
+                      int is_base_ray, double *dist);
+/* Face.compute_normal (ctracer.pyx:1793-1800), local coordinates. */
+int rp_face_normal(rp_scene *scene, int32_t rec, const double *p, uint64_t n, double *normal);
+/* Shape.point_inside (ctracer.pyx:1657-1658) for the shape program at `prog`. */
+int rp_shape_inside(rp_scene *scene, int32_t prog, const double *xy, uint64_t n, int32_t *inside);
+/* Distortion.z_offset_and_gradient / z_offset (ctracer.pyx:1703-1729):
+ * out4[i] = (dz/dx, dz/dy, z, z_offset). */
+int rp_distortion_eval(rp_scene *scene, int32_t distortion, const double *xy, uint64_t n, double *out4);
+/* InterfaceMaterial.eval_child_ray (ctracer.pyx:1620-1632): children of ray i
+ * in records 2i, 2i+1 (188-byte format), their number in n_children[i]. */
+int rp_material_eval(rp_scene *scene, int32_t material, const void *rays, const uint32_t *ray_idx,
+                     const double *points, const double *normals, const double *tangents, uint64_t n,
+                     void *children, int32_t *n_children);
+/* Convert_to_SP (cmaterials.pyx:94-101). */
+int rp_convert_to_sp(rp_ctx *ctx, const void *rays, const double *normals, uint64_t n, void *out_rays);
+/* BaseDispersionCurve.evaluate_n (cmaterials.pyx:230-239) for curve `curve`
+ * of the scene: complex index per wavelength (re, im pairs). */
+int rp_dispersion_eval(rp_scene *scene, int32_t curve, const double *wavelengths, uint64_t n,
+                       double *out_re_im);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RP_GB300_H */

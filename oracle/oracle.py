@@ -1,0 +1,200 @@
+"""ctypes front end of the C restatement oracle (oracle/rp_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py to check or time the reference algorithm on the
+host.  The product package never imports this module.
+
+Scenes are passed as the table form of include/rp_gb300.h (built by
+``raypier_optics_gb300.scene``), rays as the reference's 188-byte records.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "rp_oracle.c")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "librp_oracle.so")
+
+_lib = None
+_lock = threading.Lock()
+
+
+def build(force=False):
+    """gcc -O2 -ffp-contract=off: the reference's own optimisation level and no
+    FMA contraction, so results match the reference's C bit for bit."""
+    os.makedirs(BUILD, exist_ok=True)
+    hdr = os.path.join(REPO, "include", "rp_gb300.h")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC),
+                                                                           os.path.getmtime(hdr)):
+        return LIB
+    tmp = LIB + ".tmp"
+    subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fPIC", "-shared",
+                    "-std=gnu11", "-o", tmp, SRC, "-lm"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def load():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            lib = ctypes.CDLL(LIB)
+            P, I, U64, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double
+            lib.rp_oracle_trace_rays.argtypes = [P, P, ctypes.c_int64, P, U64, I, ctypes.c_float, D, P, U64, P, I,
+                                                 ctypes.POINTER(I), P]
+            lib.rp_oracle_trace_segment.argtypes = [P, P, ctypes.c_int64, P, U64, ctypes.c_float, I, I, D, P, U64,
+                                                    ctypes.POINTER(U64), P]
+            lib.rp_oracle_face_intersect.argtypes = [P, I, P, P, I]
+            lib.rp_oracle_face_intersect.restype = D
+            lib.rp_oracle_face_normal.argtypes = [P, I, P, P]
+            lib.rp_oracle_shape_inside.argtypes = [P, I, D, D]
+            lib.rp_oracle_distortion.argtypes = [P, I, D, D, P, P]
+            lib.rp_oracle_convert_to_sp.argtypes = [P, P, P]
+            lib.rp_oracle_eval_child_ray.argtypes = [P, P, ctypes.c_int64, I, P, ctypes.c_uint32, P, P, P, P]
+            lib.rp_oracle_dispersion_n.argtypes = [P, I, P, ctypes.c_int64, P]
+            _lib = lib
+        return _lib
+
+
+def _rays(records):
+    from raypier_optics_gb300.ctracer import ray_dtype
+    r = np.ascontiguousarray(records)
+    assert r.dtype == ray_dtype
+    return r
+
+
+def trace_rays(tables, wavelengths, records, recursion_limit, max_length, e2_terminate=0.0, max_total=None):
+    """trace_rays (core/tracer.py:9-47) on the host.  Returns (list of
+    generation record arrays, face hit counts per face record)."""
+    from raypier_optics_gb300.ctracer import ray_dtype
+    lib = load()
+    rin = _rays(records).copy()
+    n = rin.shape[0]
+    cap = max_total if max_total else max(n * (2 ** min(recursion_limit, 24)), 16)
+    while True:
+        out = np.zeros(cap, dtype=ray_dtype)
+        offs = np.zeros(recursion_limit + 2, dtype=np.uint64)
+        counts = np.zeros(tables.faces.shape[0], dtype=np.uint32)
+        ng = ctypes.c_int(0)
+        desc = tables.desc()
+        wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+        rc = lib.rp_oracle_trace_rays(ctypes.byref(desc), wl.ctypes.data, wl.shape[0], rin.ctypes.data, n,
+                                      int(recursion_limit), ctypes.c_float(max_length), float(e2_terminate),
+                                      out.ctypes.data, cap, offs.ctypes.data, recursion_limit + 1, ctypes.byref(ng),
+                                      counts.ctypes.data)
+        if rc == -2 and not max_total:
+            cap *= 2
+            continue
+        if rc != 0:
+            raise RuntimeError(f"oracle trace_rays failed with {rc}")
+        gens = [out[int(offs[g]):int(offs[g + 1])].copy() for g in range(ng.value)]
+        return gens, counts
+
+
+def trace_segment(tables, wavelengths, records, max_length, e2_terminate=0.0, one_list=-1, one_face=-1):
+    """One generation (trace_segment_c).  Returns (mutated input, children, face counts)."""
+    from raypier_optics_gb300.ctracer import ray_dtype
+    lib = load()
+    rin = _rays(records).copy()
+    n = rin.shape[0]
+    out = np.zeros(max(2 * n, 1), dtype=ray_dtype)
+    n_out = ctypes.c_uint64(0)
+    counts = np.zeros(tables.faces.shape[0], dtype=np.uint32)
+    desc = tables.desc()
+    wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+    rc = lib.rp_oracle_trace_segment(ctypes.byref(desc), wl.ctypes.data, wl.shape[0], rin.ctypes.data, n,
+                                     ctypes.c_float(max_length), one_list, one_face, float(e2_terminate),
+                                     out.ctypes.data, out.shape[0], ctypes.byref(n_out), counts.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle trace_segment failed with {rc}")
+    return rin, out[:n_out.value].copy(), counts
+
+
+def face_intersect(tables, rec, p1, p2, is_base_ray):
+    lib = load()
+    desc = tables.desc()
+    p1 = np.ascontiguousarray(p1, dtype=np.double).reshape(-1, 3)
+    p2 = np.ascontiguousarray(p2, dtype=np.double).reshape(-1, 3)
+    return np.array([lib.rp_oracle_face_intersect(ctypes.byref(desc), rec, p1[i].ctypes.data, p2[i].ctypes.data,
+                                                  int(is_base_ray)) for i in range(p1.shape[0])])
+
+
+def face_normal(tables, rec, p):
+    lib = load()
+    desc = tables.desc()
+    p = np.ascontiguousarray(p, dtype=np.double).reshape(-1, 3)
+    out = np.zeros_like(p)
+    for i in range(p.shape[0]):
+        o = np.zeros(3)
+        lib.rp_oracle_face_normal(ctypes.byref(desc), rec, p[i].ctypes.data, o.ctypes.data)
+        out[i] = o
+    return out
+
+
+def shape_inside(tables, prog, xy):
+    lib = load()
+    desc = tables.desc()
+    xy = np.asarray(xy, dtype=np.double).reshape(-1, 2)
+    return np.array([bool(lib.rp_oracle_shape_inside(ctypes.byref(desc), prog, x, y)) for x, y in xy])
+
+
+def distortion(tables, d, x, y):
+    lib = load()
+    desc = tables.desc()
+    out = np.zeros((len(x), 4))
+    for i in range(len(x)):
+        o = np.zeros(3)
+        z = ctypes.c_double(0)
+        lib.rp_oracle_distortion(ctypes.byref(desc), d, float(x[i]), float(y[i]), o.ctypes.data, ctypes.byref(z))
+        out[i, :3] = o
+        out[i, 3] = z.value
+    return out
+
+
+def convert_to_sp(records, normals):
+    lib = load()
+    r = _rays(records)
+    nn = np.ascontiguousarray(normals, dtype=np.double).reshape(-1, 3)
+    out = np.zeros_like(r)
+    for i in range(r.shape[0]):
+        lib.rp_oracle_convert_to_sp(r[i:i + 1].ctypes.data, nn[i].ctypes.data, out[i:i + 1].ctypes.data)
+    return out
+
+
+def eval_child_rays(tables, wavelengths, mat, records, idx, points, normals, tangents):
+    from raypier_optics_gb300.ctracer import ray_dtype
+    lib = load()
+    desc = tables.desc()
+    wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+    r = _rays(records)
+    P = np.ascontiguousarray(points, dtype=np.double).reshape(-1, 3)
+    N = np.ascontiguousarray(normals, dtype=np.double).reshape(-1, 3)
+    T = np.ascontiguousarray(tangents, dtype=np.double).reshape(-1, 3)
+    res = []
+    for i in range(r.shape[0]):
+        out = np.zeros(2, dtype=ray_dtype)
+        k = lib.rp_oracle_eval_child_ray(ctypes.byref(desc), wl.ctypes.data, wl.shape[0], mat, r[i:i + 1].ctypes.data,
+                                         int(idx[i]), P[i].ctypes.data, N[i].ctypes.data, T[i].ctypes.data,
+                                         out.ctypes.data)
+        if k < 0:
+            raise RuntimeError("oracle material evaluation failed")
+        res.append(out[:k].copy())
+    return res
+
+
+def dispersion_n(tables, curve, wavelengths):
+    lib = load()
+    desc = tables.desc()
+    wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+    out = np.zeros(2 * wl.shape[0])
+    if lib.rp_oracle_dispersion_n(ctypes.byref(desc), curve, wl.ctypes.data, wl.shape[0], out.ctypes.data):
+        raise ValueError("wavelength outside the dispersion curve's range")
+    return out[0::2] + 1j * out[1::2]

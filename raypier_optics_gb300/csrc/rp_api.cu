@@ -1,0 +1,662 @@
+// rp_api.cu -- the C ABI (include/rp_gb300.h): contexts, scenes, device ray
+// buffers and the trace entry points.  No C++ exception crosses the boundary;
+// every entry point returns an rp status code.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/rp_gb300.h"
+#include "rp_kernels.cuh"
+
+using namespace rp;
+
+static thread_local char g_last_error[256] = "";
+
+static int cuda_fail(cudaError_t e, const char *what) {
+    snprintf(g_last_error, sizeof g_last_error, "%s: %s", what, cudaGetErrorString(e));
+    return RP_ERR_CUDA;
+}
+#define CK(call)                                          \
+    do {                                                  \
+        cudaError_t _e = (call);                          \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+    } while (0)
+
+struct rp_ctx {
+    int device;
+    cudaStream_t stream;
+    uint64_t budget;
+    uint64_t in_use;
+    // per-generation scan scratch: [counter | out_count | err | pad | stats[2] | tile states...]
+    unsigned char *scratch;
+    size_t scratch_bytes;
+    unsigned long long *h_pinned;  // 8 words of pinned host memory for small read-backs
+    cudaEvent_t ev0, ev1;
+};
+
+struct rp_scene {
+    rp_ctx *ctx;
+    DevScene S;               // device pointers
+    void *dev_block;          // one allocation holding every table
+    size_t dev_bytes;
+    unsigned *face_counts;    // per face record
+    int n_faces;
+    size_t smem;              // bytes of tables staged per block
+    int smem_tables;
+    const rp_dispersion *disp;  // device copy of the dispersion curve table
+    int n_disp;
+    std::vector<rp_face> host_faces;
+    std::vector<rp_facelist> host_lists;
+};
+
+struct rp_rays {
+    rp_ctx *ctx;
+    uint64_t cap, n;
+    void *block;
+    size_t bytes;
+    RaySoA soa;
+};
+
+// ---- memory accounting ------------------------------------------------------
+static int ctx_alloc(rp_ctx *ctx, void **p, size_t bytes) {
+    if (ctx->budget && ctx->in_use + bytes > ctx->budget) {
+        snprintf(g_last_error, sizeof g_last_error, "device budget of %llu bytes exceeded",
+                 (unsigned long long)ctx->budget);
+        return RP_ERR_BUDGET;
+    }
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    ctx->in_use += bytes;
+    return RP_OK;
+}
+static void ctx_free(rp_ctx *ctx, void *p, size_t bytes) {
+    if (!p) return;
+    cudaFree(p);
+    ctx->in_use -= bytes;
+}
+
+extern "C" {
+
+int rp_version(void) { return RP_ABI_VERSION; }
+
+const char *rp_status_string(int s) {
+    switch (s) {
+        case RP_OK: return "ok";
+        case RP_ERR_INVALID: return "invalid argument";
+        case RP_ERR_CAPACITY: return "output capacity exceeded";
+        case RP_ERR_BUDGET: return "device memory budget exceeded";
+        case RP_ERR_TIMEOUT: return "bounded device wait timed out";
+        case RP_ERR_CUDA: return "CUDA error";
+        case RP_ERR_UNSUPPORTED: return "unsupported face/material type";
+        case RP_ERR_NOMEM: return "host allocation failed";
+        default: return "unknown status";
+    }
+}
+
+const char *rp_last_error(void) { return g_last_error; }
+
+int rp_ctx_create(int device, uint64_t hbm_budget, rp_ctx **out) {
+    if (!out) return RP_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return RP_ERR_INVALID;
+    CK(cudaSetDevice(device));
+    rp_ctx *c = new (std::nothrow) rp_ctx();
+    if (!c) return RP_ERR_NOMEM;
+    c->device = device;
+    c->budget = hbm_budget;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_pinned, 8 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "rp_ctx_create");
+    }
+    *out = c;
+    return RP_OK;
+}
+
+int rp_ctx_destroy(rp_ctx *c) {
+    if (!c) return RP_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    if (c->scratch) cudaFree(c->scratch);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    cudaEventDestroy(c->ev0);
+    cudaEventDestroy(c->ev1);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return RP_OK;
+}
+
+int rp_ctx_synchronize(rp_ctx *c) {
+    if (!c) return RP_ERR_INVALID;
+    CK(cudaStreamSynchronize(c->stream));
+    return RP_OK;
+}
+
+int rp_ctx_memory(rp_ctx *c, uint64_t *bytes) {
+    if (!c || !bytes) return RP_ERR_INVALID;
+    *bytes = c->in_use + c->scratch_bytes;
+    return RP_OK;
+}
+
+// ---- scenes -------------------------------------------------------------------
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static int validate_scene(const rp_scene_desc *d) {
+    if (!d || d->n_lists < 0 || d->n_faces < 0 || d->n_face_records < d->n_faces || d->n_materials < 0 ||
+        d->n_shape_ops < 0 || d->n_distortions < 0 || d->n_dispersions < 0 || d->n_aux < 0)
+        return RP_ERR_INVALID;
+    int expect = 0;
+    for (int l = 0; l < d->n_lists; l++) {
+        const rp_facelist &L = d->lists[l];
+        if (L.first_face != expect || L.n_faces < 0) return RP_ERR_INVALID;
+        expect += L.n_faces;
+    }
+    if (expect != d->n_faces) return RP_ERR_INVALID;
+    for (int f = 0; f < d->n_face_records; f++) {
+        const rp_face &F = d->faces[f];
+        if (F.type < RP_FACE_NONE || F.type > RP_FACE_ELLIPTICAL_PLANE) return RP_ERR_UNSUPPORTED;
+        if (f < d->n_faces && (F.material < 0 || F.material >= d->n_materials)) return RP_ERR_INVALID;
+        if (F.shape >= d->n_shape_ops) return RP_ERR_INVALID;
+        if (F.aux < 0 || F.aux + F.n_aux0 * (F.n_aux1 > 0 ? F.n_aux1 : 2) > d->n_aux + 0) {
+            if (F.type == RP_FACE_EXTPOLY || F.type == RP_FACE_ORIENTED_POLYGON || F.type == RP_FACE_POLYGON)
+                return RP_ERR_INVALID;
+        }
+        if (F.type == RP_FACE_EXTPOLY && (F.n_aux0 < 1 || F.n_aux0 > 8 || F.n_aux1 < 1 || F.n_aux1 > 8))
+            return RP_ERR_UNSUPPORTED;
+        if (F.type == RP_FACE_DISTORTION) {
+            if (F.base < d->n_faces || F.base >= d->n_face_records) return RP_ERR_INVALID;
+            if (d->faces[F.base].type == RP_FACE_DISTORTION) return RP_ERR_UNSUPPORTED;
+            if (F.distortion < 0 || F.distortion >= d->n_distortions) return RP_ERR_INVALID;
+        }
+    }
+    for (int m = 0; m < d->n_materials; m++) {
+        const rp_material &M = d->materials[m];
+        if (M.type < RP_MAT_NONE || M.type > RP_MAT_RECT_APERTURE) return RP_ERR_UNSUPPORTED;
+        if (M.type == RP_MAT_FULL_DIELECTRIC_DISPERSIVE &&
+            (M.curve_inside < 0 || M.curve_inside >= d->n_dispersions || M.curve_outside < 0 ||
+             M.curve_outside >= d->n_dispersions))
+            return RP_ERR_INVALID;
+    }
+    for (int c = 0; c < d->n_dispersions; c++) {
+        int fid = d->dispersions[c].formula_id;
+        if (fid < 0 || fid > 3) return RP_ERR_UNSUPPORTED;
+    }
+    for (int k = 0; k < d->n_distortions; k++) {
+        const rp_distortion &D = d->distortions[k];
+        if (D.type == RP_DIST_ZERNIKE && (D.k_max < 0 || D.k_max > 48)) return RP_ERR_UNSUPPORTED;
+    }
+    return RP_OK;
+}
+
+int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengths, int64_t n_wl, rp_scene **out) {
+    if (!ctx || !out) return RP_ERR_INVALID;
+    *out = nullptr;
+    int v = validate_scene(d);
+    if (v != RP_OK) {
+        snprintf(g_last_error, sizeof g_last_error, "malformed or unsupported scene");
+        return v;
+    }
+    if (n_wl < 0 || (n_wl > 0 && !wavelengths)) return RP_ERR_INVALID;
+    // wavelength range check: BaseDispersionCurve.c_evaluate_n raises ValueError (cmaterials.pyx:220-224)
+    for (int c = 0; c < d->n_dispersions; c++) {
+        const rp_dispersion &D = d->dispersions[c];
+        for (int64_t i = 0; i < n_wl; i++) {
+            if (wavelengths[i] < D.wavelength_min || wavelengths[i] > D.wavelength_max) {
+                snprintf(g_last_error, sizeof g_last_error,
+                         "Wavelength (%f) outside range of dispersion curve (%f -> %f)", wavelengths[i],
+                         D.wavelength_min, D.wavelength_max);
+                return RP_ERR_INVALID;
+            }
+        }
+    }
+    CK(cudaSetDevice(ctx->device));
+    rp_scene *s = new (std::nothrow) rp_scene();
+    if (!s) return RP_ERR_NOMEM;
+    s->ctx = ctx;
+    s->n_faces = d->n_faces;
+    s->host_faces.assign(d->faces, d->faces + d->n_face_records);
+    s->host_lists.assign(d->lists, d->lists + d->n_lists);
+    size_t o_lists = 0;
+    size_t o_faces = o_lists + align256(sizeof(rp_facelist) * d->n_lists);
+    size_t o_mats = o_faces + align256(sizeof(rp_face) * d->n_face_records);
+    size_t o_shapes = o_mats + align256(sizeof(rp_material) * d->n_materials);
+    size_t o_dists = o_shapes + align256(sizeof(rp_shape_op) * d->n_shape_ops);
+    size_t o_disp = o_dists + align256(sizeof(rp_distortion) * d->n_distortions);
+    size_t o_aux = o_disp + align256(sizeof(rp_dispersion) * d->n_dispersions);
+    size_t o_wl = o_aux + align256(sizeof(double) * d->n_aux);
+    size_t o_ntab = o_wl + align256(sizeof(double) * (size_t)n_wl);
+    size_t o_cnt = o_ntab + align256(sizeof(double2) * (size_t)n_wl * d->n_dispersions);
+    size_t total = o_cnt + align256(sizeof(unsigned) * (d->n_face_records + 1));
+    int rc = ctx_alloc(ctx, &s->dev_block, total);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    s->dev_bytes = total;
+    unsigned char *b = (unsigned char *)s->dev_block;
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaSuccess;
+#define UP(off, ptr, bytes) \
+    if (e == cudaSuccess && (bytes) > 0) e = cudaMemcpyAsync(b + (off), (ptr), (bytes), cudaMemcpyHostToDevice, st)
+    UP(o_lists, d->lists, sizeof(rp_facelist) * d->n_lists);
+    UP(o_faces, d->faces, sizeof(rp_face) * d->n_face_records);
+    UP(o_mats, d->materials, sizeof(rp_material) * d->n_materials);
+    UP(o_shapes, d->shape_ops, sizeof(rp_shape_op) * d->n_shape_ops);
+    UP(o_dists, d->distortions, sizeof(rp_distortion) * d->n_distortions);
+    UP(o_disp, d->dispersions, sizeof(rp_dispersion) * d->n_dispersions);
+    UP(o_aux, d->aux, sizeof(double) * d->n_aux);
+    UP(o_wl, wavelengths, sizeof(double) * (size_t)n_wl);
+#undef UP
+    if (e == cudaSuccess) e = cudaMemsetAsync(b + o_cnt, 0, sizeof(unsigned) * (d->n_face_records + 1), st);
+    DevScene &S = s->S;
+    S.lists = (const rp_facelist *)(b + o_lists);
+    S.faces = (const rp_face *)(b + o_faces);
+    S.mats = (const rp_material *)(b + o_mats);
+    S.shapes = (const rp_shape_op *)(b + o_shapes);
+    S.dists = (const rp_distortion *)(b + o_dists);
+    S.aux = (const double *)(b + o_aux);
+    S.ntab = (const double2 *)(b + o_ntab);
+    S.n_wl = n_wl;
+    S.n_lists = d->n_lists;
+    S.n_faces = d->n_faces;
+    S.n_recs = d->n_face_records;
+    S.n_mats = d->n_materials;
+    S.n_shapes = d->n_shape_ops;
+    S.n_dists = d->n_distortions;
+    s->face_counts = (unsigned *)(b + o_cnt);
+    s->disp = (const rp_dispersion *)(b + o_disp);
+    s->n_disp = d->n_dispersions;
+    if (e == cudaSuccess)
+        e = launch_dispersion_table((const rp_dispersion *)(b + o_disp), d->n_dispersions, (const double *)(b + o_aux),
+                                    (const double *)(b + o_wl), n_wl, (double2 *)(b + o_ntab), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        ctx_free(ctx, s->dev_block, s->dev_bytes);
+        delete s;
+        return cuda_fail(e, "rp_scene_create");
+    }
+    s->smem = generation_smem_bytes(d->n_lists, d->n_face_records, d->n_materials, d->n_faces);
+    s->smem_tables = 1;
+    if (s->smem > 160 * 1024) {  // tables too large to stage: read them from global memory
+        s->smem_tables = 0;
+        s->smem = sizeof(unsigned) * (size_t)d->n_faces;
+    }
+    *out = s;
+    return RP_OK;
+}
+
+int rp_scene_destroy(rp_scene *s) {
+    if (!s) return RP_ERR_INVALID;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    ctx_free(s->ctx, s->dev_block, s->dev_bytes);
+    delete s;
+    return RP_OK;
+}
+
+int rp_scene_face_counts(rp_scene *s, uint32_t *counts, int32_t n_faces, int reset) {
+    if (!s || !counts || n_faces != s->n_faces) return RP_ERR_INVALID;
+    CK(cudaSetDevice(s->ctx->device));
+    CK(cudaMemcpyAsync(counts, s->face_counts, sizeof(unsigned) * n_faces, cudaMemcpyDeviceToHost, s->ctx->stream));
+    if (reset) CK(cudaMemsetAsync(s->face_counts, 0, sizeof(unsigned) * n_faces, s->ctx->stream));
+    CK(cudaStreamSynchronize(s->ctx->stream));
+    return RP_OK;
+}
+
+// ---- rays ---------------------------------------------------------------------
+static void soa_carve(rp_rays *r) {
+    unsigned char *b = (unsigned char *)r->block;
+    size_t c = r->cap, off = 0;
+    auto take = [&](size_t elem) {
+        unsigned char *p = b + off;
+        off += align256(elem * c);
+        return p;
+    };
+    RaySoA &s = r->soa;
+    s.ox = (double *)take(8); s.oy = (double *)take(8); s.oz = (double *)take(8);
+    s.dx = (double *)take(8); s.dy = (double *)take(8); s.dz = (double *)take(8);
+    s.nx = (double *)take(8); s.ny = (double *)take(8); s.nz = (double *)take(8);
+    s.ex = (double *)take(8); s.ey = (double *)take(8); s.ez = (double *)take(8);
+    s.n = (double2 *)take(16); s.e1 = (double2 *)take(16); s.e2 = (double2 *)take(16);
+    s.len = (double *)take(8); s.phase = (double *)take(8); s.opl = (double *)take(8);
+    s.wl = (unsigned *)take(4); s.parent = (unsigned *)take(4); s.endf = (unsigned *)take(4);
+    s.ident = (unsigned *)take(4); s.type = (unsigned *)take(4);
+}
+
+static size_t soa_bytes(uint64_t cap) {
+    size_t c = cap ? cap : 1, t = 0;
+    const size_t sizes[] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 16, 16, 16, 8, 8, 8, 4, 4, 4, 4, 4};
+    for (size_t e : sizes) t += align256(e * c);
+    return t;
+}
+
+int rp_rays_alloc(rp_ctx *ctx, uint64_t cap, rp_rays **out) {
+    if (!ctx || !out) return RP_ERR_INVALID;
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    rp_rays *r = new (std::nothrow) rp_rays();
+    if (!r) return RP_ERR_NOMEM;
+    r->ctx = ctx;
+    r->cap = cap ? cap : 1;
+    r->n = 0;
+    r->bytes = soa_bytes(r->cap);
+    int rc = ctx_alloc(ctx, &r->block, r->bytes);
+    if (rc) {
+        delete r;
+        return rc;
+    }
+    soa_carve(r);
+    *out = r;
+    return RP_OK;
+}
+
+int rp_rays_free(rp_rays *r) {
+    if (!r) return RP_ERR_INVALID;
+    cudaSetDevice(r->ctx->device);
+    cudaStreamSynchronize(r->ctx->stream);
+    ctx_free(r->ctx, r->block, r->bytes);
+    delete r;
+    return RP_OK;
+}
+
+int rp_rays_count(const rp_rays *r, uint64_t *n) {
+    if (!r || !n) return RP_ERR_INVALID;
+    *n = r->n;
+    return RP_OK;
+}
+
+int rp_rays_capacity(const rp_rays *r, uint64_t *cap) {
+    if (!r || !cap) return RP_ERR_INVALID;
+    *cap = r->cap;
+    return RP_OK;
+}
+
+// Host AoS <-> device SoA goes through a device staging buffer of packed
+// records (one cudaMemcpyAsync) and the layout kernels.
+static int with_staging(rp_ctx *ctx, size_t bytes, void **p) { return ctx_alloc(ctx, p, bytes); }
+
+int rp_rays_upload_aos(rp_rays *r, const void *records, uint64_t n) {
+    if (!r || (n && !records)) return RP_ERR_INVALID;
+    if (n > r->cap) return RP_ERR_CAPACITY;
+    rp_ctx *ctx = r->ctx;
+    CK(cudaSetDevice(ctx->device));
+    void *stage = nullptr;
+    size_t bytes = (size_t)n * RP_RAY_BYTES;
+    if (n) {
+        int rc = with_staging(ctx, bytes, &stage);
+        if (rc) return rc;
+        cudaError_t e = cudaMemcpyAsync(stage, records, bytes, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = launch_aos_to_soa(stage, r->soa, n, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        ctx_free(ctx, stage, bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "rp_rays_upload_aos");
+    }
+    r->n = n;
+    return RP_OK;
+}
+
+int rp_rays_download_aos(const rp_rays *r, void *records, uint64_t n) {
+    if (!r || (n && !records)) return RP_ERR_INVALID;
+    if (n > r->n) return RP_ERR_CAPACITY;
+    rp_ctx *ctx = r->ctx;
+    CK(cudaSetDevice(ctx->device));
+    if (!n) return RP_OK;
+    void *stage = nullptr;
+    size_t bytes = (size_t)n * RP_RAY_BYTES;
+    int rc = with_staging(ctx, bytes, &stage);
+    if (rc) return rc;
+    cudaError_t e = launch_soa_to_aos(r->soa, stage, n, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(records, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    ctx_free(ctx, stage, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "rp_rays_download_aos");
+    return RP_OK;
+}
+
+int rp_rays_field(const rp_rays *r, const char *name, void **p) {
+    if (!r || !name || !p) return RP_ERR_INVALID;
+    const RaySoA &s = r->soa;
+    struct {
+        const char *n;
+        void *p;
+    } t[] = {{"origin_x", s.ox}, {"origin_y", s.oy}, {"origin_z", s.oz}, {"direction_x", s.dx},
+             {"direction_y", s.dy}, {"direction_z", s.dz}, {"normal_x", s.nx}, {"normal_y", s.ny},
+             {"normal_z", s.nz}, {"E_vector_x", s.ex}, {"E_vector_y", s.ey}, {"E_vector_z", s.ez},
+             {"refractive_index", s.n}, {"E1_amp", s.e1}, {"E2_amp", s.e2}, {"length", s.len},
+             {"phase", s.phase}, {"accumulated_path", s.opl}, {"wavelength_idx", s.wl},
+             {"parent_idx", s.parent}, {"end_face_idx", s.endf}, {"ray_ident", s.ident},
+             {"ray_type_id", s.type}};
+    for (auto &e : t)
+        if (!strcmp(e.n, name)) {
+            *p = e.p;
+            return RP_OK;
+        }
+    return RP_ERR_INVALID;
+}
+
+// ---- tracing ------------------------------------------------------------------
+#define SCRATCH_HDR 64
+
+static int ensure_scratch(rp_ctx *ctx, uint64_t n_tiles) {
+    size_t need = SCRATCH_HDR + n_tiles * sizeof(unsigned long long);
+    if (need <= ctx->scratch_bytes) return RP_OK;
+    if (ctx->scratch) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->scratch);
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+    }
+    size_t bytes = need * 2;
+    if (ctx->budget && ctx->in_use + bytes > ctx->budget) return RP_ERR_BUDGET;
+    CK(cudaMalloc((void **)&ctx->scratch, bytes));
+    ctx->scratch_bytes = bytes;
+    return RP_OK;
+}
+
+// Launches one generation; on return h_pinned[0] holds the child count,
+// h_pinned[1] the error bits (valid after the stream is synchronised).
+static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float max_length, uint32_t flags,
+                      double e2, int emit, int one_list, int one_face) {
+    uint64_t n_in = in->n;
+    uint64_t n_tiles = (n_in + RP_BLOCK - 1) / RP_BLOCK;
+    int rc = ensure_scratch(ctx, n_tiles);
+    if (rc) return rc;
+    unsigned char *sc = ctx->scratch;
+    CK(cudaMemsetAsync(sc, 0, SCRATCH_HDR + n_tiles * sizeof(unsigned long long), ctx->stream));
+    GenArgs a;
+    memset(&a, 0, sizeof a);
+    a.in = in->soa;
+    a.out = out ? out->soa : in->soa;
+    a.n_in = n_in;
+    a.out_cap = out ? out->cap : 0;
+    a.max_len = (double)max_length;
+    a.e2_term = e2;
+    a.emit = emit;
+    a.one_list = one_list;
+    a.one_face = one_face;
+    a.S = s->S;
+    a.smem_tables = s->smem_tables;
+    a.tile_counter = (unsigned *)(sc + 0);
+    a.out_count = (unsigned long long *)(sc + 8);
+    a.err = (unsigned *)(sc + 16);
+    a.stats = (unsigned long long *)(sc + 32);
+    a.tile_state = (unsigned long long *)(sc + SCRATCH_HDR);
+    a.face_counts = s->face_counts;
+    cudaError_t e = (flags & RP_TRACE_MIXED) ? launch_generation_mixed(a, s->smem, ctx->stream)
+                                             : launch_generation_plain(a, s->smem, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "generation kernel launch");
+    CK(cudaMemcpyAsync(ctx->h_pinned, sc + 8, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    return RP_OK;
+}
+
+static int finish_gen(rp_ctx *ctx, rp_rays *out, int emit, rp_stats *st, uint64_t n_in) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    unsigned long long cnt = ctx->h_pinned[0];
+    unsigned err = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
+    unsigned long long hits = ctx->h_pinned[3], term = ctx->h_pinned[4];
+    if (st) {
+        st->rays_in += n_in;
+        st->hits += hits;
+        st->terminated += term;
+    }
+    if (err & ERR_TIMEOUT) {
+        snprintf(g_last_error, sizeof g_last_error, "look-back wait gave up");
+        return RP_ERR_TIMEOUT;
+    }
+    if (err & (ERR_ZK_STACK | ERR_SHAPE_STACK)) {
+        snprintf(g_last_error, sizeof g_last_error, "device evaluation limit hit (err=0x%x)", err);
+        return RP_ERR_INVALID;
+    }
+    if (!emit) return RP_OK;
+    if ((err & ERR_OVERFLOW) || cnt > out->cap) {
+        out->n = 0;
+        return RP_ERR_CAPACITY;
+    }
+    out->n = cnt;
+    if (st) st->rays_out += cnt;
+    return RP_OK;
+}
+
+int rp_trace_segment(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float max_length, uint32_t flags,
+                     double e2, rp_stats *st) {
+    if (!ctx || !s || !in || !out || in == out || s->ctx != ctx) return RP_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    out->n = 0;
+    if (in->n == 0) return RP_OK;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    int rc = launch_gen(ctx, s, in, out, max_length, flags, e2, 1, -1, -1);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    rc = finish_gen(ctx, out, 1, st, in->n);
+    if (st) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        st->device_ms += ms;
+    }
+    return rc;
+}
+
+int rp_trace_one_face_segment(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, int32_t list_idx,
+                              int32_t face_idx, float max_length, uint32_t flags, double e2, rp_stats *st) {
+    if (!ctx || !s || !in || !out || in == out || s->ctx != ctx) return RP_ERR_INVALID;
+    if (list_idx < 0 || list_idx >= s->S.n_lists) return RP_ERR_INVALID;
+    if (face_idx < 0 || face_idx >= s->host_lists[list_idx].n_faces) return RP_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    out->n = 0;
+    if (in->n == 0) return RP_OK;
+    int rc = launch_gen(ctx, s, in, out, max_length, flags, e2, 1, list_idx, face_idx);
+    if (rc) return rc;
+    return finish_gen(ctx, out, 1, st, in->n);
+}
+
+int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, int32_t recursion_limit,
+                  float max_length, uint32_t flags, double e2, int32_t *n_gens, rp_stats *st) {
+    if (!ctx || !s || !gens || !gens[0] || max_gens < 1 || !n_gens || s->ctx != ctx) return RP_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    *n_gens = 0;
+    for (int g = 1; g < max_gens; g++) gens[g] = nullptr;
+    int count = 0;
+    rp_rays *rays = gens[0];
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    int rc = RP_OK;
+    // core/tracer.py:40-45: while rays.n_rays > 0 and count < recursion_limit
+    while (rays->n > 0 && count < recursion_limit) {
+        int last = (count + 1 == recursion_limit);  // children of this generation are discarded
+        rp_rays *next = nullptr;
+        if (!last) {
+            if (count + 1 >= max_gens) {
+                rc = RP_ERR_CAPACITY;
+                break;
+            }
+            rc = rp_rays_alloc(ctx, rays->n * 2, &next);
+            if (rc) break;
+        }
+        rc = launch_gen(ctx, s, rays, next, max_length, flags, e2, last ? 0 : 1, -1, -1);
+        if (rc == RP_OK) rc = finish_gen(ctx, next, last ? 0 : 1, st, rays->n);
+        if (rc) {
+            if (next) rp_rays_free(next);
+            break;
+        }
+        count++;
+        if (last) break;
+        gens[count] = next;
+        rays = next;
+        if (next->n == 0) break;
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    if (st) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        st->device_ms += ms;
+    }
+    // traced generations: those with rays that were traced
+    *n_gens = count;
+    if (rc == RP_OK && count < max_gens && gens[count] && gens[count]->n == 0) {
+        rp_rays_free(gens[count]);
+        gens[count] = nullptr;
+    }
+    return rc;
+}
+
+int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_t n, int32_t recursion_limit,
+                       float max_length, uint32_t flags, double e2, void *out_records, uint64_t out_cap,
+                       uint64_t *gen_offsets, int32_t max_gens, int32_t *n_gens, rp_stats *st) {
+    if (!ctx || !s || (n && !in_records) || !gen_offsets || !n_gens || max_gens < 1) return RP_ERR_INVALID;
+    std::vector<rp_rays *> gens(max_gens + 1, nullptr);
+    int rc = rp_rays_alloc(ctx, n, &gens[0]);
+    if (rc) return rc;
+    rc = rp_rays_upload_aos(gens[0], in_records, n);
+    if (rc == RP_OK) rc = rp_trace_rays(ctx, s, gens.data(), max_gens, recursion_limit, max_length, flags, e2, n_gens, st);
+    if (rc == RP_OK) {
+        uint64_t off = 0;
+        gen_offsets[0] = 0;
+        for (int g = 0; g < *n_gens; g++) {
+            uint64_t c = gens[g]->n;
+            if (off + c > out_cap) {
+                rc = RP_ERR_CAPACITY;
+                break;
+            }
+            rc = rp_rays_download_aos(gens[g], (unsigned char *)out_records + off * RP_RAY_BYTES, c);
+            if (rc) break;
+            off += c;
+            gen_offsets[g + 1] = off;
+        }
+    }
+    for (auto *g : gens)
+        if (g) rp_rays_free(g);
+    return rc;
+}
+
+// internal accessors for rp_unit.cu (not part of the public header)
+int rp__scene_view(rp_scene *s, DevScene *out, cudaStream_t *st, int *device) {
+    if (!s) return RP_ERR_INVALID;
+    *out = s->S;
+    *st = s->ctx->stream;
+    *device = s->ctx->device;
+    return RP_OK;
+}
+
+int rp__ctx_stream(rp_ctx *c, cudaStream_t *st, int *device) {
+    if (!c) return RP_ERR_INVALID;
+    *st = c->stream;
+    *device = c->device;
+    return RP_OK;
+}
+
+int rp__scene_curve(rp_scene *s, const rp_dispersion **dcurve, int *n_curves) {
+    if (!s) return RP_ERR_INVALID;
+    *dcurve = s->disp;
+    *n_curves = s->n_disp;
+    return RP_OK;
+}
+
+}  // extern "C"

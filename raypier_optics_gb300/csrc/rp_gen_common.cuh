@@ -1,0 +1,166 @@
+// rp_gen_common.cuh -- the parts of a generation kernel that do not depend on
+// the arithmetic path: shared-memory staging of the scene tables, the
+// block-wide scan of per-ray child counts, the decoupled look-back across
+// tiles and the stable scatter of children.
+//
+// Ordering contract (the reference's RayCollection.add_ray_c append order,
+// raypier/core/ctracer.pyx:1004-1012 driven by trace_segment_c 2083-2117):
+// children are stored in ascending parent index, and a parent's children in
+// emission order (reflected before transmitted).  Tiles take tickets from an
+// atomic counter so that every tile a tile waits on is already running; every
+// wait is bounded and reports ERR_TIMEOUT instead of hanging.
+#pragma once
+#include <cuda/atomic>
+
+#include "rp_kernels.cuh"
+
+namespace rp {
+
+#define RP_LOOKBACK_SPIN_LIMIT (1 << 22)
+
+__device__ __forceinline__ unsigned long long ld_state(unsigned long long *p) {
+    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> r(*p);
+    return r.load(cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ void st_state(unsigned long long *p, unsigned long long v) {
+    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> r(*p);
+    r.store(v, cuda::memory_order_relaxed);
+}
+
+// Stages lists / faces / materials in shared memory; returns the scene view.
+__device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char *smem, unsigned **s_counts) {
+    DevScene S = A.S;
+    size_t nl = (size_t)S.n_lists * sizeof(rp_facelist) / 8;
+    size_t nf = (size_t)S.n_recs * sizeof(rp_face) / 8;
+    size_t nm = (size_t)S.n_mats * sizeof(rp_material) / 8;
+    double *dst = reinterpret_cast<double *>(smem);
+    if (A.smem_tables) {
+        const double *src = reinterpret_cast<const double *>(A.S.lists);
+        for (size_t k = threadIdx.x; k < nl; k += blockDim.x) dst[k] = src[k];
+        src = reinterpret_cast<const double *>(A.S.faces);
+        for (size_t k = threadIdx.x; k < nf; k += blockDim.x) dst[nl + k] = src[k];
+        src = reinterpret_cast<const double *>(A.S.mats);
+        for (size_t k = threadIdx.x; k < nm; k += blockDim.x) dst[nl + nf + k] = src[k];
+        S.lists = reinterpret_cast<const rp_facelist *>(dst);
+        S.faces = reinterpret_cast<const rp_face *>(dst + nl);
+        S.mats = reinterpret_cast<const rp_material *>(dst + nl + nf);
+    }
+    unsigned *cnt = reinterpret_cast<unsigned *>(dst + nl + nf + nm);
+    for (int k = threadIdx.x; k < S.n_faces; k += blockDim.x) cnt[k] = 0;
+    *s_counts = cnt;
+    return S;
+}
+
+// Exclusive block scan of `c` plus the tile's global offset (decoupled
+// look-back).  Returns the thread's global exclusive offset; *total_out gets
+// the block total.  Must be called by all threads of the block.
+__device__ __forceinline__ unsigned long long block_offsets(const GenArgs &A, unsigned tile, unsigned c,
+                                                            unsigned *total_out) {
+    __shared__ unsigned s_warp[RP_BLOCK / 32];
+    __shared__ unsigned long long s_base;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned v = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (unsigned)o) v += t;
+    }
+    if (lane == 31) s_warp[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = (lane < RP_BLOCK / 32) ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (unsigned)o) w += t;
+        }
+        if (lane < RP_BLOCK / 32) s_warp[lane] = w;  // inclusive warp prefixes
+        unsigned long long agg = __shfl_sync(0xffffffffu, w, RP_BLOCK / 32 - 1);
+        unsigned long long excl = 0;
+        if (tile == 0) {
+            if (lane == 0) st_state(&A.tile_state[0], RP_TILE_PREFIX | agg);
+        } else {
+            if (lane == 0) st_state(&A.tile_state[tile], RP_TILE_AGG | agg);
+            long long j = (long long)tile - 1;
+            int spins = 0;
+            while (true) {
+                long long idx = j - (long long)lane;
+                unsigned long long s = (idx >= 0) ? ld_state(&A.tile_state[idx]) : RP_TILE_PREFIX;
+                unsigned flag = (unsigned)(s >> 62);
+                unsigned pm = __ballot_sync(0xffffffffu, flag == 2u);
+                unsigned nr = __ballot_sync(0xffffffffu, flag == 0u);
+                int first_p = pm ? (__ffs(pm) - 1) : 31;
+                unsigned relevant = (first_p == 31) ? 0xffffffffu : ((2u << first_p) - 1u);
+                if (nr & relevant) {
+                    if (++spins > RP_LOOKBACK_SPIN_LIMIT) {
+                        if (lane == 0) atomicOr(A.err, ERR_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                unsigned long long val = ((unsigned)lane <= (unsigned)first_p) ? (s & RP_TILE_VALUE_MASK) : 0ull;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) val += __shfl_down_sync(0xffffffffu, val, o);
+                val = __shfl_sync(0xffffffffu, val, 0);
+                excl += val;
+                if (pm) break;
+                j -= 32;
+            }
+            if (lane == 0) st_state(&A.tile_state[tile], RP_TILE_PREFIX | (excl + agg));
+        }
+        if (lane == 0) {
+            s_base = excl;
+            if (tile == gridDim.x - 1) *A.out_count = excl + agg;
+        }
+    }
+    __syncthreads();
+    unsigned incl_warp_before = (warp > 0) ? s_warp[warp - 1] : 0u;
+    *total_out = s_warp[RP_BLOCK / 32 - 1];
+    return s_base + incl_warp_before + (v - c);
+}
+
+// Writes one child record at slot k of `out`.
+__device__ __forceinline__ void store_child(const RaySoA &out, unsigned long long k, const ChildCommon &cc,
+                                            const Child &ch, double phase, unsigned wl, unsigned parent,
+                                            unsigned endf, unsigned ident) {
+    out.ox[k] = cc.origin.x;
+    out.oy[k] = cc.origin.y;
+    out.oz[k] = cc.origin.z;
+    out.dx[k] = ch.d.x;
+    out.dy[k] = ch.d.y;
+    out.dz[k] = ch.d.z;
+    out.nx[k] = cc.normal.x;
+    out.ny[k] = cc.normal.y;
+    out.nz[k] = cc.normal.z;
+    out.ex[k] = cc.E.x;
+    out.ey[k] = cc.E.y;
+    out.ez[k] = cc.E.z;
+    out.n[k] = ch.n;
+    out.e1[k] = ch.e1;
+    out.e2[k] = ch.e2;
+    out.len[k] = ch.len;
+    out.phase[k] = phase;
+    out.opl[k] = cc.opl;
+    out.wl[k] = wl;
+    out.parent[k] = parent;
+    out.endf[k] = endf;
+    out.ident[k] = ident;
+    out.type[k] = ch.type;
+}
+
+// |E1|^2 + |E2|^2 in the order the oracle uses for the termination rule.
+__device__ __forceinline__ double child_e2(const Child &c) {
+    return c.e1.x * c.e1.x + c.e1.y * c.e1.y + c.e2.x * c.e2.x + c.e2.y * c.e2.y;
+}
+
+// Flushes shared-memory hit counters and block statistics.
+__device__ __forceinline__ void flush_counts(const GenArgs &A, const DevScene &S, unsigned *s_counts) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < S.n_faces; k += blockDim.x) {
+        unsigned c = s_counts[k];
+        if (c) atomicAdd(&A.face_counts[k], c);
+    }
+}
+
+}  // namespace rp

@@ -1,0 +1,313 @@
+// rp_trace.cu -- plain FP64 generation kernel (one launch per generation) and
+// the layout kernels.  Compiled with --fmad=false: every FP64 operation of the
+// nearest-hit search and of the materials rounds as the reference's C does.
+//
+// One thread traces one ray of the generation (trace_segment_c,
+// raypier/core/ctracer.pyx:2062-2118):
+//   1. length = (double)(float)max_length, end_face_idx = -1, far point;
+//   2. for every face list: origin and far point to local coordinates, test
+//      each face, keep the nearest with tolerance < dist < length (strict, so
+//      the earlier face wins a tie: FaceList.intersect_c 1882-1904);
+//   3. on a hit: count it, hit point, orientation (compute_orientation_c
+//      1939-1953), material evaluation into 0..2 children;
+//   4. children are placed by a block scan + decoupled look-back and written
+//      as structure-of-arrays.
+#include "rp_gen_common.cuh"
+
+namespace rp {
+
+__global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ unsigned s_tile;
+    __shared__ unsigned s_hits, s_term;
+    unsigned *s_counts;
+    DevScene S = stage_tables(A, smem, &s_counts);
+    if (threadIdx.x == 0) {
+        s_tile = atomicAdd(A.tile_counter, 1u);
+        s_hits = 0;
+        s_term = 0;
+    }
+    __syncthreads();
+    const unsigned tile = s_tile;
+    const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
+    const bool active = i < A.n_in;
+
+    int best = -1, best_list = -1;
+    double len = A.max_len;
+    v3 o = mkv(0, 0, 0), d = mkv(0, 0, 0);
+    if (active) {
+        o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
+        d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
+        v3 pend = addv(o, mulvs(d, A.max_len));
+        int l0 = 0, l1 = S.n_lists;
+        if (A.one_list >= 0) {
+            l0 = A.one_list;
+            l1 = A.one_list + 1;
+        }
+        for (int l = l0; l < l1; l++) {
+            const rp_facelist &L = S.lists[l];
+            v3 p1 = xform(L.inv_trans.m, L.inv_trans.t, o);
+            v3 p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
+            int f0 = L.first_face, f1 = L.first_face + L.n_faces;
+            if (A.one_face >= 0) {
+                f0 = L.first_face + A.one_face;
+                f1 = f0 + 1;
+            }
+            for (int f = f0; f < f1; f++) {
+                const rp_face &F = S.faces[f];
+                double dist = face_isect(S, F, p1, p2, A.err);
+                if (F.tolerance < dist && dist < len) {
+                    len = dist;
+                    best = f;
+                    best_list = l;
+                }
+            }
+        }
+        A.in.len[i] = len;
+        A.in.endf[i] = best >= 0 ? (unsigned)S.faces[best].idx : 0xFFFFFFFFu;
+        if (best >= 0) {
+            atomicAdd(&s_counts[best], 1u);
+            atomicAdd(&s_hits, 1u);
+        }
+    }
+
+    if (!A.emit) {
+        flush_counts(A, S, s_counts);
+        if (threadIdx.x == 0) atomicAdd(&A.stats[0], (unsigned long long)s_hits);
+        return;
+    }
+
+    // material evaluation
+    Child ch[2];
+    ChildCommon cc;
+    int nc = 0;
+    if (active && best >= 0) {
+        const rp_facelist &L = S.lists[best_list];
+        const rp_face &F = S.faces[best];
+        v3 point = addv(o, mulvs(d, len));
+        v3 lp = xform(L.inv_trans.m, L.inv_trans.t, point);
+        v3 nrm = face_normal(S, F, lp, A.err);
+        v3 tng = face_tangent(F);
+        if (F.invert_normal) {
+            nrm = negv(nrm);
+            tng = negv(tng);
+        }
+        nrm = rotv(L.trans.m, nrm);
+        tng = rotv(L.trans.m, tng);
+        if (F.material >= 0) {
+            RayState r;
+            r.o = o;
+            r.d = d;
+            r.E = mkv(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
+            r.n = A.in.n[i];
+            r.e1 = A.in.e1[i];
+            r.e2 = A.in.e2[i];
+            r.len = len;
+            r.opl = A.in.opl[i];
+            r.type = A.in.type[i];
+            r.wl = A.in.wl[i];
+            nc = eval_children(S, S.mats[F.material], r, point, nrm, tng, cc, ch);
+            if (A.e2_term > 0.0 && nc > 0) {
+                int w = 0;
+                for (int k = 0; k < nc; k++) {
+                    if (!(child_e2(ch[k]) < A.e2_term)) {
+                        if (w != k) ch[w] = ch[k];
+                        w++;
+                    }
+                }
+                if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
+                nc = w;
+            }
+        }
+    }
+
+    unsigned total;
+    unsigned long long base = block_offsets(A, tile, (unsigned)nc, &total);
+    if (nc > 0) {
+        double phase = A.in.phase[i];
+        unsigned wl = A.in.wl[i], ident = A.in.ident[i];
+        unsigned endf = (unsigned)S.faces[best].idx;
+        for (int k = 0; k < nc; k++) {
+            unsigned long long slot = base + k;
+            if (slot < A.out_cap) store_child(A.out, slot, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
+            else atomicOr(A.err, ERR_OVERFLOW);
+        }
+    }
+    flush_counts(A, S, s_counts);
+    if (threadIdx.x == 0) {
+        atomicAdd(&A.stats[0], (unsigned long long)s_hits);
+        if (s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
+    }
+}
+
+size_t generation_smem_bytes(int n_lists, int n_recs, int n_mats, int n_faces) {
+    return (size_t)n_lists * sizeof(rp_facelist) + (size_t)n_recs * sizeof(rp_face) +
+           (size_t)n_mats * sizeof(rp_material) + (size_t)n_faces * sizeof(unsigned);
+}
+
+cudaError_t launch_generation_plain(const GenArgs &a, size_t smem, cudaStream_t st) {
+    if (a.n_in == 0) return cudaSuccess;
+    unsigned grid = (unsigned)((a.n_in + RP_BLOCK - 1) / RP_BLOCK);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(generation_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    generation_plain_kernel<<<grid, RP_BLOCK, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ---- AoS <-> SoA ----------------------------------------------------------
+// The packed 188-byte record (include/rp_gb300.h rp_ray) is not 16-byte
+// aligned per ray, but 128 consecutive records (24,064 bytes) are, so a block
+// moves its 128 records through shared memory with 16-byte accesses and each
+// thread then (de)assembles its own record from 4-byte words.
+#define RP_AOS_WORDS (RP_RAY_BYTES / 4)
+
+__device__ __forceinline__ double w2d(const unsigned *w, int k) {
+    return __hiloint2double((int)w[k + 1], (int)w[k]);
+}
+__device__ __forceinline__ void d2w(unsigned *w, int k, double v) {
+    w[k] = (unsigned)__double2loint(v);
+    w[k + 1] = (unsigned)__double2hiint(v);
+}
+
+__global__ void __launch_bounds__(RP_BLOCK) aos_to_soa_kernel(const unsigned char *aos, RaySoA soa,
+                                                                unsigned long long n) {
+    __shared__ __align__(16) unsigned sw[RP_BLOCK * RP_AOS_WORDS];
+    unsigned long long r0 = (unsigned long long)blockIdx.x * RP_BLOCK;
+    unsigned long long nr = n - r0 < RP_BLOCK ? n - r0 : RP_BLOCK;
+    const unsigned *src = reinterpret_cast<const unsigned *>(aos + r0 * RP_RAY_BYTES);
+    unsigned nwords = (unsigned)(nr * RP_AOS_WORDS);
+    if (nr == RP_BLOCK) {
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+        uint4 *d4 = reinterpret_cast<uint4 *>(sw);
+        for (unsigned k = threadIdx.x; k < nwords / 4; k += RP_BLOCK) d4[k] = s4[k];
+    } else {
+        for (unsigned k = threadIdx.x; k < nwords; k += RP_BLOCK) sw[k] = src[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < nr) {
+        const unsigned *w = sw + threadIdx.x * RP_AOS_WORDS;
+        unsigned long long i = r0 + threadIdx.x;
+        soa.ox[i] = w2d(w, 0);  soa.oy[i] = w2d(w, 2);  soa.oz[i] = w2d(w, 4);
+        soa.dx[i] = w2d(w, 6);  soa.dy[i] = w2d(w, 8);  soa.dz[i] = w2d(w, 10);
+        soa.nx[i] = w2d(w, 12); soa.ny[i] = w2d(w, 14); soa.nz[i] = w2d(w, 16);
+        soa.ex[i] = w2d(w, 18); soa.ey[i] = w2d(w, 20); soa.ez[i] = w2d(w, 22);
+        soa.n[i] = make_double2(w2d(w, 24), w2d(w, 26));
+        soa.e1[i] = make_double2(w2d(w, 28), w2d(w, 30));
+        soa.e2[i] = make_double2(w2d(w, 32), w2d(w, 34));
+        soa.len[i] = w2d(w, 36);
+        soa.phase[i] = w2d(w, 38);
+        soa.opl[i] = w2d(w, 40);
+        soa.wl[i] = w[42];
+        soa.parent[i] = w[43];
+        soa.endf[i] = w[44];
+        soa.ident[i] = w[45];
+        soa.type[i] = w[46];
+    }
+}
+
+__global__ void __launch_bounds__(RP_BLOCK) soa_to_aos_kernel(RaySoA soa, unsigned char *aos,
+                                                                unsigned long long n) {
+    __shared__ __align__(16) unsigned sw[RP_BLOCK * RP_AOS_WORDS];
+    unsigned long long r0 = (unsigned long long)blockIdx.x * RP_BLOCK;
+    unsigned long long nr = n - r0 < RP_BLOCK ? n - r0 : RP_BLOCK;
+    if (threadIdx.x < nr) {
+        unsigned *w = sw + threadIdx.x * RP_AOS_WORDS;
+        unsigned long long i = r0 + threadIdx.x;
+        d2w(w, 0, soa.ox[i]);  d2w(w, 2, soa.oy[i]);  d2w(w, 4, soa.oz[i]);
+        d2w(w, 6, soa.dx[i]);  d2w(w, 8, soa.dy[i]);  d2w(w, 10, soa.dz[i]);
+        d2w(w, 12, soa.nx[i]); d2w(w, 14, soa.ny[i]); d2w(w, 16, soa.nz[i]);
+        d2w(w, 18, soa.ex[i]); d2w(w, 20, soa.ey[i]); d2w(w, 22, soa.ez[i]);
+        double2 c = soa.n[i];
+        d2w(w, 24, c.x); d2w(w, 26, c.y);
+        c = soa.e1[i];
+        d2w(w, 28, c.x); d2w(w, 30, c.y);
+        c = soa.e2[i];
+        d2w(w, 32, c.x); d2w(w, 34, c.y);
+        d2w(w, 36, soa.len[i]);
+        d2w(w, 38, soa.phase[i]);
+        d2w(w, 40, soa.opl[i]);
+        w[42] = soa.wl[i];
+        w[43] = soa.parent[i];
+        w[44] = soa.endf[i];
+        w[45] = soa.ident[i];
+        w[46] = soa.type[i];
+    }
+    __syncthreads();
+    unsigned *dst = reinterpret_cast<unsigned *>(aos + r0 * RP_RAY_BYTES);
+    unsigned nwords = (unsigned)(nr * RP_AOS_WORDS);
+    if (nr == RP_BLOCK) {
+        uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(sw);
+        for (unsigned k = threadIdx.x; k < nwords / 4; k += RP_BLOCK) d4[k] = s4[k];
+    } else {
+        for (unsigned k = threadIdx.x; k < nwords; k += RP_BLOCK) dst[k] = sw[k];
+    }
+}
+
+cudaError_t launch_aos_to_soa(const void *aos, RaySoA soa, unsigned long long n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    unsigned grid = (unsigned)((n + RP_BLOCK - 1) / RP_BLOCK);
+    aos_to_soa_kernel<<<grid, RP_BLOCK, 0, st>>>(reinterpret_cast<const unsigned char *>(aos), soa, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(RaySoA soa, void *aos, unsigned long long n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    unsigned grid = (unsigned)((n + RP_BLOCK - 1) / RP_BLOCK);
+    soa_to_aos_kernel<<<grid, RP_BLOCK, 0, st>>>(soa, reinterpret_cast<unsigned char *>(aos), n);
+    return cudaGetLastError();
+}
+
+// ---- dispersion tables: BaseDispersionCurve.c_evaluate_n (cmaterials.pyx:206-228)
+static __device__ double curve_n(const rp_dispersion &c, const double *coefs, double wavelen) {
+    switch (c.formula_id) {
+        case 0: return coefs[0];  // nondispersive_0, 107-108
+        case 1: {                 // sellmeier_1, 110-119
+            double n2 = 1.0, wl2 = wavelen * wavelen;
+            n2 += coefs[0];
+            for (int i = 0; i < (c.n_coefs - 1) / 2; i++) {
+                double b = coefs[2 * i + 2];
+                n2 += coefs[2 * i + 1] * wl2 / (wl2 - b * b);
+            }
+            return sqrt(n2);
+        }
+        case 2: {  // sellmeier_2, 121-130
+            double n2 = 1.0, wl2 = wavelen * wavelen;
+            n2 += coefs[0];
+            for (int i = 0; i < (c.n_coefs - 1) / 2; i++) n2 += coefs[2 * i + 1] * wl2 / (wl2 - coefs[2 * i + 2]);
+            return sqrt(n2);
+        }
+        case 3: {  // sellmeier_3, 133-140
+            double n2 = coefs[0];
+            for (int i = 1; i < c.n_coefs - 1; i += 2) n2 += coefs[i] * (pow(wavelen, coefs[i + 1]));
+            return sqrt(n2);
+        }
+        default: return nan_d();
+    }
+}
+
+__global__ void dispersion_table_kernel(const rp_dispersion *curves, int n_curves, const double *aux,
+                                        const double *wl, long long n_wl, double2 *ntab) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n_curves * n_wl) return;
+    int c = (int)(t / n_wl);
+    long long i = t - (long long)c * n_wl;
+    rp_dispersion cv = curves[c];
+    double n_imag = 0.0001 * cv.absorption / (4 * 3.14159265358979323846);
+    ntab[t] = make_double2(curve_n(cv, aux + cv.aux, wl[i]), n_imag * wl[i]);
+}
+
+cudaError_t launch_dispersion_table(const rp_dispersion *curves, int n_curves, const double *aux,
+                                    const double *wl, long long n_wl, double2 *ntab, cudaStream_t st) {
+    long long n = (long long)n_curves * n_wl;
+    if (n == 0) return cudaSuccess;
+    dispersion_table_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(curves, n_curves, aux, wl, n_wl, ntab);
+    return cudaGetLastError();
+}
+
+}  // namespace rp
