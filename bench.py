@@ -1,0 +1,352 @@
+"""Benchmark of the non-sequential tracing hot path on GB300.
+
+Workload (default): the 1,048,576-ray, 10-face polarised doublet/asphere
+system with per-ray Sellmeier dispersion and Fresnel splitting, 8
+generations, |E|^2 < 1e-6 termination (raypier_optics_gb300.workloads.config2).
+One step = one full trace_rays of that workload.
+
+  value  ray-segments/s with the input rays already resident in HBM
+         (rp_trace_rays on a device buffer; scene uploaded once)
+  e2e    the same metric through the C-ABI host-buffer call
+         rp_trace_rays_host: pinned host input records -> device -> all
+         generations back into pinned host memory, copies inside the timing
+  roofline  the generation kernel's algorithmic HBM bytes / its measured time
+  cpu_baseline  the reference's Cython tracer (or the C port when the reference
+         cannot be built) on the host cores, on a bounded sample
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+       [--workload config2|config1|config3] [--flags plain|mixed]
+Under torchrun (N > 1) every rank traces its own 1,048,576-ray shard (weak
+scaling: independent rays, no data-path collective); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+METRIC = "ray-segments/s at 1M rays, mixed vs plain FP64 on 1 GB300; p50/p99 job latency"
+UNIT = "ray-segments/s"
+# algorithmic bytes per traced ray (SoA): origin, direction, E_vector (72),
+# n, E1, E2 (48), OPL, phase (16), wavelength_idx, type, ident (12), the
+# per-ray wavelength (8); written back: length, end_face_idx (12)
+BYTES_PER_SEGMENT = 72 + 48 + 16 + 12 + 8 + 12
+BYTES_PER_CHILD = 188
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
+    ap.add_argument("--flags", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--rays", type=int, default=0, help="override the ray count")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="rays in the CPU-baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def workload(name, rays_override=0, rank=0):
+    from raypier_optics_gb300 import ctracer
+    from raypier_optics_gb300 import workloads as W
+    if name == "config1":
+        n = rays_override or 4096
+        rays, wl = W.config1_rays(ctracer.ray_dtype, n)
+        return W.config1_spec(), rays, wl, W.CONFIG1, False
+    if name == "config2":
+        n = rays_override or (1 << 20)
+        rays, wl = W.config2_rays(ctracer.ray_dtype, n, seed=2 + 1000 * rank)
+        return W.config2_spec(), rays, wl, W.CONFIG2, True
+    n = rays_override or (1 << 20)
+    rays, wl = W.config3_rays(ctracer.ray_dtype, n, first_block=rank * ((n + 65535) // 65536))
+    return W.config3_spec(), rays, wl, W.CONFIG3, False
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                               f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(name, rays, wl, per_ray, sample):
+    import cpu_bench
+    n = min(sample, rays.shape[0])
+    idx = np.linspace(0, rays.shape[0] - 1, n).astype(np.int64)
+    r = cpu_bench.time_cpu(name, rays[idx], wl, per_ray)
+    r["sample"] = (f"{n} rays spread over the {rays.shape[0]}-ray workload, all generations, "
+                   f"{r['cores']} processes on {cpu_bench.cpu_model()}")
+    return r
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    spec, rays, wl, P, per_ray = workload(args.workload, args.rays)
+    import cpu_bench
+    sample = args.cpu_sample or 16384
+    n = min(sample, rays.shape[0])
+    idx = np.linspace(0, rays.shape[0] - 1, n).astype(np.int64)
+    for _ in range(args.warmup):
+        cpu_bench.time_cpu(args.workload, rays[idx[: max(len(idx) // 8, 64)]], wl, per_ray)
+    vals, segs, secs, res = [], 0, 0.0, None
+    for _ in range(args.steps):
+        res = cpu_bench.time_cpu(args.workload, rays[idx], wl, per_ray)
+        segs += res["segments"]
+        secs += res["seconds"]
+    value = segs / secs
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, PCG64)",
+            "impl": "reference",
+            "config": {"workload": f"{args.workload}: {rays.shape[0]} rays, sampled", "rays_per_step": n,
+                       "recursion_limit": P["recursion_limit"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["cores"], "kind": res["kind"],
+                             "sample": f"{n} rays of {rays.shape[0]} per step, {res['cores']} processes on "
+                                       f"{cpu_bench.cpu_model()}"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    rank, world, local = dist_env()
+    spec, rays, wl, P, per_ray = workload(args.workload, args.rays, rank)
+
+    # CPU baseline first: its worker processes start before any GPU context exists
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.workload, rays, wl, per_ray, args.cpu_sample or 16384)
+
+    from raypier_optics_gb300 import _native, runtime, scene
+    from raypier_optics_gb300 import workloads as W
+    from raypier_optics_gb300.ctracer import ray_dtype
+    import types
+    from raypier_optics_gb300 import cdistortions, cfaces, cmaterials, cshapes, ctracer
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        tdist.init_process_group("gloo")
+        dist = tdist
+        device = local
+    else:
+        device = 0
+    ctx = runtime.Context(device)
+    lib = ctx.lib
+    ns = types.SimpleNamespace(ctracer=ctracer, cfaces=cfaces, cmaterials=cmaterials, cshapes=cshapes,
+                               cdistortions=cdistortions)
+    lists = W.build_scene(spec, ns)
+    faces = [f for fl in lists for f in fl.faces]
+    for i, f in enumerate(faces):
+        f.idx = i
+        f.update()
+    tables = scene.compile_scene(lists)
+    dscene = runtime.DeviceScene(ctx, tables, wl)
+    flags = 1 if args.flags == "mixed" else 0
+    e2 = P["e2_terminate"]
+    rl = P["recursion_limit"]
+    max_len = ctypes.c_float(P["max_length"])
+    n = rays.shape[0]
+    max_gens = rl + 1
+
+    # ---- device-resident throughput ---------------------------------------------------
+    g0 = runtime.DeviceRays(ctx, n)
+    g0.upload(np.ascontiguousarray(rays))
+
+    def step(stats):
+        gens = (ctypes.c_void_p * max_gens)()
+        gens[0] = g0.handle
+        ng = ctypes.c_int32(0)
+        _native.check(lib.rp_trace_rays(ctx.handle, dscene.handle, gens, max_gens, rl, max_len, flags, e2,
+                                        ctypes.byref(ng), ctypes.byref(stats)), "rp_trace_rays")
+        for g in range(1, max_gens):
+            if gens[g]:
+                lib.rp_rays_free(ctypes.c_void_p(gens[g]))
+        return ng.value
+
+    for _ in range(max(args.warmup, 0)):
+        step(_native.Stats())
+    ctx.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(device)
+    clocks.start()
+    stats = _native.Stats()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ng = step(stats)
+    ctx.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_s = stats.device_ms / 1000.0
+    segs = stats.rays_in
+    children = stats.rays_out
+    if dist:
+        import torch
+        t = torch.tensor([dev_s, float(segs)], dtype=torch.float64)
+        tmax = torch.tensor([dev_s], dtype=torch.float64)
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        tsum = torch.tensor([float(segs)], dtype=torch.float64)
+        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        dev_s, segs_total = float(tmax[0]), float(tsum[0])
+    else:
+        segs_total = float(segs)
+    value = segs_total / dev_s
+    seg_per_step = segs / args.steps
+
+    # roofline of the generation kernel
+    alg_bytes = segs * BYTES_PER_SEGMENT + children * BYTES_PER_CHILD
+    kern_s = stats.kernel_ms / 1000.0
+    achieved = alg_bytes / kern_s / 1e9
+    peak, peak_kind = measured_peak_hbm()
+
+    # ---- end to end through the host-buffer C ABI -----------------------------------------
+    # output capacity: the measured segment count of a step plus headroom
+    out_cap = int(seg_per_step * 1.05) + n
+    pin_in = ctypes.c_void_p()
+    pin_out = ctypes.c_void_p()
+    _native.check(lib.rp_host_alloc(n * 188, ctypes.byref(pin_in)), "rp_host_alloc")
+    _native.check(lib.rp_host_alloc(out_cap * 188, ctypes.byref(pin_out)), "rp_host_alloc")
+    ctypes.memmove(pin_in, np.ascontiguousarray(rays).ctypes.data, n * 188)
+    offs = (ctypes.c_uint64 * (max_gens + 1))()
+    e2e_steps = max(1, min(args.steps, 5))
+
+    def e2e_step(st):
+        ng = ctypes.c_int32(0)
+        _native.check(lib.rp_trace_rays_host(ctx.handle, dscene.handle, pin_in, n, rl, max_len, flags, e2, pin_out,
+                                             out_cap, offs, max_gens, ctypes.byref(ng), ctypes.byref(st)),
+                      "rp_trace_rays_host")
+        return offs[ng.value]
+
+    e2e_step(_native.Stats())
+    ctx.synchronize()
+    if dist:
+        dist.barrier()
+    est = _native.Stats()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(e2e_steps):
+        d2h += e2e_step(est) * 188
+    ctx.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        import torch
+        tmax = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        e2e_s = float(tmax[0])
+    e2e_value = (est.rays_in * world) / e2e_s
+    lib.rp_host_free(pin_in)
+    lib.rp_host_free(pin_out)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if flags == 0 else "f32+f64",
+            "data": "synthetic (seeded PCG64 rays; no dataset)",
+            "config": {"workload": f"{args.workload}: {n} rays, {len(faces)} faces, {rl} generations, "
+                                   f"|E|^2<{e2} termination, path={args.flags}",
+                       "segments_per_step": seg_per_step, "generations": ng,
+                       "l2": "inputs larger than L2 (197 MB of input records, GBs of generations per step)",
+                       "timing": "CUDA events on the library stream around each trace call (device time); "
+                                 f"host wall {1000.0 * wall / args.steps:.2f} ms/step"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 188,
+                    "d2h_bytes_per_step": int(d2h / e2e_steps), "steps": e2e_steps,
+                    "api": "rp_trace_rays_host (pinned host records in and out)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "generation_plain_kernel" if flags == 0 else "generation_mixed_kernel",
+                         "note": f"algorithmic bytes {BYTES_PER_SEGMENT} B/segment + {BYTES_PER_CHILD} B/child "
+                                 f"over summed generation-kernel time; peak {peak_kind}"},
+            "gpu_launches": int(stats.launches),
+            "clocks": clk,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": cpu["kind"],
+                                    "sample": cpu["sample"]}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

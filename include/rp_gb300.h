@@ -208,7 +208,10 @@ typedef struct rp_stats {
     uint64_t rays_out;       /* children kept */
     uint64_t hits;           /* rays that hit a face */
     uint64_t terminated;     /* children dropped by the |E|^2 rule */
-    double   device_ms;      /* device time of the traced generations */
+    double   device_ms;      /* device time of the call (CUDA events on the context stream) */
+    double   kernel_ms;      /* summed device time of the generation kernels alone */
+    uint64_t launches;       /* kernels this library launched for the call */
+    uint64_t generations;    /* generation kernels among them */
 } rp_stats;
 
 /* Trace flags. */
@@ -231,8 +234,13 @@ const char *rp_last_error(void);
 int rp_ctx_create(int device, uint64_t hbm_budget, rp_ctx **out);
 int rp_ctx_destroy(rp_ctx *ctx);
 int rp_ctx_synchronize(rp_ctx *ctx);
-/* Bytes of device memory the context holds. */
+/* Bytes of device memory the context holds (live buffers, cached blocks and scratch). */
 int rp_ctx_memory(rp_ctx *ctx, uint64_t *bytes_in_use);
+/* Return cached device blocks of freed ray buffers to CUDA. */
+int rp_ctx_trim(rp_ctx *ctx);
+/* Page-locked host memory for fast host<->device copies of ray records. */
+int rp_host_alloc(uint64_t bytes, void **ptr);
+int rp_host_free(void *ptr);
 
 /* ---- scenes ------------------------------------------------------------- */
 /* Upload a scene.  `wavelengths` is the RayCollection.wavelengths array that

@@ -133,7 +133,8 @@ class SceneDesc(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("rays_in", ctypes.c_uint64), ("rays_out", ctypes.c_uint64),
                 ("hits", ctypes.c_uint64), ("terminated", ctypes.c_uint64),
-                ("device_ms", ctypes.c_double)]
+                ("device_ms", ctypes.c_double), ("kernel_ms", ctypes.c_double),
+                ("launches", ctypes.c_uint64), ("generations", ctypes.c_uint64)]
 
 
 # Every symbol the header declares, with its ctypes signature.
@@ -147,6 +148,9 @@ _SIGS = {
     "rp_ctx_destroy": (_I, [_P]),
     "rp_ctx_synchronize": (_I, [_P]),
     "rp_ctx_memory": (_I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    "rp_ctx_trim": (_I, [_P]),
+    "rp_host_alloc": (_I, [ctypes.c_uint64, ctypes.POINTER(_P)]),
+    "rp_host_free": (_I, [_P]),
     "rp_scene_create": (_I, [_P, ctypes.POINTER(SceneDesc), _P, ctypes.c_int64, ctypes.POINTER(_P)]),
     "rp_scene_destroy": (_I, [_P]),
     "rp_scene_face_counts": (_I, [_P, _P, ctypes.c_int32, _I]),

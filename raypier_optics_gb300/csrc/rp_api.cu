@@ -25,11 +25,19 @@ static int cuda_fail(cudaError_t e, const char *what) {
         if (_e != cudaSuccess) return cuda_fail(_e, #call); \
     } while (0)
 
+struct PoolBlock {
+    void *p;
+    size_t bytes;
+};
+
 struct rp_ctx {
     int device;
     cudaStream_t stream;
     uint64_t budget;
-    uint64_t in_use;
+    uint64_t in_use;                 // bytes of live allocations
+    std::vector<PoolBlock> pool;     // freed blocks kept for reuse
+    uint64_t pooled;                 // bytes in `pool`
+    std::vector<cudaEvent_t> gen_ev; // per-generation kernel events (pairs)
     // per-generation scan scratch: [counter | out_count | err | pad | stats[2] | tile states...]
     unsigned char *scratch;
     size_t scratch_bytes;
@@ -60,22 +68,59 @@ struct rp_rays {
     RaySoA soa;
 };
 
-// ---- memory accounting ------------------------------------------------------
-static int ctx_alloc(rp_ctx *ctx, void **p, size_t bytes) {
+// ---- memory: a per-context caching allocator ----------------------------------
+// Freed blocks are kept and handed out again to requests of up to the same
+// size (best fit, at most 2x larger), so a steady tracing loop allocates no
+// device memory after its first iteration.  Blocks are released to CUDA when
+// the budget would otherwise be exceeded, by rp_ctx_trim, and at destroy.
+static void pool_release_all(rp_ctx *ctx) {
+    for (auto &b : ctx->pool) cudaFree(b.p);
+    ctx->pool.clear();
+    ctx->pooled = 0;
+}
+
+static int ctx_alloc(rp_ctx *ctx, void **p, size_t bytes, size_t *got) {
+    bytes = bytes ? bytes : 16;
+    *got = bytes;
+    int best = -1;
+    for (size_t k = 0; k < ctx->pool.size(); k++) {
+        size_t b = ctx->pool[k].bytes;
+        if (b >= bytes && b <= 2 * bytes && (best < 0 || b < ctx->pool[best].bytes)) best = (int)k;
+    }
+    if (best >= 0) {
+        *p = ctx->pool[best].p;
+        size_t b = ctx->pool[best].bytes;
+        *got = b;
+        ctx->pool.erase(ctx->pool.begin() + best);
+        ctx->pooled -= b;
+        ctx->in_use += b;
+        return RP_OK;
+    }
+    if (ctx->budget && ctx->in_use + ctx->pooled + bytes > ctx->budget) pool_release_all(ctx);
     if (ctx->budget && ctx->in_use + bytes > ctx->budget) {
         snprintf(g_last_error, sizeof g_last_error, "device budget of %llu bytes exceeded",
                  (unsigned long long)ctx->budget);
         return RP_ERR_BUDGET;
     }
-    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation && !ctx->pool.empty()) {
+        cudaGetLastError();
+        pool_release_all(ctx);
+        e = cudaMalloc(p, bytes);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
     ctx->in_use += bytes;
     return RP_OK;
 }
+
+// Returns the block to the pool; `bytes` must be the size it was allocated
+// with (pool blocks keep their own size).
 static void ctx_free(rp_ctx *ctx, void *p, size_t bytes) {
     if (!p) return;
-    cudaFree(p);
+    bytes = bytes ? bytes : 16;
     ctx->in_use -= bytes;
+    ctx->pool.push_back(PoolBlock{p, bytes});
+    ctx->pooled += bytes;
 }
 
 extern "C" {
@@ -125,6 +170,8 @@ int rp_ctx_destroy(rp_ctx *c) {
     if (!c) return RP_ERR_INVALID;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    pool_release_all(c);
+    for (auto ev : c->gen_ev) cudaEventDestroy(ev);
     if (c->scratch) cudaFree(c->scratch);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     cudaEventDestroy(c->ev0);
@@ -142,7 +189,27 @@ int rp_ctx_synchronize(rp_ctx *c) {
 
 int rp_ctx_memory(rp_ctx *c, uint64_t *bytes) {
     if (!c || !bytes) return RP_ERR_INVALID;
-    *bytes = c->in_use + c->scratch_bytes;
+    *bytes = c->in_use + c->pooled + c->scratch_bytes;
+    return RP_OK;
+}
+
+int rp_ctx_trim(rp_ctx *c) {
+    if (!c) return RP_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    pool_release_all(c);
+    return RP_OK;
+}
+
+int rp_host_alloc(uint64_t bytes, void **ptr) {
+    if (!ptr) return RP_ERR_INVALID;
+    CK(cudaMallocHost(ptr, bytes ? bytes : 16));
+    return RP_OK;
+}
+
+int rp_host_free(void *ptr) {
+    if (!ptr) return RP_OK;
+    CK(cudaFreeHost(ptr));
     return RP_OK;
 }
 
@@ -160,17 +227,23 @@ static int validate_scene(const rp_scene_desc *d) {
         expect += L.n_faces;
     }
     if (expect != d->n_faces) return RP_ERR_INVALID;
+    auto aux_ok = [&](long long off, long long count) { return off >= 0 && count >= 0 && off + count <= d->n_aux; };
+    for (int k = 0; k < d->n_shape_ops; k++) {
+        const rp_shape_op &op = d->shape_ops[k];
+        if (op.op < RP_SHAPE_END || op.op > RP_SHAPE_NOT) return RP_ERR_UNSUPPORTED;
+        if (op.op == RP_SHAPE_POLYGON && !aux_ok(op.aux, 2LL * op.n)) return RP_ERR_INVALID;
+    }
     for (int f = 0; f < d->n_face_records; f++) {
         const rp_face &F = d->faces[f];
         if (F.type < RP_FACE_NONE || F.type > RP_FACE_ELLIPTICAL_PLANE) return RP_ERR_UNSUPPORTED;
         if (f < d->n_faces && (F.material < 0 || F.material >= d->n_materials)) return RP_ERR_INVALID;
-        if (F.shape >= d->n_shape_ops) return RP_ERR_INVALID;
-        if (F.aux < 0 || F.aux + F.n_aux0 * (F.n_aux1 > 0 ? F.n_aux1 : 2) > d->n_aux + 0) {
-            if (F.type == RP_FACE_EXTPOLY || F.type == RP_FACE_ORIENTED_POLYGON || F.type == RP_FACE_POLYGON)
-                return RP_ERR_INVALID;
+        if (F.shape < -1 || F.shape >= d->n_shape_ops) return RP_ERR_INVALID;
+        if (F.type == RP_FACE_EXTPOLY) {
+            if (F.n_aux0 < 1 || F.n_aux0 > 8 || F.n_aux1 < 1 || F.n_aux1 > 8) return RP_ERR_UNSUPPORTED;
+            if (!aux_ok(F.aux, (long long)F.n_aux0 * F.n_aux1)) return RP_ERR_INVALID;
         }
-        if (F.type == RP_FACE_EXTPOLY && (F.n_aux0 < 1 || F.n_aux0 > 8 || F.n_aux1 < 1 || F.n_aux1 > 8))
-            return RP_ERR_UNSUPPORTED;
+        if ((F.type == RP_FACE_ORIENTED_POLYGON || F.type == RP_FACE_POLYGON) && !aux_ok(F.aux, 2LL * F.n_aux0))
+            return RP_ERR_INVALID;
         if (F.type == RP_FACE_DISTORTION) {
             if (F.base < d->n_faces || F.base >= d->n_face_records) return RP_ERR_INVALID;
             if (d->faces[F.base].type == RP_FACE_DISTORTION) return RP_ERR_UNSUPPORTED;
@@ -191,8 +264,18 @@ static int validate_scene(const rp_scene_desc *d) {
     }
     for (int k = 0; k < d->n_distortions; k++) {
         const rp_distortion &D = d->distortions[k];
-        if (D.type == RP_DIST_ZERNIKE && (D.k_max < 0 || D.k_max > 48)) return RP_ERR_UNSUPPORTED;
+        if (D.type != RP_DIST_ZERNIKE && D.type != RP_DIST_SIMPLE_J7) return RP_ERR_UNSUPPORTED;
+        if (D.type == RP_DIST_ZERNIKE) {
+            if (D.k_max < 0 || D.k_max > 48) return RP_ERR_UNSUPPORTED;
+            if (!aux_ok(D.aux, 5LL * D.n_coefs)) return RP_ERR_INVALID;
+            for (int i = 0; i < D.n_coefs; i++) {
+                double n = d->aux[D.aux + 5 * i + 1], m = d->aux[D.aux + 5 * i + 2], kk = d->aux[D.aux + 5 * i + 3];
+                if (n < 0 || n > 8 || m < -n || m > n || kk < 0 || kk >= 48) return RP_ERR_UNSUPPORTED;
+            }
+        }
     }
+    for (int c = 0; c < d->n_dispersions; c++)
+        if (!aux_ok(d->dispersions[c].aux, d->dispersions[c].n_coefs)) return RP_ERR_INVALID;
     return RP_OK;
 }
 
@@ -235,12 +318,11 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     size_t o_ntab = o_wl + align256(sizeof(double) * (size_t)n_wl);
     size_t o_cnt = o_ntab + align256(sizeof(double2) * (size_t)n_wl * d->n_dispersions);
     size_t total = o_cnt + align256(sizeof(unsigned) * (d->n_face_records + 1));
-    int rc = ctx_alloc(ctx, &s->dev_block, total);
+    int rc = ctx_alloc(ctx, &s->dev_block, total, &s->dev_bytes);
     if (rc) {
         delete s;
         return rc;
     }
-    s->dev_bytes = total;
     unsigned char *b = (unsigned char *)s->dev_block;
     cudaStream_t st = ctx->stream;
     cudaError_t e = cudaSuccess;
@@ -347,8 +429,7 @@ int rp_rays_alloc(rp_ctx *ctx, uint64_t cap, rp_rays **out) {
     r->ctx = ctx;
     r->cap = cap ? cap : 1;
     r->n = 0;
-    r->bytes = soa_bytes(r->cap);
-    int rc = ctx_alloc(ctx, &r->block, r->bytes);
+    int rc = ctx_alloc(ctx, &r->block, soa_bytes(r->cap), &r->bytes);
     if (rc) {
         delete r;
         return rc;
@@ -381,7 +462,7 @@ int rp_rays_capacity(const rp_rays *r, uint64_t *cap) {
 
 // Host AoS <-> device SoA goes through a device staging buffer of packed
 // records (one cudaMemcpyAsync) and the layout kernels.
-static int with_staging(rp_ctx *ctx, size_t bytes, void **p) { return ctx_alloc(ctx, p, bytes); }
+static int with_staging(rp_ctx *ctx, size_t bytes, void **p, size_t *got) { return ctx_alloc(ctx, p, bytes, got); }
 
 int rp_rays_upload_aos(rp_rays *r, const void *records, uint64_t n) {
     if (!r || (n && !records)) return RP_ERR_INVALID;
@@ -389,14 +470,14 @@ int rp_rays_upload_aos(rp_rays *r, const void *records, uint64_t n) {
     rp_ctx *ctx = r->ctx;
     CK(cudaSetDevice(ctx->device));
     void *stage = nullptr;
-    size_t bytes = (size_t)n * RP_RAY_BYTES;
+    size_t bytes = (size_t)n * RP_RAY_BYTES, got = 0;
     if (n) {
-        int rc = with_staging(ctx, bytes, &stage);
+        int rc = with_staging(ctx, bytes, &stage, &got);
         if (rc) return rc;
         cudaError_t e = cudaMemcpyAsync(stage, records, bytes, cudaMemcpyHostToDevice, ctx->stream);
         if (e == cudaSuccess) e = launch_aos_to_soa(stage, r->soa, n, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        ctx_free(ctx, stage, bytes);
+        ctx_free(ctx, stage, got);
         if (e != cudaSuccess) return cuda_fail(e, "rp_rays_upload_aos");
     }
     r->n = n;
@@ -410,13 +491,13 @@ int rp_rays_download_aos(const rp_rays *r, void *records, uint64_t n) {
     CK(cudaSetDevice(ctx->device));
     if (!n) return RP_OK;
     void *stage = nullptr;
-    size_t bytes = (size_t)n * RP_RAY_BYTES;
-    int rc = with_staging(ctx, bytes, &stage);
+    size_t bytes = (size_t)n * RP_RAY_BYTES, got = 0;
+    int rc = with_staging(ctx, bytes, &stage, &got);
     if (rc) return rc;
     cudaError_t e = launch_soa_to_aos(r->soa, stage, n, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(records, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    ctx_free(ctx, stage, bytes);
+    ctx_free(ctx, stage, got);
     if (e != cudaSuccess) return cuda_fail(e, "rp_rays_download_aos");
     return RP_OK;
 }
@@ -490,9 +571,15 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float
     a.stats = (unsigned long long *)(sc + 32);
     a.tile_state = (unsigned long long *)(sc + SCRATCH_HDR);
     a.face_counts = s->face_counts;
+    if (ctx->gen_ev.empty()) {
+        ctx->gen_ev.resize(2);
+        for (auto &ev : ctx->gen_ev) CK(cudaEventCreate(&ev));
+    }
+    CK(cudaEventRecord(ctx->gen_ev[0], ctx->stream));
     cudaError_t e = (flags & RP_TRACE_MIXED) ? launch_generation_mixed(a, s->smem, ctx->stream)
                                              : launch_generation_plain(a, s->smem, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "generation kernel launch");
+    CK(cudaEventRecord(ctx->gen_ev[1], ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_pinned, sc + 8, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     return RP_OK;
 }
@@ -503,13 +590,22 @@ static int finish_gen(rp_ctx *ctx, rp_rays *out, int emit, rp_stats *st, uint64_
     unsigned err = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
     unsigned long long hits = ctx->h_pinned[3], term = ctx->h_pinned[4];
     if (st) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->gen_ev[0], ctx->gen_ev[1]);
         st->rays_in += n_in;
         st->hits += hits;
         st->terminated += term;
+        st->kernel_ms += ms;
+        st->launches += 1;
+        st->generations += 1;
     }
     if (err & ERR_TIMEOUT) {
         snprintf(g_last_error, sizeof g_last_error, "look-back wait gave up");
         return RP_ERR_TIMEOUT;
+    }
+    if (err & ERR_WAVELENGTH) {
+        snprintf(g_last_error, sizeof g_last_error, "a ray's wavelength_idx is outside the wavelength table");
+        return RP_ERR_INVALID;
     }
     if (err & (ERR_ZK_STACK | ERR_SHAPE_STACK)) {
         snprintf(g_last_error, sizeof g_last_error, "device evaluation limit hit (err=0x%x)", err);
@@ -615,6 +711,7 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_
     int rc = rp_rays_alloc(ctx, n, &gens[0]);
     if (rc) return rc;
     rc = rp_rays_upload_aos(gens[0], in_records, n);
+    if (rc == RP_OK && st && n) st->launches += 1;  // layout kernel of the upload
     if (rc == RP_OK) rc = rp_trace_rays(ctx, s, gens.data(), max_gens, recursion_limit, max_length, flags, e2, n_gens, st);
     if (rc == RP_OK) {
         uint64_t off = 0;
@@ -627,6 +724,7 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_
             }
             rc = rp_rays_download_aos(gens[g], (unsigned char *)out_records + off * RP_RAY_BYTES, c);
             if (rc) break;
+            if (st && c) st->launches += 1;  // layout kernel of the download
             off += c;
             gen_offsets[g + 1] = off;
         }

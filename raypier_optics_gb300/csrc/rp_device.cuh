@@ -30,12 +30,14 @@ enum : unsigned {
     ERR_ZK_STACK = 2u,
     ERR_SHAPE_STACK = 4u,
     ERR_OVERFLOW = 8u,
+    ERR_WAVELENGTH = 16u,
 };
 
 // ---- shapes: cshapes.pyx --------------------------------------------------
 __device__ __forceinline__ int poly_shape_inside(const double *xy, int n, double X, double Y) {
     // PolygonShape.point_inside_c, cshapes.pyx:147-168
     int ct = 0;
+    if (n < 1) return 0;
     double y1 = xy[2 * (n - 1) + 1], x1 = xy[2 * (n - 1)];
     for (int i = 0; i < n; i++) {
         double y2 = xy[2 * i + 1], x2 = xy[2 * i];
@@ -281,7 +283,7 @@ __device__ __forceinline__ double intersect_conic(v3 a, v3 d, double curvature, 
 __device__ __forceinline__ void asph_eval(const rp_face &f, v3 a, v3 d, double alpha, bool want_f, bool want_g,
                                           double *F, double *G) {
     double R = -f.p[0], beta = 1 + f.p[2];
-    int kmax = (int)f.p[11];
+    int kmax = min(max((int)f.p[11], 2), 8);
     double ux = a.x + alpha * d.x, uy = a.y + alpha * d.y;
     double r2 = (ux * ux) + (uy * uy);
     double pw[9];
@@ -384,6 +386,7 @@ __device__ __forceinline__ double extpoly_grad(const DevScene &S, const rp_face 
 __device__ __forceinline__ int point_in_polygon(const double *xy, int size, double X, double Y) {
     // point_in_polygon_c, cfaces.pyx:1050-1068
     int ct = 0;
+    if (size < 1) return 0;
     double y1 = xy[2 * (size - 1) + 1], x1 = xy[2 * (size - 1)];
     for (int i = 0; i < size; i++) {
         double y2 = xy[2 * i + 1], x2 = xy[2 * i];
@@ -785,7 +788,7 @@ __device__ __forceinline__ void convert_to_sp(const RayState &r, v3 normal, v3 &
 // children in emission order; returns their number.  `ntab` rows hold the
 // complex index of each dispersion curve per wavelength index.
 static __device__ int eval_children(const DevScene &S, const rp_material &m, const RayState &r, v3 point, v3 onormal,
-                             v3 otangent, ChildCommon &cc, Child *ch) {
+                             v3 otangent, ChildCommon &cc, Child *ch, unsigned *err) {
     const double INF = inf_d();
     switch (m.type) {
         case RP_MAT_NONE:
@@ -944,6 +947,10 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
                 n2 = out_to_in ? ni : no;
             } else {
                 long long w = (long long)r.wl;
+                if (w >= S.n_wl) {  // the reference indexes its n tables unchecked here
+                    atomicOr(err, ERR_WAVELENGTH);
+                    return 0;
+                }
                 n1 = S.ntab[(long long)(out_to_in ? m.curve_outside : m.curve_inside) * S.n_wl + w];
                 n2 = S.ntab[(long long)(out_to_in ? m.curve_inside : m.curve_outside) * S.n_wl + w];
             }

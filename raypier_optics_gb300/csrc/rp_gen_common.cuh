@@ -45,7 +45,7 @@ __device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char
         S.faces = reinterpret_cast<const rp_face *>(dst + nl);
         S.mats = reinterpret_cast<const rp_material *>(dst + nl + nf);
     }
-    unsigned *cnt = reinterpret_cast<unsigned *>(dst + nl + nf + nm);
+    unsigned *cnt = reinterpret_cast<unsigned *>(A.smem_tables ? dst + nl + nf + nm : dst);
     for (int k = threadIdx.x; k < S.n_faces; k += blockDim.x) cnt[k] = 0;
     *s_counts = cnt;
     return S;

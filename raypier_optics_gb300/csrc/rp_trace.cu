@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
             r.opl = A.in.opl[i];
             r.type = A.in.type[i];
             r.wl = A.in.wl[i];
-            nc = eval_children(S, S.mats[F.material], r, point, nrm, tng, cc, ch);
+            nc = eval_children(S, S.mats[F.material], r, point, nrm, tng, cc, ch, A.err);
             if (A.e2_term > 0.0 && nc > 0) {
                 int w = 0;
                 for (int k = 0; k < nc; k++) {

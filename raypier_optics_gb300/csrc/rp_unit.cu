@@ -112,7 +112,7 @@ static __device__ void write_child_record(unsigned char *dst, const unsigned cha
 
 __global__ void unit_material(DevScene S, int mat, const unsigned char *rays, const unsigned *idx,
                               const double *pts, const double *nrm, const double *tng, unsigned long long n,
-                              unsigned char *children, int *n_children) {
+                              unsigned char *children, int *n_children, unsigned *err) {
     unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const unsigned char *rec = rays + i * RP_RAY_BYTES;
@@ -122,7 +122,7 @@ __global__ void unit_material(DevScene S, int mat, const unsigned char *rays, co
     v3 point = mkv(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
     v3 on = mkv(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
     v3 ot = mkv(tng[3 * i], tng[3 * i + 1], tng[3 * i + 2]);
-    int nc = eval_children(S, S.mats[mat], r, point, on, ot, cc, ch);
+    int nc = eval_children(S, S.mats[mat], r, point, on, ot, cc, ch, err);
     for (int k = 0; k < nc; k++)
         write_child_record(children + (2 * i + k) * RP_RAY_BYTES, rec, cc, ch[k], idx[i]);
     n_children[i] = nc;
@@ -302,7 +302,7 @@ int rp_material_eval(rp_scene *s, int32_t mat, const void *rays, const uint32_t 
     auto *dnc = (int *)b.out(4 * n, st, e);
     auto *derr = (unsigned *)b.out(4, st, e);
     if (e == cudaSuccess) {
-        unit_material<<<grid_of(n), 128, 0, st>>>(S, mat, dr, di, dp, dn, dt, n, dc, dnc);
+        unit_material<<<grid_of(n), 128, 0, st>>>(S, mat, dr, di, dp, dn, dt, n, dc, dnc, derr);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(children, dc, (size_t)RP_RAY_BYTES * 2 * n, cudaMemcpyDeviceToHost, st);

@@ -318,17 +318,28 @@ def config3_spec(face_seed=4):
     return {"materials": mats, "lists": lists}
 
 
-def config3_rays(ray_dtype, n=16777216, seed=3):
-    rng = np.random.Generator(np.random.PCG64(seed))
-    g = rng.standard_normal((n, 2)) * 0.05
-    d = np.concatenate([g, np.ones((n, 1))], axis=1)
-    d /= np.linalg.norm(d, axis=1)[:, None]
-    xy = rng.uniform(-10.0, 10.0, (n, 2))
-    origin = np.concatenate([xy, np.full((n, 1), -60.0)], axis=1)
-    e1 = np.cross(np.array([0.0, 1.0, 0.0]), d)
-    e1 /= np.linalg.norm(e1, axis=1)[:, None]
+CONFIG3_BLOCK = 65536
+
+
+def config3_rays(ray_dtype, n=16777216, seed=3, first_block=0):
+    """Rays in blocks of 65,536 with one PCG64 stream per block, so a
+    subsample taken from the first blocks is the same rays as in the full set."""
+    n_blocks = (n + CONFIG3_BLOCK - 1) // CONFIG3_BLOCK
+    seqs = np.random.SeedSequence(seed).spawn(first_block + n_blocks)[first_block:]
     rays = np.zeros(n, dtype=ray_dtype)
-    fill_rays(rays, origin, d, e1)
+    for b, ss in enumerate(seqs):
+        lo, hi = b * CONFIG3_BLOCK, min(n, (b + 1) * CONFIG3_BLOCK)
+        m = hi - lo
+        rng = np.random.Generator(np.random.PCG64(ss))
+        g = rng.standard_normal((CONFIG3_BLOCK, 2))[:m] * 0.05
+        xy = rng.uniform(-10.0, 10.0, (CONFIG3_BLOCK, 2))[:m]
+        d = np.concatenate([g, np.ones((m, 1))], axis=1)
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        origin = np.concatenate([xy, np.full((m, 1), -60.0)], axis=1)
+        e1 = np.cross(np.array([0.0, 1.0, 0.0]), d)
+        e1 /= np.linalg.norm(e1, axis=1)[:, None]
+        fill_rays(rays[lo:hi], origin, d, e1)
+    rays['ray_ident'] = np.arange(n, dtype=np.uint32) + np.uint32(first_block * CONFIG3_BLOCK)
     return rays, np.array([0.8])
 
 

@@ -1,0 +1,378 @@
+"""Generate the golden vectors in tests/golden/ by running the reference
+raypier tracer (its Cython core built from source by oracle/build_ref.py).
+
+Run in a container that has the reference sources and Cython:
+
+    python oracle/build_ref.py && python tests/golden/make_golden.py
+
+Every fixture stores the scene description (the JSON spec understood by
+raypier_optics_gb300.workloads.build_scene), the inputs, and the reference's
+outputs.  The tests rebuild the same scene with this package's classes and
+compare the oracle and the GPU path against these outputs.
+"""
+from __future__ import annotations
+
+import contextlib
+import hashlib
+import io
+import json
+import math
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+import build_ref  # noqa: E402
+from raypier_optics_gb300 import workloads as W  # noqa: E402
+
+RNG_SEED = 20261203
+
+
+# ---- scene zoos -----------------------------------------------------------------------
+def _glass(name="glass", n_in=1.5, n_out=1.0, thr=-1.0):
+    return {"type": "FullDielectricMaterial", "kw": {"n_inside": n_in, "n_outside": n_out,
+                                                     "reflection_threshold": thr, "transmission_threshold": thr}}
+
+
+CIRC8 = {"type": "CircleShape", "kw": {"radius": 8.0, "centre": [1.0, -1.0]}}
+RECT = {"type": "RectangleShape", "kw": {"width": 10.0, "height": 6.0}}
+PENTAGON = {"type": "PolygonShape", "coordinates": [[9.0 * math.cos(a), 9.0 * math.sin(a)]
+                                                    for a in np.linspace(0, 2 * math.pi, 6)[:-1]]}
+
+
+def zernike15(rng, scale):
+    return [[W.ansi_j(*W.noll_to_nm(j)), float(rng.normal(0.0, scale))] for j in range(1, 16)]
+
+
+def face_zoo(rng):
+    """One spec per face type (plus shape and sign variants)."""
+    circ12 = {"type": "CircleShape", "kw": {"radius": 12.0}}
+    faces = {
+        "circular": {"type": "CircularFace", "kw": {"z_plane": 0.0}, "owner": {"diameter": 20.0, "offset": 1.0}},
+        "circular_inv": {"type": "CircularFace", "kw": {"z_plane": 2.0, "invert_normals": 1},
+                         "owner": {"diameter": 20.0, "offset": 0.0}},
+        "rectangular": {"type": "RectangularFace", "kw": {"z_plane": 0.0},
+                        "owner": {"length": 10.0, "width": 6.0, "offset": 1.0}},
+        "planar_circle": {"type": "ShapedPlanarFace", "kw": {"z_height": 1.0}, "shape": CIRC8},
+        "planar_rect_not_circle": {"type": "ShapedPlanarFace", "kw": {"z_height": 0.0},
+                                   "shape": {"type": "and", "a": RECT,
+                                             "b": {"type": "not", "a": {"type": "CircleShape",
+                                                                        "kw": {"radius": 2.0}}}}},
+        "planar_polygon_xor": {"type": "ShapedPlanarFace", "kw": {"z_height": 0.0},
+                               "shape": {"type": "xor", "a": PENTAGON, "b": {"type": "CircleShape",
+                                                                             "kw": {"radius": 3.0}}}},
+        "planar_or": {"type": "ShapedPlanarFace", "kw": {"z_height": 0.0},
+                      "shape": {"type": "or", "a": CIRC8, "b": RECT}},
+        "spherical_pos": {"type": "SphericalFace", "kw": {"curvature": 30.0, "z_height": 0.0},
+                          "owner": {"diameter": 20.0}},
+        "spherical_neg": {"type": "SphericalFace", "kw": {"curvature": -30.0, "z_height": 0.0, "invert_normal": 1},
+                          "owner": {"diameter": 20.0}},
+        "shaped_spherical": {"type": "ShapedSphericalFace", "kw": {"curvature": 40.0, "z_height": 0.0},
+                             "shape": RECT},
+        "conic_mirror": {"type": "ConicRevolutionFace", "kw": {"curvature": 40.0, "conic_const": -1.5},
+                         "shape": circ12, "material": "mirror"},
+        "conic_inv": {"type": "ConicRevolutionFace", "kw": {"curvature": -25.0, "conic_const": -0.5,
+                                                            "invert_normals": 1}, "shape": circ12},
+        "aspheric": {"type": "AsphericFace", "kw": {"curvature": -50.0, "conic_const": -0.6, "A4": 1e-5,
+                                                    "A6": -2e-8, "A8": 5e-11, "A10": 1e-14, "A12": -1e-17},
+                     "shape": circ12},
+        "aspheric_pos": {"type": "AsphericFace", "kw": {"curvature": 70.0, "conic_const": 0.3, "A4": -2e-6,
+                                                        "invert_normals": 1}, "shape": circ12},
+        "extpoly": {"type": "ExtendedPolynomialFace", "kw": {"norm_radius": 10.0},
+                    "attrs": {"curvature": 60.0, "conic_const": -0.2, "z_height": 0.5,
+                              "coefs": rng.normal(0.0, 1e-3, (3, 3)).tolist()}, "shape": circ12},
+        "extpoly_inv": {"type": "ExtendedPolynomialFace", "kw": {"norm_radius": 12.0, "invert_normals": 1},
+                        "attrs": {"curvature": -80.0, "conic_const": 0.0, "z_height": 0.0,
+                                  "coefs": rng.normal(0.0, 1e-4, (5, 5)).tolist()}, "shape": circ12},
+        "zernike_plane": {"type": "DistortionFace", "kw": {"accuracy": 1e-6},
+                          "base_face": {"type": "ShapedPlanarFace", "kw": {"z_height": 0.0}, "shape": circ12},
+                          "distortion": {"type": "ZernikeDistortion", "coefs": zernike15(rng, 2e-3),
+                                         "kw": {"unit_radius": 10.0}}, "shape": circ12},
+        "j7_sphere": {"type": "DistortionFace", "kw": {"accuracy": 1e-7},
+                      "base_face": {"type": "ShapedSphericalFace", "kw": {"curvature": 80.0}, "shape": circ12},
+                      "distortion": {"type": "SimpleTestZernikeJ7", "kw": {"unit_radius": 10.0,
+                                                                           "amplitude": 1e-3}},
+                      "shape": circ12},
+        "oriented_polygon": {"type": "OrientedPolygonFace",
+                             "kw": {"origin": [0.5, 0.0, 0.0], "normal": [0.1, 0.0, -1.0],
+                                    "x_axis": [1.0, 0.0, 0.1],
+                                    "xy_points": [[-8.0, -6.0], [9.0, -5.0], [0.0, 9.0]]}},
+        "polygon": {"type": "PolygonFace", "kw": {"z_plane": 0.0, "xy_points": PENTAGON["coordinates"]}},
+        "elliptical": {"type": "ElipticalPlaneFace", "kw": {"g_x": 0.1, "g_y": -0.05},
+                       "owner": {"diameter": 20.0}},
+    }
+    return faces
+
+
+def face_scene(face):
+    face = dict(face)
+    face.setdefault("material", "glass")
+    rot = W._random_rotation(np.random.Generator(np.random.PCG64(7)))
+    small = np.eye(3) + 0.05 * (rot - np.eye(3))
+    q, r = np.linalg.qr(small)
+    q = q * np.sign(np.diag(r))[None, :]
+    return {"materials": {"glass": _glass(), "mirror": {"type": "PECMaterial"},
+                          "detector": {"type": "OpaqueMaterial"}},
+            "lists": [{"rotation": q.tolist(), "translation": [0.3, -0.2, 20.0], "faces": [face]},
+                      {"translation": [0, 0, 60.0], "faces": [
+                          {"type": "CircularFace", "kw": {"z_plane": 0.0},
+                           "owner": {"diameter": 400.0, "offset": 0.0}, "material": "detector"}]}]}
+
+
+def material_zoo():
+    crown1 = {"formula_id": 1, "coefs": [0.0, 1.03961212, 0.0774596669, 0.231792344, 0.141484679, 1.01046945,
+                                         10.1779013], "absorption": 2.0}
+    poly3 = {"formula_id": 3, "coefs": [2.2, 0.011, 2.0, -0.01, -2.0, 1e-4, -4.0], "wavelength_min": 0.3}
+    const0 = {"formula_id": 0, "coefs": [1.33], "absorption": 0.5}
+    return {"curves": {"crown": W.CROWN, "flint": W.FLINT, "air": W.AIR, "crown1": crown1, "poly3": poly3,
+                       "water": const0},
+            "materials": {
+                "opaque": {"type": "OpaqueMaterial"},
+                "transparent": {"type": "TransparentMaterial"},
+                "pec": {"type": "PECMaterial"},
+                "partial": {"type": "PartiallyReflectiveMaterial", "kw": {"reflectivity": 0.3}},
+                "linpol": {"type": "LinearPolarisingMaterial"},
+                "waveplate": {"type": "WaveplateMaterial", "kw": {"retardance": 0.25, "fast_axis": [1.0, 1.0, 0.0]}},
+                "dielectric": {"type": "DielectricMaterial", "kw": {"n_inside": [1.5, 0.01], "n_outside": 1.0}},
+                "full_default": {"type": "FullDielectricMaterial", "kw": {"n_inside": 1.7, "n_outside": 1.0}},
+                "full_split": {"type": "FullDielectricMaterial",
+                               "kw": {"n_inside": [1.6, 0.02], "n_outside": 1.1,
+                                      "reflection_threshold": -1.0, "transmission_threshold": -1.0}},
+                "disp_sellmeier1": {"type": "FullDielectricDispersiveMaterial",
+                                    "kw": {"dispersion_inside": "crown1", "dispersion_outside": "air",
+                                           "reflection_threshold": -1.0, "transmission_threshold": -1.0}},
+                "disp_sellmeier2": {"type": "FullDielectricDispersiveMaterial",
+                                    "kw": {"dispersion_inside": "flint", "dispersion_outside": "crown"}},
+                "disp_poly3": {"type": "FullDielectricDispersiveMaterial",
+                               "kw": {"dispersion_inside": "poly3", "dispersion_outside": "water",
+                                      "reflection_threshold": -1.0, "transmission_threshold": -1.0}},
+                "aperture_circ": {"type": "CircularApertureMaterial",
+                                  "kw": {"outer_radius": 15.0, "radius": 6.0, "edge_width": 1.5,
+                                         "origin": [0.0, 0.0, 20.0]}},
+                "aperture_circ_inv": {"type": "CircularApertureMaterial",
+                                      "kw": {"outer_radius": 14.0, "radius": 4.0, "edge_width": 1.0,
+                                             "origin": [0.5, 0.0, 20.0], "invert": 1}},
+                "aperture_rect": {"type": "RectangularApertureMaterial",
+                                  "kw": {"outer_width": 20.0, "outer_height": 16.0, "width": 8.0, "height": 5.0,
+                                         "edge_width": 1.0, "origin": [0.0, 0.0, 20.0]}},
+            }}
+
+
+def material_scene(mat_name):
+    zoo = material_zoo()
+    spec = {"curves": zoo["curves"], "materials": {mat_name: zoo["materials"][mat_name],
+                                                   "detector": {"type": "OpaqueMaterial"}},
+            "lists": [{"translation": [0, 0, 20.0], "faces": [
+                {"type": "CircularFace", "kw": {"z_plane": 0.0}, "owner": {"diameter": 40.0, "offset": 0.0},
+                 "material": mat_name}]},
+                      {"translation": [0, 0, 0.0], "faces": [
+                          {"type": "CircularFace", "kw": {"z_plane": -30.0},
+                           "owner": {"diameter": 400.0, "offset": 0.0}, "material": "detector"},
+                          {"type": "CircularFace", "kw": {"z_plane": 70.0, "invert_normals": 1},
+                           "owner": {"diameter": 400.0, "offset": 0.0}, "material": "detector"}]}]}
+    return spec
+
+
+def random_rays(ray_dtype, rng, n, z0, zdir, tilt, spread, per_ray_wl=False, wl_range=(0.45, 0.9)):
+    th = rng.uniform(0.0, tilt, n)
+    ph = rng.uniform(0.0, 2 * math.pi, n)
+    d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), zdir * np.cos(th)], axis=1)
+    o = np.stack([rng.uniform(-spread, spread, n), rng.uniform(-spread, spread, n), np.full(n, z0)], axis=1)
+    e1 = np.cross(np.array([0.0, 1.0, 0.0]), d)
+    e1 /= np.linalg.norm(e1, axis=1)[:, None]
+    rays = np.zeros(n, dtype=ray_dtype)
+    W.fill_rays(rays, o, d, e1)
+    rays['E1_amp'] = rng.normal(0, 1, n) + 1j * rng.normal(0, 1, n)
+    rays['E2_amp'] = rng.normal(0, 1, n) + 1j * rng.normal(0, 1, n)
+    rays['phase'] = rng.uniform(0, 1, n)
+    rays['accumulated_path'] = rng.uniform(0, 5, n)
+    rays['ray_type_id'] = rng.integers(0, 4, n)
+    if per_ray_wl:
+        rays['wavelength_idx'] = np.arange(n, dtype=np.uint32)
+        return rays, rng.uniform(wl_range[0], wl_range[1], n)
+    return rays, np.array([0.55])
+
+
+# ---- running the reference --------------------------------------------------------------
+def run_reference(ref, spec, rays, wl, recursion_limit, max_length):
+    lists = W.build_scene(spec, ref)
+    rc = ref.ctracer.RayCollection.from_array(rays.copy())
+    rc.wavelengths = np.asarray(wl, dtype=np.double)
+    with contextlib.redirect_stdout(io.StringIO()):
+        traced, all_faces = ref.tracer.trace_rays(rc, lists, recursion_limit=recursion_limit, max_length=max_length)
+    gens = [t.copy_as_array() for t in traced]
+    counts = np.array([f.count for f in all_faces], dtype=np.uint32)
+    return gens, counts
+
+
+def save_trace_case(path, spec, rays, wl, params, gens, counts):
+    offs = np.cumsum([0] + [len(g) for g in gens]).astype(np.uint64)
+    out = np.concatenate(gens) if gens else np.zeros(0, dtype=rays.dtype)
+    np.savez_compressed(path, spec=np.array(json.dumps(spec)), params=np.array(json.dumps(params)),
+                        rays=rays, wl=np.asarray(wl, dtype=np.double), out=out, offsets=offs, counts=counts)
+
+
+def index_digest(gens):
+    h = hashlib.sha256()
+    for g in gens:
+        for f in ("wavelength_idx", "parent_idx", "end_face_idx", "ray_ident", "ray_type_id"):
+            h.update(np.ascontiguousarray(g[f]).tobytes())
+    return h.hexdigest()
+
+
+def full_digest(g):
+    return hashlib.sha256(np.ascontiguousarray(g).tobytes()).hexdigest()
+
+
+def main():
+    ref = build_ref.load()
+    rdt = ref.ctracer.ray_dtype
+    rng = np.random.Generator(np.random.PCG64(RNG_SEED))
+    out_dir = HERE
+
+    # configuration 1: full-size digests and a 64-ray subset in full
+    spec1 = W.config1_spec()
+    rays1, wl1 = W.config1_rays(rdt)
+    P1 = dict(W.CONFIG1)
+    gens, counts = run_reference(ref, spec1, rays1, wl1, P1["recursion_limit"], P1["max_length"])
+    with open(os.path.join(out_dir, "config1_full.json"), "w") as f:
+        json.dump({"n_rays": int(len(rays1)), "gen_sizes": [len(g) for g in gens],
+                   "segments": int(sum(len(g) for g in gens)), "face_counts": counts.tolist(),
+                   "index_sha256": index_digest(gens), "gen_sha256": [full_digest(g) for g in gens],
+                   "params": P1}, f, indent=1)
+    sub = rays1[::64].copy()
+    sub['ray_ident'] = np.arange(len(sub), dtype=np.uint32) * 64
+    gens, counts = run_reference(ref, spec1, sub, wl1, P1["recursion_limit"], P1["max_length"])
+    save_trace_case(os.path.join(out_dir, "config1_sub64.npz"), spec1, sub, wl1, P1, gens, counts)
+
+    # configuration 2: 24 rays spread over the 1,048,576-ray set
+    rays2, wl2 = W.config2_rays(rdt)
+    idx = np.linspace(0, len(rays2) - 1, 24).astype(np.int64)
+    sub, swl = W.subsample(rays2, wl2, idx, per_ray_wavelength=True)
+    P2 = dict(W.CONFIG2)
+    gens, counts = run_reference(ref, W.config2_spec(), sub, swl, P2["recursion_limit"], P2["max_length"])
+    save_trace_case(os.path.join(out_dir, "config2_sub24.npz"), W.config2_spec(), sub, swl, P2, gens, counts)
+
+    # configuration 3: the first 48 rays of the 16,777,216-ray set
+    rays3, wl3 = W.config3_rays(rdt, 48)
+    P3 = dict(W.CONFIG3)
+    gens, counts = run_reference(ref, W.config3_spec(), rays3, wl3, P3["recursion_limit"], P3["max_length"])
+    save_trace_case(os.path.join(out_dir, "config3_sub48.npz"), W.config3_spec(), rays3, wl3, P3, gens, counts)
+
+    # face zoo: each face type in its own scene, rays from both sides
+    zoo = face_zoo(rng)
+    units = {}
+    for name, face in zoo.items():
+        spec = face_scene(face)
+        r1, wl = random_rays(rdt, rng, 40, -10.0, +1.0, 0.35, 13.0)
+        r2, _ = random_rays(rdt, rng, 24, 45.0, -1.0, 0.35, 13.0)
+        rays = np.concatenate([r1, r2])
+        rays['ray_ident'] = np.arange(len(rays), dtype=np.uint32)
+        params = {"recursion_limit": 4, "max_length": 200.0, "e2_terminate": 0.0}
+        gens, counts = run_reference(ref, spec, rays, wl, params["recursion_limit"], params["max_length"])
+        save_trace_case(os.path.join(out_dir, f"face_{name}.npz"), spec, rays, wl, params, gens, counts)
+        # unit calls on the same face: intersect (base and non-base rays) and normals
+        lists = W.build_scene(spec, ref)
+        f = lists[0].faces[0]
+        f.update()
+        p1 = np.stack([rng.uniform(-14, 14, 64), rng.uniform(-14, 14, 64), rng.uniform(-30, -2, 64)], axis=1)
+        p2 = np.stack([rng.uniform(-14, 14, 64), rng.uniform(-14, 14, 64), rng.uniform(2, 60, 64)], axis=1)
+        p2[:8] = p1[:8] + np.array([0, 0, 80.0])
+        d_base = np.array([f.intersect(tuple(a), tuple(b), 1) for a, b in zip(p1, p2)])
+        d_free = np.array([f.intersect(tuple(a), tuple(b), 0) for a, b in zip(p1, p2)])
+        pts = np.stack([rng.uniform(-9, 9, 32), rng.uniform(-9, 9, 32), rng.uniform(-1, 1, 32)], axis=1)
+        nrm = np.array([f.compute_normal(tuple(p)) for p in pts])
+        units[f"face_{name}_p1"] = p1
+        units[f"face_{name}_p2"] = p2
+        units[f"face_{name}_dist_base"] = d_base
+        units[f"face_{name}_dist_free"] = d_free
+        units[f"face_{name}_pts"] = pts
+        units[f"face_{name}_normal"] = nrm
+        shape = getattr(f, "shape", None)
+        if shape is not None:
+            xy = rng.uniform(-11, 11, (200, 2))
+            units[f"face_{name}_xy"] = xy
+            units[f"face_{name}_inside"] = np.array([bool(shape.point_inside(x, y)) for x, y in xy])
+        if hasattr(f, "distortion") and f.distortion is not None:
+            x = np.concatenate([[0.0, 1e-9], rng.uniform(-12, 12, 98)])
+            y = np.concatenate([[0.0, 0.0], rng.uniform(-12, 12, 98)])
+            units[f"face_{name}_dist_x"] = x
+            units[f"face_{name}_dist_y"] = y
+            units[f"face_{name}_dist_zg"] = np.asarray(f.distortion.z_offset_and_gradient(x, y))
+            units[f"face_{name}_dist_z"] = np.asarray(f.distortion.z_offset(x, y))
+
+    # material zoo: each material on a plane, rays from both sides at up to 70 degrees
+    mz = material_zoo()
+    for name in mz["materials"]:
+        spec = material_scene(name)
+        per_ray = name.startswith("disp_")
+        r1, wla = random_rays(rdt, rng, 40, 0.0, +1.0, 1.2, 12.0, per_ray_wl=per_ray)
+        r2, wlb = random_rays(rdt, rng, 24, 40.0, -1.0, 1.2, 12.0, per_ray_wl=per_ray)
+        rays = np.concatenate([r1, r2])
+        rays['ray_ident'] = np.arange(len(rays), dtype=np.uint32)
+        if per_ray:
+            rays['wavelength_idx'] = np.arange(len(rays), dtype=np.uint32)
+            wl = np.concatenate([wla, wlb])
+        else:
+            wl = wla
+        params = {"recursion_limit": 3, "max_length": 300.0, "e2_terminate": 0.0}
+        gens, counts = run_reference(ref, spec, rays, wl, params["recursion_limit"], params["max_length"])
+        save_trace_case(os.path.join(out_dir, f"mat_{name}.npz"), spec, rays, wl, params, gens, counts)
+        # eval_child_ray unit calls with random orientations
+        lists = W.build_scene(spec, ref)
+        mat = lists[0].faces[0].material
+        mat.wavelengths = np.asarray(wl, dtype=np.double)
+        rc = ref.ctracer.RayCollection.from_array(rays.copy())
+        nrm = rng.normal(0, 1, (len(rays), 3))
+        nrm[:4] = rays['direction'][:4]          # normal incidence cases
+        tng = rng.normal(0, 1, (len(rays), 3))
+        pts = rng.uniform(-10, 10, (len(rays), 3))
+        pts[:, 2] += 20.0
+        kids, nk = [], []
+        for i in range(len(rays)):
+            out = ref.ctracer.RayCollection(2)
+            mat.eval_child_ray(rc[i], i, tuple(pts[i]), tuple(nrm[i]), tuple(tng[i]), out)
+            a = out.copy_as_array()
+            nk.append(len(a))
+            kids.append(a)
+        units[f"mat_{name}_normals"] = nrm
+        units[f"mat_{name}_tangents"] = tng
+        units[f"mat_{name}_points"] = pts
+        units[f"mat_{name}_nkids"] = np.array(nk)
+        units[f"mat_{name}_kids"] = np.concatenate(kids) if kids else np.zeros(0, rdt)
+
+    # Convert_to_SP
+    rays, _ = random_rays(rdt, rng, 64, 0.0, 1.0, 1.0, 5.0)
+    nrm = rng.normal(0, 1, (64, 3))
+    nrm[:4] = rays['direction'][:4]
+    rc = ref.ctracer.RayCollection.from_array(rays.copy())
+    sp = [ref.cmaterials.Convert_to_SP(rc[i], tuple(nrm[i])) for i in range(64)]
+    units["sp_rays"] = rays
+    units["sp_normals"] = nrm
+    tmp = ref.ctracer.RayCollection(64)
+    for r in sp:
+        tmp.add_ray(r)
+    units["sp_out"] = tmp.copy_as_array()
+
+    # dispersion curves
+    wl = np.linspace(0.35, 1.6, 60)
+    for name, c in material_zoo()["curves"].items():
+        curve = W._make_curve(c, ref)
+        units[f"curve_{name}_n"] = np.asarray(curve.evaluate_n(wl))
+    units["curve_wl"] = wl
+    units["curve_specs"] = np.array(json.dumps(material_zoo()["curves"]))
+
+    np.savez_compressed(os.path.join(out_dir, "units.npz"), **units)
+    np.savez_compressed(os.path.join(out_dir, "face_zoo_specs.npz"),
+                        specs=np.array(json.dumps({k: face_scene(v) for k, v in zoo.items()})))
+    print("golden vectors written to", out_dir)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,79 @@
+"""Shared test utilities: golden-case loading, scene construction with this
+package's classes, and record comparison at the parity tolerances
+(indices bit-exact; floating point within 1e-9 relative)."""
+from __future__ import annotations
+
+import glob
+import json
+import os
+import platform
+import types
+
+import numpy as np
+
+from raypier_optics_gb300 import cdistortions, cfaces, cmaterials, cshapes, ctracer, scene
+from raypier_optics_gb300 import workloads as W
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+NS = types.SimpleNamespace(ctracer=ctracer, cfaces=cfaces, cmaterials=cmaterials, cshapes=cshapes,
+                           cdistortions=cdistortions)
+INDEX_FIELDS = ("wavelength_idx", "parent_idx", "end_face_idx", "ray_ident", "ray_type_id")
+FLOAT_FIELDS = ("origin", "direction", "normal", "E_vector", "refractive_index", "E1_amp", "E2_amp",
+                "length", "phase", "accumulated_path")
+# parity tolerance for floating-point fields (positions, directions, fields, OPL)
+RTOL = 1e-9
+ATOL = 1e-12
+X86 = platform.machine() in ("x86_64", "AMD64")
+
+
+def trace_case_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(p).startswith(("units", "face_zoo")))
+
+
+def load_case(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    spec = json.loads(str(z["spec"]))
+    params = json.loads(str(z["params"]))
+    offs = z["offsets"].astype(np.int64)
+    out = z["out"]
+    gens = [out[offs[g]:offs[g + 1]] for g in range(len(offs) - 1)]
+    return dict(spec=spec, params=params, rays=z["rays"].astype(ctracer.ray_dtype), wl=z["wl"], gens=gens,
+                counts=z["counts"])
+
+
+def build(spec):
+    """Face lists for `spec` with face.idx assigned and params pulled, as
+    trace_rays does (core/tracer.py:28-34)."""
+    lists = W.build_scene(spec, NS)
+    all_faces = [f for fl in lists for f in fl.faces]
+    for i, f in enumerate(all_faces):
+        f.idx = i
+        f.update()
+    return lists, all_faces
+
+
+def tables_for(spec):
+    lists, all_faces = build(spec)
+    return scene.compile_scene(lists), lists, all_faces
+
+
+def assert_records(got, exp, exact=False, what=""):
+    assert len(got) == len(exp), f"{what}: {len(got)} rays vs {len(exp)}"
+    for f in INDEX_FIELDS:
+        np.testing.assert_array_equal(got[f], exp[f], err_msg=f"{what}: field {f}")
+    for f in FLOAT_FIELDS:
+        a, b = got[f], exp[f]
+        if exact:
+            a8 = np.ascontiguousarray(a).view(np.uint8)
+            b8 = np.ascontiguousarray(b).view(np.uint8)
+            assert np.array_equal(a8, b8), f"{what}: field {f} differs"
+        else:
+            np.testing.assert_allclose(a, b, rtol=RTOL, atol=ATOL, equal_nan=True, err_msg=f"{what}: field {f}")
+
+
+def assert_generations(got_gens, exp_gens, exact=False, what=""):
+    assert [len(g) for g in got_gens] == [len(g) for g in exp_gens], \
+        f"{what}: generation sizes {[len(g) for g in got_gens]} vs {[len(g) for g in exp_gens]}"
+    for g, (a, b) in enumerate(zip(got_gens, exp_gens)):
+        assert_records(a, b, exact=exact, what=f"{what} gen {g}")

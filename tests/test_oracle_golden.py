@@ -1,0 +1,71 @@
+"""The C oracle (oracle/rp_oracle.c) against the reference's golden vectors.
+
+These run on the CPU only.  On x86-64 the oracle, built with the reference's
+own flags, must reproduce the reference byte for byte; elsewhere (another
+libm) indices must still match exactly and floats within the parity
+tolerance."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import GOLDEN, X86, assert_generations, load_case, tables_for, trace_case_names
+from raypier_optics_gb300 import ctracer, workloads as W
+
+
+@pytest.mark.parametrize("name", trace_case_names())
+def test_oracle_trace_matches_reference(name):
+    c = load_case(name)
+    tables, lists, all_faces = tables_for(c["spec"])
+    p = c["params"]
+    gens, counts = oracle.trace_rays(tables, c["wl"], c["rays"], p["recursion_limit"], p["max_length"], 0.0)
+    assert_generations(gens, c["gens"], exact=X86, what=name)
+    np.testing.assert_array_equal(counts[:tables.n_faces], c["counts"])
+
+
+def _index_digest(gens):
+    h = hashlib.sha256()
+    for g in gens:
+        for f in ("wavelength_idx", "parent_idx", "end_face_idx", "ray_ident", "ray_type_id"):
+            h.update(np.ascontiguousarray(g[f]).tobytes())
+    return h.hexdigest()
+
+
+def test_oracle_config1_full_size_digest():
+    ref = json.load(open(os.path.join(GOLDEN, "config1_full.json")))
+    rays, wl = W.config1_rays(ctracer.ray_dtype)
+    tables, _, _ = tables_for(W.config1_spec())
+    p = ref["params"]
+    gens, counts = oracle.trace_rays(tables, wl, rays, p["recursion_limit"], p["max_length"], 0.0)
+    assert [len(g) for g in gens] == ref["gen_sizes"] == [4096, 8192, 8192, 16384, 24576, 40960]
+    assert sum(len(g) for g in gens) == ref["segments"] == 102400
+    assert counts[:tables.n_faces].tolist() == ref["face_counts"]
+    assert _index_digest(gens) == ref["index_sha256"]
+    if X86:
+        assert [hashlib.sha256(np.ascontiguousarray(g).tobytes()).hexdigest() for g in gens] == ref["gen_sha256"]
+
+
+def test_oracle_termination_rule_is_inactive_on_config1():
+    rays, wl = W.config1_rays(ctracer.ray_dtype, 512)
+    tables, _, _ = tables_for(W.config1_spec())
+    a, _ = oracle.trace_rays(tables, wl, rays, 6, 1000.0, 0.0)
+    b, _ = oracle.trace_rays(tables, wl, rays, 6, 1000.0, 1e-6)
+    assert [len(g) for g in a] == [len(g) for g in b]
+
+
+def test_oracle_termination_drops_weak_children_stably():
+    c = load_case("config2_sub24")
+    tables, _, _ = tables_for(c["spec"])
+    p = c["params"]
+    full, _ = oracle.trace_rays(tables, c["wl"], c["rays"], 4, p["max_length"], 0.0)
+    term, _ = oracle.trace_rays(tables, c["wl"], c["rays"], 4, p["max_length"], 0.1)
+    # generation 1 is the children of generation 0: the kept ones are the strong
+    # ones, in the same order
+    e2 = lambda g: (np.abs(g["E1_amp"]) ** 2 + np.abs(g["E2_amp"]) ** 2)
+    keep = full[1][~(e2(full[1]) < 0.1)]
+    np.testing.assert_array_equal(term[1]["parent_idx"], keep["parent_idx"])
+    np.testing.assert_array_equal(term[1]["ray_type_id"], keep["ray_type_id"])
+    assert len(term[1]) < len(full[1])
