@@ -257,6 +257,12 @@ int rp_scene_destroy(rp_scene *scene);
  * ctracer.pyx:2108). counts has n_faces entries. */
 int rp_scene_face_counts(rp_scene *scene, uint32_t *counts, int32_t n_faces, int reset);
 
+/* Host-only: the world-space boxes the nearest-hit search uses to skip faces a
+ * ray cannot reach before its current nearest hit (no counterpart in the
+ * reference, which tests every face).  out[8*f .. 8*f+5] = lo xyz, hi xyz,
+ * out[8*f+6] = 1 if face f may be skipped, 0 if it is always tested. */
+int rp_scene_bounds(const rp_scene_desc *desc, float *out, int32_t n_faces);
+
 /* ---- device ray buffers (structure-of-arrays) ---------------------------- */
 int rp_rays_alloc(rp_ctx *ctx, uint64_t capacity, rp_rays **out);
 int rp_rays_free(rp_rays *rays);

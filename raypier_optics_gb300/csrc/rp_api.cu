@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/rp_gb300.h"
+#include "rp_bounds.h"
 #include "rp_kernels.cuh"
 
 using namespace rp;
@@ -317,7 +318,8 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     size_t o_wl = o_aux + align256(sizeof(double) * d->n_aux);
     size_t o_ntab = o_wl + align256(sizeof(double) * (size_t)n_wl);
     size_t o_cnt = o_ntab + align256(sizeof(double2) * (size_t)n_wl * d->n_dispersions);
-    size_t total = o_cnt + align256(sizeof(unsigned) * (d->n_face_records + 1));
+    size_t o_bnd = o_cnt + align256(sizeof(unsigned) * (d->n_face_records + 1));
+    size_t total = o_bnd + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
     int rc = ctx_alloc(ctx, &s->dev_block, total, &s->dev_bytes);
     if (rc) {
         delete s;
@@ -336,6 +338,14 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     UP(o_disp, d->dispersions, sizeof(rp_dispersion) * d->n_dispersions);
     UP(o_aux, d->aux, sizeof(double) * d->n_aux);
     UP(o_wl, wavelengths, sizeof(double) * (size_t)n_wl);
+    std::vector<float> bounds((size_t)d->n_faces * 8 + 8, 0.0f);
+    for (int l = 0; l < d->n_lists; l++)
+        for (int k = 0; k < d->lists[l].n_faces; k++) {
+            int f = d->lists[l].first_face + k;
+            face_world_box(d, d->lists[l], d->faces[f], &bounds[(size_t)f * 8]);
+        }
+    UP(o_bnd, bounds.data(), sizeof(float) * 8 * (size_t)d->n_faces);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // `bounds` is pageable and about to go out of scope
 #undef UP
     if (e == cudaSuccess) e = cudaMemsetAsync(b + o_cnt, 0, sizeof(unsigned) * (d->n_face_records + 1), st);
     DevScene &S = s->S;
@@ -346,6 +356,8 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     S.dists = (const rp_distortion *)(b + o_dists);
     S.aux = (const double *)(b + o_aux);
     S.ntab = (const double2 *)(b + o_ntab);
+    S.bounds = (const float *)(b + o_bnd);
+    S.face_list = nullptr;
     S.n_wl = n_wl;
     S.n_lists = d->n_lists;
     S.n_faces = d->n_faces;
@@ -369,9 +381,27 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     s->smem_tables = 1;
     if (s->smem > 160 * 1024) {  // tables too large to stage: read them from global memory
         s->smem_tables = 0;
-        s->smem = sizeof(unsigned) * (size_t)d->n_faces;
+        s->smem = generation_smem_bytes(0, 0, 0, d->n_faces);
+    }
+    if (s->smem > 200 * 1024) {
+        ctx_free(ctx, s->dev_block, s->dev_bytes);
+        delete s;
+        snprintf(g_last_error, sizeof g_last_error, "scene has too many faces (%d)", d->n_faces);
+        return RP_ERR_UNSUPPORTED;
     }
     *out = s;
+    return RP_OK;
+}
+
+int rp_scene_bounds(const rp_scene_desc *d, float *out, int32_t n_faces) {
+    if (!d || !out || n_faces != d->n_faces) return RP_ERR_INVALID;
+    int v = validate_scene(d);
+    if (v != RP_OK) return v;
+    for (int l = 0; l < d->n_lists; l++)
+        for (int k = 0; k < d->lists[l].n_faces; k++) {
+            int f = d->lists[l].first_face + k;
+            face_world_box(d, d->lists[l], d->faces[f], out + (size_t)f * 8);
+        }
     return RP_OK;
 }
 
@@ -696,7 +726,7 @@ int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, in
     }
     // traced generations: those with rays that were traced
     *n_gens = count;
-    if (rc == RP_OK && count < max_gens && gens[count] && gens[count]->n == 0) {
+    if (rc == RP_OK && count > 0 && count < max_gens && gens[count] && gens[count]->n == 0) {
         rp_rays_free(gens[count]);
         gens[count] = nullptr;
     }

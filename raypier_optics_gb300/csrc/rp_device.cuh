@@ -20,6 +20,8 @@ struct DevScene {
     const rp_distortion *dists;
     const double *aux;
     const double2 *ntab;  // [n_dispersions][n_wl] complex index per curve and wavelength
+    const float *bounds;  // [n_faces][8]: world box lo[3], hi[3], skippable flag (rp_bounds.h)
+    const short *face_list;  // [n_faces]: owning face list of each traced face
     long long n_wl;
     int n_lists, n_faces, n_recs, n_mats, n_shapes, n_dists;
 };

@@ -45,8 +45,19 @@ __device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char
         S.faces = reinterpret_cast<const rp_face *>(dst + nl);
         S.mats = reinterpret_cast<const rp_material *>(dst + nl + nf);
     }
-    unsigned *cnt = reinterpret_cast<unsigned *>(A.smem_tables ? dst + nl + nf + nm : dst);
+    double *tail = A.smem_tables ? dst + nl + nf + nm : dst;
+    // per-face world boxes (8 floats each), then the face -> list map, then hit counters
+    float *bnd = reinterpret_cast<float *>(tail);
+    for (int k = threadIdx.x; k < S.n_faces * 8; k += blockDim.x) bnd[k] = A.S.bounds[k];
+    short *fl = reinterpret_cast<short *>(bnd + S.n_faces * 8);
+    for (int l = 0; l < S.n_lists; l++) {
+        int f0 = S.lists[l].first_face, n = S.lists[l].n_faces;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) fl[f0 + k] = (short)l;
+    }
+    unsigned *cnt = reinterpret_cast<unsigned *>(tail + (S.n_faces * 8 * 4 + S.n_faces * 2 + 7) / 8);
     for (int k = threadIdx.x; k < S.n_faces; k += blockDim.x) cnt[k] = 0;
+    S.bounds = bnd;
+    S.face_list = fl;
     *s_counts = cnt;
     return S;
 }

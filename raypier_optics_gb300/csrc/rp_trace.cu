@@ -16,6 +16,102 @@
 
 namespace rp {
 
+// Entry distance of the ray (FP32, unit direction) into face f's world box;
+// 0 for faces that are always tested, +inf for a miss.
+__device__ __forceinline__ float box_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
+                                           float iz) {
+    if (b[6] == 0.0f) return 0.0f;
+    float t1 = (b[0] - ox) * ix, t2 = (b[3] - ox) * ix;
+    float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
+    t1 = (b[1] - oy) * iy;
+    t2 = (b[4] - oy) * iy;
+    tmin = fmaxf(tmin, fminf(t1, t2));
+    tmax = fminf(tmax, fmaxf(t1, t2));
+    t1 = (b[2] - oz) * iz;
+    t2 = (b[5] - oz) * iz;
+    tmin = fmaxf(tmin, fminf(t1, t2));
+    tmax = fminf(tmax, fmaxf(t1, t2));
+    if (!(tmax >= tmin) || tmax < 0.0f) return __int_as_float(0x7f800000);
+    return fmaxf(tmin, 0.0f);
+}
+
+__device__ __forceinline__ float inv_dir(float v) {
+    if (fabsf(v) < 1e-30f) v = copysignf(1e-30f, v);
+    return 1.0f / v;
+}
+
+// Nearest hit over all faces (trace_segment_c's loops over face lists and
+// faces, ctracer.pyx:2092-2105, with FaceList.intersect_c 1882-1904).  The
+// reference tests every face in list order and keeps a strictly nearer
+// distance, so the result is the smallest distance in (tolerance, max_length)
+// and, among equal distances, the earliest face.  Here faces are tested in
+// order of their box entry distance and a face whose box the ray cannot reach
+// before the current nearest hit is skipped; the exact FP64 test of every
+// face that is tested is the reference's, and ties go to the lower record,
+// so the outcome is the same.
+__device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pend, double max_len, double &len,
+                                            int &best, int &best_list, unsigned *err) {
+    float ox = (float)o.x, oy = (float)o.y, oz = (float)o.z;
+    float dx = (float)d.x, dy = (float)d.y, dz = (float)d.z;
+    float il = 1.0f / sqrtf(dx * dx + dy * dy + dz * dz);
+    float ix = inv_dir(dx * il), iy = inv_dir(dy * il), iz = inv_dir(dz * il);
+    // distances along the ray are Euclidean in the reference (h * |p2 - p1|)
+    const int nf = S.n_faces;
+    const int nmask = nf < 64 ? nf : 64;
+    const float lim0 = (float)max_len * 1.000001f + 1e-4f;
+    unsigned long long cand = 0;
+    for (int f = 0; f < nmask; f++)
+        if (box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) <= lim0) cand |= 1ull << f;
+    int cur_list = -1;
+    v3 p1 = o, p2 = pend;
+    while (cand) {
+        float tsel = __int_as_float(0x7f800000);
+        int sel = -1;
+        for (unsigned long long m = cand; m; m &= m - 1) {
+            int f = __ffsll((long long)m) - 1;
+            float t = box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+            if (t < tsel) {
+                tsel = t;
+                sel = f;
+            }
+        }
+        if (sel < 0 || tsel > (float)len * 1.000001f + 1e-4f) break;
+        cand &= ~(1ull << sel);
+        int l = S.face_list[sel];
+        if (l != cur_list) {
+            const rp_facelist &L = S.lists[l];
+            p1 = xform(L.inv_trans.m, L.inv_trans.t, o);
+            p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
+            cur_list = l;
+        }
+        const rp_face &F = S.faces[sel];
+        double dist = face_isect(S, F, p1, p2, err);
+        if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && sel < best))) {
+            len = dist;
+            best = sel;
+            best_list = l;
+        }
+    }
+    // faces beyond the first 64 records: list order with the same skip test
+    for (int f = nmask; f < nf; f++) {
+        if (box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > (float)len * 1.000001f + 1e-4f) continue;
+        int l = S.face_list[f];
+        if (l != cur_list) {
+            const rp_facelist &L = S.lists[l];
+            p1 = xform(L.inv_trans.m, L.inv_trans.t, o);
+            p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
+            cur_list = l;
+        }
+        const rp_face &F = S.faces[f];
+        double dist = face_isect(S, F, p1, p2, err);
+        if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && f < best))) {
+            len = dist;
+            best = f;
+            best_list = l;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_tile;
@@ -39,29 +135,21 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
         o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
         d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
         v3 pend = addv(o, mulvs(d, A.max_len));
-        int l0 = 0, l1 = S.n_lists;
         if (A.one_list >= 0) {
-            l0 = A.one_list;
-            l1 = A.one_list + 1;
-        }
-        for (int l = l0; l < l1; l++) {
-            const rp_facelist &L = S.lists[l];
+            // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
+            const rp_facelist &L = S.lists[A.one_list];
             v3 p1 = xform(L.inv_trans.m, L.inv_trans.t, o);
             v3 p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
-            int f0 = L.first_face, f1 = L.first_face + L.n_faces;
-            if (A.one_face >= 0) {
-                f0 = L.first_face + A.one_face;
-                f1 = f0 + 1;
+            int f = L.first_face + A.one_face;
+            const rp_face &F = S.faces[f];
+            double dist = face_isect(S, F, p1, p2, A.err);
+            if (F.tolerance < dist && dist < len) {
+                len = dist;
+                best = f;
+                best_list = A.one_list;
             }
-            for (int f = f0; f < f1; f++) {
-                const rp_face &F = S.faces[f];
-                double dist = face_isect(S, F, p1, p2, A.err);
-                if (F.tolerance < dist && dist < len) {
-                    len = dist;
-                    best = f;
-                    best_list = l;
-                }
-            }
+        } else {
+            nearest_hit(S, o, d, pend, A.max_len, len, best, best_list, A.err);
         }
         A.in.len[i] = len;
         A.in.endf[i] = best >= 0 ? (unsigned)S.faces[best].idx : 0xFFFFFFFFu;
@@ -141,8 +229,10 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
 }
 
 size_t generation_smem_bytes(int n_lists, int n_recs, int n_mats, int n_faces) {
+    // tables (when staged) + boxes + face->list map (padded to 8 bytes) + hit counters
+    size_t tail = ((size_t)n_faces * 8 * 4 + (size_t)n_faces * 2 + 7) / 8 * 8 + (size_t)n_faces * sizeof(unsigned);
     return (size_t)n_lists * sizeof(rp_facelist) + (size_t)n_recs * sizeof(rp_face) +
-           (size_t)n_mats * sizeof(rp_material) + (size_t)n_faces * sizeof(unsigned);
+           (size_t)n_mats * sizeof(rp_material) + tail;
 }
 
 cudaError_t launch_generation_plain(const GenArgs &a, size_t smem, cudaStream_t st) {

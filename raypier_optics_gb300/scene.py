@@ -18,8 +18,11 @@ from .ctracer import Face, InterfaceMaterial, Shape
 
 
 def _check_type(obj, kind):
+    """Type tag of a face / material / distortion object.  A subclass that does
+    not declare its own device type (e.g. a user's Cython-level subclass of
+    Face or InterfaceMaterial in the reference) has no GPU implementation."""
     t = getattr(type(obj), "type_code", None)
-    if t is None or not hasattr(obj, "_pack"):
+    if not t or not hasattr(obj, "_pack"):
         raise NotImplementedError(f"{kind} type {type(obj).__name__} is not implemented on the GPU path")
     return t
 

@@ -197,26 +197,29 @@ def config2_spec():
     mats = {"air_crown": disp("crown", "air"), "crown_flint": disp("crown", "flint"),
             "flint_air": disp("flint", "air"), "detector": {"type": "OpaqueMaterial"}}
 
+    # cemented doublet, 50 mm: biconvex crown (R1 = 100, R2 = -80, 12 mm) and a
+    # flint meniscus (R3 = -250, 4 mm); every element has a positive edge thickness
     def doublet(z):
         return {"translation": [0, 0, z], "faces": [
-            {"type": "SphericalFace", "kw": {"curvature": -60.0, "z_height": 0.0, "invert_normal": 1},
+            {"type": "SphericalFace", "kw": {"curvature": -100.0, "z_height": 0.0, "invert_normal": 1},
              "owner": {"diameter": 50.0}, "material": "air_crown"},
-            {"type": "SphericalFace", "kw": {"curvature": 45.0, "z_height": 8.0},
+            {"type": "SphericalFace", "kw": {"curvature": 80.0, "z_height": 12.0},
              "owner": {"diameter": 50.0}, "material": "crown_flint"},
-            {"type": "SphericalFace", "kw": {"curvature": 150.0, "z_height": 11.0},
+            {"type": "SphericalFace", "kw": {"curvature": 250.0, "z_height": 16.0},
              "owner": {"diameter": 50.0}, "material": "flint_air"}]}
 
+    # even-asphere singlet, 50 mm: asphere front (sag 10.6 mm at r = 25), plane back 14 mm behind
     def asphere(z):
         circ = {"type": "CircleShape", "kw": {"radius": 25.0}}
         return {"translation": [0, 0, z], "faces": [
             {"type": "AsphericFace", "kw": {"curvature": -80.0, "z_height": 0.0, "conic_const": -0.6,
                                             "A4": 1e-5, "A6": -2e-8, "A8": 5e-11, "invert_normals": 1},
              "shape": circ, "material": "air_crown"},
-            {"type": "ShapedPlanarFace", "kw": {"z_height": 6.0}, "shape": circ, "material": "air_crown"}]}
+            {"type": "ShapedPlanarFace", "kw": {"z_height": 14.0}, "shape": circ, "material": "air_crown"}]}
 
     return {"curves": {"crown": CROWN, "flint": FLINT, "air": AIR}, "materials": mats,
-            "lists": [doublet(0.0), doublet(30.0), asphere(60.0), asphere(80.0),
-                      {"translation": [0, 0, 150], "faces": [
+            "lists": [doublet(0.0), doublet(30.0), asphere(60.0), asphere(90.0),
+                      {"translation": [0, 0, 160], "faces": [
                           {"type": "CircularFace", "kw": {"z_plane": 0.0},
                            "owner": {"diameter": 200.0, "offset": 0.0}, "material": "detector"}]}]}
 

@@ -1,0 +1,74 @@
+"""The face boxes that let the nearest-hit search skip faces must contain
+every point where the face can report a hit.  Checked on the CPU against the
+hit points of the oracle (which tests every face, as the reference does) for
+every golden scene and larger samples of the benchmark configurations."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import load_case, tables_for, trace_case_names
+from raypier_optics_gb300 import _native, ctracer
+from raypier_optics_gb300 import workloads as W
+
+
+def boxes(tables):
+    lib = _native.load()
+    out = np.zeros((tables.n_faces, 8), dtype=np.float32)
+    d = tables.desc()
+    assert lib.rp_scene_bounds(ctypes.byref(d), out.ctypes.data, tables.n_faces) == 0
+    return out
+
+
+def check_hits_inside(tables, gens):
+    b = boxes(tables)
+    idx_of = {int(f["idx"]): k for k, f in enumerate(tables.faces[:tables.n_faces])}
+    n_checked = 0
+    for g in gens:
+        hit = g["end_face_idx"] != 0xFFFFFFFF
+        pts = g["origin"][hit] + g["direction"][hit] * g["length"][hit][:, None]
+        recs = np.array([idx_of[int(i)] for i in g["end_face_idx"][hit]], dtype=np.int64)
+        for k in np.unique(recs):
+            if b[k, 6] == 0:
+                continue
+            p = pts[recs == k]
+            lo, hi = b[k, :3].astype(np.float64), b[k, 3:6].astype(np.float64)
+            inside = np.all((p >= lo) & (p <= hi), axis=1)
+            assert inside.all(), f"face record {k}: {np.count_nonzero(~inside)} hits outside its box"
+            n_checked += len(p)
+    return n_checked
+
+
+@pytest.mark.parametrize("name", trace_case_names())
+def test_golden_hits_lie_in_face_boxes(name):
+    c = load_case(name)
+    tables, _, _ = tables_for(c["spec"])
+    check_hits_inside(tables, c["gens"])
+
+
+@pytest.mark.parametrize("config", ["config1", "config2", "config3"])
+def test_benchmark_hits_lie_in_face_boxes(config):
+    if config == "config1":
+        rays, wl = W.config1_rays(ctracer.ray_dtype)
+        spec, P, per = W.config1_spec(), W.CONFIG1, False
+    elif config == "config2":
+        rays, wl = W.config2_rays(ctracer.ray_dtype, 1 << 20)
+        rays, wl = W.subsample(rays, wl, np.arange(0, 1 << 20, 128), per_ray_wavelength=True)
+        spec, P = W.config2_spec(), W.CONFIG2
+    else:
+        rays, wl = W.config3_rays(ctracer.ray_dtype, 512)
+        spec, P = W.config3_spec(), W.CONFIG3
+    tables, _, _ = tables_for(spec)
+    gens, _ = oracle.trace_rays(tables, wl, rays, P["recursion_limit"], P["max_length"], P["e2_terminate"])
+    assert check_hits_inside(tables, gens) > 0
+
+
+def test_boxes_are_tight_for_axis_aligned_faces():
+    tables, _, _ = tables_for(W.config2_spec())
+    b = boxes(tables)
+    # first doublet face: a 50 mm R=100 cap at z in [0, 3.18] (+ padding)
+    assert b[0, 6] == 1
+    assert np.allclose(b[0, :3], [-25, -25, 0], atol=2e-3) and np.allclose(b[0, 3:6], [25, 25, 3.1755], atol=2e-3)
+    # the asphere (z from 60 to 60 + 10.6)
+    assert b[6, 6] == 1 and 60 - 0.1 < b[6, 2] < 60 and 70.5 < b[6, 5] < 70.8

@@ -59,7 +59,7 @@ def test_gpu_config1_full_size_matches_reference_digest_and_oracle():
 
 @pytest.mark.parametrize("n", [1, 127, 128, 129, 4097, 65536])
 def test_gpu_config1_ragged_sizes_match_oracle(n):
-    rays, wl = W.config1_rays(ctracer.ray_dtype, max(n, 1))
+    rays, wl = W.config1_rays(ctracer.ray_dtype, max(n, 4096))
     rays = rays[:n]
     gens, _ = gpu_trace(W.config1_spec(), rays, wl, 6, 1000.0)
     tables, _, _ = tables_for(W.config1_spec())
