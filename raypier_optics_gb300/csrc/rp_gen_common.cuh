@@ -28,6 +28,7 @@ __device__ __forceinline__ void st_state(unsigned long long *p, unsigned long lo
 }
 
 // Stages lists / faces / materials in shared memory; returns the scene view.
+// The staged copies may be read only after the caller's next __syncthreads().
 __device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char *smem, unsigned **s_counts) {
     DevScene S = A.S;
     size_t nl = (size_t)S.n_lists * sizeof(rp_facelist) / 8;
@@ -50,9 +51,12 @@ __device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char
     float *bnd = reinterpret_cast<float *>(tail);
     for (int k = threadIdx.x; k < S.n_faces * 8; k += blockDim.x) bnd[k] = A.S.bounds[k];
     short *fl = reinterpret_cast<short *>(bnd + S.n_faces * 8);
+    // the list ranges are read from global memory: the shared copy above is
+    // not complete until the block's next barrier
     for (int l = 0; l < S.n_lists; l++) {
-        int f0 = S.lists[l].first_face, n = S.lists[l].n_faces;
-        for (int k = threadIdx.x; k < n; k += blockDim.x) fl[f0 + k] = (short)l;
+        int f0 = A.S.lists[l].first_face, n = A.S.lists[l].n_faces;
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            if (f0 + k < S.n_faces) fl[f0 + k] = (short)l;
     }
     unsigned *cnt = reinterpret_cast<unsigned *>(tail + (S.n_faces * 8 * 4 + S.n_faces * 2 + 7) / 8);
     for (int k = threadIdx.x; k < S.n_faces; k += blockDim.x) cnt[k] = 0;

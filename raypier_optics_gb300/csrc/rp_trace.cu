@@ -78,6 +78,10 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
         if (sel < 0 || tsel > (float)len * 1.000001f + 1e-4f) break;
         cand &= ~(1ull << sel);
         int l = S.face_list[sel];
+        if (l < 0 || l >= S.n_lists) {  // cannot happen for a validated scene
+            atomicOr(err, ERR_SHAPE_STACK);
+            break;
+        }
         if (l != cur_list) {
             const rp_facelist &L = S.lists[l];
             p1 = xform(L.inv_trans.m, L.inv_trans.t, o);
@@ -96,6 +100,10 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
     for (int f = nmask; f < nf; f++) {
         if (box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > (float)len * 1.000001f + 1e-4f) continue;
         int l = S.face_list[f];
+        if (l < 0 || l >= S.n_lists) {
+            atomicOr(err, ERR_SHAPE_STACK);
+            break;
+        }
         if (l != cur_list) {
             const rp_facelist &L = S.lists[l];
             p1 = xform(L.inv_trans.m, L.inv_trans.t, o);
