@@ -39,6 +39,7 @@ struct rp_ctx {
     std::vector<PoolBlock> pool;     // freed blocks kept for reuse
     uint64_t pooled;                 // bytes in `pool`
     std::vector<cudaEvent_t> gen_ev; // per-generation kernel events (pairs)
+    struct rp_rays *arena;           // child slots of the generation being traced
     // per-generation scan scratch: [counter | out_count | err | pad | stats[2] | tile states...]
     unsigned char *scratch;
     size_t scratch_bytes;
@@ -171,6 +172,7 @@ int rp_ctx_destroy(rp_ctx *c) {
     if (!c) return RP_ERR_INVALID;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    if (c->arena) rp_rays_free(c->arena);
     pool_release_all(c);
     for (auto ev : c->gen_ev) cudaEventDestroy(ev);
     if (c->scratch) cudaFree(c->scratch);
@@ -556,8 +558,15 @@ int rp_rays_field(const rp_rays *r, const char *name, void **p) {
 // ---- tracing ------------------------------------------------------------------
 #define SCRATCH_HDR 64
 
+// Per-generation scratch: [out_count | err | pad | stats[2] | pad], the
+// per-tile child counts and offsets, then the per-ray child counts.
+static size_t scratch_bytes_for(uint64_t n_tiles) {
+    return SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)) + align256(n_tiles * sizeof(unsigned long long)) +
+           n_tiles * RP_BLOCK;
+}
+
 static int ensure_scratch(rp_ctx *ctx, uint64_t n_tiles) {
-    size_t need = SCRATCH_HDR + n_tiles * sizeof(unsigned long long);
+    size_t need = scratch_bytes_for(n_tiles);
     if (need <= ctx->scratch_bytes) return RP_OK;
     if (ctx->scratch) {
         cudaStreamSynchronize(ctx->stream);
@@ -572,22 +581,37 @@ static int ensure_scratch(rp_ctx *ctx, uint64_t n_tiles) {
     return RP_OK;
 }
 
-// Launches one generation; on return h_pinned[0] holds the child count,
-// h_pinned[1] the error bits (valid after the stream is synchronised).
-static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float max_length, uint32_t flags,
-                      double e2, int emit, int one_list, int one_face) {
+// The child-slot arena: two ray slots per ray of the largest generation traced
+// so far (kept by the context and reused).
+static int ensure_arena(rp_ctx *ctx, uint64_t n_tiles) {
+    uint64_t need = n_tiles * RP_TILE_SLOTS;
+    if (ctx->arena && ctx->arena->cap >= need) return RP_OK;
+    if (ctx->arena) {
+        rp_rays_free(ctx->arena);
+        ctx->arena = nullptr;
+    }
+    return rp_rays_alloc(ctx, need + need / 4, &ctx->arena);
+}
+
+// Launches the generation kernel (and, when children are kept, the tile scan)
+// and queues the read-back of count / error / statistics into h_pinned.
+static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, uint32_t flags, double e2, int emit,
+                      int one_list, int one_face, GenArgs &a) {
     uint64_t n_in = in->n;
     uint64_t n_tiles = (n_in + RP_BLOCK - 1) / RP_BLOCK;
     int rc = ensure_scratch(ctx, n_tiles);
     if (rc) return rc;
+    if (emit) {
+        rc = ensure_arena(ctx, n_tiles);
+        if (rc) return rc;
+    }
     unsigned char *sc = ctx->scratch;
-    CK(cudaMemsetAsync(sc, 0, SCRATCH_HDR + n_tiles * sizeof(unsigned long long), ctx->stream));
-    GenArgs a;
+    CK(cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream));
     memset(&a, 0, sizeof a);
     a.in = in->soa;
-    a.out = out ? out->soa : in->soa;
+    a.out = in->soa;
     a.n_in = n_in;
-    a.out_cap = out ? out->cap : 0;
+    a.out_cap = 0;
     a.max_len = (double)max_length;
     a.e2_term = e2;
     a.emit = emit;
@@ -595,11 +619,14 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float
     a.one_face = one_face;
     a.S = s->S;
     a.smem_tables = s->smem_tables;
-    a.tile_counter = (unsigned *)(sc + 0);
-    a.out_count = (unsigned long long *)(sc + 8);
-    a.err = (unsigned *)(sc + 16);
-    a.stats = (unsigned long long *)(sc + 32);
-    a.tile_state = (unsigned long long *)(sc + SCRATCH_HDR);
+    a.out_count = (unsigned long long *)(sc + 0);
+    a.err = (unsigned *)(sc + 8);
+    a.stats = (unsigned long long *)(sc + 24);
+    a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
+    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)));
+    a.ray_counts = sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)) +
+                   align256(n_tiles * sizeof(unsigned long long));
+    a.scratch = emit ? ctx->arena->soa : in->soa;
     a.face_counts = s->face_counts;
     if (ctx->gen_ev.empty()) {
         ctx->gen_ev.resize(2);
@@ -610,11 +637,17 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float
                                              : launch_generation_plain(a, s->smem, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "generation kernel launch");
     CK(cudaEventRecord(ctx->gen_ev[1], ctx->stream));
-    CK(cudaMemcpyAsync(ctx->h_pinned, sc + 8, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    if (emit) {
+        e = launch_tile_scan(a, (unsigned)n_tiles, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "tile scan launch");
+    }
+    CK(cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     return RP_OK;
 }
 
-static int finish_gen(rp_ctx *ctx, rp_rays *out, int emit, rp_stats *st, uint64_t n_in) {
+// Waits for the generation, turns its error bits into a status and returns
+// the number of children in *count.
+static int finish_gen(rp_ctx *ctx, int emit, rp_stats *st, uint64_t n_in, uint64_t *count) {
     CK(cudaStreamSynchronize(ctx->stream));
     unsigned long long cnt = ctx->h_pinned[0];
     unsigned err = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
@@ -626,13 +659,10 @@ static int finish_gen(rp_ctx *ctx, rp_rays *out, int emit, rp_stats *st, uint64_
         st->hits += hits;
         st->terminated += term;
         st->kernel_ms += ms;
-        st->launches += 1;
+        st->launches += emit ? 3 : 1;  // generation, tile scan, placement
         st->generations += 1;
     }
-    if (err & ERR_TIMEOUT) {
-        snprintf(g_last_error, sizeof g_last_error, "look-back wait gave up");
-        return RP_ERR_TIMEOUT;
-    }
+    *count = emit ? cnt : 0;
     if (err & ERR_WAVELENGTH) {
         snprintf(g_last_error, sizeof g_last_error, "a ray's wavelength_idx is outside the wavelength table");
         return RP_ERR_INVALID;
@@ -641,14 +671,35 @@ static int finish_gen(rp_ctx *ctx, rp_rays *out, int emit, rp_stats *st, uint64_
         snprintf(g_last_error, sizeof g_last_error, "device evaluation limit hit (err=0x%x)", err);
         return RP_ERR_INVALID;
     }
-    if (!emit) return RP_OK;
-    if ((err & ERR_OVERFLOW) || cnt > out->cap) {
-        out->n = 0;
+    return RP_OK;
+}
+
+// Moves the generation's children into `out` (capacity checked by the caller).
+static int place_gen(rp_ctx *ctx, GenArgs &a, rp_rays *out, uint64_t count, rp_stats *st) {
+    a.out = out->soa;
+    a.out_cap = out->cap;
+    cudaError_t e = launch_place_children(a, (unsigned)((a.n_in + RP_BLOCK - 1) / RP_BLOCK), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "child placement launch");
+    out->n = count;
+    if (st) st->rays_out += count;
+    return RP_OK;
+}
+
+static int one_generation(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float max_length, uint32_t flags,
+                          double e2, int one_list, int one_face, rp_stats *st) {
+    GenArgs a;
+    uint64_t count = 0;
+    int rc = launch_gen(ctx, s, in, max_length, flags, e2, 1, one_list, one_face, a);
+    if (rc == RP_OK) rc = finish_gen(ctx, 1, st, in->n, &count);
+    if (rc) return rc;
+    if (count > out->cap) {
+        snprintf(g_last_error, sizeof g_last_error, "%llu children do not fit the output buffer",
+                 (unsigned long long)count);
         return RP_ERR_CAPACITY;
     }
-    out->n = cnt;
-    if (st) st->rays_out += cnt;
-    return RP_OK;
+    rc = place_gen(ctx, a, out, count, st);
+    if (rc == RP_OK) CK(cudaStreamSynchronize(ctx->stream));
+    return rc;
 }
 
 int rp_trace_segment(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float max_length, uint32_t flags,
@@ -658,10 +709,9 @@ int rp_trace_segment(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float 
     out->n = 0;
     if (in->n == 0) return RP_OK;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    int rc = launch_gen(ctx, s, in, out, max_length, flags, e2, 1, -1, -1);
-    if (rc) return rc;
+    int rc = one_generation(ctx, s, in, out, max_length, flags, e2, -1, -1, st);
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
-    rc = finish_gen(ctx, out, 1, st, in->n);
+    CK(cudaEventSynchronize(ctx->ev1));
     if (st) {
         float ms = 0;
         cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
@@ -678,9 +728,7 @@ int rp_trace_one_face_segment(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *ou
     CK(cudaSetDevice(ctx->device));
     out->n = 0;
     if (in->n == 0) return RP_OK;
-    int rc = launch_gen(ctx, s, in, out, max_length, flags, e2, 1, list_idx, face_idx);
-    if (rc) return rc;
-    return finish_gen(ctx, out, 1, st, in->n);
+    return one_generation(ctx, s, in, out, max_length, flags, e2, list_idx, face_idx, st);
 }
 
 int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, int32_t recursion_limit,
@@ -696,26 +744,27 @@ int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, in
     // core/tracer.py:40-45: while rays.n_rays > 0 and count < recursion_limit
     while (rays->n > 0 && count < recursion_limit) {
         int last = (count + 1 == recursion_limit);  // children of this generation are discarded
-        rp_rays *next = nullptr;
-        if (!last) {
-            if (count + 1 >= max_gens) {
-                rc = RP_ERR_CAPACITY;
-                break;
-            }
-            rc = rp_rays_alloc(ctx, rays->n * 2, &next);
-            if (rc) break;
-        }
-        rc = launch_gen(ctx, s, rays, next, max_length, flags, e2, last ? 0 : 1, -1, -1);
-        if (rc == RP_OK) rc = finish_gen(ctx, next, last ? 0 : 1, st, rays->n);
-        if (rc) {
-            if (next) rp_rays_free(next);
+        if (!last && count + 1 >= max_gens) {
+            rc = RP_ERR_CAPACITY;
             break;
         }
+        GenArgs a;
+        uint64_t n_child = 0;
+        rc = launch_gen(ctx, s, rays, max_length, flags, e2, last ? 0 : 1, -1, -1, a);
+        if (rc == RP_OK) rc = finish_gen(ctx, last ? 0 : 1, st, rays->n, &n_child);
+        if (rc) break;
         count++;
-        if (last) break;
+        if (last || n_child == 0) break;
+        rp_rays *next = nullptr;
+        rc = rp_rays_alloc(ctx, n_child, &next);  // exact size: the count is known
+        if (rc) break;
+        rc = place_gen(ctx, a, next, n_child, st);
+        if (rc) {
+            rp_rays_free(next);
+            break;
+        }
         gens[count] = next;
         rays = next;
-        if (next->n == 0) break;
     }
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaEventSynchronize(ctx->ev1));
@@ -724,12 +773,7 @@ int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, in
         cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
         st->device_ms += ms;
     }
-    // traced generations: those with rays that were traced
     *n_gens = count;
-    if (rc == RP_OK && count > 0 && count < max_gens && gens[count] && gens[count]->n == 0) {
-        rp_rays_free(gens[count]);
-        gens[count] = nullptr;
-    }
     return rc;
 }
 

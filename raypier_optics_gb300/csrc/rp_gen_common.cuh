@@ -1,31 +1,19 @@
 // rp_gen_common.cuh -- the parts of a generation kernel that do not depend on
 // the arithmetic path: shared-memory staging of the scene tables, the
-// block-wide scan of per-ray child counts, the decoupled look-back across
-// tiles and the stable scatter of children.
+// block-wide scan of per-ray child counts and the stores of children.
 //
 // Ordering contract (the reference's RayCollection.add_ray_c append order,
 // raypier/core/ctracer.pyx:1004-1012 driven by trace_segment_c 2083-2117):
 // children are stored in ascending parent index, and a parent's children in
-// emission order (reflected before transmitted).  Tiles take tickets from an
-// atomic counter so that every tile a tile waits on is already running; every
-// wait is bounded and reports ERR_TIMEOUT instead of hanging.
+// emission order (reflected before transmitted).  A tile of rays writes its
+// children, in that order, to its own slot range of a scratch arena and
+// publishes their count; a scan of the counts then gives every tile its final
+// offset and a copy kernel places the children (rp_trace.cu).  Tiles never wait
+// for one another, so a tile with slow rays does not hold up the others.
 #pragma once
-#include <cuda/atomic>
-
 #include "rp_kernels.cuh"
 
 namespace rp {
-
-#define RP_LOOKBACK_SPIN_LIMIT (1 << 22)
-
-__device__ __forceinline__ unsigned long long ld_state(unsigned long long *p) {
-    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> r(*p);
-    return r.load(cuda::memory_order_relaxed);
-}
-__device__ __forceinline__ void st_state(unsigned long long *p, unsigned long long v) {
-    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> r(*p);
-    r.store(v, cuda::memory_order_relaxed);
-}
 
 // Stages lists / faces / materials in shared memory; returns the scene view.
 // The staged copies may be read only after the caller's next __syncthreads().
@@ -66,13 +54,10 @@ __device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char
     return S;
 }
 
-// Exclusive block scan of `c` plus the tile's global offset (decoupled
-// look-back).  Returns the thread's global exclusive offset; *total_out gets
-// the block total.  Must be called by all threads of the block.
-__device__ __forceinline__ unsigned long long block_offsets(const GenArgs &A, unsigned tile, unsigned c,
-                                                            unsigned *total_out) {
+// Exclusive scan of `c` over the block; *total_out gets the block total.
+// Must be called by all threads of the block.
+__device__ __forceinline__ unsigned block_scan(unsigned c, unsigned *total_out) {
     __shared__ unsigned s_warp[RP_BLOCK / 32];
-    __shared__ unsigned long long s_base;
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned v = c;
 #pragma unroll
@@ -90,49 +75,11 @@ __device__ __forceinline__ unsigned long long block_offsets(const GenArgs &A, un
             if (lane >= (unsigned)o) w += t;
         }
         if (lane < RP_BLOCK / 32) s_warp[lane] = w;  // inclusive warp prefixes
-        unsigned long long agg = __shfl_sync(0xffffffffu, w, RP_BLOCK / 32 - 1);
-        unsigned long long excl = 0;
-        if (tile == 0) {
-            if (lane == 0) st_state(&A.tile_state[0], RP_TILE_PREFIX | agg);
-        } else {
-            if (lane == 0) st_state(&A.tile_state[tile], RP_TILE_AGG | agg);
-            long long j = (long long)tile - 1;
-            int spins = 0;
-            while (true) {
-                long long idx = j - (long long)lane;
-                unsigned long long s = (idx >= 0) ? ld_state(&A.tile_state[idx]) : RP_TILE_PREFIX;
-                unsigned flag = (unsigned)(s >> 62);
-                unsigned pm = __ballot_sync(0xffffffffu, flag == 2u);
-                unsigned nr = __ballot_sync(0xffffffffu, flag == 0u);
-                int first_p = pm ? (__ffs(pm) - 1) : 31;
-                unsigned relevant = (first_p == 31) ? 0xffffffffu : ((2u << first_p) - 1u);
-                if (nr & relevant) {
-                    if (++spins > RP_LOOKBACK_SPIN_LIMIT) {
-                        if (lane == 0) atomicOr(A.err, ERR_TIMEOUT);
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
-                }
-                unsigned long long val = ((unsigned)lane <= (unsigned)first_p) ? (s & RP_TILE_VALUE_MASK) : 0ull;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) val += __shfl_down_sync(0xffffffffu, val, o);
-                val = __shfl_sync(0xffffffffu, val, 0);
-                excl += val;
-                if (pm) break;
-                j -= 32;
-            }
-            if (lane == 0) st_state(&A.tile_state[tile], RP_TILE_PREFIX | (excl + agg));
-        }
-        if (lane == 0) {
-            s_base = excl;
-            if (tile == gridDim.x - 1) *A.out_count = excl + agg;
-        }
     }
     __syncthreads();
-    unsigned incl_warp_before = (warp > 0) ? s_warp[warp - 1] : 0u;
+    unsigned before = (warp > 0) ? s_warp[warp - 1] : 0u;
     *total_out = s_warp[RP_BLOCK / 32 - 1];
-    return s_base + incl_warp_before + (v - c);
+    return before + (v - c);
 }
 
 // Writes one child record at slot k of `out`.

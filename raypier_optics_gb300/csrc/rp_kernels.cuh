@@ -17,10 +17,12 @@ struct RaySoA {
     unsigned *wl, *parent, *endf, *ident, *type;
 };
 
-// Tile status words of the decoupled look-back scan: flag in the top 2 bits.
-#define RP_TILE_AGG (1ull << 62)
-#define RP_TILE_PREFIX (2ull << 62)
-#define RP_TILE_VALUE_MASK ((1ull << 62) - 1)
+// The children of ray i of a generation are first written to slots 2i and
+// 2i + 1 of a scratch ray arena, with their number in ray_counts[i]; once every
+// tile's total is known (tile scan) the placement kernel moves them to their
+// final, contiguous place.  No ray or tile waits for another.
+#define RP_BLOCK 128
+#define RP_TILE_SLOTS (2 * RP_BLOCK)
 
 struct GenArgs {
     RaySoA in, out;
@@ -32,19 +34,22 @@ struct GenArgs {
     int one_list, one_face;       // >= 0: sequential trace of one face of one list
     DevScene S;                   // global-memory tables
     int smem_tables;              // 1: lists/faces/materials staged in shared memory
-    unsigned *tile_counter;       // ticket counter (zeroed before launch)
-    unsigned long long *tile_state;
-    unsigned long long *out_count;  // total children (written by the last tile)
+    RaySoA scratch;                 // child slots: 2 per ray
+    unsigned char *ray_counts;      // [n_in] children of each ray (0..2)
+    unsigned *tile_counts;          // [n_tiles] children of each tile
+    unsigned long long *tile_offsets;  // [n_tiles] exclusive prefix (scan kernel)
+    unsigned long long *out_count;  // total children (scan kernel)
     unsigned *err;                  // error bits
     unsigned *face_counts;          // per face record hit counters
     unsigned long long *stats;      // [0] hits, [1] terminated children
 };
 
-#define RP_BLOCK 128
-
 // launchers (rp_trace.cu / rp_mixed.cu); return cudaError_t
 cudaError_t launch_generation_plain(const GenArgs &a, size_t smem, cudaStream_t st);
 cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st);
+// tile-count scan (one block) and the scatter of children to their final slots
+cudaError_t launch_tile_scan(const GenArgs &a, unsigned n_tiles, cudaStream_t st);
+cudaError_t launch_place_children(const GenArgs &a, unsigned n_tiles, cudaStream_t st);
 cudaError_t launch_aos_to_soa(const void *aos, RaySoA soa, unsigned long long n, cudaStream_t st);
 cudaError_t launch_soa_to_aos(RaySoA soa, void *aos, unsigned long long n, cudaStream_t st);
 cudaError_t launch_dispersion_table(const rp_dispersion *curves, int n_curves, const double *aux,

@@ -122,17 +122,16 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
 
 __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ unsigned s_tile;
-    __shared__ unsigned s_hits, s_term;
+    __shared__ unsigned s_hits, s_term, s_children;
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
     if (threadIdx.x == 0) {
-        s_tile = atomicAdd(A.tile_counter, 1u);
         s_hits = 0;
         s_term = 0;
+        s_children = 0;
     }
     __syncthreads();
-    const unsigned tile = s_tile;
+    const unsigned tile = blockIdx.x;
     const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
     const bool active = i < A.n_in;
 
@@ -217,19 +216,16 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
         }
     }
 
-    unsigned total;
-    unsigned long long base = block_offsets(A, tile, (unsigned)nc, &total);
     if (nc > 0) {
         double phase = A.in.phase[i];
         unsigned wl = A.in.wl[i], ident = A.in.ident[i];
         unsigned endf = (unsigned)S.faces[best].idx;
-        for (int k = 0; k < nc; k++) {
-            unsigned long long slot = base + k;
-            if (slot < A.out_cap) store_child(A.out, slot, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
-            else atomicOr(A.err, ERR_OVERFLOW);
-        }
+        for (int k = 0; k < nc; k++) store_child(A.scratch, 2 * i + k, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
+        atomicAdd(&s_children, (unsigned)nc);
     }
+    if (active) A.ray_counts[i] = (unsigned char)nc;
     flush_counts(A, S, s_counts);
+    if (threadIdx.x == 0) A.tile_counts[tile] = s_children;
     if (threadIdx.x == 0) {
         atomicAdd(&A.stats[0], (unsigned long long)s_hits);
         if (s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
@@ -254,6 +250,74 @@ cudaError_t launch_generation_plain(const GenArgs &a, size_t smem, cudaStream_t 
         configured = smem;
     }
     generation_plain_kernel<<<grid, RP_BLOCK, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ---- child placement ------------------------------------------------------
+// One block scans the per-tile child counts (exclusive prefix + total).
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *counts, unsigned n_tiles,
+                                                         unsigned long long *offsets, unsigned long long *total) {
+    __shared__ unsigned long long s_part[1024];
+    __shared__ unsigned long long s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (unsigned base = 0; base < n_tiles; base += 1024) {
+        unsigned i = base + threadIdx.x;
+        unsigned long long v = i < n_tiles ? counts[i] : 0;
+        s_part[threadIdx.x] = v;
+        __syncthreads();
+        for (unsigned o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
+            unsigned long long t = threadIdx.x >= o ? s_part[threadIdx.x - o] : 0;
+            __syncthreads();
+            s_part[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < n_tiles) offsets[i] = s_carry + s_part[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += s_part[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = s_carry;
+}
+
+cudaError_t launch_tile_scan(const GenArgs &a, unsigned n_tiles, cudaStream_t st) {
+    tile_scan_kernel<<<1, 1024, 0, st>>>(a.tile_counts, n_tiles, a.tile_offsets, a.out_count);
+    return cudaGetLastError();
+}
+
+// Moves each ray's children from its two scratch slots to their final place:
+// tile offset + the exclusive scan of the tile's per-ray counts.
+__device__ __forceinline__ void copy_ray(const RaySoA &s, unsigned long long src, const RaySoA &o,
+                                         unsigned long long dst) {
+    o.ox[dst] = s.ox[src]; o.oy[dst] = s.oy[src]; o.oz[dst] = s.oz[src];
+    o.dx[dst] = s.dx[src]; o.dy[dst] = s.dy[src]; o.dz[dst] = s.dz[src];
+    o.nx[dst] = s.nx[src]; o.ny[dst] = s.ny[src]; o.nz[dst] = s.nz[src];
+    o.ex[dst] = s.ex[src]; o.ey[dst] = s.ey[src]; o.ez[dst] = s.ez[src];
+    o.n[dst] = s.n[src]; o.e1[dst] = s.e1[src]; o.e2[dst] = s.e2[src];
+    o.len[dst] = s.len[src]; o.phase[dst] = s.phase[src]; o.opl[dst] = s.opl[src];
+    o.wl[dst] = s.wl[src]; o.parent[dst] = s.parent[src]; o.endf[dst] = s.endf[src];
+    o.ident[dst] = s.ident[src]; o.type[dst] = s.type[src];
+}
+
+__global__ void __launch_bounds__(RP_BLOCK) place_children_kernel(GenArgs A) {
+    const unsigned tile = blockIdx.x;
+    const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
+    unsigned c = i < A.n_in ? A.ray_counts[i] : 0u;
+    unsigned total;
+    unsigned excl = block_scan(c, &total);
+    unsigned long long base = A.tile_offsets[tile] + excl;
+    for (unsigned k = 0; k < c; k++) {
+        if (base + k >= A.out_cap) {
+            atomicOr(A.err, ERR_OVERFLOW);
+            return;
+        }
+        copy_ray(A.scratch, 2 * i + k, A.out, base + k);
+    }
+}
+
+cudaError_t launch_place_children(const GenArgs &a, unsigned n_tiles, cudaStream_t st) {
+    if (n_tiles == 0) return cudaSuccess;
+    place_children_kernel<<<n_tiles, RP_BLOCK, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -79,7 +79,8 @@ def trace_rays(input_rays, face_lists, recursion_limit=100, max_length=100.0, fl
         traced.append(rc)
         prev = rc
     # free generations the driver allocated but the reference would not return
-    for g in range(n_gens.value, max_gens):
+    # (gens[0] is the caller's input buffer and stays with input_rays)
+    for g in range(max(n_gens.value, 1), max_gens):
         if gens[g]:
             lib.rp_rays_free(ctypes.c_void_p(gens[g]))
     _apply_counts(scene, tables)
