@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--rays", type=int, default=0, help="override the ray count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     ap.add_argument("--cpu-sample", type=int, default=0, help="rays in the CPU-baseline sample")
     return ap.parse_args()
 
@@ -231,47 +232,56 @@ def main():
     g0 = runtime.DeviceRays(ctx, n)
     g0.upload(np.ascontiguousarray(rays))
 
-    def step(stats):
+    def step(stats, fl):
         gens = (ctypes.c_void_p * max_gens)()
         gens[0] = g0.handle
         ng = ctypes.c_int32(0)
-        _native.check(lib.rp_trace_rays(ctx.handle, dscene.handle, gens, max_gens, rl, max_len, flags, e2,
+        _native.check(lib.rp_trace_rays(ctx.handle, dscene.handle, gens, max_gens, rl, max_len, fl, e2,
                                         ctypes.byref(ng), ctypes.byref(stats)), "rp_trace_rays")
         for g in range(1, max_gens):
             if gens[g]:
                 lib.rp_rays_free(ctypes.c_void_p(gens[g]))
         return ng.value
 
-    for _ in range(max(args.warmup, 0)):
-        step(_native.Stats())
-    ctx.synchronize()
-    if dist:
-        dist.barrier()
-    clocks = ClockSampler(device)
-    clocks.start()
-    stats = _native.Stats()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        ng = step(stats)
-    ctx.synchronize()
-    wall = time.perf_counter() - t0
-    clk = clocks.stop()
-    dev_s = stats.device_ms / 1000.0
+    def timed(fl, sample_clocks):
+        for _ in range(max(args.warmup, 0)):
+            step(_native.Stats(), fl)
+        ctx.synchronize()
+        if dist:
+            dist.barrier()
+        clocks = ClockSampler(device) if sample_clocks else None
+        if clocks:
+            clocks.start()
+        st = _native.Stats()
+        t0 = time.perf_counter()
+        ng = 0
+        for _ in range(args.steps):
+            ng = step(st, fl)
+        ctx.synchronize()
+        wall = time.perf_counter() - t0
+        clk = clocks.stop() if clocks else None
+        dev_s = st.device_ms / 1000.0
+        segs = float(st.rays_in)
+        if dist:
+            import torch
+            tmax = torch.tensor([dev_s], dtype=torch.float64)
+            dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+            tsum = torch.tensor([segs], dtype=torch.float64)
+            dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+            dev_s, segs = float(tmax[0]), float(tsum[0])
+        return st, dev_s, wall, clk, ng, segs / dev_s
+
+    stats, dev_s, wall, clk, ng, value = timed(flags, True)
     segs = stats.rays_in
     children = stats.rays_out
-    if dist:
-        import torch
-        t = torch.tensor([dev_s, float(segs)], dtype=torch.float64)
-        tmax = torch.tensor([dev_s], dtype=torch.float64)
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        tsum = torch.tensor([float(segs)], dtype=torch.float64)
-        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
-        dev_s, segs_total = float(tmax[0]), float(tsum[0])
-    else:
-        segs_total = float(segs)
-    value = segs_total / dev_s
     seg_per_step = segs / args.steps
-
+    mixed = None
+    if flags == 0 and not args.no_mixed:
+        mst, mdev_s, mwall, _, _, mvalue = timed(1, False)
+        mixed = {"value": mvalue, "unit": UNIT, "ms_per_step": 1000.0 * mdev_s / args.steps,
+                 "speedup_vs_plain_fp64": mvalue / value, "kernel": "generation_mixed_kernel",
+                 "kernel_ms_per_step": mst.kernel_ms / args.steps,
+                 "precision_vs_plain_fp64": precision_sample(ctx, spec, rays, wl, P, per_ray)}
     # roofline of the generation kernel
     alg_bytes = segs * BYTES_PER_SEGMENT + children * BYTES_PER_CHILD
     kern_s = stats.kernel_ms / 1000.0
@@ -285,7 +295,7 @@ def main():
                                             seg_per_step, dist, world)
     if rank == 0:
         emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
-             achieved, peak, peak_kind, flags, stats, clk, cpu)
+             achieved, peak, peak_kind, flags, stats, clk, cpu, mixed)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -333,8 +343,29 @@ def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, s
     return e2e_value, d2h, e2e_steps
 
 
+def precision_sample(ctx, spec, rays, wl, P, per_ray, n_sample=16384):
+    """Error of the mixed path against the plain FP64 path on a ray sample."""
+    import types
+    from raypier_optics_gb300 import cdistortions, cfaces, cmaterials, cshapes, ctracer, precision, tracer
+    from raypier_optics_gb300 import workloads as W
+    ns = types.SimpleNamespace(ctracer=ctracer, cfaces=cfaces, cmaterials=cmaterials, cshapes=cshapes,
+                               cdistortions=cdistortions)
+    idx = np.linspace(0, rays.shape[0] - 1, min(n_sample, rays.shape[0])).astype(np.int64)
+    sub, swl = W.subsample(rays, wl, idx, per_ray_wavelength=per_ray)
+    out = []
+    for fl in (tracer.RP_TRACE_PLAIN_FP64, tracer.RP_TRACE_MIXED):
+        rc = ctracer.RayCollection.from_array(sub)
+        rc.wavelengths = swl
+        traced, _ = tracer.trace_rays(rc, W.build_scene(spec, ns), recursion_limit=P["recursion_limit"],
+                                      max_length=P["max_length"], flags=fl, e2_terminate=P["e2_terminate"], ctx=ctx)
+        out.append([t.copy_as_array() for t in traced])
+    st = precision.compare_traces(out[1], out[0])
+    st["sample_rays"] = int(len(sub))
+    return st
+
+
 def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
-         achieved, peak, peak_kind, flags, stats, clk, cpu):
+         achieved, peak, peak_kind, flags, stats, clk, cpu, mixed=None):
     if True:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -358,6 +389,8 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
             "gpu_launches": int(stats.launches),
             "clocks": clk,
         }
+        if mixed is not None:
+            line["mixed"] = mixed
         if cpu is not None:
             line["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": cpu["kind"],
                                     "sample": cpu["sample"]}

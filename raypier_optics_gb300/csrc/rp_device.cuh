@@ -522,10 +522,9 @@ static __device__ double face_isect_base(const DevScene &S, const rp_face &f, v3
             for (int i = 0; i < 100; i++) {
                 a1 += dz;
                 if (dz * dz < tol) { conv = true; break; }
-                asph_eval(f, a, d, a1, true, false, &fv, &gv);
+                asph_eval(f, a, d, a1, true, true, &fv, &gv);  // f and its derivative share r^2 and the root
                 if (fabs(fv) > fabs(f_last)) return RP_MISS;
                 f_last = fv;
-                asph_eval(f, a, d, a1, false, true, &fv, &gv);
                 dz = -fv / gv;
             }
             if (!conv) return RP_MISS;
@@ -765,9 +764,9 @@ struct ChildCommon {
 // convert_to_sp (cmaterials.pyx:49-91).  Returns false at normal incidence,
 // where the reference returns the ray unchanged.
 __device__ __forceinline__ void convert_to_sp(const RayState &r, v3 normal, v3 &E_out, cx &e1_out, cx &e2_out) {
-    v3 E2_vector = normv(crossv(r.d, r.E));
-    v3 E1_vector = normv(crossv(E2_vector, r.d));
-    normal = normv(normal);
+    v3 E2_vector = normv_fast(crossv(r.d, r.E));
+    v3 E1_vector = normv_fast(crossv(E2_vector, r.d));
+    normal = normv_fast(normal);
     v3 S = crossv(r.d, normal);
     if (fabs(S.x) < 1.0e-10 && fabs(S.y) < 1.0e-10 && fabs(S.z) < 1.0e-10) {
         E_out = r.E;
@@ -775,8 +774,8 @@ __device__ __forceinline__ void convert_to_sp(const RayState &r, v3 normal, v3 &
         e2_out = r.e2;
         return;
     }
-    S = normv(S);
-    v3 P = normv(crossv(r.d, S));
+    S = normv_fast(S);
+    v3 P = normv_fast(crossv(r.d, S));
     double A = dotv(E1_vector, S);
     double B = dotv(E2_vector, S);
     e1_out = mkc(r.e1.x * A + r.e2.x * B, r.e1.y * A + r.e2.y * B);
@@ -796,7 +795,7 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
         case RP_MAT_NONE:
         case RP_MAT_OPAQUE: return 0;  // cmaterials.pyx:245-251
         case RP_MAT_TRANSPARENT: {     // cmaterials.pyx:260-278
-            v3 normal = normv(onormal);
+            v3 normal = normv_fast(onormal);
             cx e1, e2;
             convert_to_sp(r, normal, cc.E, e1, e2);
             cc.opl = r.opl + (r.len * r.n.x);
@@ -811,7 +810,7 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
             return 1;
         }
         case RP_MAT_PEC: {  // cmaterials.pyx:285-319
-            v3 normal = normv(onormal);
+            v3 normal = normv_fast(onormal);
             cx e1, e2;
             convert_to_sp(r, normal, cc.E, e1, e2);
             double cosTheta = dotv(normal, r.d);
@@ -829,8 +828,8 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
         }
         case RP_MAT_PARTIAL:               // cmaterials.pyx:344-397
         case RP_MAT_LINEAR_POLARISING: {   // cmaterials.pyx:404-455
-            v3 normal = normv(onormal);
-            v3 ind = normv(r.d);
+            v3 normal = normv_fast(onormal);
+            v3 ind = normv_fast(r.d);
             cx e1, e2;
             convert_to_sp(r, normal, cc.E, e1, e2);
             double cosTheta = dotv(normal, ind);
@@ -862,8 +861,8 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
             return 2;
         }
         case RP_MAT_WAVEPLATE: {  // cmaterials.pyx:527-551
-            v3 normal = normv(onormal);
-            v3 ind = normv(r.d);
+            v3 normal = normv_fast(onormal);
+            v3 ind = normv_fast(r.d);
             cx e1, e2;
             convert_to_sp(r, mkv(m.p[2], m.p[3], m.p[4]), cc.E, e1, e2);
             cc.opl = r.opl + (r.len * r.n.x);
@@ -879,8 +878,8 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
             return 1;
         }
         case RP_MAT_DIELECTRIC: {  // cmaterials.pyx:589-680
-            v3 normal = normv(onormal);
-            v3 ind = normv(r.d);
+            v3 normal = normv_fast(onormal);
+            v3 ind = normv_fast(r.d);
             cx e1, e2;
             convert_to_sp(r, normal, cc.E, e1, e2);
             cc.opl = r.opl + (r.len * r.n.x);
@@ -930,8 +929,8 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
         }
         case RP_MAT_FULL_DIELECTRIC:
         case RP_MAT_FULL_DIELECTRIC_DISPERSIVE: {  // cmaterials.pyx:756-872, 897-1013
-            v3 normal = normv(onormal);
-            v3 ind = normv(r.d);
+            v3 normal = normv_fast(onormal);
+            v3 ind = normv_fast(r.d);
             cx E1, E2;
             convert_to_sp(r, normal, cc.E, E1, E2);
             cc.opl = r.opl + (r.len * r.n.x);
@@ -970,8 +969,7 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
             R_s = cmul(R_s, E1);
             R_p = cmul(R_p, E2);
             int nc = 0;
-            double ars = cabs_(R_s), arp = cabs_(R_p);
-            if (((n1.x * (ars * ars + arp * arp)) / P_in) > m.reflection_threshold) {
+            if (((n1.x * (cabs2_(R_s) + cabs2_(R_p))) / P_in) > m.reflection_threshold) {
                 ch[0].d = subv(ind, mulvs(ctn, 2.0));
                 ch[0].len = INF;
                 ch[0].e1 = R_s;
@@ -989,8 +987,7 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
             cx num = cmuls(cmuls(n1, 2.0 * cos1), aspect);
             cx T_p = cmul(cdiv(num, den_p), E2);
             cx T_s = cmul(cdiv(num, den_s), E1);
-            double ats = cabs_(T_s), atp = cabs_(T_p);
-            if (((n2.x * (ats * ats + atp * atp)) / P_in) > m.transmission_threshold) {
+            if (((n2.x * (cabs2_(T_s) + cabs2_(T_p))) / P_in) > m.transmission_threshold) {
                 ch[nc].d = transmitted;
                 ch[nc].len = INF;
                 ch[nc].e1 = T_s;
@@ -1006,7 +1003,7 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
             if (r_ > m.p[0]) return 0;
             double atten = (0.5 + (0.5 * erf(((m.p[1] - r_) / m.p[2]))));
             if (m.p[3] != 0.0) atten = (1.0 - atten);
-            v3 normal = normv(onormal);
+            v3 normal = normv_fast(onormal);
             cx e1, e2;
             convert_to_sp(r, normal, cc.E, e1, e2);
             cc.opl = r.opl + (r.len * r.n.x);
@@ -1033,7 +1030,7 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
             atten = (atten * (0.5 - (0.5 * erf(((py - y) / width)))));
             atten = (atten * (0.5 - (0.5 * erf(((-(py + y)) / width)))));
             if (m.p[5] != 0.0) atten = (1.0 - atten);
-            v3 normal = normv(onormal);
+            v3 normal = normv_fast(onormal);
             cx e1, e2;
             convert_to_sp(r, normal, cc.E, e1, e2);
             cc.opl = r.opl + (r.len * r.n.x);

@@ -38,6 +38,13 @@ __device__ __forceinline__ v3 normv(v3 a) {
     double m = sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
     return mkv(a.x / m, a.y / m, a.z / m);
 }
+// Normalisation with one reciprocal instead of three divisions: within an ulp
+// of norm_, used where the result is a direction / polarisation vector
+// (materials, face normals) rather than a distance that selects a face.
+__device__ __forceinline__ v3 normv_fast(v3 a) {
+    double inv = 1.0 / sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    return mkv(a.x * inv, a.y * inv, a.z * inv);
+}
 // sep_ (ctracer.pyx:108-113)
 __device__ __forceinline__ double sepv(v3 p1, v3 p2) {
     double a = p2.x - p1.x, b = p2.y - p1.y, c = p2.z - p1.z;
@@ -96,29 +103,25 @@ __device__ __forceinline__ cx csub(cx a, cx b) { return mkc(a.x - b.x, a.y - b.y
 __device__ __forceinline__ cx cmul(cx a, cx b) { return mkc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 // Complex times (s + 0i): equals cmul(a, (s,0)) up to the sign of zero.
 __device__ __forceinline__ cx cmuls(cx a, double s) { return mkc(a.x * s, a.y * s); }
-// Complex division by Smith's algorithm (R. L. Smith, "Algorithm 116: Complex
-// division", CACM 5(8), 1962), one reciprocal of the scaled denominator.
+// Complex division a / b = a conj(b) / |b|^2 with one reciprocal.  The
+// operands here (refractive indices, Fresnel denominators) are of order one,
+// far from the range where |b|^2 could overflow or underflow.
 __device__ __forceinline__ cx cdiv(cx a, cx b) {
-    if (fabs(b.x) >= fabs(b.y)) {
-        double r = b.y / b.x;
-        double inv = 1.0 / (b.x + b.y * r);
-        return mkc((a.x + a.y * r) * inv, (a.y - a.x * r) * inv);
-    } else {
-        double r = b.x / b.y;
-        double inv = 1.0 / (b.x * r + b.y);
-        return mkc((a.x * r + a.y) * inv, (a.y * r - a.x) * inv);
-    }
+    double inv = 1.0 / (b.x * b.x + b.y * b.y);
+    return mkc((a.x * b.x + a.y * b.y) * inv, (a.y * b.x - a.x * b.y) * inv);
 }
 // Principal complex square root (W. Kahan, "Branch cuts for complex elementary
 // functions", 1987): t = sqrt((|x| + |z|)/2).
 __device__ __forceinline__ cx csqrt_(cx z) {
     double x = z.x, y = z.y;
     if (x == 0.0 && y == 0.0) return mkc(0.0, y);
-    double t = sqrt((fabs(x) + hypot(x, y)) * 0.5);
-    if (x >= 0.0) return mkc(t, y / (2.0 * t));
-    return mkc(fabs(y) / (2.0 * t), copysign(t, y));
+    double t = sqrt((fabs(x) + sqrt(x * x + y * y)) * 0.5);
+    double h = 0.5 / t;
+    if (x >= 0.0) return mkc(t, y * h);
+    return mkc(fabs(y) * h, copysign(t, y));
 }
-__device__ __forceinline__ double cabs_(cx z) { return hypot(z.x, z.y); }
+// |z|^2 (the reference squares cabs(z))
+__device__ __forceinline__ double cabs2_(cx z) { return z.x * z.x + z.y * z.y; }
 
 __device__ __forceinline__ double inf_d() { return __longlong_as_double(0x7ff0000000000000LL); }
 __device__ __forceinline__ double nan_d() { return __longlong_as_double(0x7ff8000000000000LL); }

@@ -130,7 +130,8 @@ def test_gpu_trace_one_face_segment_matches_oracle():
 
 # ---- single-plugin calls against the reference's unit outputs ----------------------------
 UNITS = np.load(os.path.join(GOLDEN, "units.npz"))
-FACE_NAMES = sorted({k[5:-9] for k in UNITS.files if k.startswith("face_") and k.endswith("_dist_base")})
+FACE_NAMES = sorted({k[len("face_"):-len("_dist_base")] for k in UNITS.files
+                     if k.startswith("face_") and k.endswith("_dist_base")})
 
 
 @pytest.mark.parametrize("name", FACE_NAMES)
@@ -154,7 +155,8 @@ def test_gpu_face_intersect_and_normal_match_reference(name):
         np.testing.assert_allclose(out[:, 3], UNITS[f"face_{name}_dist_z"], rtol=1e-9, atol=1e-15)
 
 
-MAT_NAMES = sorted({k[4:-6] for k in UNITS.files if k.startswith("mat_") and k.endswith("_nkids")})
+MAT_NAMES = sorted({k[len("mat_"):-len("_nkids")] for k in UNITS.files
+                    if k.startswith("mat_") and k.endswith("_nkids")})
 
 
 @pytest.mark.parametrize("name", MAT_NAMES)
