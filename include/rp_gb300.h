@@ -313,6 +313,34 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *scene, const void *in_records, uin
                        uint64_t *gen_offsets, int32_t max_gens, int32_t *n_gens,
                        rp_stats *stats);
 
+/* Allocation-free rp_trace_segment.  No counterpart in the reference: this is
+ * an addition of this library.  Same arguments, results and status codes as
+ * rp_trace_segment, for callers that must not allocate device memory during a
+ * trace: a process whose HBM is already claimed by another caching allocator
+ * (so a cudaMalloc would fail or force that allocator to give memory back),
+ * or a loop that cannot afford the device-wide synchronisation cudaFree
+ * implies while other streams run.  The call makes no cudaMalloc, cudaFree,
+ * host allocation or allocating library call: its scratch (child slots,
+ * per-tile and per-ray counts, counters) is one fixed device array of about
+ * 6.2 MB inside this library, sized for RP_NOALLOC_MAX_RAYS input rays.
+ *  - More than RP_NOALLOC_MAX_RAYS rays in `in`: RP_ERR_CAPACITY, nothing
+ *    launched, rp_last_error() says so.
+ *  - The first call on each device does a one-time set-up (it looks up the
+ *    scratch array's device address, which loads this library's device code
+ *    on that device): make that first call before any stream capture.
+ *  - The counters at the start of the scratch must be zero when the
+ *    generation kernel starts; the call clears them itself on its stream.
+ *    Every other scratch byte is written before it is read.
+ *  - There is one scratch array per device: calls on the same device must
+ *    not overlap (another host thread, or another context on that device).
+ *    Overlapping calls race on the scratch and corrupt each other's results.
+ * stats->kernel_ms and stats->device_ms both receive the generation kernel's
+ * time. */
+#define RP_NOALLOC_MAX_RAYS 16384
+int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *scene, rp_rays *in, rp_rays *out,
+                             float max_length, uint32_t flags, double e2_terminate,
+                             rp_stats *stats);
+
 /* ---- single-plugin calls (batches of independent inputs, host buffers) ---- */
 /* Face.intersect (ctracer.pyx:1769-1777): distance along p1->p2 (local
  * coordinates, 3 doubles per point) to face record `rec`, -1 for a miss. */

@@ -173,6 +173,8 @@ _SIGS = {
                                 ctypes.c_uint32, ctypes.c_double, _P, ctypes.c_uint64,
                                 ctypes.POINTER(ctypes.c_uint64), ctypes.c_int32,
                                 ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(Stats)]),
+    "rp_trace_segment_noalloc": (_I, [_P, _P, _P, _P, ctypes.c_float, ctypes.c_uint32, ctypes.c_double,
+                                      ctypes.POINTER(Stats)]),
     "rp_face_intersect": (_I, [_P, ctypes.c_int32, _P, _P, ctypes.c_uint64, _I, _P]),
     "rp_face_normal": (_I, [_P, ctypes.c_int32, _P, ctypes.c_uint64, _P]),
     "rp_shape_inside": (_I, [_P, ctypes.c_int32, _P, ctypes.c_uint64, _P]),

@@ -5,6 +5,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -806,6 +807,150 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_
     for (auto *g : gens)
         if (g) rp_rays_free(g);
     return rc;
+}
+
+// ---- allocation-free single generation -------------------------------------
+// rp_trace_segment_noalloc runs the same three kernels as rp_trace_segment
+// (generation, tile scan, placement) but takes every scratch byte from one
+// fixed device array, laid out for RP_NOALLOC_MAX_RAYS input rays:
+//   [0, 64)       counters: child total (u64 @0), error bits (u32 @8),
+//                 hits and terminated children (2 x u64 @24) -- zeroed per call
+//   tile_counts   u32 per 128-ray tile
+//   tile_offsets  u64 per tile
+//   ray_counts    u8 per ray
+//   child slots   2 per ray, structure of arrays (188 bytes per slot)
+#define NA_TILES (RP_NOALLOC_MAX_RAYS / RP_BLOCK)
+#define NA_SLOTS ((size_t)NA_TILES * RP_TILE_SLOTS)
+#define NA_OFF_TILE_COUNTS ((size_t)SCRATCH_HDR)
+#define NA_OFF_TILE_OFFSETS (NA_OFF_TILE_COUNTS + (((size_t)NA_TILES * 4 + 255) & ~(size_t)255))
+#define NA_OFF_RAY_COUNTS (NA_OFF_TILE_OFFSETS + (((size_t)NA_TILES * 8 + 255) & ~(size_t)255))
+#define NA_OFF_SLOTS ((NA_OFF_RAY_COUNTS + RP_NOALLOC_MAX_RAYS + 255) & ~(size_t)255)
+#define NA_SLOT_BYTES ((size_t)RP_RAY_BYTES * NA_SLOTS)
+#define NA_TOTAL (NA_OFF_SLOTS + NA_SLOT_BYTES)
+#define NA_MAX_DEVICES 64
+
+static_assert(RP_NOALLOC_MAX_RAYS % RP_BLOCK == 0, "the ray limit must be whole tiles");
+static_assert(NA_SLOTS % 64 == 0, "each SoA field of the slot arena must be a multiple of 256 bytes");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_TOTAL];
+
+static unsigned char *g_noalloc_base[NA_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+// One-time set-up per device, with that device current: the device address
+// of g_noalloc_scratch (resolving it loads this file's device code there).
+static int noalloc_scratch(int device, unsigned char **base) {
+    if (device < 0 || device >= NA_MAX_DEVICES) {
+        snprintf(g_last_error, sizeof g_last_error, "rp_trace_segment_noalloc: device %d beyond its table of %d",
+                 device, NA_MAX_DEVICES);
+        return RP_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_base[device]) {
+        if (soa_bytes(NA_SLOTS) != NA_SLOT_BYTES) {
+            snprintf(g_last_error, sizeof g_last_error, "rp_trace_segment_noalloc: slot arena layout mismatch");
+            return RP_ERR_INVALID;
+        }
+        void *p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        if (!p || ((uintptr_t)p & 255)) {
+            snprintf(g_last_error, sizeof g_last_error, "rp_trace_segment_noalloc: bad scratch address");
+            return RP_ERR_CUDA;
+        }
+        g_noalloc_base[device] = (unsigned char *)p;
+    }
+    *base = g_noalloc_base[device];
+    return RP_OK;
+}
+
+int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float max_length, uint32_t flags,
+                             double e2, rp_stats *st) {
+    if (!ctx || !s || !in || !out || in == out || s->ctx != ctx) return RP_ERR_INVALID;
+    if (in->n > RP_NOALLOC_MAX_RAYS) {
+        snprintf(g_last_error, sizeof g_last_error,
+                 "rp_trace_segment_noalloc: %llu input rays exceed its fixed limit of %d (use rp_trace_segment)",
+                 (unsigned long long)in->n, RP_NOALLOC_MAX_RAYS);
+        return RP_ERR_CAPACITY;
+    }
+    CK(cudaSetDevice(ctx->device));
+    unsigned char *sc = nullptr;
+    int rc = noalloc_scratch(ctx->device, &sc);
+    if (rc) return rc;
+    out->n = 0;
+    if (in->n == 0) return RP_OK;
+    const uint64_t n_tiles = (in->n + RP_BLOCK - 1) / RP_BLOCK;
+
+    rp_rays slots;  // a view of the slot arena; owns nothing
+    memset(&slots, 0, sizeof slots);
+    slots.block = sc + NA_OFF_SLOTS;
+    slots.cap = NA_SLOTS;
+    soa_carve(&slots);
+
+    GenArgs a;
+    memset(&a, 0, sizeof a);
+    a.in = in->soa;
+    a.out = in->soa;
+    a.n_in = in->n;
+    a.max_len = (double)max_length;
+    a.e2_term = e2;
+    a.emit = 1;
+    a.one_list = -1;
+    a.one_face = -1;
+    a.S = s->S;
+    a.smem_tables = s->smem_tables;
+    a.out_count = (unsigned long long *)(sc + 0);
+    a.err = (unsigned *)(sc + 8);
+    a.stats = (unsigned long long *)(sc + 24);
+    a.tile_counts = (unsigned *)(sc + NA_OFF_TILE_COUNTS);
+    a.tile_offsets = (unsigned long long *)(sc + NA_OFF_TILE_OFFSETS);
+    a.ray_counts = sc + NA_OFF_RAY_COUNTS;
+    a.scratch = slots.soa;
+    a.face_counts = s->face_counts;
+
+    CK(cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    cudaError_t e = (flags & RP_TRACE_MIXED) ? launch_generation_mixed(a, s->smem, ctx->stream)
+                                             : launch_generation_plain(a, s->smem, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "generation kernel launch");
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    e = launch_tile_scan(a, (unsigned)n_tiles, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "tile scan launch");
+    CK(cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+
+    const unsigned long long count = ctx->h_pinned[0];
+    const unsigned err = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
+    if (st) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        st->rays_in += in->n;
+        st->hits += ctx->h_pinned[3];
+        st->terminated += ctx->h_pinned[4];
+        st->kernel_ms += ms;
+        st->device_ms += ms;
+        st->launches += 3;
+        st->generations += 1;
+    }
+    if (err & ERR_WAVELENGTH) {
+        snprintf(g_last_error, sizeof g_last_error, "a ray's wavelength_idx is outside the wavelength table");
+        return RP_ERR_INVALID;
+    }
+    if (err & (ERR_ZK_STACK | ERR_SHAPE_STACK)) {
+        snprintf(g_last_error, sizeof g_last_error, "device evaluation limit hit (err=0x%x)", err);
+        return RP_ERR_INVALID;
+    }
+    if (count > out->cap) {
+        snprintf(g_last_error, sizeof g_last_error, "%llu children do not fit the output buffer", count);
+        return RP_ERR_CAPACITY;
+    }
+    a.out = out->soa;
+    a.out_cap = out->cap;
+    e = launch_place_children(a, (unsigned)n_tiles, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "child placement launch");
+    CK(cudaStreamSynchronize(ctx->stream));
+    out->n = count;
+    if (st) st->rays_out += count;
+    return RP_OK;
 }
 
 // internal accessors for rp_unit.cu (not part of the public header)
