@@ -321,7 +321,7 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *scene, const void *in_records, uin
  * or a loop that cannot afford the device-wide synchronisation cudaFree
  * implies while other streams run.  The call makes no cudaMalloc, cudaFree,
  * host allocation or allocating library call: its scratch (child slots,
- * per-tile and per-ray counts, counters) is one fixed device array of about
+ * per-tile counts and offsets, counters) is one fixed device array of about
  * 6.2 MB inside this library, sized for RP_NOALLOC_MAX_RAYS input rays.
  *  - More than RP_NOALLOC_MAX_RAYS rays in `in`: RP_ERR_CAPACITY, nothing
  *    launched, rp_last_error() says so.

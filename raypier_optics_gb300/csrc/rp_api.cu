@@ -559,11 +559,10 @@ int rp_rays_field(const rp_rays *r, const char *name, void **p) {
 // ---- tracing ------------------------------------------------------------------
 #define SCRATCH_HDR 64
 
-// Per-generation scratch: [out_count | err | pad | stats[2] | pad], the
-// per-tile child counts and offsets, then the per-ray child counts.
+// Per-generation scratch: [out_count | err | pad | stats[2] | pad], then the
+// per-tile child counts and offsets.
 static size_t scratch_bytes_for(uint64_t n_tiles) {
-    return SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)) + align256(n_tiles * sizeof(unsigned long long)) +
-           n_tiles * RP_BLOCK;
+    return SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)) + align256(n_tiles * sizeof(unsigned long long));
 }
 
 static int ensure_scratch(rp_ctx *ctx, uint64_t n_tiles) {
@@ -625,8 +624,6 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
     a.stats = (unsigned long long *)(sc + 24);
     a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
     a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)));
-    a.ray_counts = sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)) +
-                   align256(n_tiles * sizeof(unsigned long long));
     a.scratch = emit ? ctx->arena->soa : in->soa;
     a.face_counts = s->face_counts;
     if (ctx->gen_ev.empty()) {
@@ -817,14 +814,12 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_
 //                 hits and terminated children (2 x u64 @24) -- zeroed per call
 //   tile_counts   u32 per 128-ray tile
 //   tile_offsets  u64 per tile
-//   ray_counts    u8 per ray
 //   child slots   2 per ray, structure of arrays (188 bytes per slot)
 #define NA_TILES (RP_NOALLOC_MAX_RAYS / RP_BLOCK)
 #define NA_SLOTS ((size_t)NA_TILES * RP_TILE_SLOTS)
 #define NA_OFF_TILE_COUNTS ((size_t)SCRATCH_HDR)
 #define NA_OFF_TILE_OFFSETS (NA_OFF_TILE_COUNTS + (((size_t)NA_TILES * 4 + 255) & ~(size_t)255))
-#define NA_OFF_RAY_COUNTS (NA_OFF_TILE_OFFSETS + (((size_t)NA_TILES * 8 + 255) & ~(size_t)255))
-#define NA_OFF_SLOTS ((NA_OFF_RAY_COUNTS + RP_NOALLOC_MAX_RAYS + 255) & ~(size_t)255)
+#define NA_OFF_SLOTS ((NA_OFF_TILE_OFFSETS + (size_t)NA_TILES * 8 + 255) & ~(size_t)255)
 #define NA_SLOT_BYTES ((size_t)RP_RAY_BYTES * NA_SLOTS)
 #define NA_TOTAL (NA_OFF_SLOTS + NA_SLOT_BYTES)
 #define NA_MAX_DEVICES 64
@@ -903,7 +898,6 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     a.stats = (unsigned long long *)(sc + 24);
     a.tile_counts = (unsigned *)(sc + NA_OFF_TILE_COUNTS);
     a.tile_offsets = (unsigned long long *)(sc + NA_OFF_TILE_OFFSETS);
-    a.ray_counts = sc + NA_OFF_RAY_COUNTS;
     a.scratch = slots.soa;
     a.face_counts = s->face_counts;
 

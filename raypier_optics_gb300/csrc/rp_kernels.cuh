@@ -17,9 +17,11 @@ struct RaySoA {
     unsigned *wl, *parent, *endf, *ident, *type;
 };
 
-// The children of ray i of a generation are first written to slots 2i and
-// 2i + 1 of a scratch ray arena, with their number in ray_counts[i]; once every
-// tile's total is known (tile scan) the placement kernel moves them to their
+// A tile of RP_BLOCK rays owns RP_TILE_SLOTS consecutive slots of a scratch
+// ray arena (two per ray).  The generation kernel writes the tile's children
+// to the front of that range in parent order (block scan of the per-ray
+// counts) and their number to tile_counts[tile]; once every tile's total is
+// known (tile scan) the placement kernel copies each tile's children to their
 // final, contiguous place.  No ray or tile waits for another.
 #define RP_BLOCK 128
 #define RP_TILE_SLOTS (2 * RP_BLOCK)
@@ -34,8 +36,7 @@ struct GenArgs {
     int one_list, one_face;       // >= 0: sequential trace of one face of one list
     DevScene S;                   // global-memory tables
     int smem_tables;              // 1: lists/faces/materials staged in shared memory
-    RaySoA scratch;                 // child slots: 2 per ray
-    unsigned char *ray_counts;      // [n_in] children of each ray (0..2)
+    RaySoA scratch;                 // child slots: RP_TILE_SLOTS per tile
     unsigned *tile_counts;          // [n_tiles] children of each tile
     unsigned long long *tile_offsets;  // [n_tiles] exclusive prefix (scan kernel)
     unsigned long long *out_count;  // total children (scan kernel)

@@ -462,13 +462,12 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
 
 __global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ unsigned s_hits, s_term, s_children;
+    __shared__ unsigned s_hits, s_term;
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
     if (threadIdx.x == 0) {
         s_hits = 0;
         s_term = 0;
-        s_children = 0;
     }
     __syncthreads();
     const unsigned tile = blockIdx.x;
@@ -623,16 +622,19 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A) {
             }
         }
     }
+    // children go to the tile's slot range in parent order: the exclusive
+    // block scan of the per-ray counts is each ray's first slot
+    unsigned tile_children;
+    const unsigned excl = block_scan((unsigned)nc, &tile_children);
     if (nc > 0) {
         double phase = A.in.phase[i];
         unsigned wl = A.in.wl[i], ident = A.in.ident[i];
         unsigned endf = (unsigned)S.faces[best].idx;
-        for (int k = 0; k < nc; k++) store_child(A.scratch, 2 * i + k, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
-        atomicAdd(&s_children, (unsigned)nc);
+        const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
+        for (int k = 0; k < nc; k++) store_child(A.scratch, slot + k, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
     }
-    if (active) A.ray_counts[i] = (unsigned char)nc;
     flush_counts(A, S, s_counts);
-    if (threadIdx.x == 0) A.tile_counts[tile] = s_children;
+    if (threadIdx.x == 0) A.tile_counts[tile] = tile_children;
     if (threadIdx.x == 0) {
         atomicAdd(&A.stats[0], (unsigned long long)s_hits);
         if (s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);

@@ -122,13 +122,12 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
 
 __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ unsigned s_hits, s_term, s_children;
+    __shared__ unsigned s_hits, s_term;
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
     if (threadIdx.x == 0) {
         s_hits = 0;
         s_term = 0;
-        s_children = 0;
     }
     __syncthreads();
     const unsigned tile = blockIdx.x;
@@ -216,16 +215,19 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
         }
     }
 
+    // children go to the tile's slot range in parent order: the exclusive
+    // block scan of the per-ray counts is each ray's first slot
+    unsigned tile_children;
+    const unsigned excl = block_scan((unsigned)nc, &tile_children);
     if (nc > 0) {
         double phase = A.in.phase[i];
         unsigned wl = A.in.wl[i], ident = A.in.ident[i];
         unsigned endf = (unsigned)S.faces[best].idx;
-        for (int k = 0; k < nc; k++) store_child(A.scratch, 2 * i + k, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
-        atomicAdd(&s_children, (unsigned)nc);
+        const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
+        for (int k = 0; k < nc; k++) store_child(A.scratch, slot + k, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
     }
-    if (active) A.ray_counts[i] = (unsigned char)nc;
     flush_counts(A, S, s_counts);
-    if (threadIdx.x == 0) A.tile_counts[tile] = s_children;
+    if (threadIdx.x == 0) A.tile_counts[tile] = tile_children;
     if (threadIdx.x == 0) {
         atomicAdd(&A.stats[0], (unsigned long long)s_hits);
         if (s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
@@ -285,8 +287,9 @@ cudaError_t launch_tile_scan(const GenArgs &a, unsigned n_tiles, cudaStream_t st
     return cudaGetLastError();
 }
 
-// Moves each ray's children from its two scratch slots to their final place:
-// tile offset + the exclusive scan of the tile's per-ray counts.
+// Moves each tile's children from the front of its slot range to their final
+// place: one block per tile, a straight coalesced copy of tile_counts[tile]
+// records to tile_offsets[tile].
 __device__ __forceinline__ void copy_ray(const RaySoA &s, unsigned long long src, const RaySoA &o,
                                          unsigned long long dst) {
     o.ox[dst] = s.ox[src]; o.oy[dst] = s.oy[src]; o.oz[dst] = s.oz[src];
@@ -301,18 +304,14 @@ __device__ __forceinline__ void copy_ray(const RaySoA &s, unsigned long long src
 
 __global__ void __launch_bounds__(RP_BLOCK) place_children_kernel(GenArgs A) {
     const unsigned tile = blockIdx.x;
-    const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
-    unsigned c = i < A.n_in ? A.ray_counts[i] : 0u;
-    unsigned total;
-    unsigned excl = block_scan(c, &total);
-    unsigned long long base = A.tile_offsets[tile] + excl;
-    for (unsigned k = 0; k < c; k++) {
-        if (base + k >= A.out_cap) {
-            atomicOr(A.err, ERR_OVERFLOW);
-            return;
-        }
-        copy_ray(A.scratch, 2 * i + k, A.out, base + k);
+    const unsigned count = A.tile_counts[tile];
+    const unsigned long long base = A.tile_offsets[tile];
+    if (count > RP_TILE_SLOTS || base + count > A.out_cap) {
+        if (threadIdx.x == 0) atomicOr(A.err, ERR_OVERFLOW);
+        return;
     }
+    const unsigned long long src = (unsigned long long)tile * RP_TILE_SLOTS;
+    for (unsigned j = threadIdx.x; j < count; j += RP_BLOCK) copy_ray(A.scratch, src + j, A.out, base + j);
 }
 
 cudaError_t launch_place_children(const GenArgs &a, unsigned n_tiles, cudaStream_t st) {
