@@ -1,28 +1,145 @@
-// rp_mixed.cu -- mixed FP32/FP64 generation kernel.
+// rp_mixed.cu -- the mixed-precision generation kernel.
 //
-// Same generation structure as the plain kernel (rp_trace.cu): culled
-// nearest-first face search, orientation, material, per-ray child slots.  The
-// arithmetic is split by what needs 64-bit precision:
+// GB300 runs FP64 arithmetic, and every conversion instruction between double
+// and float, at about 1/64 of its FP32 rate, so this kernel keeps the FP64 pipe
+// almost idle and splits the work by what precision it needs:
 //
-//   FP64  ray origins and hit points; the distance along the ray to a face
-//         (planes: one FP64 division; spheres and conics: the quadratic root;
-//         aspheres and polynomial faces: FP32 Newton iterations followed by a
-//         final FP64 Newton step); the Euclidean length correction for a
-//         direction that is not exactly unit; accumulated optical path length.
-//   FP32  directions (stored as double), face normals, the S/P projection,
-//         Fresnel coefficients, polarisation amplitudes and E-vectors, the
-//         Snell direction update, aperture and shape tests.
+//   float-float (a pair of floats, about 48 significant bits)
+//         ray origins and hit points, the face-list-frame origin and direction,
+//         the ray parameter of a hit, Euclidean lengths and the optical path.
+//         A hit on a curved face is found in FP32 and then corrected by a
+//         Newton step whose residual is evaluated at the float-float ray point
+//         (relative to the face vertex, where FP32 resolves well below a
+//         nanometre), so roots reach float-float accuracy without FP64.
+//   FP32  directions of children, face normals, the S/P projection, Fresnel
+//         coefficients, polarisation amplitudes and E-vectors, Snell's law,
+//         aperture and shape tests, the asphere Newton iterations.
+//   integer pipe
+//         every conversion between the double-precision ray records and
+//         float / float-float (bit manipulation instead of F2F instructions).
+//   FP64  one addition per stored origin coordinate, length and optical path
+//         (float-float -> double); the faces and materials this kernel does not
+//         specialise (distortion, extended polynomial, polygons, elliptical
+//         plane; partial mirror, polarisers, waveplate, apertures) reuse the
+//         plain path's FP64 device functions.
 //
-// The TU is compiled with FMA contraction on.  Distortion faces and the rarer
-// materials reuse the FP64 device functions of the plain path.  Results agree
-// with the FP64 oracle to the accuracy reported in the precision test (nm in
-// position / OPL, rad in direction); index fields can differ for rays that
-// graze an aperture edge, which is why parity for this path is statistical.
+// The TU is compiled with FMA contraction on.  Index fields agree with the
+// FP64 oracle except for rays that graze an aperture edge or a face, which is
+// why parity for this path is statistical (see the precision report).
 #include "rp_gen_common.cuh"
 
 namespace rp {
 namespace mx {
 
+// ---- float-float arithmetic ------------------------------------------------
+// Error-free transforms: TwoSum (Knuth), Fast2Sum (Dekker), the FMA product.
+// The double-word operations follow Joldes, Muller & Popescu, "Tight and
+// rigorous error bounds for basic building blocks of double-word arithmetic",
+// ACM TOMS 44(2), 2017 (DWPlusDW, DWPlusFP, DWTimesDW, DWTimesFP).
+struct ff {
+    float hi, lo;
+};
+__device__ __forceinline__ ff ffm(float hi, float lo) {
+    ff r;
+    r.hi = hi;
+    r.lo = lo;
+    return r;
+}
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    return ffm(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+    float s = a + b;
+    return ffm(s, b - (s - a));
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+    float p = a * b;
+    return ffm(p, fmaf(a, b, -p));
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    ff s = two_sum(a.hi, b.hi), t = two_sum(a.lo, b.lo);
+    s.lo += t.hi;
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo += t.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ffm(-a.hi, -a.lo); }
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+    ff s = two_sum(a.hi, b);
+    s.lo += a.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    ff p = two_prod(a.hi, b.hi);
+    p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+    return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+    ff p = two_prod(a.hi, b);
+    p.lo = fmaf(a.lo, b, p.lo);
+    return fast_two_sum(p.hi, p.lo);
+}
+// a / b: FP32 quotient, float-float residual, one correction
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+    float q1 = __fdividef(a.hi, b.hi);
+    ff r = ff_sub(a, ff_mul_f(b, q1));
+    return fast_two_sum(q1, __fdividef(r.hi, b.hi));
+}
+__device__ __forceinline__ ff ff_sqrt(ff a) {
+    if (!(a.hi > 0.0f)) return ffm(sqrtf(a.hi), 0.0f);
+    float s = sqrtf(a.hi);
+    ff e = ff_sub(a, two_prod(s, s));
+    return fast_two_sum(s, e.hi * (0.5f / s));
+}
+__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool ff_eq(ff a, ff b) { return a.hi == b.hi && a.lo == b.lo; }
+
+// ---- conversions on the integer pipe ---------------------------------------
+// double -> float, round to nearest even; magnitudes below 2^-126 flush to a
+// signed zero, above the float range to infinity.
+__device__ __forceinline__ float f_of_d(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned s = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // exponent re-biased for float
+    unsigned r = ((unsigned)e << 23) + (((hi & 0xfffffu) << 3) | (lo >> 29));
+    const unsigned rest = lo & 0x1fffffffu;
+    r += (unsigned)(rest > 0x10000000u) | ((unsigned)(rest == 0x10000000u) & (r & 1u));
+    if (e <= 0) r = 0u;
+    else if (e >= 255) r = (((hi & 0x7ff00000u) == 0x7ff00000u) && (((hi & 0xfffffu) | lo) != 0u)) ? 0x7fc00000u : 0x7f800000u;
+    return __uint_as_float(s | r);
+}
+// float -> double, exact; float subnormals flush to a signed zero.
+__device__ __forceinline__ double d_of_f(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned s = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    unsigned hi = s | ((e + 896u) << 20) | (m >> 3), lo = m << 29;
+    if (e == 0u) {
+        hi = s;
+        lo = 0u;
+    } else if (e == 255u) {
+        hi = s | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u);
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+// double -> float-float: the top 24 significant bits and the remaining 29 bits
+// rounded to a float (about 48 bits in all), renormalised.  Magnitudes outside
+// [2^-74, 2^128) keep only the rounded float.
+__device__ __forceinline__ ff ff_of_d(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int E = (int)((hi >> 20) & 0x7ffu) - 1023;
+    if (E < -74 || E > 127) return ffm(f_of_d(x), 0.0f);
+    const unsigned s = hi & 0x80000000u;
+    const float h = __uint_as_float(s | ((unsigned)(E + 127) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+    float l = __uint2float_rn(lo & 0x1fffffffu) * __uint_as_float((unsigned)(E + 75) << 23);
+    return fast_two_sum(h, s ? -l : l);
+}
+// float-float -> double: hi + lo is exact in double (one FP64 addition)
+__device__ __forceinline__ double d_of_ff(ff a) { return d_of_f(a.hi) + d_of_f(a.lo); }
+
+// ---- FP32 vectors and complex numbers ----------------------------------------
 struct f3 {
     float x, y, z;
 };
@@ -35,15 +152,8 @@ __device__ __forceinline__ f3 cross3(f3 a, f3 b) {
     return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 __device__ __forceinline__ f3 norm3(f3 a) { return mul3(a, rsqrtf(dot3(a, a))); }
-__device__ __forceinline__ f3 tof(v3 a) { return mk3((float)a.x, (float)a.y, (float)a.z); }
-__device__ __forceinline__ v3 tod(f3 a) { return mkv(a.x, a.y, a.z); }
-__device__ __forceinline__ f3 rot3(const double *m, f3 p) {
-    return mk3(p.x * (float)m[0] + p.y * (float)m[1] + p.z * (float)m[2],
-               p.x * (float)m[3] + p.y * (float)m[4] + p.z * (float)m[5],
-               p.x * (float)m[6] + p.y * (float)m[7] + p.z * (float)m[8]);
-}
+__device__ __forceinline__ f3 f3_of_d(double x, double y, double z) { return mk3(f_of_d(x), f_of_d(y), f_of_d(z)); }
 
-// complex float
 typedef float2 cf;
 __device__ __forceinline__ cf cfm(float r, float i) { return make_float2(r, i); }
 __device__ __forceinline__ cf cadd(cf a, cf b) { return cfm(a.x + b.x, a.y + b.y); }
@@ -54,246 +164,422 @@ __device__ __forceinline__ cf cdiv(cf a, cf b) {
     float inv = 1.0f / (b.x * b.x + b.y * b.y);
     return cfm((a.x * b.x + a.y * b.y) * inv, (a.y * b.x - a.x * b.y) * inv);
 }
-__device__ __forceinline__ cf csqrtf_(cf z) {
+__device__ __forceinline__ cf csqrtf_(cf z) {  // Kahan's principal square root, as the FP64 path
     float x = z.x, y = z.y;
     if (x == 0.0f && y == 0.0f) return cfm(0.0f, y);
     float t = sqrtf((fabsf(x) + sqrtf(x * x + y * y)) * 0.5f);
-    if (x >= 0.0f) return cfm(t, y / (2.0f * t));
-    return cfm(fabsf(y) / (2.0f * t), copysignf(t, y));
+    float h = 0.5f / t;
+    if (x >= 0.0f) return cfm(t, y * h);
+    return cfm(fabsf(y) * h, copysignf(t, y));
 }
 __device__ __forceinline__ float cabs2(cf z) { return z.x * z.x + z.y * z.y; }
+__device__ __forceinline__ cf cf_of_d(double2 z) { return cfm(f_of_d(z.x), f_of_d(z.y)); }
 
-// 1/x in FP64 from an FP32 estimate and two Newton steps (relative error ~1e-16)
-__device__ __forceinline__ double drcp(double x) {
-    double r = (double)(1.0f / (float)x);
-    r = r * (2.0 - x * r);
-    r = r * (2.0 - x * r);
-    return r;
-}
-
-// Ray in a face list's frame: FP64 origin, FP32 unit direction, the same
-// direction as double, and the Euclidean-length factor |d| of the stored
-// direction (distances are Euclidean in the reference).
-struct LRay {
-    v3 p;      // local origin (FP64)
-    f3 df;     // local direction (FP32)
-    v3 dd;     // local direction (FP64 copy of df)
+// ---- per-block tables ----------------------------------------------------------
+// A face list's maps in the forms used here: global -> local as float-float
+// (rotation and translation) with a flag for an identity rotation, and the
+// local -> global rotation in FP32 for normals.
+struct MxList {
+    float ri_hi[9], ri_lo[9];
+    float ti_hi[3], ti_lo[3];
+    float r[9];
+    int ident;
+    int pad[2];
+};
+// A face's parameters in FP32, its plane / vertex height as float-float and its
+// smallest accepted ray parameter (tolerance * max_length, the reference's
+// h < tolerance test with h = t / max_length).
+struct MxFace {
+    float p[RP_FACE_NPARAM];
+    float zv_hi, zv_lo;
+    float tmin;
+    float tol;  // Face.tolerance (a distance) in FP32
 };
 
-#define MX_MISS (-1.0)
-
-__device__ __forceinline__ double plane_t(double z, const LRay &R) {
-    // t with p.z + t d.z = z; FP64 numerator, FP64-refined reciprocal
-    if (R.dd.z == 0.0) return MX_MISS;
-    return (z - R.p.z) * drcp(R.dd.z);
+__host__ __device__ __forceinline__ size_t mx_tables_bytes(int n_lists, int n_faces) {
+    return (size_t)n_lists * sizeof(MxList) + (size_t)n_faces * sizeof(MxFace);
 }
 
-__device__ __forceinline__ int shape_in(const DevScene &S, int prog, float x, float y, unsigned *err) {
-    return shape_inside(S, prog, (double)x, (double)y, err);
+// Index of the parameter that holds the plane height / vertex z of each face type.
+__device__ __forceinline__ int vertex_param(int type) {
+    switch (type) {
+        case RP_FACE_CIRCULAR: return 2;
+        case RP_FACE_RECTANGULAR: return 3;
+        case RP_FACE_SHAPED_PLANAR: return 0;
+        case RP_FACE_SPHERICAL: return 2;
+        case RP_FACE_SHAPED_SPHERICAL: return 1;
+        case RP_FACE_CONIC: return 1;
+        case RP_FACE_ASPHERIC: return 1;
+        default: return -1;
+    }
 }
 
-// Sphere / conic: roots of a t^2 + b t + c = 0 in FP64 (the quadratic that
-// loses precision to cancellation at large radius and grazing incidence).
-__device__ __forceinline__ bool quad_roots(double a, double b, double c, double &t1, double &t2) {
-    double disc = b * b - 4.0 * a * c;
-    if (disc < 0.0) return false;
-    double sd = sqrt(disc);
-    double inv2a = 0.5 * drcp(a);
-    t1 = (-b + sd) * inv2a;
-    t2 = (-b - sd) * inv2a;
-    return true;
-}
-
-__device__ double face_t_mixed(const DevScene &S, const rp_face &f, const LRay &R, double tmax, unsigned *err) {
-    // Returns the ray parameter of a valid hit (hit = p + t d), or MX_MISS.
-    const double tol_t = f.tolerance;  // faces compare their tolerance to the fraction h = t / tmax
-    switch (f.type) {
-        case RP_FACE_CIRCULAR: {
-            double t = plane_t(f.p[2], R);
-            if (t < tol_t * tmax || t > tmax) return MX_MISS;
-            float X = (float)(R.p.x + t * R.dd.x - f.p[1]), Y = (float)(R.p.y + t * R.dd.y);
-            float dd = (float)f.p[0];
-            if (X * X + Y * Y > dd * dd * 0.25f) return MX_MISS;
-            return t;
+// Fills the tables from the FP64 tables in global memory (the shared copies of
+// those are not complete until the caller's next barrier).
+__device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace *mf, float max_len) {
+    for (int l = threadIdx.x; l < A.S.n_lists; l += blockDim.x) {
+        const rp_facelist &L = A.S.lists[l];
+        MxList &o = ml[l];
+        for (int k = 0; k < 9; k++) {
+            ff v = ff_of_d(L.inv_trans.m[k]);
+            o.ri_hi[k] = v.hi;
+            o.ri_lo[k] = v.lo;
+            o.r[k] = f_of_d(L.trans.m[k]);
         }
-        case RP_FACE_RECTANGULAR: {
-            double t = plane_t(f.p[3], R);
-            if (t < tol_t * tmax || t > tmax) return MX_MISS;
-            float X = (float)(R.p.x + t * R.dd.x - f.p[2]), Y = (float)(R.p.y + t * R.dd.y);
-            if (X * X > (float)(f.p[0] * f.p[0] / 4)) return MX_MISS;
-            if (Y * Y > (float)(f.p[1] * f.p[1] / 4)) return MX_MISS;
-            return t;
+        for (int k = 0; k < 3; k++) {
+            ff v = ff_of_d(L.inv_trans.t[k]);
+            o.ti_hi[k] = v.hi;
+            o.ti_lo[k] = v.lo;
         }
+        const double *m = L.inv_trans.m;
+        o.ident = (m[0] == 1.0 && m[4] == 1.0 && m[8] == 1.0 && m[1] == 0.0 && m[2] == 0.0 && m[3] == 0.0 &&
+                   m[5] == 0.0 && m[6] == 0.0 && m[7] == 0.0);
+    }
+    for (int f = threadIdx.x; f < A.S.n_faces; f += blockDim.x) {
+        const rp_face &F = A.S.faces[f];
+        MxFace &o = mf[f];
+        for (int k = 0; k < RP_FACE_NPARAM; k++) o.p[k] = f_of_d(F.p[k]);
+        int vp = vertex_param(F.type);
+        ff z = vp >= 0 ? ff_of_d(F.p[vp]) : ffm(0.0f, 0.0f);
+        o.zv_hi = z.hi;
+        o.zv_lo = z.lo;
+        o.tmin = f_of_d(F.tolerance) * max_len;
+        o.tol = f_of_d(F.tolerance);
+    }
+}
+
+// ---- rays in a face list's frame ---------------------------------------------
+struct LRay {
+    ff px, py, pz;  // origin
+    ff dx, dy, dz;  // direction (the world direction rotated; not renormalised)
+};
+
+__device__ __forceinline__ ff ff_of(const float *hi, const float *lo, int k) { return ffm(hi[k], lo[k]); }
+
+// v' = R v (+ t), float-float
+__device__ __forceinline__ void ff_rotate(const MxList &L, const ff v[3], ff out[3], bool translate) {
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        ff acc = ff_mul(ff_of(L.ri_hi, L.ri_lo, 3 * r), v[0]);
+        acc = ff_add(acc, ff_mul(ff_of(L.ri_hi, L.ri_lo, 3 * r + 1), v[1]));
+        acc = ff_add(acc, ff_mul(ff_of(L.ri_hi, L.ri_lo, 3 * r + 2), v[2]));
+        if (translate) acc = ff_add(acc, ff_of(L.ti_hi, L.ti_lo, r));
+        out[r] = acc;
+    }
+}
+
+__device__ __forceinline__ LRay local_ray(const MxList &L, const ff O[3], const ff D[3]) {
+    LRay R;
+    if (L.ident) {
+        R.px = ff_add(O[0], ff_of(L.ti_hi, L.ti_lo, 0));
+        R.py = ff_add(O[1], ff_of(L.ti_hi, L.ti_lo, 1));
+        R.pz = ff_add(O[2], ff_of(L.ti_hi, L.ti_lo, 2));
+        R.dx = D[0];
+        R.dy = D[1];
+        R.dz = D[2];
+    } else {
+        ff p[3], d[3];
+        ff_rotate(L, O, p, true);
+        ff_rotate(L, D, d, false);
+        R.px = p[0];
+        R.py = p[1];
+        R.pz = p[2];
+        R.dx = d[0];
+        R.dy = d[1];
+        R.dz = d[2];
+    }
+    return R;
+}
+
+// ---- shapes in FP32 (cshapes.pyx) ----------------------------------------------
+// The postfix program of rp_shape_op with the operand stack kept as bits.
+__device__ int shape_in_f(const DevScene &S, int prog, float x, float y, unsigned *err) {
+    if (prog < 0) return 1;
+    unsigned bits = 0u;
+    int sp = 0;
+    for (int k = prog; k < S.n_shapes; k++) {
+        const rp_shape_op &op = S.shapes[k];
+        unsigned v;
+        switch (op.op) {
+            case RP_SHAPE_END: return sp > 0 ? (int)(bits & 1u) : 1;
+            case RP_SHAPE_TRUE: v = 1u; break;
+            case RP_SHAPE_CIRCLE: {
+                float dx = x - f_of_d(op.a), dy = y - f_of_d(op.b), c = f_of_d(op.c);
+                v = (dx * dx + dy * dy < c * c) ? 1u : 0u;
+                break;
+            }
+            case RP_SHAPE_RECT: {
+                float dx = x - f_of_d(op.a), dy = y - f_of_d(op.b);
+                v = ((2.0f * fabsf(dx) < f_of_d(op.c)) && (2.0f * fabsf(dy) < f_of_d(op.d))) ? 1u : 0u;
+                break;
+            }
+            case RP_SHAPE_POLYGON: v = (unsigned)poly_shape_inside(S.aux + op.aux, op.n, d_of_f(x), d_of_f(y)); break;
+            case RP_SHAPE_AND:
+            case RP_SHAPE_OR:
+            case RP_SHAPE_XOR: {
+                if (sp < 2) goto bad;
+                unsigned b = bits & 1u, a = (bits >> 1) & 1u;
+                bits >>= 2;
+                sp -= 2;
+                v = op.op == RP_SHAPE_AND ? (a & b) : op.op == RP_SHAPE_OR ? (a | b) : (a ^ b);
+                break;
+            }
+            case RP_SHAPE_NOT: {
+                if (sp < 1) goto bad;
+                v = (~bits) & 1u;
+                bits >>= 1;
+                sp -= 1;
+                break;
+            }
+            default: goto bad;
+        }
+        bits = (bits << 1) | v;
+        if (++sp >= 31) goto bad;
+    }
+    return sp > 0 ? (int)(bits & 1u) : 1;
+bad:
+    atomicOr(err, ERR_SHAPE_STACK);
+    return 0;
+}
+
+// ---- face intersections --------------------------------------------------------
+#define MX_MISS_T (-1.0f)
+__device__ __forceinline__ ff miss_t() { return ffm(MX_MISS_T, 0.0f); }
+
+// U = P + t Dl relative to the face vertex, rounded to FP32 (the coordinates
+// are of the order of the aperture, so FP32 resolves them to well below 1 nm).
+__device__ __forceinline__ f3 vertex_point(const LRay &R, ff zv, ff t) {
+    ff ux = ff_add(R.px, ff_mul(t, R.dx));
+    ff uy = ff_add(R.py, ff_mul(t, R.dy));
+    ff uz = ff_sub(ff_add(R.pz, ff_mul(t, R.dz)), zv);
+    return mk3(ux.hi + ux.lo, uy.hi + uy.lo, uz.hi + uz.lo);
+}
+
+// Newton correction of a quadric root: F = beta z^2 - 2 Rq z + x^2 + y^2 in
+// vertex coordinates (a sphere is beta = 1, Rq = -curvature).
+__device__ __forceinline__ ff refine_quadric(const LRay &R, ff zv, float t0, float beta, float Rq) {
+    ff t = ffm(t0, 0.0f);
+    const float dx = R.dx.hi, dy = R.dy.hi, dz = R.dz.hi;
+#pragma unroll 1
+    for (int it = 0; it < 2; it++) {
+        f3 u = vertex_point(R, zv, t);
+        float F = fmaf(beta * u.z - 2.0f * Rq, u.z, fmaf(u.x, u.x, u.y * u.y));
+        float G = 2.0f * ((beta * u.z - Rq) * dz + u.x * dx + u.y * dy);
+        float step = -F / G;
+        if (!isfinite(step)) break;
+        t = ff_add_f(t, step);
+        if (fabsf(step) <= 1e-7f * (1.0f + fabsf(t.hi))) break;
+    }
+    return t;
+}
+
+// Asphere sag residual f = sag(r^2) - z and its derivative along the ray, FP32.
+__device__ __forceinline__ void asph_fg(const MxFace &M, float Rq, float beta, f3 u, float dx, float dy, float dz,
+                                        float &fv, float &g) {
+    const float R2 = Rq * Rq;
+    const float A4 = M.p[3], A6 = M.p[4], A8 = M.p[5], A10 = M.p[6], A12 = M.p[7], A14 = M.p[8], A16 = M.p[9];
+    float r2 = u.x * u.x + u.y * u.y;
+    float root = sqrtf(1.0f - beta * r2 / R2);
+    float poly = r2 * r2 * (A4 + r2 * (A6 + r2 * (A8 + r2 * (A10 + r2 * (A12 + r2 * (A14 + r2 * A16))))));
+    float inv = 1.0f / (Rq * (1.0f + root));
+    fv = r2 * inv - u.z + poly;
+    float dr2 = 2.0f * (dx * u.x + dy * u.y);
+    float dsag = inv + beta * r2 * inv * inv / (2.0f * Rq * root);
+    float dpoly = r2 * (2.0f * A4 + r2 * (3.0f * A6 + r2 * (4.0f * A8 + r2 * (5.0f * A10 +
+                  r2 * (6.0f * A12 + r2 * (7.0f * A14 + r2 * 8.0f * A16))))));
+    g = (dsag + dpoly) * dr2 - dz;
+}
+
+// Ray parameter of the hit of face F (hit = P + t Dl), miss_t() for a miss;
+// `fb` is set for face types left to the FP64 path.
+__device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R, float tmax, unsigned *err,
+                     bool &fb) {
+    fb = false;
+    const ff zv = ffm(M.zv_hi, M.zv_lo);
+    switch (F.type) {
+        case RP_FACE_CIRCULAR:
+        case RP_FACE_RECTANGULAR:
         case RP_FACE_SHAPED_PLANAR: {
-            double t = plane_t(f.p[0], R);
-            if (t < tol_t * tmax || t > tmax) return MX_MISS;
-            float X = (float)(R.p.x + t * R.dd.x), Y = (float)(R.p.y + t * R.dd.y);
-            if (!shape_in(S, f.shape, X, Y, err)) return MX_MISS;
+            // cfaces.pyx:147-175, 364-396, 201-227: plane z = zv
+            ff t = ff_div(ff_sub(zv, R.pz), R.dz);
+            if (!(t.hi >= M.tmin) || t.hi > tmax) return miss_t();
+            float X = fmaf(t.hi, R.dx.hi, R.px.hi), Y = fmaf(t.hi, R.dy.hi, R.py.hi);
+            if (F.type == RP_FACE_CIRCULAR) {
+                X -= M.p[1];
+                if (X * X + Y * Y > M.p[0] * M.p[0] * 0.25f) return miss_t();
+            } else if (F.type == RP_FACE_RECTANGULAR) {
+                X -= M.p[2];
+                if (X * X > M.p[0] * M.p[0] * 0.25f) return miss_t();
+                if (Y * Y > M.p[1] * M.p[1] * 0.25f) return miss_t();
+            } else if (!shape_in_f(S, F.shape, X, Y, err)) {
+                return miss_t();
+            }
             return t;
         }
         case RP_FACE_SPHERICAL:
         case RP_FACE_SHAPED_SPHERICAL: {
-            bool plain = f.type == RP_FACE_SPHERICAL;
-            double c = plain ? f.p[1] : f.p[0], zh = plain ? f.p[2] : f.p[1];
-            double cz = zh - c;
-            v3 q = mkv(R.p.x, R.p.y, R.p.z - cz);
-            double a = dotv(R.dd, R.dd), b = 2.0 * dotv(R.dd, q), cc = dotv(q, q) - c * c;
-            double t1, t2;
-            if (!quad_roots(a, b, cc, t1, t2)) return MX_MISS;
-            const double INF = inf_d();
-            float z1 = (float)(q.z + t1 * R.dd.z), z2 = (float)(q.z + t2 * R.dd.z);
-            if (c >= 0) {
-                if (z1 < 0.0f) t1 = INF;
-                if (z2 < 0.0f) t2 = INF;
+            // cfaces.pyx:418-482, 512-592, in vertex coordinates: centre at z = -c
+            const bool plain = F.type == RP_FACE_SPHERICAL;
+            const float c = plain ? M.p[1] : M.p[0];
+            const float px = R.px.hi, py = R.py.hi;
+            const ff pzr = ff_sub(R.pz, zv);
+            const float pz = pzr.hi;
+            const float dx = R.dx.hi, dy = R.dy.hi, dz = R.dz.hi;
+            float a = dx * dx + dy * dy + dz * dz;
+            float b = 2.0f * (dx * px + dy * py + dz * (pz + c));
+            float cc = px * px + py * py + pz * (pz + 2.0f * c);
+            float disc = b * b - 4.0f * a * cc;
+            if (disc < 0.0f) return miss_t();
+            float q = -0.5f * (b + copysignf(sqrtf(disc), b));
+            float t1 = q / a, t2 = (q != 0.0f) ? cc / q : t1;
+            const float INF = __int_as_float(0x7f800000);
+            float zc1 = pz + c + t1 * dz, zc2 = pz + c + t2 * dz;  // z relative to the centre
+            if (c >= 0.0f) {
+                if (zc1 < 0.0f) t1 = INF;
+                if (zc2 < 0.0f) t2 = INF;
             } else {
-                if (z1 > 0.0f) t1 = INF;
-                if (z2 > 0.0f) t2 = INF;
+                if (zc1 > 0.0f) t1 = INF;
+                if (zc2 > 0.0f) t2 = INF;
             }
-            float x1 = (float)(R.p.x + t1 * R.dd.x), y1 = (float)(R.p.y + t1 * R.dd.y);
-            float x2 = (float)(R.p.x + t2 * R.dd.x), y2 = (float)(R.p.y + t2 * R.dd.y);
+            float x1 = px + t1 * dx, y1 = py + t1 * dy, x2 = px + t2 * dx, y2 = py + t2 * dy;
             if (plain) {
-                float DD = (float)(f.p[0] * f.p[0] / 4.0);
+                float DD = M.p[0] * M.p[0] * 0.25f;
                 if (x1 * x1 + y1 * y1 > DD) t1 = INF;
                 if (x2 * x2 + y2 * y2 > DD) t2 = INF;
             } else {
-                if (!shape_in(S, f.shape, x1, y1, err)) t1 = INF;
-                if (!shape_in(S, f.shape, x2, y2, err)) t2 = INF;
+                if (t1 != INF && !shape_in_f(S, F.shape, x1, y1, err)) t1 = INF;
+                if (t2 != INF && !shape_in_f(S, F.shape, x2, y2, err)) t2 = INF;
             }
-            if (t2 < t1) t1 = t2;
-            if (t1 > tmax || t1 < tol_t * tmax) return MX_MISS;
-            return t1;
+            float t = fminf(t1, t2);
+            if (!(t <= tmax) || !(t >= M.tmin)) return miss_t();
+            ff tt = refine_quadric(R, zv, t, 1.0f, -c);
+            if (!(tt.hi <= tmax) || !(tt.hi >= M.tmin)) return miss_t();
+            return tt;
         }
-        case RP_FACE_CONIC: {
-            // beta z^2 - 2 R z + r^2 = 0 along the ray (cfaces.pyx:1695-1747)
-            double Rr = -f.p[0], beta = 1 + f.p[2];
-            v3 a = mkv(R.p.x, R.p.y, R.p.z - f.p[1]);
-            v3 d = R.dd;
-            double A = beta * beta * d.z * d.z + beta * (d.x * d.x + d.y * d.y);
-            double B = -2 * Rr * beta * d.z + 2 * beta * (a.x * d.x + a.y * d.y) + 2 * a.z * beta * beta * d.z;
-            double C = -2 * Rr * a.z * beta + beta * (a.x * a.x + a.y * a.y) + a.z * a.z * beta * beta;
-            double disc = B * B - 4 * A * C;
-            if (disc < 0) return MX_MISS;
-            double sd = sqrt(disc), inv2a = 0.5 * drcp(A);
-            double t = (Rr * beta * d.z <= 0) ? (-B + sd) * inv2a : (-B - sd) * inv2a;
-            float X = (float)(a.x + t * d.x), Y = (float)(a.y + t * d.y);
-            if (!shape_in(S, f.shape, X, Y, err)) return MX_MISS;
-            if (t > tmax || t < tol_t * tmax) return MX_MISS;
-            return t;
-        }
+        case RP_FACE_CONIC:
         case RP_FACE_ASPHERIC: {
-            // conic start, FP32 Newton on the sag residual, one FP64 step last
-            double Rr = -f.p[0], beta = 1 + f.p[2];
-            v3 a = mkv(R.p.x, R.p.y, R.p.z - f.p[1]);
-            v3 d = R.dd;
-            double A = beta * beta * d.z * d.z + beta * (d.x * d.x + d.y * d.y);
-            double B = -2 * Rr * beta * d.z + 2 * beta * (a.x * d.x + a.y * d.y) + 2 * a.z * beta * beta * d.z;
-            double C = -2 * Rr * a.z * beta + beta * (a.x * a.x + a.y * a.y) + a.z * a.z * beta * beta;
-            double disc = B * B - 4 * A * C;
-            double t = MX_MISS;
-            if (disc >= 0) {
-                double sd = sqrt(disc), inv2a = 0.5 * drcp(A);
-                t = (Rr * beta * d.z <= 0) ? (-B + sd) * inv2a : (-B - sd) * inv2a;
+            // intersect_conic (cfaces.pyx:1695-1747) in vertex coordinates, the
+            // reference's choice of root by the sign of R beta d_z
+            const float Rq = -M.p[0], beta = 1.0f + M.p[2];
+            const float px = R.px.hi, py = R.py.hi;
+            const float pz = ff_sub(R.pz, zv).hi;
+            const float dx = R.dx.hi, dy = R.dy.hi, dz = R.dz.hi;
+            const float b2 = beta * beta;
+            float A = b2 * dz * dz + beta * (dx * dx + dy * dy);
+            float B = -2.0f * Rq * beta * dz + 2.0f * beta * (px * dx + py * dy) + 2.0f * pz * b2 * dz;
+            float C = -2.0f * Rq * pz * beta + beta * (px * px + py * py) + pz * pz * b2;
+            float disc = B * B - 4.0f * A * C;
+            float t;
+            if (disc < 0.0f) {
+                t = -tmax;  // intersect_conic's -1 (a fraction of the segment): the asphere starts from there
+            } else {
+                float sd = sqrtf(disc);
+                bool plus = Rq * beta * dz <= 0.0f;
+                if (A == 0.0f) t = plus ? (-B + sd) / (2.0f * A) : (-B - sd) / (2.0f * A);
+                else if (plus) t = (B > 0.0f) ? (2.0f * C) / (-B - sd) : (-B + sd) / (2.0f * A);
+                else t = (B < 0.0f) ? (2.0f * C) / (-B + sd) : (-B - sd) / (2.0f * A);
             }
-            const float Rf = (float)Rr, bf = (float)beta, R2f = Rf * Rf;
-            const float A4 = (float)f.p[3], A6 = (float)f.p[4], A8 = (float)f.p[5], A10 = (float)f.p[6],
-                        A12 = (float)f.p[7], A14 = (float)f.p[8], A16 = (float)f.p[9];
-            // residual f(t) = sag(r(t)) - z(t) and df/dt in FP32, relative to the start t0
-            float ax = (float)a.x, ay = (float)a.y, az = (float)a.z;
-            float dx = R.df.x, dy = R.df.y, dz = R.df.z;
-            float tf = (float)t;
-            float f_last = 0.0f;
-            bool conv = false;
-            for (int it = 0; it < 100; it++) {
-                float ux = ax + tf * dx, uy = ay + tf * dy;
-                float r2 = ux * ux + uy * uy;
-                float root = sqrtf(1.0f - bf * r2 / R2f);
-                float poly = r2 * r2 * (A4 + r2 * (A6 + r2 * (A8 + r2 * (A10 + r2 * (A12 + r2 * (A14 + r2 * A16))))));
-                float fv = r2 / (Rf * (1.0f + root)) - (az + tf * dz) + poly;
-                if (it > 0 && fabsf(fv) > fabsf(f_last) && fabsf(fv) > 1e-6f * (1.0f + fabsf(az))) return MX_MISS;
-                f_last = fv;
-                float dr2 = 2.0f * (dx * ux + dy * uy);
-                float dsag = 1.0f / (Rf * (1.0f + root)) + bf * r2 / (2.0f * Rf * R2f * root * (1.0f + root) * (1.0f + root));
-                float dpoly = r2 * (2.0f * A4 + r2 * (3.0f * A6 + r2 * (4.0f * A8 + r2 * (5.0f * A10 +
-                              r2 * (6.0f * A12 + r2 * (7.0f * A14 + r2 * 8.0f * A16))))));
-                float g = (dsag + dpoly) * dr2 - dz;
-                float step = -fv / g;
-                tf += step;
-                if (!(fabsf(step) <= 1e-5f * (1.0f + fabsf(tf)))) continue;
-                conv = true;
-                break;
+            ff tt;
+            if (F.type == RP_FACE_CONIC) {
+                if (!(t <= tmax) || !(t >= M.tmin)) return miss_t();  // D < 0 gives -1: a miss
+                tt = refine_quadric(R, zv, t, beta, Rq);
+            } else {
+                // asphere: Newton on the sag residual in FP32 from the conic root
+                // (cfaces.pyx:1908-1974), then corrections at float-float points
+                float tf = t, f_last = 0.0f;
+                bool conv = false;
+                const f3 p0 = mk3(px, py, pz);
+                for (int it = 0; it < 100; it++) {
+                    f3 u = add3(p0, mul3(mk3(dx, dy, dz), tf));
+                    float fv, g;
+                    asph_fg(M, Rq, beta, u, dx, dy, dz, fv, g);
+                    if (it > 0 && fabsf(fv) > fabsf(f_last) && fabsf(fv) > 1e-6f * (1.0f + fabsf(u.z))) return miss_t();
+                    f_last = fv;
+                    float step = -fv / g;
+                    tf += step;
+                    if (fabsf(step) <= 1e-5f * (1.0f + fabsf(tf))) {
+                        conv = true;
+                        break;
+                    }
+                }
+                if (!conv || !isfinite(tf)) return miss_t();
+                tt = ffm(tf, 0.0f);
+#pragma unroll 1
+                for (int it = 0; it < 2; it++) {
+                    f3 u = vertex_point(R, zv, tt);
+                    float fv, g;
+                    asph_fg(M, Rq, beta, u, dx, dy, dz, fv, g);
+                    float step = -fv / g;
+                    if (!isfinite(step)) break;
+                    tt = ff_add_f(tt, step);
+                    if (fabsf(step) <= 1e-7f * (1.0f + fabsf(tt.hi))) break;
+                }
             }
-            if (!conv || !isfinite(tf)) return MX_MISS;
-            // last Newton step in FP64
-            double td = (double)tf;
-            {
-                double ux = a.x + td * d.x, uy = a.y + td * d.y;
-                double r2 = ux * ux + uy * uy;
-                double root = sqrt(1.0 - beta * r2 / (Rr * Rr));
-                double poly = r2 * r2 * (f.p[3] + r2 * (f.p[4] + r2 * (f.p[5] + r2 * (f.p[6] +
-                              r2 * (f.p[7] + r2 * (f.p[8] + r2 * f.p[9]))))));
-                double fv = r2 / (Rr * (1.0 + root)) - (a.z + td * d.z) + poly;
-                double dr2 = 2.0 * (d.x * ux + d.y * uy);
-                double dsag = 1.0 / (Rr * (1.0 + root)) +
-                              beta * r2 / (2.0 * Rr * Rr * Rr * root * (1.0 + root) * (1.0 + root));
-                double dpoly = r2 * (2.0 * f.p[3] + r2 * (3.0 * f.p[4] + r2 * (4.0 * f.p[5] + r2 * (5.0 * f.p[6] +
-                               r2 * (6.0 * f.p[7] + r2 * (7.0 * f.p[8] + r2 * 8.0 * f.p[9]))))));
-                double g = (dsag + dpoly) * dr2 - d.z;
-                td = td - fv / g;
-            }
-            if (!isfinite(td)) return MX_MISS;
-            float X = (float)(a.x + td * d.x), Y = (float)(a.y + td * d.y);
-            if (!shape_in(S, f.shape, X, Y, err)) return MX_MISS;
-            if (td > tmax || td < tol_t * tmax) return MX_MISS;
-            return td;
+            f3 u = vertex_point(R, zv, tt);
+            if (!shape_in_f(S, F.shape, u.x, u.y, err)) return miss_t();
+            if (!(tt.hi <= tmax) || !(tt.hi >= M.tmin)) return miss_t();
+            return tt;
         }
-        default:
-            return MX_MISS - 1.0;  // not handled here: use the FP64 path
+        default: fb = true; return miss_t();
     }
 }
 
-// FP32 face normals (local frame) from an FP64 local hit point.
-__device__ f3 face_normal_mixed(const DevScene &S, const rp_face &f, v3 p, unsigned *err, bool &handled) {
-    handled = true;
-    switch (f.type) {
-        case RP_FACE_CIRCULAR: return mk3(0, 0, f.invert_normals ? 1.0f : -1.0f);
-        case RP_FACE_SHAPED_PLANAR: return mk3(0, 0, 1);
-        case RP_FACE_RECTANGULAR: return mk3(0, 0, -1);
+// FP32 normal of a specialised face at a point in vertex coordinates; false
+// for faces left to the FP64 path.
+__device__ __forceinline__ bool face_normal_f(const rp_face &F, const MxFace &M, f3 u, f3 &n) {
+    switch (F.type) {
+        case RP_FACE_CIRCULAR: n = mk3(0.0f, 0.0f, F.invert_normals ? 1.0f : -1.0f); return true;
+        case RP_FACE_SHAPED_PLANAR: n = mk3(0.0f, 0.0f, 1.0f); return true;
+        case RP_FACE_RECTANGULAR: n = mk3(0.0f, 0.0f, -1.0f); return true;
         case RP_FACE_SPHERICAL:
-        case RP_FACE_SHAPED_SPHERICAL: {
-            bool plain = f.type == RP_FACE_SPHERICAL;
-            double c = plain ? f.p[1] : f.p[0], zh = plain ? f.p[2] : f.p[1];
-            f3 q = mk3((float)p.x, (float)p.y, (float)(p.z - (zh - c)));
-            if (c < 0) q = mk3(-q.x, -q.y, -q.z);
-            return norm3(q);
+        case RP_FACE_SHAPED_SPHERICAL: {  // cfaces.pyx:485-498, 594-606
+            float c = F.type == RP_FACE_SPHERICAL ? M.p[1] : M.p[0];
+            f3 q = mk3(u.x, u.y, u.z + c);
+            if (c < 0.0f) q = mk3(-q.x, -q.y, -q.z);
+            n = norm3(q);
+            return true;
         }
-        case RP_FACE_CONIC: {
-            float Rr = (float)(-f.p[0]), beta = (float)(1 + f.p[2]);
-            float sign = f.invert_normals ? -1.0f : 1.0f;
-            float pz = (float)(p.z - f.p[1]);
-            f3 g = mk3(-(float)p.x * 2 * beta, -(float)p.y * 2 * beta, 2 * beta * (Rr - beta * pz));
-            if (Rr * beta < 0) sign = -sign;
-            return norm3(mul3(g, sign));
+        case RP_FACE_CONIC: {  // cfaces.pyx:1796-1820
+            float Rq = -M.p[0], beta = 1.0f + M.p[2];
+            float sign = F.invert_normals ? -1.0f : 1.0f;
+            if (Rq * beta < 0.0f) sign = -sign;
+            f3 g = mk3(-u.x * 2.0f * beta, -u.y * 2.0f * beta, 2.0f * beta * (Rq - beta * u.z));
+            n = norm3(mul3(g, sign));
+            return true;
         }
-        case RP_FACE_ASPHERIC: {
-            float Rr = (float)(-f.p[0]), beta = (float)(1 + f.p[2]);
-            float sign = f.invert_normals ? -1.0f : 1.0f;
-            float x = (float)p.x, y = (float)p.y;
-            float r2 = x * x + y * y;
-            float root = sqrtf(1.0f - beta * r2 / (Rr * Rr));
-            float A4 = (float)f.p[3], A6 = (float)f.p[4], A8 = (float)f.p[5], A10 = (float)f.p[6],
-                  A12 = (float)f.p[7], A14 = (float)f.p[8], A16 = (float)f.p[9];
-            float df = r2 * (4 * A4 + r2 * (6 * A6 + r2 * (8 * A8 + r2 * (10 * A10 + r2 * (12 * A12 +
-                       r2 * (14 * A14 + r2 * 16 * A16))))));
-            df += 2.0f / (Rr * (1.0f + root));
-            df += beta * r2 / (Rr * Rr * Rr * root * (1.0f + root) * (1.0f + root));
-            return norm3(mul3(mk3(-df * x, -df * y, 1.0f), sign));
+        case RP_FACE_ASPHERIC: {  // cfaces.pyx:1976-2005
+            float Rq = -M.p[0], beta = 1.0f + M.p[2];
+            float sign = F.invert_normals ? -1.0f : 1.0f;
+            float r2 = u.x * u.x + u.y * u.y;
+            float root = sqrtf(1.0f - beta * r2 / (Rq * Rq));
+            float df = r2 * (4.0f * M.p[3] + r2 * (6.0f * M.p[4] + r2 * (8.0f * M.p[5] + r2 * (10.0f * M.p[6] +
+                       r2 * (12.0f * M.p[7] + r2 * (14.0f * M.p[8] + r2 * 16.0f * M.p[9]))))));
+            float inv = 1.0f / (Rq * (1.0f + root));
+            df += 2.0f * inv + beta * r2 * inv * inv / (Rq * root);
+            n = norm3(mul3(mk3(-df * u.x, -df * u.y, 1.0f), sign));
+            return true;
         }
-        default: handled = false; return mk3(0, 0, 0);
+        default: return false;
     }
 }
+
+// ---- materials in FP32 ------------------------------------------------------------
+struct RayF {
+    f3 d;         // direction (unit to FP32 rounding)
+    f3 E;         // E_vector
+    cf e1, e2;    // E1_amp, E2_amp
+    double2 n;    // refractive_index (copied to transparent / PEC children)
+    unsigned type, wl;
+};
+struct ChildF {
+    f3 d;
+    cf e1, e2;
+    double2 n;
+    unsigned type;
+};
 
 // convert_to_sp in FP32 (cmaterials.pyx:49-91)
-__device__ __forceinline__ void sp_mixed(f3 d, f3 E, cf e1, cf e2, f3 normal, f3 &Eo, cf &e1o, cf &e2o) {
+__device__ __forceinline__ void sp_f(f3 d, f3 E, cf e1, cf e2, f3 normal, f3 &Eo, cf &e1o, cf &e2o) {
     f3 E2v = norm3(cross3(d, E));
     f3 E1v = norm3(cross3(E2v, d));
     f3 Sv = cross3(d, normal);
@@ -313,80 +599,70 @@ __device__ __forceinline__ void sp_mixed(f3 d, f3 E, cf e1, cf e2, f3 normal, f3
     Eo = Sv;
 }
 
-// Material evaluation for the common materials in FP32 (OPL and the hit point
-// stay FP64).  Returns -1 for materials left to the FP64 path.
-__device__ int eval_mixed(const DevScene &S, const rp_material &m, const RayState &r, v3 point, f3 nrm_in,
-                          ChildCommon &cc, Child *ch, unsigned *err) {
-    const double INF = inf_d();
+__device__ __forceinline__ bool mat_specialised(int type) {
+    return type == RP_MAT_NONE || type == RP_MAT_OPAQUE || type == RP_MAT_PEC || type == RP_MAT_DIELECTRIC ||
+           type == RP_MAT_FULL_DIELECTRIC || type == RP_MAT_FULL_DIELECTRIC_DISPERSIVE || type == RP_MAT_TRANSPARENT;
+}
+
+// Children of a hit for the specialised materials (cmaterials.pyx:260-278
+// Transparent, 292-319 PEC, 589-680 Dielectric, 756-872 FullDielectric,
+// 897-1013 FullDielectricDispersive).  Eo receives the children's shared
+// E_vector; returns the number of children.
+__device__ int eval_f(const DevScene &S, const rp_material &m, const RayF &r, f3 normal, f3 &Eo, ChildF *ch,
+                      unsigned *err) {
     if (m.type == RP_MAT_NONE || m.type == RP_MAT_OPAQUE) return 0;
-    if (m.type != RP_MAT_PEC && m.type != RP_MAT_DIELECTRIC && m.type != RP_MAT_FULL_DIELECTRIC &&
-        m.type != RP_MAT_FULL_DIELECTRIC_DISPERSIVE && m.type != RP_MAT_TRANSPARENT)
-        return -1;
-    f3 normal = norm3(nrm_in);
-    f3 d = tof(r.d);
-    f3 ind = norm3(d);
-    f3 E = tof(r.E);
-    cf e1 = cfm((float)r.e1.x, (float)r.e1.y), e2 = cfm((float)r.e2.x, (float)r.e2.y);
-    f3 Eo;
+    normal = norm3(normal);
+    const f3 d = r.d, ind = norm3(d);
     cf E1, E2;
-    sp_mixed(d, E, e1, e2, normal, Eo, E1, E2);
-    cc.E = tod(Eo);
-    cc.opl = r.opl + r.len * r.n.x;  // FP64
-    cc.origin = point;
-    cc.normal = tod(normal);
+    sp_f(d, r.E, r.e1, r.e2, normal, Eo, E1, E2);
     if (m.type == RP_MAT_TRANSPARENT) {
-        ch[0].d = r.d;
+        ch[0].d = d;
         ch[0].n = r.n;
-        ch[0].e1 = make_double2(E1.x, E1.y);
-        ch[0].e2 = make_double2(E2.x, E2.y);
-        ch[0].len = INF;
+        ch[0].e1 = E1;
+        ch[0].e2 = E2;
         ch[0].type = r.type & ~RP_REFL_RAY;
         return 1;
     }
-    float cosTheta = dot3(normal, m.type == RP_MAT_PEC ? d : ind);
-    f3 ctn = mul3(normal, cosTheta);
+    const float cosTheta = dot3(normal, m.type == RP_MAT_PEC ? d : ind);
+    const f3 ctn = mul3(normal, cosTheta);
     if (m.type == RP_MAT_PEC) {
-        ch[0].d = tod(sub3(d, mul3(ctn, 2.0f)));
+        ch[0].d = sub3(d, mul3(ctn, 2.0f));
         ch[0].n = r.n;
-        ch[0].e1 = make_double2(-E1.x, -E1.y);
-        ch[0].e2 = make_double2(E2.x, E2.y);
-        ch[0].len = INF;
+        ch[0].e1 = cfm(-E1.x, -E1.y);
+        ch[0].e2 = E2;
         ch[0].type = r.type | RP_REFL_RAY;
         return 1;
     }
-    float cos1 = fabsf(cosTheta);
-    bool out_to_in = cosTheta < 0.0f;
+    const float cos1 = fabsf(cosTheta);
+    const bool out_to_in = cosTheta < 0.0f;
+    const float flip = out_to_in ? 1.0f : -1.0f;
     if (m.type == RP_MAT_DIELECTRIC) {
-        float n1 = (float)(out_to_in ? m.n_outside[0] : m.n_inside[0]);
-        float n2 = (float)(out_to_in ? m.n_inside[0] : m.n_outside[0]);
+        float n1 = f_of_d(out_to_in ? m.n_outside[0] : m.n_inside[0]);
+        float n2 = f_of_d(out_to_in ? m.n_inside[0] : m.n_outside[0]);
         ch[0].n = out_to_in ? make_double2(m.n_inside[0], m.n_inside[1]) : make_double2(m.n_outside[0], m.n_outside[1]);
-        float flip = out_to_in ? 1.0f : -1.0f;
         float q = n2 / n1;
         float N2_sin2 = cosTheta * cosTheta + (q * q - 1.0f);
-        ch[0].len = INF;
         if (N2_sin2 < 0.0f) {
-            ch[0].d = tod(sub3(ind, mul3(ctn, 2.0f)));
-            ch[0].e1 = make_double2(-E1.x, -E1.y);
-            ch[0].e2 = make_double2(-E2.x, -E2.y);
+            ch[0].d = sub3(ind, mul3(ctn, 2.0f));
+            ch[0].e1 = cfm(-E1.x, -E1.y);
+            ch[0].e2 = cfm(-E2.x, -E2.y);
             ch[0].type = r.type | RP_REFL_RAY;
         } else {
             f3 tg2 = mul3(sub3(ind, ctn), n1 / n2);
             float c2 = sqrtf(1.0f - dot3(tg2, tg2));
             f3 tr = sub3(tg2, mul3(normal, c2 * flip));
             float cos2 = fabsf(dot3(tr, normal));
-            float aspect = sqrtf(cos2 / cos1) * (2 * n1) * cos1;
+            float aspect = sqrtf(cos2 / cos1) * (2.0f * n1) * cos1;
             float T_p = aspect / (n2 * cos1 + n1 * cos2);
             float T_s = aspect / (n2 * cos2 + n1 * cos1);
-            ch[0].d = tod(tr);
-            ch[0].e1 = make_double2(E1.x * T_s, E1.y * T_s);
-            ch[0].e2 = make_double2(E2.x * T_p, E2.y * T_p);
+            ch[0].d = tr;
+            ch[0].e1 = cmuls(E1, T_s);
+            ch[0].e2 = cmuls(E2, T_p);
             ch[0].type = r.type & ~RP_REFL_RAY;
         }
         return 1;
     }
-    // FullDielectric / FullDielectricDispersive (cmaterials.pyx:756-872, 897-1013)
-    float sin1 = sqrtf(fabsf(1.0f - cos1 * cos1));
-    cf n1, n2;
+    // FullDielectric / FullDielectricDispersive
     double2 n1d, n2d;
     if (m.type == RP_MAT_FULL_DIELECTRIC) {
         double2 ni = make_double2(m.n_inside[0], m.n_inside[1]), no = make_double2(m.n_outside[0], m.n_outside[1]);
@@ -401,23 +677,21 @@ __device__ int eval_mixed(const DevScene &S, const rp_material &m, const RayStat
         n1d = S.ntab[(long long)(out_to_in ? m.curve_outside : m.curve_inside) * S.n_wl + w];
         n2d = S.ntab[(long long)(out_to_in ? m.curve_inside : m.curve_outside) * S.n_wl + w];
     }
-    n1 = cfm((float)n1d.x, (float)n1d.y);
-    n2 = cfm((float)n2d.x, (float)n2d.y);
-    float flip = out_to_in ? 1.0f : -1.0f;
+    const cf n1 = cf_of_d(n1d), n2 = cf_of_d(n2d);
+    const float sin1 = sqrtf(fabsf(1.0f - cos1 * cos1));
     cf sin2 = cdiv(cmuls(n1, sin1), n2);
     cf cos2 = csqrtf_(csub(cfm(1.0f, 0.0f), cmul(sin2, sin2)));
-    float P_in = n1.x * (cabs2(E1) + cabs2(E2));
+    const float P_in = n1.x * (cabs2(E1) + cabs2(E2));
     if (P_in == 0.0f) return 0;
     cf n2c1 = cmuls(n2, cos1), n1c2 = cmul(n1, cos2), n2c2 = cmul(n2, cos2), n1c1 = cmuls(n1, cos1);
     cf den_p = cadd(n2c1, n1c2), den_s = cadd(n2c2, n1c1);
-    cf R_p = cmul(cdiv(cfm(n1c2.x - n2c1.x, n1c2.y - n2c1.y), den_p), E2);
-    cf R_s = cmul(cdiv(cfm(n1c1.x - n2c2.x, n1c1.y - n2c2.y), den_s), E1);
+    cf R_p = cmul(cdiv(csub(n1c2, n2c1), den_p), E2);
+    cf R_s = cmul(cdiv(csub(n1c1, n2c2), den_s), E1);
     int nc = 0;
-    if ((n1.x * (cabs2(R_s) + cabs2(R_p))) / P_in > (float)m.reflection_threshold) {
-        ch[0].d = tod(sub3(ind, mul3(ctn, 2.0f)));
-        ch[0].len = INF;
-        ch[0].e1 = make_double2(R_s.x, R_s.y);
-        ch[0].e2 = make_double2(-R_p.x, -R_p.y);
+    if ((n1.x * (cabs2(R_s) + cabs2(R_p))) / P_in > f_of_d(m.reflection_threshold)) {
+        ch[0].d = sub3(ind, mul3(ctn, 2.0f));
+        ch[0].e1 = R_s;
+        ch[0].e2 = cfm(-R_p.x, -R_p.y);
         ch[0].n = n1d;
         ch[0].type = r.type | RP_REFL_RAY;
         nc = 1;
@@ -429,16 +703,140 @@ __device__ int eval_mixed(const DevScene &S, const rp_material &m, const RayStat
     cf num = cmuls(n1, 2.0f * cos1 * aspect);
     cf T_p = cmul(cdiv(num, den_p), E2);
     cf T_s = cmul(cdiv(num, den_s), E1);
-    if ((n2.x * (cabs2(T_s) + cabs2(T_p))) / P_in > (float)m.transmission_threshold) {
-        ch[nc].d = tod(tr);
-        ch[nc].len = INF;
-        ch[nc].e1 = make_double2(T_s.x, T_s.y);
-        ch[nc].e2 = make_double2(T_p.x, T_p.y);
+    if ((n2.x * (cabs2(T_s) + cabs2(T_p))) / P_in > f_of_d(m.transmission_threshold)) {
+        ch[nc].d = tr;
+        ch[nc].e1 = T_s;
+        ch[nc].e2 = T_p;
         ch[nc].n = n2d;
         ch[nc].type = r.type & ~RP_REFL_RAY;
         nc++;
     }
     return nc;
+}
+
+// Writes one child from FP32 fields (exact widening on the integer pipe).
+__device__ __forceinline__ void store_child_f(const RaySoA &out, unsigned long long k, const double *origin,
+                                              f3 normal, f3 E, double opl, const ChildF &c, double phase,
+                                              unsigned wl, unsigned parent, unsigned endf, unsigned ident) {
+    out.ox[k] = origin[0];
+    out.oy[k] = origin[1];
+    out.oz[k] = origin[2];
+    out.dx[k] = d_of_f(c.d.x);
+    out.dy[k] = d_of_f(c.d.y);
+    out.dz[k] = d_of_f(c.d.z);
+    out.nx[k] = d_of_f(normal.x);
+    out.ny[k] = d_of_f(normal.y);
+    out.nz[k] = d_of_f(normal.z);
+    out.ex[k] = d_of_f(E.x);
+    out.ey[k] = d_of_f(E.y);
+    out.ez[k] = d_of_f(E.z);
+    out.n[k] = c.n;
+    out.e1[k] = make_double2(d_of_f(c.e1.x), d_of_f(c.e1.y));
+    out.e2[k] = make_double2(d_of_f(c.e2.x), d_of_f(c.e2.y));
+    out.len[k] = __longlong_as_double(0x7ff0000000000000LL);
+    out.phase[k] = phase;
+    out.opl[k] = opl;
+    out.wl[k] = wl;
+    out.parent[k] = parent;
+    out.endf[k] = endf;
+    out.ident[k] = ident;
+    out.type[k] = c.type;
+}
+
+// ---- the nearest-hit search --------------------------------------------------------
+struct Best {
+    ff len;  // Euclidean distance of the nearest hit so far
+    ff t;    // its ray parameter
+    int face, list;
+};
+
+// The FP64 paths for faces and materials this kernel does not specialise are
+// kept out of line so that their registers and stack do not weigh on the
+// specialised path.
+
+// FP64 distance for a face type this kernel does not specialise.
+__device__ __noinline__ double fallback_dist(const GenArgs &A, const DevScene &S, const rp_face &F, int l,
+                                                unsigned long long i) {
+    const rp_facelist &L = S.lists[l];
+    v3 o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
+    v3 d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
+    v3 pend = addv(o, mulvs(d, A.max_len));
+    return face_isect(S, F, xform(L.inv_trans.m, L.inv_trans.t, o), xform(L.inv_trans.m, L.inv_trans.t, pend), A.err);
+}
+
+// FP32 world normal of a face type this kernel does not specialise, from the
+// FP64 normal at the local hit point.
+__device__ __noinline__ f3 fallback_normal(const DevScene &S, const rp_face &F, int l, v3 lp, unsigned *err) {
+    v3 n64 = face_normal(S, F, lp, err);
+    if (F.invert_normal) n64 = negv(n64);
+    n64 = rotv(S.lists[l].trans.m, n64);
+    return f3_of_d(n64.x, n64.y, n64.z);
+}
+
+// Children of a material this kernel does not specialise (polarisers,
+// waveplate, partial mirror, apertures, ...) through the FP64 path, after the
+// termination filter; *term receives the number of children dropped by it.
+__device__ __noinline__ int fallback_children(const GenArgs &A, const DevScene &S, const rp_face &F,
+                                              const rp_material &Mt, int l, unsigned long long i, double len,
+                                              const double *origin, f3 nrm, ChildCommon *ccd, Child *chd,
+                                              unsigned *term) {
+    v3 tng = face_tangent(F);
+    if (F.invert_normal) tng = negv(tng);
+    tng = rotv(S.lists[l].trans.m, tng);
+    RayState r;
+    r.o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
+    r.d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
+    r.E = mkv(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
+    r.n = A.in.n[i];
+    r.e1 = A.in.e1[i];
+    r.e2 = A.in.e2[i];
+    r.len = len;
+    r.opl = A.in.opl[i];
+    r.type = A.in.type[i];
+    r.wl = A.in.wl[i];
+    int nc = eval_children(S, Mt, r, mkv(origin[0], origin[1], origin[2]),
+                           mkv(d_of_f(nrm.x), d_of_f(nrm.y), d_of_f(nrm.z)), tng, *ccd, chd, A.err);
+    if (A.e2_term > 0.0 && nc > 0) {
+        int w = 0;
+        for (int k = 0; k < nc; k++) {
+            if (!(child_e2(chd[k]) < A.e2_term)) {
+                if (w != k) chd[w] = chd[k];
+                w++;
+            }
+        }
+        *term = (unsigned)(nc - w);
+        nc = w;
+    }
+    return nc;
+}
+
+__device__ __forceinline__ void try_face(const GenArgs &A, const DevScene &S, const MxList *ml, const MxFace *mf,
+                                         int f, int l, int &cur, LRay &R, const ff *O, const ff *D, ff dlen,
+                                         float tmax, unsigned long long i, Best &b) {
+    if (l != cur) {
+        R = local_ray(ml[l], O, D);
+        cur = l;
+    }
+    const rp_face &F = S.faces[f];
+    bool fb;
+    ff t = face_t(S, F, mf[f], R, tmax, A.err, fb);
+    ff dist;
+    if (fb) {
+        double dd = fallback_dist(A, S, F, l, i);
+        if (!(F.tolerance < dd)) return;  // also rejects NO_INTERSECTION (-1)
+        dist = ff_of_d(dd);
+        t = ff_div(dist, dlen);
+    } else {
+        if (t.hi < 0.0f) return;
+        dist = ff_mul(t, dlen);
+        if (!(mf[f].tol < dist.hi)) return;
+    }
+    if (ff_lt(dist, b.len) || (ff_eq(dist, b.len) && b.face >= 0 && f < b.face)) {
+        b.len = dist;
+        b.t = t;
+        b.face = f;
+        b.list = l;
+    }
 }
 
 }  // namespace mx
@@ -460,11 +858,16 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
     return fmaxf(tmin, 0.0f);
 }
 
-__global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A) {
+__global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A, unsigned mx_off) {
+    using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_hits, s_term;
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
+    MxList *ml = reinterpret_cast<MxList *>(smem + mx_off);
+    MxFace *mf = reinterpret_cast<MxFace *>(ml + A.S.n_lists);
+    const float max_len = f_of_d(A.max_len);  // exact: max_length is a float
+    stage_mixed(A, ml, mf, max_len);
     if (threadIdx.x == 0) {
         s_hits = 0;
         s_term = 0;
@@ -474,95 +877,74 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A) {
     const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
     const bool active = i < A.n_in;
 
-    int best = -1, best_list = -1;
-    double len = A.max_len;   // Euclidean distance of the current nearest hit
-    v3 o = mkv(0, 0, 0), d = mkv(0, 0, 0);
-    double dlen = 1.0;        // |d| of the stored direction
+    Best b;
+    b.len = ffm(max_len, 0.0f);
+    b.t = ffm(0.0f, 0.0f);
+    b.face = -1;
+    b.list = -1;
+    ff O[3], D[3], dlen = ffm(1.0f, 0.0f);
     if (active) {
-        o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
-        d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
-        double d2 = d.x * d.x + d.y * d.y + d.z * d.z;
-        dlen = 1.0 + 0.5 * (d2 - 1.0);  // first order in |d|^2 - 1 (directions are unit to FP32 rounding)
-        const double tmax = A.max_len;  // the far point is origin + d * max_length (ray parameter)
-        mx::f3 df = mx::mk3((float)d.x, (float)d.y, (float)d.z);
-        float il = rsqrtf(mx::dot3(df, df));
-        float ix = 1.0f / ((fabsf(df.x * il) < 1e-30f) ? copysignf(1e-30f, df.x) : df.x * il);
-        float iy = 1.0f / ((fabsf(df.y * il) < 1e-30f) ? copysignf(1e-30f, df.y) : df.y * il);
-        float iz = 1.0f / ((fabsf(df.z * il) < 1e-30f) ? copysignf(1e-30f, df.z) : df.z * il);
-        float ox = (float)o.x, oy = (float)o.y, oz = (float)o.z;
-        const int nf = S.n_faces;
-        const int nmask = nf < 64 ? nf : 64;
-        const float lim0 = (float)A.max_len * 1.000001f + 1e-4f;
-        unsigned long long cand = 0;
+        O[0] = ff_of_d(A.in.ox[i]);
+        O[1] = ff_of_d(A.in.oy[i]);
+        O[2] = ff_of_d(A.in.oz[i]);
+        D[0] = ff_of_d(A.in.dx[i]);
+        D[1] = ff_of_d(A.in.dy[i]);
+        D[2] = ff_of_d(A.in.dz[i]);
+        dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
+        int cur = -1;
+        LRay R;
         if (A.one_list >= 0) {
-            int f = S.lists[A.one_list].first_face + A.one_face;
-            if (f < 64) cand = 1ull << f;
+            // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
+            const int f = S.lists[A.one_list].first_face + A.one_face;
+            try_face(A, S, ml, mf, f, A.one_list, cur, R, O, D, dlen, max_len, i, b);
         } else {
+            // culled nearest-first search over the first 64 faces, then the rest in order
+            const float dfx = D[0].hi, dfy = D[1].hi, dfz = D[2].hi;
+            const float il = rsqrtf(dfx * dfx + dfy * dfy + dfz * dfz);
+            const float ix = 1.0f / ((fabsf(dfx * il) < 1e-30f) ? copysignf(1e-30f, dfx) : dfx * il);
+            const float iy = 1.0f / ((fabsf(dfy * il) < 1e-30f) ? copysignf(1e-30f, dfy) : dfy * il);
+            const float iz = 1.0f / ((fabsf(dfz * il) < 1e-30f) ? copysignf(1e-30f, dfz) : dfz * il);
+            const float ox = O[0].hi, oy = O[1].hi, oz = O[2].hi;
+            const int nf = S.n_faces;
+            const int nmask = nf < 64 ? nf : 64;
+            const float lim0 = max_len * 1.000001f + 1e-4f;
+            unsigned long long cand = 0;
             for (int f = 0; f < nmask; f++)
                 if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) <= lim0) cand |= 1ull << f;
-        }
-        int cur_list = -1;
-        mx::LRay R;
-        v3 p1 = o, p2 = o;
-        v3 pend = addv(o, mulvs(d, A.max_len));
-        while (cand) {
-            float tsel = __int_as_float(0x7f800000);
-            int sel = -1;
-            for (unsigned long long m = cand; m; m &= m - 1) {
-                int f = __ffsll((long long)m) - 1;
-                float t = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                if (t < tsel) {
-                    tsel = t;
-                    sel = f;
+            while (cand) {
+                float tsel = __int_as_float(0x7f800000);
+                int sel = -1;
+                for (unsigned long long m = cand; m; m &= m - 1) {
+                    int f = __ffsll((long long)m) - 1;
+                    float t = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+                    if (t < tsel) {
+                        tsel = t;
+                        sel = f;
+                    }
                 }
+                if (sel < 0 || tsel > b.len.hi * 1.000001f + 1e-4f) break;
+                cand &= ~(1ull << sel);
+                int l = S.face_list[sel];
+                if (l < 0 || l >= S.n_lists) {
+                    atomicOr(A.err, ERR_SHAPE_STACK);
+                    break;
+                }
+                try_face(A, S, ml, mf, sel, l, cur, R, O, D, dlen, max_len, i, b);
             }
-            if (sel < 0 || tsel > (float)len * 1.000001f + 1e-4f) break;
-            cand &= ~(1ull << sel);
-            int l = S.face_list[sel];
-            if (l < 0 || l >= S.n_lists) {
-                atomicOr(A.err, ERR_SHAPE_STACK);
-                break;
-            }
-            const rp_facelist &L = S.lists[l];
-            if (l != cur_list) {
-                R.p = xform(L.inv_trans.m, L.inv_trans.t, o);
-                R.df = mx::rot3(L.inv_trans.m, df);
-                R.dd = mkv(R.df.x, R.df.y, R.df.z);
-                p1 = R.p;
-                p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
-                cur_list = l;
-            }
-            const rp_face &F = S.faces[sel];
-            double t = mx::face_t_mixed(S, F, R, tmax, A.err);
-            double dist;
-            if (t < MX_MISS - 0.5) {
-                dist = face_isect(S, F, p1, p2, A.err);  // FP64 path (distortion, polygons, ...)
-            } else {
-                dist = (t == MX_MISS) ? MX_MISS : t * dlen;
-            }
-            if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && sel < best))) {
-                len = dist;
-                best = sel;
-                best_list = l;
+            for (int f = nmask; f < nf; f++) {
+                if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f) continue;
+                int l = S.face_list[f];
+                if (l < 0 || l >= S.n_lists) {
+                    atomicOr(A.err, ERR_SHAPE_STACK);
+                    break;
+                }
+                try_face(A, S, ml, mf, f, l, cur, R, O, D, dlen, max_len, i, b);
             }
         }
-        for (int f = nmask; f < nf && A.one_list < 0; f++) {  // faces beyond the first 64: FP64 path
-            int l = S.face_list[f];
-            if (l < 0 || l >= S.n_lists) break;
-            const rp_facelist &L = S.lists[l];
-            v3 q1 = xform(L.inv_trans.m, L.inv_trans.t, o), q2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
-            const rp_face &F = S.faces[f];
-            double dist = face_isect(S, F, q1, q2, A.err);
-            if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && f < best))) {
-                len = dist;
-                best = f;
-                best_list = l;
-            }
-        }
-        A.in.len[i] = len;
-        A.in.endf[i] = best >= 0 ? (unsigned)S.faces[best].idx : 0xFFFFFFFFu;
-        if (best >= 0) {
-            atomicAdd(&s_counts[best], 1u);
+        A.in.len[i] = d_of_ff(b.len);
+        A.in.endf[i] = b.face >= 0 ? (unsigned)S.faces[b.face].idx : 0xFFFFFFFFu;
+        if (b.face >= 0) {
+            atomicAdd(&s_counts[b.face], 1u);
             atomicAdd(&s_hits, 1u);
         }
     }
@@ -573,52 +955,75 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A) {
         return;
     }
 
-    Child ch[2];
-    ChildCommon cc;
+    // ---- material ----
     int nc = 0;
-    if (active && best >= 0) {
-        const rp_facelist &L = S.lists[best_list];
-        const rp_face &F = S.faces[best];
-        v3 point = addv(o, mulvs(d, len / dlen));  // FP64 hit point
-        v3 lp = xform(L.inv_trans.m, L.inv_trans.t, point);
-        bool handled;
-        mx::f3 nl = mx::face_normal_mixed(S, F, lp, A.err, handled);
-        v3 nrm, tng = face_tangent(F);
-        if (handled) {
-            if (F.invert_normal) nl = mx::mk3(-nl.x, -nl.y, -nl.z);
-            nrm = mx::tod(mx::rot3(L.trans.m, nl));
+    ChildF ch[2];
+    f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);
+    double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
+    bool fp64_children = false;
+    Child chd[2];
+    ChildCommon ccd;
+    if (active && b.face >= 0) {
+        const rp_face &F = S.faces[b.face];
+        const MxFace &M = mf[b.face];
+        const MxList &L = ml[b.list];
+        ff P[3];
+        P[0] = ff_add(O[0], ff_mul(b.t, D[0]));
+        P[1] = ff_add(O[1], ff_mul(b.t, D[1]));
+        P[2] = ff_add(O[2], ff_mul(b.t, D[2]));
+        origin[0] = d_of_ff(P[0]);
+        origin[1] = d_of_ff(P[1]);
+        origin[2] = d_of_ff(P[2]);
+        // the hit in the face list's frame, relative to the face vertex
+        ff lp[3];
+        if (L.ident) {
+            lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
+            lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
+            lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
         } else {
-            nrm = face_normal(S, F, lp, A.err);
-            if (F.invert_normal) nrm = negv(nrm);
-            nrm = rotv(L.trans.m, nrm);
+            ff_rotate(L, P, lp, true);
         }
-        if (F.invert_normal) tng = negv(tng);
-        tng = rotv(L.trans.m, tng);
+        f3 u = mk3(lp[0].hi + lp[0].lo, lp[1].hi + lp[1].lo, ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)).hi);
+        f3 nl;
+        if (face_normal_f(F, M, u, nl)) {
+            if (F.invert_normal) nl = mk3(-nl.x, -nl.y, -nl.z);
+            nrm = mk3(L.r[0] * nl.x + L.r[1] * nl.y + L.r[2] * nl.z, L.r[3] * nl.x + L.r[4] * nl.y + L.r[5] * nl.z,
+                      L.r[6] * nl.x + L.r[7] * nl.y + L.r[8] * nl.z);
+        } else {
+            nrm = fallback_normal(S, F, b.list, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
+        }
         if (F.material >= 0) {
-            RayState r;
-            r.o = o;
-            r.d = d;
-            r.E = mkv(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
-            r.n = A.in.n[i];
-            r.e1 = A.in.e1[i];
-            r.e2 = A.in.e2[i];
-            r.len = len;
-            r.opl = A.in.opl[i];
-            r.type = A.in.type[i];
-            r.wl = A.in.wl[i];
-            const rp_material &M = S.mats[F.material];
-            nc = mx::eval_mixed(S, M, r, point, mx::tof(nrm), cc, ch, A.err);
-            if (nc < 0) nc = eval_children(S, M, r, point, nrm, tng, cc, ch, A.err);
-            if (A.e2_term > 0.0 && nc > 0) {
-                int w = 0;
-                for (int k = 0; k < nc; k++) {
-                    if (!(child_e2(ch[k]) < A.e2_term)) {
-                        if (w != k) ch[w] = ch[k];
-                        w++;
+            const rp_material &Mt = S.mats[F.material];
+            const ff lenn = ff_mul(b.len, ff_of_d(A.in.n[i].x));
+            opl = d_of_ff(ff_add(ff_of_d(A.in.opl[i]), lenn));
+            if (mat_specialised(Mt.type)) {
+                RayF r;
+                r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
+                r.E = f3_of_d(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
+                r.e1 = cf_of_d(A.in.e1[i]);
+                r.e2 = cf_of_d(A.in.e2[i]);
+                r.n = A.in.n[i];
+                r.type = A.in.type[i];
+                r.wl = A.in.wl[i];
+                nc = eval_f(S, Mt, r, nrm, Eo, ch, A.err);
+                nrm = norm3(nrm);
+                if (A.e2_term > 0.0 && nc > 0) {
+                    const float e2t = f_of_d(A.e2_term);
+                    int w = 0;
+                    for (int k = 0; k < nc; k++) {
+                        if (!(cabs2(ch[k].e1) + cabs2(ch[k].e2) < e2t)) {
+                            if (w != k) ch[w] = ch[k];
+                            w++;
+                        }
                     }
+                    if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
+                    nc = w;
                 }
-                if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
-                nc = w;
+            } else {
+                unsigned term = 0;
+                nc = fallback_children(A, S, F, Mt, b.list, i, d_of_ff(b.len), origin, nrm, &ccd, chd, &term);
+                fp64_children = true;
+                if (term) atomicAdd(&s_term, term);
             }
         }
     }
@@ -627,11 +1032,16 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A) {
     unsigned tile_children;
     const unsigned excl = block_scan((unsigned)nc, &tile_children);
     if (nc > 0) {
-        double phase = A.in.phase[i];
-        unsigned wl = A.in.wl[i], ident = A.in.ident[i];
-        unsigned endf = (unsigned)S.faces[best].idx;
+        const double phase = A.in.phase[i];
+        const unsigned wl = A.in.wl[i], ident = A.in.ident[i];
+        const unsigned endf = (unsigned)S.faces[b.face].idx;
         const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
-        for (int k = 0; k < nc; k++) store_child(A.scratch, slot + k, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
+        for (int k = 0; k < nc; k++) {
+            if (fp64_children)
+                store_child(A.scratch, slot + k, ccd, chd[k], phase, wl, (unsigned)i, endf, ident);
+            else
+                store_child_f(A.scratch, slot + k, origin, nrm, Eo, opl, ch[k], phase, wl, (unsigned)i, endf, ident);
+        }
     }
     flush_counts(A, S, s_counts);
     if (threadIdx.x == 0) A.tile_counts[tile] = tile_children;
@@ -643,15 +1053,18 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A) {
 
 cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st) {
     if (a.n_in == 0) return cudaSuccess;
+    const size_t off = (smem + 15) & ~(size_t)15;
+    const size_t total = off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
+    if (total > 220 * 1024) return cudaErrorInvalidConfiguration;  // scene too large for the per-block tables
     unsigned grid = (unsigned)((a.n_in + RP_BLOCK - 1) / RP_BLOCK);
     static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
+    if (total > 48 * 1024 && total > configured) {
         cudaError_t e = cudaFuncSetAttribute(generation_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+                                             (int)total);
         if (e != cudaSuccess) return e;
-        configured = smem;
+        configured = total;
     }
-    generation_mixed_kernel<<<grid, RP_BLOCK, smem, st>>>(a);
+    generation_mixed_kernel<<<grid, RP_BLOCK, total, st>>>(a, (unsigned)off);
     return cudaGetLastError();
 }
 
