@@ -41,7 +41,7 @@ struct rp_ctx {
     uint64_t pooled;                 // bytes in `pool`
     std::vector<cudaEvent_t> gen_ev; // per-generation kernel events (pairs)
     struct rp_rays *arena;           // child slots of the generation being traced
-    // per-generation scan scratch: [counter | out_count | err | pad | stats[2] | tile states...]
+    // per-generation scratch: [out_count | err | pad | stats[2] | tile counter | pad | tile counts, offsets]
     unsigned char *scratch;
     size_t scratch_bytes;
     unsigned long long *h_pinned;  // 8 words of pinned host memory for small read-backs
@@ -57,6 +57,7 @@ struct rp_scene {
     int n_faces;
     size_t smem;              // bytes of tables staged per block
     int smem_tables;
+    int mixed_fallback;       // faces or materials the mixed kernel leaves to its FP64 code
     const rp_dispersion *disp;  // device copy of the dispersion curve table
     int n_disp;
     std::vector<rp_face> host_faces;
@@ -311,6 +312,19 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     s->n_faces = d->n_faces;
     s->host_faces.assign(d->faces, d->faces + d->n_face_records);
     s->host_lists.assign(d->lists, d->lists + d->n_lists);
+    s->mixed_fallback = 0;
+    for (int f = 0; f < d->n_faces; f++) {
+        int t = d->faces[f].type;
+        if (t != RP_FACE_CIRCULAR && t != RP_FACE_RECTANGULAR && t != RP_FACE_SHAPED_PLANAR &&
+            t != RP_FACE_SPHERICAL && t != RP_FACE_SHAPED_SPHERICAL && t != RP_FACE_CONIC && t != RP_FACE_ASPHERIC)
+            s->mixed_fallback = 1;
+    }
+    for (int m = 0; m < d->n_materials; m++) {
+        int t = d->materials[m].type;
+        if (t != RP_MAT_NONE && t != RP_MAT_OPAQUE && t != RP_MAT_PEC && t != RP_MAT_DIELECTRIC &&
+            t != RP_MAT_FULL_DIELECTRIC && t != RP_MAT_FULL_DIELECTRIC_DISPERSIVE && t != RP_MAT_TRANSPARENT)
+            s->mixed_fallback = 1;
+    }
     size_t o_lists = 0;
     size_t o_faces = o_lists + align256(sizeof(rp_facelist) * d->n_lists);
     size_t o_mats = o_faces + align256(sizeof(rp_face) * d->n_face_records);
@@ -559,7 +573,7 @@ int rp_rays_field(const rp_rays *r, const char *name, void **p) {
 // ---- tracing ------------------------------------------------------------------
 #define SCRATCH_HDR 64
 
-// Per-generation scratch: [out_count | err | pad | stats[2] | pad], then the
+// Per-generation scratch: [out_count | err | pad | stats[2] | tile counter | pad], then the
 // per-tile child counts and offsets.
 static size_t scratch_bytes_for(uint64_t n_tiles) {
     return SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)) + align256(n_tiles * sizeof(unsigned long long));
@@ -619,9 +633,11 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
     a.one_face = one_face;
     a.S = s->S;
     a.smem_tables = s->smem_tables;
+    a.mixed_fallback = s->mixed_fallback;
     a.out_count = (unsigned long long *)(sc + 0);
     a.err = (unsigned *)(sc + 8);
     a.stats = (unsigned long long *)(sc + 24);
+    a.tile_next = (unsigned *)(sc + 40);
     a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
     a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)));
     a.scratch = emit ? ctx->arena->soa : in->soa;
@@ -811,7 +827,8 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_
 // (generation, tile scan, placement) but takes every scratch byte from one
 // fixed device array, laid out for RP_NOALLOC_MAX_RAYS input rays:
 //   [0, 64)       counters: child total (u64 @0), error bits (u32 @8),
-//                 hits and terminated children (2 x u64 @24) -- zeroed per call
+//                 hits and terminated children (2 x u64 @24), next tile to
+//                 trace (u32 @40) -- zeroed per call
 //   tile_counts   u32 per 128-ray tile
 //   tile_offsets  u64 per tile
 //   child slots   2 per ray, structure of arrays (188 bytes per slot)
@@ -893,9 +910,11 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     a.one_face = -1;
     a.S = s->S;
     a.smem_tables = s->smem_tables;
+    a.mixed_fallback = s->mixed_fallback;
     a.out_count = (unsigned long long *)(sc + 0);
     a.err = (unsigned *)(sc + 8);
     a.stats = (unsigned long long *)(sc + 24);
+    a.tile_next = (unsigned *)(sc + 40);
     a.tile_counts = (unsigned *)(sc + NA_OFF_TILE_COUNTS);
     a.tile_offsets = (unsigned long long *)(sc + NA_OFF_TILE_OFFSETS);
     a.scratch = slots.soa;

@@ -36,6 +36,7 @@ struct GenArgs {
     int one_list, one_face;       // >= 0: sequential trace of one face of one list
     DevScene S;                   // global-memory tables
     int smem_tables;              // 1: lists/faces/materials staged in shared memory
+    int mixed_fallback;           // mixed kernel: the scene has faces / materials only its FP64 code handles
     RaySoA scratch;                 // child slots: RP_TILE_SLOTS per tile
     unsigned *tile_counts;          // [n_tiles] children of each tile
     unsigned long long *tile_offsets;  // [n_tiles] exclusive prefix (scan kernel)
@@ -43,6 +44,7 @@ struct GenArgs {
     unsigned *err;                  // error bits
     unsigned *face_counts;          // per face record hit counters
     unsigned long long *stats;      // [0] hits, [1] terminated children
+    unsigned *tile_next;            // next tile to trace (kernels that loop over tiles; zeroed per launch)
 };
 
 // launchers (rp_trace.cu / rp_mixed.cu); return cudaError_t

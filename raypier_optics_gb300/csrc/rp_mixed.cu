@@ -755,7 +755,7 @@ struct Best {
 // specialised path.
 
 // FP64 distance for a face type this kernel does not specialise.
-__device__ __noinline__ double fallback_dist(const GenArgs &A, const DevScene &S, const rp_face &F, int l,
+__device__ __forceinline__ double fallback_dist(const GenArgs &A, const DevScene &S, const rp_face &F, int l,
                                                 unsigned long long i) {
     const rp_facelist &L = S.lists[l];
     v3 o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
@@ -810,33 +810,49 @@ __device__ __noinline__ int fallback_children(const GenArgs &A, const DevScene &
     return nc;
 }
 
-__device__ __forceinline__ void try_face(const GenArgs &A, const DevScene &S, const MxList *ml, const MxFace *mf,
-                                         int f, int l, int &cur, LRay &R, const ff *O, const ff *D, ff dlen,
-                                         float tmax, unsigned long long i, Best &b) {
-    if (l != cur) {
-        R = local_ray(ml[l], O, D);
-        cur = l;
-    }
-    const rp_face &F = S.faces[f];
-    bool fb;
-    ff t = face_t(S, F, mf[f], R, tmax, A.err, fb);
-    ff dist;
-    if (fb) {
-        double dd = fallback_dist(A, S, F, l, i);
-        if (!(F.tolerance < dd)) return;  // also rejects NO_INTERSECTION (-1)
-        dist = ff_of_d(dd);
-        t = ff_div(dist, dlen);
-    } else {
-        if (t.hi < 0.0f) return;
-        dist = ff_mul(t, dlen);
-        if (!(mf[f].tol < dist.hi)) return;
-    }
+// Face types the specialised path handles (the rest go through the FP64 path).
+__device__ __forceinline__ bool face_specialised(int type) {
+    return type == RP_FACE_CIRCULAR || type == RP_FACE_RECTANGULAR || type == RP_FACE_SHAPED_PLANAR ||
+           type == RP_FACE_SPHERICAL || type == RP_FACE_SHAPED_SPHERICAL || type == RP_FACE_CONIC ||
+           type == RP_FACE_ASPHERIC;
+}
+
+// Keeps the hit if it is nearer than b (the reference's strict `dist < length`,
+// ties to the lower face index as in the oracle's order of evaluation).
+__device__ __forceinline__ void keep_nearest(ff dist, ff t, int f, int l, Best &b) {
     if (ff_lt(dist, b.len) || (ff_eq(dist, b.len) && b.face >= 0 && f < b.face)) {
         b.len = dist;
         b.t = t;
         b.face = f;
         b.list = l;
     }
+}
+
+// Tests a specialised face (the caller checks face_specialised).
+__device__ __forceinline__ void try_face(const DevScene &S, const MxList *ml, const MxFace *mf, int f, int l,
+                                         int &cur, LRay &R, const ff *O, const ff *D, ff dlen, float tmax,
+                                         unsigned *err, Best &b) {
+    if (l != cur) {
+        R = local_ray(ml[l], O, D);
+        cur = l;
+    }
+    bool fb;
+    ff t = face_t(S, S.faces[f], mf[f], R, tmax, err, fb);
+    if (t.hi < 0.0f) return;
+    ff dist = ff_mul(t, dlen);
+    if (!(mf[f].tol < dist.hi)) return;
+    keep_nearest(dist, t, f, l, b);
+}
+
+// Tests a face through the FP64 path.  Out of line: called only for face types
+// the specialised path does not handle, after the specialised search.
+__device__ __noinline__ void try_face_fp64(const GenArgs &A, const DevScene &S, int f, int l, unsigned long long i,
+                                           ff dlen, Best &b) {
+    const rp_face &F = S.faces[f];
+    double dd = fallback_dist(A, S, F, l, i);
+    if (!(F.tolerance < dd)) return;  // also rejects NO_INTERSECTION (-1)
+    ff dist = ff_of_d(dd);
+    keep_nearest(dist, ff_div(dist, dlen), f, l, b);
 }
 
 }  // namespace mx
@@ -858,213 +874,281 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
     return fmaxf(tmin, 0.0f);
 }
 
-__global__ void __launch_bounds__(RP_BLOCK) generation_mixed_kernel(GenArgs A, unsigned mx_off) {
+// One block stages the tables once and then traces tiles of RP_BLOCK rays
+// taken from a launch-wide counter until none are left, so the staging is paid
+// once per resident block and slow tiles do not hold up a static share.
+// Dynamic shared memory: the plain kernel's tables, the mixed tables at mx_off
+// and, at tb_off, each thread's box-entry distance per culled face.
+template <bool FB>
+__global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A, unsigned mx_off, unsigned tb_off) {
     using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ unsigned s_hits, s_term;
+    __shared__ unsigned s_hits, s_term, s_tile;
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
     MxList *ml = reinterpret_cast<MxList *>(smem + mx_off);
     MxFace *mf = reinterpret_cast<MxFace *>(ml + A.S.n_lists);
+    float *tb = reinterpret_cast<float *>(smem + tb_off) + threadIdx.x;  // tb[f * RP_BLOCK]
     const float max_len = f_of_d(A.max_len);  // exact: max_length is a float
     stage_mixed(A, ml, mf, max_len);
     if (threadIdx.x == 0) {
         s_hits = 0;
         s_term = 0;
     }
-    __syncthreads();
-    const unsigned tile = blockIdx.x;
-    const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
-    const bool active = i < A.n_in;
+    const unsigned long long n_tiles = (A.n_in + RP_BLOCK - 1) / RP_BLOCK;
+    const float e2t = f_of_d(A.e2_term);
 
-    Best b;
-    b.len = ffm(max_len, 0.0f);
-    b.t = ffm(0.0f, 0.0f);
-    b.face = -1;
-    b.list = -1;
-    ff O[3], D[3], dlen = ffm(1.0f, 0.0f);
-    if (active) {
-        O[0] = ff_of_d(A.in.ox[i]);
-        O[1] = ff_of_d(A.in.oy[i]);
-        O[2] = ff_of_d(A.in.oz[i]);
-        D[0] = ff_of_d(A.in.dx[i]);
-        D[1] = ff_of_d(A.in.dy[i]);
-        D[2] = ff_of_d(A.in.dz[i]);
-        dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
-        int cur = -1;
-        LRay R;
-        if (A.one_list >= 0) {
-            // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
-            const int f = S.lists[A.one_list].first_face + A.one_face;
-            try_face(A, S, ml, mf, f, A.one_list, cur, R, O, D, dlen, max_len, i, b);
-        } else {
-            // culled nearest-first search over the first 64 faces, then the rest in order
-            const float dfx = D[0].hi, dfy = D[1].hi, dfz = D[2].hi;
-            const float il = rsqrtf(dfx * dfx + dfy * dfy + dfz * dfz);
-            const float ix = 1.0f / ((fabsf(dfx * il) < 1e-30f) ? copysignf(1e-30f, dfx) : dfx * il);
-            const float iy = 1.0f / ((fabsf(dfy * il) < 1e-30f) ? copysignf(1e-30f, dfy) : dfy * il);
-            const float iz = 1.0f / ((fabsf(dfz * il) < 1e-30f) ? copysignf(1e-30f, dfz) : dfz * il);
-            const float ox = O[0].hi, oy = O[1].hi, oz = O[2].hi;
-            const int nf = S.n_faces;
-            const int nmask = nf < 64 ? nf : 64;
-            const float lim0 = max_len * 1.000001f + 1e-4f;
-            unsigned long long cand = 0;
-            for (int f = 0; f < nmask; f++)
-                if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) <= lim0) cand |= 1ull << f;
-            while (cand) {
-                float tsel = __int_as_float(0x7f800000);
-                int sel = -1;
-                for (unsigned long long m = cand; m; m &= m - 1) {
-                    int f = __ffsll((long long)m) - 1;
-                    float t = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                    if (t < tsel) {
-                        tsel = t;
-                        sel = f;
-                    }
-                }
-                if (sel < 0 || tsel > b.len.hi * 1.000001f + 1e-4f) break;
-                cand &= ~(1ull << sel);
-                int l = S.face_list[sel];
-                if (l < 0 || l >= S.n_lists) {
-                    atomicOr(A.err, ERR_SHAPE_STACK);
-                    break;
-                }
-                try_face(A, S, ml, mf, sel, l, cur, R, O, D, dlen, max_len, i, b);
-            }
-            for (int f = nmask; f < nf; f++) {
-                if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f) continue;
-                int l = S.face_list[f];
-                if (l < 0 || l >= S.n_lists) {
-                    atomicOr(A.err, ERR_SHAPE_STACK);
-                    break;
-                }
-                try_face(A, S, ml, mf, f, l, cur, R, O, D, dlen, max_len, i, b);
-            }
-        }
-        A.in.len[i] = d_of_ff(b.len);
-        A.in.endf[i] = b.face >= 0 ? (unsigned)S.faces[b.face].idx : 0xFFFFFFFFu;
-        if (b.face >= 0) {
-            atomicAdd(&s_counts[b.face], 1u);
-            atomicAdd(&s_hits, 1u);
-        }
-    }
+    for (;;) {
+        __syncthreads();  // every thread is done with the previous tile's s_tile and scan
+        if (threadIdx.x == 0) s_tile = atomicAdd(A.tile_next, 1u);
+        __syncthreads();
+        const unsigned tile = s_tile;
+        if (tile >= n_tiles) break;
+        const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
+        const bool active = i < A.n_in;
 
-    if (!A.emit) {
-        flush_counts(A, S, s_counts);
-        if (threadIdx.x == 0) atomicAdd(&A.stats[0], (unsigned long long)s_hits);
-        return;
-    }
-
-    // ---- material ----
-    int nc = 0;
-    ChildF ch[2];
-    f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);
-    double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
-    bool fp64_children = false;
-    Child chd[2];
-    ChildCommon ccd;
-    if (active && b.face >= 0) {
-        const rp_face &F = S.faces[b.face];
-        const MxFace &M = mf[b.face];
-        const MxList &L = ml[b.list];
-        ff P[3];
-        P[0] = ff_add(O[0], ff_mul(b.t, D[0]));
-        P[1] = ff_add(O[1], ff_mul(b.t, D[1]));
-        P[2] = ff_add(O[2], ff_mul(b.t, D[2]));
-        origin[0] = d_of_ff(P[0]);
-        origin[1] = d_of_ff(P[1]);
-        origin[2] = d_of_ff(P[2]);
-        // the hit in the face list's frame, relative to the face vertex
-        ff lp[3];
-        if (L.ident) {
-            lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
-            lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
-            lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
-        } else {
-            ff_rotate(L, P, lp, true);
-        }
-        f3 u = mk3(lp[0].hi + lp[0].lo, lp[1].hi + lp[1].lo, ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)).hi);
-        f3 nl;
-        if (face_normal_f(F, M, u, nl)) {
-            if (F.invert_normal) nl = mk3(-nl.x, -nl.y, -nl.z);
-            nrm = mk3(L.r[0] * nl.x + L.r[1] * nl.y + L.r[2] * nl.z, L.r[3] * nl.x + L.r[4] * nl.y + L.r[5] * nl.z,
-                      L.r[6] * nl.x + L.r[7] * nl.y + L.r[8] * nl.z);
-        } else {
-            nrm = fallback_normal(S, F, b.list, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
-        }
-        if (F.material >= 0) {
-            const rp_material &Mt = S.mats[F.material];
-            const ff lenn = ff_mul(b.len, ff_of_d(A.in.n[i].x));
-            opl = d_of_ff(ff_add(ff_of_d(A.in.opl[i]), lenn));
-            if (mat_specialised(Mt.type)) {
-                RayF r;
-                r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
-                r.E = f3_of_d(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
-                r.e1 = cf_of_d(A.in.e1[i]);
-                r.e2 = cf_of_d(A.in.e2[i]);
-                r.n = A.in.n[i];
-                r.type = A.in.type[i];
-                r.wl = A.in.wl[i];
-                nc = eval_f(S, Mt, r, nrm, Eo, ch, A.err);
-                nrm = norm3(nrm);
-                if (A.e2_term > 0.0 && nc > 0) {
-                    const float e2t = f_of_d(A.e2_term);
-                    int w = 0;
-                    for (int k = 0; k < nc; k++) {
-                        if (!(cabs2(ch[k].e1) + cabs2(ch[k].e2) < e2t)) {
-                            if (w != k) ch[w] = ch[k];
-                            w++;
+        Best b;
+        b.len = ffm(max_len, 0.0f);
+        b.t = ffm(0.0f, 0.0f);
+        b.face = -1;
+        b.list = -1;
+        ff O[3], D[3], dlen = ffm(1.0f, 0.0f);
+        if (active) {
+            O[0] = ff_of_d(A.in.ox[i]);
+            O[1] = ff_of_d(A.in.oy[i]);
+            O[2] = ff_of_d(A.in.oz[i]);
+            D[0] = ff_of_d(A.in.dx[i]);
+            D[1] = ff_of_d(A.in.dy[i]);
+            D[2] = ff_of_d(A.in.dz[i]);
+            dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
+            int cur = -1;
+            LRay R;
+            unsigned long long pend = 0;  // culled faces left to the FP64 path
+            if (A.one_list >= 0) {
+                // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
+                const int f = S.lists[A.one_list].first_face + A.one_face;
+                if (face_specialised(S.faces[f].type))
+                    try_face(S, ml, mf, f, A.one_list, cur, R, O, D, dlen, max_len, A.err, b);
+                else if constexpr (FB)
+                    try_face_fp64(A, S, f, A.one_list, i, dlen, b);
+            } else {
+                // culled nearest-first search over the first 64 faces, then the rest in order
+                const float dfx = D[0].hi, dfy = D[1].hi, dfz = D[2].hi;
+                const float il = rsqrtf(dfx * dfx + dfy * dfy + dfz * dfz);
+                const float ix = 1.0f / ((fabsf(dfx * il) < 1e-30f) ? copysignf(1e-30f, dfx) : dfx * il);
+                const float iy = 1.0f / ((fabsf(dfy * il) < 1e-30f) ? copysignf(1e-30f, dfy) : dfy * il);
+                const float iz = 1.0f / ((fabsf(dfz * il) < 1e-30f) ? copysignf(1e-30f, dfz) : dfz * il);
+                const float ox = O[0].hi, oy = O[1].hi, oz = O[2].hi;
+                const int nf = S.n_faces;
+                const int nmask = nf < 64 ? nf : 64;
+                const float lim0 = max_len * 1.000001f + 1e-4f;
+                unsigned long long cand = 0;
+                for (int f = 0; f < nmask; f++) {
+                    float te = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+                    tb[f * RP_BLOCK] = te;
+                    if (te <= lim0) cand |= 1ull << f;
+                }
+                while (cand) {
+                    float tsel = __int_as_float(0x7f800000);
+                    int sel = -1;
+                    for (unsigned long long m = cand; m; m &= m - 1) {
+                        int f = __ffsll((long long)m) - 1;
+                        float t = tb[f * RP_BLOCK];
+                        if (t < tsel) {
+                            tsel = t;
+                            sel = f;
                         }
                     }
-                    if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
-                    nc = w;
+                    if (sel < 0 || tsel > b.len.hi * 1.000001f + 1e-4f) break;
+                    cand &= ~(1ull << sel);
+                    int l = S.face_list[sel];
+                    if (l < 0 || l >= S.n_lists) {
+                        atomicOr(A.err, ERR_SHAPE_STACK);
+                        break;
+                    }
+                    if (face_specialised(S.faces[sel].type))
+                        try_face(S, ml, mf, sel, l, cur, R, O, D, dlen, max_len, A.err, b);
+                    else
+                        pend |= 1ull << sel;
                 }
-            } else {
-                unsigned term = 0;
-                nc = fallback_children(A, S, F, Mt, b.list, i, d_of_ff(b.len), origin, nrm, &ccd, chd, &term);
-                fp64_children = true;
-                if (term) atomicAdd(&s_term, term);
+                for (int f = nmask; f < nf; f++) {
+                    if (!face_specialised(S.faces[f].type)) continue;
+                    if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f) continue;
+                    int l = S.face_list[f];
+                    if (l < 0 || l >= S.n_lists) {
+                        atomicOr(A.err, ERR_SHAPE_STACK);
+                        break;
+                    }
+                    try_face(S, ml, mf, f, l, cur, R, O, D, dlen, max_len, A.err, b);
+                }
+                // the FP64 faces: the nearest hit does not depend on the order of
+                // the tests, and the box bound stays valid against the final length
+                for (int f = 0; FB && f < nf; f++) {
+                    if (f < nmask) {
+                        if (!((pend >> f) & 1ull) || tb[f * RP_BLOCK] > b.len.hi * 1.000001f + 1e-4f) continue;
+                    } else {
+                        if (face_specialised(S.faces[f].type)) continue;
+                        if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f)
+                            continue;
+                    }
+                    int l = S.face_list[f];
+                    if (l < 0 || l >= S.n_lists) {
+                        atomicOr(A.err, ERR_SHAPE_STACK);
+                        break;
+                    }
+                    if constexpr (FB) try_face_fp64(A, S, f, l, i, dlen, b);
+                }
+            }
+            A.in.len[i] = d_of_ff(b.len);
+            A.in.endf[i] = b.face >= 0 ? (unsigned)S.faces[b.face].idx : 0xFFFFFFFFu;
+            if (b.face >= 0) {
+                atomicAdd(&s_counts[b.face], 1u);
+                atomicAdd(&s_hits, 1u);
             }
         }
-    }
-    // children go to the tile's slot range in parent order: the exclusive
-    // block scan of the per-ray counts is each ray's first slot
-    unsigned tile_children;
-    const unsigned excl = block_scan((unsigned)nc, &tile_children);
-    if (nc > 0) {
-        const double phase = A.in.phase[i];
-        const unsigned wl = A.in.wl[i], ident = A.in.ident[i];
-        const unsigned endf = (unsigned)S.faces[b.face].idx;
-        const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
-        for (int k = 0; k < nc; k++) {
-            if (fp64_children)
-                store_child(A.scratch, slot + k, ccd, chd[k], phase, wl, (unsigned)i, endf, ident);
-            else
-                store_child_f(A.scratch, slot + k, origin, nrm, Eo, opl, ch[k], phase, wl, (unsigned)i, endf, ident);
+        if (!A.emit) continue;
+
+        // ---- material ----
+        int nc = 0;
+        ChildF ch[2];
+        f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);
+        double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
+        bool fp64_children = false;
+        Child chd[2];
+        ChildCommon ccd;
+        if (active && b.face >= 0) {
+            const rp_face &F = S.faces[b.face];
+            const MxFace &M = mf[b.face];
+            const MxList &L = ml[b.list];
+            ff P[3];
+            P[0] = ff_add(O[0], ff_mul(b.t, D[0]));
+            P[1] = ff_add(O[1], ff_mul(b.t, D[1]));
+            P[2] = ff_add(O[2], ff_mul(b.t, D[2]));
+            origin[0] = d_of_ff(P[0]);
+            origin[1] = d_of_ff(P[1]);
+            origin[2] = d_of_ff(P[2]);
+            // the hit in the face list's frame, relative to the face vertex
+            ff lp[3];
+            if (L.ident) {
+                lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
+                lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
+                lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
+            } else {
+                ff_rotate(L, P, lp, true);
+            }
+            f3 u = mk3(lp[0].hi + lp[0].lo, lp[1].hi + lp[1].lo, ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)).hi);
+            f3 nl;
+            if (face_normal_f(F, M, u, nl)) {
+                if (F.invert_normal) nl = mk3(-nl.x, -nl.y, -nl.z);
+                nrm = mk3(L.r[0] * nl.x + L.r[1] * nl.y + L.r[2] * nl.z, L.r[3] * nl.x + L.r[4] * nl.y + L.r[5] * nl.z,
+                          L.r[6] * nl.x + L.r[7] * nl.y + L.r[8] * nl.z);
+            } else if constexpr (FB) {
+                nrm = fallback_normal(S, F, b.list, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
+            }
+            if (F.material >= 0) {
+                const rp_material &Mt = S.mats[F.material];
+                const ff lenn = ff_mul(b.len, ff_of_d(A.in.n[i].x));
+                opl = d_of_ff(ff_add(ff_of_d(A.in.opl[i]), lenn));
+                if (mat_specialised(Mt.type)) {
+                    RayF r;
+                    r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
+                    r.E = f3_of_d(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
+                    r.e1 = cf_of_d(A.in.e1[i]);
+                    r.e2 = cf_of_d(A.in.e2[i]);
+                    r.n = A.in.n[i];
+                    r.type = A.in.type[i];
+                    r.wl = A.in.wl[i];
+                    nc = eval_f(S, Mt, r, nrm, Eo, ch, A.err);
+                    nrm = norm3(nrm);
+                    if (A.e2_term > 0.0 && nc > 0) {
+                        int w = 0;
+                        for (int k = 0; k < nc; k++) {
+                            if (!(cabs2(ch[k].e1) + cabs2(ch[k].e2) < e2t)) {
+                                if (w != k) ch[w] = ch[k];
+                                w++;
+                            }
+                        }
+                        if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
+                        nc = w;
+                    }
+                } else if constexpr (FB) {
+                    unsigned term = 0;
+                    nc = fallback_children(A, S, F, Mt, b.list, i, d_of_ff(b.len), origin, nrm, &ccd, chd, &term);
+                    fp64_children = true;
+                    if (term) atomicAdd(&s_term, term);
+                }
+            }
         }
+        // children go to the tile's slot range in parent order: the exclusive
+        // block scan of the per-ray counts is each ray's first slot
+        unsigned tile_children;
+        const unsigned excl = block_scan((unsigned)nc, &tile_children);
+        if (nc > 0) {
+            const double phase = A.in.phase[i];
+            const unsigned wl = A.in.wl[i], ident = A.in.ident[i];
+            const unsigned endf = (unsigned)S.faces[b.face].idx;
+            const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
+            for (int k = 0; k < nc; k++) {
+                if (FB && fp64_children)
+                    store_child(A.scratch, slot + k, ccd, chd[k], phase, wl, (unsigned)i, endf, ident);
+                else
+                    store_child_f(A.scratch, slot + k, origin, nrm, Eo, opl, ch[k], phase, wl, (unsigned)i, endf,
+                                  ident);
+            }
+        }
+        if (threadIdx.x == 0) A.tile_counts[tile] = tile_children;
     }
     flush_counts(A, S, s_counts);
-    if (threadIdx.x == 0) A.tile_counts[tile] = tile_children;
     if (threadIdx.x == 0) {
         atomicAdd(&A.stats[0], (unsigned long long)s_hits);
         if (s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
     }
 }
 
+// Resident blocks per SM for one instantiation and shared-memory size, cached.
+template <bool FB>
+static cudaError_t mixed_grid_blocks(size_t total, int *blocks) {
+    static int cached_dev = -1, cached_blocks = 0;
+    static size_t cached_total = 0;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev != cached_dev || total != cached_total) {
+        if (total > 48 * 1024) {
+            e = cudaFuncSetAttribute(generation_mixed_kernel<FB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)total);
+            if (e != cudaSuccess) return e;
+        }
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, generation_mixed_kernel<FB>, RP_BLOCK, total);
+        if (e != cudaSuccess) return e;
+        cached_blocks = (per_sm > 0 ? per_sm : 1) * sms;
+        cached_dev = dev;
+        cached_total = total;
+    }
+    *blocks = cached_blocks;
+    return cudaSuccess;
+}
+
+// The scene's faces and materials decide the instantiation: without FP64
+// fallbacks the kernel carries no out-of-line calls and their register cost.
 cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st) {
     if (a.n_in == 0) return cudaSuccess;
-    const size_t off = (smem + 15) & ~(size_t)15;
-    const size_t total = off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
+    const size_t mx_off = (smem + 15) & ~(size_t)15;
+    const size_t tb_off = mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
+    const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
+    const size_t total = tb_off + (size_t)nmask * RP_BLOCK * sizeof(float);
     if (total > 220 * 1024) return cudaErrorInvalidConfiguration;  // scene too large for the per-block tables
-    unsigned grid = (unsigned)((a.n_in + RP_BLOCK - 1) / RP_BLOCK);
-    static size_t configured = 0;
-    if (total > 48 * 1024 && total > configured) {
-        cudaError_t e = cudaFuncSetAttribute(generation_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)total);
-        if (e != cudaSuccess) return e;
-        configured = total;
-    }
-    generation_mixed_kernel<<<grid, RP_BLOCK, total, st>>>(a, (unsigned)off);
+    int blocks = 0;
+    cudaError_t e = a.mixed_fallback ? mixed_grid_blocks<true>(total, &blocks) : mixed_grid_blocks<false>(total, &blocks);
+    if (e != cudaSuccess) return e;
+    const unsigned long long n_tiles = (a.n_in + RP_BLOCK - 1) / RP_BLOCK;
+    const unsigned grid = (unsigned)(n_tiles < (unsigned long long)blocks ? n_tiles : blocks);
+    if (a.mixed_fallback)
+        generation_mixed_kernel<true><<<grid, RP_BLOCK, total, st>>>(a, (unsigned)mx_off, (unsigned)tb_off);
+    else
+        generation_mixed_kernel<false><<<grid, RP_BLOCK, total, st>>>(a, (unsigned)mx_off, (unsigned)tb_off);
     return cudaGetLastError();
 }
 
