@@ -97,6 +97,28 @@ __device__ __forceinline__ ff ff_sqrt(ff a) {
 __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool ff_eq(ff a, ff b) { return a.hi == b.hi && a.lo == b.lo; }
 
+struct ff3 {
+    ff x, y, z;
+};
+__device__ __forceinline__ ff3 mkff3(ff x, ff y, ff z) {
+    ff3 r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    return r;
+}
+__device__ __forceinline__ ff ff_dot3(const ff3 &a, const ff3 &b) {
+    return ff_add(ff_add(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_mul(a.z, b.z));
+}
+__device__ __forceinline__ ff3 ff3_scale(const ff3 &a, ff s) { return mkff3(ff_mul(a.x, s), ff_mul(a.y, s), ff_mul(a.z, s)); }
+__device__ __forceinline__ ff3 ff3_sub(const ff3 &a, const ff3 &b) {
+    return mkff3(ff_sub(a.x, b.x), ff_sub(a.y, b.y), ff_sub(a.z, b.z));
+}
+__device__ __forceinline__ ff3 ff3_neg(const ff3 &a) { return mkff3(ff_neg(a.x), ff_neg(a.y), ff_neg(a.z)); }
+__device__ __forceinline__ ff3 ff3_unit(const ff3 &a) {
+    return ff3_scale(a, ff_div(ffm(1.0f, 0.0f), ff_sqrt(ff_dot3(a, a))));
+}
+
 // ---- conversions on the integer pipe ---------------------------------------
 // double -> float, round to nearest even; magnitudes below 2^-126 flush to a
 // signed zero, above the float range to infinity.
@@ -176,15 +198,15 @@ __device__ __forceinline__ float cabs2(cf z) { return z.x * z.x + z.y * z.y; }
 __device__ __forceinline__ cf cf_of_d(double2 z) { return cfm(f_of_d(z.x), f_of_d(z.y)); }
 
 // ---- per-block tables ----------------------------------------------------------
-// A face list's maps in the forms used here: global -> local as float-float
-// (rotation and translation) with a flag for an identity rotation, and the
-// local -> global rotation in FP32 for normals.
+// A face list's maps in the forms used here, as float-float: global -> local
+// (rotation and translation) and the local -> global rotation for normals,
+// with a flag for an identity rotation.
 struct MxList {
     float ri_hi[9], ri_lo[9];
     float ti_hi[3], ti_lo[3];
-    float r[9];
+    float r_hi[9], r_lo[9];
     int ident;
-    int pad[2];
+    int pad[1];
 };
 // A face's parameters in FP32, its plane / vertex height as float-float and its
 // smallest accepted ray parameter (tolerance * max_length, the reference's
@@ -224,7 +246,9 @@ __device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace
             ff v = ff_of_d(L.inv_trans.m[k]);
             o.ri_hi[k] = v.hi;
             o.ri_lo[k] = v.lo;
-            o.r[k] = f_of_d(L.trans.m[k]);
+            ff w = ff_of_d(L.trans.m[k]);
+            o.r_hi[k] = w.hi;
+            o.r_lo[k] = w.lo;
         }
         for (int k = 0; k < 3; k++) {
             ff v = ff_of_d(L.inv_trans.t[k]);
@@ -232,8 +256,11 @@ __device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace
             o.ti_lo[k] = v.lo;
         }
         const double *m = L.inv_trans.m;
+        const double *w = L.trans.m;
         o.ident = (m[0] == 1.0 && m[4] == 1.0 && m[8] == 1.0 && m[1] == 0.0 && m[2] == 0.0 && m[3] == 0.0 &&
-                   m[5] == 0.0 && m[6] == 0.0 && m[7] == 0.0);
+                   m[5] == 0.0 && m[6] == 0.0 && m[7] == 0.0) &&
+                  (w[0] == 1.0 && w[4] == 1.0 && w[8] == 1.0 && w[1] == 0.0 && w[2] == 0.0 && w[3] == 0.0 &&
+                   w[5] == 0.0 && w[6] == 0.0 && w[7] == 0.0);
     }
     for (int f = threadIdx.x; f < A.S.n_faces; f += blockDim.x) {
         const rp_face &F = A.S.faces[f];
@@ -524,39 +551,43 @@ __device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const
     }
 }
 
-// FP32 normal of a specialised face at a point in vertex coordinates; false
-// for faces left to the FP64 path.
-__device__ __forceinline__ bool face_normal_f(const rp_face &F, const MxFace &M, f3 u, f3 &n) {
+// Unit normal of a specialised face in float-float at a hit given in vertex
+// coordinates (x, y and z relative to the vertex); false for faces left to the
+// FP64 path.  Face parameters are the FP32 copies.
+__device__ __forceinline__ bool face_normal_ff(const rp_face &F, const MxFace &M, ff x, ff y, ff z, ff3 &n) {
+    const ff zero = ffm(0.0f, 0.0f);
     switch (F.type) {
-        case RP_FACE_CIRCULAR: n = mk3(0.0f, 0.0f, F.invert_normals ? 1.0f : -1.0f); return true;
-        case RP_FACE_SHAPED_PLANAR: n = mk3(0.0f, 0.0f, 1.0f); return true;
-        case RP_FACE_RECTANGULAR: n = mk3(0.0f, 0.0f, -1.0f); return true;
+        case RP_FACE_CIRCULAR: n = mkff3(zero, zero, ffm(F.invert_normals ? 1.0f : -1.0f, 0.0f)); return true;
+        case RP_FACE_SHAPED_PLANAR: n = mkff3(zero, zero, ffm(1.0f, 0.0f)); return true;
+        case RP_FACE_RECTANGULAR: n = mkff3(zero, zero, ffm(-1.0f, 0.0f)); return true;
         case RP_FACE_SPHERICAL:
-        case RP_FACE_SHAPED_SPHERICAL: {  // cfaces.pyx:485-498, 594-606
+        case RP_FACE_SHAPED_SPHERICAL: {  // cfaces.pyx:485-498, 594-606: (p - centre), flipped for c < 0
             float c = F.type == RP_FACE_SPHERICAL ? M.p[1] : M.p[0];
-            f3 q = mk3(u.x, u.y, u.z + c);
-            if (c < 0.0f) q = mk3(-q.x, -q.y, -q.z);
-            n = norm3(q);
+            ff3 q = mkff3(x, y, ff_add_f(z, c));
+            if (c < 0.0f) q = ff3_neg(q);
+            n = ff3_unit(q);
             return true;
         }
         case RP_FACE_CONIC: {  // cfaces.pyx:1796-1820
             float Rq = -M.p[0], beta = 1.0f + M.p[2];
             float sign = F.invert_normals ? -1.0f : 1.0f;
             if (Rq * beta < 0.0f) sign = -sign;
-            f3 g = mk3(-u.x * 2.0f * beta, -u.y * 2.0f * beta, 2.0f * beta * (Rq - beta * u.z));
-            n = norm3(mul3(g, sign));
+            ff3 g = mkff3(ff_mul_f(x, -2.0f * beta * sign), ff_mul_f(y, -2.0f * beta * sign),
+                          ff_mul_f(ff_add_f(ff_mul_f(z, -beta), Rq), 2.0f * beta * sign));
+            n = ff3_unit(g);
             return true;
         }
         case RP_FACE_ASPHERIC: {  // cfaces.pyx:1976-2005
             float Rq = -M.p[0], beta = 1.0f + M.p[2];
             float sign = F.invert_normals ? -1.0f : 1.0f;
-            float r2 = u.x * u.x + u.y * u.y;
+            float xf = x.hi + x.lo, yf = y.hi + y.lo;
+            float r2 = xf * xf + yf * yf;
             float root = sqrtf(1.0f - beta * r2 / (Rq * Rq));
             float df = r2 * (4.0f * M.p[3] + r2 * (6.0f * M.p[4] + r2 * (8.0f * M.p[5] + r2 * (10.0f * M.p[6] +
                        r2 * (12.0f * M.p[7] + r2 * (14.0f * M.p[8] + r2 * 16.0f * M.p[9]))))));
             float inv = 1.0f / (Rq * (1.0f + root));
             df += 2.0f * inv + beta * r2 * inv * inv / (Rq * root);
-            n = norm3(mul3(mk3(-df * u.x, -df * u.y, 1.0f), sign));
+            n = ff3_unit(mkff3(ff_mul_f(x, -df * sign), ff_mul_f(y, -df * sign), ffm(sign, 0.0f)));
             return true;
         }
         default: return false;
@@ -572,7 +603,7 @@ struct RayF {
     unsigned type, wl;
 };
 struct ChildF {
-    f3 d;
+    ff3 d;
     cf e1, e2;
     double2 n;
     unsigned type;
@@ -606,56 +637,65 @@ __device__ __forceinline__ bool mat_specialised(int type) {
 
 // Children of a hit for the specialised materials (cmaterials.pyx:260-278
 // Transparent, 292-319 PEC, 589-680 Dielectric, 756-872 FullDielectric,
-// 897-1013 FullDielectricDispersive).  Eo receives the children's shared
-// E_vector; returns the number of children.
-__device__ int eval_f(const DevScene &S, const rp_material &m, const RayF &r, f3 normal, f3 &Eo, ChildF *ch,
-                      unsigned *err) {
+// 897-1013 FullDielectricDispersive).  Directions (reflection, Snell's law) are
+// float-float from the float-float ray direction D, its unit vector ind and
+// the unit normal nn; the S/P projection, Fresnel coefficients and amplitudes
+// are FP32.  Eo receives the children's shared E_vector; returns the number of
+// children.
+__device__ int eval_f(const DevScene &S, const rp_material &m, const RayF &r, const ff3 &D, const ff3 &ind,
+                      const ff3 &nn, f3 &Eo, ChildF *ch, unsigned *err) {
     if (m.type == RP_MAT_NONE || m.type == RP_MAT_OPAQUE) return 0;
-    normal = norm3(normal);
-    const f3 d = r.d, ind = norm3(d);
+    const f3 normal = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
     cf E1, E2;
-    sp_f(d, r.E, r.e1, r.e2, normal, Eo, E1, E2);
+    sp_f(r.d, r.E, r.e1, r.e2, normal, Eo, E1, E2);
     if (m.type == RP_MAT_TRANSPARENT) {
-        ch[0].d = d;
+        ch[0].d = D;
         ch[0].n = r.n;
         ch[0].e1 = E1;
         ch[0].e2 = E2;
         ch[0].type = r.type & ~RP_REFL_RAY;
         return 1;
     }
-    const float cosTheta = dot3(normal, m.type == RP_MAT_PEC ? d : ind);
-    const f3 ctn = mul3(normal, cosTheta);
+    const ff cosT = ff_dot3(nn, m.type == RP_MAT_PEC ? D : ind);
+    const ff3 ctn2 = ff3_scale(nn, ff_mul_f(cosT, 2.0f));
     if (m.type == RP_MAT_PEC) {
-        ch[0].d = sub3(d, mul3(ctn, 2.0f));
+        ch[0].d = ff3_sub(D, ctn2);
         ch[0].n = r.n;
         ch[0].e1 = cfm(-E1.x, -E1.y);
         ch[0].e2 = E2;
         ch[0].type = r.type | RP_REFL_RAY;
         return 1;
     }
+    const float cosTheta = cosT.hi;
     const float cos1 = fabsf(cosTheta);
     const bool out_to_in = cosTheta < 0.0f;
     const float flip = out_to_in ? 1.0f : -1.0f;
+    // Snell's law in vector form: tg2 = (ind - cos n) n1/n2, t = tg2 - n sqrt(1 - |tg2|^2) flip
+    auto refract = [&](ff ratio, float &cos2) -> ff3 {
+        ff3 tg2 = ff3_scale(ff3_sub(ind, ff3_scale(nn, cosT)), ratio);
+        ff c2 = ff_sqrt(ff_sub(ffm(1.0f, 0.0f), ff_dot3(tg2, tg2)));
+        ff3 tr = ff3_sub(tg2, ff3_scale(nn, ff_mul_f(c2, flip)));
+        cos2 = fabsf(ff_dot3(tr, nn).hi);
+        return tr;
+    };
     if (m.type == RP_MAT_DIELECTRIC) {
-        float n1 = f_of_d(out_to_in ? m.n_outside[0] : m.n_inside[0]);
-        float n2 = f_of_d(out_to_in ? m.n_inside[0] : m.n_outside[0]);
+        const double n1d = out_to_in ? m.n_outside[0] : m.n_inside[0];
+        const double n2d = out_to_in ? m.n_inside[0] : m.n_outside[0];
+        const float n1 = f_of_d(n1d), n2 = f_of_d(n2d);
         ch[0].n = out_to_in ? make_double2(m.n_inside[0], m.n_inside[1]) : make_double2(m.n_outside[0], m.n_outside[1]);
         float q = n2 / n1;
         float N2_sin2 = cosTheta * cosTheta + (q * q - 1.0f);
         if (N2_sin2 < 0.0f) {
-            ch[0].d = sub3(ind, mul3(ctn, 2.0f));
+            ch[0].d = ff3_sub(ind, ctn2);
             ch[0].e1 = cfm(-E1.x, -E1.y);
             ch[0].e2 = cfm(-E2.x, -E2.y);
             ch[0].type = r.type | RP_REFL_RAY;
         } else {
-            f3 tg2 = mul3(sub3(ind, ctn), n1 / n2);
-            float c2 = sqrtf(1.0f - dot3(tg2, tg2));
-            f3 tr = sub3(tg2, mul3(normal, c2 * flip));
-            float cos2 = fabsf(dot3(tr, normal));
+            float cos2;
+            ch[0].d = refract(ff_div(ff_of_d(n1d), ff_of_d(n2d)), cos2);
             float aspect = sqrtf(cos2 / cos1) * (2.0f * n1) * cos1;
             float T_p = aspect / (n2 * cos1 + n1 * cos2);
             float T_s = aspect / (n2 * cos2 + n1 * cos1);
-            ch[0].d = tr;
             ch[0].e1 = cmuls(E1, T_s);
             ch[0].e2 = cmuls(E2, T_p);
             ch[0].type = r.type & ~RP_REFL_RAY;
@@ -689,22 +729,20 @@ __device__ int eval_f(const DevScene &S, const rp_material &m, const RayF &r, f3
     cf R_s = cmul(cdiv(csub(n1c1, n2c2), den_s), E1);
     int nc = 0;
     if ((n1.x * (cabs2(R_s) + cabs2(R_p))) / P_in > f_of_d(m.reflection_threshold)) {
-        ch[0].d = sub3(ind, mul3(ctn, 2.0f));
+        ch[0].d = ff3_sub(ind, ctn2);
         ch[0].e1 = R_s;
         ch[0].e2 = cfm(-R_p.x, -R_p.y);
         ch[0].n = n1d;
         ch[0].type = r.type | RP_REFL_RAY;
         nc = 1;
     }
-    f3 tg2 = mul3(sub3(ind, ctn), n1.x / n2.x);
-    float c2 = sqrtf(1.0f - dot3(tg2, tg2));
-    f3 tr = sub3(tg2, mul3(normal, c2 * flip));
     float aspect = sqrtf(cos2.x / cos1);
     cf num = cmuls(n1, 2.0f * cos1 * aspect);
     cf T_p = cmul(cdiv(num, den_p), E2);
     cf T_s = cmul(cdiv(num, den_s), E1);
     if ((n2.x * (cabs2(T_s) + cabs2(T_p))) / P_in > f_of_d(m.transmission_threshold)) {
-        ch[nc].d = tr;
+        float c2unused;
+        ch[nc].d = refract(ff_div(ff_of_d(n1d.x), ff_of_d(n2d.x)), c2unused);
         ch[nc].e1 = T_s;
         ch[nc].e2 = T_p;
         ch[nc].n = n2d;
@@ -721,9 +759,9 @@ __device__ __forceinline__ void store_child_f(const RaySoA &out, unsigned long l
     out.ox[k] = origin[0];
     out.oy[k] = origin[1];
     out.oz[k] = origin[2];
-    out.dx[k] = d_of_f(c.d.x);
-    out.dy[k] = d_of_f(c.d.y);
-    out.dz[k] = d_of_f(c.d.z);
+    out.dx[k] = d_of_ff(c.d.x);
+    out.dy[k] = d_of_ff(c.d.y);
+    out.dz[k] = d_of_ff(c.d.z);
     out.nx[k] = d_of_f(normal.x);
     out.ny[k] = d_of_f(normal.y);
     out.nz[k] = d_of_f(normal.z);
@@ -1011,7 +1049,7 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
         // ---- material ----
         int nc = 0;
         ChildF ch[2];
-        f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);
+        f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);  // unit normal (FP32 copy), E_vector
         double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
         bool fp64_children = false;
         Child chd[2];
@@ -1036,15 +1074,23 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
             } else {
                 ff_rotate(L, P, lp, true);
             }
-            f3 u = mk3(lp[0].hi + lp[0].lo, lp[1].hi + lp[1].lo, ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)).hi);
-            f3 nl;
-            if (face_normal_f(F, M, u, nl)) {
-                if (F.invert_normal) nl = mk3(-nl.x, -nl.y, -nl.z);
-                nrm = mk3(L.r[0] * nl.x + L.r[1] * nl.y + L.r[2] * nl.z, L.r[3] * nl.x + L.r[4] * nl.y + L.r[5] * nl.z,
-                          L.r[6] * nl.x + L.r[7] * nl.y + L.r[8] * nl.z);
+            ff3 nn;
+            if (face_normal_ff(F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
+                if (F.invert_normal) nn = ff3_neg(nn);
+                if (!L.ident) {
+                    ff v[3] = {nn.x, nn.y, nn.z}, w[3];
+#pragma unroll
+                    for (int rr = 0; rr < 3; rr++)
+                        w[rr] = ff_add(ff_add(ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr), v[0]),
+                                              ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 1), v[1])),
+                                       ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 2), v[2]));
+                    nn = mkff3(w[0], w[1], w[2]);
+                }
             } else if constexpr (FB) {
-                nrm = fallback_normal(S, F, b.list, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
+                f3 n32 = fallback_normal(S, F, b.list, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
+                nn = mkff3(ffm(n32.x, 0.0f), ffm(n32.y, 0.0f), ffm(n32.z, 0.0f));
             }
+            nrm = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
             if (F.material >= 0) {
                 const rp_material &Mt = S.mats[F.material];
                 const ff lenn = ff_mul(b.len, ff_of_d(A.in.n[i].x));
@@ -1058,8 +1104,9 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
                     r.n = A.in.n[i];
                     r.type = A.in.type[i];
                     r.wl = A.in.wl[i];
-                    nc = eval_f(S, Mt, r, nrm, Eo, ch, A.err);
-                    nrm = norm3(nrm);
+                    const ff3 Dff = mkff3(D[0], D[1], D[2]);
+                    const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
+                    nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
                     if (A.e2_term > 0.0 && nc > 0) {
                         int w = 0;
                         for (int k = 0; k < nc; k++) {
