@@ -893,6 +893,63 @@ __device__ __noinline__ void try_face_fp64(const GenArgs &A, const DevScene &S, 
     keep_nearest(dist, ff_div(dist, dlen), f, l, b);
 }
 
+// ---- input prefetch ----------------------------------------------------------
+// One tile's input fields in shared memory (structure of arrays, one slot per
+// thread).  Each thread copies its own ray's fields with cp.async, so a tile's
+// loads are in flight while the previous tile computes, and a thread waits
+// only for its own copies (cp.async.wait_group).
+struct TileIn {
+    double ox[RP_BLOCK], oy[RP_BLOCK], oz[RP_BLOCK], dx[RP_BLOCK], dy[RP_BLOCK], dz[RP_BLOCK];
+    double ex[RP_BLOCK], ey[RP_BLOCK], ez[RP_BLOCK];
+    double2 n[RP_BLOCK], e1[RP_BLOCK], e2[RP_BLOCK];
+    double opl[RP_BLOCK], phase[RP_BLOCK];
+    unsigned wl[RP_BLOCK], type[RP_BLOCK], ident[RP_BLOCK], pad[RP_BLOCK];
+};
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Queues the copy of ray i's fields into slot threadIdx.x of `buf` (nothing
+// for i beyond the generation) and closes the thread's copy group.
+__device__ __forceinline__ void prefetch_ray(TileIn *buf, const RaySoA &in, unsigned long long i, unsigned long long n) {
+    if (i < n) {
+        const unsigned t = threadIdx.x;
+        cp_async8(&buf->ox[t], &in.ox[i]);
+        cp_async8(&buf->oy[t], &in.oy[i]);
+        cp_async8(&buf->oz[t], &in.oz[i]);
+        cp_async8(&buf->dx[t], &in.dx[i]);
+        cp_async8(&buf->dy[t], &in.dy[i]);
+        cp_async8(&buf->dz[t], &in.dz[i]);
+        cp_async8(&buf->ex[t], &in.ex[i]);
+        cp_async8(&buf->ey[t], &in.ey[i]);
+        cp_async8(&buf->ez[t], &in.ez[i]);
+        cp_async16(&buf->n[t], &in.n[i]);
+        cp_async16(&buf->e1[t], &in.e1[i]);
+        cp_async16(&buf->e2[t], &in.e2[i]);
+        cp_async8(&buf->opl[t], &in.opl[i]);
+        cp_async8(&buf->phase[t], &in.phase[i]);
+        cp_async4(&buf->wl[t], &in.wl[i]);
+        cp_async4(&buf->type[t], &in.type[i]);
+        cp_async4(&buf->ident[t], &in.ident[i]);
+    }
+    cp_async_commit();
+}
+
 }  // namespace mx
 
 __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
@@ -918,10 +975,12 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
 // Dynamic shared memory: the plain kernel's tables, the mixed tables at mx_off
 // and, at tb_off, each thread's box-entry distance per culled face.
 template <bool FB>
-__global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A, unsigned mx_off, unsigned tb_off) {
+__global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A, unsigned mx_off, unsigned tb_off,
+                                                                      unsigned in_off) {
     using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_hits, s_term, s_tile;
+    TileIn *bufs = reinterpret_cast<TileIn *>(smem + in_off);  // two tiles, double-buffered
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
     MxList *ml = reinterpret_cast<MxList *>(smem + mx_off);
@@ -936,12 +995,25 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
     const unsigned long long n_tiles = (A.n_in + RP_BLOCK - 1) / RP_BLOCK;
     const float e2t = f_of_d(A.e2_term);
 
-    for (;;) {
-        __syncthreads();  // every thread is done with the previous tile's s_tile and scan
+    // tiles come from a launch-wide counter; the next tile's inputs are copied
+    // into the other buffer while this one is traced
+    if (threadIdx.x == 0) s_tile = atomicAdd(A.tile_next, 1u);
+    __syncthreads();
+    unsigned tile = s_tile;
+    if (tile < n_tiles) prefetch_ray(&bufs[0], A.in, (unsigned long long)tile * RP_BLOCK + threadIdx.x, A.n_in);
+    for (unsigned k = 0;; k++) {
+        if (tile >= n_tiles) break;
+        __syncthreads();  // every thread has read s_tile and finished the previous tile's scan
         if (threadIdx.x == 0) s_tile = atomicAdd(A.tile_next, 1u);
         __syncthreads();
-        const unsigned tile = s_tile;
-        if (tile >= n_tiles) break;
+        const unsigned next = s_tile;
+        if (next < n_tiles)
+            prefetch_ray(&bufs[(k + 1) & 1], A.in, (unsigned long long)next * RP_BLOCK + threadIdx.x, A.n_in);
+        else
+            cp_async_commit();
+        cp_async_wait_prev();  // this thread's copies for `tile` have landed
+        const TileIn &in = bufs[k & 1];
+        const unsigned t = threadIdx.x;
         const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
         const bool active = i < A.n_in;
 
@@ -952,12 +1024,12 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
         b.list = -1;
         ff O[3], D[3], dlen = ffm(1.0f, 0.0f);
         if (active) {
-            O[0] = ff_of_d(A.in.ox[i]);
-            O[1] = ff_of_d(A.in.oy[i]);
-            O[2] = ff_of_d(A.in.oz[i]);
-            D[0] = ff_of_d(A.in.dx[i]);
-            D[1] = ff_of_d(A.in.dy[i]);
-            D[2] = ff_of_d(A.in.dz[i]);
+            O[0] = ff_of_d(in.ox[t]);
+            O[1] = ff_of_d(in.oy[t]);
+            O[2] = ff_of_d(in.oz[t]);
+            D[0] = ff_of_d(in.dx[t]);
+            D[1] = ff_of_d(in.dy[t]);
+            D[2] = ff_of_d(in.dz[t]);
             dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
             int cur = -1;
             LRay R;
@@ -1044,7 +1116,10 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
                 atomicAdd(&s_hits, 1u);
             }
         }
-        if (!A.emit) continue;
+        if (!A.emit) {
+            tile = next;
+            continue;
+        }
 
         // ---- material ----
         int nc = 0;
@@ -1093,17 +1168,17 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
             nrm = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
             if (F.material >= 0) {
                 const rp_material &Mt = S.mats[F.material];
-                const ff lenn = ff_mul(b.len, ff_of_d(A.in.n[i].x));
-                opl = d_of_ff(ff_add(ff_of_d(A.in.opl[i]), lenn));
+                const ff lenn = ff_mul(b.len, ff_of_d(in.n[t].x));
+                opl = d_of_ff(ff_add(ff_of_d(in.opl[t]), lenn));
                 if (mat_specialised(Mt.type)) {
                     RayF r;
                     r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
-                    r.E = f3_of_d(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
-                    r.e1 = cf_of_d(A.in.e1[i]);
-                    r.e2 = cf_of_d(A.in.e2[i]);
-                    r.n = A.in.n[i];
-                    r.type = A.in.type[i];
-                    r.wl = A.in.wl[i];
+                    r.E = f3_of_d(in.ex[t], in.ey[t], in.ez[t]);
+                    r.e1 = cf_of_d(in.e1[t]);
+                    r.e2 = cf_of_d(in.e2[t]);
+                    r.n = in.n[t];
+                    r.type = in.type[t];
+                    r.wl = in.wl[t];
                     const ff3 Dff = mkff3(D[0], D[1], D[2]);
                     const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
                     nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
@@ -1131,8 +1206,8 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
         unsigned tile_children;
         const unsigned excl = block_scan((unsigned)nc, &tile_children);
         if (nc > 0) {
-            const double phase = A.in.phase[i];
-            const unsigned wl = A.in.wl[i], ident = A.in.ident[i];
+            const double phase = in.phase[t];
+            const unsigned wl = in.wl[t], ident = in.ident[t];
             const unsigned endf = (unsigned)S.faces[b.face].idx;
             const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
             for (int k = 0; k < nc; k++) {
@@ -1144,6 +1219,7 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
             }
         }
         if (threadIdx.x == 0) A.tile_counts[tile] = tile_children;
+        tile = next;
     }
     flush_counts(A, S, s_counts);
     if (threadIdx.x == 0) {
@@ -1185,7 +1261,8 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
     const size_t mx_off = (smem + 15) & ~(size_t)15;
     const size_t tb_off = mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
     const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
-    const size_t total = tb_off + (size_t)nmask * RP_BLOCK * sizeof(float);
+    const size_t in_off = (tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
+    const size_t total = in_off + 2 * sizeof(mx::TileIn);
     if (total > 220 * 1024) return cudaErrorInvalidConfiguration;  // scene too large for the per-block tables
     int blocks = 0;
     cudaError_t e = a.mixed_fallback ? mixed_grid_blocks<true>(total, &blocks) : mixed_grid_blocks<false>(total, &blocks);
@@ -1193,9 +1270,11 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
     const unsigned long long n_tiles = (a.n_in + RP_BLOCK - 1) / RP_BLOCK;
     const unsigned grid = (unsigned)(n_tiles < (unsigned long long)blocks ? n_tiles : blocks);
     if (a.mixed_fallback)
-        generation_mixed_kernel<true><<<grid, RP_BLOCK, total, st>>>(a, (unsigned)mx_off, (unsigned)tb_off);
+        generation_mixed_kernel<true><<<grid, RP_BLOCK, total, st>>>(a, (unsigned)mx_off, (unsigned)tb_off,
+                                                                     (unsigned)in_off);
     else
-        generation_mixed_kernel<false><<<grid, RP_BLOCK, total, st>>>(a, (unsigned)mx_off, (unsigned)tb_off);
+        generation_mixed_kernel<false><<<grid, RP_BLOCK, total, st>>>(a, (unsigned)mx_off, (unsigned)tb_off,
+                                                                      (unsigned)in_off);
     return cudaGetLastError();
 }
 
