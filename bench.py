@@ -5,8 +5,11 @@ system with per-ray Sellmeier dispersion and Fresnel splitting, 8
 generations, |E|^2 < 1e-6 termination (raypier_optics_gb300.workloads.config2).
 One step = one full trace_rays of that workload.
 
-  value  ray-segments/s with the input rays already resident in HBM
-         (rp_trace_rays on a device buffer; scene uploaded once)
+  value  ray-segments/s of the mixed FP32 / float-float path with the input
+         rays already resident in HBM (rp_trace_rays on a device buffer; scene
+         uploaded once); `plain_fp64` holds the all-FP64 path on the same
+         workload and `precision_vs_plain_fp64` the mixed path's error
+         against it (--flags plain makes the FP64 path the headline)
   e2e    the same metric through the C-ABI host-buffer call
          rp_trace_rays_host: pinned host input records -> device -> all
          generations back into pinned host memory, copies inside the timing
@@ -45,6 +48,10 @@ UNIT = "ray-segments/s"
 # per-ray wavelength (8); written back: length, end_face_idx (12)
 BYTES_PER_SEGMENT = 72 + 48 + 16 + 12 + 8 + 12
 BYTES_PER_CHILD = 188
+# DRAM bytes per input ray of one generation launch (dram__bytes_read.sum +
+# dram__bytes_write.sum from ncu on generation 3 of the 262,144-ray config-2
+# trace, 1,046,875 rays; profiles/traffic_generation_placement_config2_262144rays.md)
+NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 403.5, "generation_mixed_kernel": 423.6}
 
 
 def parse():
@@ -54,11 +61,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
-    ap.add_argument("--flags", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--flags", default="mixed", choices=["plain", "mixed"])
     ap.add_argument("--rays", type=int, default=0, help="override the ray count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
-    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the second path's leg (plain FP64 when the "
+                    "headline is mixed, mixed when it is plain) and the precision sample")
     ap.add_argument("--cpu-sample", type=int, default=0, help="rays in the CPU-baseline sample")
     return ap.parse_args()
 
@@ -275,13 +283,15 @@ def main():
     segs = stats.rays_in
     children = stats.rays_out
     seg_per_step = segs / args.steps
-    mixed = None
-    if flags == 0 and not args.no_mixed:
-        mst, mdev_s, mwall, _, _, mvalue = timed(1, False)
-        mixed = {"value": mvalue, "unit": UNIT, "ms_per_step": 1000.0 * mdev_s / args.steps,
-                 "speedup_vs_plain_fp64": mvalue / value, "kernel": "generation_mixed_kernel",
-                 "kernel_ms_per_step": mst.kernel_ms / args.steps,
-                 "precision_vs_plain_fp64": precision_sample(ctx, spec, rays, wl, P, per_ray)}
+    other = None
+    if not args.no_mixed:
+        ost, odev_s, _, _, _, ovalue = timed(1 - flags, False)
+        other = {"value": ovalue, "unit": UNIT, "ms_per_step": 1000.0 * odev_s / args.steps,
+                 "kernel": "generation_mixed_kernel" if flags == 0 else "generation_plain_kernel",
+                 "kernel_ms_per_step": ost.kernel_ms / args.steps}
+        mixed_v, plain_v = (ovalue, value) if flags == 0 else (value, ovalue)
+        other["speedup_mixed_vs_plain_fp64"] = mixed_v / plain_v
+        other["precision_vs_plain_fp64"] = precision_sample(ctx, spec, rays, wl, P, per_ray)
     # roofline of the generation kernel
     alg_bytes = segs * BYTES_PER_SEGMENT + children * BYTES_PER_CHILD
     kern_s = stats.kernel_ms / 1000.0
@@ -295,7 +305,7 @@ def main():
                                             seg_per_step, dist, world)
     if rank == 0:
         emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
-             achieved, peak, peak_kind, flags, stats, clk, cpu, mixed)
+             achieved, peak, peak_kind, flags, stats, clk, cpu, other)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -365,12 +375,13 @@ def precision_sample(ctx, spec, rays, wl, P, per_ray, n_sample=16384):
 
 
 def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
-         achieved, peak, peak_kind, flags, stats, clk, cpu, mixed=None):
+         achieved, peak, peak_kind, flags, stats, clk, cpu, other=None):
+    kernel = "generation_plain_kernel" if flags == 0 else "generation_mixed_kernel"
     if True:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if flags == 0 else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if flags == 0 else "f32+float-float",
             "data": "synthetic (seeded PCG64 rays; no dataset)",
             "config": {"workload": f"{args.workload}: {n} rays, {len(faces)} faces, {rl} generations, "
                                    f"|E|^2<{e2} termination, path={args.flags}",
@@ -382,15 +393,17 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
                      "d2h_bytes_per_step": int(d2h / e2e_steps), "steps": e2e_steps,
                      "api": "rp_trace_rays_host (pinned host records in and out)"} if e2e_value else None),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": "generation_plain_kernel" if flags == 0 else "generation_mixed_kernel",
+                         "frac": achieved / peak,
+                         "traffic": NCU_TRAFFIC_PER_RAY[kernel] * stats.rays_in / max(stats.generations, 1),
+                         "kernel": kernel,
                          "note": f"algorithmic bytes {BYTES_PER_SEGMENT} B/segment + {BYTES_PER_CHILD} B/child "
-                                 f"over summed generation-kernel time; peak {peak_kind}"},
+                                 f"over summed generation-kernel time; peak {peak_kind}; traffic = ncu DRAM "
+                                 f"bytes per input ray x rays per launch (average launch)"},
             "gpu_launches": int(stats.launches),
             "clocks": clk,
         }
-        if mixed is not None:
-            line["mixed"] = mixed
+        if other is not None:
+            line["mixed" if flags == 0 else "plain_fp64"] = other
         if cpu is not None:
             line["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": cpu["kind"],
                                     "sample": cpu["sample"]}
