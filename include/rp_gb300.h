@@ -313,6 +313,41 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *scene, const void *in_records, uin
                        uint64_t *gen_offsets, int32_t max_gens, int32_t *n_gens,
                        rp_stats *stats);
 
+/* ---- differentiable sequential lens ------------------------------------- */
+/* No counterpart in the reference: raypier has no gradients.  A stack of even
+ * aspheres traced in order (each surface an AsphericFace with a circular
+ * aperture, cfaces.pyx:1840-2025, refracting as DielectricMaterial,
+ * cmaterials.pyx:589-680, from n_index[k] to n_index[k+1]) onto an image plane
+ * (CircularFace); the loss is the RMS spot radius of the rays that reach it.
+ * The forward runs the plain path's FP64 face and material arithmetic, so it
+ * equals rp_trace_rays on the same faces bit for bit; the backward is a
+ * hand-written adjoint that recomputes each surface from the ray states the
+ * forward kept.
+ * params[5 * n_surfaces]: curvature[n] (raypier sign, R = -curvature),
+ * conic[n], A4[n], A6[n], thickness[n] (vertex to next vertex; the last one
+ * from the last vertex to the image plane).  Surface 0's vertex is at z0. */
+typedef struct rp_lens_desc {
+    int32_t n_surfaces;            /* 1 .. 64 */
+    int32_t reserved;
+    double z0;
+    double max_length;             /* segment length of the intersection tests (trace max_length) */
+    double atol;                   /* AsphericFace.atol */
+    double tolerance;              /* Face.tolerance */
+    const double *semi_diameter;   /* [n_surfaces] aperture radius */
+    const double *n_index;         /* [n_surfaces + 1] real index before surface 0 and after each surface */
+} rp_lens_desc;
+typedef struct rp_lens rp_lens;
+int rp_lens_create(rp_ctx *ctx, const rp_lens_desc *desc, uint64_t max_rays, rp_lens **out);
+int rp_lens_destroy(rp_lens *lens);
+/* Traces `rays` (origins and directions of a device buffer; unit directions)
+ * and returns the RMS spot radius and the number of rays that reached the
+ * image.  RP_ERR_INVALID when an aperture reaches a conic's rim. */
+int rp_lens_forward(rp_lens *lens, const double *params, const rp_rays *rays, double *loss, uint64_t *n_valid);
+/* d loss / d params of the last forward (same rays, unchanged since). */
+int rp_lens_backward(rp_lens *lens, double *grad);
+/* Image-plane x, y and reached flags of the last forward's first n rays. */
+int rp_lens_image(const rp_lens *lens, double *xy, uint8_t *valid, uint64_t n);
+
 /* Allocation-free rp_trace_segment.  No counterpart in the reference: this is
  * an addition of this library.  Same arguments, results and status codes as
  * rp_trace_segment, for callers that must not allocate device memory during a

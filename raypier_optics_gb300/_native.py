@@ -31,6 +31,7 @@ SOURCES = [
     ("rp_mixed.cu", ["--fmad=true"]),
     ("rp_api.cu", ["--fmad=false"]),
     ("rp_unit.cu", ["--fmad=false"]),
+    ("rp_lens.cu", ["--fmad=false"]),
 ]
 
 
@@ -130,6 +131,12 @@ class SceneDesc(ctypes.Structure):
                 ("aux", ctypes.c_void_p)]
 
 
+class LensDesc(ctypes.Structure):
+    _fields_ = [("n_surfaces", ctypes.c_int32), ("reserved", ctypes.c_int32), ("z0", ctypes.c_double),
+                ("max_length", ctypes.c_double), ("atol", ctypes.c_double), ("tolerance", ctypes.c_double),
+                ("semi_diameter", ctypes.c_void_p), ("n_index", ctypes.c_void_p)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("rays_in", ctypes.c_uint64), ("rays_out", ctypes.c_uint64),
                 ("hits", ctypes.c_uint64), ("terminated", ctypes.c_uint64),
@@ -175,6 +182,11 @@ _SIGS = {
                                 ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(Stats)]),
     "rp_trace_segment_noalloc": (_I, [_P, _P, _P, _P, ctypes.c_float, ctypes.c_uint32, ctypes.c_double,
                                       ctypes.POINTER(Stats)]),
+    "rp_lens_create": (_I, [_P, _P, ctypes.c_uint64, ctypes.POINTER(_P)]),
+    "rp_lens_destroy": (_I, [_P]),
+    "rp_lens_forward": (_I, [_P, _P, _P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]),
+    "rp_lens_backward": (_I, [_P, _P]),
+    "rp_lens_image": (_I, [_P, _P, _P, ctypes.c_uint64]),
     "rp_face_intersect": (_I, [_P, ctypes.c_int32, _P, _P, ctypes.c_uint64, _I, _P]),
     "rp_face_normal": (_I, [_P, ctypes.c_int32, _P, ctypes.c_uint64, _P]),
     "rp_shape_inside": (_I, [_P, ctypes.c_int32, _P, ctypes.c_uint64, _P]),

@@ -3,6 +3,7 @@
 // every entry point returns an rp status code.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -963,6 +964,241 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     CK(cudaStreamSynchronize(ctx->stream));
     out->n = count;
     if (st) st->rays_out += count;
+    return RP_OK;
+}
+
+// ---- differentiable sequential lens --------------------------------------------
+struct rp_lens {
+    rp_ctx *ctx;
+    int n_surf;
+    double z0, max_len, atol, tol;
+    std::vector<double> semi, nidx;
+    uint64_t cap;
+    void *block;
+    size_t bytes;
+    LensArgs a;                   // device pointers; rays / counts of the last forward
+    unsigned blocks_cap;
+    std::vector<double> params;   // of the last forward
+    double n_valid, loss;
+    int have_forward;
+};
+
+static size_t lens_layout(int n_surf, uint64_t cap, size_t off[8]) {
+    const unsigned nb = lens_block_count(cap ? cap : 1);
+    size_t o = 0;
+    off[0] = o; o += align256(sizeof(rp_face) * (n_surf + 1));                   // faces
+    off[1] = o; o += align256(sizeof(double) * (n_surf + 1));                    // indices
+    off[2] = o; o += align256(sizeof(rp_shape_op) * 2 * n_surf);                 // apertures
+    off[3] = o; o += align256(sizeof(double) * 6 * (n_surf + 1) * (cap ? cap : 1));  // states
+    off[4] = o; o += align256(sizeof(double) * 2 * (cap ? cap : 1));             // image points
+    off[5] = o; o += align256(cap ? cap : 1);                                    // valid flags
+    off[6] = o; o += align256(sizeof(double) * 3 * nb);                          // partial sums
+    off[7] = o; o += align256(sizeof(double) * (5 * n_surf + 1) * nb + 64);      // gradient sums, error word
+    return o;
+}
+
+// Face records of the lens for `params` (AsphericFace packing as the Python
+// face classes do; the image plane is a CircularFace).
+static void lens_tables(const rp_lens *L, const double *prm, std::vector<rp_face> &faces,
+                        std::vector<rp_shape_op> &shapes) {
+    const int n = L->n_surf;
+    faces.assign(n + 1, rp_face());
+    shapes.assign(2 * n, rp_shape_op());
+    double z = L->z0;
+    for (int k = 0; k < n; k++) {
+        rp_face &F = faces[k];
+        memset(&F, 0, sizeof F);
+        F.type = RP_FACE_ASPHERIC;
+        F.idx = k;
+        F.material = -1;
+        F.shape = 2 * k;
+        F.base = -1;
+        F.distortion = -1;
+        F.tolerance = L->tol;
+        const double c = prm[k], A4 = prm[2 * n + k], A6 = prm[3 * n + k];
+        F.p[0] = c;
+        F.p[1] = z;
+        F.p[2] = prm[n + k];
+        F.p[3] = A4;
+        F.p[4] = A6;
+        F.p[10] = L->atol;
+        F.p[11] = A6 != 0.0 ? 3.0 : 2.0;
+        F.p[12] = pow(-c, 3.0);
+        rp_shape_op &S = shapes[2 * k];
+        S.op = RP_SHAPE_CIRCLE;
+        S.c = L->semi[k];
+        shapes[2 * k + 1].op = RP_SHAPE_END;
+        z += prm[4 * n + k];
+    }
+    rp_face &I = faces[n];
+    memset(&I, 0, sizeof I);
+    I.type = RP_FACE_CIRCULAR;
+    I.idx = n;
+    I.material = -1;
+    I.shape = -1;
+    I.base = -1;
+    I.distortion = -1;
+    I.tolerance = L->tol;
+    I.p[0] = 1.0e9;  // diameter: the image plane catches every ray
+    I.p[2] = z;
+}
+
+int rp_lens_create(rp_ctx *ctx, const rp_lens_desc *d, uint64_t max_rays, rp_lens **out) {
+    if (!ctx || !d || !out || d->n_surfaces < 1 || d->n_surfaces > 64 || !d->semi_diameter || !d->n_index)
+        return RP_ERR_INVALID;
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    rp_lens *L = new (std::nothrow) rp_lens();
+    if (!L) return RP_ERR_NOMEM;
+    L->ctx = ctx;
+    L->n_surf = d->n_surfaces;
+    L->z0 = d->z0;
+    L->max_len = d->max_length;
+    L->atol = d->atol;
+    L->tol = d->tolerance;
+    L->semi.assign(d->semi_diameter, d->semi_diameter + d->n_surfaces);
+    L->nidx.assign(d->n_index, d->n_index + d->n_surfaces + 1);
+    L->cap = max_rays;
+    size_t off[8];
+    size_t total = lens_layout(L->n_surf, max_rays, off);
+    int rc = ctx_alloc(ctx, &L->block, total, &L->bytes);
+    if (rc) {
+        delete L;
+        return rc;
+    }
+    unsigned char *b = (unsigned char *)L->block;
+    memset(&L->a, 0, sizeof L->a);
+    L->a.n_surf = L->n_surf;
+    L->a.faces = (const rp_face *)(b + off[0]);
+    L->a.nidx = (const double *)(b + off[1]);
+    L->a.S.shapes = (const rp_shape_op *)(b + off[2]);
+    L->a.S.n_shapes = 2 * L->n_surf;
+    L->a.max_len = L->max_len;
+    L->a.state = (double *)(b + off[3]);
+    L->a.img = (double *)(b + off[4]);
+    L->a.valid = b + off[5];
+    L->a.part = (double *)(b + off[6]);
+    L->a.gpart = (double *)(b + off[7]);
+    L->blocks_cap = lens_block_count(max_rays ? max_rays : 1);
+    L->a.err = (unsigned *)(b + off[7] + sizeof(double) * (5 * L->n_surf + 1) * L->blocks_cap);
+    CK(cudaMemcpyAsync((void *)L->a.nidx, L->nidx.data(), sizeof(double) * (L->n_surf + 1), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *out = L;
+    return RP_OK;
+}
+
+int rp_lens_destroy(rp_lens *L) {
+    if (!L) return RP_ERR_INVALID;
+    cudaSetDevice(L->ctx->device);
+    cudaStreamSynchronize(L->ctx->stream);
+    ctx_free(L->ctx, L->block, L->bytes);
+    delete L;
+    return RP_OK;
+}
+
+int rp_lens_forward(rp_lens *L, const double *params, const rp_rays *rays, double *loss, uint64_t *n_valid) {
+    if (!L || !params || !rays || !loss || rays->ctx != L->ctx) return RP_ERR_INVALID;
+    if (rays->n > L->cap) {
+        snprintf(g_last_error, sizeof g_last_error, "%llu rays exceed the lens capacity of %llu",
+                 (unsigned long long)rays->n, (unsigned long long)L->cap);
+        return RP_ERR_CAPACITY;
+    }
+    rp_ctx *ctx = L->ctx;
+    CK(cudaSetDevice(ctx->device));
+    const int n = L->n_surf;
+    for (int k = 0; k < n; k++) {
+        const double R = -params[k], beta = 1.0 + params[n + k];
+        if (!(R != 0.0) || !(beta * L->semi[k] * L->semi[k] < R * R) || !(params[4 * n + k] == params[4 * n + k])) {
+            snprintf(g_last_error, sizeof g_last_error,
+                     "lens surface %d: the aperture reaches the conic's rim (1 - beta r^2 / R^2 <= 0)", k);
+            return RP_ERR_INVALID;
+        }
+    }
+    std::vector<rp_face> faces;
+    std::vector<rp_shape_op> shapes;
+    lens_tables(L, params, faces, shapes);
+    CK(cudaMemcpyAsync((void *)L->a.faces, faces.data(), sizeof(rp_face) * faces.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync((void *)L->a.S.shapes, shapes.data(), sizeof(rp_shape_op) * shapes.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(L->a.err, 0, sizeof(unsigned), ctx->stream));
+    L->a.in = rays->soa;
+    L->a.n = rays->n;
+    const unsigned nb = lens_block_count(rays->n);
+    cudaError_t e = launch_lens_forward(L->a, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "lens forward launch");
+    std::vector<double> part(3 * (size_t)nb);
+    if (rays->n) CK(cudaMemcpyAsync(part.data(), L->a.part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    double cnt = 0.0, sx = 0.0, sy = 0.0;
+    for (unsigned b = 0; b < nb; b++) {
+        cnt += part[3 * b];
+        sx += part[3 * b + 1];
+        sy += part[3 * b + 2];
+    }
+    L->a.xm = cnt > 0 ? sx / cnt : 0.0;
+    L->a.ym = cnt > 0 ? sy / cnt : 0.0;
+    double s2 = 0.0;
+    if (cnt > 0) {
+        e = launch_lens_spread(L->a, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "lens spread launch");
+        CK(cudaMemcpyAsync(part.data(), L->a.part, sizeof(double) * nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (unsigned b = 0; b < nb; b++) s2 += part[b];
+    }
+    L->n_valid = cnt;
+    L->loss = cnt > 0 ? sqrt(s2 / cnt) : 0.0;
+    L->params.assign(params, params + 5 * n);
+    L->have_forward = 1;
+    *loss = L->loss;
+    if (n_valid) *n_valid = (uint64_t)cnt;
+    return RP_OK;
+}
+
+int rp_lens_backward(rp_lens *L, double *grad) {
+    if (!L || !grad) return RP_ERR_INVALID;
+    if (!L->have_forward) {
+        snprintf(g_last_error, sizeof g_last_error, "rp_lens_backward needs a forward first");
+        return RP_ERR_INVALID;
+    }
+    rp_ctx *ctx = L->ctx;
+    CK(cudaSetDevice(ctx->device));
+    const int n = L->n_surf, np = 5 * n + 1;
+    for (int j = 0; j < 5 * n; j++) grad[j] = 0.0;
+    if (!(L->n_valid > 0) || !(L->loss > 0)) return RP_OK;
+    L->a.scale = 1.0 / (L->n_valid * L->loss);
+    const unsigned nb = lens_block_count(L->a.n);
+    cudaError_t e = launch_lens_backward(L->a, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "lens backward launch");
+    std::vector<double> gp((size_t)np * nb);
+    CK(cudaMemcpyAsync(gp.data(), L->a.gpart, sizeof(double) * gp.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::vector<double> g(np, 0.0);
+    for (unsigned b = 0; b < nb; b++)
+        for (int j = 0; j < np; j++) g[j] += gp[(size_t)b * np + j];
+    // per surface (dR, dbeta, dA4, dA6, dz_k) and dz_image -> the parameter vector
+    double zacc = g[5 * n];  // d/dz_image
+    for (int k = n - 1; k >= 0; k--) {
+        grad[k] = -g[5 * k];             // curvature = -R
+        grad[n + k] = g[5 * k + 1];      // conic: beta = 1 + conic
+        grad[2 * n + k] = g[5 * k + 2];  // A4
+        grad[3 * n + k] = g[5 * k + 3];  // A6
+        grad[4 * n + k] = zacc;          // thickness k moves every vertex after k and the image plane
+        zacc += g[5 * k + 4];
+    }
+    return RP_OK;
+}
+
+int rp_lens_image(const rp_lens *L, double *xy, uint8_t *valid, uint64_t n) {
+    if (!L || !xy || !valid || n > L->a.n) return RP_ERR_INVALID;
+    CK(cudaSetDevice(L->ctx->device));
+    if (n) {
+        CK(cudaMemcpyAsync(xy, L->a.img, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, L->ctx->stream));
+        CK(cudaMemcpyAsync(valid, L->a.valid, n, cudaMemcpyDeviceToHost, L->ctx->stream));
+    }
+    CK(cudaStreamSynchronize(L->ctx->stream));
     return RP_OK;
 }
 

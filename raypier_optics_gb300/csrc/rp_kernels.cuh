@@ -59,4 +59,26 @@ cudaError_t launch_dispersion_table(const rp_dispersion *curves, int n_curves, c
                                     const double *wl, long long n_wl, double2 *ntab, cudaStream_t st);
 size_t generation_smem_bytes(int n_lists, int n_recs, int n_mats, int n_faces);
 
+// ---- differentiable sequential lens (rp_lens.cu) ----
+struct LensArgs {
+    int n_surf;                 // aspheric surfaces; faces[n_surf] is the image plane
+    const rp_face *faces;       // [n_surf + 1]
+    const double *nidx;         // [n_surf + 1] index before surface 0 and after each surface
+    DevScene S;                 // shape table (apertures) for the face functions
+    double max_len;             // segment length of the intersection tests
+    RaySoA in;                  // input rays (origin, direction)
+    unsigned long long n;
+    double *state;              // [(n_surf + 1) * 6 * n] p, d in front of each surface and the image plane
+    double *img;                // [2 n] image-plane x, y
+    unsigned char *valid;       // [n] ray reached the image
+    double *part;               // per-block partial sums
+    double *gpart;              // [blocks][5 n_surf + 1] per-block gradient sums
+    double xm, ym, scale;       // centroid and 1 / (N * loss) for the adjoint
+    unsigned *err;
+};
+cudaError_t launch_lens_forward(const LensArgs &L, cudaStream_t st);
+cudaError_t launch_lens_spread(const LensArgs &L, cudaStream_t st);
+cudaError_t launch_lens_backward(const LensArgs &L, cudaStream_t st);
+unsigned lens_block_count(unsigned long long n);
+
 }  // namespace rp

@@ -361,3 +361,67 @@ def subsample(rays, wavelengths, idx, per_ray_wavelength):
 
 def spec_copy(spec):
     return copy.deepcopy(spec)
+
+
+# ---- configuration 4 (differentiable lens) ---------------------------------------------
+# A four-element, eight-face Cooke-triplet-like objective (glasses 1.62 / 1.62 /
+# 1.52 and a 1.62 field element), even aspheres throughout.  Optical radii
+# (positive: centre of curvature behind the vertex) are stored with raypier's
+# sign, curvature = -R.  Nominal best focus for the 8 mm collimated beam lies
+# 39.4 mm behind the last vertex.
+LENS4_RADII = [22.0, -400.0, -28.0, 22.0, 60.0, -25.0, 30.0, 45.0]
+LENS4_CONIC = [-0.20, 0.10, 0.15, -0.10, 0.20, -0.15, 0.10, -0.20]
+LENS4_A4 = [2.0e-6, -1.0e-6, 1.5e-6, -2.0e-6, 1.0e-6, 2.0e-6, -1.5e-6, 1.0e-6]
+LENS4_A6 = [-1.0e-8, 2.0e-8, -1.5e-8, 1.0e-8, -2.0e-8, 1.5e-8, 1.0e-8, -1.0e-8]
+LENS4_THICKNESS = [3.5, 4.0, 1.2, 4.0, 3.0, 1.0, 2.5, 39.4]
+LENS4_SEMI = [9.0, 9.0, 8.0, 8.0, 8.0, 8.0, 8.0, 8.0]
+LENS4_INDEX = [1.0, 1.62, 1.0, 1.62, 1.0, 1.52, 1.0, 1.62, 1.0]
+CONFIG4 = {"n_rays": 262144, "beam_radius": 4.0, "wavelength": 0.587, "z_start": -10.0, "max_length": 1000.0,
+           "atol": 1.0e-8, "tolerance": 1.0e-4, "perturbation": 0.02, "seed": 4, "fd_step": 1.0e-6}
+
+
+def config4_nominal():
+    """The 40 nominal parameters: curvature[8] (raypier sign), conic[8], A4[8], A6[8], thickness[8]."""
+    return np.array([-r for r in LENS4_RADII] + LENS4_CONIC + LENS4_A4 + LENS4_A6 + LENS4_THICKNESS,
+                    dtype=np.double)
+
+
+def config4_params(seed=None):
+    """Nominal parameters with seeded uniform perturbations of +-2 %."""
+    rng = np.random.Generator(np.random.PCG64(CONFIG4["seed"] if seed is None else seed))
+    p = config4_nominal()
+    return p * (1.0 + rng.uniform(-CONFIG4["perturbation"], CONFIG4["perturbation"], p.shape[0]))
+
+
+def config4_rays(ray_dtype, n=None):
+    """Collimated rays on a hexagonal grid filling the 8 mm beam, starting at z = -10."""
+    n = n or CONFIG4["n_rays"]
+    x, y = hex_grid(max(n, 7), CONFIG4["beam_radius"])
+    x, y = x[:n], y[:n]
+    rays = np.zeros(n, dtype=ray_dtype)
+    origin = np.stack([x, y, np.full(n, CONFIG4["z_start"])], axis=1)
+    fill_rays(rays, origin, (0.0, 0.0, 1.0), (1.0, 0.0, 0.0))
+    return rays, np.array([CONFIG4["wavelength"]])
+
+
+def config4_spec(params):
+    """The lens as an ordinary raypier scene: one face list, every surface an
+    AsphericFace with its normal turned to -z and a DielectricMaterial whose
+    outside is the medium in front of it, then the image plane (a detector)."""
+    n = len(LENS4_RADII)
+    params = np.asarray(params, dtype=np.double)
+    faces, mats = [], {"image": {"type": "OpaqueMaterial"}}
+    z = 0.0
+    for k in range(n):
+        mats[f"s{k}"] = {"type": "DielectricMaterial",
+                         "kw": {"n_inside": LENS4_INDEX[k + 1], "n_outside": LENS4_INDEX[k]}}
+        faces.append({"type": "AsphericFace",
+                      "kw": {"curvature": float(params[k]), "z_height": z, "conic_const": float(params[n + k]),
+                             "A4": float(params[2 * n + k]), "A6": float(params[3 * n + k]),
+                             "atol": CONFIG4["atol"], "invert_normal": 1},
+                      "shape": {"type": "CircleShape", "kw": {"radius": LENS4_SEMI[k]}},
+                      "material": f"s{k}"})
+        z += float(params[4 * n + k])
+    faces.append({"type": "CircularFace", "kw": {"z_plane": z},
+                  "owner": {"diameter": 1.0e9, "offset": 0.0}, "material": "image"})
+    return {"materials": mats, "lists": [{"translation": [0, 0, 0], "faces": faces}]}

@@ -4,6 +4,7 @@ raypier tracer (its Cython core built from source by oracle/build_ref.py).
 Run in a container that has the reference sources and Cython:
 
     python oracle/build_ref.py && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --lens     # only the configuration-4 lens case
 
 Every fixture stores the scene description (the JSON spec understood by
 raypier_optics_gb300.workloads.build_scene), the inputs, and the reference's
@@ -371,8 +372,25 @@ def main():
     np.savez_compressed(os.path.join(out_dir, "units.npz"), **units)
     np.savez_compressed(os.path.join(out_dir, "face_zoo_specs.npz"),
                         specs=np.array(json.dumps({k: face_scene(v) for k, v in zoo.items()})))
+    lens_case(ref, out_dir)
     print("golden vectors written to", out_dir)
 
 
+def lens_case(ref, out_dir):
+    """Configuration 4: the perturbed eight-surface lens as an ordinary scene
+    (AsphericFace + DielectricMaterial, image plane), 64 rays of the 262,144-ray
+    grid, traced by the reference's trace_rays."""
+    rays4, wl4 = W.config4_rays(ref.ctracer.ray_dtype)
+    idx = np.linspace(0, len(rays4) - 1, 64).astype(np.int64)
+    sub = rays4[idx].copy()
+    spec = W.config4_spec(W.config4_params())
+    P4 = {"recursion_limit": 10, "max_length": W.CONFIG4["max_length"], "e2_terminate": 0.0}
+    gens, counts = run_reference(ref, spec, sub, wl4, P4["recursion_limit"], P4["max_length"])
+    save_trace_case(os.path.join(out_dir, "config4_sub64.npz"), spec, sub, wl4, P4, gens, counts)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--lens"]:
+        lens_case(build_ref.load(), HERE)
+    else:
+        main()
