@@ -348,6 +348,67 @@ int rp_lens_backward(rp_lens *lens, double *grad);
 /* Image-plane x, y and reached flags of the last forward's first n rays. */
 int rp_lens_image(const rp_lens *lens, double *xy, uint8_t *valid, uint64_t n);
 
+/* ---- trace-job server ----------------------------------------------------- */
+/* No counterpart in the reference (its traces run one at a time in the caller's
+ * thread).  A server owns `lanes` contexts on one device; submitted jobs wait
+ * in one FIFO queue and start as soon as a lane is free and the HBM budget
+ * admits their estimated footprint, so jobs overlap on the device.  A job is
+ * a whole trace_rays (core/tracer.py:9-47) of rays generated on the device
+ * from a source description; each generation runs as one CUDA graph.  The
+ * result is the job's counters and the tallies of the rays that ended on its
+ * detector face, reduced on the device in a fixed order (the same whether the
+ * job runs alone or among others).  Submit and wait may be called from any
+ * thread. */
+#define RP_SOURCE_POINT_CONE      1  /* point at `origin`, directions uniform in a cone of `half_angle` about +z */
+#define RP_SOURCE_COLLIMATED_DISC 2  /* directions +z, origins uniform over a disc of `radius` about `origin` */
+typedef struct rp_source_desc {
+    int32_t type;
+    int32_t reserved;
+    uint64_t n_rays;
+    uint64_t seed;            /* counter-based: ray i depends only on (seed, i) */
+    double origin[3];
+    double half_angle;        /* rad */
+    double radius;            /* mm */
+    /* every ray: E linearly polarised at a uniform angle about the ray,
+     * E1 = 1, n = 1, wavelength_idx uniform over the job's wavelengths */
+} rp_source_desc;
+
+typedef struct rp_job_desc {
+    const rp_scene_desc *scene;   /* copied at submit */
+    const double *wavelengths;    /* copied at submit */
+    int64_t n_wl;
+    rp_source_desc source;
+    int32_t recursion_limit;
+    float max_length;
+    uint32_t flags;               /* RP_TRACE_PLAIN_FP64 / RP_TRACE_MIXED */
+    int32_t detector_face;        /* Face.idx whose hits are tallied, -1: none */
+    double e2_terminate;
+} rp_job_desc;
+
+typedef struct rp_job_result {
+    int32_t status;               /* RP_OK or the failing call's status */
+    int32_t generations;
+    uint64_t segments;            /* rays traced over all generations */
+    uint64_t detector_hits;
+    double detector_power;        /* sum of (|E1|^2 + |E2|^2) Re(n) over the detector hits */
+    double sum_x, sum_y, sum_xx, sum_yy;  /* of the detector hit points */
+    double t_submit_ms, t_start_ms, t_done_ms;  /* server clock */
+} rp_job_result;
+
+/* The source rays of a job into a device buffer (capacity >= n_rays), for
+ * tracing them with the other entry points. */
+int rp_source_generate(rp_ctx *ctx, const rp_source_desc *source, uint32_t n_wl, rp_rays *out);
+
+typedef struct rp_server rp_server;
+int rp_server_create(int device, uint64_t hbm_budget, int32_t lanes, rp_server **out);
+int rp_server_submit(rp_server *server, const rp_job_desc *job, uint64_t *job_id);
+/* Blocks until the job is done; copies its per-face hit counts (n_faces of
+ * them) when face_counts is not NULL.  A job id can be waited for once. */
+int rp_server_wait(rp_server *server, uint64_t job_id, rp_job_result *result, uint32_t *face_counts,
+                   int32_t n_faces);
+/* Finishes the queued jobs, then stops the lanes. */
+int rp_server_destroy(rp_server *server);
+
 /* Allocation-free rp_trace_segment.  No counterpart in the reference: this is
  * an addition of this library.  Same arguments, results and status codes as
  * rp_trace_segment, for callers that must not allocate device memory during a

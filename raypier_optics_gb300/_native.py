@@ -32,6 +32,7 @@ SOURCES = [
     ("rp_api.cu", ["--fmad=false"]),
     ("rp_unit.cu", ["--fmad=false"]),
     ("rp_lens.cu", ["--fmad=false"]),
+    ("rp_serve.cu", ["--fmad=false"]),
 ]
 
 
@@ -137,6 +138,26 @@ class LensDesc(ctypes.Structure):
                 ("semi_diameter", ctypes.c_void_p), ("n_index", ctypes.c_void_p)]
 
 
+class SourceDesc(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("reserved", ctypes.c_int32), ("n_rays", ctypes.c_uint64),
+                ("seed", ctypes.c_uint64), ("origin", ctypes.c_double * 3), ("half_angle", ctypes.c_double),
+                ("radius", ctypes.c_double)]
+
+
+class JobDesc(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("wavelengths", ctypes.c_void_p), ("n_wl", ctypes.c_int64),
+                ("source", SourceDesc), ("recursion_limit", ctypes.c_int32), ("max_length", ctypes.c_float),
+                ("flags", ctypes.c_uint32), ("detector_face", ctypes.c_int32), ("e2_terminate", ctypes.c_double)]
+
+
+class JobResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("generations", ctypes.c_int32), ("segments", ctypes.c_uint64),
+                ("detector_hits", ctypes.c_uint64), ("detector_power", ctypes.c_double),
+                ("sum_x", ctypes.c_double), ("sum_y", ctypes.c_double), ("sum_xx", ctypes.c_double),
+                ("sum_yy", ctypes.c_double), ("t_submit_ms", ctypes.c_double), ("t_start_ms", ctypes.c_double),
+                ("t_done_ms", ctypes.c_double)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("rays_in", ctypes.c_uint64), ("rays_out", ctypes.c_uint64),
                 ("hits", ctypes.c_uint64), ("terminated", ctypes.c_uint64),
@@ -187,6 +208,11 @@ _SIGS = {
     "rp_lens_forward": (_I, [_P, _P, _P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]),
     "rp_lens_backward": (_I, [_P, _P]),
     "rp_lens_image": (_I, [_P, _P, _P, ctypes.c_uint64]),
+    "rp_source_generate": (_I, [_P, ctypes.POINTER(SourceDesc), ctypes.c_uint32, _P]),
+    "rp_server_create": (_I, [_I, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(_P)]),
+    "rp_server_submit": (_I, [_P, ctypes.POINTER(JobDesc), ctypes.POINTER(ctypes.c_uint64)]),
+    "rp_server_wait": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(JobResult), _P, ctypes.c_int32]),
+    "rp_server_destroy": (_I, [_P]),
     "rp_face_intersect": (_I, [_P, ctypes.c_int32, _P, _P, ctypes.c_uint64, _I, _P]),
     "rp_face_normal": (_I, [_P, ctypes.c_int32, _P, ctypes.c_uint64, _P]),
     "rp_shape_inside": (_I, [_P, ctypes.c_int32, _P, ctypes.c_uint64, _P]),

@@ -1,0 +1,65 @@
+// rp_internal.h -- definitions shared by the C-ABI translation units
+// (rp_api.cu: contexts, scenes, rays, tracing; rp_serve.cu: the job server).
+// Not part of the public header.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <vector>
+
+#include "../../include/rp_gb300.h"
+#include "rp_kernels.cuh"
+
+using namespace rp;
+
+struct PoolBlock {
+    void *p;
+    size_t bytes;
+};
+
+struct rp_ctx {
+    int device;
+    cudaStream_t stream;
+    uint64_t budget;
+    uint64_t in_use;                 // bytes of live allocations
+    std::vector<PoolBlock> pool;     // freed blocks kept for reuse
+    uint64_t pooled;                 // bytes in `pool`
+    std::vector<cudaEvent_t> gen_ev; // per-generation kernel events (pairs)
+    struct rp_rays *arena;           // child slots of the generation being traced
+    // per-generation scratch: [out_count | err | pad | stats[2] | tile counter | pad | tile counts, offsets]
+    unsigned char *scratch;
+    size_t scratch_bytes;
+    unsigned long long *h_pinned;  // 8 words of pinned host memory for small read-backs
+    cudaEvent_t ev0, ev1;
+};
+
+struct rp_scene {
+    rp_ctx *ctx;
+    DevScene S;               // device pointers
+    void *dev_block;          // one allocation holding every table
+    size_t dev_bytes;
+    unsigned *face_counts;    // per face record
+    int n_faces;
+    size_t smem;              // bytes of tables staged per block
+    int smem_tables;
+    int mixed_fallback;       // faces or materials the mixed kernel leaves to its FP64 code
+    const rp_dispersion *disp;  // device copy of the dispersion curve table
+    int n_disp;
+    std::vector<rp_face> host_faces;
+    std::vector<rp_facelist> host_lists;
+};
+
+struct rp_rays {
+    rp_ctx *ctx;
+    uint64_t cap, n;
+    void *block;
+    size_t bytes;
+    RaySoA soa;
+};
+
+
+// helpers implemented in rp_api.cu
+int rp__ctx_alloc(rp_ctx *ctx, void **p, size_t bytes, size_t *got);
+void rp__ctx_free(rp_ctx *ctx, void *p, size_t bytes);
+int rp__cuda_fail(cudaError_t e, const char *what);
+void rp__set_error(const char *fmt, ...);

@@ -50,6 +50,10 @@ struct GenArgs {
 // launchers (rp_trace.cu / rp_mixed.cu); return cudaError_t
 cudaError_t launch_generation_plain(const GenArgs &a, size_t smem, cudaStream_t st);
 cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st);
+// one-time per-configuration set-up (attributes, occupancy), so that a following
+// launch of the same configuration can be stream-captured
+cudaError_t prepare_generation_plain(const GenArgs &a, size_t smem);
+cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem);
 // tile-count scan (one block) and the scatter of children to their final slots
 cudaError_t launch_tile_scan(const GenArgs &a, unsigned n_tiles, cudaStream_t st);
 cudaError_t launch_place_children(const GenArgs &a, unsigned n_tiles, cudaStream_t st);

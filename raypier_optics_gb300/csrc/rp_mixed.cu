@@ -26,6 +26,9 @@
 // The TU is compiled with FMA contraction on.  Index fields agree with the
 // FP64 oracle except for rays that graze an aperture edge or a face, which is
 // why parity for this path is statistical (see the precision report).
+#include <map>
+#include <mutex>
+
 #include "rp_gen_common.cuh"
 
 namespace rp {
@@ -1228,41 +1231,63 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
     }
 }
 
-// Resident blocks per SM for one instantiation and shared-memory size, cached.
+// Resident blocks for one instantiation and shared-memory size, cached per
+// (device, size) under a lock: several host threads (server lanes) launch.
 template <bool FB>
 static cudaError_t mixed_grid_blocks(size_t total, int *blocks) {
-    static int cached_dev = -1, cached_blocks = 0;
-    static size_t cached_total = 0;
-    int dev = 0, sms = 0, per_sm = 0;
+    static std::mutex mu;
+    static std::map<std::pair<int, size_t>, int> cache;
+    static std::map<int, size_t> limit;  // the kernel's shared-memory limit per device: only ever raised
+    int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev != cached_dev || total != cached_total) {
-        if (total > 48 * 1024) {
-            e = cudaFuncSetAttribute(generation_mixed_kernel<FB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)total);
-            if (e != cudaSuccess) return e;
-        }
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, generation_mixed_kernel<FB>, RP_BLOCK, total);
-        if (e != cudaSuccess) return e;
-        cached_blocks = (per_sm > 0 ? per_sm : 1) * sms;
-        cached_dev = dev;
-        cached_total = total;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find({dev, total});
+    if (it != cache.end()) {
+        *blocks = it->second;
+        return cudaSuccess;
     }
-    *blocks = cached_blocks;
+    if (limit[dev] < total) {
+        e = cudaFuncSetAttribute(generation_mixed_kernel<FB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)total);
+        if (e != cudaSuccess) return e;
+        limit[dev] = total;
+    }
+    int sms = 0, per_sm = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, generation_mixed_kernel<FB>, RP_BLOCK, total);
+    if (e != cudaSuccess) return e;
+    *blocks = (per_sm > 0 ? per_sm : 1) * sms;
+    cache[{dev, total}] = *blocks;
     return cudaSuccess;
+}
+
+static size_t mixed_smem_total(const GenArgs &a, size_t smem, size_t *mx_off, size_t *tb_off, size_t *in_off) {
+    *mx_off = (smem + 15) & ~(size_t)15;
+    *tb_off = *mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
+    const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
+    *in_off = (*tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
+    return *in_off + 2 * sizeof(mx::TileIn);
+}
+
+// Runs the one-time per-size set-up of the launch (attribute, occupancy) so
+// that a later launch of the same configuration makes no other CUDA call, as
+// stream capture requires.
+cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem) {
+    size_t mx_off, tb_off, in_off;
+    const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off);
+    if (total > 220 * 1024) return cudaErrorInvalidConfiguration;
+    int blocks = 0;
+    return a.mixed_fallback ? mixed_grid_blocks<true>(total, &blocks) : mixed_grid_blocks<false>(total, &blocks);
 }
 
 // The scene's faces and materials decide the instantiation: without FP64
 // fallbacks the kernel carries no out-of-line calls and their register cost.
 cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st) {
     if (a.n_in == 0) return cudaSuccess;
-    const size_t mx_off = (smem + 15) & ~(size_t)15;
-    const size_t tb_off = mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
-    const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
-    const size_t in_off = (tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
-    const size_t total = in_off + 2 * sizeof(mx::TileIn);
+    size_t mx_off, tb_off, in_off;
+    const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off);
     if (total > 220 * 1024) return cudaErrorInvalidConfiguration;  // scene too large for the per-block tables
     int blocks = 0;
     cudaError_t e = a.mixed_fallback ? mixed_grid_blocks<true>(total, &blocks) : mixed_grid_blocks<false>(total, &blocks);

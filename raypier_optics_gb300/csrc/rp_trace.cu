@@ -12,6 +12,9 @@
 //      1939-1953), material evaluation into 0..2 children;
 //   4. children are placed by a block scan + decoupled look-back and written
 //      as structure-of-arrays.
+#include <map>
+#include <mutex>
+
 #include "rp_gen_common.cuh"
 
 namespace rp {
@@ -244,15 +247,27 @@ size_t generation_smem_bytes(int n_lists, int n_recs, int n_mats, int n_faces) {
 cudaError_t launch_generation_plain(const GenArgs &a, size_t smem, cudaStream_t st) {
     if (a.n_in == 0) return cudaSuccess;
     unsigned grid = (unsigned)((a.n_in + RP_BLOCK - 1) / RP_BLOCK);
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(generation_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    cudaError_t e = prepare_generation_plain(a, smem);
+    if (e != cudaSuccess) return e;
     generation_plain_kernel<<<grid, RP_BLOCK, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+// Raises the kernel's dynamic shared-memory limit once per device to the
+// largest size seen (under a lock: several host threads launch).
+cudaError_t prepare_generation_plain(const GenArgs &a, size_t smem) {
+    (void)a;
+    if (smem <= 48 * 1024) return cudaSuccess;
+    static std::mutex mu;
+    static std::map<int, size_t> configured;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (configured[dev] >= smem) return cudaSuccess;
+    e = cudaFuncSetAttribute(generation_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) configured[dev] = smem;
+    return e;
 }
 
 // ---- child placement ------------------------------------------------------

@@ -425,3 +425,74 @@ def config4_spec(params):
     faces.append({"type": "CircularFace", "kw": {"z_plane": z},
                   "owner": {"diameter": 1.0e9, "offset": 0.0}, "material": "image"})
     return {"materials": mats, "lists": [{"translation": [0, 0, 0], "faces": faces}]}
+
+
+# ---- configuration 5 (serving) -----------------------------------------------------
+CONFIG5 = {"n_jobs": 10000, "rate": 200.0, "seed": 5, "min_rays": 1000, "max_rays": 4000000,
+           "wl_range": (0.4, 1.0), "n_wavelengths": 256, "hbm_budget": 120 * 10**9, "n_systems": 256,
+           "recursion_limit": 8, "max_length": 1000.0, "e2_terminate": 1e-6}
+
+
+def config5_system(rng, n_elements):
+    """A random coaxial system of `n_elements` singlets (2 faces each) drawn
+    from configuration 2's face mix (spherical, conic, aspheric, plane), crown
+    or flint with Sellmeier dispersion and the materials' default Fresnel
+    thresholds, followed by a detector: 2 n_elements + 1 faces.  Every face's
+    normal points to +z at its vertex, so a face's material has the medium in
+    front as `inside` (DielectricMaterial's out-to-in test is normal . d < 0)."""
+    mats = {"detector": {"type": "OpaqueMaterial"}}
+    for g in ("crown", "flint"):
+        mats[f"in_{g}"] = {"type": "FullDielectricDispersiveMaterial",
+                           "kw": {"dispersion_inside": "air", "dispersion_outside": g}}
+        mats[f"out_{g}"] = {"type": "FullDielectricDispersiveMaterial",
+                            "kw": {"dispersion_inside": g, "dispersion_outside": "air"}}
+    circ = {"type": "CircleShape", "kw": {"radius": 12.5}}
+    faces, z = [], 0.0
+
+    def surface(z_height, mat):
+        kind = rng.integers(0, 4)
+        R = float(rng.uniform(60.0, 400.0)) * (1.0 if rng.uniform() < 0.5 else -1.0)
+        if kind == 0:
+            return {"type": "SphericalFace", "kw": {"curvature": -R, "z_height": z_height},
+                    "owner": {"diameter": 25.0}, "material": mat}
+        if kind == 1:
+            return {"type": "ConicRevolutionFace", "kw": {"curvature": -R, "z_height": z_height,
+                                                          "conic_const": float(rng.uniform(-1.5, 0.5))},
+                    "shape": circ, "material": mat}
+        if kind == 2:
+            return {"type": "AsphericFace", "kw": {"curvature": -R, "z_height": z_height,
+                                                   "conic_const": float(rng.uniform(-1.0, 0.0)),
+                                                   "A4": float(rng.normal(0.0, 1e-6)),
+                                                   "A6": float(rng.normal(0.0, 1e-9))},
+                    "shape": circ, "material": mat}
+        return {"type": "ShapedPlanarFace", "kw": {"z_height": z_height}, "shape": circ, "material": mat}
+
+    for _ in range(n_elements):
+        g = "crown" if rng.uniform() < 0.5 else "flint"
+        faces.append(surface(z, f"in_{g}"))
+        z += float(rng.uniform(4.0, 8.0))
+        faces.append(surface(z, f"out_{g}"))
+        z += float(rng.uniform(3.0, 10.0))
+    faces.append({"type": "CircularFace", "kw": {"z_plane": z + 20.0}, "owner": {"diameter": 400.0, "offset": 0.0},
+                  "material": "detector"})
+    return {"curves": {"crown": CROWN, "flint": FLINT, "air": AIR}, "materials": mats,
+            "lists": [{"translation": [0, 0, 0], "faces": faces}]}
+
+
+def config5_jobs(n_jobs=None, seed=None):
+    """The seeded job stream: (arrival time s, system index, n_rays, source seed,
+    source type, wavelengths), with `CONFIG5["n_systems"]` distinct systems
+    of 3-39 faces that jobs draw from, arrivals Poisson at CONFIG5["rate"]/s and
+    ray counts log-uniform over [1e3, 4e6]."""
+    C = CONFIG5
+    n_jobs = C["n_jobs"] if n_jobs is None else n_jobs
+    rng = np.random.Generator(np.random.PCG64(C["seed"] if seed is None else seed))
+    systems = [config5_system(rng, int(rng.integers(1, 20))) for _ in range(C["n_systems"])]
+    t = np.cumsum(rng.exponential(1.0 / C["rate"], n_jobs))
+    sys_idx = rng.integers(0, len(systems), n_jobs)
+    n_rays = np.exp(rng.uniform(math.log(C["min_rays"]), math.log(C["max_rays"]), n_jobs)).astype(np.int64)
+    seeds = rng.integers(1, 2**62, n_jobs)
+    kinds = rng.integers(1, 3, n_jobs)  # point cone or collimated disc
+    wls = [np.sort(rng.uniform(C["wl_range"][0], C["wl_range"][1], C["n_wavelengths"])) for _ in range(n_jobs)]
+    return systems, [{"t": float(t[k]), "system": int(sys_idx[k]), "n_rays": int(n_rays[k]), "seed": int(seeds[k]),
+                      "source": int(kinds[k]), "wavelengths": wls[k]} for k in range(n_jobs)]
