@@ -68,6 +68,12 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true", help="skip the second path's leg (plain FP64 when the "
                     "headline is mixed, mixed when it is plain) and the precision sample")
     ap.add_argument("--cpu-sample", type=int, default=0, help="rays in the CPU-baseline sample")
+    ap.add_argument("--no-serving", action="store_true", help="skip the job-server stream (configuration 5)")
+    ap.add_argument("--serving-jobs", type=int, default=10000, help="jobs in the served stream")
+    ap.add_argument("--serving-lanes", type=int, default=8)
+    ap.add_argument("--serving-baseline-jobs", type=int, default=500,
+                    help="jobs of the same stream run one at a time through the plain FP64 path")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-lens leg (configuration 4)")
     return ap.parse_args()
 
 
@@ -303,9 +309,14 @@ def main():
     if not args.no_e2e:
         e2e_value, d2h, e2e_steps = run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens,
                                             seg_per_step, dist, world)
+    extra = {}
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        extra["adjoint"] = adjoint_leg(ctx)
+    if rank == 0 and world == 1 and not args.no_serving:
+        extra["serving"] = serving_leg(args)
     if rank == 0:
         emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
-             achieved, peak, peak_kind, flags, stats, clk, cpu, other)
+             achieved, peak, peak_kind, flags, stats, clk, cpu, other, extra)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -353,6 +364,63 @@ def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, s
     return e2e_value, d2h, e2e_steps
 
 
+def adjoint_leg(ctx, reps=5):
+    """Configuration 4: forward (RMS spot radius) and hand-written adjoint of the
+    eight-surface lens on 262,144 rays, host wall time per call (each call
+    synchronises)."""
+    from raypier_optics_gb300 import lens
+    from raypier_optics_gb300 import workloads as W
+    L = lens.config4_lens(ctx=ctx)
+    p = W.config4_params()
+    for _ in range(2):
+        L.forward(p)
+        L.backward()
+    tf = tb = 0.0
+    loss = 0.0
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        loss, nv = L.forward(p)
+        t1 = time.perf_counter()
+        g = L.backward()
+        tb += time.perf_counter() - t1
+        tf += t1 - t0
+    L.close()
+    return {"workload": "config4: 262144 rays, 8 even-asphere surfaces, 40 FP64 parameters, loss = RMS spot radius",
+            "forward_ms": 1000.0 * tf / reps, "backward_ms": 1000.0 * tb / reps, "loss_mm": loss,
+            "rays_reaching_image": int(nv), "grad_norm": float(np.linalg.norm(g)),
+            "check": "tests/test_gpu_lens.py: adjoint vs central differences (step 1e-6 rel), all 40 parameters"}
+
+
+def serving_leg(args):
+    """Configuration 5: a Poisson stream of jobs (systems of 3-39 faces from the
+    configuration-2 face mix, log-uniform 1e3-4e6 rays, wavelengths 0.4-1.0 um)
+    replayed in real time against the job server (mixed path, 8 lanes, 120 GB
+    budget); the first jobs of the same stream also run one at a time through
+    the plain FP64 path."""
+    from raypier_optics_gb300 import serve
+    from raypier_optics_gb300 import workloads as W
+    C = W.CONFIG5
+    systems, jobs = W.config5_jobs(args.serving_jobs)
+    compiled = [serve.CompiledSystem(s) for s in systems]
+    srv = serve.Server(hbm_budget=C["hbm_budget"], lanes=args.serving_lanes)
+    res, wall = serve.run_stream(srv, compiled, jobs, flags=1, recursion_limit=C["recursion_limit"],
+                                 e2_terminate=C["e2_terminate"])
+    srv.close()
+    out = serve.latency_summary(res)
+    out.update({"rate_jobs_per_s": C["rate"], "lanes": args.serving_lanes, "hbm_budget_bytes": C["hbm_budget"],
+                "path": "mixed", "wall_s": wall, "p99_over_p50": out["p99_ms"] / out["p50_ms"]})
+    nb = min(args.serving_baseline_jobs, len(jobs))
+    if nb > 0:
+        srv = serve.Server(hbm_budget=C["hbm_budget"], lanes=1)
+        bres, bwall = serve.run_stream(srv, compiled, jobs[:nb], flags=0, recursion_limit=C["recursion_limit"],
+                                       e2_terminate=C["e2_terminate"])
+        srv.close()
+        b = serve.latency_summary(bres)
+        b.update({"path": "plain FP64, one job at a time", "wall_s": bwall})
+        out["plain_one_at_a_time_fp64"] = b
+    return out
+
+
 def precision_sample(ctx, spec, rays, wl, P, per_ray, n_sample=16384):
     """Error of the mixed path against the plain FP64 path on a ray sample."""
     import types
@@ -375,7 +443,7 @@ def precision_sample(ctx, spec, rays, wl, P, per_ray, n_sample=16384):
 
 
 def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
-         achieved, peak, peak_kind, flags, stats, clk, cpu, other=None):
+         achieved, peak, peak_kind, flags, stats, clk, cpu, other=None, extra=None):
     kernel = "generation_plain_kernel" if flags == 0 else "generation_mixed_kernel"
     if True:
         line = {
@@ -404,6 +472,8 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
         }
         if other is not None:
             line["mixed" if flags == 0 else "plain_fp64"] = other
+        if extra:
+            line.update(extra)
         if cpu is not None:
             line["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": cpu["kind"],
                                     "sample": cpu["sample"]}

@@ -62,6 +62,8 @@ def test_struct_layouts_match_the_header():
              sizeof(rp_material), sizeof(rp_dispersion), sizeof(rp_scene_desc), sizeof(rp_stats));
       printf("%zu %zu %zu %zu\n", offsetof(rp_ray, refractive_index), offsetof(rp_ray, length),
              offsetof(rp_ray, wavelength_idx), offsetof(rp_face, p));
+      printf("%zu %zu %zu %zu %zu %zu\n", sizeof(rp_lens_desc), sizeof(rp_source_desc), sizeof(rp_job_desc),
+             sizeof(rp_job_result), offsetof(rp_job_desc, source), offsetof(rp_job_result, t_submit_ms));
       return 0; }
     '''
     with tempfile.TemporaryDirectory() as d:
@@ -86,3 +88,10 @@ def test_struct_layouts_match_the_header():
     assert offs[1] == ray_dtype.fields['length'][1]
     assert offs[2] == ray_dtype.fields['wavelength_idx'][1]
     assert offs[3] == _native.FACE_DT.fields['p'][1]
+    more = list(map(int, out[2].split()))
+    assert more[0] == ctypes.sizeof(_native.LensDesc)
+    assert more[1] == ctypes.sizeof(_native.SourceDesc)
+    assert more[2] == ctypes.sizeof(_native.JobDesc)
+    assert more[3] == ctypes.sizeof(_native.JobResult)
+    assert more[4] == _native.JobDesc.source.offset
+    assert more[5] == _native.JobResult.t_submit_ms.offset
