@@ -156,8 +156,14 @@ enum rp_material_type {
     RP_MAT_FULL_DIELECTRIC_DISPERSIVE = 9, /* FullDielectricDispersiveMaterial cmaterials.pyx:875-1013 */
     RP_MAT_CIRCULAR_APERTURE = 10,   /* CircularApertureMaterial  cmaterials.pyx:1602-1662
                                         p: outer_radius, radius, edge_width, invert, origin[3] */
-    RP_MAT_RECT_APERTURE = 11        /* RectangularApertureMaterial cmaterials.pyx:1665-1763
+    RP_MAT_RECT_APERTURE = 11,       /* RectangularApertureMaterial cmaterials.pyx:1665-1763
                                         p: outer_width, outer_height, width, height, edge_width, invert, origin[3] */
+    RP_MAT_SINGLE_LAYER_COATED = 12, /* SingleLayerCoatedMaterial cmaterials.pyx:1017-1184
+                                        n_inside, n_outside; p: n_coating (re, im), thickness (um) */
+    RP_MAT_COATED_DISPERSIVE = 13,   /* CoatedDispersiveMaterial  cmaterials.pyx:1187-1381
+                                        curve_inside, curve_outside; p: curve_coating, coating_thickness (um) */
+    RP_MAT_DIFFRACTION_GRATING = 14  /* DiffractionGratingMaterial cmaterials.pyx:1437-1543
+                                        p: lines_per_mm, order, efficiency, origin[3] */
 };
 typedef struct rp_material {
     int32_t type;

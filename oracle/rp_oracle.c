@@ -787,6 +787,7 @@ typedef struct {
     const rp_scene_desc *s;
     const cplx *n_tab;   /* [n_dispersions][n_wl] */
     int64_t n_wl;
+    const double *wl;    /* the wavelengths (InterfaceMaterial._wavelengths) */
 } mat_ctx;
 
 static void fresnel_split(const mat_ctx *mc, const rp_material *m, cplx n1_in, cplx n2_in,
@@ -866,6 +867,120 @@ static void fresnel_split(const mat_ctx *mc, const rp_material *m, cplx n1_in, c
         sp_ray.E2_amp[0] = creal(T_p); sp_ray.E2_amp[1] = cimag(T_p);
         sp_ray.parent_idx = idx;
         sp_ray.refractive_index[0] = creal(n2); sp_ray.refractive_index[1] = cimag(n2);
+        sp_ray.ray_type_id &= ~RP_REFL_RAY;
+        add_ray(out, &sp_ray);
+    }
+}
+
+static inline cplx cplx_of_parts(double re, double im) { /* x.real + I*x.imag as Cython emits it */
+    return cfp(re, 0) + (cfp(0, 1.0) * cfp(im, 0));
+}
+
+static void coated_split(const mat_ctx *mc, const rp_material *m, const rp_ray *in_ray, uint32_t idx, vec point,
+                         orient_t orient, ray_sink *out) {
+    /* SingleLayerCoatedMaterial.eval_child_ray_c (cmaterials.pyx:1026-1184) and
+     * CoatedDispersiveMaterial.eval_child_ray_c (cmaterials.pyx:1228-1381) */
+    cplx n1, n2, n3, cos2, sin2, cos3, sin3, R_p, R_s, T_p, T_s, E1_amp, E2_amp;
+    cplx n1cos1, n2cos2, n3cos3, n1cos2, n2cos1, n2cos3, n3cos2, ep1, ep2, M00, M01, M10, M11, phi;
+    double cosTheta, cos1, sin1, P_in, tan_mag_sq, c2, aspect, wavelength, dwc, thickness;
+    int flip;
+    const int disp = m->type == RP_MAT_COATED_DISPERSIVE;
+    const uint32_t w = in_ray->wavelength_idx;
+    wavelength = mc->wl[w];
+    vec normal = norm_(orient.normal);
+    vec in_direction = norm_(ld_v(in_ray->direction));
+    rp_ray sp_ray = convert_to_sp(*in_ray, normal);
+    sp_ray.accumulated_path = sp_ray.accumulated_path + (sp_ray.length * sp_ray.refractive_index[0]);
+    E1_amp = cplx_of_parts(sp_ray.E1_amp[0], sp_ray.E1_amp[1]);
+    E2_amp = cplx_of_parts(sp_ray.E2_amp[0], sp_ray.E2_amp[1]);
+    cosTheta = dotprod_(normal, in_direction);
+    cos1 = fabs(cosTheta);
+    sin1 = sqrt(fabs((1.0 - (cos1 * cos1))));
+    cplx ni, no;
+    if (disp) {
+        cplx ctemp = mc->n_tab[(int64_t)m->p[0] * mc->n_wl + w];
+        n2 = cplx_of_parts(creal(ctemp), cimag(ctemp));
+        ni = mc->n_tab[m->curve_inside * mc->n_wl + w];
+        no = mc->n_tab[m->curve_outside * mc->n_wl + w];
+        thickness = m->p[1];
+    } else {
+        n2 = cplx_of_parts(m->p[0], m->p[1]);
+        ni = cfp(m->n_inside[0], m->n_inside[1]);
+        no = cfp(m->n_outside[0], m->n_outside[1]);
+        thickness = m->p[2];
+    }
+    if (cosTheta < 0.0) {
+        n1 = cplx_of_parts(creal(no), cimag(no));
+        n3 = cplx_of_parts(creal(ni), cimag(ni));
+        flip = 1;
+    } else {
+        n1 = cplx_of_parts(creal(ni), cimag(ni));
+        n3 = cplx_of_parts(creal(no), cimag(no));
+        flip = -1;
+    }
+    sin2 = (n1 * cfp(sin1, 0)) / n2;
+    cos2 = csqrt(cfp(1, 0) - (sin2 * sin2));
+    sin3 = (n1 * cfp(sin1, 0)) / n3;
+    cos3 = csqrt(cfp(1, 0) - (sin3 * sin3));
+    vec cosThetaNormal = multvs_(normal, cosTheta);
+    P_in = creal(n1) * (((pow(creal(E1_amp), 2.0) + pow(cimag(E1_amp), 2.0)) + pow(creal(E2_amp), 2.0)) +
+                        pow(cimag(E2_amp), 2.0));
+    if (P_in == 0.0) return;
+    n1cos1 = n1 * cfp(cos1, 0);
+    n2cos2 = n2 * cos2;
+    n3cos3 = n3 * cos3;
+    dwc = ((2.0 * M_PI) * thickness) / wavelength;
+    phi = (((-cfp(0, 1.0)) * cfp(dwc, 0)) * (n2 - (sin2 * sin2))) / cos2;
+    ep1 = cexp(phi) / ((cfp(4, 0) * n2cos2) * n3cos3);
+    ep2 = cexp(cfp(-2L, 0) * phi);
+    M00 = (-ep1) * (((n1cos1 - n2cos2) * (n2cos2 + n3cos3)) + (((n1cos1 + n2cos2) * (n2cos2 - n3cos3)) * ep2));
+    M01 = ep1 * ((((n1cos1 - n2cos2) * (n2cos2 - n3cos3)) * ep2) + ((n1cos1 + n2cos2) * (n2cos2 + n3cos3)));
+    M10 = ep1 * (((n1cos1 - n2cos2) * (n2cos2 - n3cos3)) + (((n1cos1 + n2cos2) * (n2cos2 + n3cos3)) * ep2));
+    M11 = (-ep1) * ((((n1cos1 - n2cos2) * (n2cos2 + n3cos3)) * ep2) + ((n1cos1 + n2cos2) * (n2cos2 - n3cos3)));
+    R_s = (-M00) / M01;
+    T_s = M10 + (M11 * R_s);
+    n1cos2 = n1 * cos2;
+    n2cos1 = n2 * cfp(cos1, 0);
+    n2cos3 = n2 * cos3;
+    n3cos2 = n3 * cos2;
+    M00 = (-ep1) * (((n1cos2 - n2cos1) * (n2cos3 + n3cos2)) + (((n1cos2 + n2cos1) * (n2cos3 - n3cos2)) * ep2));
+    M01 = ep1 * ((((n1cos2 - n2cos1) * (n2cos3 - n3cos2)) * ep2) + ((n1cos2 + n2cos1) * (n2cos3 + n3cos2)));
+    M10 = ep1 * (((n1cos2 - n2cos1) * (n2cos3 - n3cos2)) + (((n1cos2 + n2cos1) * (n2cos3 + n3cos2)) * ep2));
+    M11 = (-ep1) * ((((n1cos2 - n2cos1) * (n2cos3 + n3cos2)) * ep2) + ((n1cos2 + n2cos1) * (n2cos3 - n3cos2)));
+    R_p = (-M00) / M01;
+    T_p = M10 + (M11 * R_p);
+    R_s = R_s * E1_amp;
+    R_p = R_p * E2_amp;
+    if (((creal(n1) * (pow(cabs(R_s), 2.0) + pow(cabs(R_p), 2.0))) / P_in) > m->reflection_threshold) {
+        vec reflected = subvv_(in_direction, multvs_(cosThetaNormal, 2.0));
+        st_v(sp_ray.origin, point);
+        st_v(sp_ray.normal, normal);
+        st_v(sp_ray.direction, reflected);
+        sp_ray.length = rp_inf();
+        sp_ray.E1_amp[0] = creal(R_s); sp_ray.E1_amp[1] = cimag(R_s);
+        sp_ray.E2_amp[0] = -creal(R_p); sp_ray.E2_amp[1] = -cimag(R_p);
+        sp_ray.parent_idx = idx;
+        sp_ray.refractive_index[0] = creal(n1); sp_ray.refractive_index[1] = cimag(n1);
+        sp_ray.ray_type_id |= RP_REFL_RAY;
+        add_ray(out, &sp_ray);
+    }
+    vec tangent = subvv_(in_direction, cosThetaNormal);
+    vec tg2 = multvs_(tangent, creal(n1) / creal(n3));
+    tan_mag_sq = mag_sq_(tg2);
+    c2 = sqrt(1 - tan_mag_sq);
+    vec transmitted = subvv_(tg2, multvs_(normal, (c2 * flip)));
+    aspect = sqrt(creal(cos3) / cos1);
+    T_s = T_s * (E1_amp * cfp(aspect, 0));
+    T_p = T_p * (E2_amp * cfp(aspect, 0));
+    if (((creal(n3) * (pow(cabs(T_s), 2.0) + pow(cabs(T_p), 2.0))) / P_in) > m->transmission_threshold) {
+        st_v(sp_ray.origin, point);
+        st_v(sp_ray.normal, normal);
+        st_v(sp_ray.direction, transmitted);
+        sp_ray.length = rp_inf();
+        sp_ray.E1_amp[0] = creal(T_s); sp_ray.E1_amp[1] = cimag(T_s);
+        sp_ray.E2_amp[0] = creal(T_p); sp_ray.E2_amp[1] = cimag(T_p);
+        sp_ray.parent_idx = idx;
+        sp_ray.refractive_index[0] = creal(n3); sp_ray.refractive_index[1] = cimag(n3);
         sp_ray.ray_type_id &= ~RP_REFL_RAY;
         add_ray(out, &sp_ray);
     }
@@ -1045,6 +1160,46 @@ static void eval_child_ray(const mat_ctx *mc, const rp_material *m, const rp_ray
     case RP_MAT_FULL_DIELECTRIC_DISPERSIVE:
         fresnel_split(mc, m, 0, 0, 1, in_ray, idx, point, orient, out);
         return;
+    case RP_MAT_SINGLE_LAYER_COATED:
+    case RP_MAT_COATED_DISPERSIVE:
+        coated_split(mc, m, in_ray, idx, point, orient, out);
+        return;
+    case RP_MAT_DIFFRACTION_GRATING: { /* cmaterials.pyx:1474-1543; p: lines_per_mm, order, efficiency, origin */
+        vec normal = norm_(orient.normal);
+        vec tangent = norm_(orient.tangent);
+        vec tangent2 = cross_(normal, tangent);
+        double wavelen = mc->wl[in_ray->wavelength_idx];
+        double line_spacing = (1000.0 / m->p[0]);
+        vec reflected = norm_(ld_v(in_ray->direction));
+        double k_z = dotprod_(normal, reflected);
+        double k_y = dotprod_(tangent2, reflected);
+        double k_x = dotprod_(tangent, reflected);
+        int sign = (k_z < 0.0) ? 1 : -1;
+        int order = (int)m->p[1];
+        k_x = (k_x - ((order * wavelen) / (line_spacing * in_ray->refractive_index[0])));
+        k_z = ((1.0 - (k_x * k_x)) - (k_y * k_y));
+        if (k_z < 0) return;
+        k_z = (sign * sqrt(k_z));
+        reflected = multvs_(tangent, k_x);
+        reflected = addvv_(reflected, multvs_(tangent2, k_y));
+        reflected = addvv_(reflected, multvs_(normal, k_z));
+        rp_ray sp_ray = convert_to_sp(*in_ray, normal);
+        sp_ray.accumulated_path = (sp_ray.accumulated_path + (sp_ray.length * sp_ray.refractive_index[0]));
+        st_v(sp_ray.origin, point);
+        st_v(sp_ray.normal, normal);
+        st_v(sp_ray.direction, reflected);
+        double eff = m->p[2];
+        sp_ray.E1_amp[0] = ((-sp_ray.E1_amp[0]) * eff);
+        sp_ray.E1_amp[1] = ((-sp_ray.E1_amp[1]) * eff);
+        sp_ray.E2_amp[0] = (sp_ray.E2_amp[0] * eff);
+        sp_ray.E2_amp[1] = (sp_ray.E2_amp[1] * eff);
+        sp_ray.parent_idx = idx;
+        sp_ray.ray_type_id |= RP_REFL_RAY;
+        sp_ray.phase = (sp_ray.phase + (((((1000.0 * dotprod_(subvv_(ld_v(&m->p[3]), point), tangent)) * order) *
+                                          2.0) * M_PI) / line_spacing));
+        add_ray(out, &sp_ray);
+        return;
+    }
     case RP_MAT_CIRCULAR_APERTURE: { /* cmaterials.pyx:1639-1662; p: outer_radius, radius, edge_width, invert, origin */
         vec origin = ld_v(&m->p[4]);
         double width = m->p[2];
@@ -1257,7 +1412,7 @@ int rp_oracle_version(void) { return RP_ABI_VERSION; }
 int rp_oracle_trace_segment(const rp_scene_desc *s, const double *wl, int64_t n_wl, rp_ray *rays, uint64_t n,
                             float max_length, int one_list, int one_face, double e2_terminate,
                             rp_ray *out, uint64_t out_cap, uint64_t *n_out, uint32_t *face_counts) {
-    mat_ctx mc = {s, NULL, n_wl};
+    mat_ctx mc = {s, NULL, n_wl, wl};
     cplx *tab = NULL;
     int rc = build_n_tables(s, wl, n_wl, &tab);
     if (rc) return rc;
@@ -1274,7 +1429,7 @@ int rp_oracle_trace_rays(const rp_scene_desc *s, const double *wl, int64_t n_wl,
                          int recursion_limit, float max_length, double e2_terminate, rp_ray *out,
                          uint64_t out_cap, uint64_t *gen_offsets, int max_gens, int *n_gens,
                          uint32_t *face_counts) {
-    mat_ctx mc = {s, NULL, n_wl};
+    mat_ctx mc = {s, NULL, n_wl, wl};
     cplx *tab = NULL;
     int rc = build_n_tables(s, wl, n_wl, &tab);
     if (rc) return rc;
@@ -1330,7 +1485,7 @@ void rp_oracle_convert_to_sp(const rp_ray *in, const double *normal, rp_ray *out
 int rp_oracle_eval_child_ray(const rp_scene_desc *s, const double *wl, int64_t n_wl, int mat, const rp_ray *in,
                              uint32_t idx, const double *point, const double *normal, const double *tangent,
                              rp_ray *out2) {
-    mat_ctx mc = {s, NULL, n_wl};
+    mat_ctx mc = {s, NULL, n_wl, wl};
     cplx *tab = NULL;
     if (build_n_tables(s, wl, n_wl, &tab)) return -1;
     mc.n_tab = tab;

@@ -17,7 +17,7 @@ from .ctracer import InterfaceMaterial, Ray
 
 (MAT_NONE, MAT_OPAQUE, MAT_TRANSPARENT, MAT_PEC, MAT_PARTIAL, MAT_LINEAR_POLARISING, MAT_WAVEPLATE,
  MAT_DIELECTRIC, MAT_FULL_DIELECTRIC, MAT_FULL_DIELECTRIC_DISPERSIVE, MAT_CIRCULAR_APERTURE,
- MAT_RECT_APERTURE) = range(12)
+ MAT_RECT_APERTURE, MAT_SINGLE_LAYER_COATED, MAT_COATED_DISPERSIVE, MAT_DIFFRACTION_GRATING) = range(15)
 
 
 def Convert_to_SP(ray, normal):
@@ -232,6 +232,63 @@ class FullDielectricDispersiveMaterial(InterfaceMaterial):
         rec['curve_outside'] = tables.add_dispersion(self.dispersion_outside)
         rec['reflection_threshold'] = self.reflection_threshold
         rec['transmission_threshold'] = self.transmission_threshold
+
+
+class SingleLayerCoatedMaterial(FullDielectricMaterial):
+    """cmaterials.pyx:1017-1184: Fresnel coefficients of one thin film (index
+    n_coating, thickness in microns) on the interface, by the reference's
+    characteristic-matrix product; the ray's wavelength enters the film phase."""
+    type_code = MAT_SINGLE_LAYER_COATED
+
+    def _pack(self, rec, tables):
+        super()._pack(rec, tables)
+        c = complex(self.n_coating)
+        rec['p'][:3] = (c.real, c.imag, float(self.thickness))
+
+
+class CoatedDispersiveMaterial(InterfaceMaterial):
+    """cmaterials.pyx:1187-1381: the single-layer coating with every index
+    (inside, outside, coating) from a dispersion curve at the ray's wavelength."""
+    type_code = MAT_COATED_DISPERSIVE
+
+    def __init__(self, **kwds):
+        super().__init__(**kwds)
+        self.reflection_threshold = float(kwds.get('reflection_threshold', 0.1))
+        self.transmission_threshold = float(kwds.get('transmission_threshold', 0.1))
+        self.dispersion_inside = kwds.get("dispersion_inside", vacuum)
+        self.dispersion_outside = kwds.get("dispersion_outside", vacuum)
+        self.dispersion_coating = kwds.get("dispersion_coating", vacuum)
+        self.coating_thickness = float(kwds.get("coating_thickness", 0.1))
+
+    def on_set_wavelengths(self):
+        self.dispersion_inside._check_range(self._wavelengths)
+        self.dispersion_outside._check_range(self._wavelengths)
+        self.dispersion_coating._check_range(self._wavelengths)
+
+    def _pack(self, rec, tables):
+        rec['curve_inside'] = tables.add_dispersion(self.dispersion_inside)
+        rec['curve_outside'] = tables.add_dispersion(self.dispersion_outside)
+        rec['p'][0] = float(tables.add_dispersion(self.dispersion_coating))
+        rec['p'][1] = self.coating_thickness
+        rec['reflection_threshold'] = self.reflection_threshold
+        rec['transmission_threshold'] = self.transmission_threshold
+
+
+class DiffractionGratingMaterial(InterfaceMaterial):
+    """cmaterials.pyx:1437-1543: a reflective grating; the diffracted direction
+    shifts the component along the face tangent by order * wavelength /
+    (line spacing * n), and the grating phase depends on the offset from `origin`."""
+    type_code = MAT_DIFFRACTION_GRATING
+
+    def __init__(self, **kwds):
+        super().__init__(**kwds)
+        self.lines_per_mm = float(kwds.get("lines_per_mm", 1000))
+        self.order = int(kwds.get("order", 1))
+        self.efficiency = float(kwds.get("efficiency", 1.0))
+        self.origin = tuple(map(float, kwds.get("origin", (0.0, 0.0, 0.0))))
+
+    def _pack(self, rec, tables):
+        rec['p'][:6] = (self.lines_per_mm, float(self.order), self.efficiency) + tuple(self.origin)
 
 
 class CircularApertureMaterial(InterfaceMaterial):

@@ -221,10 +221,13 @@ static int validate_scene(const rp_scene_desc *d) {
     }
     for (int m = 0; m < d->n_materials; m++) {
         const rp_material &M = d->materials[m];
-        if (M.type < RP_MAT_NONE || M.type > RP_MAT_RECT_APERTURE) return RP_ERR_UNSUPPORTED;
-        if (M.type == RP_MAT_FULL_DIELECTRIC_DISPERSIVE &&
+        if (M.type < RP_MAT_NONE || M.type > RP_MAT_DIFFRACTION_GRATING) return RP_ERR_UNSUPPORTED;
+        if ((M.type == RP_MAT_FULL_DIELECTRIC_DISPERSIVE || M.type == RP_MAT_COATED_DISPERSIVE) &&
             (M.curve_inside < 0 || M.curve_inside >= d->n_dispersions || M.curve_outside < 0 ||
              M.curve_outside >= d->n_dispersions))
+            return RP_ERR_INVALID;
+        if (M.type == RP_MAT_COATED_DISPERSIVE &&
+            !(M.p[0] >= 0.0 && M.p[0] < (double)d->n_dispersions && M.p[0] == (double)(int)M.p[0]))
             return RP_ERR_INVALID;
     }
     for (int c = 0; c < d->n_dispersions; c++) {
@@ -340,6 +343,7 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     S.bounds = (const float *)(b + o_bnd);
     S.face_list = nullptr;
     S.n_wl = n_wl;
+    S.wl = (const double *)(b + o_wl);
     S.n_lists = d->n_lists;
     S.n_faces = d->n_faces;
     S.n_recs = d->n_face_records;

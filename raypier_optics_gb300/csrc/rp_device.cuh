@@ -20,6 +20,7 @@ struct DevScene {
     const rp_distortion *dists;
     const double *aux;
     const double2 *ntab;  // [n_dispersions][n_wl] complex index per curve and wavelength
+    const double *wl;     // [n_wl] the wavelengths (um)
     const float *bounds;  // [n_faces][8]: world box lo[3], hi[3], skippable flag (rp_bounds.h)
     const short *face_list;  // [n_faces]: owning face list of each traced face
     long long n_wl;
@@ -759,6 +760,7 @@ struct Child {
 struct ChildCommon {
     v3 origin, normal, E;
     double opl;
+    double dphase;  // added to the parent's phase (the grating phase; 0 otherwise)
 };
 
 // convert_to_sp (cmaterials.pyx:49-91).  Returns false at normal incidence,
@@ -785,12 +787,126 @@ __device__ __forceinline__ void convert_to_sp(const RayState &r, v3 normal, v3 &
     E_out = S;
 }
 
+// e^z (CUDA's exp, sin and cos; the reference calls glibc's cexp)
+__device__ __forceinline__ cx cexp_(cx z) {
+    double e = exp(z.x), s, c;
+    sincos(z.y, &s, &c);
+    return mkc(e * c, e * s);
+}
+
+// SingleLayerCoatedMaterial.eval_child_ray_c (cmaterials.pyx:1026-1184) and
+// CoatedDispersiveMaterial.eval_child_ray_c (1228-1381): Fresnel coefficients
+// of a single thin film (index n2, thickness in um) between n1 and n3 by the
+// reference's characteristic-matrix product, with its phase
+// phi = -i (2 pi t / lambda) (n2 - sin2^2) / cos2.
+static __device__ int coated_children(const DevScene &S, const rp_material &m, const RayState &r, v3 point,
+                                      v3 onormal, ChildCommon &cc, Child *ch, unsigned *err) {
+    const double INF = inf_d();
+    const long long w = (long long)r.wl;
+    if (w >= S.n_wl) {
+        atomicOr(err, ERR_WAVELENGTH);
+        return 0;
+    }
+    const double wavelength = S.wl[w];
+    v3 normal = normv_fast(onormal);
+    v3 ind = normv_fast(r.d);
+    cx E1, E2;
+    convert_to_sp(r, normal, cc.E, E1, E2);
+    cc.opl = r.opl + (r.len * r.n.x);
+    cc.origin = point;
+    cc.normal = normal;
+    const double cosTheta = dotv(normal, ind);
+    const double cos1 = fabs(cosTheta);
+    const double sin1 = sqrt(fabs(1 - cos1 * cos1));
+    const bool out_to_in = cosTheta < 0.0;
+    cx n1, n2, n3;
+    double thickness;
+    if (m.type == RP_MAT_SINGLE_LAYER_COATED) {
+        cx ni = mkc(m.n_inside[0], 0.0 + m.n_inside[1]), no = mkc(m.n_outside[0], 0.0 + m.n_outside[1]);
+        n2 = mkc(m.p[0], 0.0 + m.p[1]);
+        n1 = out_to_in ? no : ni;
+        n3 = out_to_in ? ni : no;
+        thickness = m.p[2];
+    } else {
+        const cx ni = S.ntab[(long long)m.curve_inside * S.n_wl + w];
+        const cx no = S.ntab[(long long)m.curve_outside * S.n_wl + w];
+        const cx nc = S.ntab[(long long)m.p[0] * S.n_wl + w];
+        n2 = mkc(nc.x, 0.0 + nc.y);
+        n1 = out_to_in ? mkc(no.x, 0.0 + no.y) : mkc(ni.x, 0.0 + ni.y);
+        n3 = out_to_in ? mkc(ni.x, 0.0 + ni.y) : mkc(no.x, 0.0 + no.y);
+        thickness = m.p[1];
+    }
+    const double flip = out_to_in ? 1 : -1;
+    const cx sin2 = cdiv(cmuls(n1, sin1), n2);
+    const cx cos2 = csqrt_(csub(mkc(1.0, 0.0), cmul(sin2, sin2)));
+    const cx sin3 = cdiv(cmuls(n1, sin1), n3);
+    const cx cos3 = csqrt_(csub(mkc(1.0, 0.0), cmul(sin3, sin3)));
+    const v3 ctn = mulvs(normal, cosTheta);
+    const double P_in = n1.x * (((E1.x * E1.x + E1.y * E1.y) + E2.x * E2.x) + E2.y * E2.y);
+    if (P_in == 0.0) return 0;
+    const cx n1cos1 = cmuls(n1, cos1), n2cos2 = cmul(n2, cos2), n3cos3 = cmul(n3, cos3);
+    const double dwc = ((2.0 * 3.141592653589793) * thickness) / wavelength;
+    // -i dwc = (0, -dwc)
+    const cx phi = cdiv(cmul(mkc(0.0, -dwc), csub(n2, cmul(sin2, sin2))), cos2);
+    const cx ep1 = cdiv(cexp_(phi), cmul(cmuls(n2cos2, 4.0), n3cos3));
+    const cx ep2 = cexp_(cmuls(phi, -2.0));
+    // s polarisation
+    cx a = csub(n1cos1, n2cos2), bq = cadd(n1cos1, n2cos2), c = cadd(n2cos2, n3cos3), d = csub(n2cos2, n3cos3);
+    cx M00 = cmul(mkc(-ep1.x, -ep1.y), cadd(cmul(a, c), cmul(cmul(bq, d), ep2)));
+    cx M01 = cmul(ep1, cadd(cmul(cmul(a, d), ep2), cmul(bq, c)));
+    cx M10 = cmul(ep1, cadd(cmul(a, d), cmul(cmul(bq, c), ep2)));
+    cx M11 = cmul(mkc(-ep1.x, -ep1.y), cadd(cmul(cmul(a, c), ep2), cmul(bq, d)));
+    cx R_s = cdiv(mkc(-M00.x, -M00.y), M01);
+    cx T_s = cadd(M10, cmul(M11, R_s));
+    // p polarisation
+    const cx n1cos2 = cmul(n1, cos2), n2cos1 = cmuls(n2, cos1), n2cos3 = cmul(n2, cos3), n3cos2 = cmul(n3, cos2);
+    a = csub(n1cos2, n2cos1);
+    bq = cadd(n1cos2, n2cos1);
+    c = cadd(n2cos3, n3cos2);
+    d = csub(n2cos3, n3cos2);
+    M00 = cmul(mkc(-ep1.x, -ep1.y), cadd(cmul(a, c), cmul(cmul(bq, d), ep2)));
+    M01 = cmul(ep1, cadd(cmul(cmul(a, d), ep2), cmul(bq, c)));
+    M10 = cmul(ep1, cadd(cmul(a, d), cmul(cmul(bq, c), ep2)));
+    M11 = cmul(mkc(-ep1.x, -ep1.y), cadd(cmul(cmul(a, c), ep2), cmul(bq, d)));
+    cx R_p = cdiv(mkc(-M00.x, -M00.y), M01);
+    cx T_p = cadd(M10, cmul(M11, R_p));
+    R_s = cmul(R_s, E1);
+    R_p = cmul(R_p, E2);
+    int nc = 0;
+    if (((n1.x * (cabs2_(R_s) + cabs2_(R_p))) / P_in) > m.reflection_threshold) {
+        ch[0].d = subv(ind, mulvs(ctn, 2.0));
+        ch[0].len = INF;
+        ch[0].e1 = R_s;
+        ch[0].e2 = mkc(-R_p.x, -R_p.y);
+        ch[0].n = n1;
+        ch[0].type = r.type | RP_REFL_RAY;
+        nc = 1;
+    }
+    v3 tg2 = mulvs(subv(ind, ctn), n1.x / n3.x);
+    double c2 = sqrt(1 - magsq(tg2));
+    v3 transmitted = subv(tg2, mulvs(normal, (c2 * flip)));
+    double aspect = sqrt(cos3.x / cos1);
+    T_s = cmul(T_s, cmuls(E1, aspect));
+    T_p = cmul(T_p, cmuls(E2, aspect));
+    if (((n3.x * (cabs2_(T_s) + cabs2_(T_p))) / P_in) > m.transmission_threshold) {
+        ch[nc].d = transmitted;
+        ch[nc].len = INF;
+        ch[nc].e1 = T_s;
+        ch[nc].e2 = T_p;
+        ch[nc].n = n3;
+        ch[nc].type = r.type & ~RP_REFL_RAY;
+        nc++;
+    }
+    return nc;
+}
+
 // InterfaceMaterial.eval_child_ray_c for every material type.  Writes up to two
 // children in emission order; returns their number.  `ntab` rows hold the
 // complex index of each dispersion curve per wavelength index.
 static __device__ int eval_children(const DevScene &S, const rp_material &m, const RayState &r, v3 point, v3 onormal,
                              v3 otangent, ChildCommon &cc, Child *ch, unsigned *err) {
     const double INF = inf_d();
+    cc.dphase = 0.0;
     switch (m.type) {
         case RP_MAT_NONE:
         case RP_MAT_OPAQUE: return 0;  // cmaterials.pyx:245-251
@@ -997,6 +1113,45 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
                 nc++;
             }
             return nc;
+        }
+        case RP_MAT_SINGLE_LAYER_COATED:
+        case RP_MAT_COATED_DISPERSIVE:
+            return coated_children(S, m, r, point, onormal, cc, ch, err);
+        case RP_MAT_DIFFRACTION_GRATING: {  // cmaterials.pyx:1474-1543
+            const long long w = (long long)r.wl;
+            if (w >= S.n_wl) {
+                atomicOr(err, ERR_WAVELENGTH);
+                return 0;
+            }
+            v3 normal = normv_fast(onormal);
+            v3 tangent = normv_fast(otangent);  // the grating vector
+            v3 tangent2 = crossv(normal, tangent);  // along the lines
+            const double wavelen = S.wl[w];
+            const double line_spacing = 1000.0 / m.p[0];  // um
+            v3 refl = normv_fast(r.d);
+            double k_z = dotv(normal, refl), k_y = dotv(tangent2, refl), k_x = dotv(tangent, refl);
+            const double sign = k_z < 0.0 ? 1.0 : -1.0;
+            const double order = m.p[1];
+            k_x = k_x - ((order * wavelen) / (line_spacing * r.n.x));
+            k_z = ((1.0 - (k_x * k_x)) - (k_y * k_y));
+            if (k_z < 0) return 0;  // evanescent order
+            k_z = sign * sqrt(k_z);
+            refl = addv(addv(mulvs(tangent, k_x), mulvs(tangent2, k_y)), mulvs(normal, k_z));
+            cx e1, e2;
+            convert_to_sp(r, normal, cc.E, e1, e2);
+            cc.opl = r.opl + (r.len * r.n.x);
+            cc.origin = point;
+            cc.normal = normal;
+            cc.dphase = ((((1000.0 * dotv(subv(mkv(m.p[3], m.p[4], m.p[5]), point), tangent)) * order) * 2.0) *
+                         3.141592653589793) / line_spacing;
+            const double eff = m.p[2];
+            ch[0].d = refl;
+            ch[0].n = r.n;
+            ch[0].e1 = mkc((-e1.x) * eff, (-e1.y) * eff);
+            ch[0].e2 = mkc(e2.x * eff, e2.y * eff);
+            ch[0].len = r.len;  // the reference keeps the parent's length here
+            ch[0].type = r.type | RP_REFL_RAY;
+            return 1;
         }
         case RP_MAT_CIRCULAR_APERTURE: {  // cmaterials.pyx:1639-1662
             double r_ = sqrt(magsq(subv(mkv(m.p[4], m.p[5], m.p[6]), point)));

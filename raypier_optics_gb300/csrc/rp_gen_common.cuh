@@ -102,7 +102,7 @@ __device__ __forceinline__ void store_child(const RaySoA &out, unsigned long lon
     out.e1[k] = ch.e1;
     out.e2[k] = ch.e2;
     out.len[k] = ch.len;
-    out.phase[k] = phase;
+    out.phase[k] = phase + cc.dphase;
     out.opl[k] = cc.opl;
     out.wl[k] = wl;
     out.parent[k] = parent;

@@ -94,7 +94,7 @@ static __device__ RayState load_record(const unsigned char *r) {
 }
 
 static __device__ void write_child_record(unsigned char *dst, const unsigned char *parent, const ChildCommon &cc,
-                                   const Child &ch, unsigned pidx) {
+                                   const Child &ch, unsigned pidx, double phase) {
     for (int k = 0; k < RP_RAY_BYTES / 4; k++)
         reinterpret_cast<unsigned *>(dst)[k] = reinterpret_cast<const unsigned *>(parent)[k];
     wr(dst, 0, cc.origin.x); wr(dst, 8, cc.origin.y); wr(dst, 16, cc.origin.z);
@@ -105,6 +105,7 @@ static __device__ void write_child_record(unsigned char *dst, const unsigned cha
     wr(dst, 112, ch.e1.x); wr(dst, 120, ch.e1.y);
     wr(dst, 128, ch.e2.x); wr(dst, 136, ch.e2.y);
     wr(dst, 144, ch.len);
+    wr(dst, 152, phase + cc.dphase);
     wr(dst, 160, cc.opl);
     wru(dst, 172, pidx);
     wru(dst, 184, ch.type);
@@ -124,7 +125,7 @@ __global__ void unit_material(DevScene S, int mat, const unsigned char *rays, co
     v3 ot = mkv(tng[3 * i], tng[3 * i + 1], tng[3 * i + 2]);
     int nc = eval_children(S, S.mats[mat], r, point, on, ot, cc, ch, err);
     for (int k = 0; k < nc; k++)
-        write_child_record(children + (2 * i + k) * RP_RAY_BYTES, rec, cc, ch[k], idx[i]);
+        write_child_record(children + (2 * i + k) * RP_RAY_BYTES, rec, cc, ch[k], idx[i], r.phase);
     n_children[i] = nc;
 }
 

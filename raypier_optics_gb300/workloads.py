@@ -70,7 +70,7 @@ def _make_curve(spec, ns):
 def _make_material(spec, ns, curves):
     cls = getattr(ns.cmaterials, spec["type"])
     kw = dict(spec.get("kw", {}))
-    for k in ("dispersion_inside", "dispersion_outside"):
+    for k in ("dispersion_inside", "dispersion_outside", "dispersion_coating"):
         if k in kw:
             kw[k] = curves[kw[k]]
     for k in ("n_inside", "n_outside", "n_coating"):

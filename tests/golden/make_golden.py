@@ -5,6 +5,7 @@ Run in a container that has the reference sources and Cython:
 
     python oracle/build_ref.py && python tests/golden/make_golden.py
     python tests/golden/make_golden.py --lens     # only the configuration-4 lens case
+    python tests/golden/make_golden.py --coated   # only the coated-material cases
 
 Every fixture stores the scene description (the JSON spec understood by
 raypier_optics_gb300.workloads.build_scene), the inputs, and the reference's
@@ -165,8 +166,40 @@ def material_zoo():
             }}
 
 
-def material_scene(mat_name):
-    zoo = material_zoo()
+def coated_zoo():
+    """Materials added after the first zoo -- thin-film coatings
+    (SingleLayerCoatedMaterial, CoatedDispersiveMaterial) and diffraction
+    gratings -- in their own fixtures."""
+    crown1 = material_zoo()["curves"]["crown1"]
+    mgf2 = {"formula_id": 0, "coefs": [1.38]}
+    film = {"formula_id": 0, "coefs": [2.05], "absorption": 0.8}
+    return {"curves": {"crown1": crown1, "flint": W.FLINT, "crown": W.CROWN, "air": W.AIR, "mgf2": mgf2,
+                       "film": film},
+            "materials": {
+                "coated_single": {"type": "SingleLayerCoatedMaterial",
+                                  "kw": {"n_inside": 1.5, "n_outside": 1.0, "n_coating": 1.38, "thickness": 0.1,
+                                         "reflection_threshold": -1.0, "transmission_threshold": -1.0}},
+                "coated_single_abs": {"type": "SingleLayerCoatedMaterial",
+                                      "kw": {"n_inside": [1.7, 0.01], "n_outside": 1.0, "n_coating": [2.1, 0.005],
+                                             "thickness": 0.35, "reflection_threshold": -1.0,
+                                             "transmission_threshold": -1.0}},
+                "coated_disp": {"type": "CoatedDispersiveMaterial",
+                                "kw": {"dispersion_inside": "crown1", "dispersion_outside": "air",
+                                       "dispersion_coating": "mgf2", "coating_thickness": 0.2,
+                                       "reflection_threshold": -1.0, "transmission_threshold": -1.0}},
+                "coated_disp_default": {"type": "CoatedDispersiveMaterial",
+                                        "kw": {"dispersion_inside": "flint", "dispersion_outside": "crown",
+                                               "dispersion_coating": "film", "coating_thickness": 0.15}},
+                "grating": {"type": "DiffractionGratingMaterial",
+                            "kw": {"lines_per_mm": 600.0, "order": 1, "efficiency": 0.8,
+                                   "origin": [0.3, -0.2, 20.0]}},
+                "grating_m2": {"type": "DiffractionGratingMaterial",
+                               "kw": {"lines_per_mm": 1200.0, "order": -2, "efficiency": 1.0}},
+            }}
+
+
+def material_scene(mat_name, zoo=None):
+    zoo = zoo or material_zoo()
     spec = {"curves": zoo["curves"], "materials": {mat_name: zoo["materials"][mat_name],
                                                    "detector": {"type": "OpaqueMaterial"}},
             "lists": [{"translation": [0, 0, 20.0], "faces": [
@@ -373,7 +406,52 @@ def main():
     np.savez_compressed(os.path.join(out_dir, "face_zoo_specs.npz"),
                         specs=np.array(json.dumps({k: face_scene(v) for k, v in zoo.items()})))
     lens_case(ref, out_dir)
+    coated_case(ref, out_dir)
     print("golden vectors written to", out_dir)
+
+
+def coated_case(ref, out_dir):
+    """The coated materials: trace cases mat_<name>.npz and eval_child_ray
+    unit vectors in units_coated.npz, with their own random stream."""
+    rdt = ref.ctracer.ray_dtype
+    rng = np.random.Generator(np.random.PCG64(RNG_SEED + 41))
+    zoo = coated_zoo()
+    units = {}
+    for name in zoo["materials"]:
+        spec = material_scene(name, zoo)
+        per_ray = name.startswith("coated_disp")
+        r1, wla = random_rays(rdt, rng, 40, 0.0, +1.0, 1.2, 12.0, per_ray_wl=True, wl_range=(0.4, 1.0))
+        r2, wlb = random_rays(rdt, rng, 24, 40.0, -1.0, 1.2, 12.0, per_ray_wl=True, wl_range=(0.4, 1.0))
+        rays = np.concatenate([r1, r2])
+        rays['ray_ident'] = np.arange(len(rays), dtype=np.uint32)
+        rays['wavelength_idx'] = np.arange(len(rays), dtype=np.uint32)
+        wl = np.concatenate([wla, wlb])
+        params = {"recursion_limit": 3, "max_length": 300.0, "e2_terminate": 0.0}
+        gens, counts = run_reference(ref, spec, rays, wl, params["recursion_limit"], params["max_length"])
+        save_trace_case(os.path.join(out_dir, f"mat_{name}.npz"), spec, rays, wl, params, gens, counts)
+        lists = W.build_scene(spec, ref)
+        mat = lists[0].faces[0].material
+        mat.wavelengths = np.asarray(wl, dtype=np.double)
+        rc = ref.ctracer.RayCollection.from_array(rays.copy())
+        nrm = rng.normal(0, 1, (len(rays), 3))
+        nrm[:4] = rays['direction'][:4]
+        tng = rng.normal(0, 1, (len(rays), 3))
+        pts = rng.uniform(-10, 10, (len(rays), 3))
+        pts[:, 2] += 20.0
+        kids, nk = [], []
+        for i in range(len(rays)):
+            out = ref.ctracer.RayCollection(2)
+            mat.eval_child_ray(rc[i], i, tuple(pts[i]), tuple(nrm[i]), tuple(tng[i]), out)
+            a = out.copy_as_array()
+            nk.append(len(a))
+            kids.append(a)
+        units[f"mat_{name}_normals"] = nrm
+        units[f"mat_{name}_tangents"] = tng
+        units[f"mat_{name}_points"] = pts
+        units[f"mat_{name}_nkids"] = np.array(nk)
+        units[f"mat_{name}_kids"] = np.concatenate(kids) if kids else np.zeros(0, rdt)
+    np.savez_compressed(os.path.join(out_dir, "units_coated.npz"), **units)
+
 
 
 def lens_case(ref, out_dir):
@@ -392,5 +470,7 @@ def lens_case(ref, out_dir):
 if __name__ == "__main__":
     if sys.argv[1:] == ["--lens"]:
         lens_case(build_ref.load(), HERE)
+    elif sys.argv[1:] == ["--coated"]:
+        coated_case(build_ref.load(), HERE)
     else:
         main()

@@ -31,6 +31,18 @@ def trace_case_names():
                   if not os.path.basename(p).startswith(("units", "face_zoo")))
 
 
+def load_units():
+    """The reference's single-call outputs: units.npz plus the coated-material
+    vectors of units_coated.npz, as one mapping."""
+    out = dict(np.load(os.path.join(GOLDEN, "units.npz")))
+    out.update(dict(np.load(os.path.join(GOLDEN, "units_coated.npz"))))
+    return out
+
+
+def material_unit_names(units):
+    return sorted({k[len("mat_"):-len("_nkids")] for k in units if k.startswith("mat_") and k.endswith("_nkids")})
+
+
 def load_case(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     spec = json.loads(str(z["spec"]))

@@ -14,8 +14,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import (GOLDEN, assert_generations, assert_records, build, load_case, tables_for,
-                     trace_case_names)
+from helpers import (GOLDEN, assert_generations, assert_records, build, load_case, tables_for, trace_case_names, load_units, material_unit_names)
 from raypier_optics_gb300 import cmaterials, ctracer, scene, tracer, unitcalls
 from raypier_optics_gb300 import workloads as W
 from raypier_optics_gb300.ctracer import RayCollection
@@ -129,8 +128,8 @@ def test_gpu_trace_one_face_segment_matches_oracle():
 
 
 # ---- single-plugin calls against the reference's unit outputs ----------------------------
-UNITS = np.load(os.path.join(GOLDEN, "units.npz"))
-FACE_NAMES = sorted({k[len("face_"):-len("_dist_base")] for k in UNITS.files
+UNITS = load_units()
+FACE_NAMES = sorted({k[len("face_"):-len("_dist_base")] for k in UNITS
                      if k.startswith("face_") and k.endswith("_dist_base")})
 
 
@@ -146,17 +145,16 @@ def test_gpu_face_intersect_and_normal_match_reference(name):
                                rtol=1e-9, atol=1e-12)
     np.testing.assert_allclose(unitcalls.face_normal(f, UNITS[f"face_{name}_pts"]), UNITS[f"face_{name}_normal"],
                                rtol=1e-9, atol=1e-12)
-    if f"face_{name}_xy" in UNITS.files:
+    if f"face_{name}_xy" in UNITS:
         np.testing.assert_array_equal(unitcalls.shape_inside(f.shape, UNITS[f"face_{name}_xy"]),
                                       UNITS[f"face_{name}_inside"])
-    if f"face_{name}_dist_zg" in UNITS.files:
+    if f"face_{name}_dist_zg" in UNITS:
         out = unitcalls.distortion_eval(f.distortion, UNITS[f"face_{name}_dist_x"], UNITS[f"face_{name}_dist_y"])
         np.testing.assert_allclose(out[:, :3], UNITS[f"face_{name}_dist_zg"], rtol=1e-9, atol=1e-15)
         np.testing.assert_allclose(out[:, 3], UNITS[f"face_{name}_dist_z"], rtol=1e-9, atol=1e-15)
 
 
-MAT_NAMES = sorted({k[len("mat_"):-len("_nkids")] for k in UNITS.files
-                    if k.startswith("mat_") and k.endswith("_nkids")})
+MAT_NAMES = material_unit_names(UNITS)
 
 
 @pytest.mark.parametrize("name", MAT_NAMES)

@@ -12,7 +12,8 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import GOLDEN, X86, assert_generations, load_case, tables_for, trace_case_names
+from helpers import (GOLDEN, X86, assert_generations, assert_records, load_case, load_units,
+                     material_unit_names, tables_for, trace_case_names)
 from raypier_optics_gb300 import ctracer, workloads as W
 
 
@@ -69,3 +70,21 @@ def test_oracle_termination_drops_weak_children_stably():
     np.testing.assert_array_equal(term[1]["parent_idx"], keep["parent_idx"])
     np.testing.assert_array_equal(term[1]["ray_type_id"], keep["ray_type_id"])
     assert len(term[1]) < len(full[1])
+
+
+UNITS = load_units()
+
+
+@pytest.mark.parametrize("name", material_unit_names(UNITS))
+def test_oracle_material_eval_matches_reference(name):
+    """eval_child_ray of every material (random orientations, normal incidence
+    among them) against the reference's own calls."""
+    c = load_case("mat_" + name)
+    tables, lists, _ = tables_for(c["spec"])
+    mat_idx = 0  # the material of the case's first face is the first in the table
+    kids = oracle.eval_child_rays(tables, c["wl"], mat_idx, c["rays"], np.arange(len(c["rays"])),
+                                  UNITS[f"mat_{name}_points"], UNITS[f"mat_{name}_normals"],
+                                  UNITS[f"mat_{name}_tangents"])
+    np.testing.assert_array_equal([len(k) for k in kids], UNITS[f"mat_{name}_nkids"])
+    got = np.concatenate(kids) if kids else np.zeros(0, dtype=ctracer.ray_dtype)
+    assert_records(got, UNITS[f"mat_{name}_kids"], exact=X86, what=name)
