@@ -87,7 +87,13 @@ enum rp_face_type {
     RP_FACE_DISTORTION = 9,    /* DistortionFace        cfaces.pyx:2323-2438 p: accuracy; base, distortion */
     RP_FACE_ORIENTED_POLYGON = 10, /* OrientedPolygonFace cfaces.pyx:1121-1222 p: origin[3], normal[3], x_axis[3], y_axis[3]; aux: xy[n_aux0][2] */
     RP_FACE_POLYGON = 11,      /* PolygonFace           cfaces.pyx:1077-1118 p: z_plane; aux: xy[n_aux0][2] */
-    RP_FACE_ELLIPTICAL_PLANE = 12 /* ElipticalPlaneFace cfaces.pyx:313-351  p: g_x, g_y, diameter */
+    RP_FACE_ELLIPTICAL_PLANE = 12, /* ElipticalPlaneFace cfaces.pyx:313-351  p: g_x, g_y, diameter */
+    RP_FACE_OFF_AXIS_PARABOLIC = 13, /* OffAxisParabolicFace cfaces.pyx:1224-1315 p: EFL, diameter, height */
+    RP_FACE_ELLIPSOIDAL = 14,  /* EllipsoidalFace       cfaces.pyx:1318-1410 p: major, minor, x1, x2, y1, y2, z1, z2;
+                                  aux: trans m[9] t[3], inv_trans m[9] t[3] (24 doubles) */
+    RP_FACE_SADDLE = 15,       /* SaddleFace            cfaces.pyx:1413-1511 p: z_height, curvature */
+    RP_FACE_CYLINDRICAL = 16,  /* CylindericalFace      cfaces.pyx:1516-1602 p: z_height, radius */
+    RP_FACE_AXICON = 17        /* AxiconFace            cfaces.pyx:1605-1680 p: z_height, gradient */
 };
 
 #define RP_FACE_NPARAM 16

@@ -578,6 +578,190 @@ static isect_t face_intersect(const rp_scene_desc *s, const rp_face *f, vec p1, 
         }
         return out;
     }
+    case RP_FACE_OFF_AXIS_PARABOLIC: { /* cfaces.pyx:1228-1297; p: EFL, diameter, height */
+        double efl = f->p[0], A = 1 / (2 * f->p[0]);
+        double a, b, c, d, a1, a2;
+        vec sv = subvv_(p2, p1), r = p1, pt1, pt2;
+        r.z += efl / 2.;
+        a = A * (pow(sv.x, 2.0) + pow(sv.y, 2.0));
+        b = 2 * A * (r.x * sv.x + r.y * sv.y) - sv.z;
+        c = A * (pow(r.x, 2.0) + pow(r.y, 2.0)) - r.z;
+        d = pow(b, 2.0) - 4 * a * c;
+        if (d < 0) return NO_INTERSECTION;
+        if (a < 1e-10) {
+            a1 = -c / b;
+            pt1 = addvv_(r, multvs_(sv, a1));
+            pt1.x -= efl;
+            if ((pt1.x * pt1.x + pt1.y * pt1.y) > (f->p[1] / 2)) return NO_INTERSECTION;
+            if (a1 > 1.0 || a1 < f->tolerance) return NO_INTERSECTION;
+            out.dist = a1 * sep_(p1, p2);
+            return out;
+        }
+        d = sqrt(d);
+        a1 = (-b + d) / (2 * a);
+        pt1 = addvv_(r, multvs_(sv, a1));
+        a2 = (-b - d) / (2 * a);
+        pt2 = addvv_(r, multvs_(sv, a2));
+        pt1.x -= efl;
+        pt2.x -= efl;
+        if (is_base_ray) {
+            d = f->p[1];
+            d *= d / 4.;
+            if ((pt1.x * pt1.x + pt1.y * pt1.y) > d) a1 = rp_inf();
+            if ((pt2.x * pt2.x + pt2.y * pt2.y) > d) a2 = rp_inf();
+        }
+        if (a2 < a1) a1 = a2;
+        if (a1 > 1.0 || a1 < f->tolerance) return NO_INTERSECTION;
+        out.dist = a1 * sep_(p1, p2);
+        return out;
+    }
+    case RP_FACE_ELLIPSOIDAL: { /* cfaces.pyx:1339-1384; p: major, minor, x1, x2, y1, y2, z1, z2 */
+        const rp_transform *trans = (const rp_transform *)(s->aux + f->aux);
+        vec S = subvv_(p2, p1);
+        vec r = transform_c(trans, p1);
+        vec sv = transform_c(trans, p2);
+        double A, B, a, b, c, d, root1, root2;
+        sv = subvv_(sv, r);
+        B = pow(f->p[1], 2.0);
+        A = pow(f->p[0], 2.0);
+        a = A * (sv.z * sv.z + sv.y * sv.y) + B * sv.x * sv.x;
+        b = 2 * (A * (r.z * sv.z + r.y * sv.y) + B * r.x * sv.x);
+        c = A * (r.z * r.z + r.y * r.y) + B * r.x * r.x - A * B;
+        d = b * b - 4 * a * c;
+        d = sqrt(d);
+        root1 = (-b + d) / (2 * a);
+        root2 = (-b - d) / (2 * a);
+        p2 = addvv_(p1, multvs_(S, root2));
+        p1 = addvv_(p1, multvs_(S, root1));
+        if (is_base_ray) {
+            if (!(f->p[2] < p2.x && p2.x < f->p[3])) root2 = 2;
+            if (!(f->p[4] < p2.y && p2.y < f->p[5])) root2 = 2;
+            if (!(f->p[6] < p2.z && p2.z < f->p[7])) root2 = 2;
+            if (!(f->p[2] < p1.x && p1.x < f->p[3])) root1 = 2;
+            if (!(f->p[4] < p1.y && p1.y < f->p[5])) root1 = 2;
+            if (!(f->p[6] < p1.z && p1.z < f->p[7])) root1 = 2;
+        }
+        if (root1 < f->tolerance) root1 = 2;
+        if (root2 < f->tolerance) root2 = 2;
+        if (root1 > root2) root1 = root2;
+        if (root1 > 1) return NO_INTERSECTION;
+        out.dist = root1 * mag_(S);
+        return out;
+    }
+    case RP_FACE_SADDLE: { /* cfaces.pyx:1421-1495; p: z_height, curvature */
+        double A = sqrt(6.0), root, denom, a1, a2;
+        vec d, p, pt1, pt2;
+        A *= f->p[1];
+        p = p1;
+        p.z -= f->p[0];
+        d = subvv_(p2, p1);
+        if (d.x == 0.0) {
+            a1 = (-A * (p.x * p.y) + p.z) / (A * d.y * p.x - d.z);
+            a2 = rp_inf();
+        } else if (d.y == 0.0) {
+            a1 = (-A * (p.x * p.y) + p.z) / (A * d.x * p.y - d.z);
+            a2 = rp_inf();
+        } else {
+            root = (pow(A, 2.0)) * (pow(d.x, 2.0)) * (pow(p.y, 2.0)) - 2 * (pow(A, 2.0)) * d.x * d.y * p.x * p.y +
+                   (pow(A, 2.0)) * (pow(d.y, 2.0)) * (pow(p.x, 2.0)) + 4 * A * d.x * d.y * p.z -
+                   2 * A * d.x * d.z * p.y - 2 * A * d.y * d.z * p.x + pow(d.z, 2.0);
+            if (root < 0) return NO_INTERSECTION;
+            root = sqrt(root);
+            denom = 2 * A * (d.x * d.y);
+            a1 = a2 = -A * d.x * p.y - A * d.y * p.x + d.z;
+            a1 += root;
+            a2 -= root;
+            a1 /= denom;
+            a2 /= denom;
+        }
+        pt1 = addvv_(p1, multvs_(d, a1));
+        pt2 = addvv_(p1, multvs_(d, a2));
+        if (a1 < 0.0) a1 = rp_inf();
+        if (a2 < 0.0) a2 = rp_inf();
+        if (is_base_ray) {
+            if (!shape_inside(s, f->shape, pt1.x, pt1.y)) a1 = rp_inf();
+            if (!shape_inside(s, f->shape, pt2.x, pt2.y)) a2 = rp_inf();
+        }
+        if (a2 < a1) a1 = a2;
+        if (a1 > 1.0 || a1 < f->tolerance) return NO_INTERSECTION;
+        out.dist = a1 * sep_(p1, p2);
+        return out;
+    }
+    case RP_FACE_CYLINDRICAL: { /* cfaces.pyx:1524-1582; p: z_height, radius */
+        double R = f->p[1], R2 = R * R, a1, a2, cz, ox2, oz2, dx2, dz2, denom, root;
+        vec d, o, pt1, pt2;
+        o = p1;
+        o.z -= f->p[0];
+        d = subvv_(p2, p1);
+        ox2 = o.x * o.x;
+        oz2 = o.z * o.z;
+        dx2 = d.x * d.x;
+        dz2 = d.z * d.z;
+        root = R2 * dz2 - 2 * R * dx2 * o.z + 2 * R * d.x * d.z * o.x - dx2 * oz2 + 2 * d.x * d.z * o.x * o.z -
+               dz2 * ox2;
+        if (root < 0) return NO_INTERSECTION;
+        root = sqrt(root);
+        denom = dx2 + dz2;
+        a1 = a2 = -R * d.z - d.x * o.x - d.z * o.z;
+        a1 += root;
+        a2 -= root;
+        a1 /= denom;
+        a2 /= denom;
+        pt1 = addvv_(p1, multvs_(d, a1));
+        pt2 = addvv_(p1, multvs_(d, a2));
+        cz = f->p[0] - f->p[1];
+        if (R >= 0) {
+            if (pt1.z < cz) a1 = rp_inf();
+            if (pt2.z < cz) a2 = rp_inf();
+        } else {
+            if (pt1.z > cz) a1 = rp_inf();
+            if (pt2.z > cz) a2 = rp_inf();
+        }
+        if (is_base_ray) {
+            if (!shape_inside(s, f->shape, pt1.x, pt1.y)) a1 = rp_inf();
+            if (!shape_inside(s, f->shape, pt2.x, pt2.y)) a2 = rp_inf();
+        }
+        if (a2 < a1) a1 = a2;
+        if (a1 > 1.0 || a1 < f->tolerance) return NO_INTERSECTION;
+        out.dist = a1 * sep_(p1, p2);
+        return out;
+    }
+    case RP_FACE_AXICON: { /* cfaces.pyx:1617-1664; p: z_height, gradient */
+        double a1, a2, root, ox2, oy2, oz2, dx2, dy2, dz2, beta2, denom, beta = f->p[1];
+        vec o, d, pt1, pt2;
+        d = subvv_(p2, p1);
+        o = p1;
+        o.z -= f->p[0];
+        beta2 = beta * beta;
+        ox2 = o.x * o.x;
+        oy2 = o.y * o.y;
+        oz2 = o.z * o.z;
+        dx2 = d.x * d.x;
+        dy2 = d.y * d.y;
+        dz2 = d.z * d.z;
+        root = -beta2 * dx2 * oy2 + 2 * beta2 * d.x * d.y * o.x * o.y - beta2 * dy2 * ox2 + dx2 * oz2 -
+               2 * d.x * d.z * o.x * o.z + dy2 * oz2 - 2 * d.y * d.z * o.y * o.z + dz2 * ox2 + dz2 * oy2;
+        denom = (beta2 * dx2 + beta2 * dy2 - dz2);
+        if (root < 0) return NO_INTERSECTION;
+        root = beta * sqrt(root);
+        a1 = -beta2 * d.x * o.x - beta2 * d.y * o.y + d.z * o.z;
+        a2 = a1 + root;
+        a1 -= root;
+        a1 /= denom;
+        a2 /= denom;
+        pt1 = addvv_(p1, multvs_(d, a1));
+        pt2 = addvv_(p1, multvs_(d, a2));
+        if (pt1.z > f->p[0]) a1 = rp_inf();
+        if (pt2.z > f->p[0]) a2 = rp_inf();
+        if (is_base_ray) {
+            if (!shape_inside(s, f->shape, pt1.x, pt1.y)) a1 = rp_inf();
+            if (!shape_inside(s, f->shape, pt2.x, pt2.y)) a2 = rp_inf();
+        }
+        if (a2 < a1) a1 = a2;
+        if (a1 > 1.0 || a1 < f->tolerance) return NO_INTERSECTION;
+        out.dist = a1 * sep_(p1, p2);
+        return out;
+    }
     case RP_FACE_DISTORTION: { /* cfaces.pyx:2341-2407 */
         const rp_face *face = &s->faces[f->base];
         const rp_distortion *dist = &s->distortions[f->distortion];
@@ -719,6 +903,51 @@ static vec face_normal(const rp_scene_desc *s, const rp_face *f, vec p, int piec
     }
     case RP_FACE_ORIENTED_POLYGON: /* cfaces.pyx:1183-1184 */
         return ld_v(&f->p[3]);
+    case RP_FACE_OFF_AXIS_PARABOLIC: { /* cfaces.pyx:1299-1315 */
+        double A = 1 / (2 * f->p[0]), B, dz, m2;
+        vec n;
+        m2 = p.x * p.x + p.y * p.y;
+        B = 4 * m2 * A * A;
+        dz = -sqrt(B / (B + 1));
+        m2 = sqrt(m2);
+        n.x = -(dz * p.x) / m2;
+        n.y = -(dz * p.y) / m2;
+        n.z = -1 / sqrt(B + 1);
+        return n;
+    }
+    case RP_FACE_ELLIPSOIDAL: { /* cfaces.pyx:1386-1396 */
+        const rp_transform *trans = (const rp_transform *)(s->aux + f->aux);
+        vec n;
+        p = transform_c(trans, p);
+        n.x = p.x / -(pow(f->p[0], 2.0));
+        n.y = p.y / -(pow(f->p[1], 2.0));
+        n.z = p.z / -(pow(f->p[1], 2.0));
+        n = rotate_c(trans + 1, n);
+        return norm_(n);
+    }
+    case RP_FACE_SADDLE: { /* cfaces.pyx:1497-1508 */
+        double rt6 = sqrt(6) * f->p[1];
+        vec n;
+        n.z = 1.0;
+        n.x = -rt6 * p.y;
+        n.y = -rt6 * p.x;
+        return norm_(n);
+    }
+    case RP_FACE_CYLINDRICAL: /* cfaces.pyx:1584-1595 */
+        p.z -= (f->p[0] - f->p[1]);
+        if (f->p[1] < 0) {
+            p.z = -p.z;
+            p.x = -p.x;
+        }
+        p.y = 0;
+        return norm_(p);
+    case RP_FACE_AXICON: { /* cfaces.pyx:1666-1677 */
+        double beta = f->p[1], r = sqrt(p.x * p.x + p.y * p.y);
+        p.z = 1.0;
+        p.x = beta * p.x / r;
+        p.y = beta * p.y / r;
+        return p;
+    }
     case RP_FACE_DISTORTION: { /* cfaces.pyx:2409-2422 */
         const rp_face *base = &s->faces[f->base];
         vec dxdyz = z_offset_and_gradient_c(s, &s->distortions[f->distortion], p.x, p.y);

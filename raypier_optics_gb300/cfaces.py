@@ -12,10 +12,11 @@ import math
 
 import numpy as np
 
-from .ctracer import Face, Shape, norm, cross
+from .ctracer import Face, Shape, Transform, norm, cross
 
 FACE_NONE, CIRCULAR, RECTANGULAR, SHAPED_PLANAR, SPHERICAL, SHAPED_SPHERICAL, CONIC, ASPHERIC, EXTPOLY, \
-    DISTORTION, ORIENTED_POLYGON, POLYGON, ELLIPTICAL_PLANE = range(13)
+    DISTORTION, ORIENTED_POLYGON, POLYGON, ELLIPTICAL_PLANE, OFF_AXIS_PARABOLIC, ELLIPSOIDAL, SADDLE, CYLINDRICAL, \
+    AXICON = range(18)
 
 
 class ShapedFace(Face):
@@ -326,6 +327,133 @@ class OrientedPolygonFace(Face):
         rec['p'][:12] = list(self._origin) + list(self._normal) + list(self._x_axis) + list(self._y_axis)
         rec['aux'] = tables.add_aux(np.ascontiguousarray(self._xy_points).reshape(-1))
         rec['n_aux0'] = self._xy_points.shape[0]
+
+
+class OffAxisParabolicFace(Face):
+    """cfaces.pyx:1224-1315: the paraboloid z + EFL/2 = (x^2 + y^2) / (2 EFL)
+    cut by a circular aperture of `diameter` centred on x = EFL;
+    p = (EFL, diameter, height).  The keywords EFL / diameter / height are
+    accepted for convenience (the reference's owner sets the attributes)."""
+    type_code = OFF_AXIS_PARABOLIC
+
+    def __init__(self, owner=None, tolerance=0.0001, max_length=100, material=None, **kwds):
+        super().__init__(owner, tolerance, max_length, material, **kwds)
+        self.EFL = float(kwds.get("EFL", 0.0))
+        self.diameter = float(kwds.get("diameter", 0.0))
+        self.height = float(kwds.get("height", 0.0))
+
+    def _pack(self, rec, tables):
+        rec['p'][:3] = (self.EFL, self.diameter, self.height)
+
+
+class EllipsoidalFace(Face):
+    """cfaces.pyx:1318-1410: an ellipsoid of revolution about the x axis of
+    its own frame (semi-axes major, minor), reached from the face-list frame by
+    `transform` and back by `inverse_transform`, clipped to the open block
+    x1 < x < x2, y1 < y < y2, z1 < z < z2 of the face-list frame.
+    p = (major, minor, x1, x2, y1, y2, z1, z2); aux = trans (m, t), inv_trans (m, t)."""
+    type_code = ELLIPSOIDAL
+
+    def __init__(self, owner=None, tolerance=0.0001, max_length=100, material=None, **kwds):
+        super().__init__(owner, tolerance, max_length, material, **kwds)
+        self.major = float(kwds.get("major", 0.0))
+        self.minor = float(kwds.get("minor", 0.0))
+        for k in ("x1", "x2", "y1", "y2", "z1", "z2"):
+            setattr(self, k, float(kwds.get(k, 0.0)))
+        self.transform = Transform()
+        self.inverse_transform = Transform()
+
+    def update(self):
+        """ellipsoids.py owner protocol (cfaces.pyx:1398-1405): ellipse_trans,
+        axes and the X/Y/Z bounds are pulled when the owner provides them."""
+        super().update()
+        owner = self.owner
+        if owner is None or not hasattr(owner, "ellipse_trans"):
+            return
+        self.sync_transform(owner.ellipse_trans)
+        self.major, self.minor = owner.axes
+        self.x1, self.x2 = owner.X_bounds
+        self.y1, self.y2 = owner.Y_bounds
+        self.z1, self.z2 = owner.Z_bounds
+
+    def sync_transform(self, vtk_trans):
+        """cfaces.pyx:1398-1410: copies a 4x4 affine map (anything with
+        ``matrix.get_element(i, j)`` and ``linear_inverse``) into transform and
+        inverse_transform."""
+        def split(t):
+            m = t.matrix
+            return ([[m.get_element(i, j) for j in range(3)] for i in range(3)],
+                    [m.get_element(i, 3) for i in range(3)])
+        rot, dt = split(vtk_trans)
+        self.transform = Transform(rotation=rot, translation=dt)
+        rot, dt = split(vtk_trans.linear_inverse)
+        self.inverse_transform = Transform(rotation=rot, translation=dt)
+
+    def _pack(self, rec, tables):
+        rec['p'][:8] = (self.major, self.minor, self.x1, self.x2, self.y1, self.y2, self.z1, self.z2)
+        t, ti = self.transform, self.inverse_transform
+        rec['aux'] = tables.add_aux(np.concatenate([np.ravel(t.rotation), t.translation,
+                                                    np.ravel(ti.rotation), ti.translation]))
+        rec['n_aux0'] = 24
+
+
+class SaddleFace(ShapedFace):
+    """cfaces.pyx:1413-1511: z = z_height + sqrt(6) curvature x y;
+    p = (z_height, curvature)."""
+    type_code = SADDLE
+    params = []
+
+    def __init__(self, owner=None, tolerance=0.0001, max_length=100, material=None, **kwds):
+        super().__init__(owner, tolerance, max_length, material, **kwds)
+        self.z_height = float(kwds.get("z_height", 0.0))
+        self.curvature = float(kwds.get("curvature", 0.0))
+
+    def _pack(self, rec, tables):
+        rec['p'][:2] = (self.z_height, self.curvature)
+        self._pack_shape(rec, tables)
+
+    def eval_z_c(self, x, y):
+        return math.sqrt(6) * self.curvature * x * y
+
+
+class CylindericalFace(ShapedFace):
+    """cfaces.pyx:1516-1602: a cylinder of `radius` with its axis along y,
+    vertex at z_height; p = (z_height, radius)."""
+    type_code = CYLINDRICAL
+    params = []
+
+    def __init__(self, owner=None, tolerance=0.0001, max_length=100, material=None, **kwds):
+        super().__init__(owner, tolerance, max_length, material, **kwds)
+        self.z_height = float(kwds.get("z_height", 0.0))
+        self.radius = float(kwds.get("radius", 100.0))
+
+    def _pack(self, rec, tables):
+        rec['p'][:2] = (self.z_height, self.radius)
+        self._pack_shape(rec, tables)
+
+    def eval_z_c(self, x, y):
+        R = self.radius
+        if R >= 0:
+            return self.z_height + math.sqrt(R * R - x * x) - R
+        return self.z_height - math.sqrt(R * R - x * x) - R
+
+
+class AxiconFace(ShapedFace):
+    """cfaces.pyx:1605-1680: the cone z = z_height - gradient r;
+    p = (z_height, gradient)."""
+    type_code = AXICON
+
+    def __init__(self, owner=None, tolerance=0.0001, max_length=100, material=None, **kwds):
+        super().__init__(owner, tolerance, max_length, material, **kwds)
+        self.z_height = float(kwds.get("z_height", 0.0))
+        self.gradient = float(kwds.get("gradient", 0.0))
+
+    def _pack(self, rec, tables):
+        rec['p'][:2] = (self.z_height, self.gradient)
+        self._pack_shape(rec, tables)
+
+    def eval_z_c(self, x, y):
+        return self.z_height - (self.gradient * math.sqrt(x * x + y * y))
 
 
 def point_in_polygon(X, Y, point_list):

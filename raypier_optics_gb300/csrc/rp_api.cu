@@ -204,7 +204,8 @@ static int validate_scene(const rp_scene_desc *d) {
     }
     for (int f = 0; f < d->n_face_records; f++) {
         const rp_face &F = d->faces[f];
-        if (F.type < RP_FACE_NONE || F.type > RP_FACE_ELLIPTICAL_PLANE) return RP_ERR_UNSUPPORTED;
+        if (F.type < RP_FACE_NONE || F.type > RP_FACE_AXICON) return RP_ERR_UNSUPPORTED;
+        if (F.type == RP_FACE_ELLIPSOIDAL && !aux_ok(F.aux, 24)) return RP_ERR_INVALID;
         if (f < d->n_faces && (F.material < 0 || F.material >= d->n_materials)) return RP_ERR_INVALID;
         if (F.shape < -1 || F.shape >= d->n_shape_ops) return RP_ERR_INVALID;
         if (F.type == RP_FACE_EXTPOLY) {

@@ -252,8 +252,33 @@ inline bool face_local_box(const rp_scene_desc *d, const rp_face &f, double lo[3
                              std::pow(ry / std::fabs(rho), j);
             return set(b.x0, b.x1, b.y0, b.y1, z0 - bound + p[3], z1 + bound + p[3]);
         }
+        case RP_FACE_ELLIPSOIDAL:  // hits lie strictly inside the block (cfaces.pyx:1362-1376)
+            return set(p[2], p[3], p[4], p[5], p[6], p[7]);
+        case RP_FACE_SADDLE: {  // z = z_height + sqrt(6) c x y: extremes at the corners of the shape box
+            Box2 b = shape_box(d, f.shape);
+            if (!b.bounded) return false;
+            double A = std::sqrt(6.0) * p[1];
+            double z0 = INFINITY, z1 = -INFINITY;
+            for (double x : {b.x0, b.x1})
+                for (double y : {b.y0, b.y1}) {
+                    z0 = std::min(z0, A * x * y);
+                    z1 = std::max(z1, A * x * y);
+                }
+            return set(b.x0, b.x1, b.y0, b.y1, p[0] + z0, p[0] + z1);
+        }
+        case RP_FACE_CYLINDRICAL: {  // the kept half lies between the vertex and the axis
+            Box2 b = shape_box(d, f.shape);
+            if (!b.bounded) return false;
+            double cz = p[0] - p[1];
+            return set(b.x0, b.x1, b.y0, b.y1, std::min(p[0], cz), std::max(p[0], cz));
+        }
+        case RP_FACE_AXICON: {  // |z - z_height| = |gradient| r with z <= z_height
+            Box2 b = shape_box(d, f.shape);
+            if (!b.bounded) return false;
+            return set(b.x0, b.x1, b.y0, b.y1, p[0] - std::fabs(p[1]) * b.rmax, p[0]);
+        }
         default:
-            return false;  // DistortionFace and the base Face: always tested
+            return false;  // DistortionFace, OffAxisParabolicFace and the base Face: always tested
     }
 }
 

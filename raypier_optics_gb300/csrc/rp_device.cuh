@@ -576,6 +576,174 @@ static __device__ double face_isect_base(const DevScene &S, const rp_face &f, v3
             }
             return h;
         }
+        case RP_FACE_OFF_AXIS_PARABOLIC: {  // cfaces.pyx:1228-1297; p: EFL, diameter
+            // paraboloid z + efl/2 = A (x^2 + y^2), aperture centred on x = efl
+            const double efl = f.p[0], A = 1 / (2 * efl);
+            v3 s = subv(p2, p1);
+            v3 r = p1;
+            r.z += efl / 2.;
+            double a = A * (s.x * s.x + s.y * s.y);
+            double b = 2 * A * (r.x * s.x + r.y * s.y) - s.z;
+            double c = A * (r.x * r.x + r.y * r.y) - r.z;
+            double d = b * b - 4 * a * c;
+            if (d < 0) return RP_MISS;
+            if (a < 1e-10) {
+                // near-axial ray: the linear root; the aperture test here
+                // compares r^2 with diameter/2, as the reference does
+                double a1 = -c / b;
+                v3 pt1 = addv(r, mulvs(s, a1));
+                pt1.x -= efl;
+                if ((pt1.x * pt1.x + pt1.y * pt1.y) > (f.p[1] / 2)) return RP_MISS;
+                if (a1 > 1.0 || a1 < f.tolerance) return RP_MISS;
+                return a1 * sepv(p1, p2);
+            }
+            d = sqrt(d);
+            double a1 = (-b + d) / (2 * a);
+            v3 pt1 = addv(r, mulvs(s, a1));
+            double a2 = (-b - d) / (2 * a);
+            v3 pt2 = addv(r, mulvs(s, a2));
+            pt1.x -= efl;
+            pt2.x -= efl;
+            if (is_base_ray) {
+                double dd = f.p[1];
+                dd *= dd / 4.;
+                if ((pt1.x * pt1.x + pt1.y * pt1.y) > dd) a1 = inf_d();
+                if ((pt2.x * pt2.x + pt2.y * pt2.y) > dd) a2 = inf_d();
+            }
+            if (a2 < a1) a1 = a2;
+            if (a1 > 1.0 || a1 < f.tolerance) return RP_MISS;
+            return a1 * sepv(p1, p2);
+        }
+        case RP_FACE_ELLIPSOIDAL: {  // cfaces.pyx:1339-1384; p: major, minor, x1, x2, y1, y2, z1, z2
+            const double *T = S.aux + f.aux;  // trans (m, t): the face-list frame -> the ellipse frame
+            v3 Sv = subv(p2, p1);
+            v3 r = xform(T, T + 9, p1);
+            v3 s = subv(xform(T, T + 9, p2), r);
+            double B = f.p[1] * f.p[1], A = f.p[0] * f.p[0];
+            double a = A * (s.z * s.z + s.y * s.y) + B * s.x * s.x;
+            double b = 2 * (A * (r.z * s.z + r.y * s.y) + B * r.x * s.x);
+            double c = A * (r.z * r.z + r.y * r.y) + B * r.x * r.x - A * B;
+            double d = sqrt(b * b - 4 * a * c);  // NaN for a miss: every bound test below fails
+            double root1 = (-b + d) / (2 * a);
+            double root2 = (-b - d) / (2 * a);
+            v3 q2 = addv(p1, mulvs(Sv, root2));
+            v3 q1 = addv(p1, mulvs(Sv, root1));
+            if (is_base_ray) {
+                if (!(f.p[2] < q2.x && q2.x < f.p[3])) root2 = 2;
+                if (!(f.p[4] < q2.y && q2.y < f.p[5])) root2 = 2;
+                if (!(f.p[6] < q2.z && q2.z < f.p[7])) root2 = 2;
+                if (!(f.p[2] < q1.x && q1.x < f.p[3])) root1 = 2;
+                if (!(f.p[4] < q1.y && q1.y < f.p[5])) root1 = 2;
+                if (!(f.p[6] < q1.z && q1.z < f.p[7])) root1 = 2;
+            }
+            if (root1 < f.tolerance) root1 = 2;
+            if (root2 < f.tolerance) root2 = 2;
+            if (root1 > root2) root1 = root2;
+            if (root1 > 1) return RP_MISS;
+            return root1 * magv(Sv);  // NaN (never a hit) when the ray misses a non-base test
+        }
+        case RP_FACE_SADDLE: {  // cfaces.pyx:1421-1495; p: z_height, curvature; z = sqrt(6) c x y
+            double A = sqrt(6.0) * f.p[1];
+            v3 p = p1;
+            p.z -= f.p[0];
+            v3 d = subv(p2, p1);
+            double a1, a2;
+            if (d.x == 0.0) {
+                a1 = (-A * (p.x * p.y) + p.z) / (A * d.y * p.x - d.z);
+                a2 = inf_d();
+            } else if (d.y == 0.0) {
+                a1 = (-A * (p.x * p.y) + p.z) / (A * d.x * p.y - d.z);
+                a2 = inf_d();
+            } else {
+                double A2 = A * A;
+                double root = A2 * (d.x * d.x) * (p.y * p.y) - 2 * A2 * d.x * d.y * p.x * p.y +
+                              A2 * (d.y * d.y) * (p.x * p.x) + 4 * A * d.x * d.y * p.z - 2 * A * d.x * d.z * p.y -
+                              2 * A * d.y * d.z * p.x + d.z * d.z;
+                if (root < 0) return RP_MISS;
+                root = sqrt(root);
+                double denom = 2 * A * (d.x * d.y);
+                a1 = a2 = -A * d.x * p.y - A * d.y * p.x + d.z;
+                a1 += root;
+                a2 -= root;
+                a1 /= denom;
+                a2 /= denom;
+            }
+            v3 pt1 = addv(p1, mulvs(d, a1));
+            v3 pt2 = addv(p1, mulvs(d, a2));
+            if (a1 < 0.0) a1 = inf_d();
+            if (a2 < 0.0) a2 = inf_d();
+            if (is_base_ray) {
+                if (!shape_inside(S, f.shape, pt1.x, pt1.y, err)) a1 = inf_d();
+                if (!shape_inside(S, f.shape, pt2.x, pt2.y, err)) a2 = inf_d();
+            }
+            if (a2 < a1) a1 = a2;
+            if (a1 > 1.0 || a1 < f.tolerance) return RP_MISS;
+            return a1 * sepv(p1, p2);
+        }
+        case RP_FACE_CYLINDRICAL: {  // cfaces.pyx:1524-1582; p: z_height, radius (axis along y)
+            const double R = f.p[1], R2 = R * R;
+            v3 o = p1;
+            o.z -= f.p[0];
+            v3 d = subv(p2, p1);
+            double ox2 = o.x * o.x, oz2 = o.z * o.z, dx2 = d.x * d.x, dz2 = d.z * d.z;
+            double root = R2 * dz2 - 2 * R * dx2 * o.z + 2 * R * d.x * d.z * o.x - dx2 * oz2 +
+                          2 * d.x * d.z * o.x * o.z - dz2 * ox2;
+            if (root < 0) return RP_MISS;
+            root = sqrt(root);
+            double denom = dx2 + dz2;
+            double a1, a2;
+            a1 = a2 = -R * d.z - d.x * o.x - d.z * o.z;
+            a1 += root;
+            a2 -= root;
+            a1 /= denom;
+            a2 /= denom;
+            v3 pt1 = addv(p1, mulvs(d, a1));
+            v3 pt2 = addv(p1, mulvs(d, a2));
+            double cz = f.p[0] - R;
+            if (R >= 0) {
+                if (pt1.z < cz) a1 = inf_d();
+                if (pt2.z < cz) a2 = inf_d();
+            } else {
+                if (pt1.z > cz) a1 = inf_d();
+                if (pt2.z > cz) a2 = inf_d();
+            }
+            if (is_base_ray) {
+                if (!shape_inside(S, f.shape, pt1.x, pt1.y, err)) a1 = inf_d();
+                if (!shape_inside(S, f.shape, pt2.x, pt2.y, err)) a2 = inf_d();
+            }
+            if (a2 < a1) a1 = a2;
+            if (a1 > 1.0 || a1 < f.tolerance) return RP_MISS;
+            return a1 * sepv(p1, p2);
+        }
+        case RP_FACE_AXICON: {  // cfaces.pyx:1617-1664; p: z_height, gradient; z = z_height - gradient r
+            const double beta = f.p[1], beta2 = beta * beta;
+            v3 d = subv(p2, p1);
+            v3 o = p1;
+            o.z -= f.p[0];
+            double ox2 = o.x * o.x, oy2 = o.y * o.y, oz2 = o.z * o.z;
+            double dx2 = d.x * d.x, dy2 = d.y * d.y, dz2 = d.z * d.z;
+            double root = -beta2 * dx2 * oy2 + 2 * beta2 * d.x * d.y * o.x * o.y - beta2 * dy2 * ox2 + dx2 * oz2 -
+                          2 * d.x * d.z * o.x * o.z + dy2 * oz2 - 2 * d.y * d.z * o.y * o.z + dz2 * ox2 + dz2 * oy2;
+            double denom = (beta2 * dx2 + beta2 * dy2 - dz2);
+            if (root < 0) return RP_MISS;
+            root = beta * sqrt(root);
+            double a1 = -beta2 * d.x * o.x - beta2 * d.y * o.y + d.z * o.z;
+            double a2 = a1 + root;
+            a1 -= root;
+            a1 /= denom;
+            a2 /= denom;
+            v3 pt1 = addv(p1, mulvs(d, a1));
+            v3 pt2 = addv(p1, mulvs(d, a2));
+            if (pt1.z > f.p[0]) a1 = inf_d();
+            if (pt2.z > f.p[0]) a2 = inf_d();
+            if (is_base_ray) {
+                if (!shape_inside(S, f.shape, pt1.x, pt1.y, err)) a1 = inf_d();
+                if (!shape_inside(S, f.shape, pt2.x, pt2.y, err)) a2 = inf_d();
+            }
+            if (a2 < a1) a1 = a2;
+            if (a1 > 1.0 || a1 < f.tolerance) return RP_MISS;
+            return a1 * sepv(p1, p2);
+        }
         default: return RP_MISS;
     }
 }
@@ -665,6 +833,39 @@ static __device__ v3 face_normal_base(const DevScene &S, const rp_face &f, v3 p)
             return normv(g);
         }
         case RP_FACE_ORIENTED_POLYGON: return mkv(f.p[3], f.p[4], f.p[5]);  // 1183-1184
+        case RP_FACE_OFF_AXIS_PARABOLIC: {  // 1299-1315 (unit length by construction)
+            double A = 1 / (2 * f.p[0]);
+            double m2 = p.x * p.x + p.y * p.y;
+            double B = 4 * m2 * A * A;
+            double dz = -sqrt(B / (B + 1));
+            m2 = sqrt(m2);
+            return mkv(-(dz * p.x) / m2, -(dz * p.y) / m2, -1 / sqrt(B + 1));
+        }
+        case RP_FACE_ELLIPSOIDAL: {  // 1386-1396: gradient in the ellipse frame, rotated back
+            const double *T = S.aux + f.aux;
+            p = xform(T, T + 9, p);
+            double ma2 = f.p[0] * f.p[0], mi2 = f.p[1] * f.p[1];
+            v3 n = mkv(p.x / -ma2, p.y / -mi2, p.z / -mi2);
+            return normv(rotv(T + 12, n));
+        }
+        case RP_FACE_SADDLE: {  // 1497-1508
+            double rt6 = sqrt(6.0) * f.p[1];
+            return normv(mkv(-rt6 * p.y, -rt6 * p.x, 1.0));
+        }
+        case RP_FACE_CYLINDRICAL: {  // 1584-1595
+            p.z -= (f.p[0] - f.p[1]);
+            if (f.p[1] < 0) {
+                p.z = -p.z;
+                p.x = -p.x;
+            }
+            p.y = 0;
+            return normv(p);
+        }
+        case RP_FACE_AXICON: {  // 1666-1677: not normalised, as in the reference
+            double beta = f.p[1];
+            double r = sqrt(p.x * p.x + p.y * p.y);
+            return mkv(beta * p.x / r, beta * p.y / r, 1.0);
+        }
         default: return p;  // Face.compute_normal_c, ctracer.pyx:1783-1784
     }
 }

@@ -86,10 +86,35 @@ def _make_distortion(spec, ns):
     return getattr(ns.cdistortions, spec["type"])(**spec.get("kw", {}))
 
 
+class AffineMatrix:
+    """A 4x4 affine map offering the two members EllipsoidalFace reads from
+    its owner's VTK transform (ellipsoids.py ellipse_trans):
+    ``matrix.get_element(i, j)`` and ``linear_inverse``.  The inverse is
+    given, not computed, so that every platform sees the same bits."""
+
+    def __init__(self, matrix, inverse):
+        self._m = np.asarray(matrix, dtype=np.float64).reshape(4, 4)
+        self._inv = np.asarray(inverse, dtype=np.float64).reshape(4, 4)
+
+    @property
+    def matrix(self):
+        return self
+
+    def get_element(self, i, j):
+        return float(self._m[i, j])
+
+    @property
+    def linear_inverse(self):
+        return AffineMatrix(self._inv, self._m)
+
+
 def _make_face(spec, ns, materials, curves):
     cls = getattr(ns.cfaces, spec["type"])
     kw = dict(spec.get("kw", {}))
-    owner = types.SimpleNamespace(**spec.get("owner", {}))
+    owner_kw = dict(spec.get("owner", {}))
+    if "ellipse_trans" in owner_kw:
+        owner_kw["ellipse_trans"] = AffineMatrix(**owner_kw["ellipse_trans"])
+    owner = types.SimpleNamespace(**owner_kw)
     if "shape" in spec:
         kw["shape"] = _make_shape(spec["shape"], ns)
     if "base_face" in spec:

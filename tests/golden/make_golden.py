@@ -6,6 +6,8 @@ Run in a container that has the reference sources and Cython:
     python oracle/build_ref.py && python tests/golden/make_golden.py
     python tests/golden/make_golden.py --lens     # only the configuration-4 lens case
     python tests/golden/make_golden.py --coated   # only the coated-material cases
+    python tests/golden/make_golden.py --faces2   # only the second face set
+    python tests/golden/make_golden.py --sequential  # only the trace_ray_sequence case
 
 Every fixture stores the scene description (the JSON spec understood by
 raypier_optics_gb300.workloads.build_scene), the inputs, and the reference's
@@ -126,6 +128,57 @@ def face_scene(face):
                           {"type": "CircularFace", "kw": {"z_plane": 0.0},
                            "owner": {"diameter": 400.0, "offset": 0.0}, "material": "detector"}]}]}
 
+
+def ellipse_trans(f1, f2):
+    """The owner's ellipse_trans of an ellipsoid with foci f1, f2 (ellipsoids.py
+    config_trans): the face-list frame -> a frame with the major axis along x
+    and the centre at the origin, with its exact inverse."""
+    f1, f2 = np.asarray(f1, dtype=float), np.asarray(f2, dtype=float)
+    c = (f1 + f2) / 2
+    ex = (f2 - f1) / np.linalg.norm(f2 - f1)
+    ey = np.cross([0.0, 0.0, 1.0], ex)
+    ey /= np.linalg.norm(ey)
+    ez = np.cross(ex, ey)
+    R = np.stack([ex, ey, ez])
+    M = np.eye(4)
+    M[:3, :3] = R
+    M[:3, 3] = -R @ c
+    Mi = np.eye(4)
+    Mi[:3, :3] = R.T
+    Mi[:3, 3] = c
+    return {"matrix": M.tolist(), "inverse": Mi.tolist()}
+
+
+def face_zoo2():
+    """The faces of the second set: off-axis paraboloid, ellipsoid, saddle,
+    cylinder and axicon (cfaces.pyx:1224-1680)."""
+    circ12 = {"type": "CircleShape", "kw": {"radius": 12.0}}
+    f1, f2, size = (-4.0, 1.0, 2.0), (5.0, -2.0, 28.0), 60.0
+    h = float(np.linalg.norm(np.subtract(f2, f1)))
+    axes = [size / 2.0, 0.5 * math.sqrt(size ** 2 - h ** 2)]
+    return {
+        "oap": {"type": "OffAxisParabolicFace", "attrs": {"EFL": 12.0, "diameter": 30.0}, "material": "mirror",
+                "rotate": False},
+        "ellipsoid": {"type": "EllipsoidalFace", "material": "mirror",
+                      "owner": {"ellipse_trans": ellipse_trans(f1, f2), "axes": axes, "X_bounds": [-20.0, 20.0],
+                                "Y_bounds": [-20.0, 20.0], "Z_bounds": [2.0, 40.0]}},
+        "saddle": {"type": "SaddleFace", "kw": {"z_height": 0.5, "curvature": 0.02}, "shape": circ12},
+        "saddle_rect": {"type": "SaddleFace", "kw": {"z_height": -1.0, "curvature": -0.01}, "shape": RECT},
+        "cylinder": {"type": "CylindericalFace", "kw": {"z_height": 0.0, "radius": 30.0}, "shape": circ12},
+        "cylinder_neg": {"type": "CylindericalFace", "kw": {"z_height": 1.0, "radius": -25.0, "invert_normal": 1},
+                         "shape": RECT},
+        "axicon": {"type": "AxiconFace", "kw": {"z_height": 1.0, "gradient": 0.3}, "shape": circ12},
+        "axicon_neg": {"type": "AxiconFace", "kw": {"z_height": -1.0, "gradient": -0.2}, "shape": PENTAGON},
+    }
+
+
+def face_scene2(face):
+    face = dict(face)
+    rotate = face.pop("rotate", True)
+    spec = face_scene(face)
+    if not rotate:
+        spec["lists"][0].pop("rotation")
+    return spec
 
 def material_zoo():
     crown1 = {"formula_id": 1, "coefs": [0.0, 1.03961212, 0.0774596669, 0.231792344, 0.141484679, 1.01046945,
@@ -407,6 +460,8 @@ def main():
                         specs=np.array(json.dumps({k: face_scene(v) for k, v in zoo.items()})))
     lens_case(ref, out_dir)
     coated_case(ref, out_dir)
+    faces2_case(ref, out_dir)
+    sequential_case(ref, out_dir)
     print("golden vectors written to", out_dir)
 
 
@@ -453,6 +508,77 @@ def coated_case(ref, out_dir):
     np.savez_compressed(os.path.join(out_dir, "units_coated.npz"), **units)
 
 
+def faces2_case(ref, out_dir):
+    """The second face set: trace cases face_<name>.npz, unit vectors in
+    units_faces2.npz and the scene specs in face_zoo2_specs.npz, with their
+    own random stream."""
+    rdt = ref.ctracer.ray_dtype
+    rng = np.random.Generator(np.random.PCG64(RNG_SEED + 77))
+    zoo = face_zoo2()
+    units = {}
+    specs = {}
+    for name, face in zoo.items():
+        spec = face_scene2(face)
+        specs[name] = spec
+        r1, wl = random_rays(rdt, rng, 40, -10.0, +1.0, 0.35, 13.0)
+        r2, _ = random_rays(rdt, rng, 24, 45.0, -1.0, 0.35, 13.0)
+        if name == "oap":  # axis-parallel rays take the reference's linear-root branch
+            r1['direction'][:6] = (0.0, 0.0, 1.0)
+            r1['E_vector'][:6] = (1.0, 0.0, 0.0)
+            r1['origin'][:6, 0] = rng.uniform(9.5, 14.5, 6)
+            r1['origin'][:6, 1] = rng.uniform(-2.5, 2.5, 6)
+        rays = np.concatenate([r1, r2])
+        rays['ray_ident'] = np.arange(len(rays), dtype=np.uint32)
+        params = {"recursion_limit": 4, "max_length": 200.0, "e2_terminate": 0.0}
+        gens, counts = run_reference(ref, spec, rays, wl, params["recursion_limit"], params["max_length"])
+        save_trace_case(os.path.join(out_dir, f"face_{name}.npz"), spec, rays, wl, params, gens, counts)
+        lists = W.build_scene(spec, ref)
+        f = lists[0].faces[0]
+        f.update()
+        p1 = np.stack([rng.uniform(-14, 14, 64), rng.uniform(-14, 14, 64), rng.uniform(-30, -2, 64)], axis=1)
+        p2 = np.stack([rng.uniform(-14, 14, 64), rng.uniform(-14, 14, 64), rng.uniform(2, 60, 64)], axis=1)
+        if name == "oap":
+            p1[:8, 0] = rng.uniform(9.5, 14.5, 8)
+            p1[:8, 1] = rng.uniform(-2.5, 2.5, 8)
+        p2[:8] = p1[:8] + np.array([0, 0, 80.0])
+        p2[8:12, 0] = p1[8:12, 0]   # d.x == 0 only
+        p2[12:16, 1] = p1[12:16, 1]  # d.y == 0 only
+        d_base = np.array([f.intersect(tuple(a), tuple(b), 1) for a, b in zip(p1, p2)])
+        d_free = np.array([f.intersect(tuple(a), tuple(b), 0) for a, b in zip(p1, p2)])
+        pts = np.stack([rng.uniform(-9, 9, 32), rng.uniform(-9, 9, 32), rng.uniform(-1, 1, 32)], axis=1)
+        nrm = np.array([f.compute_normal(tuple(p)) for p in pts])
+        units[f"face_{name}_p1"] = p1
+        units[f"face_{name}_p2"] = p2
+        units[f"face_{name}_dist_base"] = d_base
+        units[f"face_{name}_dist_free"] = d_free
+        units[f"face_{name}_pts"] = pts
+        units[f"face_{name}_normal"] = nrm
+    np.savez_compressed(os.path.join(out_dir, "units_faces2.npz"), **units)
+    np.savez_compressed(os.path.join(out_dir, "face_zoo2_specs.npz"), specs=np.array(json.dumps(specs)))
+
+
+def sequential_case(ref, out_dir):
+    """core/tracer.py trace_ray_sequence on the configuration-1 lens: each
+    face list appears twice in the sequence, so face.idx is each face's last
+    position in the chained face list, as the reference assigns it."""
+    rdt = ref.ctracer.ray_dtype
+    rng = np.random.Generator(np.random.PCG64(RNG_SEED + 91))
+    spec = W.config1_spec()
+    seq = [[0, 0], [0, 1], [1, 0], [1, 1], [2, 0]]
+    rays, wl = random_rays(rdt, rng, 64, -5.0, +1.0, 0.2, 6.0)
+    rays['ray_ident'] = np.arange(len(rays), dtype=np.uint32)
+    params = {"recursion_limit": 10, "max_length": 1000.0, "sequence": seq}
+    lists = W.build_scene(spec, ref)
+    rc = ref.ctracer.RayCollection.from_array(rays.copy())
+    rc.wavelengths = np.asarray(wl, dtype=np.double)
+    with contextlib.redirect_stdout(io.StringIO()):
+        traced, all_faces = ref.tracer.trace_ray_sequence(rc, [(lists[l], f) for l, f in seq],
+                                                          recursion_limit=params["recursion_limit"],
+                                                          max_length=params["max_length"])
+    gens = [t.copy_as_array() for t in traced]
+    counts = np.array([f.count for f in all_faces], dtype=np.uint32)
+    save_trace_case(os.path.join(out_dir, "seq_config1.npz"), spec, rays, wl, params, gens, counts)
+
 
 def lens_case(ref, out_dir):
     """Configuration 4: the perturbed eight-surface lens as an ordinary scene
@@ -472,5 +598,9 @@ if __name__ == "__main__":
         lens_case(build_ref.load(), HERE)
     elif sys.argv[1:] == ["--coated"]:
         coated_case(build_ref.load(), HERE)
+    elif sys.argv[1:] == ["--faces2"]:
+        faces2_case(build_ref.load(), HERE)
+    elif sys.argv[1:] == ["--sequential"]:
+        sequential_case(build_ref.load(), HERE)
     else:
         main()

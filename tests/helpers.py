@@ -28,15 +28,30 @@ X86 = platform.machine() in ("x86_64", "AMD64")
 
 def trace_case_names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith(("units", "face_zoo")))
+                  if not os.path.basename(p).startswith(("units", "face_zoo", "seq_")))
 
 
 def load_units():
     """The reference's single-call outputs: units.npz plus the coated-material
-    vectors of units_coated.npz, as one mapping."""
+    vectors of units_coated.npz and the second face set of units_faces2.npz,
+    as one mapping."""
     out = dict(np.load(os.path.join(GOLDEN, "units.npz")))
-    out.update(dict(np.load(os.path.join(GOLDEN, "units_coated.npz"))))
+    for extra in ("units_coated.npz", "units_faces2.npz"):
+        out.update(dict(np.load(os.path.join(GOLDEN, extra))))
     return out
+
+
+def load_face_specs():
+    """Scene spec of every face-zoo case, keyed by face name."""
+    specs = {}
+    for f in ("face_zoo_specs.npz", "face_zoo2_specs.npz"):
+        specs.update(json.loads(str(np.load(os.path.join(GOLDEN, f))["specs"])))
+    return specs
+
+
+def face_unit_names(units):
+    return sorted({k[len("face_"):-len("_dist_base")] for k in units
+                   if k.startswith("face_") and k.endswith("_dist_base")})
 
 
 def material_unit_names(units):

@@ -72,3 +72,26 @@ def test_boxes_are_tight_for_axis_aligned_faces():
     assert np.allclose(b[0, :3], [-25, -25, 0], atol=2e-3) and np.allclose(b[0, 3:6], [25, 25, 3.1755], atol=2e-3)
     # the asphere (z from 60 to 60 + 10.6)
     assert b[6, 6] == 1 and 60 - 0.1 < b[6, 2] < 60 and 70.5 < b[6, 5] < 70.8
+
+
+@pytest.mark.parametrize("name", ["ellipsoid", "saddle", "saddle_rect", "cylinder", "cylinder_neg", "axicon",
+                                  "axicon_neg"])
+def test_curved_face_boxes_hold_on_dense_samples(name):
+    """4096 seeded rays from both sides, through the face scenes of the golden
+    set: every hit the oracle reports lies in its face's box."""
+    from helpers import load_face_specs
+    spec = load_face_specs()[name]
+    rng = np.random.Generator(np.random.PCG64(5))
+    n = 4096
+    th = rng.uniform(0.0, 0.6, n)
+    ph = rng.uniform(0.0, 2 * np.pi, n)
+    up = rng.uniform(size=n) < 0.5
+    d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.where(up, 1.0, -1.0) * np.cos(th)], axis=1)
+    o = np.stack([rng.uniform(-16, 16, n), rng.uniform(-16, 16, n), np.where(up, -10.0, 45.0)], axis=1)
+    e = np.cross(np.array([0.0, 1.0, 0.0]), d)
+    e /= np.linalg.norm(e, axis=1)[:, None]
+    rays = W.fill_rays(np.zeros(n, dtype=ctracer.ray_dtype), o, d, e)
+    tables, _, _ = tables_for(spec)
+    assert boxes(tables)[0, 6] == 1
+    gens, _ = oracle.trace_rays(tables, np.array([0.55]), rays, 4, 200.0, 0.0)
+    assert check_hits_inside(tables, gens) > 100

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import build, tables_for
+from helpers import build, load_case, tables_for, trace_case_names
 from raypier_optics_gb300 import ctracer, precision, tracer
 from raypier_optics_gb300 import workloads as W
 from raypier_optics_gb300.ctracer import RayCollection
@@ -63,3 +63,21 @@ def test_mixed_path_config3_runs_and_mostly_agrees():
     st = precision.compare_traces(gens, ogens)
     print("config3", st)
     assert st["index_agreement"] > 0.99
+
+
+@pytest.mark.parametrize("name", [n for n in trace_case_names() if n.startswith(("face_", "mat_"))])
+def test_mixed_path_on_every_face_and_material_case(name):
+    """Each face and material type through the mixed kernel (its float-float
+    code where it has one, its FP64 code otherwise) against the reference's
+    golden trace of the same rays."""
+    c = load_case(name)
+    P = dict(c["params"])
+    P.setdefault("e2_terminate", 0.0)
+    gens = mixed_trace(c["spec"], c["rays"], c["wl"], P)
+    st = precision.compare_traces(gens, c["gens"])
+    sizes, osizes = [len(g) for g in gens], [len(g) for g in c["gens"]]
+    assert len(sizes) == len(osizes) and all(abs(a - b) <= 2 for a, b in zip(sizes, osizes)), (sizes, osizes)
+    assert st["index_agreement"] > 0.97, st
+    if st["position_nm"]["p99"] is not None:
+        assert st["position_nm"]["p99"] < POSITION_NM_P99, st
+        assert st["opl_nm"]["p99"] < OPL_NM_P99, st

@@ -14,7 +14,8 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import (GOLDEN, assert_generations, assert_records, build, load_case, tables_for, trace_case_names, load_units, material_unit_names)
+from helpers import (GOLDEN, assert_generations, assert_records, build, face_unit_names, load_case,
+                     load_face_specs, load_units, material_unit_names, tables_for, trace_case_names)
 from raypier_optics_gb300 import cmaterials, ctracer, scene, tracer, unitcalls
 from raypier_optics_gb300 import workloads as W
 from raypier_optics_gb300.ctracer import RayCollection
@@ -129,14 +130,13 @@ def test_gpu_trace_one_face_segment_matches_oracle():
 
 # ---- single-plugin calls against the reference's unit outputs ----------------------------
 UNITS = load_units()
-FACE_NAMES = sorted({k[len("face_"):-len("_dist_base")] for k in UNITS
-                     if k.startswith("face_") and k.endswith("_dist_base")})
+FACE_NAMES = face_unit_names(UNITS)
+FACE_SPECS = load_face_specs()
 
 
 @pytest.mark.parametrize("name", FACE_NAMES)
 def test_gpu_face_intersect_and_normal_match_reference(name):
-    specs = json.loads(str(np.load(os.path.join(GOLDEN, "face_zoo_specs.npz"))["specs"]))
-    lists, _ = build(specs[name])
+    lists, _ = build(FACE_SPECS[name])
     f = lists[0].faces[0]
     p1, p2 = UNITS[f"face_{name}_p1"], UNITS[f"face_{name}_p2"]
     np.testing.assert_allclose(unitcalls.face_intersect(f, p1, p2, 1), UNITS[f"face_{name}_dist_base"],

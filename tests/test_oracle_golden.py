@@ -12,8 +12,8 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import (GOLDEN, X86, assert_generations, assert_records, load_case, load_units,
-                     material_unit_names, tables_for, trace_case_names)
+from helpers import (GOLDEN, X86, assert_generations, assert_records, face_unit_names, load_case,
+                     load_face_specs, load_units, material_unit_names, tables_for, trace_case_names)
 from raypier_optics_gb300 import ctracer, workloads as W
 
 
@@ -88,3 +88,20 @@ def test_oracle_material_eval_matches_reference(name):
     np.testing.assert_array_equal([len(k) for k in kids], UNITS[f"mat_{name}_nkids"])
     got = np.concatenate(kids) if kids else np.zeros(0, dtype=ctracer.ray_dtype)
     assert_records(got, UNITS[f"mat_{name}_kids"], exact=X86, what=name)
+
+
+@pytest.mark.parametrize("name", face_unit_names(UNITS))
+def test_oracle_face_intersect_and_normal_match_reference(name):
+    """Face.intersect (base and non-base rays, axis-parallel segments among
+    them) and Face.compute_normal of every face type against the reference's
+    own calls; NaN where the reference returns NaN."""
+    tables, lists, _ = tables_for(load_face_specs()[name])
+    p1, p2 = UNITS[f"face_{name}_p1"], UNITS[f"face_{name}_p2"]
+    got = [oracle.face_intersect(tables, 0, p1, p2, 1), oracle.face_intersect(tables, 0, p1, p2, 0),
+           oracle.face_normal(tables, 0, UNITS[f"face_{name}_pts"])]
+    exp = [UNITS[f"face_{name}_dist_base"], UNITS[f"face_{name}_dist_free"], UNITS[f"face_{name}_normal"]]
+    for a, b in zip(got, exp):
+        if X86:
+            assert np.array_equal(a, b, equal_nan=True), (name, a, b)
+        else:
+            np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-15)
