@@ -55,6 +55,23 @@ typedef struct rp_ray {
 
 #define RP_RAY_BYTES 188
 #define RP_REFL_RAY  1u          /* ctracer.pyx:19 REFL_RAY */
+#define RP_GAUSSLET_RAY 2u       /* ctracer.pyx:21 GAUSSLET */
+
+/* Gausslet record: a base ray and six parabasal rays, byte-identical to
+ * ctracer.gausslet_dtype (ctracer.pxd:54-64 para_t / gausslet_t,
+ * ctracer.pyx:66-76): 80 + 668 bytes, packed. */
+#pragma pack(push, 1)
+typedef struct rp_para {
+    double origin[3], direction[3], normal[3];
+    double length;
+} rp_para;
+typedef struct rp_gausslet {
+    rp_ray base_ray;
+    rp_para para[6];
+} rp_gausslet;
+#pragma pack(pop)
+#define RP_PARA_BYTES 80
+#define RP_GAUSSLET_BYTES 668
 #define RP_NO_FACE   0xFFFFFFFFu /* end_face_idx of a ray that hit nothing */
 
 /* ---- scene tables ------------------------------------------------------- */
@@ -168,8 +185,10 @@ enum rp_material_type {
                                         n_inside, n_outside; p: n_coating (re, im), thickness (um) */
     RP_MAT_COATED_DISPERSIVE = 13,   /* CoatedDispersiveMaterial  cmaterials.pyx:1187-1381
                                         curve_inside, curve_outside; p: curve_coating, coating_thickness (um) */
-    RP_MAT_DIFFRACTION_GRATING = 14  /* DiffractionGratingMaterial cmaterials.pyx:1437-1543
+    RP_MAT_DIFFRACTION_GRATING = 14, /* DiffractionGratingMaterial cmaterials.pyx:1437-1543
                                         p: lines_per_mm, order, efficiency, origin[3] */
+    RP_MAT_RESAMPLE_GAUSSLET = 15    /* ResampleGaussletMaterial  cmaterials.pyx:1766-1830: emits no
+                                        child; a Gausslet generation reports the gausslets it captured */
 };
 typedef struct rp_material {
     int32_t type;
@@ -324,6 +343,55 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *scene, const void *in_records, uin
                        double e2_terminate, void *out_records, uint64_t out_cap,
                        uint64_t *gen_offsets, int32_t max_gens, int32_t *n_gens,
                        rp_stats *stats);
+
+/* ---- Gausslets ----------------------------------------------------------- */
+/* Device Gausslet buffers: the base rays as a ray buffer plus the six
+ * parabasal rays as structure-of-arrays. */
+typedef struct rp_gausslets rp_gausslets;
+int rp_gausslets_alloc(rp_ctx *ctx, uint64_t capacity, rp_gausslets **out);
+int rp_gausslets_free(rp_gausslets *g);
+int rp_gausslets_count(const rp_gausslets *g, uint64_t *n);
+/* Copy n packed 668-byte records in (GaussletCollection.from_array,
+ * ctracer.pyx:1303-1318) or out (GaussletCollection.copy_as_array, 1286-1292). */
+int rp_gausslets_upload(rp_gausslets *g, const void *records, uint64_t n);
+int rp_gausslets_download(const rp_gausslets *g, void *records, uint64_t n);
+
+/* One Gausslet generation: replaces trace_gausslet_c (ctracer.pyx:2214-2282)
+ * and, with list_idx / face_idx >= 0, trace_one_face_gausslet_c (2285-2350),
+ * both through trace_parabasal_rays (2353-2385).  The base ray finds its face
+ * as a ray does (its length is not reset first: the reference resets lengths
+ * at the end of each generation); the six parabasal rays are then tested
+ * against that face alone without its aperture; if every one meets it, each
+ * child of the base ray becomes a child gausslet whose parabasal rays the
+ * material bends (eval_parabasal_ray_c, cmaterials.pyx:683-724, 1393-1433,
+ * 1544-1600, ctracer.pyx:1588-1610).  `in` is mutated as in the reference
+ * (base length and end_face_idx, lengths of the parabasal rays tested); the
+ * children's base and parabasal lengths are set to max_length
+ * (reset_length_c, ctracer.pyx:1224-1230).  `max_length` is a double here, as
+ * in the reference's Gausslet path.  captured (optional, host array of n_in
+ * int32) receives for each input gausslet 1 + the material index of the
+ * RP_MAT_RESAMPLE_GAUSSLET material that captured it, else 0: the caller runs
+ * the decomposition (eval_decomposed_rays_c, cmaterials.pyx:1820-1830). */
+int rp_trace_gausslet_segment(rp_ctx *ctx, rp_scene *scene, rp_gausslets *in, rp_gausslets *out,
+                              int32_t list_idx, int32_t face_idx, double max_length,
+                              int32_t *captured, rp_stats *stats);
+
+/* ---- post-trace capture -------------------------------------------------- */
+/* Replaces select_ray_intersections (ctracer.pyx:1981-2015) for one traced
+ * collection: a copy of every ray of `in` (which is not modified) is
+ * intersected with the faces of face list `list_idx` of `scene`, from its
+ * origin to origin + direction * length (FaceList.intersect_c, 1882-1904);
+ * the copies that meet a face are written to `out` in input order, with the
+ * nearest face's distance as length, its index as end_face_idx and
+ * wavelength_idx + wl_offset (the collection's offset in the concatenated
+ * wavelength lists; the caller maps the concatenation onto its unique values,
+ * 2010-2015). */
+int rp_select_intersections(rp_ctx *ctx, rp_scene *scene, int32_t list_idx, rp_rays *in, rp_rays *out,
+                            uint32_t wl_offset);
+/* The same for gausslets, by their base rays (select_gausslet_intersections,
+ * ctracer.pyx:2018-2058); the parabasal rays are copied unchanged. */
+int rp_select_gausslet_intersections(rp_ctx *ctx, rp_scene *scene, int32_t list_idx, rp_gausslets *in,
+                                     rp_gausslets *out, uint32_t wl_offset);
 
 /* ---- differentiable sequential lens ------------------------------------- */
 /* No counterpart in the reference: raypier has no gradients.  A stack of even

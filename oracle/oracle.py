@@ -60,6 +60,10 @@ def load():
             lib.rp_oracle_convert_to_sp.argtypes = [P, P, P]
             lib.rp_oracle_eval_child_ray.argtypes = [P, P, ctypes.c_int64, I, P, ctypes.c_uint32, P, P, P, P]
             lib.rp_oracle_dispersion_n.argtypes = [P, I, P, ctypes.c_int64, P]
+            lib.rp_oracle_trace_gausslet_segment.argtypes = [P, P, ctypes.c_int64, P, U64, D, I, I, P, U64,
+                                                             ctypes.POINTER(U64), P, P]
+            lib.rp_oracle_select_intersections.argtypes = [P, I, P, U64, ctypes.c_uint32, P, ctypes.POINTER(U64)]
+            lib.rp_oracle_eval_parabasal.argtypes = [P, P, ctypes.c_int64, I, P, P, P, P, P, ctypes.c_uint32, P]
             _lib = lib
         return _lib
 
@@ -198,3 +202,119 @@ def dispersion_n(tables, curve, wavelengths):
     if lib.rp_oracle_dispersion_n(ctypes.byref(desc), curve, wl.ctypes.data, wl.shape[0], out.ctypes.data):
         raise ValueError("wavelength outside the dispersion curve's range")
     return out[0::2] + 1j * out[1::2]
+
+
+# ---- Gausslets ----------------------------------------------------------------------
+def trace_gausslet_segment(tables, wavelengths, records, max_length, one_list=-1, one_face=-1):
+    """One Gausslet generation (trace_gausslet_c / trace_one_face_gausslet_c)
+    before the decomposition step and the final length reset.  Returns
+    (mutated input, children, face counts, captured material + 1 per input)."""
+    from raypier_optics_gb300.ctracer import gausslet_dtype
+    lib = load()
+    gin = np.ascontiguousarray(records).copy()
+    assert gin.dtype == gausslet_dtype
+    n = gin.shape[0]
+    out = np.zeros(max(2 * n, 1), dtype=gausslet_dtype)
+    n_out = ctypes.c_uint64(0)
+    counts = np.zeros(tables.faces.shape[0], dtype=np.uint32)
+    captured = np.zeros(max(n, 1), dtype=np.int32)
+    desc = tables.desc()
+    wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+    rc = lib.rp_oracle_trace_gausslet_segment(ctypes.byref(desc), wl.ctypes.data, wl.shape[0], gin.ctypes.data, n,
+                                              float(max_length), one_list, one_face, out.ctypes.data, out.shape[0],
+                                              ctypes.byref(n_out), counts.ctypes.data, captured.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle trace_gausslet_segment failed with {rc}")
+    return gin, out[:n_out.value].copy(), counts, captured[:n]
+
+
+def trace_gausslets(tables, wavelengths, records, recursion_limit, max_length, decompose=None, sequence=None):
+    """trace_rays / trace_ray_sequence (core/tracer.py:9-99) for gausslets on
+    the host.  `decompose` maps a material index to a callable taking the
+    captured gausslet records and returning the records to append (the
+    ResampleGaussletMaterial eval_func, cmaterials.pyx:1820-1830); `sequence`
+    is a list of (list index, face index) steps.  Returns (generations, counts)."""
+    from raypier_optics_gb300.ctracer import gausslet_dtype
+    g = np.ascontiguousarray(records).copy()
+    g['base_ray']['length'] = max_length
+    g['para_rays']['length'] = max_length
+    counts = np.zeros(tables.faces.shape[0], dtype=np.uint32)
+
+    def generation(before, li, fi):
+        mutated, kids, c, captured = trace_gausslet_segment(tables, wavelengths, before, max_length, li, fi)
+        counts[:] += c
+        if decompose:
+            # decomposition faces in face order (core/tracer.py:37, ctracer.pyx:2274-2278);
+            # a material's captures go to its first face with hits, later faces
+            # sharing it see an empty set.  A captured gausslet is the record as
+            # the material saw it: base ray intersected, parabasal rays not yet.
+            done = set()
+            for rec in range(tables.n_faces):
+                m = int(tables.faces[rec]['material'])
+                if m in decompose and counts[rec]:
+                    sel = captured == m + 1 if m not in done else np.zeros(len(mutated), dtype=bool)
+                    done.add(m)
+                    counts[rec] = 0
+                    cap = mutated[sel].copy()
+                    cap['para_rays'] = before[sel]['para_rays']
+                    extra = decompose[m](cap)
+                    kids = np.concatenate([kids, np.asarray(extra, dtype=gausslet_dtype)])
+        kids['base_ray']['length'] = max_length
+        kids['para_rays']['length'] = max_length
+        return mutated, kids
+
+    gens = []
+    if sequence is None:   # core/tracer.py:40-45
+        rays, count = g, 0
+        while len(rays) > 0 and count < recursion_limit:
+            gens.append(rays)
+            gens[-1], rays = generation(rays, -1, -1)
+            count += 1
+    else:                  # core/tracer.py:88-97
+        gens.append(g)
+        for count, (li, fi) in enumerate(sequence):
+            gens[-1], kids = generation(gens[-1], li, fi)
+            if count > recursion_limit or len(kids) == 0:
+                break
+            gens.append(kids)
+    return gens, counts
+
+
+def eval_parabasal(tables, wavelengths, mat, base_ray, direction, point, normal, tangent, ray_type):
+    """InterfaceMaterial.eval_parabasal_ray of one material.  Returns a para_dtype record."""
+    from raypier_optics_gb300.ctracer import para_dtype
+    lib = load()
+    desc = tables.desc()
+    wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+    b = np.ascontiguousarray(base_ray).reshape(1)
+    out = np.zeros(1, dtype=para_dtype)
+    vs = [np.ascontiguousarray(v, dtype=np.double) for v in (direction, point, normal, tangent)]
+    rc = lib.rp_oracle_eval_parabasal(ctypes.byref(desc), wl.ctypes.data, wl.shape[0], mat, b.ctypes.data,
+                                      vs[0].ctypes.data, vs[1].ctypes.data, vs[2].ctypes.data, vs[3].ctypes.data,
+                                      int(ray_type), out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("oracle eval_parabasal failed")
+    return out[0]
+
+
+def select_ray_intersections(tables, list_idx, collections):
+    """select_ray_intersections (ctracer.pyx:1981-2015) on the host:
+    `collections` is a list of (ray records, wavelengths).  Returns (records,
+    merged wavelengths)."""
+    from raypier_optics_gb300.ctracer import ray_dtype
+    lib = load()
+    desc = tables.desc()
+    parts, wls, offset = [], [], 0
+    for recs, wl in collections:
+        r = _rays(recs)
+        out = np.zeros(max(len(r), 1), dtype=ray_dtype)
+        n = ctypes.c_uint64(0)
+        lib.rp_oracle_select_intersections(ctypes.byref(desc), list_idx, r.ctypes.data, len(r), offset,
+                                           out.ctypes.data, ctypes.byref(n))
+        parts.append(out[:n.value].copy())
+        wls.append(np.asarray(wl, dtype=np.double))
+        offset += len(wl)
+    recs = np.concatenate(parts)
+    reduced, inverse = np.unique(np.concatenate(wls), return_inverse=True)
+    recs['wavelength_idx'] = inverse.reshape(-1)[recs['wavelength_idx']]
+    return recs, reduced

@@ -1635,6 +1635,169 @@ static int trace_generation(const rp_scene_desc *s, const mat_ctx *mc, rp_ray *r
     return sink.overflow ? -2 : 0;
 }
 
+/* ---- Gausslets: ctracer.pyx:2214-2385 ------------------------------------ */
+/* InterfaceMaterial.eval_parabasal_ray_c and its overrides:
+ * ctracer.pyx:1588-1610 (base), cmaterials.pyx:683-724 (DielectricMaterial, and
+ * so FullDielectric and SingleLayerCoated), 1393-1433 (CoatedDispersive),
+ * 1544-1600 (DiffractionGrating). */
+static rp_para eval_parabasal_ray(const mat_ctx *mc, const rp_material *m, const rp_ray *base_ray, vec direction,
+                                  vec point, orient_t orient, uint32_t ray_type_id) {
+    rp_para para_out;
+    vec normal = norm_(orient.normal), out_dir;
+    switch (m->type) {
+    case RP_MAT_DIELECTRIC:
+    case RP_MAT_FULL_DIELECTRIC:
+    case RP_MAT_SINGLE_LAYER_COATED:
+    case RP_MAT_COATED_DISPERSIVE: {
+        double cosTheta, n1, n2, n_in, n_out;
+        int flip;
+        if (m->type == RP_MAT_COATED_DISPERSIVE) {
+            n_in = creal(mc->n_tab[(int64_t)m->curve_inside * mc->n_wl + base_ray->wavelength_idx]);
+            n_out = creal(mc->n_tab[(int64_t)m->curve_outside * mc->n_wl + base_ray->wavelength_idx]);
+        } else {
+            n_in = m->n_inside[0];
+            n_out = m->n_outside[0];
+        }
+        direction = norm_(direction);
+        cosTheta = dotprod_(normal, direction);
+        vec cosThetaNormal = multvs_(normal, cosTheta);
+        if (cosTheta < 0.0) { n1 = n_out; n2 = n_in; flip = 1; }
+        else { n1 = n_in; n2 = n_out; flip = -1; }
+        if (ray_type_id & RP_REFL_RAY) {
+            out_dir = subvv_(direction, multvs_(cosThetaNormal, 2));
+        } else {
+            vec tangent = subvv_(direction, cosThetaNormal);
+            vec tg2 = multvs_(tangent, n1 / n2);
+            double tan_mag_sq = mag_sq_(tg2);
+            double c2 = sqrt(1 - tan_mag_sq);
+            out_dir = subvv_(tg2, multvs_(normal, c2 * flip));
+        }
+        break;
+    }
+    case RP_MAT_DIFFRACTION_GRATING: {
+        vec tangent = norm_(orient.tangent), tangent2 = cross_(normal, tangent), reflected;
+        double wavelen = mc->wl[base_ray->wavelength_idx];
+        double line_spacing = 1000.0 / m->p[0];
+        double k_x, k_y, k_z;
+        int sign;
+        reflected = norm_(direction);
+        k_z = dotprod_(normal, reflected);
+        k_y = dotprod_(tangent2, reflected);
+        k_x = dotprod_(tangent, reflected);
+        sign = k_z < 0.0 ? 1 : -1;
+        k_x = k_x - (int)m->p[1] * wavelen / (line_spacing * base_ray->refractive_index[0]);
+        k_z = 1 - (k_x * k_x) - (k_y * k_y);
+        k_z = sign * sqrt(k_z);
+        reflected = multvs_(tangent, k_x);
+        reflected = addvv_(reflected, multvs_(tangent2, k_y));
+        reflected = addvv_(reflected, multvs_(normal, k_z));
+        out_dir = reflected;
+        break;
+    }
+    default:
+        if (ray_type_id & RP_REFL_RAY) {
+            double cosTheta = dotprod_(normal, direction);
+            vec cosThetaNormal = multvs_(normal, cosTheta);
+            out_dir = subvv_(direction, multvs_(cosThetaNormal, 2));
+        } else {
+            out_dir = direction;
+        }
+        break;
+    }
+    st_v(para_out.direction, out_dir);
+    st_v(para_out.origin, point);
+    st_v(para_out.normal, normal);
+    para_out.length = rp_inf();
+    return para_out;
+}
+
+typedef struct {
+    rp_gausslet *g;
+    uint64_t n, cap;
+    int overflow;
+} gausslet_sink;
+
+/* trace_parabasal_rays, ctracer.pyx:2353-2385 */
+static void trace_parabasal_rays(const rp_scene_desc *s, const mat_ctx *mc, rp_gausslet *g_in, const rp_ray *base_rays,
+                                 uint64_t n_base, const rp_face *face, const rp_facelist *fl, gausslet_sink *out,
+                                 double max_length) {
+    vec point[6];
+    orient_t orient[6];
+    for (int j = 0; j < 6; j++) {
+        rp_para *para_ray = &g_in->para[j];
+        vec ray_end = addvv_(ld_v(para_ray->origin), multvs_(ld_v(para_ray->direction), max_length));
+        /* FaceList.intersect_para_c, ctracer.pyx:1914-1926 */
+        vec p1 = transform_c(&fl->inv_trans, ld_v(para_ray->origin));
+        vec p2 = transform_c(&fl->inv_trans, ray_end);
+        isect_t it_para = face_intersect(s, face, p1, p2, 0);
+        if (face->tolerance < it_para.dist && it_para.dist < para_ray->length) {
+            para_ray->length = it_para.dist;
+            it_para.face_idx = face->idx;
+        }
+        if (it_para.face_idx < 0) return;
+        point[j] = addvv_(ld_v(para_ray->origin), multvs_(ld_v(para_ray->direction), para_ray->length));
+        orient[j] = compute_orientation(s, fl, face, point[j], &it_para);
+    }
+    const rp_material *m = &s->materials[face->material];
+    for (uint64_t i = 0; i < n_base; i++) {
+        rp_gausslet gausslet;
+        gausslet.base_ray = base_rays[i];
+        for (int j = 0; j < 6; j++)
+            gausslet.para[j] = eval_parabasal_ray(mc, m, &base_rays[i], ld_v(g_in->para[j].direction), point[j],
+                                                  orient[j], gausslet.base_ray.ray_type_id);
+        if (out->n >= out->cap) { out->overflow = 1; return; }
+        out->g[out->n++] = gausslet;
+    }
+}
+
+/* trace_gausslet_c (ctracer.pyx:2214-2282); one_list/one_face select
+ * trace_one_face_gausslet_c (2285-2350).  captured[i] = 1 + material index of
+ * a ResampleGaussletMaterial that captured gausslet i (its
+ * eval_child_ray_c, cmaterials.pyx:1806-1818); the decomposition itself and
+ * the final reset_length_c are left to the caller. */
+static int trace_gausslet_generation(const rp_scene_desc *s, const mat_ctx *mc, rp_gausslet *gausslets, uint64_t n,
+                                     double max_length, int one_list, int one_face, gausslet_sink *out,
+                                     uint32_t *face_counts, int32_t *captured) {
+    int nearest_set = -1;
+    isect_t nearest_it = {0, -1, 0};
+    for (uint64_t i = 0; i < n; i++) {
+        rp_gausslet *gausslet = gausslets + i;
+        rp_ray *ray = &gausslet->base_ray;
+        if (captured) captured[i] = 0;
+        ray->end_face_idx = (uint32_t)-1;
+        int nearest_idx = -1;
+        vec point = addvv_(ld_v(ray->origin), multvs_(ld_v(ray->direction), max_length));
+        if (one_list >= 0) {
+            isect_t it = facelist_intersect(s, &s->lists[one_list], ray, point, one_face);
+            if (it.face_idx >= 0) { nearest_set = one_list; nearest_it = it; nearest_idx = it.face_idx; }
+        } else {
+            for (int j = 0; j < s->n_lists; j++) {
+                isect_t it = facelist_intersect(s, &s->lists[j], ray, point, -1);
+                if (it.face_idx >= 0) { nearest_set = j; nearest_it = it; nearest_idx = it.face_idx; }
+            }
+        }
+        if (nearest_idx >= 0) {
+            int rec = find_face_record(s, nearest_idx);
+            if (rec < 0) return -1;
+            const rp_face *face = &s->faces[rec];
+            if (face_counts) face_counts[rec] += 1;
+            point = addvv_(ld_v(ray->origin), multvs_(ld_v(ray->direction), ray->length));
+            const rp_facelist *fl = &s->lists[nearest_set];
+            orient_t orient = compute_orientation(s, fl, face, point, &nearest_it);
+            rp_ray kids[2];
+            ray_sink child_rays = {kids, 0, 2, 0};
+            const rp_material *m = &s->materials[face->material];
+            if (m->type == RP_MAT_RESAMPLE_GAUSSLET) {
+                if ((ray->ray_type_id & RP_GAUSSLET_RAY) && captured) captured[i] = face->material + 1;
+            } else {
+                eval_child_ray(mc, m, ray, (uint32_t)i, point, orient, &child_rays);
+            }
+            trace_parabasal_rays(s, mc, gausslet, kids, child_rays.n, face, fl, out, max_length);
+        }
+    }
+    return out->overflow ? -2 : 0;
+}
+
 /* ---- exported oracle API ------------------------------------------------ */
 int rp_oracle_version(void) { return RP_ABI_VERSION; }
 
@@ -1736,3 +1899,55 @@ int rp_oracle_dispersion_n(const rp_scene_desc *s, int curve, const double *wl, 
 }
 
 int rp_oracle_owning_list(const rp_scene_desc *s, int rec) { return owning_list(s, rec); }
+
+/* One Gausslet generation; see trace_gausslet_generation.  The children's
+ * lengths are left as the materials wrote them (the caller appends any
+ * decomposition output and then resets lengths, ctracer.pyx:2274-2281). */
+int rp_oracle_trace_gausslet_segment(const rp_scene_desc *s, const double *wl, int64_t n_wl, rp_gausslet *g,
+                                     uint64_t n, double max_length, int one_list, int one_face, rp_gausslet *out,
+                                     uint64_t out_cap, uint64_t *n_out, uint32_t *face_counts, int32_t *captured) {
+    mat_ctx mc = {s, NULL, n_wl, wl};
+    cplx *tab = NULL;
+    int rc = build_n_tables(s, wl, n_wl, &tab);
+    if (rc) return rc;
+    mc.n_tab = tab;
+    gausslet_sink sink = {out, 0, out_cap, 0};
+    rc = trace_gausslet_generation(s, &mc, g, n, max_length, one_list, one_face, &sink, face_counts, captured);
+    *n_out = sink.n;
+    free(tab);
+    return rc;
+}
+
+/* InterfaceMaterial.eval_parabasal_ray (ctracer.pyx:1634-1644) of material `mat`. */
+int rp_oracle_eval_parabasal(const rp_scene_desc *s, const double *wl, int64_t n_wl, int mat, const rp_ray *base,
+                             const double *direction, const double *point, const double *normal,
+                             const double *tangent, uint32_t ray_type, rp_para *out) {
+    mat_ctx mc = {s, NULL, n_wl, wl};
+    cplx *tab = NULL;
+    if (build_n_tables(s, wl, n_wl, &tab)) return -1;
+    mc.n_tab = tab;
+    orient_t o = {ld_v(normal), ld_v(tangent)};
+    *out = eval_parabasal_ray(&mc, &s->materials[mat], base, ld_v(direction), ld_v(point), o, ray_type);
+    free(tab);
+    return 0;
+}
+
+/* select_ray_intersections' per-collection loop (ctracer.pyx:1996-2008): a
+ * copy of each ray is intersected with face list `list` from its origin to
+ * origin + direction * length; the copies that meet a face are appended with
+ * wavelength_idx + wl_offset. */
+int rp_oracle_select_intersections(const rp_scene_desc *s, int list, const rp_ray *rays, uint64_t n,
+                                   uint32_t wl_offset, rp_ray *out, uint64_t *n_out) {
+    uint64_t k = 0;
+    for (uint64_t i = 0; i < n; i++) {
+        rp_ray ray = rays[i];
+        vec point = addvv_(ld_v(ray.origin), multvs_(ld_v(ray.direction), ray.length));
+        isect_t it = facelist_intersect(s, &s->lists[list], &ray, point, -1);
+        if (it.face_idx >= 0) {
+            ray.wavelength_idx += wl_offset;
+            out[k++] = ray;
+        }
+    }
+    *n_out = k;
+    return 0;
+}

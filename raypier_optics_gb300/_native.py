@@ -33,6 +33,8 @@ SOURCES = [
     ("rp_unit.cu", ["--fmad=false"]),
     ("rp_lens.cu", ["--fmad=false"]),
     ("rp_serve.cu", ["--fmad=false"]),
+    ("rp_gausslet.cu", ["--fmad=false"]),
+    ("rp_capture.cu", ["--fmad=false"]),
 ]
 
 
@@ -188,6 +190,15 @@ _SIGS = {
     "rp_rays_count": (_I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "rp_rays_capacity": (_I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "rp_rays_upload_aos": (_I, [_P, _P, ctypes.c_uint64]),
+    "rp_gausslets_alloc": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(_P)]),
+    "rp_gausslets_free": (_I, [_P]),
+    "rp_gausslets_count": (_I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    "rp_gausslets_upload": (_I, [_P, _P, ctypes.c_uint64]),
+    "rp_gausslets_download": (_I, [_P, _P, ctypes.c_uint64]),
+    "rp_select_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
+    "rp_select_gausslet_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
+    "rp_trace_gausslet_segment": (_I, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _P,
+                                       ctypes.POINTER(Stats)]),
     "rp_rays_download_aos": (_I, [_P, _P, ctypes.c_uint64]),
     "rp_rays_field": (_I, [_P, ctypes.c_char_p, ctypes.POINTER(_P)]),
     "rp_trace_segment": (_I, [_P, _P, _P, _P, ctypes.c_float, ctypes.c_uint32, ctypes.c_double,

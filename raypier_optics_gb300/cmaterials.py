@@ -13,11 +13,12 @@ import math
 
 import numpy as np
 
-from .ctracer import InterfaceMaterial, Ray
+from .ctracer import GaussletCollection, InterfaceMaterial, Ray
 
 (MAT_NONE, MAT_OPAQUE, MAT_TRANSPARENT, MAT_PEC, MAT_PARTIAL, MAT_LINEAR_POLARISING, MAT_WAVEPLATE,
  MAT_DIELECTRIC, MAT_FULL_DIELECTRIC, MAT_FULL_DIELECTRIC_DISPERSIVE, MAT_CIRCULAR_APERTURE,
- MAT_RECT_APERTURE, MAT_SINGLE_LAYER_COATED, MAT_COATED_DISPERSIVE, MAT_DIFFRACTION_GRATING) = range(15)
+ MAT_RECT_APERTURE, MAT_SINGLE_LAYER_COATED, MAT_COATED_DISPERSIVE, MAT_DIFFRACTION_GRATING,
+ MAT_RESAMPLE_GAUSSLET) = range(16)
 
 
 def Convert_to_SP(ray, normal):
@@ -324,3 +325,45 @@ class RectangularApertureMaterial(InterfaceMaterial):
     def _pack(self, rec, tables):
         rec['p'][:9] = (self.outer_width, self.outer_height, self.width, self.height, self.edge_width,
                         float(self.invert)) + tuple(self.origin)
+
+
+class ResampleGaussletMaterial(InterfaceMaterial):
+    """cmaterials.pyx:1766-1830: a decomposition pseudo-material.  During a
+    Gausslet generation it captures every gausslet whose base ray carries the
+    GAUSSLET bit; after the generation ``eval_func`` maps the captured
+    GaussletCollection to new gausslets that are appended to the generation.
+    It emits no child rays."""
+    type_code = MAT_RESAMPLE_GAUSSLET
+
+    def __init__(self, **kwds):
+        super().__init__(**kwds)
+        self.capture_count = 0
+        self.captured_rays = GaussletCollection(kwds.get("size", 2))
+        self._evaluation_func = None
+        func = kwds.get("eval_func", None)
+        if func is not None:
+            self.eval_func = func
+
+    @property
+    def eval_func(self):
+        return self._evaluation_func
+
+    @eval_func.setter
+    def eval_func(self, obj):
+        if not callable(obj):
+            raise ValueError("The eval_func property must be a callable.")
+        self._evaluation_func = obj
+
+    def is_decomp_material(self):
+        return True
+
+    def _pack(self, rec, tables):
+        pass
+
+    def eval_decomposed_rays(self, new_rays):
+        """eval_decomposed_rays_c (cmaterials.pyx:1820-1830): appends
+        eval_func(captured gausslets) to `new_rays` and clears the capture."""
+        self.captured_rays.wavelengths = new_rays.wavelengths
+        gc = self._evaluation_func(self.captured_rays)
+        new_rays.extend(gc)
+        self.captured_rays.clear_ray_list()

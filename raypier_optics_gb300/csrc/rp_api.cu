@@ -222,7 +222,7 @@ static int validate_scene(const rp_scene_desc *d) {
     }
     for (int m = 0; m < d->n_materials; m++) {
         const rp_material &M = d->materials[m];
-        if (M.type < RP_MAT_NONE || M.type > RP_MAT_DIFFRACTION_GRATING) return RP_ERR_UNSUPPORTED;
+        if (M.type < RP_MAT_NONE || M.type > RP_MAT_RESAMPLE_GAUSSLET) return RP_ERR_UNSUPPORTED;
         if ((M.type == RP_MAT_FULL_DIELECTRIC_DISPERSIVE || M.type == RP_MAT_COATED_DISPERSIVE) &&
             (M.curve_inside < 0 || M.curve_inside >= d->n_dispersions || M.curve_outside < 0 ||
              M.curve_outside >= d->n_dispersions))
@@ -789,6 +789,300 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_
     for (auto *g : gens)
         if (g) rp_rays_free(g);
     return rc;
+}
+
+// ---- Gausslets ------------------------------------------------------------------
+struct rp_gausslets {
+    rp_ctx *ctx;
+    rp_rays *base;   // base rays; base->n is the gausslet count
+    double *para;    // RP_PARA_ARRAYS arrays of cap doubles
+    size_t para_bytes;
+    uint64_t cap;
+};
+
+int rp_gausslets_alloc(rp_ctx *ctx, uint64_t cap, rp_gausslets **out) {
+    if (!ctx || !out) return RP_ERR_INVALID;
+    *out = nullptr;
+    rp_gausslets *g = new (std::nothrow) rp_gausslets();
+    if (!g) return RP_ERR_NOMEM;
+    g->ctx = ctx;
+    g->cap = cap ? cap : 1;
+    int rc = rp_rays_alloc(ctx, g->cap, &g->base);
+    if (rc == RP_OK) rc = ctx_alloc(ctx, (void **)&g->para, (size_t)RP_PARA_ARRAYS * g->cap * sizeof(double),
+                                    &g->para_bytes);
+    if (rc) {
+        if (g->base) rp_rays_free(g->base);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return RP_OK;
+}
+
+int rp_gausslets_free(rp_gausslets *g) {
+    if (!g) return RP_ERR_INVALID;
+    rp_rays_free(g->base);  // synchronises the stream
+    ctx_free(g->ctx, g->para, g->para_bytes);
+    delete g;
+    return RP_OK;
+}
+
+int rp_gausslets_count(const rp_gausslets *g, uint64_t *n) {
+    if (!g || !n) return RP_ERR_INVALID;
+    *n = g->base->n;
+    return RP_OK;
+}
+
+int rp_gausslets_upload(rp_gausslets *g, const void *records, uint64_t n) {
+    if (!g || (n && !records)) return RP_ERR_INVALID;
+    if (n > g->cap) return RP_ERR_CAPACITY;
+    rp_ctx *ctx = g->ctx;
+    CK(cudaSetDevice(ctx->device));
+    if (n) {
+        void *stage = nullptr;
+        size_t bytes = (size_t)n * RP_GAUSSLET_BYTES, got = 0;
+        int rc = with_staging(ctx, bytes, &stage, &got);
+        if (rc) return rc;
+        cudaError_t e = cudaMemcpyAsync(stage, records, bytes, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = launch_gausslet_aos_to_soa(stage, g->base->soa, g->para, g->cap, n, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        ctx_free(ctx, stage, got);
+        if (e != cudaSuccess) return cuda_fail(e, "rp_gausslets_upload");
+    }
+    g->base->n = n;
+    return RP_OK;
+}
+
+int rp_gausslets_download(const rp_gausslets *g, void *records, uint64_t n) {
+    if (!g || (n && !records)) return RP_ERR_INVALID;
+    if (n > g->base->n) return RP_ERR_CAPACITY;
+    rp_ctx *ctx = g->ctx;
+    CK(cudaSetDevice(ctx->device));
+    if (!n) return RP_OK;
+    void *stage = nullptr;
+    size_t bytes = (size_t)n * RP_GAUSSLET_BYTES, got = 0;
+    int rc = with_staging(ctx, bytes, &stage, &got);
+    if (rc) return rc;
+    cudaError_t e = launch_gausslet_soa_to_aos(g->base->soa, g->para, g->cap, stage, n, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(records, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    ctx_free(ctx, stage, got);
+    if (e != cudaSuccess) return cuda_fail(e, "rp_gausslets_download");
+    return RP_OK;
+}
+
+int rp_trace_gausslet_segment(rp_ctx *ctx, rp_scene *s, rp_gausslets *in, rp_gausslets *out, int32_t list_idx,
+                              int32_t face_idx, double max_length, int32_t *captured, rp_stats *st) {
+    if (!ctx || !s || !in || !out || in == out || s->ctx != ctx || in->ctx != ctx || out->ctx != ctx)
+        return RP_ERR_INVALID;
+    if (list_idx >= 0) {
+        if (list_idx >= s->S.n_lists) return RP_ERR_INVALID;
+        if (face_idx < 0 || face_idx >= s->host_lists[list_idx].n_faces) return RP_ERR_INVALID;
+    }
+    CK(cudaSetDevice(ctx->device));
+    out->base->n = 0;
+    const uint64_t n_in = in->base->n;
+    if (captured)
+        for (uint64_t i = 0; i < n_in; i++) captured[i] = 0;
+    if (n_in == 0) return RP_OK;
+    const uint64_t n_tiles = (n_in + RP_BLOCK - 1) / RP_BLOCK;
+    int rc = ensure_scratch(ctx, n_tiles);
+    if (rc == RP_OK) rc = ensure_arena(ctx, n_tiles);
+    if (rc) return rc;
+    const uint64_t slots = n_tiles * RP_TILE_SLOTS;
+    double *pscratch = nullptr;
+    int *dcap = nullptr;
+    size_t pbytes = 0, cbytes = 0;
+    rc = ctx_alloc(ctx, (void **)&pscratch, (size_t)RP_PARA_ARRAYS * slots * sizeof(double), &pbytes);
+    if (rc) return rc;
+    if (captured) {
+        rc = ctx_alloc(ctx, (void **)&dcap, n_in * sizeof(int), &cbytes);
+        if (rc) {
+            ctx_free(ctx, pscratch, pbytes);
+            return rc;
+        }
+    }
+    auto release = [&]() {
+        cudaStreamSynchronize(ctx->stream);
+        ctx_free(ctx, pscratch, pbytes);
+        if (dcap) ctx_free(ctx, dcap, cbytes);
+    };
+    unsigned char *sc = ctx->scratch;
+    GaussArgs ga;
+    memset(&ga, 0, sizeof ga);
+    GenArgs &a = ga.g;
+    a.in = in->base->soa;
+    a.out = out->base->soa;
+    a.n_in = n_in;
+    a.out_cap = out->cap;
+    a.max_len = max_length;
+    a.emit = 1;
+    a.one_list = list_idx >= 0 ? list_idx : -1;
+    a.one_face = list_idx >= 0 ? face_idx : -1;
+    a.S = s->S;
+    a.smem_tables = s->smem_tables;
+    a.out_count = (unsigned long long *)(sc + 0);
+    a.err = (unsigned *)(sc + 8);
+    a.stats = (unsigned long long *)(sc + 24);
+    a.tile_next = (unsigned *)(sc + 40);
+    a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
+    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)));
+    a.scratch = ctx->arena->soa;
+    a.face_counts = s->face_counts;
+    ga.pin = in->para;
+    ga.pin_cap = in->cap;
+    ga.pscratch = pscratch;
+    ga.pscratch_cap = slots;
+    ga.pout = out->para;
+    ga.pout_cap = out->cap;
+    ga.captured = dcap;
+    cudaError_t e = cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream);
+    if (e == cudaSuccess && dcap) e = cudaMemsetAsync(dcap, 0, n_in * sizeof(int), ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev0, ctx->stream);
+    if (e == cudaSuccess) e = launch_gausslet_generation(ga, s->smem, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, ctx->stream);
+    if (e == cudaSuccess) e = launch_tile_scan(a, (unsigned)n_tiles, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        release();
+        return cuda_fail(e, "gausslet generation");
+    }
+    const unsigned long long count = ctx->h_pinned[0];
+    const unsigned err = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
+    if (st) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        st->rays_in += n_in;
+        st->hits += ctx->h_pinned[3];
+        st->kernel_ms += ms;
+        st->device_ms += ms;
+        st->launches += 3;  // generation, tile scan, placement
+        st->generations += 1;
+    }
+    if (err & ERR_WAVELENGTH) {
+        release();
+        snprintf(g_last_error, sizeof g_last_error, "a ray's wavelength_idx is outside the wavelength table");
+        return RP_ERR_INVALID;
+    }
+    if (err & (ERR_ZK_STACK | ERR_SHAPE_STACK)) {
+        release();
+        snprintf(g_last_error, sizeof g_last_error, "device evaluation limit hit (err=0x%x)", err);
+        return RP_ERR_INVALID;
+    }
+    if (count > out->cap) {
+        release();
+        snprintf(g_last_error, sizeof g_last_error, "%llu child gausslets do not fit the output buffer", count);
+        return RP_ERR_CAPACITY;
+    }
+    e = launch_gausslet_place(ga, (unsigned)n_tiles, ctx->stream);
+    if (e == cudaSuccess && dcap)
+        e = cudaMemcpyAsync(captured, dcap, n_in * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    release();
+    if (e != cudaSuccess) return cuda_fail(e, "gausslet placement");
+    out->base->n = count;
+    if (st) st->rays_out += count;
+    return RP_OK;
+}
+
+// ---- post-trace capture ---------------------------------------------------------
+// Shared by rp_select_intersections and rp_select_gausslet_intersections: the
+// capture kernel writes each hit ray (and its parabasal rays) to its tile's
+// slots, then the tile scan and the placement kernel compact them.
+static int capture_common(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_rays *in_base, const double *pin,
+                          uint64_t pin_cap, rp_rays *out_base, double *pout, uint64_t pout_cap, uint32_t wl_offset,
+                          uint64_t *n_out) {
+    if (list_idx < 0 || list_idx >= s->S.n_lists) return RP_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    *n_out = 0;
+    out_base->n = 0;
+    const uint64_t n_in = in_base->n;
+    if (n_in == 0) return RP_OK;
+    const uint64_t n_tiles = (n_in + RP_BLOCK - 1) / RP_BLOCK;
+    int rc = ensure_scratch(ctx, n_tiles);
+    if (rc == RP_OK) rc = ensure_arena(ctx, n_tiles);
+    if (rc) return rc;
+    const int with_para = pin != nullptr;
+    const uint64_t slots = n_tiles * RP_TILE_SLOTS;
+    double *pscratch = nullptr;
+    size_t pbytes = 0;
+    if (with_para) {
+        rc = ctx_alloc(ctx, (void **)&pscratch, (size_t)RP_PARA_ARRAYS * slots * sizeof(double), &pbytes);
+        if (rc) return rc;
+    }
+    unsigned char *sc = ctx->scratch;
+    GaussArgs ga;
+    memset(&ga, 0, sizeof ga);
+    GenArgs &a = ga.g;
+    a.in = in_base->soa;
+    a.out = out_base->soa;
+    a.n_in = n_in;
+    a.out_cap = out_base->cap;
+    a.one_list = list_idx;
+    a.one_face = -1;
+    a.S = s->S;
+    a.smem_tables = s->smem_tables;
+    a.out_count = (unsigned long long *)(sc + 0);
+    a.err = (unsigned *)(sc + 8);
+    a.stats = (unsigned long long *)(sc + 24);
+    a.tile_next = (unsigned *)(sc + 40);
+    a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
+    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)));
+    a.scratch = ctx->arena->soa;
+    a.face_counts = s->face_counts;
+    ga.pin = const_cast<double *>(pin);
+    ga.pin_cap = pin_cap;
+    ga.pscratch = pscratch;
+    ga.pscratch_cap = slots;
+    ga.pout = pout;
+    ga.pout_cap = pout_cap;
+    cudaError_t e = cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream);
+    if (e == cudaSuccess) e = launch_capture(ga, wl_offset, with_para, s->smem, ctx->stream);
+    if (e == cudaSuccess) e = launch_tile_scan(a, (unsigned)n_tiles, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->h_pinned, sc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        if (pscratch) ctx_free(ctx, pscratch, pbytes);
+        return cuda_fail(e, "capture kernel");
+    }
+    const unsigned long long count = ctx->h_pinned[0];
+    const unsigned err = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
+    if (err & (ERR_ZK_STACK | ERR_SHAPE_STACK)) {
+        if (pscratch) ctx_free(ctx, pscratch, pbytes);
+        snprintf(g_last_error, sizeof g_last_error, "device evaluation limit hit (err=0x%x)", err);
+        return RP_ERR_INVALID;
+    }
+    if (count > out_base->cap || (with_para && count > pout_cap)) {
+        if (pscratch) ctx_free(ctx, pscratch, pbytes);
+        snprintf(g_last_error, sizeof g_last_error, "%llu captured rays do not fit the output buffer", count);
+        return RP_ERR_CAPACITY;
+    }
+    e = with_para ? launch_gausslet_place(ga, (unsigned)n_tiles, ctx->stream)
+                  : launch_place_children(a, (unsigned)n_tiles, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (pscratch) ctx_free(ctx, pscratch, pbytes);
+    if (e != cudaSuccess) return cuda_fail(e, "capture placement");
+    out_base->n = count;
+    *n_out = count;
+    return RP_OK;
+}
+
+int rp_select_intersections(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_rays *in, rp_rays *out,
+                            uint32_t wl_offset) {
+    if (!ctx || !s || !in || !out || in == out || s->ctx != ctx) return RP_ERR_INVALID;
+    uint64_t n = 0;
+    return capture_common(ctx, s, list_idx, in, nullptr, 0, out, nullptr, 0, wl_offset, &n);
+}
+
+int rp_select_gausslet_intersections(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_gausslets *in,
+                                     rp_gausslets *out, uint32_t wl_offset) {
+    if (!ctx || !s || !in || !out || in == out || s->ctx != ctx) return RP_ERR_INVALID;
+    uint64_t n = 0;
+    return capture_common(ctx, s, list_idx, in->base, in->para, in->cap, out->base, out->para, out->cap, wl_offset,
+                          &n);
 }
 
 // ---- allocation-free single generation -------------------------------------

@@ -1404,4 +1404,100 @@ static __device__ int eval_children(const DevScene &S, const rp_material &m, con
     }
 }
 
+// ---- Gausslets ------------------------------------------------------------
+// FaceList.intersect_para_c's face test (ctracer.pyx:1914-1926): the face's
+// intersect_c with is_base_ray = 0, i.e. without its aperture or shape
+// (DistortionFace checks its shape either way, cfaces.pyx:2412).
+__device__ __forceinline__ double face_isect_para(const DevScene &S, const rp_face &f, v3 p1, v3 p2, unsigned *err) {
+    if (f.type == RP_FACE_DISTORTION) return distortion_isect(S, f, p1, p2, err);
+    return face_isect_base(S, f, p1, p2, 0, err);
+}
+
+// InterfaceMaterial.eval_parabasal_ray_c of every material type: the
+// direction and normal of a parabasal ray that met the face at a point with
+// orientation (onormal, otangent), for the child base ray `base` (its
+// refractive index, wavelength index and type).  Normalisations are the
+// reference's norm_ (three divisions).
+__device__ __forceinline__ void eval_parabasal(const DevScene &S, const rp_material &m, cx base_n, unsigned base_wl,
+                                               unsigned base_type, v3 direction, v3 onormal, v3 otangent,
+                                               v3 &dir_out, v3 &normal_out, unsigned *err) {
+    v3 normal = normv(onormal);
+    normal_out = normal;
+    switch (m.type) {
+        case RP_MAT_DIELECTRIC:
+        case RP_MAT_FULL_DIELECTRIC:
+        case RP_MAT_SINGLE_LAYER_COATED:
+        case RP_MAT_COATED_DISPERSIVE: {  // cmaterials.pyx:683-724 and 1393-1433
+            double n_in, n_out;
+            if (m.type == RP_MAT_COATED_DISPERSIVE) {
+                const long long w = (long long)base_wl;
+                if (w >= S.n_wl) {
+                    atomicOr(err, ERR_WAVELENGTH);
+                    dir_out = direction;
+                    return;
+                }
+                n_in = S.ntab[(long long)m.curve_inside * S.n_wl + w].x;
+                n_out = S.ntab[(long long)m.curve_outside * S.n_wl + w].x;
+            } else {
+                n_in = m.n_inside[0];
+                n_out = m.n_outside[0];
+            }
+            direction = normv(direction);
+            double cosTheta = dotv(normal, direction);
+            v3 cosThetaNormal = mulvs(normal, cosTheta);
+            double n1, n2;
+            int flip;
+            if (cosTheta < 0.0) {
+                n1 = n_out;
+                n2 = n_in;
+                flip = 1;
+            } else {
+                n1 = n_in;
+                n2 = n_out;
+                flip = -1;
+            }
+            if (base_type & RP_REFL_RAY) {
+                dir_out = subv(direction, mulvs(cosThetaNormal, 2));
+            } else {
+                v3 tg2 = mulvs(subv(direction, cosThetaNormal), n1 / n2);
+                double c2 = sqrt(1 - magsq(tg2));
+                dir_out = subv(tg2, mulvs(normal, c2 * flip));
+            }
+            return;
+        }
+        case RP_MAT_DIFFRACTION_GRATING: {  // cmaterials.pyx:1544-1600
+            const long long w = (long long)base_wl;
+            if (w >= S.n_wl) {
+                atomicOr(err, ERR_WAVELENGTH);
+                dir_out = direction;
+                return;
+            }
+            v3 tangent = normv(otangent);
+            v3 tangent2 = crossv(normal, tangent);
+            const double wavelen = S.wl[w];
+            const double line_spacing = 1000.0 / m.p[0];
+            v3 refl = normv(direction);
+            double k_z = dotv(normal, refl), k_y = dotv(tangent2, refl), k_x = dotv(tangent, refl);
+            const int sign = k_z < 0.0 ? 1 : -1;
+            k_x = k_x - m.p[1] * wavelen / (line_spacing * base_n.x);
+            k_z = 1 - (k_x * k_x) - (k_y * k_y);
+            k_z = sign * sqrt(k_z);  // NaN for an evanescent order, as in the reference
+            refl = mulvs(tangent, k_x);
+            refl = addv(refl, mulvs(tangent2, k_y));
+            dir_out = addv(refl, mulvs(normal, k_z));
+            return;
+        }
+        default: {  // InterfaceMaterial, ctracer.pyx:1588-1610
+            if (base_type & RP_REFL_RAY) {
+                double cosTheta = dotv(normal, direction);
+                v3 cosThetaNormal = mulvs(normal, cosTheta);
+                dir_out = subv(direction, mulvs(cosThetaNormal, 2));
+            } else {
+                dir_out = direction;
+            }
+            return;
+        }
+    }
+}
+
 }  // namespace rp

@@ -63,6 +63,29 @@ cudaError_t launch_dispersion_table(const rp_dispersion *curves, int n_curves, c
                                     const double *wl, long long n_wl, double2 *ntab, cudaStream_t st);
 size_t generation_smem_bytes(int n_lists, int n_recs, int n_mats, int n_faces);
 
+// ---- Gausslets (rp_gausslet.cu) ----
+// Parabasal ray j's field f (0-2 origin, 3-5 direction, 6-8 normal, 9 length)
+// of gausslet i lives at para[(j * RP_PARA_FIELDS + f) * cap + i].
+#define RP_PARA_FIELDS 10
+#define RP_PARA_ARRAYS (6 * RP_PARA_FIELDS)
+struct GaussArgs {
+    GenArgs g;                       // base rays: in, child slots, output, as for a ray generation
+    double *pin;                     // parabasal rays of the input (lengths of those tested are updated)
+    unsigned long long pin_cap;
+    double *pscratch;                // parabasal rays of the child slots
+    unsigned long long pscratch_cap;
+    double *pout;                    // parabasal rays of the output
+    unsigned long long pout_cap;
+    int *captured;                   // [n_in] 1 + material of a decomposition material that captured it (or null)
+};
+cudaError_t launch_gausslet_generation(const GaussArgs &a, size_t smem, cudaStream_t st);
+cudaError_t launch_gausslet_place(const GaussArgs &a, unsigned n_tiles, cudaStream_t st);
+cudaError_t launch_capture(const GaussArgs &a, unsigned wl_offset, int with_para, size_t smem, cudaStream_t st);
+cudaError_t launch_gausslet_aos_to_soa(const void *aos, RaySoA soa, double *para, unsigned long long cap,
+                                       unsigned long long n, cudaStream_t st);
+cudaError_t launch_gausslet_soa_to_aos(RaySoA soa, const double *para, unsigned long long cap, void *aos,
+                                       unsigned long long n, cudaStream_t st);
+
 // ---- differentiable sequential lens (rp_lens.cu) ----
 struct LensArgs {
     int n_surf;                 // aspheric surfaces; faces[n_surf] is the image plane

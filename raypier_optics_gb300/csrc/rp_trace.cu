@@ -15,113 +15,9 @@
 #include <map>
 #include <mutex>
 
-#include "rp_gen_common.cuh"
+#include "rp_nearest.cuh"
 
 namespace rp {
-
-// Entry distance of the ray (FP32, unit direction) into face f's world box;
-// 0 for faces that are always tested, +inf for a miss.
-__device__ __forceinline__ float box_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
-                                           float iz) {
-    if (b[6] == 0.0f) return 0.0f;
-    float t1 = (b[0] - ox) * ix, t2 = (b[3] - ox) * ix;
-    float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
-    t1 = (b[1] - oy) * iy;
-    t2 = (b[4] - oy) * iy;
-    tmin = fmaxf(tmin, fminf(t1, t2));
-    tmax = fminf(tmax, fmaxf(t1, t2));
-    t1 = (b[2] - oz) * iz;
-    t2 = (b[5] - oz) * iz;
-    tmin = fmaxf(tmin, fminf(t1, t2));
-    tmax = fminf(tmax, fmaxf(t1, t2));
-    if (!(tmax >= tmin) || tmax < 0.0f) return __int_as_float(0x7f800000);
-    return fmaxf(tmin, 0.0f);
-}
-
-__device__ __forceinline__ float inv_dir(float v) {
-    if (fabsf(v) < 1e-30f) v = copysignf(1e-30f, v);
-    return 1.0f / v;
-}
-
-// Nearest hit over all faces (trace_segment_c's loops over face lists and
-// faces, ctracer.pyx:2092-2105, with FaceList.intersect_c 1882-1904).  The
-// reference tests every face in list order and keeps a strictly nearer
-// distance, so the result is the smallest distance in (tolerance, max_length)
-// and, among equal distances, the earliest face.  Here faces are tested in
-// order of their box entry distance and a face whose box the ray cannot reach
-// before the current nearest hit is skipped; the exact FP64 test of every
-// face that is tested is the reference's, and ties go to the lower record,
-// so the outcome is the same.
-__device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pend, double max_len, double &len,
-                                            int &best, int &best_list, unsigned *err) {
-    float ox = (float)o.x, oy = (float)o.y, oz = (float)o.z;
-    float dx = (float)d.x, dy = (float)d.y, dz = (float)d.z;
-    float il = 1.0f / sqrtf(dx * dx + dy * dy + dz * dz);
-    float ix = inv_dir(dx * il), iy = inv_dir(dy * il), iz = inv_dir(dz * il);
-    // distances along the ray are Euclidean in the reference (h * |p2 - p1|)
-    const int nf = S.n_faces;
-    const int nmask = nf < 64 ? nf : 64;
-    const float lim0 = (float)max_len * 1.000001f + 1e-4f;
-    unsigned long long cand = 0;
-    for (int f = 0; f < nmask; f++)
-        if (box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) <= lim0) cand |= 1ull << f;
-    int cur_list = -1;
-    v3 p1 = o, p2 = pend;
-    while (cand) {
-        float tsel = __int_as_float(0x7f800000);
-        int sel = -1;
-        for (unsigned long long m = cand; m; m &= m - 1) {
-            int f = __ffsll((long long)m) - 1;
-            float t = box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-            if (t < tsel) {
-                tsel = t;
-                sel = f;
-            }
-        }
-        if (sel < 0 || tsel > (float)len * 1.000001f + 1e-4f) break;
-        cand &= ~(1ull << sel);
-        int l = S.face_list[sel];
-        if (l < 0 || l >= S.n_lists) {  // cannot happen for a validated scene
-            atomicOr(err, ERR_SHAPE_STACK);
-            break;
-        }
-        if (l != cur_list) {
-            const rp_facelist &L = S.lists[l];
-            p1 = xform(L.inv_trans.m, L.inv_trans.t, o);
-            p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
-            cur_list = l;
-        }
-        const rp_face &F = S.faces[sel];
-        double dist = face_isect(S, F, p1, p2, err);
-        if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && sel < best))) {
-            len = dist;
-            best = sel;
-            best_list = l;
-        }
-    }
-    // faces beyond the first 64 records: list order with the same skip test
-    for (int f = nmask; f < nf; f++) {
-        if (box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > (float)len * 1.000001f + 1e-4f) continue;
-        int l = S.face_list[f];
-        if (l < 0 || l >= S.n_lists) {
-            atomicOr(err, ERR_SHAPE_STACK);
-            break;
-        }
-        if (l != cur_list) {
-            const rp_facelist &L = S.lists[l];
-            p1 = xform(L.inv_trans.m, L.inv_trans.t, o);
-            p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
-            cur_list = l;
-        }
-        const rp_face &F = S.faces[f];
-        double dist = face_isect(S, F, p1, p2, err);
-        if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && f < best))) {
-            len = dist;
-            best = f;
-            best_list = l;
-        }
-    }
-}
 
 __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -305,18 +201,6 @@ cudaError_t launch_tile_scan(const GenArgs &a, unsigned n_tiles, cudaStream_t st
 // Moves each tile's children from the front of its slot range to their final
 // place: one block per tile, a straight coalesced copy of tile_counts[tile]
 // records to tile_offsets[tile].
-__device__ __forceinline__ void copy_ray(const RaySoA &s, unsigned long long src, const RaySoA &o,
-                                         unsigned long long dst) {
-    o.ox[dst] = s.ox[src]; o.oy[dst] = s.oy[src]; o.oz[dst] = s.oz[src];
-    o.dx[dst] = s.dx[src]; o.dy[dst] = s.dy[src]; o.dz[dst] = s.dz[src];
-    o.nx[dst] = s.nx[src]; o.ny[dst] = s.ny[src]; o.nz[dst] = s.nz[src];
-    o.ex[dst] = s.ex[src]; o.ey[dst] = s.ey[src]; o.ez[dst] = s.ez[src];
-    o.n[dst] = s.n[src]; o.e1[dst] = s.e1[src]; o.e2[dst] = s.e2[src];
-    o.len[dst] = s.len[src]; o.phase[dst] = s.phase[src]; o.opl[dst] = s.opl[src];
-    o.wl[dst] = s.wl[src]; o.parent[dst] = s.parent[src]; o.endf[dst] = s.endf[src];
-    o.ident[dst] = s.ident[src]; o.type[dst] = s.type[src];
-}
-
 __global__ void __launch_bounds__(RP_BLOCK) place_children_kernel(GenArgs A) {
     const unsigned tile = blockIdx.x;
     const unsigned count = A.tile_counts[tile];

@@ -46,6 +46,16 @@ ray_dtype = np.dtype([('origin', np.double, (3,)),
                       ('ray_type_id', np.uint32)])
 assert ray_dtype.itemsize == 188
 
+# ctracer.pyx:66-76
+NPARA = 6
+para_dtype = np.dtype([('origin', np.double, (3,)),
+                       ('direction', np.double, (3,)),
+                       ('normal', np.double, (3,)),
+                       ('length', np.double)])
+gausslet_dtype = np.dtype([('base_ray', ray_dtype),
+                           ('para_rays', para_dtype, (NPARA,))])
+assert gausslet_dtype.itemsize == 668
+
 REFL_RAY = 1 << 0
 GAUSSLET = 1 << 1
 PARABASAL = 1 << 2
@@ -450,6 +460,338 @@ class RayCollection:
         return h['origin'] + h['direction'] * h['length'][:, None]
 
 
+# ---- Gausslets (ctracer.pyx:315-394, 1157-1570) ------------------------------------
+class ParabasalRay:
+    """One parabasal ray (ctracer.pyx:332-394)."""
+
+    def __init__(self, **kwds):
+        self.ray = np.zeros((), dtype=para_dtype)
+        self.max_length = 1000.0
+        for k, v in kwds.items():
+            setattr(self, k, v)
+
+    def __repr__(self):
+        return "Parabasal Ray(o=%s, d=%s)" % (str(self.origin), str(self.direction))
+
+    def _vec(name):
+        def get(self):
+            return tuple(float(x) for x in self.ray[name])
+
+        def set_(self, v):
+            self.ray[name] = (v[0], v[1], v[2])
+        return property(get, set_)
+
+    origin = _vec('origin')
+    direction = _vec('direction')
+    normal = _vec('normal')
+
+    @property
+    def length(self):
+        return float(self.ray['length'])
+
+    @length.setter
+    def length(self, v):
+        self.ray['length'] = v
+
+    @property
+    def termination(self):
+        length = min(self.length, self.max_length)
+        length = float(np.float32(length))  # the reference holds it in a C float
+        o, d = self.origin, self.direction
+        return tuple(o[k] + d[k] * length for k in range(3))
+
+
+class Gausslet:
+    """A base ray with six parabasal rays (ctracer.pyx:700-752)."""
+
+    def __init__(self, **kwds):
+        self.gausslet = np.zeros((), dtype=gausslet_dtype)
+        for k, v in kwds.items():
+            setattr(self, k, v)
+
+    @property
+    def base_ray(self):
+        r = Ray()
+        r.ray[()] = self.gausslet['base_ray']
+        return r
+
+    @base_ray.setter
+    def base_ray(self, r):
+        self.gausslet['base_ray'] = r.ray
+
+    @property
+    def parabasal_rays(self):
+        out = []
+        for j in range(NPARA):
+            p = ParabasalRay()
+            p.ray[()] = self.gausslet['para_rays'][j]
+            out.append(p)
+        return tuple(out)
+
+    @parabasal_rays.setter
+    def parabasal_rays(self, rays):
+        for j, p in enumerate(rays):
+            self.gausslet['para_rays'][j] = p.ray
+
+
+class GaussletCollection:
+    """A growable collection of gausslets (ctracer.pyx:1185-1570), resident on
+    the host, the device, or both, like RayCollection."""
+
+    def __init__(self, max_size=0):
+        self._host = np.zeros(max(int(max_size), 0), dtype=gausslet_dtype)
+        self._n = 0
+        self._dev = None
+        self._host_ok = True
+        self._dev_ok = False
+        self._parent = None
+        self._wavelengths = np.zeros(0, dtype=np.double)
+
+    # -- residency --------------------------------------------------------------
+    @classmethod
+    def _from_device(cls, dev, parent=None):
+        gc = cls(0)
+        gc._dev = dev
+        gc._n = dev.count()
+        gc._host_ok = False
+        gc._dev_ok = True
+        if parent is not None:
+            gc.parent = parent
+        return gc
+
+    def _sync_host(self):
+        if not self._host_ok:
+            if self._host.shape[0] < self._n:
+                self._host = np.zeros(self._n, dtype=gausslet_dtype)
+            self._dev.download(self._host, self._n)
+            self._host_ok = True
+
+    def _device(self, ctx):
+        if self._dev_ok and self._dev is not None and self._dev.ctx is ctx:
+            return self._dev
+        self._sync_host()
+        dev = runtime.DeviceGausslets(ctx, max(self._n, 1))
+        dev.upload(self._host[:self._n])
+        self._dev = dev
+        self._dev_ok = True
+        return dev
+
+    def _mark_host_written(self):
+        self._host_ok = True
+        self._dev_ok = False
+
+    def _mark_device_written(self):
+        self._dev_ok = True
+        self._host_ok = False
+
+    # -- container API ------------------------------------------------------------
+    @property
+    def n_rays(self):
+        return self._n
+
+    @property
+    def max_size(self):
+        return max(self._host.shape[0], self._n)
+
+    def __len__(self):
+        return self._n
+
+    def __getitem__(self, idx):
+        if idx >= self._n:
+            raise IndexError("Requested index %d from a size %d array" % (idx, self._n))
+        self._sync_host()
+        g = Gausslet()
+        g.gausslet[()] = self._host[idx]
+        return g
+
+    def __setitem__(self, idx, g):
+        if idx >= self._n:
+            raise IndexError("Attempting to set index %d from a size %d array" % (idx, self._n))
+        self._sync_host()
+        self._host[idx] = g.gausslet
+        self._mark_host_written()
+
+    def __iter__(self):
+        for i in range(self._n):
+            yield self[i]
+
+    def get_gausslet_list(self):
+        return [self[i] for i in range(self._n)]
+
+    def add_gausslet(self, g):
+        self._sync_host()
+        if self._n == self._host.shape[0]:
+            cap = self._host.shape[0]
+            new = np.zeros(1 if cap == 0 else 2 * cap, dtype=gausslet_dtype)
+            new[:cap] = self._host
+            self._host = new
+        self._host[self._n] = g.gausslet
+        self._n += 1
+        self._mark_host_written()
+
+    def add_gausslet_list(self, rays):
+        for i, r in enumerate(rays):
+            if not isinstance(r, Gausslet):
+                raise TypeError("ray list contains non-Gausslet instance at index %d" % i)
+        for r in rays:
+            self.add_gausslet(r)
+
+    def clear_ray_list(self):
+        self._n = 0
+        self._mark_host_written()
+
+    def reset_length(self, max_length=INF):
+        """ctracer.pyx:1224-1235: base and parabasal lengths."""
+        self._sync_host()
+        self._host['base_ray']['length'][:self._n] = max_length
+        self._host['para_rays']['length'][:self._n] = max_length
+        self._mark_host_written()
+
+    def copy_as_array(self):
+        self._sync_host()
+        return self._host[:self._n].copy()
+
+    def extend(self, gc):
+        arr = gc.copy_as_array()
+        self._sync_host()
+        if self._n + arr.shape[0] > self._host.shape[0]:
+            new = np.zeros(self._n * 2 + arr.shape[0], dtype=gausslet_dtype)
+            new[:self._n] = self._host[:self._n]
+            self._host = new
+        self._host[self._n:self._n + arr.shape[0]] = arr
+        self._n += arr.shape[0]
+        self._mark_host_written()
+
+    @classmethod
+    def from_array(cls, data):
+        data = np.ascontiguousarray(data)
+        if data.dtype != gausslet_dtype:
+            raise ValueError("Array must have gausslet_dtype dtype")
+        gc = cls(data.shape[0])
+        gc._host[:] = data
+        gc._n = data.shape[0]
+        return gc
+
+    @classmethod
+    def from_rays(cls, data):
+        """ctracer.pyx:1320-1343: every parabasal ray starts as a copy of its base ray."""
+        data = np.ascontiguousarray(data)
+        if data.dtype != ray_dtype:
+            raise ValueError("Array must have gausslet_dtype dtype")
+        gc = cls(data.shape[0])
+        h = gc._host
+        h['base_ray'] = data
+        for f in ('origin', 'direction', 'normal'):
+            h['para_rays'][f] = data[f][:, None, :]
+        h['para_rays']['length'] = data['length'][:, None]
+        gc._n = data.shape[0]
+        return gc
+
+    @property
+    def base_rays(self):
+        """The base rays as a RayCollection copy (GaussletBaseRayView.copy_as_array)."""
+        return RayCollection.from_array(self.copy_as_array()['base_ray'])
+
+    @property
+    def wavelengths(self):
+        return np.asarray(self._wavelengths)
+
+    @wavelengths.setter
+    def wavelengths(self, wl_list):
+        self._wavelengths = np.ascontiguousarray(wl_list, dtype=np.double)
+
+    @property
+    def parent(self):
+        return self._parent
+
+    @parent.setter
+    def parent(self, gc):
+        self._parent = gc
+        self._wavelengths = gc._wavelengths
+
+    def _para(self, name):
+        self._sync_host()
+        return self._host['para_rays'][name][:self._n].copy()
+
+    para_origin = property(lambda self: self._para('origin'))
+    para_direction = property(lambda self: self._para('direction'))
+    para_normal = property(lambda self: self._para('normal'))
+    para_length = property(lambda self: self._para('length'))
+
+    @property
+    def total_power(self):
+        """ctracer.pyx:1482-1496."""
+        self._sync_host()
+        b = self._host['base_ray'][:self._n]
+        n = b['refractive_index'].real
+        pwr = 0.0
+        for i in range(self._n):
+            e1, e2 = complex(b['E1_amp'][i]), complex(b['E2_amp'][i])
+            pwr += (e1.real * e1.real) * n[i]
+            pwr += (e1.imag * e1.imag) * n[i]
+            pwr += (e2.real * e2.real) * n[i]
+            pwr += (e2.imag * e2.imag) * n[i]
+        return pwr
+
+    def scale_amplitude(self, scale):
+        self._sync_host()
+        self._host['base_ray']['E1_amp'][:self._n] *= scale
+        self._host['base_ray']['E2_amp'][:self._n] *= scale
+        self._mark_host_written()
+
+    def project_to_plane(self, origin, direction):
+        """ctracer.pyx:1397-1420: move every base and parabasal ray to the
+        plane through `origin` with normal `direction`."""
+        self._sync_host()
+        o = np.asarray(origin, dtype=np.double)
+        d = np.asarray(norm(tuple(float(x) for x in direction)))
+        b = self._host['base_ray'][:self._n]
+        a = ((o - b['origin']) @ d) / (b['direction'] @ d)
+        b['origin'] = b['origin'] + b['direction'] * a[:, None]
+        b['accumulated_path'] = b['accumulated_path'] + b['refractive_index'].real * a
+        self._host['base_ray'][:self._n] = b
+        p = self._host['para_rays'][:self._n]
+        a = ((o - p['origin']) @ d) / (p['direction'] @ d)
+        p['origin'] = p['origin'] + p['direction'] * a[..., None]
+        self._host['para_rays'][:self._n] = p
+        self._mark_host_written()
+
+    def config_parabasal_rays(self, wavelength_list, radius, working_dist):
+        """ctracer.pyx:1430-1476: parabasal rays of a circular Gaussian mode of
+        1/e^2 waist `radius` (mm) whose waist lies `working_dist` from the base
+        ray's origin."""
+        self._sync_host()
+        wl = np.asarray(wavelength_list, dtype=np.double)
+        for i in range(self._n):
+            g = self._host[i]
+            base = g['base_ray']
+            base_d = norm(tuple(float(x) for x in base['direction']))
+            o = (0.0, 1.0, 0.0) if base_d[0] > base_d[1] else (1.0, 0.0, 0.0)
+            d1 = norm(cross(base_d, o))
+            d2 = norm(cross(base_d, d1))
+            theta0 = wl[base['wavelength_idx']] / (math.pi * radius * 1000.0)
+            borigin = tuple(float(x) for x in base['origin'])
+            for j in range(0, 6, 2):
+                angle = (j * 2 * math.pi / 6)
+                oo = addvv(multvs(d1, radius * math.cos(angle)), multvs(d2, radius * math.sin(angle)))
+                oo = addvv(oo, borigin)
+                oo = addvv(oo, multvs(base_d, working_dist))
+                dd = addvv(multvs(d1, -theta0 * math.sin(angle)), multvs(d2, theta0 * math.cos(angle)))
+                da = addvv(base_d, dd)
+                db = subvv(base_d, dd)
+                para = g['para_rays']
+                para[j]['direction'] = norm(da)
+                para[j]['origin'] = subvv(oo, multvs(da, working_dist))
+                para[j + 1]['direction'] = norm(db)
+                para[j + 1]['origin'] = subvv(oo, multvs(db, working_dist))
+                para[j]['normal'] = base['normal']
+                para[j + 1]['normal'] = base['normal']
+                para[j]['length'] = base['length']
+                para[j + 1]['length'] = base['length']
+            self._host[i] = g
+        self._mark_host_written()
+
+
 # ---- plugin base classes ---------------------------------------------------------
 class InterfaceMaterial:
     """Base material (ctracer.pyx:1573-1655): generates no child rays."""
@@ -603,3 +945,71 @@ def trace_one_face_segment(rays, face_set, face_idx, all_faces, max_length=100, 
     face_set.sync_transforms()
     from .tracer import _trace_generation
     return _trace_generation(rays, [face_set], list(all_faces), max_length, one_face=(0, face_idx))
+
+
+def trace_gausslet(rays, face_sets, all_faces, max_length=100, decomp_faces=()):
+    """One Gausslet generation on the GPU (ctracer.pyx:2193-2202 -> 2214-2282)."""
+    for fs in face_sets:
+        fs.sync_transforms()
+    from .tracer import _trace_gausslet_generation
+    return _trace_gausslet_generation(rays, list(face_sets), list(all_faces), max_length,
+                                      decomp_faces=list(decomp_faces))
+
+
+def trace_one_face_gausslet(rays, face_set, face_idx, all_faces, max_length=100, decomp_faces=()):
+    """Sequential Gausslet variant (ctracer.pyx:2204-2211 -> 2285-2350)."""
+    face_set.sync_transforms()
+    from .tracer import _trace_gausslet_generation
+    return _trace_gausslet_generation(rays, [face_set], list(all_faces), max_length, one_face=(0, face_idx),
+                                      decomp_faces=list(decomp_faces))
+
+
+def _select(face_set, ray_col_list, gausslets):
+    from .scene import compile_scene
+    ctx = runtime.get_context()
+    if hasattr(face_set, "sync_transforms"):
+        face_set.sync_transforms()
+    tables = compile_scene([face_set])
+    scene = runtime.DeviceScene(ctx, tables, np.zeros(0))  # no material is evaluated here
+    wl_list, parts, offset = [], [], 0
+    dtype = gausslet_dtype if gausslets else ray_dtype
+    for rc in ray_col_list:
+        wl_list.append(np.asarray(rc.wavelengths, dtype=np.double))
+        dev = rc._device(ctx)
+        if gausslets:
+            out = runtime.DeviceGausslets(ctx, max(rc.n_rays, 1))
+            st = ctx.lib.rp_select_gausslet_intersections(ctx.handle, scene.handle, 0, dev.handle, out.handle, offset)
+        else:
+            out = runtime.DeviceRays(ctx, max(rc.n_rays, 1))
+            st = ctx.lib.rp_select_intersections(ctx.handle, scene.handle, 0, dev.handle, out.handle, offset)
+        from . import _native
+        _native.check(st, "rp_select_intersections")
+        n = out.count()
+        host = np.zeros(n, dtype=dtype)
+        out.download(host, n)
+        out.free()
+        parts.append(host)
+        offset += len(rc.wavelengths)
+    recs = np.concatenate(parts) if parts else np.zeros(0, dtype=dtype)
+    reduced, inverse = np.unique(np.concatenate(wl_list) if wl_list else np.zeros(0), return_inverse=True)
+    base = recs['base_ray'] if gausslets else recs
+    base['wavelength_idx'] = inverse.reshape(-1)[base['wavelength_idx']]
+    if gausslets:
+        recs['base_ray'] = base
+    out_col = (GaussletCollection if gausslets else RayCollection).from_array(recs)
+    out_col.wavelengths = reduced
+    return out_col
+
+
+def select_ray_intersections(face_set, ray_col_list):
+    """The rays of the traced collections that meet a face of `face_set`, with
+    their length cut to the nearest such face (ctracer.pyx:1981-2015).  The
+    intersections run on the GPU; the wavelength lists of the collections are
+    merged onto their unique values, as in the reference."""
+    return _select(face_set, list(ray_col_list), gausslets=False)
+
+
+def select_gausslet_intersections(face_set, ray_col_list):
+    """select_ray_intersections for GaussletCollections, by their base rays
+    (ctracer.pyx:2018-2058)."""
+    return _select(face_set, list(ray_col_list), gausslets=True)

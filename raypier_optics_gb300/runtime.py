@@ -54,6 +54,42 @@ def get_context(device: int = 0) -> Context:
         return ctx
 
 
+class DeviceGausslets:
+    """A device Gausslet buffer (rp_gausslets): base rays plus six parabasal rays."""
+
+    def __init__(self, ctx: Context, capacity: int):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = ctypes.c_void_p()
+        _native.check(self.lib.rp_gausslets_alloc(ctx.handle, int(capacity), ctypes.byref(h)), "rp_gausslets_alloc")
+        self.handle = h
+
+    def count(self) -> int:
+        v = ctypes.c_uint64()
+        _native.check(self.lib.rp_gausslets_count(self.handle, ctypes.byref(v)), "rp_gausslets_count")
+        return v.value
+
+    def upload(self, records: np.ndarray):
+        records = np.ascontiguousarray(records)
+        _native.check(self.lib.rp_gausslets_upload(self.handle, records.ctypes.data, records.shape[0]),
+                      "rp_gausslets_upload")
+
+    def download(self, out: np.ndarray, n: int):
+        assert out.flags.c_contiguous and out.shape[0] >= n
+        _native.check(self.lib.rp_gausslets_download(self.handle, out.ctypes.data, n), "rp_gausslets_download")
+
+    def free(self):
+        if getattr(self, "handle", None):
+            self.lib.rp_gausslets_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 class DeviceRays:
     """A device structure-of-arrays ray buffer (rp_rays)."""
 

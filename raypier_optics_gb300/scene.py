@@ -35,6 +35,7 @@ class SceneTables:
         self._faces = []           # rp_face records (numpy void scalars)
         self.face_objects = []     # record -> Face
         self._materials = []
+        self.material_objects = []  # material index -> InterfaceMaterial
         self._mat_index = {}
         self._shape_ops = []
         self._shape_index = {}
@@ -81,6 +82,7 @@ class SceneTables:
         if code:
             mat._pack(rec, self)
         self._materials.append(rec)
+        self.material_objects.append(mat)
         self._mat_index[key] = len(self._materials) - 1
         return self._mat_index[key]
 

@@ -67,9 +67,30 @@ def _make_curve(spec, ns):
                                               spec.get("wavelength_max", 1000000.0))
 
 
+def resample_shift(gc):
+    """A ResampleGaussletMaterial eval_func for tests and examples: relaunches
+    every captured gausslet 1 mm beyond the point where its base ray met the
+    face (base and parabasal rays each advanced by that distance along their
+    own direction), with the GAUSSLET bit cleared so that it is not captured
+    again.  Works on any GaussletCollection class offering copy_as_array /
+    from_array."""
+    arr = gc.copy_as_array()
+    step = arr['base_ray']['length'] + 1.0
+    b, p = arr['base_ray'], arr['para_rays']
+    arr['base_ray']['origin'] = b['origin'] + b['direction'] * step[:, None]
+    arr['para_rays']['origin'] = p['origin'] + p['direction'] * step[:, None, None]
+    arr['base_ray']['ray_type_id'] = b['ray_type_id'] & ~np.uint32(2)
+    return type(gc).from_array(arr)
+
+
+EVAL_FUNCS = {"resample_shift": resample_shift}
+
+
 def _make_material(spec, ns, curves):
     cls = getattr(ns.cmaterials, spec["type"])
     kw = dict(spec.get("kw", {}))
+    if isinstance(kw.get("eval_func"), str):
+        kw["eval_func"] = EVAL_FUNCS[kw["eval_func"]]
     for k in ("dispersion_inside", "dispersion_outside", "dispersion_coating"):
         if k in kw:
             kw[k] = curves[kw[k]]

@@ -8,6 +8,8 @@ Run in a container that has the reference sources and Cython:
     python tests/golden/make_golden.py --coated   # only the coated-material cases
     python tests/golden/make_golden.py --faces2   # only the second face set
     python tests/golden/make_golden.py --sequential  # only the trace_ray_sequence case
+    python tests/golden/make_golden.py --gausslets   # only the Gausslet cases
+    python tests/golden/make_golden.py --capture     # only the post-trace capture case
 
 Every fixture stores the scene description (the JSON spec understood by
 raypier_optics_gb300.workloads.build_scene), the inputs, and the reference's
@@ -462,6 +464,8 @@ def main():
     coated_case(ref, out_dir)
     faces2_case(ref, out_dir)
     sequential_case(ref, out_dir)
+    gausslet_cases(ref, out_dir)
+    capture_cases(ref, out_dir)
     print("golden vectors written to", out_dir)
 
 
@@ -580,6 +584,166 @@ def sequential_case(ref, out_dir):
     save_trace_case(os.path.join(out_dir, "seq_config1.npz"), spec, rays, wl, params, gens, counts)
 
 
+def gausslets_from_rays(ref, rays, wl, radius=0.05, working_dist=0.0, gausslet_bit=False):
+    """Gausslets of the reference built from rays: GaussletCollection.from_rays
+    then config_parabasal_rays (ctracer.pyx:1320-1343, 1430-1476)."""
+    r = rays.copy()
+    if gausslet_bit:
+        r['ray_type_id'] |= 2
+    gc = ref.ctracer.GaussletCollection.from_rays(r)
+    gc.config_parabasal_rays(np.asarray(wl, dtype=np.double), radius, working_dist)
+    return gc.copy_as_array()
+
+
+def run_reference_gausslets(ref, spec, gausslets, wl, recursion_limit, max_length, sequence=None):
+    lists = W.build_scene(spec, ref)
+    gc = ref.ctracer.GaussletCollection.from_array(gausslets.copy())
+    gc.wavelengths = np.asarray(wl, dtype=np.double)
+    with contextlib.redirect_stdout(io.StringIO()):
+        if sequence is None:
+            traced, all_faces = ref.tracer.trace_rays(gc, lists, recursion_limit=recursion_limit,
+                                                      max_length=max_length)
+        else:
+            traced, all_faces = ref.tracer.trace_ray_sequence(gc, [(lists[l], f) for l, f in sequence],
+                                                              recursion_limit=recursion_limit,
+                                                              max_length=max_length)
+    gens = [t.copy_as_array() for t in traced]
+    counts = np.array([f.count for f in all_faces], dtype=np.uint32)
+    return gens, counts
+
+
+def gausslet_cases(ref, out_dir):
+    """Gausslet tracing (trace_gausslet_c / trace_one_face_gausslet_c): trace
+    cases gauss_<name>.npz and eval_parabasal_ray unit vectors in
+    units_gausslet.npz, with their own random stream."""
+    gdt = ref.ctracer.gausslet_dtype
+    rdt = ref.ctracer.ray_dtype
+    rng = np.random.Generator(np.random.PCG64(RNG_SEED + 123))
+    cases = {}
+    # the configuration-1 lens, non-sequential and sequential
+    spec1 = W.config1_spec()
+    r, wl = random_rays(rdt, rng, 48, -5.0, +1.0, 0.15, 5.0)
+    cases["config1"] = (spec1, gausslets_from_rays(ref, r, wl, 0.05, 2.0), wl,
+                        {"recursion_limit": 6, "max_length": 1000.0})
+    cases["seq_config1"] = (spec1, gausslets_from_rays(ref, r, wl, 0.02, -1.0), wl,
+                            {"recursion_limit": 10, "max_length": 1000.0,
+                             "sequence": [[0, 0], [0, 1], [1, 0], [1, 1], [2, 0]]})
+    # each parabasal evaluation: base (PEC, dispersive, partial), dielectric, coatings, grating
+    zoo = material_zoo()
+    czoo = coated_zoo()
+    for name, z in (("pec", zoo), ("disp_sellmeier1", zoo), ("partial", zoo), ("full_split", zoo),
+                    ("dielectric", zoo), ("coated_single", czoo), ("coated_disp", czoo), ("grating", czoo),
+                    ("grating_m2", czoo)):
+        spec = material_scene(name, z)
+        r1, wla = random_rays(rdt, rng, 24, 0.0, +1.0, 0.6, 10.0, per_ray_wl=True, wl_range=(0.4, 1.0))
+        r2, wlb = random_rays(rdt, rng, 16, 40.0, -1.0, 0.6, 10.0, per_ray_wl=True, wl_range=(0.4, 1.0))
+        rays = np.concatenate([r1, r2])
+        rays['ray_ident'] = np.arange(len(rays), dtype=np.uint32)
+        rays['wavelength_idx'] = np.arange(len(rays), dtype=np.uint32)
+        wl = np.concatenate([wla, wlb])
+        cases["mat_" + name] = (spec, gausslets_from_rays(ref, rays, wl, 0.1, 0.5), wl,
+                                {"recursion_limit": 3, "max_length": 300.0})
+    # decomposition: a ResampleGaussletMaterial plane between two detectors
+    spec = material_scene("resample", {"curves": {}, "materials": {
+        "resample": {"type": "ResampleGaussletMaterial", "kw": {"eval_func": "resample_shift"}}}})
+    r, wl = random_rays(rdt, rng, 32, 0.0, +1.0, 0.5, 10.0)
+    g = gausslets_from_rays(ref, r, wl, 0.05, 0.0, gausslet_bit=True)
+    g['base_ray']['ray_type_id'][::4] &= ~np.uint32(2)  # some are not captured
+    cases["resample"] = (spec, g, wl, {"recursion_limit": 4, "max_length": 300.0})
+    for name, (spec, g, wl, params) in cases.items():
+        gens, counts = run_reference_gausslets(ref, spec, g, wl, params["recursion_limit"], params["max_length"],
+                                               params.get("sequence"))
+        offs = np.cumsum([0] + [len(x) for x in gens]).astype(np.uint64)
+        out = np.concatenate(gens) if gens else np.zeros(0, dtype=gdt)
+        np.savez_compressed(os.path.join(out_dir, f"gauss_{name}.npz"), spec=np.array(json.dumps(spec)),
+                            params=np.array(json.dumps(params)), gausslets=g, wl=np.asarray(wl, dtype=np.double),
+                            out=out, offsets=offs, counts=counts)
+    # eval_parabasal_ray unit calls of every material
+    units = {}
+    allm = dict(zoo["materials"])
+    allm.update(czoo["materials"])
+    curves = dict(zoo["curves"])
+    curves.update(czoo["curves"])
+    for name, mspec in allm.items():
+        spec = {"curves": curves, "materials": {name: mspec, "detector": {"type": "OpaqueMaterial"}},
+                "lists": [{"faces": [{"type": "CircularFace", "kw": {"z_plane": 0.0},
+                                      "owner": {"diameter": 40.0, "offset": 0.0}, "material": name}]}]}
+        lists = W.build_scene(spec, ref)
+        mat = lists[0].faces[0].material
+        n = 32
+        wl = rng.uniform(0.45, 0.9, n)
+        mat.wavelengths = wl
+        base, _ = random_rays(rdt, rng, n, 0.0, 1.0, 0.8, 5.0, per_ray_wl=True)
+        base['wavelength_idx'] = np.arange(n, dtype=np.uint32)
+        base['refractive_index'] = rng.uniform(1.0, 1.7, n) + 0j
+        dirs = rng.normal(0, 1, (n, 3))
+        dirs[:, 2] = np.abs(dirs[:, 2]) + 0.5
+        dirs[n // 2:, 2] *= -1
+        pts = rng.uniform(-5, 5, (n, 3))
+        nrm = rng.normal(0, 1, (n, 3))
+        nrm[:, 2] = np.abs(nrm[:, 2]) + 1.0
+        tng = rng.normal(0, 1, (n, 3))
+        refl = (np.arange(n) % 2).astype(bool)
+        rc = ref.ctracer.RayCollection.from_array(base.copy())
+        out = np.zeros(n, dtype=ref.ctracer.para_dtype)
+        for i in range(n):
+            p = mat.eval_parabasal_ray(rc[i], tuple(dirs[i]), tuple(pts[i]), tuple(nrm[i]), tuple(tng[i]),
+                                       bool(refl[i]))
+            out[i] = (p.origin, p.direction, p.normal, p.length)
+        units[f"para_{name}_spec"] = np.array(json.dumps(spec))
+        units[f"para_{name}_wl"] = wl
+        units[f"para_{name}_base"] = base
+        units[f"para_{name}_dirs"] = dirs
+        units[f"para_{name}_points"] = pts
+        units[f"para_{name}_normals"] = nrm
+        units[f"para_{name}_tangents"] = tng
+        units[f"para_{name}_refl"] = refl
+        units[f"para_{name}_out"] = out
+    np.savez_compressed(os.path.join(out_dir, "units_gausslet.npz"), **units)
+
+
+def capture_cases(ref, out_dir):
+    """select_ray_intersections / select_gausslet_intersections on traced
+    generations of the configuration-1 lens (three wavelengths listed out of
+    order, so the merge onto unique values is exercised)."""
+    rdt = ref.ctracer.ray_dtype
+    rng = np.random.Generator(np.random.PCG64(RNG_SEED + 211))
+    spec = W.config1_spec()
+    wl = np.array([0.65, 0.45, 0.55])
+    rays, _ = random_rays(rdt, rng, 64, -5.0, +1.0, 0.12, 6.0)
+    rays['wavelength_idx'] = rng.integers(0, 3, len(rays))
+    params = {"recursion_limit": 5, "max_length": 1000.0}
+    lists = W.build_scene(spec, ref)
+    rc = ref.ctracer.RayCollection.from_array(rays.copy())
+    rc.wavelengths = wl
+    with contextlib.redirect_stdout(io.StringIO()):
+        traced, _ = ref.tracer.trace_rays(rc, lists, recursion_limit=params["recursion_limit"],
+                                          max_length=params["max_length"])
+    out = {}
+    for li in (1, 2):
+        sel = ref.ctracer.select_ray_intersections(lists[li], traced)
+        out[f"rays_list{li}"] = sel.copy_as_array()
+        out[f"rays_list{li}_wl"] = np.asarray(sel.wavelengths)
+    gens = [t.copy_as_array() for t in traced]
+    offs = np.cumsum([0] + [len(g) for g in gens]).astype(np.uint64)
+    g = gausslets_from_rays(ref, rays, wl, 0.05, 1.0)
+    gc = ref.ctracer.GaussletCollection.from_array(g.copy())
+    gc.wavelengths = wl
+    lists = W.build_scene(spec, ref)
+    with contextlib.redirect_stdout(io.StringIO()):
+        gtraced, _ = ref.tracer.trace_rays(gc, lists, recursion_limit=params["recursion_limit"],
+                                           max_length=params["max_length"])
+    for li in (1, 2):
+        sel = ref.ctracer.select_gausslet_intersections(lists[li], gtraced)
+        out[f"gausslets_list{li}"] = sel.copy_as_array()
+        out[f"gausslets_list{li}_wl"] = np.asarray(sel.wavelengths)
+    ggens = [t.copy_as_array() for t in gtraced]
+    goffs = np.cumsum([0] + [len(x) for x in ggens]).astype(np.uint64)
+    np.savez_compressed(os.path.join(out_dir, "units_capture.npz"), spec=np.array(json.dumps(spec)),
+                        params=np.array(json.dumps(params)), wl=wl, rays=rays, gens=np.concatenate(gens),
+                        offsets=offs, gausslets=g, ggens=np.concatenate(ggens), goffsets=goffs, **out)
+
+
 def lens_case(ref, out_dir):
     """Configuration 4: the perturbed eight-surface lens as an ordinary scene
     (AsphericFace + DielectricMaterial, image plane), 64 rays of the 262,144-ray
@@ -602,5 +766,9 @@ if __name__ == "__main__":
         faces2_case(build_ref.load(), HERE)
     elif sys.argv[1:] == ["--sequential"]:
         sequential_case(build_ref.load(), HERE)
+    elif sys.argv[1:] == ["--gausslets"]:
+        gausslet_cases(build_ref.load(), HERE)
+    elif sys.argv[1:] == ["--capture"]:
+        capture_cases(build_ref.load(), HERE)
     else:
         main()

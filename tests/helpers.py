@@ -28,7 +28,7 @@ X86 = platform.machine() in ("x86_64", "AMD64")
 
 def trace_case_names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith(("units", "face_zoo", "seq_")))
+                  if not os.path.basename(p).startswith(("units", "face_zoo", "seq_", "gauss_")))
 
 
 def load_units():
@@ -104,3 +104,36 @@ def assert_generations(got_gens, exp_gens, exact=False, what=""):
         f"{what}: generation sizes {[len(g) for g in got_gens]} vs {[len(g) for g in exp_gens]}"
     for g, (a, b) in enumerate(zip(got_gens, exp_gens)):
         assert_records(a, b, exact=exact, what=f"{what} gen {g}")
+
+
+def gausslet_case_names():
+    return sorted(os.path.basename(p)[len("gauss_"):-4] for p in glob.glob(os.path.join(GOLDEN, "gauss_*.npz")))
+
+
+def load_gausslet_case(name):
+    z = np.load(os.path.join(GOLDEN, f"gauss_{name}.npz"))
+    offs = z["offsets"].astype(np.int64)
+    out = z["out"].astype(ctracer.gausslet_dtype)
+    return dict(spec=json.loads(str(z["spec"])), params=json.loads(str(z["params"])),
+                gausslets=z["gausslets"].astype(ctracer.gausslet_dtype), wl=z["wl"],
+                gens=[out[offs[g]:offs[g + 1]] for g in range(len(offs) - 1)], counts=z["counts"])
+
+
+def assert_gausslets(got, exp, exact=False, what=""):
+    assert len(got) == len(exp), f"{what}: {len(got)} gausslets vs {len(exp)}"
+    assert_records(np.ascontiguousarray(got["base_ray"]), np.ascontiguousarray(exp["base_ray"]), exact=exact,
+                   what=what + " base")
+    for f in ("origin", "direction", "normal", "length"):
+        a, b = got["para_rays"][f], exp["para_rays"][f]
+        if exact:
+            assert np.array_equal(np.ascontiguousarray(a).view(np.uint8), np.ascontiguousarray(b).view(np.uint8)), \
+                f"{what}: parabasal {f} differs"
+        else:
+            np.testing.assert_allclose(a, b, rtol=RTOL, atol=ATOL, equal_nan=True, err_msg=f"{what}: parabasal {f}")
+
+
+def assert_gausslet_generations(got_gens, exp_gens, exact=False, what=""):
+    assert [len(g) for g in got_gens] == [len(g) for g in exp_gens], \
+        f"{what}: generation sizes {[len(g) for g in got_gens]} vs {[len(g) for g in exp_gens]}"
+    for g, (a, b) in enumerate(zip(got_gens, exp_gens)):
+        assert_gausslets(a, b, exact=exact, what=f"{what} gen {g}")
