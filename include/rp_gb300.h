@@ -393,6 +393,35 @@ int rp_select_intersections(rp_ctx *ctx, rp_scene *scene, int32_t list_idx, rp_r
 int rp_select_gausslet_intersections(rp_ctx *ctx, rp_scene *scene, int32_t list_idx, rp_gausslets *in,
                                      rp_gausslets *out, uint32_t wl_offset);
 
+/* ---- E-field summation ---------------------------------------------------- */
+/* Gaussian-mode coefficients of each gausslet (evaluate_modes,
+ * cfields.pyx:150-234): x, y, dx, dy are n rows of `size` (1..64) parabasal
+ * offsets and slopes in the base ray's frame (core/fields.py:122-148
+ * evaluate_neighbours_gc); modes_out receives n x 3 complex (re, im)
+ * coefficients A, B, C.  RP_ERR_INVALID where the reference raises
+ * ZeroDivisionError (a degenerate fit). */
+int rp_field_evaluate_modes(rp_ctx *ctx, const double *x, const double *y, const double *dx, const double *dy,
+                            uint64_t n, int32_t size, double blending, double *modes_out);
+
+/* A set of Gaussian modes held on the device for repeated evaluation
+ * (core/fields.py:239-266 EFieldSummation): the modes' base rays (188-byte
+ * records), their n x 3 complex coefficients and the wavelength table. */
+typedef struct rp_field rp_field;
+int rp_field_create(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double *modes,
+                    const double *wavelengths, int64_t n_wavelengths, rp_field **out);
+int rp_field_destroy(rp_field *field);
+/* sum_gaussian_modes (cfields.pyx:49-117): the complex E-field at n_points
+ * points (x, y, z), E_out n_points x 3 complex (re, im), summed over the modes
+ * in order for every point, at time time_ps.  Host buffers. */
+int rp_field_evaluate(rp_field *field, const double *points, uint64_t n_points, double time_ps, double *E_out);
+/* The same with device buffers (points and E on the context's device). */
+int rp_field_evaluate_device(rp_field *field, const double *points_dev, uint64_t n_points, double time_ps,
+                             double *E_dev);
+/* One-shot sum_gaussian_modes: create, evaluate, destroy. */
+int rp_field_sum_gaussian_modes(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double *modes,
+                                const double *wavelengths, int64_t n_wavelengths, const double *points,
+                                uint64_t n_points, double time_ps, double *E_out);
+
 /* ---- differentiable sequential lens ------------------------------------- */
 /* No counterpart in the reference: raypier has no gradients.  A stack of even
  * aspheres traced in order (each surface an AsphericFace with a circular

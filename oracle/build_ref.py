@@ -2,20 +2,21 @@
 
 This is test infrastructure: it compiles the reference implementation of the
 non-sequential tracing hot path (``raypier/core/{ctracer,cmaterials,cfaces,cshapes,
-cdistortions}.pyx``) so that tests, golden-vector generation and the CPU
+cdistortions}.pyx``) and of the E-field summation that consumes its output
+(``cfields.pyx``) so that tests, golden-vector generation and the CPU
 baseline in ``bench.py`` can run the reference's own code.  Nothing in the
 product package imports it.
 
 Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
 
-1. ``cythonize`` (needs Cython and the reference sources): copies the five
-   hot-path modules plus ``ctracer.pxd`` and ``core/tracer.py`` from the
-   reference checkout into ``oracle/_ref/raypier/core/`` and generates the
+1. ``cythonize`` (needs Cython and the reference sources): copies the six
+   Cython modules plus ``ctracer.pxd`` and ``core/{tracer,fields,utils}.py``
+   from the reference checkout into ``oracle/_ref/raypier/core/`` and generates the
    ``.c`` files next to them.  Runs in the development container.
 2. ``compile`` (needs only gcc, Python headers and numpy headers): compiles each
    generated ``.c`` into an extension module with ``-O2 -ffp-contract=off``
    (no ``-march=native``: FMA contraction would change float results) and
-   ``-fopenmp`` (``cdistortions`` calls the OpenMP runtime).  Runs on any host
+   ``-fopenmp`` (``cdistortions`` and ``cfields`` call the OpenMP runtime).  Runs on any host
    the generated C travelled to, including an aarch64 host.
 
 ``load()`` imports the compiled modules through a stub ``raypier`` package,
@@ -35,7 +36,9 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 PKG_DIR = os.path.join(REF_OUT, "raypier", "core")
-MODULES = ["ctracer", "cmaterials", "cfaces", "cshapes", "cdistortions"]
+MODULES = ["ctracer", "cmaterials", "cfaces", "cshapes", "cdistortions", "cfields"]
+# pure-Python modules of the reference imported next to them
+PY_MODULES = ["tracer", "fields", "utils"]
 DEFAULT_SRC = os.environ.get("RP_REFERENCE_SRC", "/root/reference")
 
 
@@ -49,7 +52,7 @@ def cythonize(src_root: str = DEFAULT_SRC) -> None:
     if not os.path.isdir(core):
         raise FileNotFoundError(f"reference sources not found at {core}")
     os.makedirs(PKG_DIR, exist_ok=True)
-    for name in [m + ".pyx" for m in MODULES] + ["ctracer.pxd", "tracer.py"]:
+    for name in [m + ".pyx" for m in MODULES] + ["ctracer.pxd"] + [m + ".py" for m in PY_MODULES]:
         shutil.copyfile(os.path.join(core, name), os.path.join(PKG_DIR, name))
     for init in (os.path.join(REF_OUT, "raypier", "__init__.py"),
                  os.path.join(PKG_DIR, "__init__.py")):
@@ -116,7 +119,7 @@ def load():
     """Import the compiled reference modules through a stub ``raypier`` package.
 
     Returns a namespace with ``ctracer, cmaterials, cfaces, cshapes,
-    cdistortions, tracer``.
+    cdistortions, cfields, tracer, fields, utils``.
     """
     if not have_built():
         raise ImportError("reference tracer is not built (oracle/build_ref.py)")
@@ -128,7 +131,7 @@ def load():
         for k in [k for k in sys.modules if k.startswith("raypier.")]:
             del sys.modules[k]
     ns = types.SimpleNamespace()
-    for m in MODULES + ["tracer"]:
+    for m in MODULES + PY_MODULES:
         setattr(ns, m, importlib.import_module("raypier.core." + m))
     return ns
 

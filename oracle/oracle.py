@@ -63,6 +63,8 @@ def load():
             lib.rp_oracle_trace_gausslet_segment.argtypes = [P, P, ctypes.c_int64, P, U64, D, I, I, P, U64,
                                                              ctypes.POINTER(U64), P, P]
             lib.rp_oracle_select_intersections.argtypes = [P, I, P, U64, ctypes.c_uint32, P, ctypes.POINTER(U64)]
+            lib.rp_oracle_evaluate_modes.argtypes = [P, P, P, P, ctypes.c_int64, I, D, P]
+            lib.rp_oracle_sum_gaussian_modes.argtypes = [P, ctypes.c_int64, P, P, P, ctypes.c_int64, D, P]
             lib.rp_oracle_eval_parabasal.argtypes = [P, P, ctypes.c_int64, I, P, P, P, P, P, ctypes.c_uint32, P]
             _lib = lib
         return _lib
@@ -318,3 +320,29 @@ def select_ray_intersections(tables, list_idx, collections):
     reduced, inverse = np.unique(np.concatenate(wls), return_inverse=True)
     recs['wavelength_idx'] = inverse.reshape(-1)[recs['wavelength_idx']]
     return recs, reduced
+
+
+# ---- E-field summation (cfields.pyx) ------------------------------------------------
+def evaluate_modes(x, y, dx, dy, blending=1.0):
+    """evaluate_modes (cfields.pyx:225-234) on the host: n x 3 complex mode coefficients."""
+    lib = load()
+    a = [np.ascontiguousarray(v, dtype=np.double) for v in (x, y, dx, dy)]
+    n, size = a[0].shape
+    out = np.zeros((n, 3), dtype=np.complex128)
+    if lib.rp_oracle_evaluate_modes(a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data, a[3].ctypes.data, n, size,
+                                    float(blending), out.ctypes.data) != 0:
+        raise ZeroDivisionError("float division")
+    return out
+
+
+def sum_gaussian_modes(rays, modes, wavelengths, points, time_ps=0.0):
+    """sum_gaussian_modes (cfields.pyx:49-117) on the host: n_points x 3 complex."""
+    lib = load()
+    r = _rays(rays)
+    m = np.ascontiguousarray(modes, dtype=np.complex128)
+    wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+    p = np.ascontiguousarray(points, dtype=np.double).reshape(-1, 3)
+    out = np.zeros((p.shape[0], 3), dtype=np.complex128)
+    lib.rp_oracle_sum_gaussian_modes(r.ctypes.data, len(r), m.ctypes.data, wl.ctypes.data, p.ctypes.data,
+                                     p.shape[0], float(time_ps), out.ctypes.data)
+    return out

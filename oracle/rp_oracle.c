@@ -1951,3 +1951,139 @@ int rp_oracle_select_intersections(const rp_scene_desc *s, int list, const rp_ra
     *n_out = k;
     return 0;
 }
+
+/* ---- E-field summation: raypier/core/cfields.pyx -------------------------- */
+/* evaluate_one_mode (cfields.pyx:150-222): closed-form least-squares fit of
+ * the Gaussian mode coefficients to a gausslet's parabasal offsets (x, y) and
+ * slopes (dx, dy).  Returns -1 where the reference raises ZeroDivisionError
+ * (its divisions here are not cdivision). */
+static int evaluate_one_mode(double complex *out, const double *x, const double *y, const double *dx,
+                             const double *dy, double blending, int size) {
+    double a00 = 0, a01 = 0, a02 = 0, a11 = 0, a12 = 0, a22 = 0, b0 = 0, b1 = 0, b2 = 0, xi2, yi2, num, den;
+    double re[3], im[3];
+    for (int i = 0; i < size; i++) {
+        xi2 = x[i] * x[i];
+        yi2 = y[i] * y[i];
+        a00 = a00 + xi2 * xi2;
+        a01 = a01 + ((2 * xi2) * x[i]) * y[i];
+        a02 = a02 + xi2 * yi2;
+        a11 = a11 + (4 * xi2) * yi2;
+        a12 = a12 + ((2 * x[i]) * y[i]) * yi2;
+        a22 = a22 + yi2 * yi2;
+        b0 = b0 + xi2;
+        b1 = b1 + (2 * x[i]) * y[i];
+        b2 = b2 + yi2;
+    }
+    den = (((((-a00) * a11) * a22) + (a00 * pow(a12, 2.0))) + (pow(a01, 2.0) * a22)) - (((2.0 * a01) * a02) * a12)
+          + (pow(a02, 2.0) * a11);
+    if (den == 0) return -1;
+    num = blending * ((((-b0) * ((a11 * a22) - pow(a12, 2.0))) + (b1 * ((a01 * a22) - (a02 * a12))))
+                      - (b2 * ((a01 * a12) - (a02 * a11))));
+    im[0] = num / den;
+    num = (-blending) * (((b0 * ((a01 * a22) - (a02 * a12))) - (b1 * ((a00 * a22) - pow(a02, 2.0))))
+                         + (b2 * ((a00 * a12) - (a01 * a02))));
+    im[1] = num / den;
+    num = blending * ((((-b0) * ((a01 * a12) - (a02 * a11))) + (b1 * ((a00 * a12) - (a01 * a02))))
+                      - (b2 * ((a00 * a11) - pow(a01, 2.0))));
+    im[2] = num / den;
+    a00 = 0; a01 = 0; a02 = 0; a11 = 0; a12 = 0; a22 = 0; b0 = 0; b1 = 0; b2 = 0;
+    for (int i = 0; i < size; i++) {
+        xi2 = x[i] * x[i];
+        yi2 = y[i] * y[i];
+        a00 = a00 + xi2;
+        a01 = a01 + x[i] * y[i];
+        a11 = a11 + (xi2 + yi2);
+        a22 = a22 + yi2;
+        b0 = b0 + dx[i] * x[i];
+        b1 = b1 + ((dx[i] * y[i]) + (dy[i] * x[i]));
+        b2 = b2 + dy[i] * y[i];
+    }
+    a12 = a01 * a01;
+    den = ((a00 * a12) - ((a00 * a11) * a22)) + (a12 * a22);
+    if (den == 0) return -1;
+    re[0] = ((((-a12) * b2) + ((a01 * a22) * b1)) + (b0 * (a12 - (a11 * a22)))) / den;
+    re[1] = (-((((a00 * a01) * b2) - ((a00 * a22) * b1)) + ((a01 * a22) * b0))) / den;
+    re[2] = ((((a00 * a01) * b1) - (a12 * b0)) - (b2 * ((a00 * a11) - a12))) / den;
+    for (int k = 0; k < 3; k++) {
+        __real__ out[k] = re[k];
+        __imag__ out[k] = im[k];
+    }
+    return 0;
+}
+
+/* evaluate_modes (cfields.pyx:225-234): n rows of `size` parabasal samples;
+ * modes[n][3] complex as (re, im) pairs.  Returns -1 on a zero denominator. */
+int rp_oracle_evaluate_modes(const double *x, const double *y, const double *dx, const double *dy, int64_t n,
+                             int size, double blending, double *modes) {
+    for (int64_t i = 0; i < n; i++) {
+        double complex m[3];
+        if (evaluate_one_mode(m, x + i * size, y + i * size, dx + i * size, dy + i * size, blending, size))
+            return -1;
+        for (int k = 0; k < 3; k++) {
+            modes[(i * 3 + k) * 2] = creal(m[k]);
+            modes[(i * 3 + k) * 2 + 1] = cimag(m[k]);
+        }
+    }
+    return 0;
+}
+
+/* calc_mode_U (cfields.pyx:120-147) */
+static double complex calc_mode_U(double complex A, double complex B, double complex C, double complex detG0, vec pt,
+                                  vec E, vec H, vec direction, double complex k, double phase,
+                                  double inv_root_area, double complex rootI) {
+    double x = dotprod_(pt, E), y = dotprod_(pt, H), z = dotprod_(pt, direction);
+    double complex denom = (1 + (z * (A + C)) + (z * z) * detG0) * 2;
+    double complex AA = (A + z * detG0) / denom;
+    double complex CC = (C + z * detG0) / denom;
+    double complex U = cexp(I * (phase + k * (z + AA * (x * x) + B * (2 * x * y) / denom + CC * (y * y))));
+    U /= csqrt(((1 + z * A) * (1 + z * C) - (z * B) * (z * B)) * I);
+    U *= inv_root_area * rootI;
+    return U;
+}
+
+/* sum_gaussian_modes (cfields.pyx:49-117): E[n_points][3] complex as (re, im)
+ * pairs, summed over the rays in order for every point. */
+int rp_oracle_sum_gaussian_modes(const rp_ray *rays, int64_t n_rays, const double *modes, const double *wavelengths,
+                                 const double *points, int64_t n_points, double time_ps, double *E_out) {
+    const double complex rootI = csqrt(I);
+    double c = 0.299792458;
+    c *= time_ps;
+    double complex *out = calloc((size_t)(n_points > 0 ? n_points : 1) * 3, sizeof(double complex));
+    if (!out) return -1;
+    for (int64_t iray = 0; iray < n_rays; iray++) {
+        rp_ray ray = rays[iray];
+        vec E = norm_(ld_v(ray.E_vector));
+        vec D = ld_v(ray.direction);
+        vec H = norm_(cross_(D, E));
+        double k = 2000.0 * M_PI / wavelengths[ray.wavelength_idx];
+        double phase = ray.phase + (ray.accumulated_path * k) - (c * k / ray.refractive_index[0]);
+        double complex kz = ld_c(ray.refractive_index);
+        kz *= k;
+        double invk = 2. / creal(kz);
+        double complex A = ld_c(modes + iray * 6 + 0);
+        double complex B = ld_c(modes + iray * 6 + 2);
+        double complex C = ld_c(modes + iray * 6 + 4);
+        double inv_root_area = sqrt(sqrt(cimag(A) * cimag(C) - (cimag(B) * cimag(B))) * (2.0 / M_PI));
+        __imag__ A = __imag__ A * invk;
+        __imag__ B = __imag__ B * invk;
+        __imag__ C = __imag__ C * invk;
+        double complex detG0 = (A * C) - (B * B);
+        double complex E1a = ld_c(ray.E1_amp), E2a = ld_c(ray.E2_amp);
+        vec O = ld_v(ray.origin);
+        for (int64_t ipt = 0; ipt < n_points; ipt++) {
+            vec pt = {points[ipt * 3], points[ipt * 3 + 1], points[ipt * 3 + 2]};
+            pt = subvv_(pt, O);
+            double complex U = calc_mode_U(A, B, C, detG0, pt, E, H, D, kz, phase, inv_root_area, rootI);
+            double complex E1 = E1a * U, E2 = E2a * U;
+            out[ipt * 3 + 0] += (E1 * E.x + E2 * H.x);
+            out[ipt * 3 + 1] += (E1 * E.y + E2 * H.y);
+            out[ipt * 3 + 2] += (E1 * E.z + E2 * H.z);
+        }
+    }
+    for (int64_t i = 0; i < n_points * 3; i++) {
+        E_out[2 * i] = creal(out[i]);
+        E_out[2 * i + 1] = cimag(out[i]);
+    }
+    free(out);
+    return 0;
+}

@@ -35,6 +35,7 @@ SOURCES = [
     ("rp_serve.cu", ["--fmad=false"]),
     ("rp_gausslet.cu", ["--fmad=false"]),
     ("rp_capture.cu", ["--fmad=false"]),
+    ("rp_fields.cu", ["--fmad=false"]),
 ]
 
 
@@ -195,6 +196,13 @@ _SIGS = {
     "rp_gausslets_count": (_I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "rp_gausslets_upload": (_I, [_P, _P, ctypes.c_uint64]),
     "rp_gausslets_download": (_I, [_P, _P, ctypes.c_uint64]),
+    "rp_field_evaluate_modes": (_I, [_P, _P, _P, _P, _P, ctypes.c_uint64, ctypes.c_int32, ctypes.c_double, _P]),
+    "rp_field_create": (_I, [_P, _P, ctypes.c_uint64, _P, _P, ctypes.c_int64, ctypes.POINTER(_P)]),
+    "rp_field_destroy": (_I, [_P]),
+    "rp_field_evaluate": (_I, [_P, _P, ctypes.c_uint64, ctypes.c_double, _P]),
+    "rp_field_evaluate_device": (_I, [_P, _P, ctypes.c_uint64, ctypes.c_double, _P]),
+    "rp_field_sum_gaussian_modes": (_I, [_P, _P, ctypes.c_uint64, _P, _P, ctypes.c_int64, _P, ctypes.c_uint64,
+                                         ctypes.c_double, _P]),
     "rp_select_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
     "rp_select_gausslet_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
     "rp_trace_gausslet_segment": (_I, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _P,

@@ -1,0 +1,388 @@
+// rp_fields.cu -- E-field summation over Gaussian modes (raypier/core/cfields.pyx),
+// the consumer of traced rays and gausslets: the least-squares mode fit of
+// each gausslet (evaluate_modes, 150-234) and the coherent sum of every mode
+// at every evaluation point (sum_gaussian_modes with calc_mode_U, 49-147).
+// Compiled with --fmad=false, like the tracing kernels.
+//
+// The sum is points x rays complex exponentials of FP64 arguments (phases of
+// 1e4 .. 1e6 rad): one thread per evaluation point accumulates the three
+// field components over all modes in the reference's order (ray by ray), the
+// block staging the per-mode constants in shared memory one tile at a time.
+// The per-mode constants (basis, scaled curvature, determinant, phase at the
+// requested time) are computed once per evaluation by a small kernel.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <new>
+
+#include "rp_internal.h"
+
+namespace rp {
+
+// Per-mode constants of sum_gaussian_modes (cfields.pyx:76-100).
+#define RP_MODE_WORDS 28
+#define RP_FIELD_BLOCK 128
+#define RP_FIELD_TILE 32
+
+enum : unsigned { FERR_ZERO_DIV = 1u, FERR_WAVELENGTH = 2u };
+
+// Complex quotient by Smith's method (R. L. Smith, "Algorithm 116: Complex
+// division", CACM 5(8), 1962).
+__device__ __forceinline__ cx cdiv_smith(cx a, cx b) {
+    if (fabs(b.x) < fabs(b.y)) {
+        double r = b.x / b.y;
+        double den = (b.x * r) + b.y;
+        return mkc(((a.x * r) + a.y) / den, ((a.y * r) - a.x) / den);
+    }
+    double r = b.y / b.x;
+    double den = (b.y * r) + b.x;
+    return mkc(((a.y * r) + a.x) / den, (a.y - (a.x * r)) / den);
+}
+
+__device__ __forceinline__ cx cexp_f(cx z) {
+    double e = exp(z.x), s, c;
+    sincos(z.y, &s, &c);
+    return mkc(e * c, e * s);
+}
+
+// evaluate_one_mode (cfields.pyx:150-222).  Returns false on a zero
+// denominator, where the reference raises ZeroDivisionError.
+__device__ bool eval_one_mode(const double *x, const double *y, const double *dx, const double *dy, int size,
+                              double blending, cx *out) {
+    double a00 = 0, a01 = 0, a02 = 0, a11 = 0, a12 = 0, a22 = 0, b0 = 0, b1 = 0, b2 = 0;
+    for (int i = 0; i < size; i++) {
+        double xi2 = x[i] * x[i], yi2 = y[i] * y[i];
+        a00 = a00 + xi2 * xi2;
+        a01 = a01 + ((2 * xi2) * x[i]) * y[i];
+        a02 = a02 + xi2 * yi2;
+        a11 = a11 + (4 * xi2) * yi2;
+        a12 = a12 + ((2 * x[i]) * y[i]) * yi2;
+        a22 = a22 + yi2 * yi2;
+        b0 = b0 + xi2;
+        b1 = b1 + (2 * x[i]) * y[i];
+        b2 = b2 + yi2;
+    }
+    double den = ((((((-a00) * a11) * a22) + (a00 * (a12 * a12))) + ((a01 * a01) * a22)) - (((2.0 * a01) * a02) * a12)) +
+                 ((a02 * a02) * a11);
+    if (den == 0) return false;
+    double im0 = (blending * ((((-b0) * ((a11 * a22) - (a12 * a12))) + (b1 * ((a01 * a22) - (a02 * a12)))) -
+                              (b2 * ((a01 * a12) - (a02 * a11))))) / den;
+    double im1 = ((-blending) * (((b0 * ((a01 * a22) - (a02 * a12))) - (b1 * ((a00 * a22) - (a02 * a02)))) +
+                                 (b2 * ((a00 * a12) - (a01 * a02))))) / den;
+    double im2 = (blending * ((((-b0) * ((a01 * a12) - (a02 * a11))) + (b1 * ((a00 * a12) - (a01 * a02)))) -
+                              (b2 * ((a00 * a11) - (a01 * a01))))) / den;
+    a00 = a01 = a02 = a11 = a12 = a22 = b0 = b1 = b2 = 0;
+    for (int i = 0; i < size; i++) {
+        double xi2 = x[i] * x[i], yi2 = y[i] * y[i];
+        a00 = a00 + xi2;
+        a01 = a01 + x[i] * y[i];
+        a11 = a11 + (xi2 + yi2);
+        a22 = a22 + yi2;
+        b0 = b0 + dx[i] * x[i];
+        b1 = b1 + ((dx[i] * y[i]) + (dy[i] * x[i]));
+        b2 = b2 + dy[i] * y[i];
+    }
+    a12 = a01 * a01;
+    den = ((a00 * a12) - ((a00 * a11) * a22)) + (a12 * a22);
+    if (den == 0) return false;
+    out[0] = mkc(((((-a12) * b2) + ((a01 * a22) * b1)) + (b0 * (a12 - (a11 * a22)))) / den, im0);
+    out[1] = mkc((-((((a00 * a01) * b2) - ((a00 * a22) * b1)) + ((a01 * a22) * b0))) / den, im1);
+    out[2] = mkc(((((a00 * a01) * b1) - (a12 * b0)) - (b2 * ((a00 * a11) - a12))) / den, im2);
+    return true;
+}
+
+// x, y, dx, dy: n rows of `size` (at most 64) samples; modes: n x 3 complex.
+__global__ void modes_kernel(const double *x, const double *y, const double *dx, const double *dy,
+                             unsigned long long n, int size, double blending, cx *modes, unsigned *err) {
+    unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long o = i * (unsigned long long)size;
+    cx m[3];
+    if (!eval_one_mode(x + o, y + o, dx + o, dy + o, size, blending, m)) {
+        atomicOr(err, FERR_ZERO_DIV);
+        m[0] = m[1] = m[2] = mkc(nan_d(), nan_d());
+    }
+    modes[3 * i] = m[0];
+    modes[3 * i + 1] = m[1];
+    modes[3 * i + 2] = m[2];
+}
+
+// Per-mode constants (cfields.pyx:76-100) for time `time_ps`.
+__global__ void mode_constants_kernel(RaySoA r, unsigned long long n, const cx *modes, const double *wl, long long n_wl,
+                                      double time_ps, double *P, unsigned *err) {
+    unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double c = 0.299792458;
+    c *= time_ps;
+    v3 D = mkv(r.dx[i], r.dy[i], r.dz[i]);
+    v3 E = normv(mkv(r.ex[i], r.ey[i], r.ez[i]));
+    v3 H = normv(crossv(D, E));
+    unsigned w = r.wl[i];
+    if ((long long)w >= n_wl) {
+        atomicOr(err, FERR_WAVELENGTH);
+        w = 0;
+    }
+    double k = 2000.0 * 3.14159265358979323846 / wl[w];
+    cx n_idx = r.n[i];
+    double phase = r.phase[i] + (r.opl[i] * k) - (c * k / n_idx.x);
+    cx kz = mkc(n_idx.x * k, n_idx.y * k);
+    double invk = 2. / kz.x;
+    cx A = modes[3 * i], B = modes[3 * i + 1], C = modes[3 * i + 2];
+    double inv_root_area = sqrt(sqrt(A.y * C.y - (B.y * B.y)) * (2.0 / 3.14159265358979323846));
+    A.y *= invk;
+    B.y *= invk;
+    C.y *= invk;
+    cx detG0 = csub(cmul(A, C), cmul(B, B));
+    double *p = P + i * RP_MODE_WORDS;
+    p[0] = r.ox[i]; p[1] = r.oy[i]; p[2] = r.oz[i];
+    p[3] = E.x; p[4] = E.y; p[5] = E.z;
+    p[6] = H.x; p[7] = H.y; p[8] = H.z;
+    p[9] = D.x; p[10] = D.y; p[11] = D.z;
+    p[12] = A.x; p[13] = A.y; p[14] = B.x; p[15] = B.y; p[16] = C.x; p[17] = C.y;
+    p[18] = detG0.x; p[19] = detG0.y;
+    p[20] = kz.x; p[21] = kz.y;
+    p[22] = phase;
+    p[23] = inv_root_area;
+    cx e1 = r.e1[i], e2 = r.e2[i];
+    p[24] = e1.x; p[25] = e1.y; p[26] = e2.x; p[27] = e2.y;
+}
+
+// calc_mode_U (cfields.pyx:120-147) of the mode whose constants are `p`.
+__device__ __forceinline__ cx mode_U(const double *p, double px, double py, double pz) {
+    v3 pt = mkv(px - p[0], py - p[1], pz - p[2]);
+    double x = dotv(pt, mkv(p[3], p[4], p[5]));
+    double y = dotv(pt, mkv(p[6], p[7], p[8]));
+    double z = dotv(pt, mkv(p[9], p[10], p[11]));
+    const cx A = mkc(p[12], p[13]), B = mkc(p[14], p[15]), C = mkc(p[16], p[17]), G = mkc(p[18], p[19]);
+    const cx k = mkc(p[20], p[21]);
+    cx denom = cmuls(cadd(cadd(mkc(1.0, 0.0), cmuls(cadd(A, C), z)), cmuls(G, z * z)), 2.0);
+    cx AA = cdiv_smith(cadd(A, cmuls(G, z)), denom);
+    cx CC = cdiv_smith(cadd(C, cmuls(G, z)), denom);
+    cx t = cadd(cadd(cadd(mkc(z, 0.0), cmuls(AA, x * x)), cdiv_smith(cmuls(B, 2 * x * y), denom)), cmuls(CC, y * y));
+    cx w = cmul(k, t);
+    w.x = p[22] + w.x;
+    cx U = cexp_f(mkc(-w.y, w.x));  // exp(i w)
+    cx q = csub(cmul(cadd(mkc(1.0, 0.0), cmuls(A, z)), cadd(mkc(1.0, 0.0), cmuls(C, z))),
+                cmul(cmuls(B, z), cmuls(B, z)));
+    U = cdiv_smith(U, csqrt_(mkc(-q.y, q.x)));  // csqrt(q i)
+    const double h = 0.70710678118654752440;  // sqrt(i) = (1 + i) / sqrt(2)
+    return cmul(U, mkc(p[23] * h, p[23] * h));
+}
+
+__global__ void __launch_bounds__(RP_FIELD_BLOCK) field_sum_kernel(const double *P, unsigned long long n_modes,
+                                                                   const double *pts, unsigned long long n_pts,
+                                                                   cx *E_out) {
+    __shared__ double sp[RP_FIELD_TILE * RP_MODE_WORDS];
+    const unsigned long long ipt = (unsigned long long)blockIdx.x * RP_FIELD_BLOCK + threadIdx.x;
+    const bool active = ipt < n_pts;
+    double px = 0, py = 0, pz = 0;
+    if (active) {
+        px = pts[3 * ipt];
+        py = pts[3 * ipt + 1];
+        pz = pts[3 * ipt + 2];
+    }
+    cx o0 = mkc(0, 0), o1 = mkc(0, 0), o2 = mkc(0, 0);
+    for (unsigned long long t0 = 0; t0 < n_modes; t0 += RP_FIELD_TILE) {
+        const unsigned nt = (unsigned)(n_modes - t0 < RP_FIELD_TILE ? n_modes - t0 : RP_FIELD_TILE);
+        __syncthreads();
+        for (unsigned k = threadIdx.x; k < nt * RP_MODE_WORDS; k += RP_FIELD_BLOCK) sp[k] = P[t0 * RP_MODE_WORDS + k];
+        __syncthreads();
+        if (active) {
+            for (unsigned j = 0; j < nt; j++) {
+                const double *p = sp + j * RP_MODE_WORDS;
+                cx U = mode_U(p, px, py, pz);
+                cx E1 = cmul(mkc(p[24], p[25]), U), E2 = cmul(mkc(p[26], p[27]), U);
+                o0 = cadd(o0, cadd(cmuls(E1, p[3]), cmuls(E2, p[6])));
+                o1 = cadd(o1, cadd(cmuls(E1, p[4]), cmuls(E2, p[7])));
+                o2 = cadd(o2, cadd(cmuls(E1, p[5]), cmuls(E2, p[8])));
+            }
+        }
+    }
+    if (active) {
+        E_out[3 * ipt] = o0;
+        E_out[3 * ipt + 1] = o1;
+        E_out[3 * ipt + 2] = o2;
+    }
+}
+
+}  // namespace rp
+
+using namespace rp;
+
+// ---- C ABI ----------------------------------------------------------------------
+struct rp_field {
+    rp_ctx *ctx;
+    uint64_t n_modes;
+    rp_rays *rays;     // the modes' base rays
+    cx *modes;         // n_modes x 3
+    double *wl;        // the wavelength table
+    int64_t n_wl;
+    double *consts;    // n_modes x RP_MODE_WORDS
+    unsigned *err;
+    size_t modes_bytes, wl_bytes, consts_bytes, err_bytes;
+};
+
+static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+#define FCK(call)                                              \
+    do {                                                       \
+        cudaError_t _e = (call);                               \
+        if (_e != cudaSuccess) return rp__cuda_fail(_e, #call); \
+    } while (0)
+
+extern "C" {
+
+int rp_field_evaluate_modes(rp_ctx *ctx, const double *x, const double *y, const double *dx, const double *dy,
+                            uint64_t n, int32_t size, double blending, double *modes_out) {
+    if (!ctx || (n && (!x || !y || !dx || !dy || !modes_out)) || size < 1 || size > 64) return RP_ERR_INVALID;
+    if (n == 0) return RP_OK;
+    FCK(cudaSetDevice(ctx->device));
+    // every array of the block starts on a 256-byte boundary (the modes are
+    // 16-byte double2 stores)
+    const size_t in_b = align_up((size_t)n * size * sizeof(double)), out_b = align_up((size_t)n * 3 * sizeof(cx));
+    unsigned char *blk = nullptr;
+    size_t got = 0;
+    int rc = rp__ctx_alloc(ctx, (void **)&blk, 4 * in_b + out_b + 256, &got);
+    if (rc) return rc;
+    double *d[4];
+    for (int k = 0; k < 4; k++) d[k] = (double *)(blk + k * in_b);
+    cx *m = (cx *)(blk + 4 * in_b);
+    unsigned *err = (unsigned *)(blk + 4 * in_b + out_b);
+    const size_t copy_b = (size_t)n * size * sizeof(double);
+    const double *h[4] = {x, y, dx, dy};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 4 && e == cudaSuccess; k++)
+        e = cudaMemcpyAsync(d[k], h[k], copy_b, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(unsigned), ctx->stream);
+    if (e == cudaSuccess) {
+        modes_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(d[0], d[1], d[2], d[3], n, size, blending,
+                                                                         m, err);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(modes_out, m, (size_t)n * 3 * sizeof(cx), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned, err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    unsigned ferr = (unsigned)(ctx->h_pinned[0] & 0xffffffffu);
+    rp__ctx_free(ctx, blk, got);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "rp_field_evaluate_modes");
+    if (ferr & FERR_ZERO_DIV) {
+        rp__set_error("float division");
+        return RP_ERR_INVALID;
+    }
+    return RP_OK;
+}
+
+int rp_field_create(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double *modes, const double *wavelengths,
+                    int64_t n_wl, rp_field **out) {
+    if (!ctx || !out || (n_rays && (!rays || !modes)) || n_wl < 0 || (n_wl && !wavelengths)) return RP_ERR_INVALID;
+    *out = nullptr;
+    FCK(cudaSetDevice(ctx->device));
+    rp_field *f = new (std::nothrow) rp_field();
+    if (!f) return RP_ERR_NOMEM;
+    f->ctx = ctx;
+    f->n_modes = n_rays;
+    f->n_wl = n_wl;
+    int rc = rp_rays_alloc(ctx, n_rays ? n_rays : 1, &f->rays);
+    if (rc == RP_OK) rc = rp_rays_upload_aos(f->rays, rays, n_rays);
+    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->modes, (size_t)(n_rays ? n_rays : 1) * 3 * sizeof(cx),
+                                        &f->modes_bytes);
+    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->wl, (size_t)(n_wl ? n_wl : 1) * sizeof(double), &f->wl_bytes);
+    if (rc == RP_OK)
+        rc = rp__ctx_alloc(ctx, (void **)&f->consts, (size_t)(n_rays ? n_rays : 1) * RP_MODE_WORDS * sizeof(double),
+                           &f->consts_bytes);
+    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->err, sizeof(unsigned), &f->err_bytes);
+    if (rc == RP_OK) {
+        cudaError_t e = cudaSuccess;
+        if (n_rays) e = cudaMemcpyAsync(f->modes, modes, (size_t)n_rays * 3 * sizeof(cx), cudaMemcpyHostToDevice,
+                                        ctx->stream);
+        if (e == cudaSuccess && n_wl)
+            e = cudaMemcpyAsync(f->wl, wavelengths, (size_t)n_wl * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = rp__cuda_fail(e, "rp_field_create");
+    }
+    if (rc) {
+        rp_field_destroy(f);
+        return rc;
+    }
+    *out = f;
+    return RP_OK;
+}
+
+int rp_field_destroy(rp_field *f) {
+    if (!f) return RP_ERR_INVALID;
+    rp_ctx *ctx = f->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (f->rays) rp_rays_free(f->rays);
+    if (f->modes) rp__ctx_free(ctx, f->modes, f->modes_bytes);
+    if (f->wl) rp__ctx_free(ctx, f->wl, f->wl_bytes);
+    if (f->consts) rp__ctx_free(ctx, f->consts, f->consts_bytes);
+    if (f->err) rp__ctx_free(ctx, f->err, f->err_bytes);
+    delete f;
+    return RP_OK;
+}
+
+int rp_field_evaluate_device(rp_field *f, const double *points_dev, uint64_t n_points, double time_ps, double *E_dev) {
+    if (!f || (n_points && (!points_dev || !E_dev))) return RP_ERR_INVALID;
+    // the kernel stores E as 16-byte complex pairs and reads 8-byte coordinates
+    if (((uintptr_t)E_dev & 15) || ((uintptr_t)points_dev & 7)) return RP_ERR_INVALID;
+    rp_ctx *ctx = f->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    if (n_points == 0) return RP_OK;
+    FCK(cudaMemsetAsync(f->err, 0, sizeof(unsigned), ctx->stream));
+    if (f->n_modes) {
+        mode_constants_kernel<<<(unsigned)((f->n_modes + 127) / 128), 128, 0, ctx->stream>>>(
+            f->rays->soa, f->n_modes, f->modes, f->wl, f->n_wl, time_ps, f->consts, f->err);
+        FCK(cudaGetLastError());
+    }
+    field_sum_kernel<<<(unsigned)((n_points + RP_FIELD_BLOCK - 1) / RP_FIELD_BLOCK), RP_FIELD_BLOCK, 0, ctx->stream>>>(
+        f->consts, f->n_modes, points_dev, n_points, (cx *)E_dev);
+    FCK(cudaGetLastError());
+    FCK(cudaMemcpyAsync(ctx->h_pinned, f->err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    FCK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_pinned[0] & FERR_WAVELENGTH) {
+        rp__set_error("a ray's wavelength_idx is outside the wavelength table");
+        return RP_ERR_INVALID;
+    }
+    return RP_OK;
+}
+
+int rp_field_evaluate(rp_field *f, const double *points, uint64_t n_points, double time_ps, double *E_out) {
+    if (!f || (n_points && (!points || !E_out))) return RP_ERR_INVALID;
+    rp_ctx *ctx = f->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    if (n_points == 0) return RP_OK;
+    const size_t pb = (size_t)n_points * 3 * sizeof(double), eb = (size_t)n_points * 3 * sizeof(cx);
+    unsigned char *blk = nullptr;
+    size_t got = 0;
+    int rc = rp__ctx_alloc(ctx, (void **)&blk, align_up(pb) + eb, &got);
+    if (rc) return rc;
+    double *dp = (double *)blk, *de = (double *)(blk + align_up(pb));  // E on a 256-byte boundary
+    cudaError_t e = cudaMemcpyAsync(dp, points, pb, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) {
+        rp__ctx_free(ctx, blk, got);
+        return rp__cuda_fail(e, "rp_field_evaluate");
+    }
+    rc = rp_field_evaluate_device(f, dp, n_points, time_ps, de);
+    if (rc == RP_OK) {
+        e = cudaMemcpyAsync(E_out, de, eb, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = rp__cuda_fail(e, "rp_field_evaluate");
+    }
+    rp__ctx_free(ctx, blk, got);
+    return rc;
+}
+
+int rp_field_sum_gaussian_modes(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double *modes,
+                                const double *wavelengths, int64_t n_wl, const double *points, uint64_t n_points,
+                                double time_ps, double *E_out) {
+    rp_field *f = nullptr;
+    int rc = rp_field_create(ctx, rays, n_rays, modes, wavelengths, n_wl, &f);
+    if (rc) return rc;
+    rc = rp_field_evaluate(f, points, n_points, time_ps, E_out);
+    rp_field_destroy(f);
+    return rc;
+}
+
+}  // extern "C"

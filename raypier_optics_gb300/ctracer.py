@@ -286,6 +286,7 @@ class RayCollection:
         self._parent = None
         self._wavelengths = np.zeros(0, dtype=np.double)
         self._neighbours = None
+        self._nb_source = None
 
     # -- residency ------------------------------------------------------------
     @classmethod
@@ -426,11 +427,35 @@ class RayCollection:
 
     @property
     def neighbours(self):
-        return self._neighbours
+        """Indices of each ray's neighbours (n, k), -1 where there is none.  A
+        child generation derives them from its parent's through parent_idx and
+        the reflected / transmitted type (ctracer.pyx:1084-1131)."""
+        if self._parent is None:
+            return None if self._neighbours is None else np.asarray(self._neighbours)
+        pnb = self._parent.neighbours
+        if pnb is None:
+            return None if self._neighbours is None else np.asarray(self._neighbours)
+        if self._neighbours is None or self._nb_source is not pnb:
+            self._neighbours = self._eval_neighbours(np.asarray(pnb))
+            self._nb_source = pnb
+        return np.asarray(self._neighbours)
 
     @neighbours.setter
     def neighbours(self, nb):
-        self._neighbours = nb
+        self._neighbours = np.asarray(nb, dtype=np.int32)
+        self._nb_source = None
+
+    def _eval_neighbours(self, pnb):
+        self._sync_host()
+        h = self._host[:self._n]
+        rtype = (h['ray_type_id'] & REFL_RAY).astype(np.int64)
+        pidx = h['parent_idx'].astype(np.int64)
+        rmap = np.full((self._parent.n_rays, 2), -1, dtype=np.int32)
+        for i in range(self._n):   # later children of one parent and type win, as in the reference
+            rmap[pidx[i], rtype[i]] = i
+        cand = pnb[pidx]
+        nb = np.where(cand >= 0, rmap[np.maximum(cand, 0), rtype[:, None]], -1).astype(np.int32)
+        return nb
 
     # -- field views (ctracer.pyx:755-969) ----------------------------------------
     def _field(self, name):

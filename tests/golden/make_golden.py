@@ -10,6 +10,7 @@ Run in a container that has the reference sources and Cython:
     python tests/golden/make_golden.py --sequential  # only the trace_ray_sequence case
     python tests/golden/make_golden.py --gausslets   # only the Gausslet cases
     python tests/golden/make_golden.py --capture     # only the post-trace capture case
+    python tests/golden/make_golden.py --fields      # only the E-field summation cases
 
 Every fixture stores the scene description (the JSON spec understood by
 raypier_optics_gb300.workloads.build_scene), the inputs, and the reference's
@@ -466,6 +467,7 @@ def main():
     sequential_case(ref, out_dir)
     gausslet_cases(ref, out_dir)
     capture_cases(ref, out_dir)
+    field_cases(ref, out_dir)
     print("golden vectors written to", out_dir)
 
 
@@ -744,6 +746,90 @@ def capture_cases(ref, out_dir):
                         offsets=offs, gausslets=g, ggens=np.concatenate(ggens), goffsets=goffs, **out)
 
 
+def hex_field(rdt, radius, spacing, z0=0.0):
+    """Rays on a hexagonal lattice travelling along +z, with the indices of
+    each ray's six lattice neighbours (-1 where the lattice ends)."""
+    m = int(radius / spacing) + 2
+    i, j = np.meshgrid(np.arange(-m, m + 1), np.arange(-m, m + 1))
+    x = (i + 0.5 * j).reshape(-1) * spacing
+    y = (j * math.sqrt(3.0) / 2.0).reshape(-1) * spacing
+    keep = x * x + y * y <= radius * radius
+    x, y = x[keep], y[keep]
+    n = len(x)
+    rays = np.zeros(n, dtype=rdt)
+    W.fill_rays(rays, np.stack([x, y, np.full(n, z0)], axis=1), (0.0, 0.0, 1.0), (1.0, 0.0, 0.0))
+    nb = np.full((n, 6), -1, dtype=np.int32)
+    for k in range(n):
+        for a in range(6):
+            ang = a * math.pi / 3.0
+            tx, ty = x[k] + spacing * math.cos(ang), y[k] + spacing * math.sin(ang)
+            hit = np.flatnonzero(np.hypot(x - tx, y - ty) < 1e-6 * spacing)
+            if hit.size:
+                nb[k, a] = hit[0]
+    return rays, nb
+
+
+def field_cases(ref, out_dir):
+    """The E-field consumers (cfields.pyx, core/fields.py): single-call
+    evaluate_modes and sum_gaussian_modes vectors, eval_Efield_from_gausslets
+    of a gausslet beam before and after the configuration-1 lens,
+    EFieldSummation at a non-zero time, and eval_Efield_from_rays of a
+    hexagonal ray field."""
+    rdt = ref.ctracer.ray_dtype
+    rng = np.random.Generator(np.random.PCG64(RNG_SEED + 307))
+    u = {}
+    # evaluate_modes on random parabasal offsets
+    x = rng.normal(0, 0.1, (64, 6))
+    y = rng.normal(0, 0.1, (64, 6))
+    dx = rng.normal(0, 1e-3, (64, 6))
+    dy = rng.normal(0, 1e-3, (64, 6))
+    u.update(modes_x=x, modes_y=y, modes_dx=dx, modes_dy=dy,
+             modes_out=np.asarray(ref.cfields.evaluate_modes(x, y, dx, dy, 1.3)))
+    # sum_gaussian_modes on random modes (positive widths) near their origins
+    n = 48
+    r, _ = random_rays(rdt, rng, n, 0.0, 1.0, 0.05, 0.5, per_ray_wl=True, wl_range=(0.5, 0.9))
+    r['wavelength_idx'] = rng.integers(0, 3, n)
+    r['refractive_index'] = 1.0 + 1e-4j
+    modes = rng.normal(0, 0.01, (n, 3)) + 1j * np.column_stack([rng.uniform(20, 40, n), rng.uniform(-2, 2, n),
+                                                                 rng.uniform(20, 40, n)])
+    wl = np.array([0.6, 0.55, 0.8])
+    pts = np.column_stack([rng.uniform(-0.6, 0.6, 300), rng.uniform(-0.6, 0.6, 300), rng.uniform(-1, 30, 300)])
+    rc = ref.ctracer.RayCollection.from_array(r.copy())
+    u.update(sum_rays=r, sum_modes=modes, sum_wl=wl, sum_points=pts,
+             sum_E=np.asarray(ref.cfields.sum_gaussian_modes(rc, modes, wl, pts, 0.0)),
+             sum_E_t=np.asarray(ref.cfields.sum_gaussian_modes(rc, modes, wl, pts, 2.5)))
+    # a gausslet beam: on its own, and after the configuration-1 lens
+    rays, nb = hex_field(rdt, 2.0, 0.4)
+    wl = np.array([0.6])
+    g = gausslets_from_rays(ref, rays, wl, 0.25, 0.0)
+    gc = ref.ctracer.GaussletCollection.from_array(g.copy())
+    gc.wavelengths = wl
+    gx, gy = np.meshgrid(np.linspace(-2.5, 2.5, 15), np.linspace(-2.5, 2.5, 15))
+    plane = np.column_stack([gx.reshape(-1), gy.reshape(-1), np.full(gx.size, 10.0)])
+    u.update(beam_gausslets=g, beam_wl=wl, beam_points=plane,
+             beam_E=np.asarray(ref.fields.eval_Efield_from_gausslets(gc, plane)))
+    lists = W.build_scene(W.config1_spec(), ref)
+    gc = ref.ctracer.GaussletCollection.from_array(g.copy())
+    gc.wavelengths = wl
+    with contextlib.redirect_stdout(io.StringIO()):
+        traced, _ = ref.tracer.trace_rays(gc, lists, recursion_limit=4, max_length=1000.0)
+    after = traced[3].copy_as_array()   # the gausslets leaving the lens towards the detector
+    fx, fz = np.meshgrid(np.linspace(-0.3, 0.3, 13), np.linspace(60.0, 110.0, 11))
+    focus = np.column_stack([fx.reshape(-1), np.zeros(fx.size), fz.reshape(-1)])
+    lens_gc = ref.ctracer.GaussletCollection.from_array(after.copy())
+    lens_gc.wavelengths = wl
+    summ = ref.fields.EFieldSummation(lens_gc)
+    u.update(lens_gausslets=after, lens_points=focus,
+             lens_E=np.asarray(ref.fields.eval_Efield_from_gausslets(lens_gc, focus)),
+             lens_E_t=np.asarray(summ.evaluate(focus.copy(), time_ps=0.7)))
+    # a ray field with lattice neighbours
+    rc = ref.ctracer.RayCollection.from_array(rays.copy())
+    rc.neighbours = nb
+    u.update(rf_rays=rays, rf_neighbours=nb, rf_points=plane,
+             rf_E=np.asarray(ref.fields.eval_Efield_from_rays(rc, plane, wl, blending=1.0)))
+    np.savez_compressed(os.path.join(out_dir, "units_fields.npz"), **u)
+
+
 def lens_case(ref, out_dir):
     """Configuration 4: the perturbed eight-surface lens as an ordinary scene
     (AsphericFace + DielectricMaterial, image plane), 64 rays of the 262,144-ray
@@ -770,5 +856,7 @@ if __name__ == "__main__":
         gausslet_cases(build_ref.load(), HERE)
     elif sys.argv[1:] == ["--capture"]:
         capture_cases(build_ref.load(), HERE)
+    elif sys.argv[1:] == ["--fields"]:
+        field_cases(build_ref.load(), HERE)
     else:
         main()
