@@ -228,11 +228,15 @@ __global__ void __launch_bounds__(RP_BLOCK) gausslet_place_kernel(GaussArgs G) {
         return;
     }
     const unsigned long long src = (unsigned long long)tile * RP_TILE_SLOTS;
-    for (unsigned j = threadIdx.x; j < count; j += RP_BLOCK) copy_ray(A.scratch, src + j, A.out, base + j);
-    for (int f = 0; f < RP_PARA_ARRAYS; f++) {
-        const double *s = G.pscratch + (unsigned long long)f * G.pscratch_cap + src;
-        double *o = G.pout + (unsigned long long)f * G.pout_cap + base;
-        for (unsigned j = threadIdx.x; j < count; j += RP_BLOCK) o[j] = s[j];
+    for (unsigned j = threadIdx.x; j < count; j += RP_BLOCK) {
+        copy_ray(A.scratch, src + j, A.out, base + j);
+        for (int pj = 0; pj < 6; pj++) {  // one parabasal ray's ten fields: loads first, then stores
+            double v[RP_PARA_FIELDS];
+#pragma unroll
+            for (int f = 0; f < RP_PARA_FIELDS; f++) v[f] = para_at(G.pscratch, G.pscratch_cap, pj, f, src + j);
+#pragma unroll
+            for (int f = 0; f < RP_PARA_FIELDS; f++) para_at(G.pout, G.pout_cap, pj, f, base + j) = v[f];
+        }
     }
 }
 

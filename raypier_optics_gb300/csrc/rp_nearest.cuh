@@ -110,17 +110,27 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
     }
 }
 
-// Copies one ray record between structure-of-arrays buffers.
+// Copies one ray record between structure-of-arrays buffers.  All 23 loads
+// are issued before the first store: the compiler cannot tell the two
+// buffers apart, so an interleaved load/store sequence would wait for each
+// load in turn.
 __device__ __forceinline__ void copy_ray(const RaySoA &s, unsigned long long src, const RaySoA &o,
                                          unsigned long long dst) {
-    o.ox[dst] = s.ox[src]; o.oy[dst] = s.oy[src]; o.oz[dst] = s.oz[src];
-    o.dx[dst] = s.dx[src]; o.dy[dst] = s.dy[src]; o.dz[dst] = s.dz[src];
-    o.nx[dst] = s.nx[src]; o.ny[dst] = s.ny[src]; o.nz[dst] = s.nz[src];
-    o.ex[dst] = s.ex[src]; o.ey[dst] = s.ey[src]; o.ez[dst] = s.ez[src];
-    o.n[dst] = s.n[src]; o.e1[dst] = s.e1[src]; o.e2[dst] = s.e2[src];
-    o.len[dst] = s.len[src]; o.phase[dst] = s.phase[src]; o.opl[dst] = s.opl[src];
-    o.wl[dst] = s.wl[src]; o.parent[dst] = s.parent[src]; o.endf[dst] = s.endf[src];
-    o.ident[dst] = s.ident[src]; o.type[dst] = s.type[src];
+    const double ox = s.ox[src], oy = s.oy[src], oz = s.oz[src];
+    const double dx = s.dx[src], dy = s.dy[src], dz = s.dz[src];
+    const double nx = s.nx[src], ny = s.ny[src], nz = s.nz[src];
+    const double ex = s.ex[src], ey = s.ey[src], ez = s.ez[src];
+    const double2 n = s.n[src], e1 = s.e1[src], e2 = s.e2[src];
+    const double len = s.len[src], phase = s.phase[src], opl = s.opl[src];
+    const unsigned wl = s.wl[src], parent = s.parent[src], endf = s.endf[src], ident = s.ident[src],
+                   type = s.type[src];
+    o.ox[dst] = ox; o.oy[dst] = oy; o.oz[dst] = oz;
+    o.dx[dst] = dx; o.dy[dst] = dy; o.dz[dst] = dz;
+    o.nx[dst] = nx; o.ny[dst] = ny; o.nz[dst] = nz;
+    o.ex[dst] = ex; o.ey[dst] = ey; o.ez[dst] = ez;
+    o.n[dst] = n; o.e1[dst] = e1; o.e2[dst] = e2;
+    o.len[dst] = len; o.phase[dst] = phase; o.opl[dst] = opl;
+    o.wl[dst] = wl; o.parent[dst] = parent; o.endf[dst] = endf; o.ident[dst] = ident; o.type[dst] = type;
 }
 
 }  // namespace rp

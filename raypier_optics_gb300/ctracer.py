@@ -22,6 +22,7 @@ calls raise.
 from __future__ import annotations
 
 import math
+import sys
 from typing import Optional
 
 import numpy as np
@@ -931,11 +932,12 @@ class FaceList:
     def sync_transforms(self):
         """Take the owner's transform (a VTK-style matrix) if it has one;
         otherwise keep the preset transforms, as the reference does
-        (ctracer.pyx:1820-1837)."""
+        (ctracer.pyx:1820-1837).  The reference's "NO OWNER" notice goes to
+        stderr here, so that stdout stays machine-readable."""
         try:
             trans = self.owner.transform
         except AttributeError:
-            print("NO OWNER", self.owner)
+            print("NO OWNER", self.owner, file=sys.stderr)
             return
         m = trans.matrix
         rot = [[m.get_element(i, j) for j in range(3)] for i in range(3)]
