@@ -544,12 +544,13 @@ int rp_rays_field(const rp_rays *r, const char *name, void **p) {
 
 // Per-generation scratch: [out_count | err | pad | stats[2] | tile counter | pad], then the
 // per-tile child counts and offsets.
-static size_t scratch_bytes_for(uint64_t n_tiles) {
-    return SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)) + align256(n_tiles * sizeof(unsigned long long));
+static size_t scratch_bytes_for(uint64_t n_sub) {
+    return SCRATCH_HDR + align256(n_sub * sizeof(unsigned)) + align256(n_sub * sizeof(unsigned long long));
 }
 
-static int ensure_scratch(rp_ctx *ctx, uint64_t n_tiles) {
-    size_t need = scratch_bytes_for(n_tiles);
+// Scratch for a generation of n_sub sub-tiles (rp_n_sub of its ray count).
+static int ensure_scratch(rp_ctx *ctx, uint64_t n_sub) {
+    size_t need = scratch_bytes_for(n_sub);
     if (need <= ctx->scratch_bytes) return RP_OK;
     if (ctx->scratch) {
         cudaStreamSynchronize(ctx->stream);
@@ -582,7 +583,8 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
                       int one_list, int one_face, GenArgs &a) {
     uint64_t n_in = in->n;
     uint64_t n_tiles = (n_in + RP_BLOCK - 1) / RP_BLOCK;
-    int rc = ensure_scratch(ctx, n_tiles);
+    const uint64_t n_sub = rp_n_sub(n_in);
+    int rc = ensure_scratch(ctx, n_sub);
     if (rc) return rc;
     if (emit) {
         rc = ensure_arena(ctx, n_tiles);
@@ -608,7 +610,7 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
     a.stats = (unsigned long long *)(sc + 24);
     a.tile_next = (unsigned *)(sc + 40);
     a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
-    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)));
+    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_sub * sizeof(unsigned)));
     a.scratch = emit ? ctx->arena->soa : in->soa;
     a.face_counts = s->face_counts;
     if (ctx->gen_ev.empty()) {
@@ -621,7 +623,7 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
     if (e != cudaSuccess) return cuda_fail(e, "generation kernel launch");
     CK(cudaEventRecord(ctx->gen_ev[1], ctx->stream));
     if (emit) {
-        e = launch_tile_scan(a, (unsigned)n_tiles, ctx->stream);
+        e = launch_tile_scan(a, n_sub, ctx->stream);
         if (e != cudaSuccess) return cuda_fail(e, "tile scan launch");
     }
     CK(cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
@@ -646,6 +648,7 @@ static int finish_gen(rp_ctx *ctx, int emit, rp_stats *st, uint64_t n_in, uint64
         st->generations += 1;
     }
     *count = emit ? cnt : 0;
+
     if (err & ERR_WAVELENGTH) {
         snprintf(g_last_error, sizeof g_last_error, "a ray's wavelength_idx is outside the wavelength table");
         return RP_ERR_INVALID;
@@ -661,7 +664,7 @@ static int finish_gen(rp_ctx *ctx, int emit, rp_stats *st, uint64_t n_in, uint64
 static int place_gen(rp_ctx *ctx, GenArgs &a, rp_rays *out, uint64_t count, rp_stats *st) {
     a.out = out->soa;
     a.out_cap = out->cap;
-    cudaError_t e = launch_place_children(a, (unsigned)((a.n_in + RP_BLOCK - 1) / RP_BLOCK), ctx->stream);
+    cudaError_t e = launch_place_children(a, rp_n_sub(a.n_in), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "child placement launch");
     out->n = count;
     if (st) st->rays_out += count;
@@ -886,7 +889,8 @@ int rp_trace_gausslet_segment(rp_ctx *ctx, rp_scene *s, rp_gausslets *in, rp_gau
         for (uint64_t i = 0; i < n_in; i++) captured[i] = 0;
     if (n_in == 0) return RP_OK;
     const uint64_t n_tiles = (n_in + RP_BLOCK - 1) / RP_BLOCK;
-    int rc = ensure_scratch(ctx, n_tiles);
+    const uint64_t n_sub = rp_n_sub(n_in);
+    int rc = ensure_scratch(ctx, n_sub);
     if (rc == RP_OK) rc = ensure_arena(ctx, n_tiles);
     if (rc) return rc;
     const uint64_t slots = n_tiles * RP_TILE_SLOTS;
@@ -926,7 +930,7 @@ int rp_trace_gausslet_segment(rp_ctx *ctx, rp_scene *s, rp_gausslets *in, rp_gau
     a.stats = (unsigned long long *)(sc + 24);
     a.tile_next = (unsigned *)(sc + 40);
     a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
-    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)));
+    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_sub * sizeof(unsigned)));
     a.scratch = ctx->arena->soa;
     a.face_counts = s->face_counts;
     ga.pin = in->para;
@@ -941,7 +945,7 @@ int rp_trace_gausslet_segment(rp_ctx *ctx, rp_scene *s, rp_gausslets *in, rp_gau
     if (e == cudaSuccess) e = cudaEventRecord(ctx->ev0, ctx->stream);
     if (e == cudaSuccess) e = launch_gausslet_generation(ga, s->smem, ctx->stream);
     if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, ctx->stream);
-    if (e == cudaSuccess) e = launch_tile_scan(a, (unsigned)n_tiles, ctx->stream);
+    if (e == cudaSuccess) e = launch_tile_scan(a, n_sub, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -976,7 +980,7 @@ int rp_trace_gausslet_segment(rp_ctx *ctx, rp_scene *s, rp_gausslets *in, rp_gau
         snprintf(g_last_error, sizeof g_last_error, "%llu child gausslets do not fit the output buffer", count);
         return RP_ERR_CAPACITY;
     }
-    e = launch_gausslet_place(ga, (unsigned)n_tiles, ctx->stream);
+    e = launch_gausslet_place(ga, n_sub, ctx->stream);
     if (e == cudaSuccess && dcap)
         e = cudaMemcpyAsync(captured, dcap, n_in * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1001,7 +1005,8 @@ static int capture_common(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_rays *i
     const uint64_t n_in = in_base->n;
     if (n_in == 0) return RP_OK;
     const uint64_t n_tiles = (n_in + RP_BLOCK - 1) / RP_BLOCK;
-    int rc = ensure_scratch(ctx, n_tiles);
+    const uint64_t n_sub = rp_n_sub(n_in);
+    int rc = ensure_scratch(ctx, n_sub);
     if (rc == RP_OK) rc = ensure_arena(ctx, n_tiles);
     if (rc) return rc;
     const int with_para = pin != nullptr;
@@ -1029,7 +1034,7 @@ static int capture_common(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_rays *i
     a.stats = (unsigned long long *)(sc + 24);
     a.tile_next = (unsigned *)(sc + 40);
     a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
-    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_tiles * sizeof(unsigned)));
+    a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_sub * sizeof(unsigned)));
     a.scratch = ctx->arena->soa;
     a.face_counts = s->face_counts;
     ga.pin = const_cast<double *>(pin);
@@ -1040,7 +1045,7 @@ static int capture_common(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_rays *i
     ga.pout_cap = pout_cap;
     cudaError_t e = cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream);
     if (e == cudaSuccess) e = launch_capture(ga, wl_offset, with_para, s->smem, ctx->stream);
-    if (e == cudaSuccess) e = launch_tile_scan(a, (unsigned)n_tiles, ctx->stream);
+    if (e == cudaSuccess) e = launch_tile_scan(a, n_sub, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_pinned, sc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1060,8 +1065,7 @@ static int capture_common(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_rays *i
         snprintf(g_last_error, sizeof g_last_error, "%llu captured rays do not fit the output buffer", count);
         return RP_ERR_CAPACITY;
     }
-    e = with_para ? launch_gausslet_place(ga, (unsigned)n_tiles, ctx->stream)
-                  : launch_place_children(a, (unsigned)n_tiles, ctx->stream);
+    e = with_para ? launch_gausslet_place(ga, n_sub, ctx->stream) : launch_place_children(a, n_sub, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (pscratch) ctx_free(ctx, pscratch, pbytes);
     if (e != cudaSuccess) return cuda_fail(e, "capture placement");
@@ -1092,14 +1096,15 @@ int rp_select_gausslet_intersections(rp_ctx *ctx, rp_scene *s, int32_t list_idx,
 //   [0, 64)       counters: child total (u64 @0), error bits (u32 @8),
 //                 hits and terminated children (2 x u64 @24), next tile to
 //                 trace (u32 @40) -- zeroed per call
-//   tile_counts   u32 per 128-ray tile
-//   tile_offsets  u64 per tile
+//   tile_counts   u32 per 32-ray sub-tile
+//   tile_offsets  u64 per sub-tile
 //   child slots   2 per ray, structure of arrays (188 bytes per slot)
 #define NA_TILES (RP_NOALLOC_MAX_RAYS / RP_BLOCK)
+#define NA_SUBS (RP_NOALLOC_MAX_RAYS / RP_SUB)
 #define NA_SLOTS ((size_t)NA_TILES * RP_TILE_SLOTS)
 #define NA_OFF_TILE_COUNTS ((size_t)SCRATCH_HDR)
-#define NA_OFF_TILE_OFFSETS (NA_OFF_TILE_COUNTS + (((size_t)NA_TILES * 4 + 255) & ~(size_t)255))
-#define NA_OFF_SLOTS ((NA_OFF_TILE_OFFSETS + (size_t)NA_TILES * 8 + 255) & ~(size_t)255)
+#define NA_OFF_TILE_OFFSETS (NA_OFF_TILE_COUNTS + (((size_t)NA_SUBS * 4 + 255) & ~(size_t)255))
+#define NA_OFF_SLOTS ((NA_OFF_TILE_OFFSETS + (size_t)NA_SUBS * 8 + 255) & ~(size_t)255)
 #define NA_SLOT_BYTES ((size_t)RP_RAY_BYTES * NA_SLOTS)
 #define NA_TOTAL (NA_OFF_SLOTS + NA_SLOT_BYTES)
 #define NA_MAX_DEVICES 64
@@ -1153,7 +1158,7 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     if (rc) return rc;
     out->n = 0;
     if (in->n == 0) return RP_OK;
-    const uint64_t n_tiles = (in->n + RP_BLOCK - 1) / RP_BLOCK;
+    const uint64_t n_sub = rp_n_sub(in->n);
 
     rp_rays slots;  // a view of the slot arena; owns nothing
     memset(&slots, 0, sizeof slots);
@@ -1189,7 +1194,7 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
                                              : launch_generation_plain(a, s->smem, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "generation kernel launch");
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
-    e = launch_tile_scan(a, (unsigned)n_tiles, ctx->stream);
+    e = launch_tile_scan(a, n_sub, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "tile scan launch");
     CK(cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1221,7 +1226,7 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     }
     a.out = out->soa;
     a.out_cap = out->cap;
-    e = launch_place_children(a, (unsigned)n_tiles, ctx->stream);
+    e = launch_place_children(a, n_sub, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "child placement launch");
     CK(cudaStreamSynchronize(ctx->stream));
     out->n = count;

@@ -8,8 +8,8 @@
 // (FaceList.intersect_c, ctracer.pyx:1882-1904).  Rays that meet a face are
 // written, in input order, with that face's distance as length and its index
 // as end_face_idx, and wavelength_idx shifted by the collection's offset into
-// the concatenated wavelength list.  Placement is the generation's: block
-// scan into tile slots, tile scan, coalesced copy.
+// the concatenated wavelength list.  Placement is the generation's: warp
+// scan into sub-tile slots, sub-tile scan, coalesced copy.
 #include "rp_nearest.cuh"
 
 namespace rp {
@@ -43,10 +43,11 @@ __global__ void __launch_bounds__(RP_BLOCK) capture_kernel(GaussArgs G, unsigned
         }
     }
     const unsigned nc = best >= 0 ? 1u : 0u;
-    unsigned tile_n;
-    const unsigned excl = block_scan(nc, &tile_n);
+    unsigned sub_n;
+    const unsigned excl = warp_scan(nc, &sub_n);
+    const unsigned long long qs = sub_tile_of_thread();
     if (nc) {
-        const unsigned long long q = (unsigned long long)tile * RP_TILE_SLOTS + excl;
+        const unsigned long long q = qs * RP_SUB_SLOTS + excl;
         copy_ray(A.in, i, A.scratch, q);
         A.scratch.len[q] = len;
         A.scratch.endf[q] = (unsigned)S.faces[best].idx;
@@ -55,7 +56,7 @@ __global__ void __launch_bounds__(RP_BLOCK) capture_kernel(GaussArgs G, unsigned
             for (int f = 0; f < RP_PARA_ARRAYS; f++)
                 G.pscratch[(unsigned long long)f * G.pscratch_cap + q] = G.pin[(unsigned long long)f * G.pin_cap + i];
     }
-    if (threadIdx.x == 0) A.tile_counts[tile] = tile_n;
+    if ((threadIdx.x & 31) == 0 && qs < rp_n_sub(A.n_in)) A.tile_counts[qs] = sub_n;
 }
 
 static cudaError_t prepare_capture(size_t smem) {

@@ -18,8 +18,9 @@
 //   4. otherwise each child of the base ray becomes a child gausslet: its
 //      parabasal rays start at their hit points and leave in the direction
 //      the material's eval_parabasal_ray_c gives for that child's type.
-// Children are placed as in a ray generation: block scan into the tile's
-// child slots, tile scan, coalesced placement (base rays and parabasal rays).
+// Children are placed as in a ray generation: warp scan into the sub-tile's
+// child slots, sub-tile scan, coalesced placement (base rays and parabasal
+// rays).
 #include <map>
 #include <mutex>
 
@@ -143,8 +144,9 @@ __global__ void __launch_bounds__(RP_BLOCK) gausslet_generation_kernel(GaussArgs
         }
     }
 
-    unsigned tile_children;
-    const unsigned excl = block_scan((unsigned)nc, &tile_children);
+    unsigned sub_children;
+    const unsigned excl = warp_scan((unsigned)nc, &sub_children);
+    const unsigned long long q = sub_tile_of_thread();
     if (nc > 0) {
         const rp_facelist &L = S.lists[best_list];
         const rp_face &F = S.faces[best];
@@ -152,7 +154,7 @@ __global__ void __launch_bounds__(RP_BLOCK) gausslet_generation_kernel(GaussArgs
         double phase = A.in.phase[i];
         unsigned wl = A.in.wl[i], ident = A.in.ident[i];
         unsigned endf = (unsigned)F.idx;
-        const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
+        const unsigned long long slot = q * RP_SUB_SLOTS + excl;
         for (int k = 0; k < nc; k++) {
             Child c = ch[k];
             c.len = A.max_len;  // reset_length_c
@@ -170,27 +172,25 @@ __global__ void __launch_bounds__(RP_BLOCK) gausslet_generation_kernel(GaussArgs
             for (int k = 0; k < nc; k++) {
                 v3 dir, pn;
                 eval_parabasal(S, M, ch[k].n, wl, ch[k].type, pd, nrm, tng, dir, pn, A.err);
-                const unsigned long long q = slot + k;
+                const unsigned long long sk = slot + k;
                 double *P = G.pscratch;
                 const unsigned long long C = G.pscratch_cap;
-                para_at(P, C, j, 0, q) = pt.x;
-                para_at(P, C, j, 1, q) = pt.y;
-                para_at(P, C, j, 2, q) = pt.z;
-                para_at(P, C, j, 3, q) = dir.x;
-                para_at(P, C, j, 4, q) = dir.y;
-                para_at(P, C, j, 5, q) = dir.z;
-                para_at(P, C, j, 6, q) = pn.x;
-                para_at(P, C, j, 7, q) = pn.y;
-                para_at(P, C, j, 8, q) = pn.z;
-                para_at(P, C, j, 9, q) = A.max_len;  // reset_length_c
+                para_at(P, C, j, 0, sk) = pt.x;
+                para_at(P, C, j, 1, sk) = pt.y;
+                para_at(P, C, j, 2, sk) = pt.z;
+                para_at(P, C, j, 3, sk) = dir.x;
+                para_at(P, C, j, 4, sk) = dir.y;
+                para_at(P, C, j, 5, sk) = dir.z;
+                para_at(P, C, j, 6, sk) = pn.x;
+                para_at(P, C, j, 7, sk) = pn.y;
+                para_at(P, C, j, 8, sk) = pn.z;
+                para_at(P, C, j, 9, sk) = A.max_len;  // reset_length_c
             }
         }
     }
+    if ((threadIdx.x & 31) == 0 && q < rp_n_sub(A.n_in)) A.tile_counts[q] = sub_children;
     flush_counts(A, S, s_counts);
-    if (threadIdx.x == 0) {
-        A.tile_counts[tile] = tile_children;
-        atomicAdd(&A.stats[0], (unsigned long long)s_hits);
-    }
+    if (threadIdx.x == 0) atomicAdd(&A.stats[0], (unsigned long long)s_hits);
 }
 
 static cudaError_t prepare_gausslet(size_t smem) {
@@ -216,19 +216,21 @@ cudaError_t launch_gausslet_generation(const GaussArgs &a, size_t smem, cudaStre
     return cudaGetLastError();
 }
 
-// Moves each tile's child gausslets (base ray and parabasal rays) to their
-// final place, as place_children_kernel does for rays.
-__global__ void __launch_bounds__(RP_BLOCK) gausslet_place_kernel(GaussArgs G) {
+// Moves each sub-tile's child gausslets (base ray and parabasal rays) to
+// their final place, as place_children_kernel does for rays.
+__global__ void __launch_bounds__(RP_BLOCK) gausslet_place_kernel(GaussArgs G, unsigned long long n_sub) {
     const GenArgs &A = G.g;
-    const unsigned tile = blockIdx.x;
-    const unsigned count = A.tile_counts[tile];
-    const unsigned long long base = A.tile_offsets[tile];
-    if (count > RP_TILE_SLOTS || base + count > A.out_cap || base + count > G.pout_cap) {
-        if (threadIdx.x == 0) atomicOr(A.err, ERR_OVERFLOW);
+    const unsigned long long q = sub_tile_of_thread();
+    if (q >= n_sub) return;
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned count = A.tile_counts[q];
+    const unsigned long long base = A.tile_offsets[q];
+    if (count > RP_SUB_SLOTS || base + count > A.out_cap || base + count > G.pout_cap) {
+        if (lane == 0) atomicOr(A.err, ERR_OVERFLOW);
         return;
     }
-    const unsigned long long src = (unsigned long long)tile * RP_TILE_SLOTS;
-    for (unsigned j = threadIdx.x; j < count; j += RP_BLOCK) {
+    const unsigned long long src = q * RP_SUB_SLOTS;
+    for (unsigned j = lane; j < count; j += RP_SUB) {
         copy_ray(A.scratch, src + j, A.out, base + j);
         for (int pj = 0; pj < 6; pj++) {  // one parabasal ray's ten fields: loads first, then stores
             double v[RP_PARA_FIELDS];
@@ -240,9 +242,10 @@ __global__ void __launch_bounds__(RP_BLOCK) gausslet_place_kernel(GaussArgs G) {
     }
 }
 
-cudaError_t launch_gausslet_place(const GaussArgs &a, unsigned n_tiles, cudaStream_t st) {
-    if (n_tiles == 0) return cudaSuccess;
-    gausslet_place_kernel<<<n_tiles, RP_BLOCK, 0, st>>>(a);
+cudaError_t launch_gausslet_place(const GaussArgs &a, unsigned long long n_sub, cudaStream_t st) {
+    if (n_sub == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)((n_sub + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK);
+    gausslet_place_kernel<<<grid, RP_BLOCK, 0, st>>>(a, n_sub);
     return cudaGetLastError();
 }
 

@@ -5,11 +5,12 @@
 // Ordering contract (the reference's RayCollection.add_ray_c append order,
 // raypier/core/ctracer.pyx:1004-1012 driven by trace_segment_c 2083-2117):
 // children are stored in ascending parent index, and a parent's children in
-// emission order (reflected before transmitted).  A tile of rays writes its
-// children, in that order, to its own slot range of a scratch arena and
-// publishes their count; a scan of the counts then gives every tile its final
-// offset and a copy kernel places the children (rp_trace.cu).  Tiles never wait
-// for one another, so a tile with slow rays does not hold up the others.
+// emission order (reflected before transmitted).  A sub-tile of 32 rays (one
+// warp) writes its children, in that order, to its own slot range of a
+// scratch arena and publishes their count; a scan of the counts then gives
+// every sub-tile its final offset and a copy kernel places the children
+// (rp_trace.cu).  Warps never wait for one another, so a warp with slow rays
+// does not hold up the others.
 #pragma once
 #include "rp_kernels.cuh"
 
@@ -80,6 +81,26 @@ __device__ __forceinline__ unsigned block_scan(unsigned c, unsigned *total_out) 
     unsigned before = (warp > 0) ? s_warp[warp - 1] : 0u;
     *total_out = s_warp[RP_BLOCK / 32 - 1];
     return before + (v - c);
+}
+
+// Exclusive scan of `c` over the warp; *total_out gets the warp total.  Must
+// be called by all 32 lanes.
+__device__ __forceinline__ unsigned warp_scan(unsigned c, unsigned *total_out) {
+    const unsigned lane = threadIdx.x & 31;
+    unsigned v = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (unsigned)o) v += t;
+    }
+    *total_out = __shfl_sync(0xffffffffu, v, 31);
+    return v - c;
+}
+
+// Sub-tile (warp) index and its first slot for a kernel that runs one thread
+// per ray with blockIdx.x * RP_BLOCK + threadIdx.x as the ray index.
+__device__ __forceinline__ unsigned long long sub_tile_of_thread() {
+    return ((unsigned long long)blockIdx.x * RP_BLOCK + threadIdx.x) / RP_SUB;
 }
 
 // Writes one child record at slot k of `out`.

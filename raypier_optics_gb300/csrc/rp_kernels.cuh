@@ -17,14 +17,20 @@ struct RaySoA {
     unsigned *wl, *parent, *endf, *ident, *type;
 };
 
-// A tile of RP_BLOCK rays owns RP_TILE_SLOTS consecutive slots of a scratch
-// ray arena (two per ray).  The generation kernel writes the tile's children
-// to the front of that range in parent order (block scan of the per-ray
-// counts) and their number to tile_counts[tile]; once every tile's total is
-// known (tile scan) the placement kernel copies each tile's children to their
-// final, contiguous place.  No ray or tile waits for another.
+// Child placement works on sub-tiles of RP_SUB rays (one warp): sub-tile q
+// owns RP_SUB_SLOTS consecutive slots of a scratch ray arena (two per ray).
+// The generation kernel writes the sub-tile's children to the front of that
+// range in parent order (warp scan of the per-ray counts) and their number to
+// tile_counts[q]; once every sub-tile's total is known (tile scan) the
+// placement kernel copies each sub-tile's children to their final, contiguous
+// place.  No ray, warp or block waits for another.  Blocks are RP_BLOCK
+// threads, so a block covers RP_BLOCK / RP_SUB sub-tiles (RP_TILE_SLOTS slots).
 #define RP_BLOCK 128
 #define RP_TILE_SLOTS (2 * RP_BLOCK)
+#define RP_SUB 32
+#define RP_SUB_SLOTS (2 * RP_SUB)
+#define RP_SUB_PER_BLOCK (RP_BLOCK / RP_SUB)
+__host__ __device__ inline unsigned long long rp_n_sub(unsigned long long n_rays) { return (n_rays + RP_SUB - 1) / RP_SUB; }
 
 struct GenArgs {
     RaySoA in, out;
@@ -38,13 +44,13 @@ struct GenArgs {
     int smem_tables;              // 1: lists/faces/materials staged in shared memory
     int mixed_fallback;           // mixed kernel: the scene has faces / materials only its FP64 code handles
     RaySoA scratch;                 // child slots: RP_TILE_SLOTS per tile
-    unsigned *tile_counts;          // [n_tiles] children of each tile
-    unsigned long long *tile_offsets;  // [n_tiles] exclusive prefix (scan kernel)
+    unsigned *tile_counts;          // [n_sub] children of each sub-tile
+    unsigned long long *tile_offsets;  // [n_sub] exclusive prefix (scan kernel)
     unsigned long long *out_count;  // total children (scan kernel)
     unsigned *err;                  // error bits
     unsigned *face_counts;          // per face record hit counters
     unsigned long long *stats;      // [0] hits, [1] terminated children
-    unsigned *tile_next;            // next tile to trace (kernels that loop over tiles; zeroed per launch)
+    unsigned *tile_next;            // next sub-tile to trace (kernels that loop over them; zeroed per launch)
 };
 
 // launchers (rp_trace.cu / rp_mixed.cu); return cudaError_t
@@ -54,9 +60,10 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
 // launch of the same configuration can be stream-captured
 cudaError_t prepare_generation_plain(const GenArgs &a, size_t smem);
 cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem);
-// tile-count scan (one block) and the scatter of children to their final slots
-cudaError_t launch_tile_scan(const GenArgs &a, unsigned n_tiles, cudaStream_t st);
-cudaError_t launch_place_children(const GenArgs &a, unsigned n_tiles, cudaStream_t st);
+// sub-tile count scan (one block) and the scatter of children to their final
+// slots (one block per RP_SUB_PER_BLOCK sub-tiles)
+cudaError_t launch_tile_scan(const GenArgs &a, unsigned long long n_sub, cudaStream_t st);
+cudaError_t launch_place_children(const GenArgs &a, unsigned long long n_sub, cudaStream_t st);
 cudaError_t launch_aos_to_soa(const void *aos, RaySoA soa, unsigned long long n, cudaStream_t st);
 cudaError_t launch_soa_to_aos(RaySoA soa, void *aos, unsigned long long n, cudaStream_t st);
 cudaError_t launch_dispersion_table(const rp_dispersion *curves, int n_curves, const double *aux,
@@ -79,7 +86,7 @@ struct GaussArgs {
     int *captured;                   // [n_in] 1 + material of a decomposition material that captured it (or null)
 };
 cudaError_t launch_gausslet_generation(const GaussArgs &a, size_t smem, cudaStream_t st);
-cudaError_t launch_gausslet_place(const GaussArgs &a, unsigned n_tiles, cudaStream_t st);
+cudaError_t launch_gausslet_place(const GaussArgs &a, unsigned long long n_sub, cudaStream_t st);
 cudaError_t launch_capture(const GaussArgs &a, unsigned wl_offset, int with_para, size_t smem, cudaStream_t st);
 cudaError_t launch_gausslet_aos_to_soa(const void *aos, RaySoA soa, double *para, unsigned long long cap,
                                        unsigned long long n, cudaStream_t st);

@@ -530,6 +530,7 @@ __device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const
                     }
                 }
                 if (!conv || !isfinite(tf)) return miss_t();
+                if (tf > fmaf(tmax, 1.0001f, 1e-3f)) return miss_t();  // beyond the bound: no correction needed
                 tt = ffm(tf, 0.0f);
                 {  // one correction at the float-float point (the FP32 iterate is within ~1e-3 mm)
                     f3 u = vertex_point(R, zv, tt);
@@ -872,7 +873,10 @@ __device__ __forceinline__ void try_face(const DevScene &S, const MxList *ml, co
         cur = l;
     }
     bool fb;
-    ff t = face_t(S, S.faces[f], mf[f], R, tmax, err, fb);
+    // a face whose FP32 root lies beyond the nearest hit so far (with a margin
+    // far above the FP32 root error) cannot win: skip its refinement
+    const float tl = b.face >= 0 ? fminf(tmax, fmaf(b.t.hi, 1.0009765625f, 1e-3f)) : tmax;
+    ff t = face_t(S, S.faces[f], mf[f], R, tl, err, fb);
     if (t.hi < 0.0f) return;
     ff dist = ff_mul(t, dlen);
     if (!(mf[f].tol < dist.hi)) return;
@@ -895,12 +899,13 @@ __device__ __noinline__ void try_face_fp64(const GenArgs &A, const DevScene &S, 
 // thread).  Each thread copies its own ray's fields with cp.async, so a tile's
 // loads are in flight while the previous tile computes, and a thread waits
 // only for its own copies (cp.async.wait_group).
+// The input fields of one sub-tile (32 rays, one warp).
 struct TileIn {
-    double ox[RP_BLOCK], oy[RP_BLOCK], oz[RP_BLOCK], dx[RP_BLOCK], dy[RP_BLOCK], dz[RP_BLOCK];
-    double ex[RP_BLOCK], ey[RP_BLOCK], ez[RP_BLOCK];
-    double2 n[RP_BLOCK], e1[RP_BLOCK], e2[RP_BLOCK];
-    double opl[RP_BLOCK], phase[RP_BLOCK];
-    unsigned wl[RP_BLOCK], type[RP_BLOCK], ident[RP_BLOCK], pad[RP_BLOCK];
+    double ox[RP_SUB], oy[RP_SUB], oz[RP_SUB], dx[RP_SUB], dy[RP_SUB], dz[RP_SUB];
+    double ex[RP_SUB], ey[RP_SUB], ez[RP_SUB];
+    double2 n[RP_SUB], e1[RP_SUB], e2[RP_SUB];
+    double opl[RP_SUB], phase[RP_SUB];
+    unsigned wl[RP_SUB], type[RP_SUB], ident[RP_SUB], pad[RP_SUB];
 };
 
 __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
@@ -921,11 +926,11 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
-// Queues the copy of ray i's fields into slot threadIdx.x of `buf` (nothing
+// Queues the copy of ray i's fields into the lane's slot of `buf` (nothing
 // for i beyond the generation) and closes the thread's copy group.
 __device__ __forceinline__ void prefetch_ray(TileIn *buf, const RaySoA &in, unsigned long long i, unsigned long long n) {
     if (i < n) {
-        const unsigned t = threadIdx.x;
+        const unsigned t = threadIdx.x & 31;
         cp_async8(&buf->ox[t], &in.ox[i]);
         cp_async8(&buf->oy[t], &in.oy[i]);
         cp_async8(&buf->oz[t], &in.oz[i]);
@@ -966,9 +971,10 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
     return fmaxf(tmin, 0.0f);
 }
 
-// One block stages the tables once and then traces tiles of RP_BLOCK rays
-// taken from a launch-wide counter until none are left, so the staging is paid
-// once per resident block and slow tiles do not hold up a static share.
+// One block stages the tables once; then each of its warps traces sub-tiles
+// of 32 rays taken from a launch-wide counter until none are left, with no
+// barrier between warps, so the staging is paid once per resident block and
+// neither a slow sub-tile nor a slow warp holds up the others.
 // Dynamic shared memory: the plain kernel's tables, the mixed tables at mx_off
 // and, at tb_off, each thread's box-entry distance per culled face.
 template <bool FB>
@@ -976,8 +982,10 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
                                                                       unsigned in_off) {
     using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ unsigned s_hits, s_term, s_tile;
-    TileIn *bufs = reinterpret_cast<TileIn *>(smem + in_off);  // two tiles, double-buffered
+    __shared__ unsigned s_hits, s_term;
+    const unsigned lane = threadIdx.x & 31;
+    // this warp's two sub-tile input buffers (double-buffered)
+    TileIn *bufs = reinterpret_cast<TileIn *>(smem + in_off) + 2 * (threadIdx.x >> 5);
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
     MxList *ml = reinterpret_cast<MxList *>(smem + mx_off);
@@ -989,29 +997,30 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
         s_hits = 0;
         s_term = 0;
     }
-    const unsigned long long n_tiles = (A.n_in + RP_BLOCK - 1) / RP_BLOCK;
+    const unsigned long long n_sub = rp_n_sub(A.n_in);
     const float e2t = f_of_d(A.e2_term);
+    __syncthreads();  // the staged tables and the counters are ready
 
-    // tiles come from a launch-wide counter; the next tile's inputs are copied
-    // into the other buffer while this one is traced
-    if (threadIdx.x == 0) s_tile = atomicAdd(A.tile_next, 1u);
-    __syncthreads();
-    unsigned tile = s_tile;
-    if (tile < n_tiles) prefetch_ray(&bufs[0], A.in, (unsigned long long)tile * RP_BLOCK + threadIdx.x, A.n_in);
+    // every warp takes sub-tiles from a launch-wide counter on its own; the
+    // next sub-tile's inputs are copied into the warp's other buffer while
+    // this one is traced (each lane copies and reads only its own slot)
+    unsigned tile = 0;
+    if (lane == 0) tile = atomicAdd(A.tile_next, 1u);
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    if (tile < n_sub) prefetch_ray(&bufs[0], A.in, (unsigned long long)tile * RP_SUB + lane, A.n_in);
     for (unsigned k = 0;; k++) {
-        if (tile >= n_tiles) break;
-        __syncthreads();  // every thread has read s_tile and finished the previous tile's scan
-        if (threadIdx.x == 0) s_tile = atomicAdd(A.tile_next, 1u);
-        __syncthreads();
-        const unsigned next = s_tile;
-        if (next < n_tiles)
-            prefetch_ray(&bufs[(k + 1) & 1], A.in, (unsigned long long)next * RP_BLOCK + threadIdx.x, A.n_in);
+        if (tile >= n_sub) break;
+        unsigned next = 0;
+        if (lane == 0) next = atomicAdd(A.tile_next, 1u);
+        next = __shfl_sync(0xffffffffu, next, 0);
+        if (next < n_sub)
+            prefetch_ray(&bufs[(k + 1) & 1], A.in, (unsigned long long)next * RP_SUB + lane, A.n_in);
         else
             cp_async_commit();
         cp_async_wait_prev();  // this thread's copies for `tile` have landed
         const TileIn &in = bufs[k & 1];
-        const unsigned t = threadIdx.x;
-        const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
+        const unsigned t = lane;
+        const unsigned long long i = (unsigned long long)tile * RP_SUB + lane;
         const bool active = i < A.n_in;
 
         Best b;
@@ -1198,15 +1207,15 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
                 }
             }
         }
-        // children go to the tile's slot range in parent order: the exclusive
-        // block scan of the per-ray counts is each ray's first slot
-        unsigned tile_children;
-        const unsigned excl = block_scan((unsigned)nc, &tile_children);
+        // children go to the sub-tile's slot range in parent order: the
+        // exclusive warp scan of the per-ray counts is each ray's first slot
+        unsigned sub_children;
+        const unsigned excl = warp_scan((unsigned)nc, &sub_children);
         if (nc > 0) {
             const double phase = in.phase[t];
             const unsigned wl = in.wl[t], ident = in.ident[t];
             const unsigned endf = (unsigned)S.faces[b.face].idx;
-            const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
+            const unsigned long long slot = (unsigned long long)tile * RP_SUB_SLOTS + excl;
             for (int k = 0; k < nc; k++) {
                 if (FB && fp64_children)
                     store_child(A.scratch, slot + k, ccd, chd[k], phase, wl, (unsigned)i, endf, ident);
@@ -1215,7 +1224,7 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
                                   ident);
             }
         }
-        if (threadIdx.x == 0) A.tile_counts[tile] = tile_children;
+        if (lane == 0) A.tile_counts[tile] = sub_children;
         tile = next;
     }
     flush_counts(A, S, s_counts);
@@ -1262,7 +1271,11 @@ static size_t mixed_smem_total(const GenArgs &a, size_t smem, size_t *mx_off, si
     *tb_off = *mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
     const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
     *in_off = (*tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
-    return *in_off + 2 * sizeof(mx::TileIn);
+    return *in_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
+}
+
+static cudaError_t mixed_blocks(const GenArgs &a, size_t total, int *blocks) {
+    return a.mixed_fallback ? mixed_grid_blocks<true>(total, blocks) : mixed_grid_blocks<false>(total, blocks);
 }
 
 // Runs the one-time per-size set-up of the launch (attribute, occupancy) so
@@ -1273,7 +1286,7 @@ cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem) {
     const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off);
     if (total > 220 * 1024) return cudaErrorInvalidConfiguration;
     int blocks = 0;
-    return a.mixed_fallback ? mixed_grid_blocks<true>(total, &blocks) : mixed_grid_blocks<false>(total, &blocks);
+    return mixed_blocks(a, total, &blocks);
 }
 
 // The scene's faces and materials decide the instantiation: without FP64
@@ -1284,16 +1297,15 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
     const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off);
     if (total > 220 * 1024) return cudaErrorInvalidConfiguration;  // scene too large for the per-block tables
     int blocks = 0;
-    cudaError_t e = a.mixed_fallback ? mixed_grid_blocks<true>(total, &blocks) : mixed_grid_blocks<false>(total, &blocks);
+    cudaError_t e = mixed_blocks(a, total, &blocks);
     if (e != cudaSuccess) return e;
     const unsigned long long n_tiles = (a.n_in + RP_BLOCK - 1) / RP_BLOCK;
     const unsigned grid = (unsigned)(n_tiles < (unsigned long long)blocks ? n_tiles : blocks);
+    const unsigned o1 = (unsigned)mx_off, o2 = (unsigned)tb_off, o3 = (unsigned)in_off;
     if (a.mixed_fallback)
-        generation_mixed_kernel<true><<<grid, RP_BLOCK, total, st>>>(a, (unsigned)mx_off, (unsigned)tb_off,
-                                                                     (unsigned)in_off);
+        generation_mixed_kernel<true><<<grid, RP_BLOCK, total, st>>>(a, o1, o2, o3);
     else
-        generation_mixed_kernel<false><<<grid, RP_BLOCK, total, st>>>(a, (unsigned)mx_off, (unsigned)tb_off,
-                                                                      (unsigned)in_off);
+        generation_mixed_kernel<false><<<grid, RP_BLOCK, total, st>>>(a, o1, o2, o3);
     return cudaGetLastError();
 }
 

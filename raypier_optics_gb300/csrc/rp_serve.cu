@@ -227,7 +227,8 @@ uint64_t job_estimate(const Job *j) {
 
 int lane_scratch(Lane *L, uint64_t n_tiles) {
     const size_t nb_tally = (size_t)((n_tiles * RP_BLOCK + RP_TALLY_BLOCK - 1) / RP_TALLY_BLOCK);
-    const size_t need = 64 + align256s(n_tiles * 4) + align256s(n_tiles * 8) + align256s(nb_tally * RP_TALLY_N * 8);
+    const uint64_t n_sub = n_tiles * RP_SUB_PER_BLOCK;  // count entries are per 32-ray sub-tile
+    const size_t need = 64 + align256s(n_sub * 4) + align256s(n_sub * 8) + align256s(nb_tally * RP_TALLY_N * 8);
     if (need <= L->scratch_bytes) return RP_OK;
     if (L->scratch) {
         cudaStreamSynchronize(L->ctx->stream);
@@ -280,9 +281,10 @@ int run_generation(Lane *L, rp_scene *sc, rp_rays *in, rp_rays *out, const Job *
     a.err = (unsigned *)(sc0 + 8);
     a.stats = (unsigned long long *)(sc0 + 24);
     a.tile_next = (unsigned *)(sc0 + 40);
+    const uint64_t n_sub = n_tiles * RP_SUB_PER_BLOCK;
     a.tile_counts = (unsigned *)(sc0 + 64);
-    a.tile_offsets = (unsigned long long *)(sc0 + 64 + align256s(n_tiles * 4));
-    double *partials = (double *)(sc0 + 64 + align256s(n_tiles * 4) + align256s(n_tiles * 8));
+    a.tile_offsets = (unsigned long long *)(sc0 + 64 + align256s(n_sub * 4));
+    double *partials = (double *)(sc0 + 64 + align256s(n_sub * 4) + align256s(n_sub * 8));
     a.scratch = emit ? L->arena->soa : in->soa;
     a.face_counts = sc->face_counts;
     const bool mixed = (j->flags & RP_TRACE_MIXED) != 0;
@@ -296,8 +298,8 @@ int run_generation(Lane *L, rp_scene *sc, rp_rays *in, rp_rays *out, const Job *
     if (e != cudaSuccess) return rp__cuda_fail(e, "cudaStreamBeginCapture");
     cudaError_t ce = cudaMemsetAsync(sc0, 0, 64, st);
     if (ce == cudaSuccess) ce = mixed ? launch_generation_mixed(a, sc->smem, st) : launch_generation_plain(a, sc->smem, st);
-    if (ce == cudaSuccess && emit) ce = launch_tile_scan(a, (unsigned)n_tiles, st);
-    if (ce == cudaSuccess && emit) ce = launch_place_children(a, (unsigned)n_tiles, st);
+    if (ce == cudaSuccess && emit) ce = launch_tile_scan(a, rp_n_sub(n), st);
+    if (ce == cudaSuccess && emit) ce = launch_place_children(a, rp_n_sub(n), st);
     if (ce == cudaSuccess && j->detector >= 0) {
         tally_kernel<<<nb_tally, RP_TALLY_BLOCK, 0, st>>>(in->soa, n, (unsigned)j->detector, partials);
         tally_finish_kernel<<<1, 32, 0, st>>>(partials, nb_tally, L->acc);

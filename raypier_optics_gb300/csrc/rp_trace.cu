@@ -114,19 +114,20 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
         }
     }
 
-    // children go to the tile's slot range in parent order: the exclusive
-    // block scan of the per-ray counts is each ray's first slot
-    unsigned tile_children;
-    const unsigned excl = block_scan((unsigned)nc, &tile_children);
+    // children go to the warp's slot range in parent order: the exclusive
+    // warp scan of the per-ray counts is each ray's first slot
+    unsigned sub_children;
+    const unsigned excl = warp_scan((unsigned)nc, &sub_children);
+    const unsigned long long q = sub_tile_of_thread();
     if (nc > 0) {
         double phase = A.in.phase[i];
         unsigned wl = A.in.wl[i], ident = A.in.ident[i];
         unsigned endf = (unsigned)S.faces[best].idx;
-        const unsigned long long slot = (unsigned long long)tile * RP_TILE_SLOTS + excl;
+        const unsigned long long slot = q * RP_SUB_SLOTS + excl;
         for (int k = 0; k < nc; k++) store_child(A.scratch, slot + k, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
     }
+    if ((threadIdx.x & 31) == 0 && q < rp_n_sub(A.n_in)) A.tile_counts[q] = sub_children;
     flush_counts(A, S, s_counts);
-    if (threadIdx.x == 0) A.tile_counts[tile] = tile_children;
     if (threadIdx.x == 0) {
         atomicAdd(&A.stats[0], (unsigned long long)s_hits);
         if (s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
@@ -167,55 +168,82 @@ cudaError_t prepare_generation_plain(const GenArgs &a, size_t smem) {
 }
 
 // ---- child placement ------------------------------------------------------
-// One block scans the per-tile child counts (exclusive prefix + total).
-__global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *counts, unsigned n_tiles,
+// One block scans the per-sub-tile child counts (exclusive prefix + total):
+// each pass covers 1024 threads x RP_SCAN_PER consecutive counts.
+#define RP_SCAN_PER 8
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *counts, unsigned long long n,
                                                          unsigned long long *offsets, unsigned long long *total) {
-    __shared__ unsigned long long s_part[1024];
+    __shared__ unsigned long long s_warp[32];
     __shared__ unsigned long long s_carry;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_carry = 0;
     __syncthreads();
-    for (unsigned base = 0; base < n_tiles; base += 1024) {
-        unsigned i = base + threadIdx.x;
-        unsigned long long v = i < n_tiles ? counts[i] : 0;
-        s_part[threadIdx.x] = v;
-        __syncthreads();
-        for (unsigned o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
-            unsigned long long t = threadIdx.x >= o ? s_part[threadIdx.x - o] : 0;
-            __syncthreads();
-            s_part[threadIdx.x] += t;
-            __syncthreads();
+    for (unsigned long long base = 0; base < n; base += 1024ull * RP_SCAN_PER) {
+        const unsigned long long i0 = base + (unsigned long long)threadIdx.x * RP_SCAN_PER;
+        unsigned v[RP_SCAN_PER];
+        unsigned long long sum = 0;
+#pragma unroll
+        for (int k = 0; k < RP_SCAN_PER; k++) {
+            v[k] = (i0 + k < n) ? counts[i0 + k] : 0u;
+            sum += v[k];
         }
-        if (i < n_tiles) offsets[i] = s_carry + s_part[threadIdx.x] - v;
+        unsigned long long x = sum;  // inclusive warp scan of the per-thread sums
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long t = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (unsigned)o) x += t;
+        }
+        if (lane == 31) s_warp[warp] = x;
         __syncthreads();
-        if (threadIdx.x == 0) s_carry += s_part[1023];
+        if (warp == 0) {
+            unsigned long long w = s_warp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= (unsigned)o) w += t;
+            }
+            s_warp[lane] = w;  // inclusive prefixes of the warp totals
+        }
+        __syncthreads();
+        unsigned long long excl = s_carry + (warp ? s_warp[warp - 1] : 0ull) + (x - sum);
+#pragma unroll
+        for (int k = 0; k < RP_SCAN_PER; k++) {
+            if (i0 + k < n) offsets[i0 + k] = excl;
+            excl += v[k];
+        }
+        __syncthreads();  // everyone has read s_carry and s_warp
+        if (threadIdx.x == 0) s_carry += s_warp[31];
         __syncthreads();
     }
     if (threadIdx.x == 0) *total = s_carry;
 }
 
-cudaError_t launch_tile_scan(const GenArgs &a, unsigned n_tiles, cudaStream_t st) {
-    tile_scan_kernel<<<1, 1024, 0, st>>>(a.tile_counts, n_tiles, a.tile_offsets, a.out_count);
+cudaError_t launch_tile_scan(const GenArgs &a, unsigned long long n_sub, cudaStream_t st) {
+    tile_scan_kernel<<<1, 1024, 0, st>>>(a.tile_counts, n_sub, a.tile_offsets, a.out_count);
     return cudaGetLastError();
 }
 
-// Moves each tile's children from the front of its slot range to their final
-// place: one block per tile, a straight coalesced copy of tile_counts[tile]
-// records to tile_offsets[tile].
-__global__ void __launch_bounds__(RP_BLOCK) place_children_kernel(GenArgs A) {
-    const unsigned tile = blockIdx.x;
-    const unsigned count = A.tile_counts[tile];
-    const unsigned long long base = A.tile_offsets[tile];
-    if (count > RP_TILE_SLOTS || base + count > A.out_cap) {
-        if (threadIdx.x == 0) atomicOr(A.err, ERR_OVERFLOW);
+// Moves each sub-tile's children from the front of its slot range to their
+// final place: one warp per sub-tile, a straight coalesced copy of
+// tile_counts[q] records to tile_offsets[q].
+__global__ void __launch_bounds__(RP_BLOCK) place_children_kernel(GenArgs A, unsigned long long n_sub) {
+    const unsigned long long q = sub_tile_of_thread();
+    if (q >= n_sub) return;
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned count = A.tile_counts[q];
+    const unsigned long long base = A.tile_offsets[q];
+    if (count > RP_SUB_SLOTS || base + count > A.out_cap) {
+        if (lane == 0) atomicOr(A.err, ERR_OVERFLOW);
         return;
     }
-    const unsigned long long src = (unsigned long long)tile * RP_TILE_SLOTS;
-    for (unsigned j = threadIdx.x; j < count; j += RP_BLOCK) copy_ray(A.scratch, src + j, A.out, base + j);
+    const unsigned long long src = q * RP_SUB_SLOTS;
+    for (unsigned j = lane; j < count; j += RP_SUB) copy_ray(A.scratch, src + j, A.out, base + j);
 }
 
-cudaError_t launch_place_children(const GenArgs &a, unsigned n_tiles, cudaStream_t st) {
-    if (n_tiles == 0) return cudaSuccess;
-    place_children_kernel<<<n_tiles, RP_BLOCK, 0, st>>>(a);
+cudaError_t launch_place_children(const GenArgs &a, unsigned long long n_sub, cudaStream_t st) {
+    if (n_sub == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)((n_sub + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK);
+    place_children_kernel<<<grid, RP_BLOCK, 0, st>>>(a, n_sub);
     return cudaGetLastError();
 }
 
