@@ -145,6 +145,7 @@ int rp_ctx_destroy(rp_ctx *c) {
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     cudaEventDestroy(c->ev0);
     cudaEventDestroy(c->ev1);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     cudaStreamDestroy(c->stream);
     delete c;
     return RP_OK;
@@ -476,9 +477,21 @@ int rp_rays_capacity(const rp_rays *r, uint64_t *cap) {
     return RP_OK;
 }
 
-// Host AoS <-> device SoA goes through a device staging buffer of packed
-// records (one cudaMemcpyAsync) and the layout kernels.
+// Host AoS <-> device SoA: when the host buffer is page-locked (and so mapped
+// into the device's address space) the layout kernel reads or writes it
+// directly across the host link; otherwise the records go through a device
+// staging buffer and one cudaMemcpyAsync.
 static int with_staging(rp_ctx *ctx, size_t bytes, void **p, size_t *got) { return ctx_alloc(ctx, p, bytes, got); }
+
+// The device address of page-locked host memory at `p`, or null.
+static void *mapped_host_ptr(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
 
 int rp_rays_upload_aos(rp_rays *r, const void *records, uint64_t n) {
     if (!r || (n && !records)) return RP_ERR_INVALID;
@@ -487,6 +500,13 @@ int rp_rays_upload_aos(rp_rays *r, const void *records, uint64_t n) {
     CK(cudaSetDevice(ctx->device));
     void *stage = nullptr;
     size_t bytes = (size_t)n * RP_RAY_BYTES, got = 0;
+    if (void *mapped = n ? mapped_host_ptr(records) : nullptr) {
+        cudaError_t e = launch_aos_to_soa(mapped, r->soa, n, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "rp_rays_upload_aos");
+        r->n = n;
+        return RP_OK;
+    }
     if (n) {
         int rc = with_staging(ctx, bytes, &stage, &got);
         if (rc) return rc;
@@ -506,6 +526,12 @@ int rp_rays_download_aos(const rp_rays *r, void *records, uint64_t n) {
     rp_ctx *ctx = r->ctx;
     CK(cudaSetDevice(ctx->device));
     if (!n) return RP_OK;
+    if (void *mapped = mapped_host_ptr(records)) {
+        cudaError_t e = launch_soa_to_aos(r->soa, mapped, n, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "rp_rays_download_aos");
+        return RP_OK;
+    }
     void *stage = nullptr;
     size_t bytes = (size_t)n * RP_RAY_BYTES, got = 0;
     int rc = with_staging(ctx, bytes, &stage, &got);
@@ -717,9 +743,13 @@ int rp_trace_one_face_segment(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *ou
     return one_generation(ctx, s, in, out, max_length, flags, e2, list_idx, face_idx, st);
 }
 
-int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, int32_t recursion_limit,
-                  float max_length, uint32_t flags, double e2, int32_t *n_gens, rp_stats *st) {
-    if (!ctx || !s || !gens || !gens[0] || max_gens < 1 || !n_gens || s->ctx != ctx) return RP_ERR_INVALID;
+// Called once generation g's records are final (its kernel has run and the
+// main stream is synchronised); a non-zero return ends the trace.
+typedef int (*gen_done_fn)(void *user, int g, rp_rays *rays);
+
+static int trace_rays_impl(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, int32_t recursion_limit,
+                           float max_length, uint32_t flags, double e2, int32_t *n_gens, rp_stats *st,
+                           gen_done_fn done, void *user) {
     CK(cudaSetDevice(ctx->device));
     *n_gens = 0;
     for (int g = 1; g < max_gens; g++) gens[g] = nullptr;
@@ -740,6 +770,7 @@ int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, in
         if (rc == RP_OK) rc = finish_gen(ctx, last ? 0 : 1, st, rays->n, &n_child);
         if (rc) break;
         count++;
+        if (done && (rc = done(user, count - 1, rays)) != RP_OK) break;
         if (last || n_child == 0) break;
         rp_rays *next = nullptr;
         rc = rp_rays_alloc(ctx, n_child, &next);  // exact size: the count is known
@@ -763,6 +794,61 @@ int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, in
     return rc;
 }
 
+int rp_trace_rays(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max_gens, int32_t recursion_limit,
+                  float max_length, uint32_t flags, double e2, int32_t *n_gens, rp_stats *st) {
+    if (!ctx || !s || !gens || !gens[0] || max_gens < 1 || !n_gens || s->ctx != ctx) return RP_ERR_INVALID;
+    return trace_rays_impl(ctx, s, gens, max_gens, recursion_limit, max_length, flags, e2, n_gens, st, nullptr,
+                           nullptr);
+}
+
+// Download of each finished generation into a page-locked output buffer while
+// the next generation is traced: the layout kernel packs the generation into
+// a device staging buffer on the main stream (a few hundred microseconds at
+// device bandwidth), and the copy stream moves it to the host with the copy
+// engine, which takes no SMs from the tracing kernels.
+struct OverlapDownload {
+    rp_ctx *ctx;
+    unsigned char *out;  // the caller's page-locked records
+    uint64_t cap, off;
+    uint64_t *gen_offsets;
+    rp_stats *st;
+    std::vector<std::pair<void *, size_t>> staging;  // freed once the copy stream is done
+    std::vector<cudaEvent_t> events;
+};
+
+static int overlap_download(void *user, int g, rp_rays *rays) {
+    OverlapDownload *d = static_cast<OverlapDownload *>(user);
+    rp_ctx *ctx = d->ctx;
+    const uint64_t n = rays->n;
+    if (d->off + n > d->cap) {
+        snprintf(g_last_error, sizeof g_last_error, "the output buffer holds %llu records",
+                 (unsigned long long)d->cap);
+        return RP_ERR_CAPACITY;
+    }
+    d->gen_offsets[g] = d->off;
+    if (n) {
+        void *stage = nullptr;
+        size_t got = 0;
+        int rc = with_staging(ctx, (size_t)n * RP_RAY_BYTES, &stage, &got);
+        if (rc) return rc;
+        d->staging.emplace_back(stage, got);
+        cudaEvent_t ev;
+        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        d->events.push_back(ev);
+        cudaError_t e = launch_soa_to_aos(rays->soa, stage, n, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ev, 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d->out + d->off * RP_RAY_BYTES, stage, (size_t)n * RP_RAY_BYTES,
+                                cudaMemcpyDeviceToHost, ctx->copy_stream);
+        if (e != cudaSuccess) return cuda_fail(e, "generation download");
+        if (d->st) d->st->launches += 1;  // layout kernel of the download
+    }
+    d->off += n;
+    d->gen_offsets[g + 1] = d->off;
+    return RP_OK;
+}
+
 int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_t n, int32_t recursion_limit,
                        float max_length, uint32_t flags, double e2, void *out_records, uint64_t out_cap,
                        uint64_t *gen_offsets, int32_t max_gens, int32_t *n_gens, rp_stats *st) {
@@ -772,21 +858,42 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_
     if (rc) return rc;
     rc = rp_rays_upload_aos(gens[0], in_records, n);
     if (rc == RP_OK && st && n) st->launches += 1;  // layout kernel of the upload
-    if (rc == RP_OK) rc = rp_trace_rays(ctx, s, gens.data(), max_gens, recursion_limit, max_length, flags, e2, n_gens, st);
-    if (rc == RP_OK) {
-        uint64_t off = 0;
-        gen_offsets[0] = 0;
-        for (int g = 0; g < *n_gens; g++) {
-            uint64_t c = gens[g]->n;
-            if (off + c > out_cap) {
-                rc = RP_ERR_CAPACITY;
-                break;
+    const bool pinned_out = out_cap && mapped_host_ptr(out_records);
+    if (rc == RP_OK && pinned_out) {
+        // page-locked output: each generation is downloaded as soon as it is
+        // final, overlapping the following generations
+        if (!ctx->copy_stream) {
+            cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) rc = cuda_fail(e, "copy stream");
+        }
+        if (rc == RP_OK) {
+            OverlapDownload d{ctx, (unsigned char *)out_records, out_cap, 0, gen_offsets, st, {}, {}};
+            gen_offsets[0] = 0;
+            rc = trace_rays_impl(ctx, s, gens.data(), max_gens, recursion_limit, max_length, flags, e2, n_gens, st,
+                                 overlap_download, &d);
+            cudaError_t e = cudaStreamSynchronize(ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->copy_stream);
+            if (rc == RP_OK && e != cudaSuccess) rc = cuda_fail(e, "generation download");
+            for (auto &b : d.staging) ctx_free(ctx, b.first, b.second);
+            for (auto ev : d.events) cudaEventDestroy(ev);
+        }
+    } else if (rc == RP_OK) {
+        rc = rp_trace_rays(ctx, s, gens.data(), max_gens, recursion_limit, max_length, flags, e2, n_gens, st);
+        if (rc == RP_OK) {
+            uint64_t off = 0;
+            gen_offsets[0] = 0;
+            for (int g = 0; g < *n_gens; g++) {
+                uint64_t c = gens[g]->n;
+                if (off + c > out_cap) {
+                    rc = RP_ERR_CAPACITY;
+                    break;
+                }
+                rc = rp_rays_download_aos(gens[g], (unsigned char *)out_records + off * RP_RAY_BYTES, c);
+                if (rc) break;
+                if (st && c) st->launches += 1;  // layout kernel of the download
+                off += c;
+                gen_offsets[g + 1] = off;
             }
-            rc = rp_rays_download_aos(gens[g], (unsigned char *)out_records + off * RP_RAY_BYTES, c);
-            if (rc) break;
-            if (st && c) st->launches += 1;  // layout kernel of the download
-            off += c;
-            gen_offsets[g + 1] = off;
         }
     }
     for (auto *g : gens)

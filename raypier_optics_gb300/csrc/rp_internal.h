@@ -31,6 +31,7 @@ struct rp_ctx {
     size_t scratch_bytes;
     unsigned long long *h_pinned;  // 8 words of pinned host memory for small read-backs
     cudaEvent_t ev0, ev1;
+    cudaStream_t copy_stream;      // downloads that overlap the next generation (created on first use)
 };
 
 struct rp_scene {

@@ -12,6 +12,7 @@
 //      1939-1953), material evaluation into 0..2 children;
 //   4. children are placed by a block scan + decoupled look-back and written
 //      as structure-of-arrays.
+#include <cstdint>
 #include <map>
 #include <mutex>
 
@@ -249,9 +250,12 @@ cudaError_t launch_place_children(const GenArgs &a, unsigned long long n_sub, cu
 
 // ---- AoS <-> SoA ----------------------------------------------------------
 // The packed 188-byte record (include/rp_gb300.h rp_ray) is not 16-byte
-// aligned per ray, but 128 consecutive records (24,064 bytes) are, so a block
-// moves its 128 records through shared memory with 16-byte accesses and each
-// thread then (de)assembles its own record from 4-byte words.
+// aligned per ray, but 128 consecutive records (24,064 bytes) are when the
+// first one is, so a block moves its 128 records through shared memory with
+// 16-byte accesses and each thread then (de)assembles its own record from
+// 4-byte words.  The packed side may be device memory or mapped pinned host
+// memory (written or read across the host link directly); a packed buffer
+// that does not start on a 16-byte boundary is moved in 4-byte words.
 #define RP_AOS_WORDS (RP_RAY_BYTES / 4)
 
 __device__ __forceinline__ double w2d(const unsigned *w, int k) {
@@ -269,7 +273,7 @@ __global__ void __launch_bounds__(RP_BLOCK) aos_to_soa_kernel(const unsigned cha
     unsigned long long nr = n - r0 < RP_BLOCK ? n - r0 : RP_BLOCK;
     const unsigned *src = reinterpret_cast<const unsigned *>(aos + r0 * RP_RAY_BYTES);
     unsigned nwords = (unsigned)(nr * RP_AOS_WORDS);
-    if (nr == RP_BLOCK) {
+    if (nr == RP_BLOCK && ((uintptr_t)aos & 15) == 0) {
         const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
         uint4 *d4 = reinterpret_cast<uint4 *>(sw);
         for (unsigned k = threadIdx.x; k < nwords / 4; k += RP_BLOCK) d4[k] = s4[k];
@@ -328,7 +332,7 @@ __global__ void __launch_bounds__(RP_BLOCK) soa_to_aos_kernel(RaySoA soa, unsign
     __syncthreads();
     unsigned *dst = reinterpret_cast<unsigned *>(aos + r0 * RP_RAY_BYTES);
     unsigned nwords = (unsigned)(nr * RP_AOS_WORDS);
-    if (nr == RP_BLOCK) {
+    if (nr == RP_BLOCK && ((uintptr_t)aos & 15) == 0) {
         uint4 *d4 = reinterpret_cast<uint4 *>(dst);
         const uint4 *s4 = reinterpret_cast<const uint4 *>(sw);
         for (unsigned k = threadIdx.x; k < nwords / 4; k += RP_BLOCK) d4[k] = s4[k];
