@@ -52,7 +52,7 @@ BYTES_PER_CHILD = 188
 # dram__bytes_write.sum from ncu on generation 3 of the 262,144-ray config-2
 # trace, 1,046,875 rays; profiles/traffic_generation_placement_config2_262144rays.md and
 # profiles/generation_mixed_kernel_config2_262144rays.md)
-NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 403.5, "generation_mixed_kernel": 421.9}
+NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 403.5, "generation_mixed_kernel": 438.1}
 
 
 def parse():
