@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--serving-baseline-jobs", type=int, default=500,
                     help="jobs of the same stream run one at a time through the plain FP64 path")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-lens leg (configuration 4)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the Gausslet, sequential and E-field legs")
     return ap.parse_args()
 
 
@@ -315,6 +317,8 @@ def main():
         extra["adjoint"] = adjoint_leg(ctx)
     if rank == 0 and world == 1 and not args.no_serving:
         extra["serving"] = serving_leg(args)
+    if rank == 0 and world == 1 and not args.no_extras:
+        extra["extras"] = extras_leg(ctx)
     if rank == 0:
         emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
              achieved, peak, peak_kind, flags, stats, clk, cpu, other, extra)
@@ -419,6 +423,84 @@ def serving_leg(args):
         b = serve.latency_summary(bres)
         b.update({"path": "plain FP64, one job at a time", "wall_s": bwall})
         out["plain_one_at_a_time_fp64"] = b
+    return out
+
+
+def extras_leg(ctx):
+    """The paths beside the headline trace, at bench sizes, each next to the
+    reference's own CPU code on a sample of the same inputs: Gausslet tracing
+    (configuration-1 lens), sequential tracing (trace_ray_sequence through the
+    same lens) and the E-field summation over the traced gausslets' modes.
+    Host wall time around each call (every call synchronises)."""
+    import types
+
+    import cpu_bench
+    from raypier_optics_gb300 import cdistortions, cfaces, cmaterials, cshapes, ctracer, fields, tracer
+    from raypier_optics_gb300 import workloads as W
+    ns = types.SimpleNamespace(ctracer=ctracer, cfaces=cfaces, cmaterials=cmaterials, cshapes=cshapes,
+                               cdistortions=cdistortions)
+    out = {}
+    seq = [[0, 0], [0, 1], [1, 0], [1, 1], [2, 0]]
+
+    # Gausslets: 65,536 gausslets (0.05 mm waist) through the config-1 lens, 6 generations, FP64
+    n = 65536
+    rays, wl = W.config1_rays(ctracer.ray_dtype, n)
+    g0 = ctracer.GaussletCollection.from_rays(rays)
+    g0.wavelengths = wl
+    g0.config_parabasal_rays(wl, 0.05, 0.0)
+    garr = g0.copy_as_array()
+    best, segs = None, 0
+    for _ in range(4):
+        gc = ctracer.GaussletCollection.from_array(garr)
+        gc.wavelengths = wl
+        lists = W.build_scene(W.config1_spec(), ns)
+        t0 = time.perf_counter()
+        traced, _ = tracer.trace_rays(gc, lists, recursion_limit=6, max_length=1000.0)
+        segs = sum(t.n_rays for t in traced)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    out["gausslets"] = {"workload": f"config-1 lens, {n} gausslets, 6 generations, FP64", "value": segs / best,
+                        "unit": "gausslet-segments/s", "segments": segs,
+                        "cpu_reference": cpu_bench.time_gausslets_cpu(garr[:: max(n // 4096, 1)], wl)}
+    last = traced[-1].copy_as_array()
+
+    # sequential: 1,048,576 rays through the five faces of the config-1 lens in order
+    n2 = 1 << 20
+    rays2, wl2 = W.config1_rays(ctracer.ray_dtype, n2)
+    best, segs = None, 0
+    for _ in range(3):
+        lists = W.build_scene(W.config1_spec(), ns)
+        rc = ctracer.RayCollection.from_array(rays2)
+        rc.wavelengths = wl2
+        t0 = time.perf_counter()
+        traced, _ = tracer.trace_ray_sequence(rc, [(lists[l], f) for l, f in seq], recursion_limit=10,
+                                              max_length=1000.0)
+        segs = sum(t.n_rays for t in traced)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    out["sequential"] = {"workload": f"config-1 lens, {n2} rays, 5-face sequence, FP64", "value": segs / best,
+                         "unit": "ray-segments/s", "segments": segs,
+                         "cpu_reference": cpu_bench.time_sequence_cpu(rays2[:: n2 // 16384], wl2, seq)}
+
+    # E-field: the modes of 16,384 traced gausslets summed at 65,536 points near the focus
+    gl = last[: 16384]
+    gc = ctracer.GaussletCollection.from_array(gl)
+    gc.wavelengths = wl
+    summ = fields.EFieldSummation(gc)
+    gx, gz = np.meshgrid(np.linspace(-0.5, 0.5, 256), np.linspace(80.0, 120.0, 256))
+    pts = np.column_stack([gx.reshape(-1), np.zeros(gx.size), gz.reshape(-1)])
+    summ.evaluate(pts[:1024])
+    best = None
+    for _ in range(3):
+        t0 = time.perf_counter()
+        summ.evaluate(pts)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    evals = len(gl) * len(pts)
+    out["efield"] = {"workload": f"{len(gl)} gausslet modes x {len(pts)} points, FP64", "value": evals / best,
+                     "unit": "mode-evaluations/s",
+                     "cpu_reference": cpu_bench.time_field_cpu(summ.base_rays.copy_as_array()[:512],
+                                                               summ.modes[:512], wl, pts[:4096])}
     return out
 
 

@@ -120,3 +120,82 @@ def cpu_model() -> str:
         pass
     import platform
     return platform.processor() or platform.machine()
+
+
+# ---- the paths beside the headline trace (bench.py's extras leg) --------------------
+def _gausslet_worker(args):
+    records, wl, seq = args
+    _setup_path()
+    import build_ref
+    from raypier_optics_gb300 import workloads as W
+    ref = build_ref.load()
+    lists = W.build_scene(W.config1_spec(), ref)
+    gc = ref.ctracer.GaussletCollection.from_array(records.astype(ref.ctracer.gausslet_dtype))
+    gc.wavelengths = wl
+    t0 = time.perf_counter()
+    with contextlib.redirect_stdout(io.StringIO()):
+        if seq:
+            traced, _ = ref.tracer.trace_ray_sequence(gc, [(lists[l], f) for l, f in seq], recursion_limit=10,
+                                                      max_length=1000.0)
+        else:
+            traced, _ = ref.tracer.trace_rays(gc, lists, recursion_limit=6, max_length=1000.0)
+    return sum(t.n_rays for t in traced), time.perf_counter() - t0
+
+
+def _sequence_worker(args):
+    records, wl, seq = args
+    _setup_path()
+    import build_ref
+    from raypier_optics_gb300 import workloads as W
+    ref = build_ref.load()
+    lists = W.build_scene(W.config1_spec(), ref)
+    rc = ref.ctracer.RayCollection.from_array(records.astype(ref.ctracer.ray_dtype))
+    rc.wavelengths = wl
+    t0 = time.perf_counter()
+    with contextlib.redirect_stdout(io.StringIO()):
+        traced, _ = ref.tracer.trace_ray_sequence(rc, [(lists[l], f) for l, f in seq], recursion_limit=10,
+                                                  max_length=1000.0)
+    return sum(t.n_rays for t in traced), time.perf_counter() - t0
+
+
+def _pool_time(worker, records, wl, seq, processes=None):
+    P = processes or len(os.sched_getaffinity(0))
+    bounds = np.linspace(0, records.shape[0], P + 1).astype(np.int64)
+    jobs = [(records[a:b].copy(), np.asarray(wl), seq) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        res = pool.map(worker, jobs, chunksize=1)
+    segs = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    return {"value": segs / busy, "segments": int(segs), "seconds": busy, "cores": len(jobs), "kind": "reference"}
+
+
+def time_gausslets_cpu(records, wl, seq=None):
+    """The reference's Gausslet trace (config-1 lens) of `records`, gausslet
+    segments per second over the host cores.  None without the reference."""
+    if not reference_available():
+        return None
+    return _pool_time(_gausslet_worker, records, wl, seq)
+
+
+def time_sequence_cpu(records, wl, seq):
+    """The reference's trace_ray_sequence of rays through the config-1 lens."""
+    if not reference_available():
+        return None
+    return _pool_time(_sequence_worker, records, wl, seq)
+
+
+def time_field_cpu(rays, modes, wl, points):
+    """The reference's sum_gaussian_modes (OpenMP over the points) in this
+    process: mode evaluations per second.  None without the reference."""
+    if not reference_available():
+        return None
+    _setup_path()
+    import build_ref
+    ref = build_ref.load()
+    rc = ref.ctracer.RayCollection.from_array(np.ascontiguousarray(rays).astype(ref.ctracer.ray_dtype))
+    t0 = time.perf_counter()
+    ref.cfields.sum_gaussian_modes(rc, np.ascontiguousarray(modes), np.asarray(wl, dtype=np.double),
+                                   np.ascontiguousarray(points), 0.0)
+    dt = time.perf_counter() - t0
+    return {"value": len(rays) * len(points) / dt, "evaluations": int(len(rays) * len(points)), "seconds": dt,
+            "cores": len(os.sched_getaffinity(0)), "kind": "reference"}
