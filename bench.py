@@ -48,6 +48,10 @@ UNIT = "ray-segments/s"
 # per-ray wavelength (8); written back: length, end_face_idx (12)
 BYTES_PER_SEGMENT = 72 + 48 + 16 + 12 + 8 + 12
 BYTES_PER_CHILD = 188
+# a ray of generation > 0 is read through the gather map (4) from its parents'
+# child slots and written to its final record by the kernel that traces it:
+# normal and parent index read (28), the record's other 176 bytes written
+BYTES_PER_GATHERED = 4 + 28 + 176
 # DRAM bytes per input ray of one generation launch (dram__bytes_read.sum +
 # dram__bytes_write.sum from ncu on generation 3 of the 262,144-ray config-2
 # trace, 1,046,875 rays; profiles/traffic_generation_placement_config2_262144rays.md and
@@ -302,7 +306,8 @@ def main():
         other["speedup_mixed_vs_plain_fp64"] = mixed_v / plain_v
         other["precision_vs_plain_fp64"] = precision_sample(ctx, spec, rays, wl, P, per_ray)
     # roofline of the generation kernel
-    alg_bytes = segs * BYTES_PER_SEGMENT + children * BYTES_PER_CHILD
+    gathered = max(segs - n * args.steps, 0)  # every generation but the first of each trace
+    alg_bytes = segs * BYTES_PER_SEGMENT + gathered * BYTES_PER_GATHERED + children * BYTES_PER_CHILD
     kern_s = stats.kernel_ms / 1000.0
     achieved = alg_bytes / kern_s / 1e9
     peak, peak_kind = measured_peak_hbm()
@@ -547,7 +552,8 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
                          "frac": achieved / peak,
                          "traffic": NCU_TRAFFIC_PER_RAY[kernel] * stats.rays_in / max(stats.generations, 1),
                          "kernel": kernel,
-                         "note": f"algorithmic bytes {BYTES_PER_SEGMENT} B/segment + {BYTES_PER_CHILD} B/child "
+                         "note": f"algorithmic bytes {BYTES_PER_SEGMENT} B/segment + {BYTES_PER_GATHERED} B per "
+                                 f"gathered ray (generations > 0) + {BYTES_PER_CHILD} B/child "
                                  f"over summed generation-kernel time; peak {peak_kind}; traffic = ncu DRAM "
                                  f"bytes per input ray x rays per launch (average launch)"},
             "gpu_launches": int(stats.launches),

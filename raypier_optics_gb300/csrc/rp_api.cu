@@ -139,6 +139,9 @@ int rp_ctx_destroy(rp_ctx *c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (c->arena) rp_rays_free(c->arena);
+    if (c->arena2) rp_rays_free(c->arena2);
+    for (int k = 0; k < 2; k++)
+        if (c->child_map[k]) ctx_free(c, c->child_map[k], c->child_map_bytes[k]);
     pool_release_all(c);
     for (auto ev : c->gen_ev) cudaEventDestroy(ev);
     if (c->scratch) cudaFree(c->scratch);
@@ -591,35 +594,67 @@ static int ensure_scratch(rp_ctx *ctx, uint64_t n_sub) {
     return RP_OK;
 }
 
-// The child-slot arena: two ray slots per ray of the largest generation traced
+// A child-slot arena: two ray slots per ray of the largest generation traced
 // so far (kept by the context and reused).
-static int ensure_arena(rp_ctx *ctx, uint64_t n_tiles) {
+static int ensure_arena_slot(rp_ctx *ctx, rp_rays **slot, uint64_t n_tiles) {
     uint64_t need = n_tiles * RP_TILE_SLOTS;
-    if (ctx->arena && ctx->arena->cap >= need) return RP_OK;
-    if (ctx->arena) {
-        rp_rays_free(ctx->arena);
-        ctx->arena = nullptr;
+    if (*slot && (*slot)->cap >= need) return RP_OK;
+    if (*slot) {
+        rp_rays_free(*slot);
+        *slot = nullptr;
     }
-    return rp_rays_alloc(ctx, need + need / 4, &ctx->arena);
+    return rp_rays_alloc(ctx, need + need / 4, slot);
 }
+static int ensure_arena(rp_ctx *ctx, uint64_t n_tiles) { return ensure_arena_slot(ctx, &ctx->arena, n_tiles); }
+
+// Gather map k of trace_rays, for the children of a generation of n_in rays
+// (at most two each).  The map it replaces was last read by a kernel the host
+// has already waited for.
+static int ensure_child_map(rp_ctx *ctx, int k, uint64_t n_in) {
+    const uint64_t need = 2 * n_in;
+    if (ctx->child_map[k] && ctx->child_map_cap[k] >= need) return RP_OK;
+    if (ctx->child_map[k]) {
+        ctx_free(ctx, ctx->child_map[k], ctx->child_map_bytes[k]);
+        ctx->child_map[k] = nullptr;
+        ctx->child_map_cap[k] = 0;
+    }
+    const uint64_t cap = need + need / 4;
+    int rc = ctx_alloc(ctx, (void **)&ctx->child_map[k], cap * sizeof(unsigned), &ctx->child_map_bytes[k]);
+    if (rc) return rc;
+    ctx->child_map_cap[k] = cap;
+    return RP_OK;
+}
+
+// Where trace_rays keeps a generation: its records in an arena read through a
+// gather map (src, in_map), and the arena and map its children go to.
+struct GenLinks {
+    rp_rays *src = nullptr;           // null: the generation's records are in place
+    const unsigned *in_map = nullptr;
+    rp_rays **arena = nullptr;        // null: the context's arena
+    unsigned *map_out = nullptr;      // null: the children are copied to their place afterwards
+    uint64_t map_cap = 0;
+};
 
 // Launches the generation kernel (and, when children are kept, the tile scan)
 // and queues the read-back of count / error / statistics into h_pinned.
 static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, uint32_t flags, double e2, int emit,
-                      int one_list, int one_face, GenArgs &a) {
+                      int one_list, int one_face, GenArgs &a, const GenLinks &lk = GenLinks()) {
     uint64_t n_in = in->n;
     uint64_t n_tiles = (n_in + RP_BLOCK - 1) / RP_BLOCK;
     const uint64_t n_sub = rp_n_sub(n_in);
+    rp_rays **arena = lk.arena ? lk.arena : &ctx->arena;
     int rc = ensure_scratch(ctx, n_sub);
     if (rc) return rc;
     if (emit) {
-        rc = ensure_arena(ctx, n_tiles);
+        rc = ensure_arena_slot(ctx, arena, n_tiles);
         if (rc) return rc;
     }
     unsigned char *sc = ctx->scratch;
     CK(cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream));
     memset(&a, 0, sizeof a);
-    a.in = in->soa;
+    a.in = lk.src ? lk.src->soa : in->soa;
+    a.in_map = lk.src ? lk.in_map : nullptr;
+    a.wb = in->soa;
     a.out = in->soa;
     a.n_in = n_in;
     a.out_cap = 0;
@@ -637,7 +672,7 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
     a.tile_next = (unsigned *)(sc + 40);
     a.tile_counts = (unsigned *)(sc + SCRATCH_HDR);
     a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_sub * sizeof(unsigned)));
-    a.scratch = emit ? ctx->arena->soa : in->soa;
+    a.scratch = emit ? (*arena)->soa : in->soa;
     a.face_counts = s->face_counts;
     if (ctx->gen_ev.empty()) {
         ctx->gen_ev.resize(2);
@@ -651,6 +686,10 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
     if (emit) {
         e = launch_tile_scan(a, n_sub, ctx->stream);
         if (e != cudaSuccess) return cuda_fail(e, "tile scan launch");
+        if (lk.map_out) {
+            e = launch_child_map(a, n_sub, lk.map_out, lk.map_cap, ctx->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "child map launch");
+        }
     }
     CK(cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     return RP_OK;
@@ -682,6 +721,10 @@ static int finish_gen(rp_ctx *ctx, int emit, rp_stats *st, uint64_t n_in, uint64
     if (err & (ERR_ZK_STACK | ERR_SHAPE_STACK)) {
         snprintf(g_last_error, sizeof g_last_error, "device evaluation limit hit (err=0x%x)", err);
         return RP_ERR_INVALID;
+    }
+    if (err & ERR_OVERFLOW) {
+        snprintf(g_last_error, sizeof g_last_error, "child slots overflowed (err=0x%x)", err);
+        return RP_ERR_CAPACITY;
     }
     return RP_OK;
 }
@@ -757,6 +800,12 @@ static int trace_rays_impl(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max
     rp_rays *rays = gens[0];
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     int rc = RP_OK;
+    // Generation g > 0 is never copied out of its parents' child arena on its
+    // own: the kernel that traces it reads each record through the gather map
+    // and writes it, with its length and end face, to gens[g].  The two arenas
+    // and maps alternate, one read while the other is written.
+    GenLinks lk;
+    int par = 0;
     // core/tracer.py:40-45: while rays.n_rays > 0 and count < recursion_limit
     while (rays->n > 0 && count < recursion_limit) {
         int last = (count + 1 == recursion_limit);  // children of this generation are discarded
@@ -764,9 +813,18 @@ static int trace_rays_impl(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max
             rc = RP_ERR_CAPACITY;
             break;
         }
+        lk.arena = par ? &ctx->arena2 : &ctx->arena;
+        lk.map_out = nullptr;
+        lk.map_cap = 0;
+        if (!last) {
+            rc = ensure_child_map(ctx, par, rays->n);
+            if (rc) break;
+            lk.map_out = ctx->child_map[par];
+            lk.map_cap = ctx->child_map_cap[par];
+        }
         GenArgs a;
         uint64_t n_child = 0;
-        rc = launch_gen(ctx, s, rays, max_length, flags, e2, last ? 0 : 1, -1, -1, a);
+        rc = launch_gen(ctx, s, rays, max_length, flags, e2, last ? 0 : 1, -1, -1, a, lk);
         if (rc == RP_OK) rc = finish_gen(ctx, last ? 0 : 1, st, rays->n, &n_child);
         if (rc) break;
         count++;
@@ -775,13 +833,13 @@ static int trace_rays_impl(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max
         rp_rays *next = nullptr;
         rc = rp_rays_alloc(ctx, n_child, &next);  // exact size: the count is known
         if (rc) break;
-        rc = place_gen(ctx, a, next, n_child, st);
-        if (rc) {
-            rp_rays_free(next);
-            break;
-        }
+        next->n = n_child;  // its records are written by the kernel that traces it
+        if (st) st->rays_out += n_child;
         gens[count] = next;
         rays = next;
+        lk.src = *lk.arena;
+        lk.in_map = ctx->child_map[par];
+        par ^= 1;
     }
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaEventSynchronize(ctx->ev1));

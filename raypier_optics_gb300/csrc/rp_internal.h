@@ -26,6 +26,10 @@ struct rp_ctx {
     uint64_t pooled;                 // bytes in `pool`
     std::vector<cudaEvent_t> gen_ev; // per-generation kernel events (pairs)
     struct rp_rays *arena;           // child slots of the generation being traced
+    struct rp_rays *arena2;          // trace_rays: the other arena (one is read while the other is written)
+    unsigned *child_map[2];          // trace_rays: gather maps of the next generation (alternating)
+    uint64_t child_map_cap[2];
+    size_t child_map_bytes[2];
     // per-generation scratch: [out_count | err | pad | stats[2] | tile counter | pad | tile counts, offsets]
     unsigned char *scratch;
     size_t scratch_bytes;

@@ -51,6 +51,14 @@ struct GenArgs {
     unsigned *face_counts;          // per face record hit counters
     unsigned long long *stats;      // [0] hits, [1] terminated children
     unsigned *tile_next;            // next sub-tile to trace (kernels that loop over them; zeroed per launch)
+    // Gathered input (the generation loop of trace_rays): when in_map is set,
+    // ray g of the generation is slot in_map[g] of `in` (the previous
+    // generation's child arena), and the kernel writes its complete record,
+    // with length and end face, to wb[g]; the children's parent index is g.
+    // Otherwise `in` holds the rays at [0, n_in) and length and end face are
+    // written there.
+    const unsigned *in_map;
+    RaySoA wb;
 };
 
 // launchers (rp_trace.cu / rp_mixed.cu); return cudaError_t
@@ -64,6 +72,10 @@ cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem);
 // slots (one block per RP_SUB_PER_BLOCK sub-tiles)
 cudaError_t launch_tile_scan(const GenArgs &a, unsigned long long n_sub, cudaStream_t st);
 cudaError_t launch_place_children(const GenArgs &a, unsigned long long n_sub, cudaStream_t st);
+// the gather map of the children instead of their copy: map[offset + j] = the
+// arena slot of the sub-tile's child j (the next generation reads through it)
+cudaError_t launch_child_map(const GenArgs &a, unsigned long long n_sub, unsigned *map, unsigned long long map_cap,
+                             cudaStream_t st);
 cudaError_t launch_aos_to_soa(const void *aos, RaySoA soa, unsigned long long n, cudaStream_t st);
 cudaError_t launch_soa_to_aos(RaySoA soa, void *aos, unsigned long long n, cudaStream_t st);
 cudaError_t launch_dispersion_table(const rp_dispersion *curves, int n_curves, const double *aux,

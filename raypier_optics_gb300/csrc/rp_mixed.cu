@@ -905,7 +905,8 @@ struct TileIn {
     double ex[RP_SUB], ey[RP_SUB], ez[RP_SUB];
     double2 n[RP_SUB], e1[RP_SUB], e2[RP_SUB];
     double opl[RP_SUB], phase[RP_SUB];
-    unsigned wl[RP_SUB], type[RP_SUB], ident[RP_SUB], pad[RP_SUB];
+    unsigned wl[RP_SUB], type[RP_SUB], ident[RP_SUB];
+    unsigned src[RP_SUB];  // the ray's index in `in` (through the gather map, or its own)
 };
 
 __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
@@ -923,14 +924,34 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
                  "l"(src)
                  : "memory");
 }
+// Writes the traced input ray's record to its final place dst of `wb`: the
+// prefetched fields from shared memory, normal and parent index from the
+// record at src of `in`, and the segment's length and end face.
+__device__ __forceinline__ void write_back(const TileIn &b, unsigned t, const RaySoA &in, unsigned long long src,
+                                           const RaySoA &wb, unsigned long long dst, double len, unsigned endf) {
+    const double nx = in.nx[src], ny = in.ny[src], nz = in.nz[src];
+    const unsigned parent = in.parent[src];
+    wb.ox[dst] = b.ox[t]; wb.oy[dst] = b.oy[t]; wb.oz[dst] = b.oz[t];
+    wb.dx[dst] = b.dx[t]; wb.dy[dst] = b.dy[t]; wb.dz[dst] = b.dz[t];
+    wb.ex[dst] = b.ex[t]; wb.ey[dst] = b.ey[t]; wb.ez[dst] = b.ez[t];
+    wb.n[dst] = b.n[t]; wb.e1[dst] = b.e1[t]; wb.e2[dst] = b.e2[t];
+    wb.len[dst] = len; wb.phase[dst] = b.phase[t]; wb.opl[dst] = b.opl[t];
+    wb.wl[dst] = b.wl[t]; wb.endf[dst] = endf; wb.ident[dst] = b.ident[t]; wb.type[dst] = b.type[t];
+    wb.nx[dst] = nx; wb.ny[dst] = ny; wb.nz[dst] = nz; wb.parent[dst] = parent;
+}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 // Queues the copy of ray i's fields into the lane's slot of `buf` (nothing
 // for i beyond the generation) and closes the thread's copy group.
-__device__ __forceinline__ void prefetch_ray(TileIn *buf, const RaySoA &in, unsigned long long i, unsigned long long n) {
+__device__ __forceinline__ void prefetch_ray(TileIn *buf, const RaySoA &in, const unsigned *map,
+                                             unsigned long long i, unsigned long long n) {
     if (i < n) {
         const unsigned t = threadIdx.x & 31;
+        const unsigned long long s = map ? (unsigned long long)map[i] : i;
+        buf->src[t] = (unsigned)s;
+        i = s;
         cp_async8(&buf->ox[t], &in.ox[i]);
         cp_async8(&buf->oy[t], &in.oy[i]);
         cp_async8(&buf->oz[t], &in.oz[i]);
@@ -977,8 +998,11 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
 // neither a slow sub-tile nor a slow warp holds up the others.
 // Dynamic shared memory: the plain kernel's tables, the mixed tables at mx_off
 // and, at tb_off, each thread's box-entry distance per culled face.
+// Three blocks (12 warps) per SM: up to 168 registers a thread and no spills;
+// at four blocks (128 registers) the spills cost more than the extra warps
+// hide (5 % slower on the lens-train benchmark).
 template <bool FB>
-__global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A, unsigned mx_off, unsigned tb_off,
+__global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A, unsigned mx_off, unsigned tb_off,
                                                                       unsigned in_off) {
     using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1004,17 +1028,18 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
     // every warp takes sub-tiles from a launch-wide counter on its own; the
     // next sub-tile's inputs are copied into the warp's other buffer while
     // this one is traced (each lane copies and reads only its own slot)
+    const bool gathered = A.in_map != nullptr;
     unsigned tile = 0;
     if (lane == 0) tile = atomicAdd(A.tile_next, 1u);
     tile = __shfl_sync(0xffffffffu, tile, 0);
-    if (tile < n_sub) prefetch_ray(&bufs[0], A.in, (unsigned long long)tile * RP_SUB + lane, A.n_in);
+    if (tile < n_sub) prefetch_ray(&bufs[0], A.in, A.in_map, (unsigned long long)tile * RP_SUB + lane, A.n_in);
     for (unsigned k = 0;; k++) {
         if (tile >= n_sub) break;
         unsigned next = 0;
         if (lane == 0) next = atomicAdd(A.tile_next, 1u);
         next = __shfl_sync(0xffffffffu, next, 0);
         if (next < n_sub)
-            prefetch_ray(&bufs[(k + 1) & 1], A.in, (unsigned long long)next * RP_SUB + lane, A.n_in);
+            prefetch_ray(&bufs[(k + 1) & 1], A.in, A.in_map, (unsigned long long)next * RP_SUB + lane, A.n_in);
         else
             cp_async_commit();
         cp_async_wait_prev();  // this thread's copies for `tile` have landed
@@ -1022,6 +1047,7 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
         const unsigned t = lane;
         const unsigned long long i = (unsigned long long)tile * RP_SUB + lane;
         const bool active = i < A.n_in;
+        const unsigned long long src = active && gathered ? (unsigned long long)in.src[t] : i;  // the record in A.in
 
         Best b;
         b.len = ffm(max_len, 0.0f);
@@ -1046,7 +1072,7 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
                 if (face_specialised(S.faces[f].type))
                     try_face(S, ml, mf, f, A.one_list, cur, R, O, D, dlen, max_len, A.err, b);
                 else if constexpr (FB)
-                    try_face_fp64(A, S, f, A.one_list, i, dlen, b);
+                    try_face_fp64(A, S, f, A.one_list, src, dlen, b);
             } else {
                 // culled nearest-first search over the first 64 faces, then the rest in order
                 const float dfx = D[0].hi, dfy = D[1].hi, dfz = D[2].hi;
@@ -1112,11 +1138,17 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
                         atomicOr(A.err, ERR_SHAPE_STACK);
                         break;
                     }
-                    if constexpr (FB) try_face_fp64(A, S, f, l, i, dlen, b);
+                    if constexpr (FB) try_face_fp64(A, S, f, l, src, dlen, b);
                 }
             }
-            A.in.len[i] = d_of_ff(b.len);
-            A.in.endf[i] = b.face >= 0 ? (unsigned)S.faces[b.face].idx : 0xFFFFFFFFu;
+            const double len64 = d_of_ff(b.len);
+            const unsigned endf = b.face >= 0 ? (unsigned)S.faces[b.face].idx : 0xFFFFFFFFu;
+            if (gathered) {
+                write_back(in, t, A.in, src, A.wb, i, len64, endf);
+            } else {
+                A.in.len[i] = len64;
+                A.in.endf[i] = endf;
+            }
             if (b.face >= 0) {
                 atomicAdd(&s_counts[b.face], 1u);
                 atomicAdd(&s_hits, 1u);
@@ -1201,7 +1233,7 @@ __global__ void __launch_bounds__(RP_BLOCK, 4) generation_mixed_kernel(GenArgs A
                     }
                 } else if constexpr (FB) {
                     unsigned term = 0;
-                    nc = fallback_children(A, S, F, Mt, b.list, i, d_of_ff(b.len), origin, nrm, &ccd, chd, &term);
+                    nc = fallback_children(A, S, F, Mt, b.list, src, d_of_ff(b.len), origin, nrm, &ccd, chd, &term);
                     fp64_children = true;
                     if (term) atomicAdd(&s_term, term);
                 }

@@ -133,4 +133,24 @@ __device__ __forceinline__ void copy_ray(const RaySoA &s, unsigned long long src
     o.wl[dst] = wl; o.parent[dst] = parent; o.endf[dst] = endf; o.ident[dst] = ident; o.type[dst] = type;
 }
 
+// Writes ray `src` of `s` to `dst` of `o` with the given length and end face
+// (a generation's input record once its segment is traced).
+__device__ __forceinline__ void pass_ray(const RaySoA &s, unsigned long long src, const RaySoA &o,
+                                         unsigned long long dst, double len, unsigned endf) {
+    const double ox = s.ox[src], oy = s.oy[src], oz = s.oz[src];
+    const double dx = s.dx[src], dy = s.dy[src], dz = s.dz[src];
+    const double nx = s.nx[src], ny = s.ny[src], nz = s.nz[src];
+    const double ex = s.ex[src], ey = s.ey[src], ez = s.ez[src];
+    const double2 n = s.n[src], e1 = s.e1[src], e2 = s.e2[src];
+    const double phase = s.phase[src], opl = s.opl[src];
+    const unsigned wl = s.wl[src], parent = s.parent[src], ident = s.ident[src], type = s.type[src];
+    o.ox[dst] = ox; o.oy[dst] = oy; o.oz[dst] = oz;
+    o.dx[dst] = dx; o.dy[dst] = dy; o.dz[dst] = dz;
+    o.nx[dst] = nx; o.ny[dst] = ny; o.nz[dst] = nz;
+    o.ex[dst] = ex; o.ey[dst] = ey; o.ez[dst] = ez;
+    o.n[dst] = n; o.e1[dst] = e1; o.e2[dst] = e2;
+    o.len[dst] = len; o.phase[dst] = phase; o.opl[dst] = opl;
+    o.wl[dst] = wl; o.parent[dst] = parent; o.endf[dst] = endf; o.ident[dst] = ident; o.type[dst] = type;
+}
+
 }  // namespace rp

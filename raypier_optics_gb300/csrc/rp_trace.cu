@@ -10,8 +10,10 @@
 //      the earlier face wins a tie: FaceList.intersect_c 1882-1904);
 //   3. on a hit: count it, hit point, orientation (compute_orientation_c
 //      1939-1953), material evaluation into 0..2 children;
-//   4. children are placed by a block scan + decoupled look-back and written
-//      as structure-of-arrays.
+//   4. children go to the warp's sub-tile slots of the child arena (warp scan
+//      of the per-ray counts); a scan of the sub-tile counts then either
+//      copies them to their final place or, inside trace_rays, gives the next
+//      generation a gather map through which it reads them.
 #include <cstdint>
 #include <map>
 #include <mutex>
@@ -33,13 +35,15 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
     const unsigned tile = blockIdx.x;
     const unsigned long long i = (unsigned long long)tile * RP_BLOCK + threadIdx.x;
     const bool active = i < A.n_in;
+    // the ray's record in `in`: gathered through the map, or in place
+    const unsigned long long src = active && A.in_map ? (unsigned long long)A.in_map[i] : i;
 
     int best = -1, best_list = -1;
     double len = A.max_len;
     v3 o = mkv(0, 0, 0), d = mkv(0, 0, 0);
     if (active) {
-        o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
-        d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
+        o = mkv(A.in.ox[src], A.in.oy[src], A.in.oz[src]);
+        d = mkv(A.in.dx[src], A.in.dy[src], A.in.dz[src]);
         v3 pend = addv(o, mulvs(d, A.max_len));
         if (A.one_list >= 0) {
             // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
@@ -57,8 +61,13 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
         } else {
             nearest_hit(S, o, d, pend, A.max_len, len, best, best_list, A.err);
         }
-        A.in.len[i] = len;
-        A.in.endf[i] = best >= 0 ? (unsigned)S.faces[best].idx : 0xFFFFFFFFu;
+        const unsigned endf = best >= 0 ? (unsigned)S.faces[best].idx : 0xFFFFFFFFu;
+        if (A.in_map) {
+            pass_ray(A.in, src, A.wb, i, len, endf);
+        } else {
+            A.in.len[i] = len;
+            A.in.endf[i] = endf;
+        }
         if (best >= 0) {
             atomicAdd(&s_counts[best], 1u);
             atomicAdd(&s_hits, 1u);
@@ -92,14 +101,14 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
             RayState r;
             r.o = o;
             r.d = d;
-            r.E = mkv(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
-            r.n = A.in.n[i];
-            r.e1 = A.in.e1[i];
-            r.e2 = A.in.e2[i];
+            r.E = mkv(A.in.ex[src], A.in.ey[src], A.in.ez[src]);
+            r.n = A.in.n[src];
+            r.e1 = A.in.e1[src];
+            r.e2 = A.in.e2[src];
             r.len = len;
-            r.opl = A.in.opl[i];
-            r.type = A.in.type[i];
-            r.wl = A.in.wl[i];
+            r.opl = A.in.opl[src];
+            r.type = A.in.type[src];
+            r.wl = A.in.wl[src];
             nc = eval_children(S, S.mats[F.material], r, point, nrm, tng, cc, ch, A.err);
             if (A.e2_term > 0.0 && nc > 0) {
                 int w = 0;
@@ -121,8 +130,8 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
     const unsigned excl = warp_scan((unsigned)nc, &sub_children);
     const unsigned long long q = sub_tile_of_thread();
     if (nc > 0) {
-        double phase = A.in.phase[i];
-        unsigned wl = A.in.wl[i], ident = A.in.ident[i];
+        double phase = A.in.phase[src];
+        unsigned wl = A.in.wl[src], ident = A.in.ident[src];
         unsigned endf = (unsigned)S.faces[best].idx;
         const unsigned long long slot = q * RP_SUB_SLOTS + excl;
         for (int k = 0; k < nc; k++) store_child(A.scratch, slot + k, cc, ch[k], phase, wl, (unsigned)i, endf, ident);
@@ -245,6 +254,35 @@ cudaError_t launch_place_children(const GenArgs &a, unsigned long long n_sub, cu
     if (n_sub == 0) return cudaSuccess;
     const unsigned grid = (unsigned)((n_sub + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK);
     place_children_kernel<<<grid, RP_BLOCK, 0, st>>>(a, n_sub);
+    return cudaGetLastError();
+}
+
+// The children's gather map instead of their copy: child j of sub-tile q is
+// ray tile_offsets[q] + j of the next generation and lives at arena slot
+// q * RP_SUB_SLOTS + j.  4 bytes per child instead of a 188-byte record read
+// and written: the next generation's kernel reads each record through the map
+// and writes it to its final place while tracing it.
+__global__ void __launch_bounds__(RP_BLOCK) child_map_kernel(const unsigned *counts,
+                                                             const unsigned long long *offsets,
+                                                             unsigned long long n_sub, unsigned *map,
+                                                             unsigned long long map_cap, unsigned *err) {
+    const unsigned long long q = sub_tile_of_thread();
+    if (q >= n_sub) return;
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned count = counts[q];
+    const unsigned long long base = offsets[q];
+    if (count > RP_SUB_SLOTS || base + count > map_cap) {
+        if (lane == 0) atomicOr(err, ERR_OVERFLOW);
+        return;
+    }
+    for (unsigned j = lane; j < count; j += RP_SUB) map[base + j] = (unsigned)(q * RP_SUB_SLOTS + j);
+}
+
+cudaError_t launch_child_map(const GenArgs &a, unsigned long long n_sub, unsigned *map, unsigned long long map_cap,
+                             cudaStream_t st) {
+    if (n_sub == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)((n_sub + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK);
+    child_map_kernel<<<grid, RP_BLOCK, 0, st>>>(a.tile_counts, a.tile_offsets, n_sub, map, map_cap, a.err);
     return cudaGetLastError();
 }
 
