@@ -908,6 +908,12 @@ struct TileIn {
     unsigned wl[RP_SUB], type[RP_SUB], ident[RP_SUB];
     unsigned src[RP_SUB];  // the ray's index in `in` (through the gather map, or its own)
 };
+// The fields of a gathered input ray the kernel only passes through to its
+// final record (one buffer per warp, filled while the sub-tile is searched).
+struct PassIn {
+    double nx[RP_SUB], ny[RP_SUB], nz[RP_SUB];
+    unsigned parent[RP_SUB];
+};
 
 __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
@@ -927,10 +933,12 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
 // Writes the traced input ray's record to its final place dst of `wb`: the
 // prefetched fields from shared memory, normal and parent index from the
 // record at src of `in`, and the segment's length and end face.
-__device__ __forceinline__ void write_back(const TileIn &b, unsigned t, const RaySoA &in, unsigned long long src,
-                                           const RaySoA &wb, unsigned long long dst, double len, unsigned endf) {
-    const double nx = in.nx[src], ny = in.ny[src], nz = in.nz[src];
-    const unsigned parent = in.parent[src];
+// Writes the traced input ray's record to its final place dst of `wb`: the
+// prefetched fields from shared memory and the segment's length and end face.
+__device__ __forceinline__ void write_back(const TileIn &b, const PassIn &p, unsigned t, const RaySoA &wb,
+                                           unsigned long long dst, double len, unsigned endf) {
+    const double nx = p.nx[t], ny = p.ny[t], nz = p.nz[t];
+    const unsigned parent = p.parent[t];
     wb.ox[dst] = b.ox[t]; wb.oy[dst] = b.oy[t]; wb.oz[dst] = b.oz[t];
     wb.dx[dst] = b.dx[t]; wb.dy[dst] = b.dy[t]; wb.dz[dst] = b.dz[t];
     wb.ex[dst] = b.ex[t]; wb.ey[dst] = b.ey[t]; wb.ez[dst] = b.ez[t];
@@ -942,14 +950,14 @@ __device__ __forceinline__ void write_back(const TileIn &b, unsigned t, const Ra
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev2() { asm volatile("cp.async.wait_group 2;\n" ::: "memory"); }
 
 // Queues the copy of ray i's fields into the lane's slot of `buf` (nothing
 // for i beyond the generation) and closes the thread's copy group.
-__device__ __forceinline__ void prefetch_ray(TileIn *buf, const RaySoA &in, const unsigned *map,
-                                             unsigned long long i, unsigned long long n) {
+__device__ __forceinline__ void prefetch_ray(TileIn *buf, const RaySoA &in, unsigned long long i, unsigned long long n,
+                                             unsigned long long s) {
     if (i < n) {
         const unsigned t = threadIdx.x & 31;
-        const unsigned long long s = map ? (unsigned long long)map[i] : i;
         buf->src[t] = (unsigned)s;
         i = s;
         cp_async8(&buf->ox[t], &in.ox[i]);
@@ -971,6 +979,29 @@ __device__ __forceinline__ void prefetch_ray(TileIn *buf, const RaySoA &in, cons
         cp_async4(&buf->ident[t], &in.ident[i]);
     }
     cp_async_commit();
+}
+
+// Queues the copy of the pass-through fields of record s (no commit).
+__device__ __forceinline__ void prefetch_pass(PassIn *p, const RaySoA &in, unsigned long long s) {
+    const unsigned t = threadIdx.x & 31;
+    cp_async8(&p->nx[t], &in.nx[s]);
+    cp_async8(&p->ny[t], &in.ny[s]);
+    cp_async8(&p->nz[t], &in.nz[s]);
+    cp_async4(&p->parent[t], &in.parent[s]);
+}
+
+// Takes the warp's next sub-tile from the launch-wide counter.
+__device__ __forceinline__ unsigned claim_sub_tile(unsigned *counter, unsigned lane) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1u);
+    return __shfl_sync(0xffffffffu, t, 0);
+}
+
+// The gather-map entry of this lane's ray in sub-tile `tile` (0 when there is
+// none), loaded a sub-tile ahead of its use so that its latency is hidden.
+__device__ __forceinline__ unsigned map_entry(const GenArgs &A, unsigned tile, unsigned lane, unsigned long long n_sub) {
+    const unsigned long long i = (unsigned long long)tile * RP_SUB + lane;
+    return (A.in_map && tile < n_sub && i < A.n_in) ? A.in_map[i] : 0u;
 }
 
 }  // namespace mx
@@ -1003,13 +1034,14 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
 // hide (5 % slower on the lens-train benchmark).
 template <bool FB>
 __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A, unsigned mx_off, unsigned tb_off,
-                                                                      unsigned in_off) {
+                                                                      unsigned in_off, unsigned pass_off) {
     using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_hits, s_term;
     const unsigned lane = threadIdx.x & 31;
     // this warp's two sub-tile input buffers (double-buffered)
     TileIn *bufs = reinterpret_cast<TileIn *>(smem + in_off) + 2 * (threadIdx.x >> 5);
+    PassIn *pass = reinterpret_cast<PassIn *>(smem + pass_off) + (threadIdx.x >> 5);
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
     MxList *ml = reinterpret_cast<MxList *>(smem + mx_off);
@@ -1028,25 +1060,40 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
     // every warp takes sub-tiles from a launch-wide counter on its own; the
     // next sub-tile's inputs are copied into the warp's other buffer while
     // this one is traced (each lane copies and reads only its own slot)
+    // (with a gathered input the map entries of a sub-tile are loaded one
+    // sub-tile before its copies are queued)
     const bool gathered = A.in_map != nullptr;
-    unsigned tile = 0;
-    if (lane == 0) tile = atomicAdd(A.tile_next, 1u);
-    tile = __shfl_sync(0xffffffffu, tile, 0);
-    if (tile < n_sub) prefetch_ray(&bufs[0], A.in, A.in_map, (unsigned long long)tile * RP_SUB + lane, A.n_in);
+    unsigned tile = claim_sub_tile(A.tile_next, lane);
+    if (tile < n_sub) {
+        const unsigned long long i0 = (unsigned long long)tile * RP_SUB + lane;
+        prefetch_ray(&bufs[0], A.in, i0, A.n_in, gathered ? (unsigned long long)map_entry(A, tile, lane, n_sub) : i0);
+    }
+    unsigned next = claim_sub_tile(A.tile_next, lane);
+    unsigned next_src = map_entry(A, next, lane, n_sub);
     for (unsigned k = 0;; k++) {
         if (tile >= n_sub) break;
-        unsigned next = 0;
-        if (lane == 0) next = atomicAdd(A.tile_next, 1u);
-        next = __shfl_sync(0xffffffffu, next, 0);
-        if (next < n_sub)
-            prefetch_ray(&bufs[(k + 1) & 1], A.in, A.in_map, (unsigned long long)next * RP_SUB + lane, A.n_in);
-        else
-            cp_async_commit();
-        cp_async_wait_prev();  // this thread's copies for `tile` have landed
+        const unsigned next2 = claim_sub_tile(A.tile_next, lane);
+        const unsigned next2_src = map_entry(A, next2, lane, n_sub);
         const TileIn &in = bufs[k & 1];
         const unsigned t = lane;
         const unsigned long long i = (unsigned long long)tile * RP_SUB + lane;
         const bool active = i < A.n_in;
+        if (gathered) {
+            // pass-through fields of this sub-tile: their own copy group, awaited at the write-back
+            if (active) prefetch_pass(pass, A.in, in.src[t]);
+            cp_async_commit();
+        }
+        const unsigned long long ni = (unsigned long long)next * RP_SUB + lane;
+        if (next < n_sub)
+            prefetch_ray(&bufs[(k + 1) & 1], A.in, ni, A.n_in, gathered ? (unsigned long long)next_src : ni);
+        else
+            cp_async_commit();
+        // this thread's copies for `tile` have landed (the pass-through group
+        // and the next sub-tile's group may still be in flight)
+        if (gathered)
+            cp_async_wait_prev2();
+        else
+            cp_async_wait_prev();
         const unsigned long long src = active && gathered ? (unsigned long long)in.src[t] : i;  // the record in A.in
 
         Best b;
@@ -1144,7 +1191,8 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
             const double len64 = d_of_ff(b.len);
             const unsigned endf = b.face >= 0 ? (unsigned)S.faces[b.face].idx : 0xFFFFFFFFu;
             if (gathered) {
-                write_back(in, t, A.in, src, A.wb, i, len64, endf);
+                cp_async_wait_prev();  // the pass-through group
+                write_back(in, *pass, t, A.wb, i, len64, endf);
             } else {
                 A.in.len[i] = len64;
                 A.in.endf[i] = endf;
@@ -1156,6 +1204,8 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
         }
         if (!A.emit) {
             tile = next;
+            next = next2;
+            next_src = next2_src;
             continue;
         }
 
@@ -1258,6 +1308,8 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
         }
         if (lane == 0) A.tile_counts[tile] = sub_children;
         tile = next;
+        next = next2;
+        next_src = next2_src;
     }
     flush_counts(A, S, s_counts);
     if (threadIdx.x == 0) {
@@ -1298,12 +1350,14 @@ static cudaError_t mixed_grid_blocks(size_t total, int *blocks) {
     return cudaSuccess;
 }
 
-static size_t mixed_smem_total(const GenArgs &a, size_t smem, size_t *mx_off, size_t *tb_off, size_t *in_off) {
+static size_t mixed_smem_total(const GenArgs &a, size_t smem, size_t *mx_off, size_t *tb_off, size_t *in_off,
+                               size_t *pass_off) {
     *mx_off = (smem + 15) & ~(size_t)15;
     *tb_off = *mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
     const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
     *in_off = (*tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
-    return *in_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
+    *pass_off = *in_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
+    return *pass_off + (a.in_map ? RP_SUB_PER_BLOCK * sizeof(mx::PassIn) : 0);
 }
 
 static cudaError_t mixed_blocks(const GenArgs &a, size_t total, int *blocks) {
@@ -1314,8 +1368,8 @@ static cudaError_t mixed_blocks(const GenArgs &a, size_t total, int *blocks) {
 // that a later launch of the same configuration makes no other CUDA call, as
 // stream capture requires.
 cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem) {
-    size_t mx_off, tb_off, in_off;
-    const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off);
+    size_t mx_off, tb_off, in_off, pass_off;
+    const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off, &pass_off);
     if (total > 220 * 1024) return cudaErrorInvalidConfiguration;
     int blocks = 0;
     return mixed_blocks(a, total, &blocks);
@@ -1325,19 +1379,19 @@ cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem) {
 // fallbacks the kernel carries no out-of-line calls and their register cost.
 cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st) {
     if (a.n_in == 0) return cudaSuccess;
-    size_t mx_off, tb_off, in_off;
-    const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off);
+    size_t mx_off, tb_off, in_off, pass_off;
+    const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off, &pass_off);
     if (total > 220 * 1024) return cudaErrorInvalidConfiguration;  // scene too large for the per-block tables
     int blocks = 0;
     cudaError_t e = mixed_blocks(a, total, &blocks);
     if (e != cudaSuccess) return e;
     const unsigned long long n_tiles = (a.n_in + RP_BLOCK - 1) / RP_BLOCK;
     const unsigned grid = (unsigned)(n_tiles < (unsigned long long)blocks ? n_tiles : blocks);
-    const unsigned o1 = (unsigned)mx_off, o2 = (unsigned)tb_off, o3 = (unsigned)in_off;
+    const unsigned o1 = (unsigned)mx_off, o2 = (unsigned)tb_off, o3 = (unsigned)in_off, o4 = (unsigned)pass_off;
     if (a.mixed_fallback)
-        generation_mixed_kernel<true><<<grid, RP_BLOCK, total, st>>>(a, o1, o2, o3);
+        generation_mixed_kernel<true><<<grid, RP_BLOCK, total, st>>>(a, o1, o2, o3, o4);
     else
-        generation_mixed_kernel<false><<<grid, RP_BLOCK, total, st>>>(a, o1, o2, o3);
+        generation_mixed_kernel<false><<<grid, RP_BLOCK, total, st>>>(a, o1, o2, o3, o4);
     return cudaGetLastError();
 }
 

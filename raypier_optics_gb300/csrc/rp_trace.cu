@@ -178,54 +178,79 @@ cudaError_t prepare_generation_plain(const GenArgs &a, size_t smem) {
 }
 
 // ---- child placement ------------------------------------------------------
-// One block scans the per-sub-tile child counts (exclusive prefix + total):
-// each pass covers 1024 threads x RP_SCAN_PER consecutive counts.
-#define RP_SCAN_PER 8
+// One block scans the per-sub-tile child counts (exclusive prefix + total).
+// Warp w owns a contiguous chunk of the counts (a multiple of 128 long): it
+// sums the chunk with 16-byte loads, one block-wide scan of the 32 chunk sums
+// gives each chunk its start, and the warp then scans its chunk 128 counts at
+// a time with a running carry, writing the offsets with 16-byte stores.
+#define RP_SCAN_SLICE 128  // counts per warp step: 4 per lane
 __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *counts, unsigned long long n,
                                                          unsigned long long *offsets, unsigned long long *total) {
     __shared__ unsigned long long s_warp[32];
-    __shared__ unsigned long long s_carry;
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_carry = 0;
-    __syncthreads();
-    for (unsigned long long base = 0; base < n; base += 1024ull * RP_SCAN_PER) {
-        const unsigned long long i0 = base + (unsigned long long)threadIdx.x * RP_SCAN_PER;
-        unsigned v[RP_SCAN_PER];
-        unsigned long long sum = 0;
-#pragma unroll
-        for (int k = 0; k < RP_SCAN_PER; k++) {
-            v[k] = (i0 + k < n) ? counts[i0 + k] : 0u;
-            sum += v[k];
+    const bool vec = ((reinterpret_cast<uintptr_t>(counts) | reinterpret_cast<uintptr_t>(offsets)) & 15) == 0;
+    const unsigned long long per = (n + 32ull * RP_SCAN_SLICE - 1) / (32ull * RP_SCAN_SLICE) * RP_SCAN_SLICE;
+    const unsigned long long c0 = per * warp < n ? per * warp : n;
+    const unsigned long long c1 = c0 + per < n ? c0 + per : n;
+    // the four counts of this lane in the slice at `base` (zeros past the chunk)
+    auto load4 = [&](unsigned long long base, unsigned &v0, unsigned &v1, unsigned &v2, unsigned &v3) {
+        const unsigned long long k = base + 4ull * lane;
+        if (vec && k + 3 < c1) {
+            const uint4 v = *reinterpret_cast<const uint4 *>(counts + k);
+            v0 = v.x; v1 = v.y; v2 = v.z; v3 = v.w;
+        } else {
+            v0 = k < c1 ? counts[k] : 0u;
+            v1 = k + 1 < c1 ? counts[k + 1] : 0u;
+            v2 = k + 2 < c1 ? counts[k + 2] : 0u;
+            v3 = k + 3 < c1 ? counts[k + 3] : 0u;
         }
-        unsigned long long x = sum;  // inclusive warp scan of the per-thread sums
+    };
+    unsigned long long sum = 0;
+#pragma unroll 4
+    for (unsigned long long base = c0; base < c1; base += RP_SCAN_SLICE) {
+        unsigned v0, v1, v2, v3;
+        load4(base, v0, v1, v2, v3);
+        sum += (unsigned long long)v0 + v1 + v2 + v3;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) s_warp[warp] = sum;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = s_warp[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            unsigned long long t = __shfl_up_sync(0xffffffffu, x, o);
+            unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (unsigned)o) w += t;
+        }
+        s_warp[lane] = w;  // inclusive prefixes of the chunk sums
+    }
+    __syncthreads();
+    unsigned long long carry = warp ? s_warp[warp - 1] : 0ull;
+    for (unsigned long long base = c0; base < c1; base += RP_SCAN_SLICE) {
+        unsigned v0, v1, v2, v3;
+        load4(base, v0, v1, v2, v3);
+        const unsigned ls = v0 + v1 + v2 + v3;
+        unsigned x = ls;  // inclusive warp scan of the lane sums
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= (unsigned)o) x += t;
         }
-        if (lane == 31) s_warp[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            unsigned long long w = s_warp[lane];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= (unsigned)o) w += t;
-            }
-            s_warp[lane] = w;  // inclusive prefixes of the warp totals
+        const unsigned long long e0 = carry + (x - ls), e1 = e0 + v0, e2 = e1 + v1, e3 = e2 + v2;
+        const unsigned long long k = base + 4ull * lane;
+        if (vec && k + 3 < c1) {
+            reinterpret_cast<ulonglong2 *>(offsets + k)[0] = make_ulonglong2(e0, e1);
+            reinterpret_cast<ulonglong2 *>(offsets + k)[1] = make_ulonglong2(e2, e3);
+        } else {
+            if (k < c1) offsets[k] = e0;
+            if (k + 1 < c1) offsets[k + 1] = e1;
+            if (k + 2 < c1) offsets[k + 2] = e2;
+            if (k + 3 < c1) offsets[k + 3] = e3;
         }
-        __syncthreads();
-        unsigned long long excl = s_carry + (warp ? s_warp[warp - 1] : 0ull) + (x - sum);
-#pragma unroll
-        for (int k = 0; k < RP_SCAN_PER; k++) {
-            if (i0 + k < n) offsets[i0 + k] = excl;
-            excl += v[k];
-        }
-        __syncthreads();  // everyone has read s_carry and s_warp
-        if (threadIdx.x == 0) s_carry += s_warp[31];
-        __syncthreads();
+        carry += __shfl_sync(0xffffffffu, x, 31);
     }
-    if (threadIdx.x == 0) *total = s_carry;
+    if (threadIdx.x == 0) *total = s_warp[31];
 }
 
 cudaError_t launch_tile_scan(const GenArgs &a, unsigned long long n_sub, cudaStream_t st) {
