@@ -440,7 +440,7 @@ def extras_leg(ctx):
     import types
 
     import cpu_bench
-    from raypier_optics_gb300 import cdistortions, cfaces, cmaterials, cshapes, ctracer, fields, tracer
+    from raypier_optics_gb300 import cdistortions, cfaces, cfields, cmaterials, cshapes, ctracer, fields, tracer
     from raypier_optics_gb300 import workloads as W
     ns = types.SimpleNamespace(ctracer=ctracer, cfaces=cfaces, cmaterials=cmaterials, cshapes=cshapes,
                                cdistortions=cdistortions)
@@ -506,6 +506,34 @@ def extras_leg(ctx):
                      "unit": "mode-evaluations/s",
                      "cpu_reference": cpu_bench.time_field_cpu(summ.base_rays.copy_as_array()[:512],
                                                                summ.modes[:512], wl, pts[:4096])}
+
+    # interaction matrix: modes on a 0.1 mm hexagonal lattice (radius 6.7 mm)
+    # against test points every 0.05 mm, pairs within 0.25 mm
+    rng = np.random.Generator(np.random.PCG64(5))
+    s3 = math.sqrt(3.0)
+    ii, jj = np.meshgrid(np.arange(-80, 81), np.arange(-80, 81))
+    hx, hy = 0.1 * (ii + 0.5 * jj).reshape(-1), 0.1 * (0.5 * s3 * jj).reshape(-1)
+    keep = hx * hx + hy * hy <= 6.7 ** 2
+    hx, hy = hx[keep].copy(), hy[keep].copy()
+    m = len(hx)
+    cur = cfields.calc_mode_curvature(hx, hy, rng.normal(0, 0.02, m), rng.normal(0, 0.02, m), rng.normal(0, 0.5, m),
+                                      rng.normal(0, 0.5, m), rng.normal(0, 0.2, m))
+    g = np.arange(-6.8, 6.8 + 1e-9, 0.05)
+    tx, ty = [v.reshape(-1).copy() for v in np.meshgrid(g, g)]
+    im_args = (hx, hy, tx, ty) + tuple(cur) + (0.6, 0.1, 0.25, 1.0, 0.05)
+    cfields.build_interaction_matrix(*im_args)
+    best, entries = None, 0
+    for _ in range(3):
+        t0 = time.perf_counter()
+        data, _ = cfields.build_interaction_matrix(*im_args)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+        entries = len(data)
+    out["interaction_matrix"] = {
+        "workload": f"{m} modes x {len(tx)} test points, {entries} pairs within 0.25 mm, FP64, host arrays in and out",
+        "value": m * len(tx) / best, "unit": "mode-point pairs/s", "entries": entries,
+        "cpu_reference": cpu_bench.time_interaction_cpu(*[a[:256] if k in (0, 1, 4, 5, 6, 7, 8, 9) else a
+                                                          for k, a in enumerate(im_args[:10])], *im_args[10:])}
     return out
 
 

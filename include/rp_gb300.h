@@ -417,6 +417,29 @@ int rp_field_evaluate(rp_field *field, const double *points, uint64_t n_points, 
 /* The same with device buffers (points and E on the context's device). */
 int rp_field_evaluate_device(rp_field *field, const double *points_dev, uint64_t n_points, double time_ps,
                              double *E_dev);
+/* calc_mode_curvature (cfields.pyx:232-290): the wavefront curvature A, B, C
+ * (d2z'/dx'2, d2z'/dx'dy', d2z'/dy'2) and the local basis x', y', z' (X, Y, Z:
+ * n x 3) at n points of a decomposition plane from the wavefront slopes dx, dy
+ * and second derivatives dx2, dy2, dxdy there (the reference's rx, ry are
+ * not used by it).  Host buffers. */
+int rp_field_mode_curvature(rp_ctx *ctx, const double *dx, const double *dy, const double *dx2, const double *dy2,
+                            const double *dxdy, uint64_t n, double *A, double *B, double *C, double *X, double *Y,
+                            double *Z);
+/* build_interaction_matrix (cfields.pyx:295-395): the field of mode i (origin
+ * rx[i], ry[i]; curvature A, B, C; basis rows X, Y, Z) at test point j (tx[j],
+ * ty[j]) for every pair no further apart than max_spacing, as COO entries
+ * (data: complex (re, im); row = i, col = j) ordered by i, then j.  *count
+ * receives the number of pairs; RP_ERR_CAPACITY (nothing written) when it
+ * exceeds cap.  Host buffers. */
+int rp_field_interaction_matrix(rp_ctx *ctx, const double *rx, const double *ry, uint64_t n_modes, const double *tx,
+                                const double *ty, uint64_t n_points, const double *A, const double *B,
+                                const double *C, const double *X, const double *Y, const double *Z,
+                                double wavelength, double spacing, double max_spacing, double blending, uint64_t cap,
+                                uint64_t *count, double *data, uint64_t *row, uint64_t *col);
+/* apply_mode_curvature (cfields.pyx:398-426): tilts the parabasal rays of
+ * every gausslet of a device collection by its curvature A[i], B[i], C[i]
+ * (host arrays, one per gausslet). */
+int rp_field_apply_mode_curvature(rp_gausslets *gausslets, const double *A, const double *B, const double *C);
 /* One-shot sum_gaussian_modes: create, evaluate, destroy. */
 int rp_field_sum_gaussian_modes(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double *modes,
                                 const double *wavelengths, int64_t n_wavelengths, const double *points,

@@ -199,3 +199,19 @@ def time_field_cpu(rays, modes, wl, points):
     dt = time.perf_counter() - t0
     return {"value": len(rays) * len(points) / dt, "evaluations": int(len(rays) * len(points)), "seconds": dt,
             "cores": len(os.sched_getaffinity(0)), "kind": "reference"}
+
+
+def time_interaction_cpu(rx, ry, tx, ty, A, B, C, X, Y, Z, wavelength, spacing, max_spacing, blending, test_spacing):
+    """The reference's build_interaction_matrix (one thread) in this process:
+    mode-point pairs tested per second.  None without the reference."""
+    if not reference_available():
+        return None
+    _setup_path()
+    import build_ref
+    ref = build_ref.load()
+    a = [np.ascontiguousarray(v, dtype=np.double) for v in (rx, ry, tx, ty, A, B, C, X, Y, Z)]
+    t0 = time.perf_counter()
+    ref.cfields.build_interaction_matrix(*a, wavelength, spacing, max_spacing, blending, test_spacing)
+    dt = time.perf_counter() - t0
+    return {"value": len(rx) * len(tx) / dt, "pairs": int(len(rx) * len(tx)), "seconds": dt, "cores": 1,
+            "kind": "reference"}

@@ -65,6 +65,11 @@ def load():
             lib.rp_oracle_select_intersections.argtypes = [P, I, P, U64, ctypes.c_uint32, P, ctypes.POINTER(U64)]
             lib.rp_oracle_evaluate_modes.argtypes = [P, P, P, P, ctypes.c_int64, I, D, P]
             lib.rp_oracle_sum_gaussian_modes.argtypes = [P, ctypes.c_int64, P, P, P, ctypes.c_int64, D, P]
+            lib.rp_oracle_mode_curvature.argtypes = [P, P, P, P, P, ctypes.c_int64, P, P, P, P, P, P]
+            lib.rp_oracle_interaction_matrix.argtypes = [P, P, ctypes.c_int64, P, P, ctypes.c_int64, P, P, P, P, P, P,
+                                                         D, D, D, D, ctypes.c_int64, P, P, P]
+            lib.rp_oracle_interaction_matrix.restype = ctypes.c_int64
+            lib.rp_oracle_apply_mode_curvature.argtypes = [P, ctypes.c_int64, P, P, P]
             lib.rp_oracle_eval_parabasal.argtypes = [P, P, ctypes.c_int64, I, P, P, P, P, P, ctypes.c_uint32, P]
             _lib = lib
         return _lib
@@ -346,3 +351,45 @@ def sum_gaussian_modes(rays, modes, wavelengths, points, time_ps=0.0):
     lib.rp_oracle_sum_gaussian_modes(r.ctypes.data, len(r), m.ctypes.data, wl.ctypes.data, p.ctypes.data,
                                      p.shape[0], float(time_ps), out.ctypes.data)
     return out
+
+
+def calc_mode_curvature(rx, ry, dx, dy, dx2, dy2, dxdy):
+    """calc_mode_curvature (cfields.pyx:232-290) on the host: (A, B, C, x, y, z)."""
+    lib = load()
+    n = len(rx)
+    a = [np.ascontiguousarray(v, dtype=np.double).reshape(-1) for v in (dx, dy, dx2, dy2, dxdy)]
+    out = [np.empty(n) for _ in range(3)] + [np.empty((n, 3)) for _ in range(3)]
+    lib.rp_oracle_mode_curvature(*[v.ctypes.data for v in a], n, *[o.ctypes.data for o in out])
+    return tuple(out)
+
+
+def build_interaction_matrix(rx, ry, tx, ty, A, B, C, x, y, z, wavelength, spacing, max_spacing, blending,
+                             test_spacing=None):
+    """build_interaction_matrix (cfields.pyx:295-395) on the host:
+    (data, (i, j)) in loop order, sized exactly (test_spacing only sizes the
+    reference's buffer)."""
+    lib = load()
+    n, L = len(rx), len(tx)
+    v = [np.ascontiguousarray(a, dtype=np.double).reshape(-1) for a in (rx, ry, A, B, C)]
+    t = [np.ascontiguousarray(a, dtype=np.double).reshape(-1) for a in (tx, ty)]
+    b = [np.ascontiguousarray(a, dtype=np.double).reshape(-1, 3) for a in (x, y, z)]
+    args = [v[0].ctypes.data, v[1].ctypes.data, n, t[0].ctypes.data, t[1].ctypes.data, L, v[2].ctypes.data,
+            v[3].ctypes.data, v[4].ctypes.data, b[0].ctypes.data, b[1].ctypes.data, b[2].ctypes.data,
+            float(wavelength), float(spacing), float(max_spacing), float(blending)]
+    ct = lib.rp_oracle_interaction_matrix(*args, 0, None, None, None)
+    data = np.zeros(max(ct, 1), np.complex128)
+    xi = np.zeros(max(ct, 1), np.uint64)
+    xj = np.zeros(max(ct, 1), np.uint64)
+    lib.rp_oracle_interaction_matrix(*args, ct, data.ctypes.data, xi.ctypes.data, xj.ctypes.data)
+    return (data[:ct], (xi[:ct], xj[:ct]))
+
+
+def apply_mode_curvature(gausslets, A, B, C):
+    """apply_mode_curvature (cfields.pyx:398-426) on the host: a new
+    gausslet_dtype array with the parabasal directions tilted."""
+    lib = load()
+    from raypier_optics_gb300.ctracer import gausslet_dtype
+    g = np.array(gausslets, dtype=gausslet_dtype, copy=True)
+    a = [np.ascontiguousarray(v, dtype=np.double).reshape(-1) for v in (A, B, C)]
+    lib.rp_oracle_apply_mode_curvature(g.ctypes.data, len(g), *[v.ctypes.data for v in a])
+    return g

@@ -2087,3 +2087,87 @@ int rp_oracle_sum_gaussian_modes(const rp_ray *rays, int64_t n_rays, const doubl
     free(out);
     return 0;
 }
+
+/* calc_mode_curvature (cfields.pyx:232-290): A, B, C and the local bases
+ * x', y', z' (n x 3) from the slopes and second derivatives. */
+void rp_oracle_mode_curvature(const double *dx, const double *dy, const double *dx2, const double *dy2,
+                              const double *dxdy, int64_t n, double *A, double *B, double *C, double *X, double *Y,
+                              double *Z) {
+    for (int64_t i = 0; i < n; i++) {
+        vec c = {-dx[i], -dy[i], 1.0};
+        c = norm_(c);
+        vec b = {0.0, 0.0, 1.0};
+        vec a = norm_(cross_(b, c));
+        b = cross_(c, a);
+        st_v(X + 3 * i, a);
+        st_v(Y + 3 * i, b);
+        st_v(Z + 3 * i, c);
+        double Fz = c.x * dx[i] + c.y * dy[i] + c.z;
+        A[i] = -(a.x * a.x * dx2[i] + 2 * a.x * a.y * dxdy[i] + a.y * a.y * dy2[i]) / Fz;
+        B[i] = -(a.x * b.x * dx2[i] + (a.x * b.y + b.x * a.y) * dxdy[i] + a.y * b.y * dy2[i]) / Fz;
+        C[i] = -(b.x * b.x * dx2[i] + 2 * b.x * b.y * dxdy[i] + b.y * b.y * dy2[i]) / Fz;
+    }
+}
+
+/* build_interaction_matrix (cfields.pyx:295-395): every (mode i, test point j)
+ * pair within max_spacing, in loop order; returns the number of pairs and
+ * writes the first `cap` of them (data as (re, im) pairs). */
+int64_t rp_oracle_interaction_matrix(const double *rx, const double *ry, int64_t n, const double *tx,
+                                     const double *ty, int64_t L, const double *A, const double *B, const double *C,
+                                     const double *X, const double *Y, const double *Z, double wavelength,
+                                     double spacing, double max_spacing, double blending, int64_t cap, double *data,
+                                     uint64_t *row, uint64_t *col) {
+    const double complex rootI = csqrt(I);
+    double phase = 0.0, inv_root_area = 1.0;
+    double k = 2000.0 * M_PI / wavelength;
+    double impart = 2 * (blending * blending) / (k * spacing * spacing);
+    int64_t ct = 0;
+    for (int64_t i = 0; i < n; i++) {
+        vec o = {rx[i], ry[i], 0.0};
+        vec a = ld_v(X + 3 * i), b = ld_v(Y + 3 * i), c = ld_v(Z + 3 * i);
+        double complex _A, _B, _C;
+        __real__ _A = A[i];
+        __real__ _B = B[i];
+        __real__ _C = C[i];
+        __imag__ _A = impart;
+        __imag__ _B = 0;
+        __imag__ _C = impart;
+        double complex detG0 = (_A * _C);
+        for (int64_t j = 0; j < L; j++) {
+            vec pt = {tx[j], ty[j], 0.0};
+            pt = subvv_(pt, o);
+            if (((pt.x * pt.x) + (pt.y * pt.y)) <= (max_spacing * max_spacing)) {
+                if (ct < cap) {
+                    double complex U = calc_mode_U(_A, _B, _C, detG0, pt, a, b, c, k, phase, inv_root_area, rootI);
+                    data[2 * ct] = creal(U);
+                    data[2 * ct + 1] = cimag(U);
+                    row[ct] = (uint64_t)i;
+                    col[ct] = (uint64_t)j;
+                }
+                ct++;
+            }
+        }
+    }
+    return ct;
+}
+
+/* apply_mode_curvature (cfields.pyx:398-426) on gausslet records in place. */
+void rp_oracle_apply_mode_curvature(rp_gausslet *g, int64_t n, const double *A, const double *B, const double *C) {
+    for (int64_t i = 0; i < n; i++) {
+        const rp_ray *ray = &g[i].base_ray;
+        vec z = ld_v(ray->direction);
+        vec x = ld_v(ray->E_vector);
+        vec y = cross_(x, z);
+        vec origin = ld_v(ray->origin);
+        for (int j = 0; j < 6; j++) {
+            rp_para *para = &g[i].para[j];
+            vec r = subvv_(ld_v(para->origin), origin);
+            double px = dotprod_(r, x);
+            double py = dotprod_(r, y);
+            vec shift = multvs_(x, (-A[i] * px - B[i] * py));
+            shift = addvv_(shift, multvs_(y, (-C[i] * py - B[i] * px)));
+            vec d = norm_(addvv_(shift, ld_v(para->direction)));
+            st_v(para->direction, d);
+        }
+    }
+}

@@ -199,6 +199,11 @@ _SIGS = {
     "rp_field_evaluate_modes": (_I, [_P, _P, _P, _P, _P, ctypes.c_uint64, ctypes.c_int32, ctypes.c_double, _P]),
     "rp_field_create": (_I, [_P, _P, ctypes.c_uint64, _P, _P, ctypes.c_int64, ctypes.POINTER(_P)]),
     "rp_field_destroy": (_I, [_P]),
+    "rp_field_mode_curvature": (_I, [_P, _P, _P, _P, _P, _P, ctypes.c_uint64, _P, _P, _P, _P, _P, _P]),
+    "rp_field_interaction_matrix": (_I, [_P, _P, _P, ctypes.c_uint64, _P, _P, ctypes.c_uint64, _P, _P, _P, _P, _P,
+                                         _P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), _P, _P, _P]),
+    "rp_field_apply_mode_curvature": (_I, [_P, _P, _P, _P]),
     "rp_field_evaluate": (_I, [_P, _P, ctypes.c_uint64, ctypes.c_double, _P]),
     "rp_field_evaluate_device": (_I, [_P, _P, ctypes.c_uint64, ctypes.c_double, _P]),
     "rp_field_sum_gaussian_modes": (_I, [_P, _P, ctypes.c_uint64, _P, _P, ctypes.c_int64, _P, ctypes.c_uint64,
@@ -263,6 +268,9 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
             fn.argtypes = args
         _lib = lib
         return lib
+
+
+RP_ERR_CAPACITY = -2  # include/rp_gb300.h: an output buffer is too small
 
 
 def check(status: int, where: str) -> None:

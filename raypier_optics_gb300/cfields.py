@@ -1,11 +1,9 @@
 """Mirror of ``raypier.core.cfields``: Gaussian-mode fitting and E-field
 summation over traced rays / gausslets, on the GPU.
 
-``evaluate_modes`` and ``sum_gaussian_modes`` keep the reference's names,
-arguments and results (cfields.pyx:49-234); the work runs in the sm_103a
-library (include/rp_gb300.h, rp_field_*).  ``calc_mode_curvature`` and
-``apply_mode_curvature`` are small per-ray host routines, restated here with
-numpy.  There is no CPU fallback for the GPU entry points.
+Every function keeps the reference's name, arguments and results
+(cfields.pyx:49-426); the work runs in the sm_103a library
+(include/rp_gb300.h, rp_field_*).  There is no CPU fallback.
 """
 from __future__ import annotations
 
@@ -14,7 +12,7 @@ import ctypes
 import numpy as np
 
 from . import _native, runtime
-from .ctracer import cross, norm, ray_dtype
+from .ctracer import ray_dtype
 
 
 def evaluate_modes(x, y, dx, dy, blending=1.0):
@@ -85,41 +83,65 @@ def sum_gaussian_modes(rays, modes, wavelengths, points, time_ps):
 
 
 def calc_mode_curvature(rx, ry, dx, dy, dx2, dy2, dxdy):
-    """Mode curvature A, B, C and local bases at each point (cfields.pyx:237-290)."""
-    N = len(rx)
-    A, B, C = np.empty(N), np.empty(N), np.empty(N)
-    X, Y, Z = np.empty((N, 3)), np.empty((N, 3)), np.empty((N, 3))
-    for i in range(N):
-        c = norm((-float(dx[i]), -float(dy[i]), 1.0))
-        a = norm(cross((0.0, 0.0, 1.0), c))
-        b = cross(c, a)
-        X[i], Y[i], Z[i] = a, b, c
-        Fz = c[0] * dx[i] + c[1] * dy[i] + c[2]
-        A[i] = -(a[0] * a[0] * dx2[i] + 2 * a[0] * a[1] * dxdy[i] + a[1] * a[1] * dy2[i]) / Fz
-        B[i] = -(a[0] * b[0] * dx2[i] + (a[0] * b[1] + b[0] * a[1]) * dxdy[i] + a[1] * b[1] * dy2[i]) / Fz
-        C[i] = -(b[0] * b[0] * dx2[i] + 2 * b[0] * b[1] * dxdy[i] + b[1] * b[1] * dy2[i]) / Fz
-    return (A, B, C, X, Y, Z)
+    """Wavefront curvature A, B, C and the local bases x', y', z' at each
+    point (cfields.pyx:232-290), on the GPU.  Returns (A, B, C, x, y, z), the
+    last three (N, 3)."""
+    ctx = runtime.get_context()
+    n = len(rx)
+    a = [np.ascontiguousarray(v, dtype=np.double).reshape(-1) for v in (dx, dy, dx2, dy2, dxdy)]
+    if any(v.shape[0] < n for v in a):
+        raise IndexError("Out of bounds on buffer access (axis 0)")
+    out = [np.empty(n) for _ in range(3)] + [np.empty((n, 3)) for _ in range(3)]
+    _native.check(ctx.lib.rp_field_mode_curvature(ctx.handle, *[v.ctypes.data for v in a], n,
+                                                  *[o.ctypes.data for o in out]), "rp_field_mode_curvature")
+    return tuple(out)
+
+
+def build_interaction_matrix(rx, ry, tx, ty, A, B, C, x, y, z, wavelength, spacing, max_spacing, blending,
+                             test_spacing):
+    """The sparse matrix of the field of mode i at test point j for every pair
+    within max_spacing (cfields.pyx:295-395), on the GPU, as the tuple
+    (data, (i, j)) that scipy.sparse.coo_matrix takes, ordered by i then j.
+    The reference sizes its output by an estimate from test_spacing and
+    writes past it when the estimate is short; here the exact count is used."""
+    ctx = runtime.get_context()
+    n, L = len(rx), len(tx)
+    v = [np.ascontiguousarray(a, dtype=np.double).reshape(-1) for a in (rx, ry, A, B, C)]
+    t = [np.ascontiguousarray(a, dtype=np.double).reshape(-1) for a in (tx, ty)]
+    b = [np.ascontiguousarray(a, dtype=np.double).reshape(-1, 3) for a in (x, y, z)]
+    if any(a.shape[0] < n for a in v + b) or t[1].shape[0] < L:
+        raise IndexError("Out of bounds on buffer access (axis 0)")
+    cap = n * (1 + int((7 * max_spacing * max_spacing) / (test_spacing * test_spacing)))
+    count = ctypes.c_uint64()
+    for _ in range(2):
+        data = np.zeros(cap, np.complex128)
+        xi = np.zeros(cap, np.uint)
+        xj = np.zeros(cap, np.uint)
+        st = ctx.lib.rp_field_interaction_matrix(
+            ctx.handle, v[0].ctypes.data, v[1].ctypes.data, n, t[0].ctypes.data, t[1].ctypes.data, L,
+            v[2].ctypes.data, v[3].ctypes.data, v[4].ctypes.data, b[0].ctypes.data, b[1].ctypes.data, b[2].ctypes.data,
+            float(wavelength), float(spacing), float(max_spacing), float(blending), cap, ctypes.byref(count),
+            data.ctypes.data, xi.ctypes.data, xj.ctypes.data)
+        if st == _native.RP_ERR_CAPACITY:
+            cap = count.value  # the estimate was short: once more at the exact size
+            continue
+        _native.check(st, "rp_field_interaction_matrix")
+        ct = count.value
+        return (data[:ct], (xi[:ct], xj[:ct]))
+    _native.check(st, "rp_field_interaction_matrix")
 
 
 def apply_mode_curvature(gc, A, B, C):
     """Tilts each gausslet's parabasal rays by the given wavefront curvature
-    (cfields.pyx:397-426)."""
-    arr = gc.copy_as_array()
-    for i in range(len(arr)):
-        ray = arr[i]['base_ray']
-        z = tuple(float(v) for v in ray['direction'])
-        x = tuple(float(v) for v in ray['E_vector'])
-        y = cross(x, z)
-        for j in range(6):
-            para = arr[i]['para_rays'][j]
-            r = tuple(float(para['origin'][k] - ray['origin'][k]) for k in range(3))
-            px = r[0] * x[0] + r[1] * x[1] + r[2] * x[2]
-            py = r[0] * y[0] + r[1] * y[1] + r[2] * y[2]
-            sx = (-A[i] * px - B[i] * py)
-            sy = (-C[i] * py - B[i] * px)
-            shift = tuple(x[k] * sx + y[k] * sy for k in range(3))
-            d = tuple(shift[k] + float(para['direction'][k]) for k in range(3))
-            arr[i]['para_rays'][j]['direction'] = norm(d)
-    new = type(gc).from_array(arr)
-    gc._host, gc._n = new._host, new._n
-    gc._mark_host_written()
+    (cfields.pyx:397-426), on the GPU, in place."""
+    ctx = runtime.get_context()
+    n = gc.n_rays
+    a = [np.ascontiguousarray(v, dtype=np.double).reshape(-1) for v in (A, B, C)]
+    if any(v.shape[0] < n for v in a):
+        raise IndexError("Out of bounds on buffer access (axis 0)")
+    if n == 0:
+        return
+    dev = gc._device(ctx)
+    _native.check(ctx.lib.rp_field_apply_mode_curvature(dev.handle, *[v.ctypes.data for v in a]),
+                  "rp_field_apply_mode_curvature")
+    gc._mark_device_written()

@@ -960,13 +960,6 @@ int rp_trace_rays_host(rp_ctx *ctx, rp_scene *s, const void *in_records, uint64_
 }
 
 // ---- Gausslets ------------------------------------------------------------------
-struct rp_gausslets {
-    rp_ctx *ctx;
-    rp_rays *base;   // base rays; base->n is the gausslet count
-    double *para;    // RP_PARA_ARRAYS arrays of cap doubles
-    size_t para_bytes;
-    uint64_t cap;
-};
 
 int rp_gausslets_alloc(rp_ctx *ctx, uint64_t cap, rp_gausslets **out) {
     if (!ctx || !out) return RP_ERR_INVALID;

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <new>
 
 #include "rp_internal.h"
@@ -205,6 +206,119 @@ __global__ void __launch_bounds__(RP_FIELD_BLOCK) field_sum_kernel(const double 
     }
 }
 
+// ---- decomposition helpers (cfields.pyx:232-426) -------------------------------
+// calc_mode_curvature (cfields.pyx:232-290): one thread per point; X, Y, Z
+// are n x 3 (the local basis x', y', z').
+__global__ void mode_curvature_kernel(const double *dx, const double *dy, const double *dx2, const double *dy2,
+                                      const double *dxdy, unsigned long long n, double *A, double *B, double *C,
+                                      double *X, double *Y, double *Z) {
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const v3 c = normv(mkv(-dx[i], -dy[i], 1.0));
+    const v3 a = normv(crossv(mkv(0.0, 0.0, 1.0), c));
+    const v3 b = crossv(c, a);
+    X[3 * i] = a.x; X[3 * i + 1] = a.y; X[3 * i + 2] = a.z;
+    Y[3 * i] = b.x; Y[3 * i + 1] = b.y; Y[3 * i + 2] = b.z;
+    Z[3 * i] = c.x; Z[3 * i + 1] = c.y; Z[3 * i + 2] = c.z;
+    const double Fz = c.x * dx[i] + c.y * dy[i] + c.z;
+    A[i] = -(a.x * a.x * dx2[i] + 2 * a.x * a.y * dxdy[i] + a.y * a.y * dy2[i]) / Fz;
+    B[i] = -(a.x * b.x * dx2[i] + (a.x * b.y + b.x * a.y) * dxdy[i] + a.y * b.y * dy2[i]) / Fz;
+    C[i] = -(b.x * b.x * dx2[i] + 2 * b.x * b.y * dxdy[i] + b.y * b.y * dy2[i]) / Fz;
+}
+
+// The pair test of build_interaction_matrix (cfields.pyx:376-380): the test
+// point relative to the mode's origin, both in the decomposition plane.
+__device__ __forceinline__ bool im_in_range(double ox, double oy, double tx, double ty, double ms2) {
+    const double px = tx - ox, py = ty - oy;
+    return (px * px) + (py * py) <= ms2;
+}
+
+struct IMArgs {
+    const double *rx, *ry, *tx, *ty, *A, *B, *C, *X, *Y, *Z;
+    unsigned long long n, L;
+    double ms2, k, impart;
+    unsigned *counts;                  // [n] pairs of each mode
+    const unsigned long long *offsets; // [n] exclusive prefix of counts
+    cx *data;                          // [cap] entries
+    unsigned long long *row, *col;
+    unsigned long long cap;
+};
+
+// One warp per mode i counts the test points within reach, 32 at a time.
+__global__ void __launch_bounds__(256) interaction_count_kernel(IMArgs M) {
+    const unsigned long long i = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (i >= M.n) return;  // whole warps
+    const double ox = M.rx[i], oy = M.ry[i];
+    unsigned c = 0;
+    for (unsigned long long j = lane; j < M.L; j += 32) c += im_in_range(ox, oy, M.tx[j], M.ty[j], M.ms2) ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) M.counts[i] = c;
+}
+
+// One warp per mode i writes its entries from offsets[i] on, in ascending j
+// (ballot + prefix popcount), each the calc_mode_U of the mode at the test
+// point (cfields.pyx:350-393: curvature as the real parts, the 1/e^2 width
+// as the imaginary parts of A and C, detG0 = A C, phase 0, unit area).
+__global__ void __launch_bounds__(256) interaction_fill_kernel(IMArgs M) {
+    const unsigned long long i = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (i >= M.n) return;  // whole warps
+    double p[RP_MODE_WORDS];
+    p[0] = M.rx[i]; p[1] = M.ry[i]; p[2] = 0.0;
+    p[3] = M.X[3 * i]; p[4] = M.X[3 * i + 1]; p[5] = M.X[3 * i + 2];
+    p[6] = M.Y[3 * i]; p[7] = M.Y[3 * i + 1]; p[8] = M.Y[3 * i + 2];
+    p[9] = M.Z[3 * i]; p[10] = M.Z[3 * i + 1]; p[11] = M.Z[3 * i + 2];
+    const cx A = mkc(M.A[i], M.impart), B = mkc(M.B[i], 0.0), C = mkc(M.C[i], M.impart);
+    const cx G = cmul(A, C);
+    p[12] = A.x; p[13] = A.y; p[14] = B.x; p[15] = B.y; p[16] = C.x; p[17] = C.y;
+    p[18] = G.x; p[19] = G.y;
+    p[20] = M.k; p[21] = 0.0;
+    p[22] = 0.0;  // phase
+    p[23] = 1.0;  // inv_root_area
+    unsigned long long pos = M.offsets[i];
+    for (unsigned long long j0 = 0; j0 < M.L; j0 += 32) {
+        const unsigned long long j = j0 + lane;
+        const bool hit = j < M.L && im_in_range(p[0], p[1], M.tx[j], M.ty[j], M.ms2);
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const unsigned long long q = pos + __popc(m & ((1u << lane) - 1u));
+            if (q < M.cap) {
+                M.data[q] = mode_U(p, M.tx[j], M.ty[j], 0.0);
+                M.row[q] = i;
+                M.col[q] = j;
+            }
+        }
+        pos += __popc(m);
+    }
+}
+
+// apply_mode_curvature (cfields.pyx:398-426): each parabasal direction of
+// gausslet i tilted by the curvature A, B, C in the base ray's (E, E x d)
+// frame and renormalised.
+__global__ void apply_curvature_kernel(RaySoA base, double *para, unsigned long long cap, unsigned long long n,
+                                       const double *A, const double *B, const double *C) {
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const v3 z = mkv(base.dx[i], base.dy[i], base.dz[i]);
+    const v3 x = mkv(base.ex[i], base.ey[i], base.ez[i]);
+    const v3 y = crossv(x, z);
+    const v3 o = mkv(base.ox[i], base.oy[i], base.oz[i]);
+    const double a = A[i], b = B[i], c = C[i];
+    for (int j = 0; j < 6; j++) {
+        double *f = para + (unsigned long long)j * RP_PARA_FIELDS * cap + i;  // field k at f[k * cap]
+        const v3 r = subv(mkv(f[0], f[cap], f[2 * cap]), o);
+        const double px = dotv(r, x), py = dotv(r, y);
+        v3 shift = mulvs(x, ((-a) * px) - (b * py));
+        shift = addv(shift, mulvs(y, ((-c) * py) - (b * px)));
+        const v3 d = normv(addv(shift, mkv(f[3 * cap], f[4 * cap], f[5 * cap])));
+        f[3 * cap] = d.x;
+        f[4 * cap] = d.y;
+        f[5 * cap] = d.z;
+    }
+}
+
 }  // namespace rp
 
 using namespace rp;
@@ -372,6 +486,156 @@ int rp_field_evaluate(rp_field *f, const double *points, uint64_t n_points, doub
     }
     rp__ctx_free(ctx, blk, got);
     return rc;
+}
+
+int rp_field_mode_curvature(rp_ctx *ctx, const double *dx, const double *dy, const double *dx2, const double *dy2,
+                            const double *dxdy, uint64_t n, double *A, double *B, double *C, double *X, double *Y,
+                            double *Z) {
+    if (!ctx || (n && (!dx || !dy || !dx2 || !dy2 || !dxdy || !A || !B || !C || !X || !Y || !Z)))
+        return RP_ERR_INVALID;
+    if (n == 0) return RP_OK;
+    FCK(cudaSetDevice(ctx->device));
+    const size_t v = align_up((size_t)n * sizeof(double)), v3b = align_up((size_t)n * 3 * sizeof(double));
+    unsigned char *blk = nullptr;
+    size_t got = 0;
+    int rc = rp__ctx_alloc(ctx, (void **)&blk, 8 * v + 3 * v3b, &got);
+    if (rc) return rc;
+    double *d[8];
+    for (int k = 0; k < 8; k++) d[k] = (double *)(blk + k * v);
+    double *dX = (double *)(blk + 8 * v), *dY = (double *)(blk + 8 * v + v3b), *dZ = (double *)(blk + 8 * v + 2 * v3b);
+    const double *h[5] = {dx, dy, dx2, dy2, dxdy};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 5 && e == cudaSuccess; k++)
+        e = cudaMemcpyAsync(d[k], h[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        mode_curvature_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(d[0], d[1], d[2], d[3], d[4], n,
+                                                                                   d[5], d[6], d[7], dX, dY, dZ);
+        e = cudaGetLastError();
+    }
+    double *out[6] = {A, B, C, X, Y, Z};
+    const double *src[6] = {d[5], d[6], d[7], dX, dY, dZ};
+    for (int k = 0; k < 6 && e == cudaSuccess; k++)
+        e = cudaMemcpyAsync(out[k], src[k], (size_t)n * (k < 3 ? 1 : 3) * sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    rp__ctx_free(ctx, blk, got);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "rp_field_mode_curvature");
+    return RP_OK;
+}
+
+int rp_field_interaction_matrix(rp_ctx *ctx, const double *rx, const double *ry, uint64_t n_modes, const double *tx,
+                                const double *ty, uint64_t n_points, const double *A, const double *B,
+                                const double *C, const double *X, const double *Y, const double *Z,
+                                double wavelength, double spacing, double max_spacing, double blending, uint64_t cap,
+                                uint64_t *count, double *data, uint64_t *row, uint64_t *col) {
+    if (!ctx || !count || (n_modes && (!rx || !ry || !A || !B || !C || !X || !Y || !Z)) || (n_points && (!tx || !ty)))
+        return RP_ERR_INVALID;
+    if (cap && (!data || !row || !col)) return RP_ERR_INVALID;
+    *count = 0;
+    if (n_modes == 0 || n_points == 0) return RP_OK;
+    FCK(cudaSetDevice(ctx->device));
+    const size_t vn = align_up((size_t)n_modes * sizeof(double)), v3n = align_up((size_t)n_modes * 3 * sizeof(double));
+    const size_t vl = align_up((size_t)n_points * sizeof(double));
+    const size_t cb = align_up((size_t)n_modes * sizeof(unsigned)), ob = align_up((size_t)n_modes * 8);
+    const size_t in_bytes = 5 * vn + 3 * v3n + 2 * vl + cb + ob + 256;
+    unsigned char *blk = nullptr;
+    size_t got = 0;
+    int rc = rp__ctx_alloc(ctx, (void **)&blk, in_bytes, &got);
+    if (rc) return rc;
+    IMArgs M;
+    memset(&M, 0, sizeof M);
+    unsigned char *q = blk;
+    auto take = [&](size_t b) { unsigned char *r = q; q += b; return r; };
+    double *drx = (double *)take(vn), *dry = (double *)take(vn), *dA = (double *)take(vn), *dB = (double *)take(vn),
+           *dC = (double *)take(vn);
+    double *dX = (double *)take(v3n), *dY = (double *)take(v3n), *dZ = (double *)take(v3n);
+    double *dtx = (double *)take(vl), *dty = (double *)take(vl);
+    M.counts = (unsigned *)take(cb);
+    unsigned long long *offs = (unsigned long long *)take(ob);
+    unsigned long long *total = (unsigned long long *)take(256);
+    struct { double *d; const double *h; size_t b; } up[] = {
+        {drx, rx, (size_t)n_modes * 8}, {dry, ry, (size_t)n_modes * 8}, {dA, A, (size_t)n_modes * 8},
+        {dB, B, (size_t)n_modes * 8},   {dC, C, (size_t)n_modes * 8},   {dX, X, (size_t)n_modes * 24},
+        {dY, Y, (size_t)n_modes * 24},  {dZ, Z, (size_t)n_modes * 24},  {dtx, tx, (size_t)n_points * 8},
+        {dty, ty, (size_t)n_points * 8}};
+    cudaError_t e = cudaSuccess;
+    for (auto &u : up)
+        if (e == cudaSuccess) e = cudaMemcpyAsync(u.d, u.h, u.b, cudaMemcpyHostToDevice, ctx->stream);
+    M.rx = drx; M.ry = dry; M.A = dA; M.B = dB; M.C = dC; M.X = dX; M.Y = dY; M.Z = dZ; M.tx = dtx; M.ty = dty;
+    M.n = n_modes;
+    M.L = n_points;
+    M.ms2 = max_spacing * max_spacing;
+    M.k = 2000.0 * 3.14159265358979323846 / wavelength;
+    M.impart = 2 * (blending * blending) / (M.k * spacing * spacing);
+    M.offsets = offs;
+    const unsigned grid = (unsigned)((n_modes * 32 + 255) / 256);
+    if (e == cudaSuccess) {
+        interaction_count_kernel<<<grid, 256, 0, ctx->stream>>>(M);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = launch_count_scan(M.counts, n_modes, offs, total, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned, total, 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    const uint64_t n_pairs = ctx->h_pinned[0];
+    if (e == cudaSuccess) *count = n_pairs;
+    if (e == cudaSuccess && n_pairs > cap) {
+        rp__ctx_free(ctx, blk, got);
+        rp__set_error("%llu matrix entries do not fit %llu", (unsigned long long)n_pairs, (unsigned long long)cap);
+        return RP_ERR_CAPACITY;
+    }
+    unsigned char *ob2 = nullptr;
+    size_t got2 = 0;
+    const size_t db = align_up((size_t)n_pairs * sizeof(cx)), ib = align_up((size_t)n_pairs * 8);
+    if (e == cudaSuccess && n_pairs) {
+        rc = rp__ctx_alloc(ctx, (void **)&ob2, db + 2 * ib, &got2);
+        if (rc) {
+            rp__ctx_free(ctx, blk, got);
+            return rc;
+        }
+        M.data = (cx *)ob2;
+        M.row = (unsigned long long *)(ob2 + db);
+        M.col = (unsigned long long *)(ob2 + db + ib);
+        M.cap = n_pairs;
+        interaction_fill_kernel<<<grid, 256, 0, ctx->stream>>>(M);
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(data, M.data, (size_t)n_pairs * sizeof(cx), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(row, M.row, (size_t)n_pairs * 8, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(col, M.col, (size_t)n_pairs * 8, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
+    if (ob2) rp__ctx_free(ctx, ob2, got2);
+    rp__ctx_free(ctx, blk, got);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "rp_field_interaction_matrix");
+    return RP_OK;
+}
+
+int rp_field_apply_mode_curvature(rp_gausslets *g, const double *A, const double *B, const double *C) {
+    if (!g || !g->base) return RP_ERR_INVALID;
+    const uint64_t n = g->base->n;
+    if (n && (!A || !B || !C)) return RP_ERR_INVALID;
+    if (n == 0) return RP_OK;
+    rp_ctx *ctx = g->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    const size_t v = align_up((size_t)n * sizeof(double));
+    unsigned char *blk = nullptr;
+    size_t got = 0;
+    int rc = rp__ctx_alloc(ctx, (void **)&blk, 3 * v, &got);
+    if (rc) return rc;
+    double *d[3] = {(double *)blk, (double *)(blk + v), (double *)(blk + 2 * v)};
+    const double *h[3] = {A, B, C};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 3 && e == cudaSuccess; k++)
+        e = cudaMemcpyAsync(d[k], h[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        apply_curvature_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(g->base->soa, g->para, g->cap, n,
+                                                                                    d[0], d[1], d[2]);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    rp__ctx_free(ctx, blk, got);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "rp_field_apply_mode_curvature");
+    return RP_OK;
 }
 
 int rp_field_sum_gaussian_modes(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double *modes,

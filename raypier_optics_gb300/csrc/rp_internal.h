@@ -54,6 +54,16 @@ struct rp_scene {
     std::vector<rp_facelist> host_lists;
 };
 
+// A device gausslet collection: base rays plus the parabasal rays' fields,
+// field f of parabasal ray j of gausslet i at para[(j * RP_PARA_FIELDS + f) * cap + i].
+struct rp_gausslets {
+    rp_ctx *ctx;
+    struct rp_rays *base;  // base rays; base->n is the gausslet count
+    double *para;          // RP_PARA_ARRAYS arrays of cap doubles
+    size_t para_bytes;
+    uint64_t cap;
+};
+
 struct rp_rays {
     rp_ctx *ctx;
     uint64_t cap, n;

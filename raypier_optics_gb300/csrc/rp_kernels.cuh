@@ -72,6 +72,9 @@ cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem);
 // slots (one block per RP_SUB_PER_BLOCK sub-tiles)
 cudaError_t launch_tile_scan(const GenArgs &a, unsigned long long n_sub, cudaStream_t st);
 cudaError_t launch_place_children(const GenArgs &a, unsigned long long n_sub, cudaStream_t st);
+// exclusive prefix of n unsigned counts (one block) and their total
+cudaError_t launch_count_scan(const unsigned *counts, unsigned long long n, unsigned long long *offsets,
+                              unsigned long long *total, cudaStream_t st);
 // the gather map of the children instead of their copy: map[offset + j] = the
 // arena slot of the sub-tile's child j (the next generation reads through it)
 cudaError_t launch_child_map(const GenArgs &a, unsigned long long n_sub, unsigned *map, unsigned long long map_cap,

@@ -253,6 +253,12 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *counts,
     if (threadIdx.x == 0) *total = s_warp[31];
 }
 
+cudaError_t launch_count_scan(const unsigned *counts, unsigned long long n, unsigned long long *offsets,
+                              unsigned long long *total, cudaStream_t st) {
+    tile_scan_kernel<<<1, 1024, 0, st>>>(counts, n, offsets, total);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tile_scan(const GenArgs &a, unsigned long long n_sub, cudaStream_t st) {
     tile_scan_kernel<<<1, 1024, 0, st>>>(a.tile_counts, n_sub, a.tile_offsets, a.out_count);
     return cudaGetLastError();

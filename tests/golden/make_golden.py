@@ -11,6 +11,7 @@ Run in a container that has the reference sources and Cython:
     python tests/golden/make_golden.py --gausslets   # only the Gausslet cases
     python tests/golden/make_golden.py --capture     # only the post-trace capture case
     python tests/golden/make_golden.py --fields      # only the E-field summation cases
+    python tests/golden/make_golden.py --fields2     # only the decomposition helpers of cfields
 
 Every fixture stores the scene description (the JSON spec understood by
 raypier_optics_gb300.workloads.build_scene), the inputs, and the reference's
@@ -830,6 +831,53 @@ def field_cases(ref, out_dir):
     np.savez_compressed(os.path.join(out_dir, "units_fields.npz"), **u)
 
 
+def field_decomp_cases(ref, out_dir):
+    """The decomposition helpers of cfields.pyx: calc_mode_curvature on random
+    slopes and second derivatives, build_interaction_matrix of modes on a
+    hexagonal lattice against a finer square grid of test points (its output
+    buffer estimate, 176 entries per mode, covers the ~80 pairs per mode), and
+    apply_mode_curvature on a gausslet beam."""
+    rdt = ref.ctracer.ray_dtype
+    rng = np.random.Generator(np.random.PCG64(RNG_SEED + 311))
+    u = {}
+    n = 40
+    dx, dy = rng.normal(0, 0.05, n), rng.normal(0, 0.05, n)
+    dx2, dy2, dxdy = rng.normal(0, 0.02, n), rng.normal(0, 0.02, n), rng.normal(0, 0.01, n)
+    rx, ry = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    u.update(mc_rx=rx, mc_ry=ry, mc_dx=dx, mc_dy=dy, mc_dx2=dx2, mc_dy2=dy2, mc_dxdy=dxdy)
+    for k, v in zip("ABCXYZ", ref.cfields.calc_mode_curvature(rx, ry, dx, dy, dx2, dy2, dxdy)):
+        u["mc_" + k] = np.asarray(v)
+    # interaction matrix: modes 0.1 mm apart, test points every 0.05 mm
+    rays, _ = hex_field(rdt, 0.6, 0.1)
+    mx, my = rays['origin'][:, 0].copy(), rays['origin'][:, 1].copy()
+    m = len(mx)
+    A, B, C, X, Y, Z = ref.cfields.calc_mode_curvature(mx, my, rng.normal(0, 0.02, m), rng.normal(0, 0.02, m),
+                                                       rng.normal(0, 0.5, m), rng.normal(0, 0.5, m),
+                                                       rng.normal(0, 0.2, m))
+    g = np.linspace(-0.7, 0.7, 29)
+    tx, ty = [v.reshape(-1).copy() for v in np.meshgrid(g, g)]
+    args = dict(wavelength=0.6, spacing=0.1, max_spacing=0.25, blending=1.0, test_spacing=0.05)
+    data, (xi, xj) = ref.cfields.build_interaction_matrix(mx, my, tx, ty, np.asarray(A), np.asarray(B),
+                                                           np.asarray(C), np.asarray(X), np.asarray(Y),
+                                                           np.asarray(Z), args["wavelength"], args["spacing"],
+                                                           args["max_spacing"], args["blending"],
+                                                           args["test_spacing"])
+    u.update(im_rx=mx, im_ry=my, im_tx=tx, im_ty=ty, im_A=np.asarray(A), im_B=np.asarray(B), im_C=np.asarray(C),
+             im_X=np.asarray(X), im_Y=np.asarray(Y), im_Z=np.asarray(Z),
+             im_args=np.array([args[k] for k in ("wavelength", "spacing", "max_spacing", "blending",
+                                                   "test_spacing")]),
+             im_data=np.asarray(data), im_i=np.asarray(xi).astype(np.uint64), im_j=np.asarray(xj).astype(np.uint64))
+    # apply_mode_curvature on a gausslet beam
+    beam, _ = hex_field(rdt, 2.0, 0.4)
+    gl = gausslets_from_rays(ref, beam, np.array([0.6]), 0.25, 0.0)
+    k = len(gl)
+    cA, cB, cC = rng.normal(0, 0.01, k), rng.normal(0, 0.005, k), rng.normal(0, 0.01, k)
+    gc = ref.ctracer.GaussletCollection.from_array(gl.copy())
+    ref.cfields.apply_mode_curvature(gc, cA, cB, cC)
+    u.update(ac_gausslets=gl, ac_A=cA, ac_B=cB, ac_C=cC, ac_out=gc.copy_as_array())
+    np.savez_compressed(os.path.join(out_dir, "units_fields2.npz"), **u)
+
+
 def lens_case(ref, out_dir):
     """Configuration 4: the perturbed eight-surface lens as an ordinary scene
     (AsphericFace + DielectricMaterial, image plane), 64 rays of the 262,144-ray
@@ -858,5 +906,7 @@ if __name__ == "__main__":
         capture_cases(build_ref.load(), HERE)
     elif sys.argv[1:] == ["--fields"]:
         field_cases(build_ref.load(), HERE)
+    elif sys.argv[1:] == ["--fields2"]:
+        field_decomp_cases(build_ref.load(), HERE)
     else:
         main()
