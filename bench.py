@@ -343,7 +343,7 @@ def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, s
     _native.check(lib.rp_host_alloc(out_cap * 188, ctypes.byref(pin_out)), "rp_host_alloc")
     ctypes.memmove(pin_in, np.ascontiguousarray(rays).ctypes.data, n * 188)
     offs = (ctypes.c_uint64 * (max_gens + 1))()
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(1, args.steps)
 
     def e2e_step(st):
         ng = ctypes.c_int32(0)
@@ -359,8 +359,11 @@ def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, s
     est = _native.Stats()
     t0 = time.perf_counter()
     d2h = 0
+    step_s = []
     for _ in range(e2e_steps):
-        d2h += e2e_step(est) * 188
+        ts = time.perf_counter()
+        d2h += e2e_step(est) * 188  # the call returns once its downloads have landed
+        step_s.append(time.perf_counter() - ts)
     ctx.synchronize()
     e2e_s = time.perf_counter() - t0
     if dist:
@@ -371,6 +374,7 @@ def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, s
     e2e_value = (est.rays_in * world) / e2e_s
     lib.rp_host_free(pin_in)
     lib.rp_host_free(pin_out)
+    run_e2e.step_ms = [1000.0 * t for t in step_s]
     return e2e_value, d2h, e2e_steps
 
 
@@ -575,7 +579,9 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
                                  f"host wall {1000.0 * wall / args.steps:.2f} ms/step"},
             "e2e": ({"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 188,
                      "d2h_bytes_per_step": int(d2h / e2e_steps), "steps": e2e_steps,
-                     "api": "rp_trace_rays_host (pinned host records in and out)"} if e2e_value else None),
+                     "api": "rp_trace_rays_host (pinned host records in and out)",
+                     "step_ms": {"min": min(run_e2e.step_ms), "median": statistics.median(run_e2e.step_ms),
+                                 "max": max(run_e2e.step_ms)}} if e2e_value else None),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": NCU_TRAFFIC_PER_RAY[kernel] * stats.rays_in / max(stats.generations, 1),

@@ -37,13 +37,27 @@ static void pool_release_all(rp_ctx *ctx) {
     ctx->pooled = 0;
 }
 
+// Pool size classes: eight per octave above 4 KB (a block is at most 12.5 %
+// larger than its request).  A block is reused only for a request of its own
+// class, so a repeated sequence of requests (one trace after another) finds
+// its blocks again instead of taking each other's and falling through to
+// cudaMalloc, whose host-side wait stalls the stream.
+static size_t size_class(size_t bytes) {
+    if (bytes <= 4096) return 4096;
+    const int e = 63 - __builtin_clzll((unsigned long long)(bytes - 1));  // 2^e < bytes <= 2^(e+1)
+    const size_t step = ((size_t)1 << e) >> 3;
+    return (bytes + step - 1) / step * step;
+}
+
 static int ctx_alloc(rp_ctx *ctx, void **p, size_t bytes, size_t *got) {
-    bytes = bytes ? bytes : 16;
+    bytes = size_class(bytes ? bytes : 16);
     *got = bytes;
     int best = -1;
     for (size_t k = 0; k < ctx->pool.size(); k++) {
-        size_t b = ctx->pool[k].bytes;
-        if (b >= bytes && b <= 2 * bytes && (best < 0 || b < ctx->pool[best].bytes)) best = (int)k;
+        if (ctx->pool[k].bytes == bytes) {
+            best = (int)k;
+            break;
+        }
     }
     if (best >= 0) {
         *p = ctx->pool[best].p;
@@ -75,7 +89,7 @@ static int ctx_alloc(rp_ctx *ctx, void **p, size_t bytes, size_t *got) {
 // with (pool blocks keep their own size).
 static void ctx_free(rp_ctx *ctx, void *p, size_t bytes) {
     if (!p) return;
-    bytes = bytes ? bytes : 16;
+    bytes = size_class(bytes ? bytes : 16);
     ctx->in_use -= bytes;
     ctx->pool.push_back(PoolBlock{p, bytes});
     ctx->pooled += bytes;
@@ -123,7 +137,8 @@ int rp_ctx_create(int device, uint64_t hbm_budget, rp_ctx **out) {
     c->device = device;
     c->budget = hbm_budget;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_pinned, 8 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&c->h_pinned, 8 * sizeof(unsigned long long), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&c->d_pinned, c->h_pinned, 0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e != cudaSuccess) {
@@ -650,7 +665,10 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
         if (rc) return rc;
     }
     unsigned char *sc = ctx->scratch;
-    CK(cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream));
+    {
+        cudaError_t ez = launch_zero_words((unsigned long long *)sc, SCRATCH_HDR / 8, ctx->stream);
+        if (ez != cudaSuccess) return cuda_fail(ez, "counter clear");
+    }
     memset(&a, 0, sizeof a);
     a.in = lk.src ? lk.src->soa : in->soa;
     a.in_map = lk.src ? lk.in_map : nullptr;
@@ -691,7 +709,8 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
             if (e != cudaSuccess) return cuda_fail(e, "child map launch");
         }
     }
-    CK(cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    e = launch_copy_words((const unsigned long long *)sc, ctx->d_pinned, 5, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "counter read-back");
     return RP_OK;
 }
 
@@ -709,7 +728,7 @@ static int finish_gen(rp_ctx *ctx, int emit, rp_stats *st, uint64_t n_in, uint64
         st->hits += hits;
         st->terminated += term;
         st->kernel_ms += ms;
-        st->launches += emit ? 3 : 1;  // generation, tile scan, placement
+        st->launches += emit ? 5 : 3;  // counter clear, generation, [tile scan, map or placement,] read-back
         st->generations += 1;
     }
     *count = emit ? cnt : 0;

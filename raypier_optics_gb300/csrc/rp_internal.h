@@ -34,6 +34,7 @@ struct rp_ctx {
     unsigned char *scratch;
     size_t scratch_bytes;
     unsigned long long *h_pinned;  // 8 words of pinned host memory for small read-backs
+    unsigned long long *d_pinned;  // h_pinned's device address (kernels store to it directly)
     cudaEvent_t ev0, ev1;
     cudaStream_t copy_stream;      // downloads that overlap the next generation (created on first use)
 };

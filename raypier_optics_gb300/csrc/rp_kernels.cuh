@@ -79,6 +79,9 @@ cudaError_t launch_count_scan(const unsigned *counts, unsigned long long n, unsi
 // arena slot of the sub-tile's child j (the next generation reads through it)
 cudaError_t launch_child_map(const GenArgs &a, unsigned long long n_sub, unsigned *map, unsigned long long map_cap,
                              cudaStream_t st);
+// at most 32 words: a copy by SM stores (dst may be mapped host memory) and a clear
+cudaError_t launch_copy_words(const unsigned long long *src, unsigned long long *dst, int n, cudaStream_t st);
+cudaError_t launch_zero_words(unsigned long long *dst, int n, cudaStream_t st);
 cudaError_t launch_aos_to_soa(const void *aos, RaySoA soa, unsigned long long n, cudaStream_t st);
 cudaError_t launch_soa_to_aos(RaySoA soa, void *aos, unsigned long long n, cudaStream_t st);
 cudaError_t launch_dispersion_table(const rp_dispersion *curves, int n_curves, const double *aux,

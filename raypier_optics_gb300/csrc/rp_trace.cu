@@ -317,6 +317,28 @@ cudaError_t launch_child_map(const GenArgs &a, unsigned long long n_sub, unsigne
     return cudaGetLastError();
 }
 
+// ---- small copies without a copy engine ----------------------------------------
+// A generation's counters go to the host by SM stores into mapped page-locked
+// memory, and the counter block is cleared by a kernel: copies and fills on
+// the stream would queue on a copy engine behind the bulk downloads of
+// earlier generations and hold the trace up.
+__global__ void copy_words_kernel(const unsigned long long *src, unsigned long long *dst, int n) {
+    if ((int)threadIdx.x < n) dst[threadIdx.x] = src[threadIdx.x];
+    __threadfence_system();
+}
+__global__ void zero_words_kernel(unsigned long long *dst, int n) {
+    if ((int)threadIdx.x < n) dst[threadIdx.x] = 0ull;
+}
+
+cudaError_t launch_copy_words(const unsigned long long *src, unsigned long long *dst, int n, cudaStream_t st) {
+    copy_words_kernel<<<1, 32, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_zero_words(unsigned long long *dst, int n, cudaStream_t st) {
+    zero_words_kernel<<<1, 32, 0, st>>>(dst, n);
+    return cudaGetLastError();
+}
+
 // ---- AoS <-> SoA ----------------------------------------------------------
 // The packed 188-byte record (include/rp_gb300.h rp_ray) is not 16-byte
 // aligned per ray, but 128 consecutive records (24,064 bytes) are when the
