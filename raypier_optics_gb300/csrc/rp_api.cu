@@ -37,27 +37,16 @@ static void pool_release_all(rp_ctx *ctx) {
     ctx->pooled = 0;
 }
 
-// Pool size classes: eight per octave above 4 KB (a block is at most 12.5 %
-// larger than its request).  A block is reused only for a request of its own
-// class, so a repeated sequence of requests (one trace after another) finds
-// its blocks again instead of taking each other's and falling through to
-// cudaMalloc, whose host-side wait stalls the stream.
-static size_t size_class(size_t bytes) {
-    if (bytes <= 4096) return 4096;
-    const int e = 63 - __builtin_clzll((unsigned long long)(bytes - 1));  // 2^e < bytes <= 2^(e+1)
-    const size_t step = ((size_t)1 << e) >> 3;
-    return (bytes + step - 1) / step * step;
-}
-
+// Best fit among the pooled blocks at most twice the request.  (Blocks kept
+// to exact size classes made the job server's lanes allocate and trim far
+// more often: p50 latency 4.9 instead of 3.2 ms.)
 static int ctx_alloc(rp_ctx *ctx, void **p, size_t bytes, size_t *got) {
-    bytes = size_class(bytes ? bytes : 16);
+    bytes = bytes ? bytes : 16;
     *got = bytes;
     int best = -1;
     for (size_t k = 0; k < ctx->pool.size(); k++) {
-        if (ctx->pool[k].bytes == bytes) {
-            best = (int)k;
-            break;
-        }
+        size_t b = ctx->pool[k].bytes;
+        if (b >= bytes && b <= 2 * bytes && (best < 0 || b < ctx->pool[best].bytes)) best = (int)k;
     }
     if (best >= 0) {
         *p = ctx->pool[best].p;
@@ -89,7 +78,7 @@ static int ctx_alloc(rp_ctx *ctx, void **p, size_t bytes, size_t *got) {
 // with (pool blocks keep their own size).
 static void ctx_free(rp_ctx *ctx, void *p, size_t bytes) {
     if (!p) return;
-    bytes = size_class(bytes ? bytes : 16);
+    bytes = bytes ? bytes : 16;
     ctx->in_use -= bytes;
     ctx->pool.push_back(PoolBlock{p, bytes});
     ctx->pooled += bytes;
