@@ -77,7 +77,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="rays in the CPU-baseline sample")
     ap.add_argument("--no-serving", action="store_true", help="skip the job-server stream (configuration 5)")
     ap.add_argument("--serving-jobs", type=int, default=10000, help="jobs in the served stream")
-    ap.add_argument("--serving-lanes", type=int, default=8)
+    ap.add_argument("--serving-lanes", type=int, default=4,
+                    help="server lanes (p99 measured 44 / 60 / 108 ms at 4 / 8 / 16 lanes)")
     ap.add_argument("--serving-baseline-jobs", type=int, default=500,
                     help="jobs of the same stream run one at a time through the plain FP64 path")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-lens leg (configuration 4)")

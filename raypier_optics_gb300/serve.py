@@ -56,7 +56,7 @@ def source_desc(kind, n_rays, seed, origin=(0.0, 0.0, -200.0), half_angle=0.05, 
 
 
 class Server:
-    def __init__(self, device=0, hbm_budget=0, lanes=8):
+    def __init__(self, device=0, hbm_budget=0, lanes=4):
         self.lib = _native.load()
         h = ctypes.c_void_p()
         _native.check(self.lib.rp_server_create(device, int(hbm_budget), lanes, ctypes.byref(h)), "rp_server_create")
