@@ -8,7 +8,8 @@
 // emission order (reflected before transmitted).  A sub-tile of 32 rays (one
 // warp) writes its children, in that order, to its own slot range of a
 // scratch arena and publishes their count; a scan of the counts then gives
-// every sub-tile its final offset and a copy kernel places the children
+// every sub-tile its final offset, and the children are copied to their
+// place or read from the slots through a gather map by the next generation
 // (rp_trace.cu).  Warps never wait for one another, so a warp with slow rays
 // does not hold up the others.
 #pragma once

@@ -23,7 +23,9 @@ struct RaySoA {
 // range in parent order (warp scan of the per-ray counts) and their number to
 // tile_counts[q]; once every sub-tile's total is known (tile scan) the
 // placement kernel copies each sub-tile's children to their final, contiguous
-// place.  No ray, warp or block waits for another.  Blocks are RP_BLOCK
+// place, or (the generation loop of trace_rays) the child-map kernel records
+// each child's slot so that the next generation reads it from there (see
+// GenArgs::in_map).  No ray, warp or block waits for another.  Blocks are RP_BLOCK
 // threads, so a block covers RP_BLOCK / RP_SUB sub-tiles (RP_TILE_SLOTS slots).
 #define RP_BLOCK 128
 #define RP_TILE_SLOTS (2 * RP_BLOCK)
@@ -43,7 +45,7 @@ struct GenArgs {
     DevScene S;                   // global-memory tables
     int smem_tables;              // 1: lists/faces/materials staged in shared memory
     int mixed_fallback;           // mixed kernel: the scene has faces / materials only its FP64 code handles
-    RaySoA scratch;                 // child slots: RP_TILE_SLOTS per tile
+    RaySoA scratch;                 // child slots: RP_SUB_SLOTS per sub-tile
     unsigned *tile_counts;          // [n_sub] children of each sub-tile
     unsigned long long *tile_offsets;  // [n_sub] exclusive prefix (scan kernel)
     unsigned long long *out_count;  // total children (scan kernel)
