@@ -316,7 +316,7 @@ def main():
     peak, peak_kind = measured_peak_hbm()
 
     # ---- end to end through the host-buffer C ABI -----------------------------------------
-    e2e_value, d2h, e2e_steps = None, 0, 0
+    e2e_value, d2h, e2e_steps = None, 0, {"steps": 0}
     if not args.no_e2e:
         e2e_value, d2h, e2e_steps = run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens,
                                             seg_per_step, dist, world)
@@ -377,8 +377,9 @@ def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, s
     e2e_value = (est.rays_in * world) / e2e_s
     lib.rp_host_free(pin_in)
     lib.rp_host_free(pin_out)
-    run_e2e.step_ms = [1000.0 * t for t in step_s]
-    return e2e_value, d2h, e2e_steps
+    step_ms = [1000.0 * t for t in step_s]
+    return e2e_value, d2h, {"steps": e2e_steps, "min": min(step_ms), "median": statistics.median(step_ms),
+                            "max": max(step_ms)}
 
 
 def adjoint_leg(ctx, reps=5):
@@ -581,10 +582,9 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
                        "timing": "CUDA events on the library stream around each trace call (device time); "
                                  f"host wall {1000.0 * wall / args.steps:.2f} ms/step"},
             "e2e": ({"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 188,
-                     "d2h_bytes_per_step": int(d2h / e2e_steps), "steps": e2e_steps,
+                     "d2h_bytes_per_step": int(d2h / e2e_steps["steps"]), "steps": e2e_steps["steps"],
                      "api": "rp_trace_rays_host (pinned host records in and out)",
-                     "step_ms": {"min": min(run_e2e.step_ms), "median": statistics.median(run_e2e.step_ms),
-                                 "max": max(run_e2e.step_ms)}} if e2e_value else None),
+                     "step_ms": {k: e2e_steps[k] for k in ("min", "median", "max")}} if e2e_value else None),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": NCU_TRAFFIC_PER_RAY[kernel] * stats.rays_in / max(stats.generations, 1),

@@ -176,6 +176,44 @@ static __device__ double zk_eval(int fn0, int k0, int n0, int m0, double r, doub
     return 0.0;
 }
 
+// The polar angle of (x, y) as its cosine and sine.  For r > 0 they are x / r
+// and y / r (within an ulp or two of cos / sin of atan2(y, x)); at the origin
+// the reference's atan2 of signed zeros decides the angle.
+__device__ __forceinline__ void polar_cs(double x, double y, double r, double &c, double &s) {
+    if (r > 0.0) {
+        c = x / r;
+        s = y / r;
+    } else {
+        const double t = atan2(y, x);
+        c = cos(t);
+        s = sin(t);
+    }
+}
+
+// cos(m t) and sin(m t) for m >= 0 from c = cos t, s = sin t (Chebyshev
+// recurrence).  The reference calls cos / sin of m * theta for every Zernike
+// term; FP64 trigonometry costs GB300's slow FP64 pipe about fifty
+// instructions a call, and a distorted face is evaluated some forty times
+// per ray test, so the terms share the angle and step up from it (the
+// results differ from the library calls by a few ulp).
+__device__ __forceinline__ void multi_angle(int m, double c, double s, double &cm, double &sm) {
+    double c0 = 1.0, s0 = 0.0, c1 = c, s1 = s;
+    if (m == 0) {
+        cm = 1.0;
+        sm = 0.0;
+        return;
+    }
+    for (int k = 2; k <= m; k++) {
+        const double c2 = 2.0 * c * c1 - c0, s2 = 2.0 * c * s1 - s0;
+        c0 = c1;
+        s0 = s1;
+        c1 = c2;
+        s1 = s2;
+    }
+    cm = c1;
+    sm = s1;
+}
+
 // ZernikeDistortion.z_offset_c (cdistortions.pyx:416-450) and the
 // SimpleTestZernikeJ7 variant (48-60).
 static __device__ double dist_z(const DevScene &S, const rp_distortion &d, double x, double y, unsigned *err) {
@@ -190,19 +228,21 @@ static __device__ double dist_z(const DevScene &S, const rp_distortion &d, doubl
     x /= d.unit_radius;
     y /= d.unit_radius;
     double r = sqrt(x * x + y * y);
-    double theta = atan2(y, x);
+    double ct, st;
+    polar_cs(x, y, r, ct, st);
     int kmax = min(d.k_max, RP_ZK_SLOTS);
     for (int i = 0; i < kmax; i++) ws[0][i] = nan_d();
     ws[0][0] = 1.0;
     const double *c = S.aux + d.aux;
     for (int i = 0; i < d.n_coefs; i++) {
         int n = (int)c[5 * i + 1], m = (int)c[5 * i + 2], k = (int)c[5 * i + 3];
-        double N, PH;
+        double N, PH, cm, sm;
         if (m == 0) N = sqrt((double)(n + 1));
         else N = sqrt((double)(2 * (n + 1)));
         N *= c[5 * i + 4];
-        if (m >= 0) PH = cos(m * theta);
-        else PH = -sin(m * theta);
+        multi_angle(abs(m), ct, st, cm, sm);
+        if (m >= 0) PH = cm;  // cos(m theta)
+        else PH = sm;         // -sin(m theta) = sin(|m| theta)
         double R = zk_eval(0, k, n, abs(m), r, ws, err);
         Z += N * R * PH;
     }
@@ -225,7 +265,8 @@ static __device__ v3 dist_zg(const DevScene &S, const rp_distortion &d, double x
     x /= d.unit_radius;
     y /= d.unit_radius;
     double r = sqrt(x * x + y * y);
-    double theta = atan2(y, x);
+    double ct, st;
+    polar_cs(x, y, r, ct, st);
     int kmax = min(d.k_max, RP_ZK_SLOTS);
     for (int i = 0; i < kmax; i++) {
         ws[0][i] = nan_d();
@@ -235,17 +276,17 @@ static __device__ v3 dist_zg(const DevScene &S, const rp_distortion &d, double x
     Z.x = 0.0;
     Z.y = 0.0;
     Z.z = 0.0;
-    double ct = cos(theta), st = sin(theta);
     const double *c = S.aux + d.aux;
     for (int i = 0; i < d.n_coefs; i++) {
         int n = (int)c[5 * i + 1], m = (int)c[5 * i + 2], k = (int)c[5 * i + 3];
-        double N, PH, PHprime;
+        double N, PH, PHprime, cm, sm;
+        multi_angle(abs(m), ct, st, cm, sm);
         if (m >= 0) {
-            PH = cos(m * theta);
-            PHprime = -m * sin(m * theta);
+            PH = cm;             // cos(m theta)
+            PHprime = -m * sm;   // -m sin(m theta)
         } else {
-            PH = -sin(m * theta);
-            PHprime = -m * cos(m * theta);
+            PH = sm;             // -sin(m theta)
+            PHprime = -m * cm;   // -m cos(m theta)
         }
         double R = zk_eval(0, k, n, abs(m), r, ws, err);
         double Rprime = zk_eval(1, k, n, abs(m), r, ws, err);
