@@ -13,6 +13,7 @@
 #include "../../include/rp_gb300.h"
 #include "rp_bounds.h"
 #include "rp_internal.h"
+#include "rp_zkprog.h"
 
 static thread_local char g_last_error[256] = "";
 
@@ -312,7 +313,23 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     size_t o_ntab = o_wl + align256(sizeof(double) * (size_t)n_wl);
     size_t o_cnt = o_ntab + align256(sizeof(double2) * (size_t)n_wl * d->n_dispersions);
     size_t o_bnd = o_cnt + align256(sizeof(unsigned) * (d->n_face_records + 1));
-    size_t total = o_bnd + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
+    // compiled Zernike programs: per distortion the z and the z-gradient one
+    std::vector<int> zk_off((size_t)2 * d->n_distortions + 2, -1);
+    std::vector<short> zk_prog;
+    for (int q = 0; q < d->n_distortions; q++) {
+        const rp_distortion &dq = d->distortions[q];
+        if (dq.type != RP_DIST_ZERNIKE || dq.aux < 0 || (int64_t)dq.aux + 5 * (int64_t)dq.n_coefs > d->n_aux) continue;
+        for (int g = 0; g < 2; g++) {
+            std::vector<short> prog;
+            if (zk_compile(dq.n_coefs, dq.k_max, d->aux + dq.aux, g == 1, prog)) {
+                zk_off[2 * q + g] = (int)zk_prog.size();
+                zk_prog.insert(zk_prog.end(), prog.begin(), prog.end());
+            }
+        }
+    }
+    size_t o_zkoff = o_bnd + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
+    size_t o_zkprog = o_zkoff + align256(sizeof(int) * zk_off.size());
+    size_t total = o_zkprog + align256(sizeof(short) * (zk_prog.size() + 1));
     int rc = ctx_alloc(ctx, &s->dev_block, total, &s->dev_bytes);
     if (rc) {
         delete s;
@@ -338,7 +355,9 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
             face_world_box(d, d->lists[l], d->faces[f], &bounds[(size_t)f * 8]);
         }
     UP(o_bnd, bounds.data(), sizeof(float) * 8 * (size_t)d->n_faces);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // `bounds` is pageable and about to go out of scope
+    UP(o_zkoff, zk_off.data(), sizeof(int) * zk_off.size());
+    UP(o_zkprog, zk_prog.data(), sizeof(short) * zk_prog.size());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host vectors are pageable and about to go out of scope
 #undef UP
     if (e == cudaSuccess) e = cudaMemsetAsync(b + o_cnt, 0, sizeof(unsigned) * (d->n_face_records + 1), st);
     DevScene &S = s->S;
@@ -351,6 +370,8 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     S.ntab = (const double2 *)(b + o_ntab);
     S.bounds = (const float *)(b + o_bnd);
     S.face_list = nullptr;
+    S.zk_off = (const int *)(b + o_zkoff);
+    S.zk_prog = (const short *)(b + o_zkprog);
     S.n_wl = n_wl;
     S.wl = (const double *)(b + o_wl);
     S.n_lists = d->n_lists;

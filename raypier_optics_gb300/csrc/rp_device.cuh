@@ -23,6 +23,8 @@ struct DevScene {
     const double *wl;     // [n_wl] the wavelengths (um)
     const float *bounds;  // [n_faces][8]: world box lo[3], hi[3], skippable flag (rp_bounds.h)
     const short *face_list;  // [n_faces]: owning face list of each traced face
+    const short *zk_prog;    // compiled Zernike programs (rp_zkprog.h), or null
+    const int *zk_off;       // [n_dists][2]: offsets of the z and z-gradient programs in zk_prog, -1 for none
     long long n_wl;
     int n_lists, n_faces, n_recs, n_mats, n_shapes, n_dists;
 };
@@ -98,6 +100,8 @@ bad:
 // in the reference's order (left operand first), and the same slot keys.
 #define RP_ZK_SLOTS 48
 #define RP_ZK_DEPTH 24
+#define RP_ZKOP_WORDS 7     // one operation of a compiled program (rp_zkprog.h)
+#define RP_ZKPROG_SLOTS 96  // a compiled program's workspace (doubles; fits the recursion's)
 struct ZkFrame {
     signed char fn, stage;
     short n, m, k;
@@ -214,6 +218,31 @@ __device__ __forceinline__ void multi_angle(int m, double c, double s, double &c
     sm = s1;
 }
 
+// Replays distortion d's compiled program (grad: the z-and-gradient one) at
+// radius r into ws and returns its result slots, or null when the recursion
+// must run instead (no program, or r not finite, where the recursion's memo
+// reads see NaN values and would repeat work the program assumes done).
+__device__ __forceinline__ const short *zk_program(const DevScene &S, const rp_distortion &d, bool grad, double r,
+                                                   double *ws) {
+    if (!S.zk_off || !isfinite(r)) return nullptr;
+    const int off = S.zk_off[2 * (int)(&d - S.dists) + (grad ? 1 : 0)];
+    if (off < 0) return nullptr;
+    const short *p = S.zk_prog + off;
+    const int n_ops = p[0];
+    ws[0] = 0.0;
+    ws[1] = 1.0;
+    const short *o = p + 3;
+    for (int j = 0; j < n_ops; j++, o += RP_ZKOP_WORDS) {
+        const double a = ws[o[2]], b = ws[o[3]], c = ws[o[4]];
+        double v;
+        if (o[1] == 0) v = r * (a + b) - c;                          // zernike_R_c
+        else if (o[1] == 1) v = (a + b) + r * (c + ws[o[5]]) - ws[o[6]];  // zernike_Rprime_c
+        else v = (a + b) - c;                                        // zernike_R_over_r_c
+        ws[o[0]] = v;
+    }
+    return o;  // the result slots follow the operations
+}
+
 // ZernikeDistortion.z_offset_c (cdistortions.pyx:416-450) and the
 // SimpleTestZernikeJ7 variant (48-60).
 static __device__ double dist_z(const DevScene &S, const rp_distortion &d, double x, double y, unsigned *err) {
@@ -230,9 +259,12 @@ static __device__ double dist_z(const DevScene &S, const rp_distortion &d, doubl
     double r = sqrt(x * x + y * y);
     double ct, st;
     polar_cs(x, y, r, ct, st);
-    int kmax = min(d.k_max, RP_ZK_SLOTS);
-    for (int i = 0; i < kmax; i++) ws[0][i] = nan_d();
-    ws[0][0] = 1.0;
+    const short *res = zk_program(S, d, false, r, &ws[0][0]);
+    if (!res) {
+        int kmax = min(d.k_max, RP_ZK_SLOTS);
+        for (int i = 0; i < kmax; i++) ws[0][i] = nan_d();
+        ws[0][0] = 1.0;
+    }
     const double *c = S.aux + d.aux;
     for (int i = 0; i < d.n_coefs; i++) {
         int n = (int)c[5 * i + 1], m = (int)c[5 * i + 2], k = (int)c[5 * i + 3];
@@ -243,7 +275,7 @@ static __device__ double dist_z(const DevScene &S, const rp_distortion &d, doubl
         multi_angle(abs(m), ct, st, cm, sm);
         if (m >= 0) PH = cm;  // cos(m theta)
         else PH = sm;         // -sin(m theta) = sin(|m| theta)
-        double R = zk_eval(0, k, n, abs(m), r, ws, err);
+        double R = res ? (&ws[0][0])[res[i]] : zk_eval(0, k, n, abs(m), r, ws, err);
         Z += N * R * PH;
     }
     return Z;
@@ -267,11 +299,14 @@ static __device__ v3 dist_zg(const DevScene &S, const rp_distortion &d, double x
     double r = sqrt(x * x + y * y);
     double ct, st;
     polar_cs(x, y, r, ct, st);
-    int kmax = min(d.k_max, RP_ZK_SLOTS);
-    for (int i = 0; i < kmax; i++) {
-        ws[0][i] = nan_d();
-        ws[1][i] = nan_d();
-        ws[2][i] = nan_d();
+    const short *res = zk_program(S, d, true, r, &ws[0][0]);
+    if (!res) {
+        int kmax = min(d.k_max, RP_ZK_SLOTS);
+        for (int i = 0; i < kmax; i++) {
+            ws[0][i] = nan_d();
+            ws[1][i] = nan_d();
+            ws[2][i] = nan_d();
+        }
     }
     Z.x = 0.0;
     Z.y = 0.0;
@@ -288,9 +323,16 @@ static __device__ v3 dist_zg(const DevScene &S, const rp_distortion &d, double x
             PH = sm;             // -sin(m theta)
             PHprime = -m * cm;   // -m cos(m theta)
         }
-        double R = zk_eval(0, k, n, abs(m), r, ws, err);
-        double Rprime = zk_eval(1, k, n, abs(m), r, ws, err);
-        double R_over_r = zk_eval(2, k, n, abs(m), r, ws, err);
+        double R, Rprime, R_over_r;
+        if (res) {
+            R = (&ws[0][0])[res[3 * i]];
+            Rprime = (&ws[0][0])[res[3 * i + 1]];
+            R_over_r = (&ws[0][0])[res[3 * i + 2]];
+        } else {
+            R = zk_eval(0, k, n, abs(m), r, ws, err);
+            Rprime = zk_eval(1, k, n, abs(m), r, ws, err);
+            R_over_r = zk_eval(2, k, n, abs(m), r, ws, err);
+        }
         if (m == 0) N = sqrt((double)(n + 1));
         else N = sqrt((double)(2 * (n + 1)));
         N *= c[5 * i + 4];
