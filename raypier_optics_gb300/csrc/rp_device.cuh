@@ -109,7 +109,7 @@ struct ZkFrame {
     double acc, acc2;
 };
 
-static __device__ double zk_eval(int fn0, int k0, int n0, int m0, double r, double (*ws)[RP_ZK_SLOTS], unsigned *err) {
+static __device__ __noinline__ double zk_eval(int fn0, int k0, int n0, int m0, double r, double (*ws)[RP_ZK_SLOTS], unsigned *err) {
     ZkFrame st[RP_ZK_DEPTH];
     int sp = 0;
     double ret = 0.0;
@@ -954,7 +954,12 @@ static __device__ v3 face_normal_base(const DevScene &S, const rp_face &f, v3 p)
 }
 
 // DistortionFace.intersect_c, cfaces.pyx:2341-2407
-static __device__ double distortion_isect(const DevScene &S, const rp_face &f, v3 p1, v3 p2, unsigned *err) {
+// Out of line (as is zk_eval): inlined at every face-test site, the distorted
+// face's iteration and Zernike code made the plain kernel's instruction
+// footprint the bottleneck on scenes that use it (instruction-fetch stalls
+// 24 per issued instruction on the 64-face clutter scene); one shared copy
+// made that scene 1.8x faster and the lens-train scene's plain path 5 %.
+static __device__ __noinline__ double distortion_isect(const DevScene &S, const rp_face &f, v3 p1, v3 p2, unsigned *err) {
     const rp_face &face = S.faces[f.base];
     const rp_distortion &dist = S.dists[f.distortion];
     double a1, a2, h = sepv(p2, p1);
