@@ -90,10 +90,12 @@ def harness(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     src = open(os.path.join(CSRC, "rp_device.cuh")).read()
-    machine = src[src.index("struct ZkFrame {"):src.index("static __device__ double zk_eval(")]
-    body = src[src.index("static __device__ double zk_eval("):]
+    start = src.rindex("static __device__", 0, src.index("double zk_eval("))
+    machine = src[src.index("struct ZkFrame {"):start]
+    body = src[start:]
     body = body[:body.index("\n}\n") + 3]
-    machine += body.replace("static __device__ ", "static ").replace("atomicOr(err, ERR_ZK_STACK)", "(*err |= 2u)")
+    body = body.replace("static __device__ __noinline__ ", "static ").replace("static __device__ ", "static ")
+    machine += body.replace("atomicOr(err, ERR_ZK_STACK)", "(*err |= 2u)")
     d = tmp_path_factory.mktemp("zk")
     cpp = d / "zk_check.cpp"
     cpp.write_text(HARNESS.replace("@MACHINE@", machine))
