@@ -86,11 +86,11 @@ def calc_mode_curvature(rx, ry, dx, dy, dx2, dy2, dxdy):
     """Wavefront curvature A, B, C and the local bases x', y', z' at each
     point (cfields.pyx:232-290), on the GPU.  Returns (A, B, C, x, y, z), the
     last three (N, 3)."""
-    ctx = runtime.get_context()
     n = len(rx)
     a = [np.ascontiguousarray(v, dtype=np.double).reshape(-1) for v in (dx, dy, dx2, dy2, dxdy)]
     if any(v.shape[0] < n for v in a):
         raise IndexError("Out of bounds on buffer access (axis 0)")
+    ctx = runtime.get_context()
     out = [np.empty(n) for _ in range(3)] + [np.empty((n, 3)) for _ in range(3)]
     _native.check(ctx.lib.rp_field_mode_curvature(ctx.handle, *[v.ctypes.data for v in a], n,
                                                   *[o.ctypes.data for o in out]), "rp_field_mode_curvature")
@@ -104,13 +104,13 @@ def build_interaction_matrix(rx, ry, tx, ty, A, B, C, x, y, z, wavelength, spaci
     (data, (i, j)) that scipy.sparse.coo_matrix takes, ordered by i then j.
     The reference sizes its output by an estimate from test_spacing and
     writes past it when the estimate is short; here the exact count is used."""
-    ctx = runtime.get_context()
     n, L = len(rx), len(tx)
     v = [np.ascontiguousarray(a, dtype=np.double).reshape(-1) for a in (rx, ry, A, B, C)]
     t = [np.ascontiguousarray(a, dtype=np.double).reshape(-1) for a in (tx, ty)]
     b = [np.ascontiguousarray(a, dtype=np.double).reshape(-1, 3) for a in (x, y, z)]
     if any(a.shape[0] < n for a in v + b) or t[1].shape[0] < L:
         raise IndexError("Out of bounds on buffer access (axis 0)")
+    ctx = runtime.get_context()
     cap = n * (1 + int((7 * max_spacing * max_spacing) / (test_spacing * test_spacing)))
     count = ctypes.c_uint64()
     for _ in range(2):
@@ -134,13 +134,13 @@ def build_interaction_matrix(rx, ry, tx, ty, A, B, C, x, y, z, wavelength, spaci
 def apply_mode_curvature(gc, A, B, C):
     """Tilts each gausslet's parabasal rays by the given wavefront curvature
     (cfields.pyx:397-426), on the GPU, in place."""
-    ctx = runtime.get_context()
     n = gc.n_rays
     a = [np.ascontiguousarray(v, dtype=np.double).reshape(-1) for v in (A, B, C)]
     if any(v.shape[0] < n for v in a):
         raise IndexError("Out of bounds on buffer access (axis 0)")
     if n == 0:
         return
+    ctx = runtime.get_context()
     dev = gc._device(ctx)
     _native.check(ctx.lib.rp_field_apply_mode_curvature(dev.handle, *[v.ctypes.data for v in a]),
                   "rp_field_apply_mode_curvature")

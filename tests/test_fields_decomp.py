@@ -131,3 +131,19 @@ def test_gpu_apply_mode_curvature_matches_reference():
     cfields.apply_mode_curvature(gc, U["ac_A"], U["ac_B"], U["ac_C"])
     got = gc.copy_as_array()
     assert got.tobytes() == U["ac_out"].astype(ctracer.gausslet_dtype).tobytes()
+
+
+def test_short_arrays_raise_before_any_device_work():
+    # the reference's bounds-checked buffers raise IndexError; here the
+    # check comes before the library is touched, so it holds without a GPU
+    from raypier_optics_gb300 import cfields
+    with pytest.raises(IndexError):
+        cfields.calc_mode_curvature(np.zeros(4), np.zeros(4), np.zeros(3), np.zeros(4), np.zeros(4), np.zeros(4),
+                                    np.zeros(4))
+    a = [U[k] for k in IM_KEYS]
+    a[4] = a[4][:-1]
+    with pytest.raises(IndexError):
+        cfields.build_interaction_matrix(*a, *U["im_args"])
+    gc = ctracer.GaussletCollection.from_array(U["ac_gausslets"].astype(ctracer.gausslet_dtype))
+    with pytest.raises(IndexError):
+        cfields.apply_mode_curvature(gc, U["ac_A"][:-1], U["ac_B"], U["ac_C"])
