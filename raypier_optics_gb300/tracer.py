@@ -80,7 +80,7 @@ def trace_rays(input_rays, face_lists, recursion_limit=100, max_length=100.0, fl
         rc = RayCollection._from_device(runtime.DeviceRays(ctx, 0, handle=ctypes.c_void_p(gens[g])), parent=prev)
         traced.append(rc)
         prev = rc
-    # free generations the driver allocated but the reference would not return
+    # free generations the library allocated but the reference would not return
     # (gens[0] is the caller's input buffer and stays with input_rays)
     for g in range(max(n_gens.value, 1), max_gens):
         if gens[g]:
