@@ -56,8 +56,7 @@ BYTES_PER_GATHERED = 4 + 28 + 176
 # dram__bytes_write.sum from ncu on generation 3 of the 262,144-ray config-2
 # trace, 1,046,875 gathered rays: the launch reads its rays through the gather
 # map and writes their records, 611.9 algorithmic bytes per ray with 1.25
-# children; profiles/generation_mixed_kernel_config2_262144rays.md and
-# profiles/traffic_generation_placement_config2_262144rays.md)
+# children)
 NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 649.2, "generation_mixed_kernel": 616.2}
 
 

@@ -355,6 +355,16 @@ int rp_gausslets_count(const rp_gausslets *g, uint64_t *n);
  * ctracer.pyx:1303-1318) or out (GaussletCollection.copy_as_array, 1286-1292). */
 int rp_gausslets_upload(rp_gausslets *g, const void *records, uint64_t n);
 int rp_gausslets_download(const rp_gausslets *g, void *records, uint64_t n);
+/* GaussletCollection.config_parabasal_rays (ctracer.pyx:1430-1476) on the
+ * device: the six parabasal rays of a circular Gaussian mode of 1/e^2 waist
+ * `radius` (mm) whose waist lies working_dist beyond each base ray's origin,
+ * at the base ray's wavelength (wavelengths[wavelength_idx], um). */
+int rp_gausslets_config_parabasal(rp_gausslets *g, const double *wavelengths, int64_t n_wavelengths, double radius,
+                                  double working_dist);
+/* GaussletCollection.total_power (ctracer.pyx:1482-1496): the sum over the
+ * base rays of (|E1|^2 + |E2|^2) Re(n), reduced on the device in a fixed
+ * order. */
+int rp_gausslets_total_power(const rp_gausslets *g, double *power);
 
 /* One Gausslet generation: replaces trace_gausslet_c (ctracer.pyx:2214-2282)
  * and, with list_idx / face_idx >= 0, trace_one_face_gausslet_c (2285-2350),
@@ -444,6 +454,42 @@ int rp_field_apply_mode_curvature(rp_gausslets *gausslets, const double *A, cons
 int rp_field_sum_gaussian_modes(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double *modes,
                                 const double *wavelengths, int64_t n_wavelengths, const double *points,
                                 uint64_t n_points, double time_ps, double *E_out);
+/* The modes of a device gausslet collection, fitted on the device and kept
+ * there: replaces the set-up of EFieldSummation / eval_Efield_from_gausslets
+ * (core/fields.py:239-247, 269-277: evaluate_neighbours_gc, 122-148, then
+ * cfields.evaluate_modes).  Each gausslet's six parabasal rays are sampled in
+ * its base ray's (E, E x d) frame and fitted in closed form; the field's base
+ * rays are the gausslets' base rays.  RP_ERR_INVALID ("float division") for a
+ * degenerate fit, where the reference raises ZeroDivisionError. */
+int rp_field_create_from_gausslets(rp_gausslets *gausslets, const double *wavelengths, int64_t n_wavelengths,
+                                   double blending, rp_field **out);
+/* The modes of a device ray lattice (eval_Efield_from_rays, core/fields.py:
+ * 195-224): with radius != 0 the rays are first moved to their intercept with
+ * the sphere of that radius about centre[3] (project_to_sphere, 51-77; every
+ * ray must meet it); each ray whose six neighbour indices (neighbours: host,
+ * n x 6 int32, -1 for none) all exist is sampled against its neighbours
+ * carried to its normal plane (evaluate_neighbours, 80-111) and fitted.  The
+ * field keeps those rays, in order. */
+int rp_field_create_from_rays(rp_rays *rays, const int32_t *neighbours, const double *centre, double radius,
+                              double blending, const double *wavelengths, int64_t n_wavelengths, rp_field **out);
+/* A field's mode count and, where the pointers are non-null, its base rays
+ * (188-byte records) and n x 3 complex mode coefficients.  Host buffers. */
+int rp_field_download(const rp_field *field, uint64_t *n_modes, void *records, double *modes);
+/* The wavefront samples the mode fit takes, as host arrays of n x 6:
+ * evaluate_neighbours_gc (core/fields.py:114-136) of a device gausslet
+ * collection ... */
+int rp_field_gausslet_samples(rp_gausslets *gausslets, double *x, double *y, double *dx, double *dy);
+/* ... and evaluate_neighbours (80-111) of a device ray lattice; kept[] (host,
+ * capacity n) receives the rows kept, *n_kept their number (the samples fill
+ * the first *n_kept rows). */
+int rp_field_ray_samples(rp_rays *rays, const int32_t *neighbours, double *x, double *y, double *dx, double *dy,
+                         uint64_t *kept, uint64_t *n_kept);
+/* project_to_sphere (core/fields.py:51-77) in place on a device buffer: each
+ * ray moves along its direction to the nearer-behind intercept with the
+ * sphere (radius about centre[3]) and its optical path by that distance
+ * times the real refractive index; hit[i] (host, n bytes) is 0 for a ray that
+ * misses the sphere (left unchanged). */
+int rp_rays_project_to_sphere(rp_rays *rays, const double *centre, double radius, uint8_t *hit);
 
 /* ---- differentiable sequential lens ------------------------------------- */
 /* No counterpart in the reference: raypier has no gradients.  A stack of even
@@ -555,7 +601,10 @@ int rp_server_destroy(rp_server *server);
  *    launched, rp_last_error() says so.
  *  - The first call on each device does a one-time set-up (it looks up the
  *    scratch array's device address, which loads this library's device code
- *    on that device): make that first call before any stream capture.
+ *    on that device): make that first call before any stream capture.  The
+ *    address is kept per device until rp_ctx_create is called for that
+ *    device again: after a reset of the device (cudaDeviceReset), create a
+ *    new context before the next call.
  *  - The counters at the start of the scratch must be zero when the
  *    generation kernel starts; the call clears them itself on its stream.
  *    Every other scratch byte is written before it is read.

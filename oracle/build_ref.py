@@ -39,7 +39,9 @@ PKG_DIR = os.path.join(REF_OUT, "raypier", "core")
 MODULES = ["ctracer", "cmaterials", "cfaces", "cshapes", "cdistortions", "cfields"]
 # pure-Python modules of the reference imported next to them
 PY_MODULES = ["tracer", "fields", "utils"]
-DEFAULT_SRC = os.environ.get("RP_REFERENCE_SRC", "/root/reference")
+# The reference checkout: RP_REFERENCE_SRC, else a directory named `reference`
+# beside this repository's root (the layout the build scripts are run in).
+DEFAULT_SRC = os.environ.get("RP_REFERENCE_SRC") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def _ext_suffix() -> str:

@@ -110,14 +110,27 @@ def time_cpu(config, records, wl, per_ray_wl, processes=None, shards=None, kind=
             "kind": kind}
 
 
+# Arm Ltd. (implementer 0x41) core part numbers of the server cores this may run on
+_ARM_PARTS = {"0xd0c": "Arm Neoverse-N1", "0xd40": "Arm Neoverse-V1", "0xd49": "Arm Neoverse-N2",
+              "0xd4f": "Arm Neoverse-V2 (NVIDIA Grace)", "0xd8e": "Arm Neoverse-N3", "0xd84": "Arm Neoverse-V3"}
+
+
 def cpu_model() -> str:
+    """The host CPU's name: /proc/cpuinfo's model name on x86, the Arm core
+    named from its part number on aarch64."""
+    part = None
     try:
         with open("/proc/cpuinfo") as f:
             for line in f:
-                if line.lower().startswith(("model name", "cpu part", "hardware")):
+                key = line.lower().split(":", 1)[0].strip()
+                if key == "model name":
                     return line.split(":", 1)[1].strip()
+                if key == "cpu part" and part is None:
+                    part = line.split(":", 1)[1].strip().lower()
     except OSError:
         pass
+    if part is not None:
+        return _ARM_PARTS.get(part, f"Arm core part {part}")
     import platform
     return platform.processor() or platform.machine()
 

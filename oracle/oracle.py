@@ -70,6 +70,10 @@ def load():
                                                          D, D, D, D, ctypes.c_int64, P, P, P]
             lib.rp_oracle_interaction_matrix.restype = ctypes.c_int64
             lib.rp_oracle_apply_mode_curvature.argtypes = [P, ctypes.c_int64, P, P, P]
+            lib.rp_oracle_gausslet_samples.argtypes = [P, ctypes.c_int64, P, P, P, P]
+            lib.rp_oracle_ray_samples.argtypes = [P, ctypes.c_int64, P, P, P, P, P, P]
+            lib.rp_oracle_ray_samples.restype = ctypes.c_int64
+            lib.rp_oracle_project_to_sphere.argtypes = [P, ctypes.c_int64, P, D, P]
             lib.rp_oracle_eval_parabasal.argtypes = [P, P, ctypes.c_int64, I, P, P, P, P, P, ctypes.c_uint32, P]
             _lib = lib
         return _lib
@@ -393,3 +397,40 @@ def apply_mode_curvature(gausslets, A, B, C):
     a = [np.ascontiguousarray(v, dtype=np.double).reshape(-1) for v in (A, B, C)]
     lib.rp_oracle_apply_mode_curvature(g.ctypes.data, len(g), *[v.ctypes.data for v in a])
     return g
+
+
+# ---- wavefront samples for the mode fit (core/fields.py:51-148) ---------------------
+def gausslet_samples(gausslets):
+    """evaluate_neighbours_gc (core/fields.py:114-136) on the host:
+    (base rays, x, y, dx, dy), each sample array n x 6."""
+    lib = load()
+    from raypier_optics_gb300.ctracer import gausslet_dtype
+    g = np.ascontiguousarray(gausslets, dtype=gausslet_dtype)
+    n = len(g)
+    out = [np.zeros((n, 6)) for _ in range(4)]
+    lib.rp_oracle_gausslet_samples(g.ctypes.data, n, *[o.ctypes.data for o in out])
+    return (g['base_ray'],) + tuple(out)
+
+
+def ray_samples(rays, neighbours):
+    """evaluate_neighbours (core/fields.py:80-111) on the host:
+    (kept rays, x, y, dx, dy)."""
+    lib = load()
+    r = _rays(rays)
+    nb = np.ascontiguousarray(neighbours, dtype=np.int32).reshape(-1, 6)
+    n = len(r)
+    out = [np.zeros((n, 6)) for _ in range(4)]
+    kept = np.zeros(n, dtype=np.int64)
+    k = lib.rp_oracle_ray_samples(r.ctypes.data, n, nb.ctypes.data, *[o.ctypes.data for o in out], kept.ctypes.data)
+    return (r[kept[:k]],) + tuple(o[:k] for o in out)
+
+
+def project_to_sphere(rays, centre, radius):
+    """project_to_sphere (core/fields.py:51-77) on the host: the rays that
+    meet the sphere, moved to it."""
+    lib = load()
+    r = np.array(_rays(rays), copy=True)
+    hit = np.zeros(len(r), dtype=np.uint8)
+    c = np.ascontiguousarray(centre, dtype=np.double).reshape(3)
+    lib.rp_oracle_project_to_sphere(r.ctypes.data, len(r), c.ctypes.data, float(radius), hit.ctypes.data)
+    return r[hit.astype(bool)]

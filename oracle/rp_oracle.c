@@ -2171,3 +2171,84 @@ void rp_oracle_apply_mode_curvature(rp_gausslet *g, int64_t n, const double *A, 
         }
     }
 }
+
+/* ---- wavefront samples for the mode fit (core/fields.py:51-148) -------------
+ * The reference forms these with numpy: a 3-term product sum over the last
+ * axis adds x, y, z left to right and numpy.cross is the usual component
+ * formula, so the C below reproduces it bit for bit. */
+
+/* evaluate_neighbours_gc (core/fields.py:114-136): offsets and slopes of each
+ * gausslet's six parabasal rays in the base ray's (E, E x d) frame. */
+void rp_oracle_gausslet_samples(const rp_gausslet *g, int64_t n, double *x, double *y, double *dx, double *dy) {
+    for (int64_t i = 0; i < n; i++) {
+        const rp_ray *b = &g[i].base_ray;
+        vec o = ld_v(b->origin), d = ld_v(b->direction), E = ld_v(b->E_vector);
+        vec H = cross_(E, d);
+        for (int j = 0; j < 6; j++) {
+            vec u = subvv_(ld_v(g[i].para[j].origin), o);
+            vec m = ld_v(g[i].para[j].direction);
+            double md = dotprod_(m, d);
+            x[i * 6 + j] = dotprod_(u, E);
+            y[i * 6 + j] = dotprod_(u, H);
+            dx[i * 6 + j] = dotprod_(m, E) / md;
+            dy[i * 6 + j] = dotprod_(m, H) / md;
+        }
+    }
+}
+
+/* evaluate_neighbours (core/fields.py:80-111): for each ray whose six
+ * neighbours all exist (kept[k] its index), the neighbours carried along
+ * their directions to the ray's normal plane, then offsets and slopes in the
+ * ray's (E, E x d) frame.  Returns the number of rows kept. */
+int64_t rp_oracle_ray_samples(const rp_ray *r, int64_t n, const int32_t *nb, double *x, double *y, double *dx,
+                              double *dy, int64_t *kept) {
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; i++) {
+        int all = 1;
+        for (int j = 0; j < 6; j++) all = all && nb[i * 6 + j] >= 0;
+        if (!all) continue;
+        vec o = ld_v(r[i].origin), d = ld_v(r[i].direction), E = ld_v(r[i].E_vector);
+        vec H = cross_(E, d);
+        for (int j = 0; j < 6; j++) {
+            const rp_ray *q = &r[nb[i * 6 + j]];
+            vec m = ld_v(q->direction);
+            vec u = subvv_(ld_v(q->origin), o);
+            double md = dotprod_(m, d);
+            double s = -dotprod_(u, d) / md;
+            u.x = u.x + s * m.x;
+            u.y = u.y + s * m.y;
+            u.z = u.z + s * m.z;
+            x[k * 6 + j] = dotprod_(u, E);
+            y[k * 6 + j] = dotprod_(u, H);
+            dx[k * 6 + j] = dotprod_(m, E) / md;
+            dy[k * 6 + j] = dotprod_(m, H) / md;
+        }
+        kept[k++] = i;
+    }
+    return k;
+}
+
+/* project_to_sphere (core/fields.py:51-77) in place: each ray that meets the
+ * sphere moves to the smaller root of |o - c + a d|^2 = radius^2 and its
+ * optical path by a Re(n); hit[i] = 0 for a ray that misses (unchanged). */
+void rp_oracle_project_to_sphere(rp_ray *r, int64_t n, const double *c, double radius, uint8_t *hit) {
+    for (int64_t i = 0; i < n; i++) {
+        vec u = {r[i].origin[0] - c[0], r[i].origin[1] - c[1], r[i].origin[2] - c[2]};
+        vec d = ld_v(r[i].direction);
+        double cc = dotprod_(u, u) - radius * radius;
+        double b = 2 * dotprod_(d, u);
+        double disc = b * b - 4 * cc;
+        if (!(disc >= 0.0)) {
+            hit[i] = 0;
+            continue;
+        }
+        double s = sqrt(disc);
+        double r1 = (-b + s) / 2, r2 = (-b - s) / 2;
+        double a = (r2 < r1 || r2 != r2) ? r2 : r1;
+        r[i].origin[0] += a * d.x;
+        r[i].origin[1] += a * d.y;
+        r[i].origin[2] += a * d.z;
+        r[i].accumulated_path += a * r[i].refractive_index[0];
+        hit[i] = 1;
+    }
+}

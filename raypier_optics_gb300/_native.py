@@ -208,6 +208,15 @@ _SIGS = {
     "rp_field_evaluate_device": (_I, [_P, _P, ctypes.c_uint64, ctypes.c_double, _P]),
     "rp_field_sum_gaussian_modes": (_I, [_P, _P, ctypes.c_uint64, _P, _P, ctypes.c_int64, _P, ctypes.c_uint64,
                                          ctypes.c_double, _P]),
+    "rp_field_create_from_gausslets": (_I, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.POINTER(_P)]),
+    "rp_field_create_from_rays": (_I, [_P, _P, _P, ctypes.c_double, ctypes.c_double, _P, ctypes.c_int64,
+                                       ctypes.POINTER(_P)]),
+    "rp_field_download": (_I, [_P, ctypes.POINTER(ctypes.c_uint64), _P, _P]),
+    "rp_field_gausslet_samples": (_I, [_P, _P, _P, _P, _P]),
+    "rp_field_ray_samples": (_I, [_P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_uint64)]),
+    "rp_rays_project_to_sphere": (_I, [_P, _P, ctypes.c_double, _P]),
+    "rp_gausslets_config_parabasal": (_I, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double]),
+    "rp_gausslets_total_power": (_I, [_P, ctypes.POINTER(ctypes.c_double)]),
     "rp_select_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
     "rp_select_gausslet_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
     "rp_trace_gausslet_segment": (_I, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _P,

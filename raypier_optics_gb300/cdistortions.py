@@ -3,37 +3,29 @@
 (cdistortions.pyx:104-136); evaluation runs on the GPU."""
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 from .ctracer import Distortion
 
 DIST_ZERNIKE, DIST_SIMPLE_J7 = 1, 2
 
-jnm_map = [(0, 0, 0)]
-
 
 def eval_nmk(j):
-    """ANSI j -> (n, m, k), extending the cached table in the reference's
-    order (cdistortions.pyx:104-141).  k is the radial-polynomial slot
-    (n//2)*(n//2+1) + |m|."""
+    """ANSI index j -> (n, m, k) of a Zernike term (cdistortions.pyx:104-141).
+
+    The terms of radial order n take the indices n(n+1)/2 .. n(n+3)/2, so n is
+    the largest integer with n(n+1)/2 <= j and the azimuthal order follows
+    from j = (n(n+2) + m)/2.  k is the slot of the radial polynomial R_n^|m|
+    in the evaluation workspace, (n//2)(n//2 + 1) + |m|."""
+    j = int(j)
     if j < 0:
         raise ValueError("J must be non-negative")
-    if j >= len(jnm_map):
-        n, m, k = jnm_map[-1]
-        while True:
-            while m < n:
-                m += 2
-                next_j = (n * (n + 2) + m) // 2
-                half_n = int(np.floor(n / 2.))
-                k = half_n * (half_n + 1) + abs(m)
-                jnm_map.append((n, m, k))
-                if next_j == j:
-                    return (n, m, k)
-                elif next_j > j:
-                    raise ValueError("Something went wrong here! Missed j value.")
-            n += 1
-            m = -2 - n
-    return tuple(jnm_map[j])
+    n = (math.isqrt(8 * j + 1) - 1) // 2
+    m = 2 * j - n * (n + 2)
+    h = n // 2
+    return (n, m, h * (h + 1) + abs(m))
 
 
 zcoefs_dtype = np.dtype([('j', np.int32), ('n', np.int32), ('m', np.int32), ('k', np.int32), ('value', np.double)])

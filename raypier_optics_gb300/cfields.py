@@ -34,11 +34,25 @@ def evaluate_modes(x, y, dx, dy, blending=1.0):
     return out
 
 
-class GaussianModes:
-    """A set of modes held on the device (rp_field) for repeated evaluation."""
+def _field_check(status, where):
+    """A degenerate mode fit is the reference's ZeroDivisionError."""
+    if status == -1:
+        lib = _native.load(build_if_needed=False)
+        if (lib.rp_last_error() or b"") == b"float division":
+            raise ZeroDivisionError("float division")
+    _native.check(status, where)
 
-    def __init__(self, rays, modes, wavelengths):
-        self.ctx = runtime.get_context()
+
+class GaussianModes:
+    """A set of modes held on the device (rp_field) for repeated evaluation:
+    from host rays and coefficients, or fitted on the device from a gausslet
+    collection (``from_gausslets``) or a ray lattice (``from_rays``)."""
+
+    def __init__(self, rays, modes, wavelengths, _handle=None, _ctx=None):
+        self.ctx = _ctx or runtime.get_context()
+        if _handle is not None:
+            self.handle = _handle
+            return
         recs = rays.copy_as_array() if hasattr(rays, "copy_as_array") else np.ascontiguousarray(rays)
         recs = np.ascontiguousarray(recs)
         assert recs.dtype == ray_dtype
@@ -51,6 +65,53 @@ class GaussianModes:
                                                    wl.ctypes.data if wl.size else None, wl.shape[0],
                                                    ctypes.byref(h)), "rp_field_create")
         self.handle = h
+
+    @classmethod
+    def from_gausslets(cls, dev_gausslets, wavelengths, blending=1.0):
+        """Modes fitted on the device to the parabasal rays of a device gausslet
+        collection (runtime.DeviceGausslets)."""
+        ctx = dev_gausslets.ctx
+        wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+        h = ctypes.c_void_p()
+        _field_check(ctx.lib.rp_field_create_from_gausslets(dev_gausslets.handle, wl.ctypes.data if wl.size else None,
+                                                            wl.shape[0], float(blending), ctypes.byref(h)),
+                     "rp_field_create_from_gausslets")
+        return cls(None, None, None, _handle=h, _ctx=ctx)
+
+    @classmethod
+    def from_rays(cls, dev_rays, neighbours, wavelengths, blending=1.0, centre=(0.0, 0.0, 0.0), radius=0.0):
+        """Modes fitted on the device to a ray lattice (runtime.DeviceRays) and
+        its (n, 6) neighbour table, after projection to the sphere of `radius`
+        about `centre` when radius is non-zero."""
+        ctx = dev_rays.ctx
+        n = dev_rays.count()
+        nb = np.ascontiguousarray(neighbours, dtype=np.int32).reshape(-1, 6)
+        if nb.shape[0] != n:
+            raise IndexError(f"boolean index did not match: {nb.shape[0]} neighbour rows for {n} rays")
+        wl = np.ascontiguousarray(wavelengths, dtype=np.double)
+        c = np.ascontiguousarray(centre, dtype=np.double).reshape(3)
+        h = ctypes.c_void_p()
+        st = ctx.lib.rp_field_create_from_rays(dev_rays.handle, nb.ctypes.data, c.ctypes.data, float(radius),
+                                               float(blending), wl.ctypes.data if wl.size else None, wl.shape[0],
+                                               ctypes.byref(h))
+        if st == -1 and b"outside the collection" in (ctx.lib.rp_last_error() or b""):
+            raise IndexError(ctx.lib.rp_last_error().decode())
+        if st == -1 and b"miss the projection sphere" in (ctx.lib.rp_last_error() or b""):
+            raise IndexError(ctx.lib.rp_last_error().decode())
+        _field_check(st, "rp_field_create_from_rays")
+        return cls(None, None, None, _handle=h, _ctx=ctx)
+
+    def download(self, records=True, modes=True):
+        """(base-ray records or None, n x 3 complex modes or None)."""
+        n = ctypes.c_uint64()
+        _native.check(self.ctx.lib.rp_field_download(self.handle, ctypes.byref(n), None, None), "rp_field_download")
+        recs = np.zeros(n.value, dtype=ray_dtype) if records else None
+        m = np.zeros((n.value, 3), dtype=np.complex128) if modes else None
+        _native.check(self.ctx.lib.rp_field_download(self.handle, ctypes.byref(n),
+                                                     recs.ctypes.data if recs is not None and n.value else None,
+                                                     m.ctypes.data if m is not None and n.value else None),
+                      "rp_field_download")
+        return recs, m
 
     def evaluate(self, points, time_ps=0.0):
         p = np.ascontiguousarray(points, dtype=np.double).reshape(-1, 3)

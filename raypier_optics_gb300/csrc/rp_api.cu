@@ -97,6 +97,10 @@ void rp__set_error(const char *fmt, ...) {
 
 extern "C" {
 
+// rp_trace_segment_noalloc's cached scratch address of a device (defined
+// with it below); a new context looks it up again.
+static void noalloc_forget(int device);
+
 int rp_version(void) { return RP_ABI_VERSION; }
 
 const char *rp_status_string(int s) {
@@ -135,6 +139,7 @@ int rp_ctx_create(int device, uint64_t hbm_budget, rp_ctx **out) {
         delete c;
         return cuda_fail(e, "rp_ctx_create");
     }
+    noalloc_forget(device);
     *out = c;
     return RP_OK;
 }
@@ -782,8 +787,17 @@ static int one_generation(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, f
         return RP_ERR_CAPACITY;
     }
     rc = place_gen(ctx, a, out, count, st);
-    if (rc == RP_OK) CK(cudaStreamSynchronize(ctx->stream));
-    return rc;
+    if (rc) return rc;
+    // the placement kernel reports an overflow in the same error word
+    CK(cudaMemcpyAsync(ctx->h_pinned, a.err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if ((unsigned)(ctx->h_pinned[0] & 0xffffffffu) & ERR_OVERFLOW) {
+        out->n = 0;
+        if (st) st->rays_out -= count;
+        snprintf(g_last_error, sizeof g_last_error, "child placement overflowed its slots or the output buffer");
+        return RP_ERR_CAPACITY;
+    }
+    return RP_OK;
 }
 
 int rp_trace_segment(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float max_length, uint32_t flags,
@@ -1061,6 +1075,73 @@ int rp_gausslets_download(const rp_gausslets *g, void *records, uint64_t n) {
     return RP_OK;
 }
 
+int rp_gausslets_config_parabasal(rp_gausslets *g, const double *wavelengths, int64_t n_wl, double radius,
+                                  double working_dist) {
+    if (!g || n_wl < 0 || (n_wl && !wavelengths)) return RP_ERR_INVALID;
+    rp_ctx *ctx = g->ctx;
+    CK(cudaSetDevice(ctx->device));
+    const uint64_t n = g->base->n;
+    if (n == 0) return RP_OK;
+    ParabasalConfig P;
+    for (int k = 0; k < 3; k++) {
+        // the angle as the reference forms it, (j * 2) * pi / 6 for j = 2k; the
+        // C library's cos / sin at run time (not a compile-time folding)
+        volatile double angle = ((double)(4 * k) * 3.141592653589793) / 6.0;
+        const double a = angle;
+        P.c[k] = cos(a);
+        P.s[k] = sin(a);
+        P.rc[k] = radius * P.c[k];
+        P.rs[k] = radius * P.s[k];
+    }
+    P.kt = (3.141592653589793 * radius) * 1000.0;
+    P.wd = working_dist;
+    const size_t wl_b = ((size_t)(n_wl ? n_wl : 1) * sizeof(double) + 255) & ~(size_t)255;
+    unsigned char *blk = nullptr;
+    size_t got = 0;
+    int rc = ctx_alloc(ctx, (void **)&blk, wl_b + 256, &got);
+    if (rc) return rc;
+    double *dwl = (double *)blk;
+    unsigned *err = (unsigned *)(blk + wl_b);
+    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(unsigned), ctx->stream);
+    if (e == cudaSuccess && n_wl)
+        e = cudaMemcpyAsync(dwl, wavelengths, (size_t)n_wl * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = launch_parabasal_config(g->base->soa, g->para, g->cap, n, dwl, n_wl, P, err, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned, err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    const unsigned ferr = (unsigned)(ctx->h_pinned[0] & 0xffffffffu);
+    ctx_free(ctx, blk, got);
+    if (e != cudaSuccess) return cuda_fail(e, "rp_gausslets_config_parabasal");
+    if (ferr) {
+        snprintf(g_last_error, sizeof g_last_error, "a gausslet's wavelength_idx is outside the wavelength list");
+        return RP_ERR_INVALID;
+    }
+    return RP_OK;
+}
+
+int rp_gausslets_total_power(const rp_gausslets *g, double *power) {
+    if (!g || !power) return RP_ERR_INVALID;
+    *power = 0.0;
+    rp_ctx *ctx = g->ctx;
+    CK(cudaSetDevice(ctx->device));
+    const uint64_t n = g->base->n;
+    if (n == 0) return RP_OK;
+    const uint64_t nb = (n + RP_POWER_BLOCK - 1) / RP_POWER_BLOCK;
+    double *part = nullptr;
+    size_t got = 0;
+    int rc = ctx_alloc(ctx, (void **)&part, nb * sizeof(double), &got);
+    if (rc) return rc;
+    std::vector<double> h(nb);
+    cudaError_t e = launch_power_partials(g->base->soa, n, part, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), part, nb * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    ctx_free(ctx, part, got);
+    if (e != cudaSuccess) return cuda_fail(e, "rp_gausslets_total_power");
+    double s = 0.0;
+    for (uint64_t b = 0; b < nb; b++) s += h[b];
+    *power = s;
+    return RP_OK;
+}
+
 int rp_trace_gausslet_segment(rp_ctx *ctx, rp_scene *s, rp_gausslets *in, rp_gausslets *out, int32_t list_idx,
                               int32_t face_idx, double max_length, int32_t *captured, rp_stats *st) {
     if (!ctx || !s || !in || !out || in == out || s->ctx != ctx || in->ctx != ctx || out->ctx != ctx)
@@ -1306,6 +1387,15 @@ static std::mutex g_noalloc_mu;
 
 // One-time set-up per device, with that device current: the device address
 // of g_noalloc_scratch (resolving it loads this file's device code there).
+// The scratch address is cached per device; a context created after a reset
+// of the device's primary context (which reloads the module, and may move
+// the array) must not use the old one, so rp_ctx_create forgets it.
+static void noalloc_forget(int device) {
+    if (device < 0 || device >= NA_MAX_DEVICES) return;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    g_noalloc_base[device] = nullptr;
+}
+
 static int noalloc_scratch(int device, unsigned char **base) {
     if (device < 0 || device >= NA_MAX_DEVICES) {
         snprintf(g_last_error, sizeof g_last_error, "rp_trace_segment_noalloc: device %d beyond its table of %d",
@@ -1333,6 +1423,7 @@ static int noalloc_scratch(int device, unsigned char **base) {
 int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, float max_length, uint32_t flags,
                              double e2, rp_stats *st) {
     if (!ctx || !s || !in || !out || in == out || s->ctx != ctx) return RP_ERR_INVALID;
+    out->n = 0;  // a rejected call leaves no stale count in a reused output buffer
     if (in->n > RP_NOALLOC_MAX_RAYS) {
         snprintf(g_last_error, sizeof g_last_error,
                  "rp_trace_segment_noalloc: %llu input rays exceed its fixed limit of %d (use rp_trace_segment)",
@@ -1343,7 +1434,6 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     unsigned char *sc = nullptr;
     int rc = noalloc_scratch(ctx->device, &sc);
     if (rc) return rc;
-    out->n = 0;
     if (in->n == 0) return RP_OK;
     const uint64_t n_sub = rp_n_sub(in->n);
 
@@ -1415,7 +1505,12 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     a.out_cap = out->cap;
     e = launch_place_children(a, n_sub, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "child placement launch");
+    CK(cudaMemcpyAsync(ctx->h_pinned, a.err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if ((unsigned)(ctx->h_pinned[0] & 0xffffffffu) & ERR_OVERFLOW) {
+        snprintf(g_last_error, sizeof g_last_error, "child placement overflowed its slots or the output buffer");
+        return RP_ERR_CAPACITY;
+    }
     out->n = count;
     if (st) st->rays_out += count;
     return RP_OK;

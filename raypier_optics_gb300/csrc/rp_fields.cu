@@ -294,6 +294,166 @@ __global__ void __launch_bounds__(256) interaction_fill_kernel(IMArgs M) {
     }
 }
 
+// ---- wavefront samples around a base ray ---------------------------------------
+// A base ray (origin o, direction d, polarisation E taken as unit, as the
+// reference does) spans the frame (E, H = E x d, d).  Each neighbouring ray
+// (origin q, direction m) samples the wavefront near the base ray: its offset
+// u = q - o expressed as (u.E, u.H) and its slope (m.E, m.H) / (m.d).  A ray of
+// a lattice is first carried along m to the plane through o normal to d
+// (u + s m, s = -(u.d) / (m.d)); the parabasal rays of a gausslet already
+// start in that plane (core/fields.py:83-148 describe both).  The mode fit
+// then takes six samples per base ray.  Dot products add x, y, z in that
+// order.
+__device__ __forceinline__ double dot_xyz(v3 a, v3 b) { return ((a.x * b.x) + (a.y * b.y)) + (a.z * b.z); }
+
+struct SampleFrame {
+    v3 o, d, E, H;
+};
+
+__device__ __forceinline__ SampleFrame sample_frame(v3 o, v3 d, v3 E) {
+    SampleFrame f;
+    f.o = o;
+    f.d = d;
+    f.E = E;
+    f.H = mkv((E.y * d.z) - (E.z * d.y), (E.z * d.x) - (E.x * d.z), (E.x * d.y) - (E.y * d.x));
+    return f;
+}
+
+__device__ __forceinline__ void wavefront_sample(const SampleFrame &f, v3 q, v3 m, bool to_plane, double *x, double *y,
+                                                 double *sx, double *sy) {
+    v3 u = mkv(q.x - f.o.x, q.y - f.o.y, q.z - f.o.z);
+    const double md = dot_xyz(m, f.d);
+    if (to_plane) {
+        const double s = (-dot_xyz(u, f.d)) / md;
+        u = mkv(u.x + (s * m.x), u.y + (s * m.y), u.z + (s * m.z));
+    }
+    *x = dot_xyz(u, f.E);
+    *y = dot_xyz(u, f.H);
+    *sx = dot_xyz(m, f.E) / md;
+    *sy = dot_xyz(m, f.H) / md;
+}
+
+// Stores sample row r (6 values per array) of x, y, dx, dy at xs[k * rows * 6 + r * 6 + j].
+__device__ __forceinline__ void store_samples(double *xs, unsigned long long rows, unsigned long long r, const double *x,
+                                              const double *y, const double *sx, const double *sy) {
+    const unsigned long long plane = rows * 6;
+    for (int j = 0; j < 6; j++) {
+        xs[r * 6 + j] = x[j];
+        xs[plane + r * 6 + j] = y[j];
+        xs[2 * plane + r * 6 + j] = sx[j];
+        xs[3 * plane + r * 6 + j] = sy[j];
+    }
+}
+
+// One gausslet per thread: its six parabasal samples, then (modes != null)
+// the mode fit.  xs (or null) receives the samples.
+__global__ void gausslet_samples_kernel(RaySoA base, const double *para, unsigned long long cap, unsigned long long n,
+                                        double blending, double *xs, cx *modes, unsigned *err) {
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SampleFrame f = sample_frame(mkv(base.ox[i], base.oy[i], base.oz[i]), mkv(base.dx[i], base.dy[i], base.dz[i]),
+                                       mkv(base.ex[i], base.ey[i], base.ez[i]));
+    double x[6], y[6], sx[6], sy[6];
+    for (int j = 0; j < 6; j++) {
+        const double *p = para + (unsigned long long)j * RP_PARA_FIELDS * cap + i;  // field k at p[k * cap]
+        wavefront_sample(f, mkv(p[0], p[cap], p[2 * cap]), mkv(p[3 * cap], p[4 * cap], p[5 * cap]), false, &x[j], &y[j],
+                         &sx[j], &sy[j]);
+    }
+    if (xs) store_samples(xs, n, i, x, y, sx, sy);
+    if (modes) {
+        cx m[3];
+        if (!eval_one_mode(x, y, sx, sy, 6, blending, m)) {
+            atomicOr(err, FERR_ZERO_DIV);
+            m[0] = m[1] = m[2] = mkc(nan_d(), nan_d());
+        }
+        modes[3 * i] = m[0];
+        modes[3 * i + 1] = m[1];
+        modes[3 * i + 2] = m[2];
+    }
+}
+
+// One kept ray per thread (kept[k]: a ray whose six lattice neighbours nb[6
+// kept[k] + j] all exist): its samples, the mode fit (modes != null) and the
+// copy of its record to row k of dst (dst.ox != null).
+__global__ void ray_samples_kernel(RaySoA r, const int *nb, const unsigned long long *kept, unsigned long long n_kept,
+                                   double blending, double *xs, cx *modes, RaySoA dst, unsigned *err) {
+    const unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_kept) return;
+    const unsigned long long i = kept[k];
+    const SampleFrame f =
+        sample_frame(mkv(r.ox[i], r.oy[i], r.oz[i]), mkv(r.dx[i], r.dy[i], r.dz[i]), mkv(r.ex[i], r.ey[i], r.ez[i]));
+    double x[6], y[6], sx[6], sy[6];
+    for (int j = 0; j < 6; j++) {
+        const unsigned long long q = (unsigned long long)nb[6 * i + j];
+        wavefront_sample(f, mkv(r.ox[q], r.oy[q], r.oz[q]), mkv(r.dx[q], r.dy[q], r.dz[q]), true, &x[j], &y[j], &sx[j],
+                         &sy[j]);
+    }
+    if (xs) store_samples(xs, n_kept, k, x, y, sx, sy);
+    if (modes) {
+        cx m[3];
+        if (!eval_one_mode(x, y, sx, sy, 6, blending, m)) {
+            atomicOr(err, FERR_ZERO_DIV);
+            m[0] = m[1] = m[2] = mkc(nan_d(), nan_d());
+        }
+        modes[3 * k] = m[0];
+        modes[3 * k + 1] = m[1];
+        modes[3 * k + 2] = m[2];
+    }
+    if (dst.ox) {
+        dst.ox[k] = r.ox[i]; dst.oy[k] = r.oy[i]; dst.oz[k] = r.oz[i];
+        dst.dx[k] = r.dx[i]; dst.dy[k] = r.dy[i]; dst.dz[k] = r.dz[i];
+        dst.nx[k] = r.nx[i]; dst.ny[k] = r.ny[i]; dst.nz[k] = r.nz[i];
+        dst.ex[k] = r.ex[i]; dst.ey[k] = r.ey[i]; dst.ez[k] = r.ez[i];
+        dst.n[k] = r.n[i]; dst.e1[k] = r.e1[i]; dst.e2[k] = r.e2[i];
+        dst.len[k] = r.len[i]; dst.phase[k] = r.phase[i]; dst.opl[k] = r.opl[i];
+        dst.wl[k] = r.wl[i]; dst.parent[k] = r.parent[i]; dst.endf[k] = r.endf[i];
+        dst.ident[k] = r.ident[i]; dst.type[k] = r.type[i];
+    }
+}
+
+// Every record of src to the same row of dst.
+__global__ void copy_rays_kernel(RaySoA s, RaySoA d, unsigned long long n) {
+    const unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    d.ox[k] = s.ox[k]; d.oy[k] = s.oy[k]; d.oz[k] = s.oz[k];
+    d.dx[k] = s.dx[k]; d.dy[k] = s.dy[k]; d.dz[k] = s.dz[k];
+    d.nx[k] = s.nx[k]; d.ny[k] = s.ny[k]; d.nz[k] = s.nz[k];
+    d.ex[k] = s.ex[k]; d.ey[k] = s.ey[k]; d.ez[k] = s.ez[k];
+    d.n[k] = s.n[k]; d.e1[k] = s.e1[k]; d.e2[k] = s.e2[k];
+    d.len[k] = s.len[k]; d.phase[k] = s.phase[k]; d.opl[k] = s.opl[k];
+    d.wl[k] = s.wl[k]; d.parent[k] = s.parent[k]; d.endf[k] = s.endf[k];
+    d.ident[k] = s.ident[k]; d.type[k] = s.type[k];
+}
+
+// Moves each ray back (or on) along its direction to the sphere of `radius`
+// about c (core/fields.py:51-77): the nearer-behind root alpha of
+// |o - c + alpha d|^2 = radius^2 (the smaller of the two), the optical path
+// adjusted by alpha times the real refractive index.  hit[i] = 0 for a ray
+// that misses the sphere (left unchanged); *n_miss counts them.
+__global__ void sphere_project_kernel(RaySoA r, unsigned long long n, double cx_, double cy_, double cz_, double radius,
+                                      unsigned char *hit, unsigned *n_miss) {
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const v3 u = mkv(r.ox[i] - cx_, r.oy[i] - cy_, r.oz[i] - cz_);
+    const v3 d = mkv(r.dx[i], r.dy[i], r.dz[i]);
+    const double c = dot_xyz(u, u) - (radius * radius);
+    const double b = 2.0 * dot_xyz(d, u);
+    const double disc = (b * b) - (4.0 * c);
+    if (!(disc >= 0.0)) {
+        hit[i] = 0;
+        atomicAdd(n_miss, 1u);
+        return;
+    }
+    const double s = sqrt(disc);
+    const double r1 = ((-b) + s) / 2.0, r2 = ((-b) - s) / 2.0;
+    const double alpha = (r2 < r1 || r2 != r2) ? r2 : r1;  // the smaller root (NaN propagates as numpy's min)
+    r.ox[i] = r.ox[i] + (alpha * d.x);
+    r.oy[i] = r.oy[i] + (alpha * d.y);
+    r.oz[i] = r.oz[i] + (alpha * d.z);
+    r.opl[i] = r.opl[i] + (alpha * r.n[i].x);
+    hit[i] = 1;
+}
+
 // apply_mode_curvature (cfields.pyx:398-426): each parabasal direction of
 // gausslet i tilted by the curvature A, B, C in the base ray's (E, E x d)
 // frame and renormalised.
@@ -387,31 +547,143 @@ int rp_field_evaluate_modes(rp_ctx *ctx, const double *x, const double *y, const
     return RP_OK;
 }
 
+}  // extern "C"
+
+// A field of n_modes modes with its wavelength table uploaded; the caller
+// fills its rays (f->rays->n) and modes.
+static int field_alloc(rp_ctx *ctx, uint64_t n_modes, const double *wavelengths, int64_t n_wl, rp_field **out) {
+    *out = nullptr;
+    rp_field *f = new (std::nothrow) rp_field();
+    if (!f) return RP_ERR_NOMEM;
+    f->ctx = ctx;
+    f->n_modes = n_modes;
+    f->n_wl = n_wl;
+    int rc = rp_rays_alloc(ctx, n_modes ? n_modes : 1, &f->rays);
+    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->modes, (size_t)(n_modes ? n_modes : 1) * 3 * sizeof(cx),
+                                        &f->modes_bytes);
+    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->wl, (size_t)(n_wl ? n_wl : 1) * sizeof(double), &f->wl_bytes);
+    if (rc == RP_OK)
+        rc = rp__ctx_alloc(ctx, (void **)&f->consts, (size_t)(n_modes ? n_modes : 1) * RP_MODE_WORDS * sizeof(double),
+                           &f->consts_bytes);
+    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->err, sizeof(unsigned), &f->err_bytes);
+    if (rc == RP_OK && n_wl) {
+        cudaError_t e =
+            cudaMemcpyAsync(f->wl, wavelengths, (size_t)n_wl * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) rc = rp__cuda_fail(e, "field wavelengths");
+    }
+    if (rc) {
+        rp_field_destroy(f);
+        return rc;
+    }
+    *out = f;
+    return RP_OK;
+}
+
+// Waits for the stream and turns the field's error word into a status.
+static int field_status(rp_field *f, const char *what) {
+    rp_ctx *ctx = f->ctx;
+    cudaError_t e = cudaMemcpyAsync(ctx->h_pinned, f->err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return rp__cuda_fail(e, what);
+    if (ctx->h_pinned[0] & FERR_ZERO_DIV) {
+        rp__set_error("float division");
+        return RP_ERR_INVALID;
+    }
+    return RP_OK;
+}
+
+// The rays of a lattice whose six neighbour indices are all >= 0 (the rays
+// the mode fit keeps, core/fields.py:98); RP_ERR_INVALID when an index names
+// no ray of the collection.
+static int kept_rows(const int32_t *nb, uint64_t n, std::vector<unsigned long long> &kept) {
+    kept.clear();
+    for (uint64_t i = 0; i < n; i++) {
+        bool all = true;
+        for (int j = 0; j < 6; j++) {
+            const int32_t v = nb[6 * i + j];
+            if (v >= 0 && (uint64_t)v >= n) {
+                rp__set_error("neighbour index %d of ray %llu is outside the collection of %llu rays", v,
+                              (unsigned long long)i, (unsigned long long)n);
+                return RP_ERR_INVALID;
+            }
+            all = all && v >= 0;
+        }
+        if (all) kept.push_back(i);
+    }
+    return RP_OK;
+}
+
+// Device copies of a lattice's neighbour table and kept rows, in one block.
+struct LatticeDev {
+    unsigned char *blk = nullptr;
+    size_t got = 0;
+    int *nb = nullptr;
+    unsigned long long *kept = nullptr;
+};
+
+static int lattice_upload(rp_ctx *ctx, const int32_t *nb, uint64_t n, const std::vector<unsigned long long> &kept,
+                          LatticeDev &L) {
+    const size_t nb_b = align_up((size_t)n * 6 * sizeof(int32_t));
+    const size_t k_b = align_up((kept.size() ? kept.size() : 1) * sizeof(unsigned long long));
+    int rc = rp__ctx_alloc(ctx, (void **)&L.blk, nb_b + k_b, &L.got);
+    if (rc) return rc;
+    L.nb = (int *)L.blk;
+    L.kept = (unsigned long long *)(L.blk + nb_b);
+    cudaError_t e = cudaMemcpyAsync(L.nb, nb, (size_t)n * 6 * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && !kept.empty())
+        e = cudaMemcpyAsync(L.kept, kept.data(), kept.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                            ctx->stream);
+    // the host vectors must outlive the copies
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "lattice upload");
+    return RP_OK;
+}
+
+// Runs sphere_project_kernel on `rays` in place; RP_ERR_INVALID when rays
+// miss the sphere and hit_host is null (the caller cannot drop them).
+static int project_rays(rp_ctx *ctx, rp_rays *rays, const double *centre, double radius, uint8_t *hit_host) {
+    const uint64_t n = rays->n;
+    if (n == 0) return RP_OK;
+    unsigned char *blk = nullptr;
+    size_t got = 0;
+    int rc = rp__ctx_alloc(ctx, (void **)&blk, 256 + align_up(n), &got);
+    if (rc) return rc;
+    unsigned *miss = (unsigned *)blk;
+    unsigned char *hit = blk + 256;
+    cudaError_t e = cudaMemsetAsync(miss, 0, sizeof(unsigned), ctx->stream);
+    if (e == cudaSuccess) {
+        sphere_project_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
+            rays->soa, n, centre[0], centre[1], centre[2], radius, hit, miss);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && hit_host) e = cudaMemcpyAsync(hit_host, hit, n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned, miss, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    const unsigned n_miss = (unsigned)(ctx->h_pinned[0] & 0xffffffffu);
+    rp__ctx_free(ctx, blk, got);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "sphere projection");
+    if (n_miss && !hit_host) {
+        rp__set_error("%u of %llu rays miss the projection sphere", n_miss, (unsigned long long)n);
+        return RP_ERR_INVALID;
+    }
+    return RP_OK;
+}
+
+extern "C" {
+
 int rp_field_create(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double *modes, const double *wavelengths,
                     int64_t n_wl, rp_field **out) {
     if (!ctx || !out || (n_rays && (!rays || !modes)) || n_wl < 0 || (n_wl && !wavelengths)) return RP_ERR_INVALID;
     *out = nullptr;
     FCK(cudaSetDevice(ctx->device));
-    rp_field *f = new (std::nothrow) rp_field();
-    if (!f) return RP_ERR_NOMEM;
-    f->ctx = ctx;
-    f->n_modes = n_rays;
-    f->n_wl = n_wl;
-    int rc = rp_rays_alloc(ctx, n_rays ? n_rays : 1, &f->rays);
-    if (rc == RP_OK) rc = rp_rays_upload_aos(f->rays, rays, n_rays);
-    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->modes, (size_t)(n_rays ? n_rays : 1) * 3 * sizeof(cx),
-                                        &f->modes_bytes);
-    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->wl, (size_t)(n_wl ? n_wl : 1) * sizeof(double), &f->wl_bytes);
-    if (rc == RP_OK)
-        rc = rp__ctx_alloc(ctx, (void **)&f->consts, (size_t)(n_rays ? n_rays : 1) * RP_MODE_WORDS * sizeof(double),
-                           &f->consts_bytes);
-    if (rc == RP_OK) rc = rp__ctx_alloc(ctx, (void **)&f->err, sizeof(unsigned), &f->err_bytes);
+    rp_field *f = nullptr;
+    int rc = field_alloc(ctx, n_rays, wavelengths, n_wl, &f);
+    if (rc) return rc;
+    rc = rp_rays_upload_aos(f->rays, rays, n_rays);
     if (rc == RP_OK) {
         cudaError_t e = cudaSuccess;
         if (n_rays) e = cudaMemcpyAsync(f->modes, modes, (size_t)n_rays * 3 * sizeof(cx), cudaMemcpyHostToDevice,
                                         ctx->stream);
-        if (e == cudaSuccess && n_wl)
-            e = cudaMemcpyAsync(f->wl, wavelengths, (size_t)n_wl * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) rc = rp__cuda_fail(e, "rp_field_create");
     }
@@ -421,6 +693,174 @@ int rp_field_create(rp_ctx *ctx, const void *rays, uint64_t n_rays, const double
     }
     *out = f;
     return RP_OK;
+}
+
+int rp_field_create_from_gausslets(rp_gausslets *g, const double *wavelengths, int64_t n_wl, double blending,
+                                   rp_field **out) {
+    if (!g || !g->base || !out || n_wl < 0 || (n_wl && !wavelengths)) return RP_ERR_INVALID;
+    *out = nullptr;
+    rp_ctx *ctx = g->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    const uint64_t n = g->base->n;
+    rp_field *f = nullptr;
+    int rc = field_alloc(ctx, n, wavelengths, n_wl, &f);
+    if (rc) return rc;
+    cudaError_t e = cudaMemsetAsync(f->err, 0, sizeof(unsigned), ctx->stream);
+    if (e == cudaSuccess && n) {
+        const unsigned blocks = (unsigned)((n + 127) / 128);
+        copy_rays_kernel<<<blocks, 128, 0, ctx->stream>>>(g->base->soa, f->rays->soa, n);
+        gausslet_samples_kernel<<<blocks, 128, 0, ctx->stream>>>(g->base->soa, g->para, g->cap, n, blending, nullptr,
+                                                                f->modes, f->err);
+        e = cudaGetLastError();
+    }
+    f->rays->n = n;
+    rc = e != cudaSuccess ? rp__cuda_fail(e, "rp_field_create_from_gausslets")
+                          : field_status(f, "rp_field_create_from_gausslets");
+    if (rc) {
+        rp_field_destroy(f);
+        return rc;
+    }
+    *out = f;
+    return RP_OK;
+}
+
+int rp_field_create_from_rays(rp_rays *rays, const int32_t *neighbours, const double *centre, double radius,
+                              double blending, const double *wavelengths, int64_t n_wl, rp_field **out) {
+    if (!rays || !out || (rays->n && !neighbours) || n_wl < 0 || (n_wl && !wavelengths) || (radius != 0.0 && !centre))
+        return RP_ERR_INVALID;
+    *out = nullptr;
+    rp_ctx *ctx = rays->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    const uint64_t n = rays->n;
+    std::vector<unsigned long long> kept;
+    int rc = kept_rows(neighbours, n, kept);
+    if (rc) return rc;
+    const uint64_t nk = kept.size();
+    LatticeDev L;
+    rp_rays *proj = nullptr;
+    rp_field *f = nullptr;
+    rc = lattice_upload(ctx, neighbours, n, kept, L);
+    RaySoA src = rays->soa;
+    if (rc == RP_OK && radius != 0.0 && n) {  // core/fields.py:201-206: a non-zero radius projects first
+        rc = rp_rays_alloc(ctx, n, &proj);
+        if (rc == RP_OK) {
+            proj->n = n;
+            copy_rays_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(rays->soa, proj->soa, n);
+            cudaError_t e = cudaGetLastError();
+            rc = e != cudaSuccess ? rp__cuda_fail(e, "ray copy") : project_rays(ctx, proj, centre, radius, nullptr);
+            src = proj->soa;
+        }
+    }
+    if (rc == RP_OK) rc = field_alloc(ctx, nk, wavelengths, n_wl, &f);
+    if (rc == RP_OK) {
+        cudaError_t e = cudaMemsetAsync(f->err, 0, sizeof(unsigned), ctx->stream);
+        if (e == cudaSuccess && nk) {
+            ray_samples_kernel<<<(unsigned)((nk + 127) / 128), 128, 0, ctx->stream>>>(src, L.nb, L.kept, nk, blending,
+                                                                                     nullptr, f->modes, f->rays->soa,
+                                                                                     f->err);
+            e = cudaGetLastError();
+        }
+        f->rays->n = nk;
+        rc = e != cudaSuccess ? rp__cuda_fail(e, "rp_field_create_from_rays") : field_status(f, "rp_field_create_from_rays");
+    }
+    if (proj) rp_rays_free(proj);
+    if (L.blk) rp__ctx_free(ctx, L.blk, L.got);
+    if (rc) {
+        if (f) rp_field_destroy(f);
+        return rc;
+    }
+    *out = f;
+    return RP_OK;
+}
+
+int rp_field_download(const rp_field *f, uint64_t *n_modes, void *records, double *modes) {
+    if (!f || !n_modes) return RP_ERR_INVALID;
+    *n_modes = f->n_modes;
+    rp_ctx *ctx = f->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    if (f->n_modes == 0) return RP_OK;
+    if (records) {
+        int rc = rp_rays_download_aos(f->rays, records, f->n_modes);
+        if (rc) return rc;
+    }
+    if (modes) {
+        FCK(cudaMemcpyAsync(modes, f->modes, (size_t)f->n_modes * 3 * sizeof(cx), cudaMemcpyDeviceToHost, ctx->stream));
+        FCK(cudaStreamSynchronize(ctx->stream));
+    }
+    return RP_OK;
+}
+
+// Copies 4 x rows x 6 samples from the device block xs to the four host arrays.
+static int download_samples(rp_ctx *ctx, const double *xs, uint64_t rows, double *x, double *y, double *dx,
+                            double *dy) {
+    const size_t b = (size_t)rows * 6 * sizeof(double);
+    double *h[4] = {x, y, dx, dy};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 4 && e == cudaSuccess; k++)
+        e = cudaMemcpyAsync(h[k], xs + (size_t)k * rows * 6, b, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "sample download");
+    return RP_OK;
+}
+
+int rp_field_gausslet_samples(rp_gausslets *g, double *x, double *y, double *dx, double *dy) {
+    if (!g || !g->base) return RP_ERR_INVALID;
+    const uint64_t n = g->base->n;
+    if (n && (!x || !y || !dx || !dy)) return RP_ERR_INVALID;
+    if (n == 0) return RP_OK;
+    rp_ctx *ctx = g->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    double *xs = nullptr;
+    size_t got = 0;
+    int rc = rp__ctx_alloc(ctx, (void **)&xs, (size_t)n * 24 * sizeof(double), &got);
+    if (rc) return rc;
+    gausslet_samples_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(g->base->soa, g->para, g->cap, n, 1.0,
+                                                                                xs, nullptr, nullptr);
+    cudaError_t e = cudaGetLastError();
+    rc = e != cudaSuccess ? rp__cuda_fail(e, "rp_field_gausslet_samples") : download_samples(ctx, xs, n, x, y, dx, dy);
+    rp__ctx_free(ctx, xs, got);
+    return rc;
+}
+
+int rp_field_ray_samples(rp_rays *rays, const int32_t *neighbours, double *x, double *y, double *dx, double *dy,
+                         uint64_t *kept_out, uint64_t *n_kept) {
+    if (!rays || !n_kept) return RP_ERR_INVALID;
+    const uint64_t n = rays->n;
+    *n_kept = 0;
+    if (n && (!neighbours || !x || !y || !dx || !dy || !kept_out)) return RP_ERR_INVALID;
+    rp_ctx *ctx = rays->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    std::vector<unsigned long long> kept;
+    int rc = kept_rows(neighbours, n, kept);
+    if (rc) return rc;
+    const uint64_t nk = kept.size();
+    *n_kept = nk;
+    for (uint64_t k = 0; k < nk; k++) kept_out[k] = kept[k];
+    if (nk == 0) return RP_OK;
+    LatticeDev L;
+    rc = lattice_upload(ctx, neighbours, n, kept, L);
+    if (rc) return rc;
+    double *xs = nullptr;
+    size_t got = 0;
+    rc = rp__ctx_alloc(ctx, (void **)&xs, (size_t)nk * 24 * sizeof(double), &got);
+    if (rc == RP_OK) {
+        RaySoA none;
+        memset(&none, 0, sizeof none);
+        ray_samples_kernel<<<(unsigned)((nk + 127) / 128), 128, 0, ctx->stream>>>(rays->soa, L.nb, L.kept, nk, 1.0, xs,
+                                                                                 nullptr, none, nullptr);
+        cudaError_t e = cudaGetLastError();
+        rc = e != cudaSuccess ? rp__cuda_fail(e, "rp_field_ray_samples") : download_samples(ctx, xs, nk, x, y, dx, dy);
+        rp__ctx_free(ctx, xs, got);
+    }
+    rp__ctx_free(ctx, L.blk, L.got);
+    return rc;
+}
+
+int rp_rays_project_to_sphere(rp_rays *rays, const double *centre, double radius, uint8_t *hit) {
+    if (!rays || !centre || (rays->n && !hit)) return RP_ERR_INVALID;
+    rp_ctx *ctx = rays->ctx;
+    FCK(cudaSetDevice(ctx->device));
+    return project_rays(ctx, rays, centre, radius, hit);
 }
 
 int rp_field_destroy(rp_field *f) {

@@ -366,4 +366,104 @@ cudaError_t launch_gausslet_soa_to_aos(RaySoA soa, const double *para, unsigned 
     return cudaGetLastError();
 }
 
+// ---- parabasal rays of a circular Gaussian mode ---------------------------------
+// GaussletCollection.config_parabasal_rays (ctracer.pyx:1430-1476), one
+// gausslet per thread.  The base direction b (normalised) and two unit
+// vectors across it, d1 = |b x o| and d2 = |b x d1| (o the y axis when
+// b_x > b_y, else the x axis), carry three pairs of parabasal rays at the
+// angles 2 pi k / 3: both start on a circle of the waist radius about the
+// waist point (the base origin moved `wd` along b) and lean by
+// +-theta0 = lambda / (pi w) towards the tangent of that circle; each is then
+// moved back by `wd` along its own direction.  P.rc/rs hold radius x cos / sin
+// and P.c/s the cos / sin of the three angles, taken from the host C library
+// so that the device reproduces the reference's values; theta0's divisor
+// (pi radius 1000, lambda in um) is P.kt.  Normal and length are the base ray's.
+__device__ __forceinline__ v3 unit_of(v3 a) {
+    const double m = sqrt(((a.x * a.x) + (a.y * a.y)) + (a.z * a.z));
+    return mkv(a.x / m, a.y / m, a.z / m);
+}
+__device__ __forceinline__ v3 cross_of(v3 a, v3 b) {
+    return mkv((a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x));
+}
+
+__global__ void parabasal_config_kernel(RaySoA b, double *para, unsigned long long cap, unsigned long long n,
+                                        const double *wl, long long n_wl, ParabasalConfig P, unsigned *err) {
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const v3 bd = unit_of(mkv(b.dx[i], b.dy[i], b.dz[i]));
+    const v3 o = bd.x > bd.y ? mkv(0.0, 1.0, 0.0) : mkv(1.0, 0.0, 0.0);
+    const v3 d1 = unit_of(cross_of(bd, o));
+    const v3 d2 = unit_of(cross_of(bd, d1));
+    const unsigned w = b.wl[i];
+    if ((long long)w >= n_wl) {
+        atomicOr(err, 1u);
+        return;
+    }
+    const double theta0 = wl[w] / P.kt;
+    const v3 org = mkv(b.ox[i], b.oy[i], b.oz[i]);
+    const double nx = b.nx[i], ny = b.ny[i], nz = b.nz[i], len = b.len[i];
+    for (int k = 0; k < 3; k++) {
+        v3 c = mkv((d1.x * P.rc[k]) + (d2.x * P.rs[k]), (d1.y * P.rc[k]) + (d2.y * P.rs[k]),
+                   (d1.z * P.rc[k]) + (d2.z * P.rs[k]));
+        c = mkv(c.x + org.x, c.y + org.y, c.z + org.z);
+        c = mkv(c.x + (bd.x * P.wd), c.y + (bd.y * P.wd), c.z + (bd.z * P.wd));
+        const double ts = (-theta0) * P.s[k], tc = theta0 * P.c[k];
+        const v3 t = mkv((d1.x * ts) + (d2.x * tc), (d1.y * ts) + (d2.y * tc), (d1.z * ts) + (d2.z * tc));
+        const v3 dir[2] = {mkv(bd.x + t.x, bd.y + t.y, bd.z + t.z), mkv(bd.x - t.x, bd.y - t.y, bd.z - t.z)};
+        for (int h = 0; h < 2; h++) {
+            const v3 u = unit_of(dir[h]);
+            const int j = 2 * k + h;
+            para_at(para, cap, j, 0, i) = c.x - (dir[h].x * P.wd);
+            para_at(para, cap, j, 1, i) = c.y - (dir[h].y * P.wd);
+            para_at(para, cap, j, 2, i) = c.z - (dir[h].z * P.wd);
+            para_at(para, cap, j, 3, i) = u.x;
+            para_at(para, cap, j, 4, i) = u.y;
+            para_at(para, cap, j, 5, i) = u.z;
+            para_at(para, cap, j, 6, i) = nx;
+            para_at(para, cap, j, 7, i) = ny;
+            para_at(para, cap, j, 8, i) = nz;
+            para_at(para, cap, j, 9, i) = len;
+        }
+    }
+}
+
+cudaError_t launch_parabasal_config(RaySoA base, double *para, unsigned long long cap, unsigned long long n,
+                                    const double *wl, long long n_wl, const ParabasalConfig &P, unsigned *err,
+                                    cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    parabasal_config_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(base, para, cap, n, wl, n_wl, P, err);
+    return cudaGetLastError();
+}
+
+// GaussletCollection.total_power (ctracer.pyx:1482-1496): the sum over the
+// base rays of (|E1|^2 + |E2|^2) n.  Each block of RP_POWER_BLOCK threads adds
+// its gausslets' terms in a fixed tree order into partial[blockIdx.x]; the
+// host adds the partials in block order, so the result does not depend on
+// scheduling.
+__global__ void __launch_bounds__(RP_POWER_BLOCK) power_partials_kernel(RaySoA b, unsigned long long n,
+                                                                        double *partial) {
+    __shared__ double s[RP_POWER_BLOCK];
+    const unsigned long long i = (unsigned long long)blockIdx.x * RP_POWER_BLOCK + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        const double nr = b.n[i].x;
+        const double2 e1 = b.e1[i], e2 = b.e2[i];
+        v = ((((e1.x * e1.x) * nr) + ((e1.y * e1.y) * nr)) + ((e2.x * e2.x) * nr)) + ((e2.y * e2.y) * nr);
+    }
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int h = RP_POWER_BLOCK / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) s[threadIdx.x] = s[threadIdx.x] + s[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
+cudaError_t launch_power_partials(RaySoA base, unsigned long long n, double *partial, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    power_partials_kernel<<<(unsigned)((n + RP_POWER_BLOCK - 1) / RP_POWER_BLOCK), RP_POWER_BLOCK, 0, st>>>(base, n,
+                                                                                                         partial);
+    return cudaGetLastError();
+}
+
 }  // namespace rp

@@ -112,6 +112,18 @@ cudaError_t launch_gausslet_aos_to_soa(const void *aos, RaySoA soa, double *para
                                        unsigned long long n, cudaStream_t st);
 cudaError_t launch_gausslet_soa_to_aos(RaySoA soa, const double *para, unsigned long long cap, void *aos,
                                        unsigned long long n, cudaStream_t st);
+// config_parabasal_rays: host-evaluated constants of the three ray pairs
+struct ParabasalConfig {
+    double rc[3], rs[3];  // radius * cos, radius * sin of the angle 2 pi k / 3
+    double c[3], s[3];    // cos, sin of that angle
+    double kt;            // pi * radius * 1000 (theta0 = wavelength / kt)
+    double wd;            // working distance
+};
+cudaError_t launch_parabasal_config(RaySoA base, double *para, unsigned long long cap, unsigned long long n,
+                                    const double *wl, long long n_wl, const ParabasalConfig &P, unsigned *err,
+                                    cudaStream_t st);
+#define RP_POWER_BLOCK 256
+cudaError_t launch_power_partials(RaySoA base, unsigned long long n, double *partial, cudaStream_t st);
 
 // ---- differentiable sequential lens (rp_lens.cu) ----
 struct LensArgs {

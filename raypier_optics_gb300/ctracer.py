@@ -21,13 +21,14 @@ calls raise.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import sys
 from typing import Optional
 
 import numpy as np
 
-from . import runtime
+from . import _native, runtime
 
 # ctracer.pyx:45-60
 ray_dtype = np.dtype([('origin', np.double, (3,)),
@@ -746,18 +747,15 @@ class GaussletCollection:
 
     @property
     def total_power(self):
-        """ctracer.pyx:1482-1496."""
-        self._sync_host()
-        b = self._host['base_ray'][:self._n]
-        n = b['refractive_index'].real
-        pwr = 0.0
-        for i in range(self._n):
-            e1, e2 = complex(b['E1_amp'][i]), complex(b['E2_amp'][i])
-            pwr += (e1.real * e1.real) * n[i]
-            pwr += (e1.imag * e1.imag) * n[i]
-            pwr += (e2.real * e2.real) * n[i]
-            pwr += (e2.imag * e2.imag) * n[i]
-        return pwr
+        """ctracer.pyx:1482-1496: the sum of (|E1|^2 + |E2|^2) Re(n) over the
+        base rays, reduced on the device."""
+        if self._n == 0:
+            return 0.0
+        ctx = runtime.get_context()
+        dev = self._device(ctx)
+        out = ctypes.c_double()
+        _native.check(ctx.lib.rp_gausslets_total_power(dev.handle, ctypes.byref(out)), "rp_gausslets_total_power")
+        return out.value
 
     def scale_amplitude(self, scale):
         self._sync_host()
@@ -785,37 +783,16 @@ class GaussletCollection:
     def config_parabasal_rays(self, wavelength_list, radius, working_dist):
         """ctracer.pyx:1430-1476: parabasal rays of a circular Gaussian mode of
         1/e^2 waist `radius` (mm) whose waist lies `working_dist` from the base
-        ray's origin."""
-        self._sync_host()
-        wl = np.asarray(wavelength_list, dtype=np.double)
-        for i in range(self._n):
-            g = self._host[i]
-            base = g['base_ray']
-            base_d = norm(tuple(float(x) for x in base['direction']))
-            o = (0.0, 1.0, 0.0) if base_d[0] > base_d[1] else (1.0, 0.0, 0.0)
-            d1 = norm(cross(base_d, o))
-            d2 = norm(cross(base_d, d1))
-            theta0 = wl[base['wavelength_idx']] / (math.pi * radius * 1000.0)
-            borigin = tuple(float(x) for x in base['origin'])
-            for j in range(0, 6, 2):
-                angle = (j * 2 * math.pi / 6)
-                oo = addvv(multvs(d1, radius * math.cos(angle)), multvs(d2, radius * math.sin(angle)))
-                oo = addvv(oo, borigin)
-                oo = addvv(oo, multvs(base_d, working_dist))
-                dd = addvv(multvs(d1, -theta0 * math.sin(angle)), multvs(d2, theta0 * math.cos(angle)))
-                da = addvv(base_d, dd)
-                db = subvv(base_d, dd)
-                para = g['para_rays']
-                para[j]['direction'] = norm(da)
-                para[j]['origin'] = subvv(oo, multvs(da, working_dist))
-                para[j + 1]['direction'] = norm(db)
-                para[j + 1]['origin'] = subvv(oo, multvs(db, working_dist))
-                para[j]['normal'] = base['normal']
-                para[j + 1]['normal'] = base['normal']
-                para[j]['length'] = base['length']
-                para[j + 1]['length'] = base['length']
-            self._host[i] = g
-        self._mark_host_written()
+        ray's origin, set on the device for every gausslet."""
+        if self._n == 0:
+            return
+        wl = np.ascontiguousarray(wavelength_list, dtype=np.double)
+        ctx = runtime.get_context()
+        dev = self._device(ctx)
+        _native.check(ctx.lib.rp_gausslets_config_parabasal(dev.handle, wl.ctypes.data if wl.size else None,
+                                                            wl.shape[0], float(radius), float(working_dist)),
+                      "rp_gausslets_config_parabasal")
+        self._mark_device_written()
 
 
 # ---- plugin base classes ---------------------------------------------------------
@@ -932,12 +909,15 @@ class FaceList:
     def sync_transforms(self):
         """Take the owner's transform (a VTK-style matrix) if it has one;
         otherwise keep the preset transforms, as the reference does
-        (ctracer.pyx:1820-1837).  The reference's "NO OWNER" notice goes to
-        stderr here, so that stdout stays machine-readable."""
+        (ctracer.pyx:1820-1837).  The reference prints "NO OWNER" on every
+        call; here the notice goes to stderr once per face list, so that
+        stdout stays machine-readable and repeated traces stay quiet."""
         try:
             trans = self.owner.transform
         except AttributeError:
-            print("NO OWNER", self.owner, file=sys.stderr)
+            if not getattr(self, "_no_owner_noted", False):
+                print("NO OWNER", self.owner, file=sys.stderr)
+                self._no_owner_noted = True
             return
         m = trans.matrix
         rot = [[m.get_element(i, j) for j in range(3)] for i in range(3)]

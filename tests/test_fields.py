@@ -29,7 +29,7 @@ def _close(got, exp, rtol):
 
 
 def _oracle_from_gausslets(g, wl, points, time_ps=0.0):
-    rays, x, y, dx, dy = fields.evaluate_neighbours_gc(g)
+    rays, x, y, dx, dy = oracle.gausslet_samples(g)
     modes = oracle.evaluate_modes(x, y, dx, dy, 1.0)
     return oracle.sum_gaussian_modes(np.ascontiguousarray(rays), modes, wl, points, time_ps)
 
@@ -57,7 +57,7 @@ def test_oracle_field_pipelines_match_reference():
     g = U["lens_gausslets"].astype(ctracer.gausslet_dtype)
     _eq(_oracle_from_gausslets(g, U["beam_wl"], U["lens_points"]), U["lens_E"])
     _eq(_oracle_from_gausslets(g, U["beam_wl"], U["lens_points"], 0.7), U["lens_E_t"])
-    rays, x, y, dx, dy = fields.evaluate_neighbours(U["rf_rays"].astype(ctracer.ray_dtype), U["rf_neighbours"])
+    rays, x, y, dx, dy = oracle.ray_samples(U["rf_rays"].astype(ctracer.ray_dtype), U["rf_neighbours"])
     _eq(oracle.sum_gaussian_modes(rays, oracle.evaluate_modes(x, y, dx, dy, 1.0), U["beam_wl"], U["rf_points"]),
         U["rf_E"])
 
@@ -118,3 +118,109 @@ def test_gpu_eval_efield_from_rays_matches_reference():
     rc = ctracer.RayCollection.from_array(U["rf_rays"].astype(ctracer.ray_dtype))
     rc.neighbours = U["rf_neighbours"]
     _close(fields.eval_Efield_from_rays(rc, U["rf_points"], U["beam_wl"]), U["rf_E"], FIELD_RTOL)
+
+
+def test_oracle_sphere_projection_keeps_the_rays_that_meet_it():
+    r = U["rf_rays"].astype(ctracer.ray_dtype)
+    c = r["origin"].mean(axis=0) + np.array([0.0, 0.0, 5.0])
+    radius = float(np.max(np.linalg.norm(r["origin"] - c, axis=1))) * 0.9
+    got = oracle.project_to_sphere(r, c, radius)
+    assert 0 < len(got) <= len(r)
+    np.testing.assert_allclose(np.linalg.norm(got["origin"] - c, axis=1), radius, rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_gpu_wavefront_samples_match_the_oracle():
+    """The device's neighbour samples (the mode fit's input) against the
+    oracle's restatement of core/fields.py:80-148, bit for bit: the same
+    operations in the same order, FP64 without contraction."""
+    g = U["lens_gausslets"].astype(ctracer.gausslet_dtype)
+    exp = oracle.gausslet_samples(g)
+    got = fields.evaluate_neighbours_gc(ctracer.GaussletCollection.from_array(g))
+    np.testing.assert_array_equal(got[0], exp[0])
+    for a, b in zip(got[1:], exp[1:]):
+        np.testing.assert_array_equal(a, b)
+    r = U["rf_rays"].astype(ctracer.ray_dtype)
+    exp = oracle.ray_samples(r, U["rf_neighbours"])
+    got = fields.evaluate_neighbours(r, U["rf_neighbours"])
+    assert len(got[0]) == len(exp[0]) and len(exp[0]) > 0
+    np.testing.assert_array_equal(got[0], exp[0])
+    for a, b in zip(got[1:], exp[1:]):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_gpu_neighbour_index_outside_the_lattice_raises():
+    r = U["rf_rays"].astype(ctracer.ray_dtype)
+    nb = np.array(U["rf_neighbours"], dtype=np.int32, copy=True)
+    nb[0, 0] = len(r)
+    with pytest.raises(IndexError):
+        fields.evaluate_neighbours(r, nb)
+
+
+@pytest.mark.gpu
+def test_gpu_sphere_projection_matches_the_oracle():
+    r = U["rf_rays"].astype(ctracer.ray_dtype)
+    c = r["origin"].mean(axis=0) + np.array([0.0, 0.0, 5.0])
+    radius = float(np.max(np.linalg.norm(r["origin"] - c, axis=1))) * 0.9
+    exp = oracle.project_to_sphere(r, c, radius)
+    got = fields.project_to_sphere(r, c, radius)
+    assert 0 < len(exp) < len(r)
+    np.testing.assert_array_equal(got, exp)
+
+
+@pytest.mark.gpu
+def test_gpu_efield_from_projected_rays_matches_the_oracle():
+    """eval_Efield_from_rays with an exit-pupil sphere every ray meets."""
+    rc = ctracer.RayCollection.from_array(U["rf_rays"].astype(ctracer.ray_dtype))
+    rc.neighbours = U["rf_neighbours"]
+    r = rc.copy_as_array()
+    c = r["origin"].mean(axis=0) - 50.0 * r["direction"].mean(axis=0)
+    radius = float(np.min(np.linalg.norm(r["origin"] - c, axis=1))) * 0.5
+    proj = oracle.project_to_sphere(r, c, radius)
+    assert len(proj) == len(r)
+    rays, x, y, dx, dy = oracle.ray_samples(proj, U["rf_neighbours"])
+    exp = oracle.sum_gaussian_modes(rays, oracle.evaluate_modes(x, y, dx, dy, 1.0), U["beam_wl"], U["rf_points"])
+    got = fields.eval_Efield_from_rays(rc, U["rf_points"], U["beam_wl"], exit_pupil_offset=radius,
+                                       exit_pupil_centre=c)
+    _close(got, exp, FIELD_RTOL)
+
+
+@pytest.mark.gpu
+def test_gpu_efield_summation_exposes_modes_and_base_rays():
+    g = U["lens_gausslets"].astype(ctracer.gausslet_dtype)
+    gc = ctracer.GaussletCollection.from_array(g)
+    gc.wavelengths = U["beam_wl"]
+    s = fields.EFieldSummation(gc)
+    rays, x, y, dx, dy = oracle.gausslet_samples(g)
+    np.testing.assert_allclose(s.modes, oracle.evaluate_modes(x, y, dx, dy, 1.0), rtol=MODES_RTOL, atol=0)
+    np.testing.assert_array_equal(s.base_rays.copy_as_array(), rays)
+    np.testing.assert_allclose(fields.ExtractGamma(gc), s.modes, rtol=0, atol=0)
+
+
+def test_gamma_propagates_the_mode_matrix():
+    """Gamma(z) equals G (1 + z G)^-1 for the symmetric 2 x 2 mode matrix."""
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        A, B, C = rng.normal(size=3) + 1j * rng.uniform(0.1, 1.0, size=3)
+        z = rng.uniform(-2, 2)
+        G = np.array([[A, B], [B, C]])
+        exp = G @ np.linalg.inv(np.eye(2) + z * G)
+        got = fields.Gamma(z, A, B, C)
+        np.testing.assert_allclose([got[0], got[1], got[2]], [exp[0, 0], exp[0, 1], exp[1, 1]], rtol=1e-12)
+
+
+def test_find_ray_gen_follows_the_chain_of_waypoints():
+    def gen(origin, direction, length):
+        a = np.zeros(4, dtype=ctracer.ray_dtype)
+        a["origin"] = origin
+        a["direction"] = direction
+        a["length"] = length
+        return ctracer.RayCollection.from_array(a)
+    gens = [gen([0, 0, 0], [0, 0, 1], 10.0), gen([0, 0, 10], [0, 0, 1], 10.0), gen([0, 0, 20], [0, 0, 1], 10.0)]
+    assert fields.find_ray_gen([0, 0, 1], gens) == 0
+    assert fields.find_ray_gen([0, 0, 9], gens) == 0
+    assert fields.find_ray_gen([0, 0, 11], gens) == 1
+    assert fields.find_ray_gen([0, 0, 19], gens) == 1
+    assert fields.find_ray_gen([0, 0, 21], gens) == 2
+    assert fields.find_ray_gen([0, 0, 40], gens) == -1

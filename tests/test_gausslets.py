@@ -93,3 +93,37 @@ def test_gpu_gausslet_trace_matches_reference(name):
                                               max_length=P["max_length"])
     assert_gausslet_generations([t.copy_as_array() for t in traced], c["gens"], what=name)
     assert [f.count for f in all_faces] == c["counts"].tolist()
+
+
+# (case, radius, working distance) of the reference's config_parabasal_rays
+# call that made each golden case's input gausslets (tests/golden/make_golden.py)
+PARABASAL_CASES = [("config1", 0.05, 2.0), ("seq_config1", 0.02, -1.0), ("mat_dielectric", 0.1, 0.5),
+                   ("mat_grating", 0.1, 0.5)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,radius,wd", PARABASAL_CASES)
+def test_gpu_config_parabasal_rays_matches_reference(name, radius, wd):
+    """GaussletCollection.config_parabasal_rays on the device reproduces the
+    reference's parabasal rays bit for bit (cos / sin of the three angles from
+    the host C library, every other operation in the reference's order)."""
+    c = load_gausslet_case(name)
+    exp = c["gausslets"]
+    gc = ctracer.GaussletCollection.from_rays(np.ascontiguousarray(exp["base_ray"]))
+    gc.config_parabasal_rays(c["wl"], radius, wd)
+    got = gc.copy_as_array()
+    for f in ("origin", "direction", "normal", "length"):
+        np.testing.assert_array_equal(got["para_rays"][f], exp["para_rays"][f], err_msg=f"{name}: parabasal {f}")
+    np.testing.assert_array_equal(got["base_ray"], exp["base_ray"])
+
+
+@pytest.mark.gpu
+def test_gpu_total_power_sums_the_base_rays():
+    c = load_gausslet_case("config1")
+    g = c["gausslets"]
+    gc = ctracer.GaussletCollection.from_array(np.concatenate([g] * 50))
+    b = gc.copy_as_array()["base_ray"]
+    n = b["refractive_index"].real
+    exp = float(np.sum((np.abs(b["E1_amp"]) ** 2 + np.abs(b["E2_amp"]) ** 2) * n))
+    assert gc.total_power == pytest.approx(exp, rel=1e-13)
+    assert ctracer.GaussletCollection(0).total_power == 0.0

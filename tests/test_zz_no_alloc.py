@@ -91,6 +91,8 @@ def test_noalloc_rejects_more_rays_than_its_limit():
     din = runtime.DeviceRays(ctx, n)
     din.upload(recs)
     dout = runtime.DeviceRays(ctx, 2 * n)
+    dout.upload(recs[:5])  # a reused output buffer: its old count must not survive the rejection
+    assert dout.count() == 5
     lib = ctx.lib
     rc = lib.rp_trace_segment_noalloc(ctx.handle, scene.handle, din.handle, dout.handle,
                                       ctypes.c_float(P["max_length"]), 0, ctypes.c_double(P["e2_terminate"]), None)
