@@ -242,7 +242,9 @@ typedef struct rp_stats {
     double   device_ms;      /* device time of the call (CUDA events on the context stream) */
     double   kernel_ms;      /* summed device time of the generation kernels alone */
     uint64_t launches;       /* kernels this library launched for the call */
-    uint64_t generations;    /* generation kernels among them */
+    uint64_t generations;    /* generations traced */
+    double   search_ms;      /* RP_TRACE_MIXED: the part of kernel_ms spent in the search kernels (the rest is
+                                the material kernels); 0 on the plain path */
 } rp_stats;
 
 /* Trace flags. */
@@ -490,6 +492,15 @@ int rp_field_ray_samples(rp_rays *rays, const int32_t *neighbours, double *x, do
  * times the real refractive index; hit[i] (host, n bytes) is 0 for a ray that
  * misses the sphere (left unchanged). */
 int rp_rays_project_to_sphere(rp_rays *rays, const double *centre, double radius, uint8_t *hit);
+
+/* ---- measurement support -------------------------------------------------- */
+/* No counterpart in the reference: the device's measured arithmetic peaks,
+ * the denominators of the pipe rooflines reported beside the HBM one.  FP64
+ * and FP32 fused multiply-add throughput (counted as two floating-point
+ * operations each) and 32-bit integer multiply-add throughput, per second,
+ * from many independent chains per thread timed with CUDA events (best of
+ * three launches after a warm-up).  Takes about a tenth of a second. */
+int rp_measure_peaks(int device, double *fp64_flops, double *fp32_flops, double *int32_ops);
 
 /* ---- differentiable sequential lens ------------------------------------- */
 /* No counterpart in the reference: raypier has no gradients.  A stack of even

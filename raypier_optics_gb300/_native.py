@@ -28,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra flags): the plain path must not contract FMAs.
 SOURCES = [
     ("rp_trace.cu", ["--fmad=false"]),
-    ("rp_mixed.cu", ["--fmad=true"]),
+    ("rp_mixed.cu", ["--fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("rp_api.cu", ["--fmad=false"]),
     ("rp_unit.cu", ["--fmad=false"]),
     ("rp_lens.cu", ["--fmad=false"]),
@@ -36,6 +36,7 @@ SOURCES = [
     ("rp_gausslet.cu", ["--fmad=false"]),
     ("rp_capture.cu", ["--fmad=false"]),
     ("rp_fields.cu", ["--fmad=false"]),
+    ("rp_peaks.cu", ["--fmad=true"]),
 ]
 
 
@@ -165,7 +166,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("rays_in", ctypes.c_uint64), ("rays_out", ctypes.c_uint64),
                 ("hits", ctypes.c_uint64), ("terminated", ctypes.c_uint64),
                 ("device_ms", ctypes.c_double), ("kernel_ms", ctypes.c_double),
-                ("launches", ctypes.c_uint64), ("generations", ctypes.c_uint64)]
+                ("launches", ctypes.c_uint64), ("generations", ctypes.c_uint64), ("search_ms", ctypes.c_double)]
 
 
 # Every symbol the header declares, with its ctypes signature.
@@ -217,6 +218,8 @@ _SIGS = {
     "rp_rays_project_to_sphere": (_I, [_P, _P, ctypes.c_double, _P]),
     "rp_gausslets_config_parabasal": (_I, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double]),
     "rp_gausslets_total_power": (_I, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "rp_measure_peaks": (_I, [_I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_double)]),
     "rp_select_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
     "rp_select_gausslet_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
     "rp_trace_gausslet_segment": (_I, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _P,

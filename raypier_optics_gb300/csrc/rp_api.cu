@@ -601,10 +601,12 @@ int rp_rays_field(const rp_rays *r, const char *name, void **p) {
 // ---- tracing ------------------------------------------------------------------
 #define SCRATCH_HDR 64
 
-// Per-generation scratch: [out_count | err | pad | stats[2] | tile counter | pad], then the
-// per-tile child counts and offsets.
+// Per-generation scratch: [out_count | err | pad | stats[2] | tile counter |
+// group counter | pad], then the per-unit child counts and offsets, then the
+// mixed path's per-ray hit hand-over (rp_hit_bytes).
 static size_t scratch_bytes_for(uint64_t n_sub) {
-    return SCRATCH_HDR + align256(n_sub * sizeof(unsigned)) + align256(n_sub * sizeof(unsigned long long));
+    return SCRATCH_HDR + align256(n_sub * sizeof(unsigned)) + align256(n_sub * sizeof(unsigned long long)) +
+           rp_hit_bytes(n_sub * RP_SUB);
 }
 
 // Scratch for a generation of n_sub sub-tiles (rp_n_sub of its ray count).
@@ -665,6 +667,21 @@ struct GenLinks {
     uint64_t map_cap = 0;
 };
 
+// The mixed path's child-slot unit and per-ray hand-over, carved from a
+// generation scratch of n_sub sub-tiles laid out as scratch_bytes_for; the
+// plain path keeps the sub-tile unit.
+void rp__set_mixed_handover(GenArgs &a, uint32_t flags, unsigned char *sc, uint64_t n_sub) {
+    a.group_next = (unsigned *)(sc + 44);
+    if (!(flags & RP_TRACE_MIXED)) {
+        a.unit_rays = RP_SUB;
+        return;
+    }
+    a.unit_rays = RP_GROUP;
+    unsigned char *h = sc + SCRATCH_HDR + align256(n_sub * sizeof(unsigned)) + align256(n_sub * sizeof(unsigned long long));
+    a.hit_t = (float2 *)h;
+    a.hit_face = (int *)(h + align256(n_sub * RP_SUB * 8));
+}
+
 // Launches the generation kernel (and, when children are kept, the tile scan)
 // and queues the read-back of count / error / statistics into h_pinned.
 static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, uint32_t flags, double e2, int emit,
@@ -707,20 +724,21 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
     a.tile_offsets = (unsigned long long *)(sc + SCRATCH_HDR + align256(n_sub * sizeof(unsigned)));
     a.scratch = emit ? (*arena)->soa : in->soa;
     a.face_counts = s->face_counts;
+    rp__set_mixed_handover(a, flags, sc, n_sub);
     if (ctx->gen_ev.empty()) {
-        ctx->gen_ev.resize(2);
+        ctx->gen_ev.resize(3);
         for (auto &ev : ctx->gen_ev) CK(cudaEventCreate(&ev));
     }
     CK(cudaEventRecord(ctx->gen_ev[0], ctx->stream));
-    cudaError_t e = (flags & RP_TRACE_MIXED) ? launch_generation_mixed(a, s->smem, ctx->stream)
+    cudaError_t e = (flags & RP_TRACE_MIXED) ? launch_generation_mixed(a, s->smem, ctx->stream, ctx->gen_ev[2])
                                              : launch_generation_plain(a, s->smem, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "generation kernel launch");
     CK(cudaEventRecord(ctx->gen_ev[1], ctx->stream));
     if (emit) {
-        e = launch_tile_scan(a, n_sub, ctx->stream);
+        e = launch_tile_scan(a, ctx->stream);
         if (e != cudaSuccess) return cuda_fail(e, "tile scan launch");
         if (lk.map_out) {
-            e = launch_child_map(a, n_sub, lk.map_out, lk.map_cap, ctx->stream);
+            e = launch_child_map(a, lk.map_out, lk.map_cap, ctx->stream);
             if (e != cudaSuccess) return cuda_fail(e, "child map launch");
         }
     }
@@ -731,19 +749,23 @@ static int launch_gen(rp_ctx *ctx, rp_scene *s, rp_rays *in, float max_length, u
 
 // Waits for the generation, turns its error bits into a status and returns
 // the number of children in *count.
-static int finish_gen(rp_ctx *ctx, int emit, rp_stats *st, uint64_t n_in, uint64_t *count) {
+static int finish_gen(rp_ctx *ctx, int emit, uint32_t flags, rp_stats *st, uint64_t n_in, uint64_t *count) {
     CK(cudaStreamSynchronize(ctx->stream));
     unsigned long long cnt = ctx->h_pinned[0];
     unsigned err = (unsigned)(ctx->h_pinned[1] & 0xffffffffu);
     unsigned long long hits = ctx->h_pinned[3], term = ctx->h_pinned[4];
     if (st) {
-        float ms = 0;
+        const bool mixed = (flags & RP_TRACE_MIXED) != 0;
+        float ms = 0, sms = 0;
         cudaEventElapsedTime(&ms, ctx->gen_ev[0], ctx->gen_ev[1]);
+        if (mixed && n_in) cudaEventElapsedTime(&sms, ctx->gen_ev[0], ctx->gen_ev[2]);
         st->rays_in += n_in;
         st->hits += hits;
         st->terminated += term;
         st->kernel_ms += ms;
-        st->launches += emit ? 5 : 3;  // counter clear, generation, [tile scan, map or placement,] read-back
+        st->search_ms += sms;
+        // counter clear, generation kernel(s), [tile scan, map or placement,] read-back
+        st->launches += (emit ? 5 : 3) + (mixed && emit && n_in ? 1 : 0);
         st->generations += 1;
     }
     *count = emit ? cnt : 0;
@@ -767,7 +789,7 @@ static int finish_gen(rp_ctx *ctx, int emit, rp_stats *st, uint64_t n_in, uint64
 static int place_gen(rp_ctx *ctx, GenArgs &a, rp_rays *out, uint64_t count, rp_stats *st) {
     a.out = out->soa;
     a.out_cap = out->cap;
-    cudaError_t e = launch_place_children(a, rp_n_sub(a.n_in), ctx->stream);
+    cudaError_t e = launch_place_children(a, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "child placement launch");
     out->n = count;
     if (st) st->rays_out += count;
@@ -779,7 +801,7 @@ static int one_generation(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out, f
     GenArgs a;
     uint64_t count = 0;
     int rc = launch_gen(ctx, s, in, max_length, flags, e2, 1, one_list, one_face, a);
-    if (rc == RP_OK) rc = finish_gen(ctx, 1, st, in->n, &count);
+    if (rc == RP_OK) rc = finish_gen(ctx, 1, flags, st, in->n, &count);
     if (rc) return rc;
     if (count > out->cap) {
         snprintf(g_last_error, sizeof g_last_error, "%llu children do not fit the output buffer",
@@ -868,7 +890,7 @@ static int trace_rays_impl(rp_ctx *ctx, rp_scene *s, rp_rays **gens, int32_t max
         GenArgs a;
         uint64_t n_child = 0;
         rc = launch_gen(ctx, s, rays, max_length, flags, e2, last ? 0 : 1, -1, -1, a, lk);
-        if (rc == RP_OK) rc = finish_gen(ctx, last ? 0 : 1, st, rays->n, &n_child);
+        if (rc == RP_OK) rc = finish_gen(ctx, last ? 0 : 1, flags, st, rays->n, &n_child);
         if (rc) break;
         count++;
         if (done && (rc = done(user, count - 1, rays)) != RP_OK) break;
@@ -1213,7 +1235,7 @@ int rp_trace_gausslet_segment(rp_ctx *ctx, rp_scene *s, rp_gausslets *in, rp_gau
     if (e == cudaSuccess) e = cudaEventRecord(ctx->ev0, ctx->stream);
     if (e == cudaSuccess) e = launch_gausslet_generation(ga, s->smem, ctx->stream);
     if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, ctx->stream);
-    if (e == cudaSuccess) e = launch_tile_scan(a, n_sub, ctx->stream);
+    if (e == cudaSuccess) e = launch_tile_scan(a, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1313,7 +1335,7 @@ static int capture_common(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_rays *i
     ga.pout_cap = pout_cap;
     cudaError_t e = cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream);
     if (e == cudaSuccess) e = launch_capture(ga, wl_offset, with_para, s->smem, ctx->stream);
-    if (e == cudaSuccess) e = launch_tile_scan(a, n_sub, ctx->stream);
+    if (e == cudaSuccess) e = launch_tile_scan(a, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_pinned, sc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1333,7 +1355,7 @@ static int capture_common(rp_ctx *ctx, rp_scene *s, int32_t list_idx, rp_rays *i
         snprintf(g_last_error, sizeof g_last_error, "%llu captured rays do not fit the output buffer", count);
         return RP_ERR_CAPACITY;
     }
-    e = with_para ? launch_gausslet_place(ga, n_sub, ctx->stream) : launch_place_children(a, n_sub, ctx->stream);
+    e = with_para ? launch_gausslet_place(ga, n_sub, ctx->stream) : launch_place_children(a, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (pscratch) ctx_free(ctx, pscratch, pbytes);
     if (e != cudaSuccess) return cuda_fail(e, "capture placement");
@@ -1364,15 +1386,18 @@ int rp_select_gausslet_intersections(rp_ctx *ctx, rp_scene *s, int32_t list_idx,
 //   [0, 64)       counters: child total (u64 @0), error bits (u32 @8),
 //                 hits and terminated children (2 x u64 @24), next tile to
 //                 trace (u32 @40) -- zeroed per call
-//   tile_counts   u32 per 32-ray sub-tile
+//   tile_counts   u32 per 32-ray sub-tile (the mixed path uses one per group)
 //   tile_offsets  u64 per sub-tile
+//   hand-over     the mixed path's hit ray parameter (8 bytes) and face (4
+//                 bytes) per ray, between its search and material kernels
 //   child slots   2 per ray, structure of arrays (188 bytes per slot)
 #define NA_TILES (RP_NOALLOC_MAX_RAYS / RP_BLOCK)
 #define NA_SUBS (RP_NOALLOC_MAX_RAYS / RP_SUB)
 #define NA_SLOTS ((size_t)NA_TILES * RP_TILE_SLOTS)
 #define NA_OFF_TILE_COUNTS ((size_t)SCRATCH_HDR)
 #define NA_OFF_TILE_OFFSETS (NA_OFF_TILE_COUNTS + (((size_t)NA_SUBS * 4 + 255) & ~(size_t)255))
-#define NA_OFF_SLOTS ((NA_OFF_TILE_OFFSETS + (size_t)NA_SUBS * 8 + 255) & ~(size_t)255)
+#define NA_OFF_HIT ((NA_OFF_TILE_OFFSETS + (size_t)NA_SUBS * 8 + 255) & ~(size_t)255)
+#define NA_OFF_SLOTS (NA_OFF_HIT + (size_t)rp_hit_bytes(RP_NOALLOC_MAX_RAYS))
 #define NA_SLOT_BYTES ((size_t)RP_RAY_BYTES * NA_SLOTS)
 #define NA_TOTAL (NA_OFF_SLOTS + NA_SLOT_BYTES)
 #define NA_MAX_DEVICES 64
@@ -1464,6 +1489,7 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     a.tile_offsets = (unsigned long long *)(sc + NA_OFF_TILE_OFFSETS);
     a.scratch = slots.soa;
     a.face_counts = s->face_counts;
+    rp__set_mixed_handover(a, flags, sc, NA_SUBS);  // the hand-over at NA_OFF_HIT
 
     CK(cudaMemsetAsync(sc, 0, SCRATCH_HDR, ctx->stream));
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
@@ -1471,7 +1497,7 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
                                              : launch_generation_plain(a, s->smem, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "generation kernel launch");
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
-    e = launch_tile_scan(a, n_sub, ctx->stream);
+    e = launch_tile_scan(a, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "tile scan launch");
     CK(cudaMemcpyAsync(ctx->h_pinned, sc, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1486,7 +1512,7 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
         st->terminated += ctx->h_pinned[4];
         st->kernel_ms += ms;
         st->device_ms += ms;
-        st->launches += 3;
+        st->launches += (flags & RP_TRACE_MIXED) ? 4 : 3;  // generation kernel(s), tile scan, placement
         st->generations += 1;
     }
     if (err & ERR_WAVELENGTH) {
@@ -1503,7 +1529,7 @@ int rp_trace_segment_noalloc(rp_ctx *ctx, rp_scene *s, rp_rays *in, rp_rays *out
     }
     a.out = out->soa;
     a.out_cap = out->cap;
-    e = launch_place_children(a, n_sub, ctx->stream);
+    e = launch_place_children(a, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "child placement launch");
     CK(cudaMemcpyAsync(ctx->h_pinned, a.err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

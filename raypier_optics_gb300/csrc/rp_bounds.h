@@ -284,11 +284,32 @@ inline bool face_local_box(const rp_scene_desc *d, const rp_face &f, double lo[3
 
 // World-space box, padded for the FP32 test in the kernel.  out[0..2] = lo,
 // out[3..5] = hi, out[6] = 1 if the face may be skipped, 0 if always tested.
+// A DistortionFace with a bounded shape gets out[6] = 2 and, in out[0..3],
+// the shape's local x0, x1, y0, y1 (padded): the reference accepts its hit
+// only where the point it returns -- always a point of the ray's line in the
+// list's frame, converged or not (cfaces.pyx:2372-2407) -- has local (x, y)
+// inside the shape, so a ray whose line never passes over that rectangle
+// cannot hit it (distortion_line_misses).
 inline void face_world_box(const rp_scene_desc *d, const rp_facelist &L, const rp_face &f, float out[8]) {
     double lo[3], hi[3];
     out[6] = 0.0f;
     out[7] = 0.0f;
     for (int k = 0; k < 6; k++) out[k] = 0.0f;
+    if (f.type == RP_FACE_DISTORTION) {
+        const Box2 b = shape_box(d, f.shape);
+        if (!b.bounded || !std::isfinite(b.x0) || !std::isfinite(b.x1) || !std::isfinite(b.y0) ||
+            !std::isfinite(b.y1))
+            return;
+        const double scale = std::max(std::max(std::fabs(b.x0), std::fabs(b.x1)), std::max(std::fabs(b.y0), std::fabs(b.y1)));
+        if (scale > 1e7) return;
+        const double pad = 1e-3 + 1e-5 * scale;
+        out[0] = (float)(b.x0 - pad);
+        out[1] = (float)(b.x1 + pad);
+        out[2] = (float)(b.y0 - pad);
+        out[3] = (float)(b.y1 + pad);
+        out[6] = 2.0f;
+        return;
+    }
     if (!face_local_box(d, f, lo, hi)) return;
     double w0[3] = {INFINITY, INFINITY, INFINITY}, w1[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int c = 0; c < 8; c++) {

@@ -56,6 +56,20 @@ __device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char
     return S;
 }
 
+// A distortion face's cull (box flag 2, rp_bounds.h): true when the line
+// through the local points p1, p2 never passes over the shape's rectangle
+// b[0..3] = x0, x1, y0, y1, i.e. all four corners lie strictly on one side of
+// the line's (x, y) projection (for a line along z: its (x, y) lies outside).
+__device__ __forceinline__ bool distortion_line_misses(const float *b, v3 p1, v3 p2) {
+    if (b[6] != 2.0f) return false;
+    const double ux = p2.x - p1.x, uy = p2.y - p1.y;
+    const double x0 = b[0], x1 = b[1], y0 = b[2], y1 = b[3];
+    if (ux == 0.0 && uy == 0.0) return p1.x < x0 || p1.x > x1 || p1.y < y0 || p1.y > y1;
+    const double s00 = ux * (y0 - p1.y) - uy * (x0 - p1.x), s01 = ux * (y1 - p1.y) - uy * (x0 - p1.x);
+    const double s10 = ux * (y0 - p1.y) - uy * (x1 - p1.x), s11 = ux * (y1 - p1.y) - uy * (x1 - p1.x);
+    return (s00 > 0.0 && s01 > 0.0 && s10 > 0.0 && s11 > 0.0) || (s00 < 0.0 && s01 < 0.0 && s10 < 0.0 && s11 < 0.0);
+}
+
 // Exclusive scan of `c` over the block; *total_out gets the block total.
 // Must be called by all threads of the block.
 __device__ __forceinline__ unsigned block_scan(unsigned c, unsigned *total_out) {

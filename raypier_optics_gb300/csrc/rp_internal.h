@@ -79,3 +79,8 @@ int rp__ctx_alloc(rp_ctx *ctx, void **p, size_t bytes, size_t *got);
 void rp__ctx_free(rp_ctx *ctx, void *p, size_t bytes);
 int rp__cuda_fail(cudaError_t e, const char *what);
 void rp__set_error(const char *fmt, ...);
+// The mixed path's child-slot unit and per-ray hand-over (search -> material
+// kernel) carved from a generation scratch block laid out as [64-byte
+// counters | n_sub u32 counts | n_sub u64 offsets | rp_hit_bytes(n_sub * 32)],
+// each part 256-byte aligned; the plain path keeps the sub-tile unit.
+extern "C" void rp__set_mixed_handover(GenArgs &a, uint32_t flags, unsigned char *sc, uint64_t n_sub);

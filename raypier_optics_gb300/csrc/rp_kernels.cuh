@@ -33,6 +33,14 @@ struct RaySoA {
 #define RP_SUB_SLOTS (2 * RP_SUB)
 #define RP_SUB_PER_BLOCK (RP_BLOCK / RP_SUB)
 __host__ __device__ inline unsigned long long rp_n_sub(unsigned long long n_rays) { return (n_rays + RP_SUB - 1) / RP_SUB; }
+// The mixed path places children by groups of RP_GROUP rays (RP_TILE_SLOTS
+// slots each): its material kernel compacts the rays of a group that produce
+// children into full warps.  The plain path's unit is the sub-tile.
+#define RP_GROUP RP_BLOCK
+__host__ __device__ inline unsigned long long rp_n_units(unsigned long long n_rays, int unit_rays) {
+    const unsigned long long u = unit_rays > 0 ? (unsigned long long)unit_rays : RP_SUB;
+    return (n_rays + u - 1) / u;
+}
 
 struct GenArgs {
     RaySoA in, out;
@@ -61,26 +69,42 @@ struct GenArgs {
     // written there.
     const unsigned *in_map;
     RaySoA wb;
+    // Child-slot unit: 0 or RP_SUB (a sub-tile of one warp, 2 * RP_SUB slots)
+    // or RP_GROUP (the mixed path: RP_TILE_SLOTS slots); tile_counts and
+    // tile_offsets then hold one entry per unit.
+    int unit_rays;
+    // The mixed path's hand-over from its search kernel to its material
+    // kernel, per ray: the ray parameter of the hit (float-float hi, lo) and
+    // the hit face record (-1: none); and the material kernel's group counter.
+    float2 *hit_t;
+    int *hit_face;
+    unsigned *group_next;
 };
+// Bytes of per-ray hand-over storage (hit_t, hit_face) the mixed path needs
+// for n rays, each array on a 256-byte boundary.
+__host__ __device__ constexpr unsigned long long rp_hit_bytes(unsigned long long n) {
+    return ((n * 8 + 255) & ~255ull) + ((n * 4 + 255) & ~255ull);
+}
 
 // launchers (rp_trace.cu / rp_mixed.cu); return cudaError_t
 cudaError_t launch_generation_plain(const GenArgs &a, size_t smem, cudaStream_t st);
-cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st);
+// (the mixed path: the search kernel, then, when children are kept, the
+// material kernel; `mid`, if given, is recorded between the two)
+cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st, cudaEvent_t mid = nullptr);
 // one-time per-configuration set-up (attributes, occupancy), so that a following
 // launch of the same configuration can be stream-captured
 cudaError_t prepare_generation_plain(const GenArgs &a, size_t smem);
 cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem);
-// sub-tile count scan (one block) and the scatter of children to their final
-// slots (one block per RP_SUB_PER_BLOCK sub-tiles)
-cudaError_t launch_tile_scan(const GenArgs &a, unsigned long long n_sub, cudaStream_t st);
-cudaError_t launch_place_children(const GenArgs &a, unsigned long long n_sub, cudaStream_t st);
+// unit count scan (one block) and the scatter of children to their final
+// slots (one warp per unit); the unit count is rp_n_units(a.n_in, a.unit_rays)
+cudaError_t launch_tile_scan(const GenArgs &a, cudaStream_t st);
+cudaError_t launch_place_children(const GenArgs &a, cudaStream_t st);
 // exclusive prefix of n unsigned counts (one block) and their total
 cudaError_t launch_count_scan(const unsigned *counts, unsigned long long n, unsigned long long *offsets,
                               unsigned long long *total, cudaStream_t st);
 // the gather map of the children instead of their copy: map[offset + j] = the
 // arena slot of the sub-tile's child j (the next generation reads through it)
-cudaError_t launch_child_map(const GenArgs &a, unsigned long long n_sub, unsigned *map, unsigned long long map_cap,
-                             cudaStream_t st);
+cudaError_t launch_child_map(const GenArgs &a, unsigned *map, unsigned long long map_cap, cudaStream_t st);
 // at most 32 words: a copy by SM stores (dst may be mapped host memory) and a clear
 cudaError_t launch_copy_words(const unsigned long long *src, unsigned long long *dst, int n, cudaStream_t st);
 cudaError_t launch_zero_words(unsigned long long *dst, int n, cudaStream_t st);

@@ -28,6 +28,7 @@
 // why parity for this path is statistical (see the precision report).
 #include <map>
 #include <mutex>
+#include <tuple>
 
 #include "rp_gen_common.cuh"
 
@@ -217,6 +218,7 @@ struct MxList {
 struct MxFace {
     float p[RP_FACE_NPARAM];
     float zv_hi, zv_lo;
+    float rq_hi, rq_lo;  // the quadric's Rq as float-float (sphere: -curvature; conic, asphere: -p[0])
     float tmin;
     float tol;  // Face.tolerance (a distance) in FP32
 };
@@ -273,6 +275,13 @@ __device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace
         ff z = vp >= 0 ? ff_of_d(F.p[vp]) : ffm(0.0f, 0.0f);
         o.zv_hi = z.hi;
         o.zv_lo = z.lo;
+        double rq = 0.0;
+        if (F.type == RP_FACE_SPHERICAL) rq = -F.p[1];
+        else if (F.type == RP_FACE_SHAPED_SPHERICAL) rq = -F.p[0];
+        else if (F.type == RP_FACE_CONIC || F.type == RP_FACE_ASPHERIC) rq = -F.p[0];
+        const ff r = ff_of_d(rq);
+        o.rq_hi = r.hi;
+        o.rq_lo = r.lo;
         o.tmin = f_of_d(F.tolerance) * max_len;
         o.tol = f_of_d(F.tolerance);
     }
@@ -376,27 +385,48 @@ bad:
 #define MX_MISS_T (-1.0f)
 __device__ __forceinline__ ff miss_t() { return ffm(MX_MISS_T, 0.0f); }
 
-// U = P + t Dl relative to the face vertex, rounded to FP32 (the coordinates
-// are of the order of the aperture, so FP32 resolves them to well below 1 nm).
+// U = P + t Dl relative to the face vertex, in float-float.
+__device__ __forceinline__ void vertex_point_ff(const LRay &R, ff zv, ff t, ff &X, ff &Y, ff &Z) {
+    X = ff_add(R.px, ff_mul(t, R.dx));
+    Y = ff_add(R.py, ff_mul(t, R.dy));
+    Z = ff_sub(ff_add(R.pz, ff_mul(t, R.dz)), zv);
+}
+// The same point rounded to FP32 (the coordinates are of the order of the
+// aperture: FP32 places them within ~1 nm, enough for aperture tests and
+// derivatives, not for the residual of a root).
 __device__ __forceinline__ f3 vertex_point(const LRay &R, ff zv, ff t) {
-    ff ux = ff_add(R.px, ff_mul(t, R.dx));
-    ff uy = ff_add(R.py, ff_mul(t, R.dy));
-    ff uz = ff_sub(ff_add(R.pz, ff_mul(t, R.dz)), zv);
-    return mk3(ux.hi + ux.lo, uy.hi + uy.lo, uz.hi + uz.lo);
+    ff X, Y, Z;
+    vertex_point_ff(R, zv, t, X, Y, Z);
+    return mk3(X.hi + X.lo, Y.hi + Y.lo, Z.hi + Z.lo);
+}
+__device__ __forceinline__ ff ff_sqr(ff a) {
+    ff p = two_prod(a.hi, a.hi);
+    p.lo = fmaf(2.0f * a.hi, a.lo, p.lo);
+    return fast_two_sum(p.hi, p.lo);
 }
 
 // Newton correction of a quadric root: F = beta z^2 - 2 Rq z + x^2 + y^2 in
-// vertex coordinates (a sphere is beta = 1, Rq = -curvature).
-__device__ __forceinline__ ff refine_quadric(const LRay &R, ff zv, float t0, float beta, float Rq) {
-    // one step: the FP32 root is within ~1e-5 of the root, so the step leaves
-    // an error of order curvature * 1e-10 mm, below the residual's own accuracy
+// vertex coordinates (a sphere is beta = 1, Rq = -curvature).  At the root the
+// terms of F cancel to a part in 10^9 of their size, so F is evaluated in
+// float-float at the float-float point (the residual at FP32-rounded
+// coordinates would leave ~0.3 nm along the ray); its derivative along the
+// ray needs only FP32.  One step takes the FP32 root (error ~1e-5 mm) to
+// ~1e-12 mm; a second is taken when the first moved the root by more than a
+// micrometre (grazing hits, where the FP32 root is poorer).
+__device__ __forceinline__ ff refine_quadric(const LRay &R, ff zv, float t0, float beta, ff Rq) {
     ff t = ffm(t0, 0.0f);
     const float dx = R.dx.hi, dy = R.dy.hi, dz = R.dz.hi;
-    f3 u = vertex_point(R, zv, t);
-    float F = fmaf(beta * u.z - 2.0f * Rq, u.z, fmaf(u.x, u.x, u.y * u.y));
-    float G = 2.0f * ((beta * u.z - Rq) * dz + u.x * dx + u.y * dy);
-    float step = -F / G;
-    if (isfinite(step)) t = ff_add_f(t, step);
+    const ff two_rq = ffm(2.0f * Rq.hi, 2.0f * Rq.lo);
+    for (int it = 0; it < 2; it++) {
+        ff X, Y, Z;
+        vertex_point_ff(R, zv, t, X, Y, Z);
+        const ff F = ff_add(ff_add(ff_sqr(X), ff_sqr(Y)), ff_mul(Z, ff_sub(ff_mul_f(Z, beta), two_rq)));
+        const float G = 2.0f * ((beta * Z.hi - Rq.hi) * dz + X.hi * dx + Y.hi * dy);
+        const float step = -F.hi / G;
+        if (!isfinite(step)) break;
+        t = ff_add_f(t, step);
+        if (fabsf(step) <= 1e-3f) break;
+    }
     return t;
 }
 
@@ -417,11 +447,30 @@ __device__ __forceinline__ void asph_fg(const MxFace &M, float Rq, float beta, f
     g = (dsag + dpoly) * dr2 - dz;
 }
 
-// Ray parameter of the hit of face F (hit = P + t Dl), miss_t() for a miss;
-// `fb` is set for face types left to the FP64 path.
-__device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R, float tmax, unsigned *err,
-                     bool &fb) {
+// The asphere's sag residual sag(r^2) - z at a float-float point: the conic
+// part r^2 / (Rq (1 + sqrt(1 - beta r^2 / Rq^2))), of the size of z and
+// cancelling against it, in float-float; the polynomial part (a small
+// fraction of the sag) in FP32.
+__device__ __forceinline__ float asph_residual_ff(const MxFace &M, ff Rq, float beta, ff X, ff Y, ff Z) {
+    const ff r2 = ff_add(ff_sqr(X), ff_sqr(Y));
+    const float k = beta / (Rq.hi * Rq.hi);
+    const ff root = ff_sqrt(ff_add_f(ff_neg(ff_mul_f(r2, k)), 1.0f));
+    const ff conic = ff_div(r2, ff_mul(Rq, ff_add_f(root, 1.0f)));
+    const float A4 = M.p[3], A6 = M.p[4], A8 = M.p[5], A10 = M.p[6], A12 = M.p[7], A14 = M.p[8], A16 = M.p[9];
+    const float q = r2.hi;
+    const float poly = q * q * (A4 + q * (A6 + q * (A8 + q * (A10 + q * (A12 + q * (A14 + q * A16))))));
+    return ff_sub(ff_add_f(conic, poly), Z).hi;
+}
+
+// Phase one of a face test: the FP32 ray parameter of face F's hit (hit =
+// P + t Dl), with bounds and aperture tested at the FP32 hit point, or
+// MX_MISS_T; `fb` is set for face types left to the FP64 path.  A plane's
+// parameter costs one float-float division, so it is returned exactly in *tff
+// (*exact set); curved faces are refined by face_refine only if they win.
+__device__ float face_t32(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R, float tmax,
+                          unsigned *err, ff *tff, bool *exact, bool &fb) {
     fb = false;
+    *exact = false;
     const ff zv = ffm(M.zv_hi, M.zv_lo);
     switch (F.type) {
         case RP_FACE_CIRCULAR:
@@ -429,19 +478,21 @@ __device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const
         case RP_FACE_SHAPED_PLANAR: {
             // cfaces.pyx:147-175, 364-396, 201-227: plane z = zv
             ff t = ff_div(ff_sub(zv, R.pz), R.dz);
-            if (!(t.hi >= M.tmin) || t.hi > tmax) return miss_t();
+            if (!(t.hi >= M.tmin) || t.hi > tmax) return MX_MISS_T;
             float X = fmaf(t.hi, R.dx.hi, R.px.hi), Y = fmaf(t.hi, R.dy.hi, R.py.hi);
             if (F.type == RP_FACE_CIRCULAR) {
                 X -= M.p[1];
-                if (X * X + Y * Y > M.p[0] * M.p[0] * 0.25f) return miss_t();
+                if (X * X + Y * Y > M.p[0] * M.p[0] * 0.25f) return MX_MISS_T;
             } else if (F.type == RP_FACE_RECTANGULAR) {
                 X -= M.p[2];
-                if (X * X > M.p[0] * M.p[0] * 0.25f) return miss_t();
-                if (Y * Y > M.p[1] * M.p[1] * 0.25f) return miss_t();
+                if (X * X > M.p[0] * M.p[0] * 0.25f) return MX_MISS_T;
+                if (Y * Y > M.p[1] * M.p[1] * 0.25f) return MX_MISS_T;
             } else if (!shape_in_f(S, F.shape, X, Y, err)) {
-                return miss_t();
+                return MX_MISS_T;
             }
-            return t;
+            *tff = t;
+            *exact = true;
+            return t.hi;
         }
         case RP_FACE_SPHERICAL:
         case RP_FACE_SHAPED_SPHERICAL: {
@@ -456,7 +507,7 @@ __device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const
             float b = 2.0f * (dx * px + dy * py + dz * (pz + c));
             float cc = px * px + py * py + pz * (pz + 2.0f * c);
             float disc = b * b - 4.0f * a * cc;
-            if (disc < 0.0f) return miss_t();
+            if (disc < 0.0f) return MX_MISS_T;
             float q = -0.5f * (b + copysignf(sqrtf(disc), b));
             float t1 = q / a, t2 = (q != 0.0f) ? cc / q : t1;
             const float INF = __int_as_float(0x7f800000);
@@ -478,10 +529,8 @@ __device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const
                 if (t2 != INF && !shape_in_f(S, F.shape, x2, y2, err)) t2 = INF;
             }
             float t = fminf(t1, t2);
-            if (!(t <= tmax) || !(t >= M.tmin)) return miss_t();
-            ff tt = refine_quadric(R, zv, t, 1.0f, -c);
-            if (!(tt.hi <= tmax) || !(tt.hi >= M.tmin)) return miss_t();
-            return tt;
+            if (!(t <= tmax) || !(t >= M.tmin)) return MX_MISS_T;
+            return t;
         }
         case RP_FACE_CONIC:
         case RP_FACE_ASPHERIC: {
@@ -506,13 +555,11 @@ __device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const
                 else if (plus) t = (B > 0.0f) ? (2.0f * C) / (-B - sd) : (-B + sd) / (2.0f * A);
                 else t = (B < 0.0f) ? (2.0f * C) / (-B + sd) : (-B - sd) / (2.0f * A);
             }
-            ff tt;
             if (F.type == RP_FACE_CONIC) {
-                if (!(t <= tmax) || !(t >= M.tmin)) return miss_t();  // D < 0 gives -1: a miss
-                tt = refine_quadric(R, zv, t, beta, Rq);
+                if (!(t <= tmax) || !(t >= M.tmin)) return MX_MISS_T;  // D < 0 gives -1: a miss
             } else {
                 // asphere: Newton on the sag residual in FP32 from the conic root
-                // (cfaces.pyx:1908-1974), then corrections at float-float points
+                // (cfaces.pyx:1908-1974)
                 float tf = t, f_last = 0.0f;
                 bool conv = false;
                 const f3 p0 = mk3(px, py, pz);
@@ -520,7 +567,7 @@ __device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const
                     f3 u = add3(p0, mul3(mk3(dx, dy, dz), tf));
                     float fv, g;
                     asph_fg(M, Rq, beta, u, dx, dy, dz, fv, g);
-                    if (it > 0 && fabsf(fv) > fabsf(f_last) && fabsf(fv) > 1e-6f * (1.0f + fabsf(u.z))) return miss_t();
+                    if (it > 0 && fabsf(fv) > fabsf(f_last) && fabsf(fv) > 1e-6f * (1.0f + fabsf(u.z))) return MX_MISS_T;
                     f_last = fv;
                     float step = -fv / g;
                     tf += step;
@@ -529,24 +576,43 @@ __device__ ff face_t(const DevScene &S, const rp_face &F, const MxFace &M, const
                         break;
                     }
                 }
-                if (!conv || !isfinite(tf)) return miss_t();
-                if (tf > fmaf(tmax, 1.0001f, 1e-3f)) return miss_t();  // beyond the bound: no correction needed
-                tt = ffm(tf, 0.0f);
-                {  // one correction at the float-float point (the FP32 iterate is within ~1e-3 mm)
-                    f3 u = vertex_point(R, zv, tt);
-                    float fv, g;
-                    asph_fg(M, Rq, beta, u, dx, dy, dz, fv, g);
-                    float step = -fv / g;
-                    if (isfinite(step)) tt = ff_add_f(tt, step);
-                }
+                if (!conv || !isfinite(tf)) return MX_MISS_T;
+                if (!(tf <= tmax) || !(tf >= M.tmin)) return MX_MISS_T;
+                t = tf;
             }
-            f3 u = vertex_point(R, zv, tt);
-            if (!shape_in_f(S, F.shape, u.x, u.y, err)) return miss_t();
-            if (!(tt.hi <= tmax) || !(tt.hi >= M.tmin)) return miss_t();
-            return tt;
+            if (!shape_in_f(S, F.shape, fmaf(t, dx, px), fmaf(t, dy, py), err)) return MX_MISS_T;
+            return t;
         }
-        default: fb = true; return miss_t();
+        default: fb = true; return MX_MISS_T;
     }
+}
+
+// Phase two, for a face that may be the nearest: its ray parameter in
+// float-float from the FP32 one, by Newton steps whose residuals are
+// evaluated in float-float (refine_quadric; the asphere's sag residual by
+// asph_residual_ff, its derivative in FP32).  The FP32 root is within
+// ~1e-5 mm, so one step suffices unless it moved the root by more than a
+// micrometre.
+__device__ __forceinline__ ff face_refine(const rp_face &F, const MxFace &M, const LRay &R, float t32) {
+    const ff zv = ffm(M.zv_hi, M.zv_lo);
+    const ff Rq = ffm(M.rq_hi, M.rq_lo);
+    if (F.type == RP_FACE_SPHERICAL || F.type == RP_FACE_SHAPED_SPHERICAL) return refine_quadric(R, zv, t32, 1.0f, Rq);
+    const float beta = 1.0f + M.p[2];
+    if (F.type == RP_FACE_CONIC) return refine_quadric(R, zv, t32, beta, Rq);
+    ff tt = ffm(t32, 0.0f);
+    const float dx = R.dx.hi, dy = R.dy.hi, dz = R.dz.hi;
+    for (int it = 0; it < 2; it++) {
+        ff X, Y, Z;
+        vertex_point_ff(R, zv, tt, X, Y, Z);
+        float fv, g;
+        asph_fg(M, Rq.hi, beta, mk3(X.hi, Y.hi, Z.hi), dx, dy, dz, fv, g);
+        fv = asph_residual_ff(M, Rq, beta, X, Y, Z);
+        const float step = -fv / g;
+        if (!isfinite(step)) break;
+        tt = ff_add_f(tt, step);
+        if (fabsf(step) <= 1e-3f) break;
+    }
+    return tt;
 }
 
 // Unit normal of a specialised face in float-float at a hit given in vertex
@@ -740,11 +806,16 @@ __device__ int eval_f(const DevScene &S, const rp_material &m, const RayF &r, co
     cf T_s = cmul(cdiv(num, den_s), E1);
     if ((n2.x * (cabs2(T_s) + cabs2(T_p))) / P_in > f_of_d(m.transmission_threshold)) {
         float c2unused;
-        ch[nc].d = refract(ff_div(ff_of_d(n1d.x), ff_of_d(n2d.x)), c2unused);
-        ch[nc].e1 = T_s;
-        ch[nc].e2 = T_p;
-        ch[nc].n = n2d;
-        ch[nc].type = r.type & ~RP_REFL_RAY;
+        ChildF tc;  // filled here and copied to a fixed slot, so the children stay in registers
+        tc.d = refract(ff_div(ff_of_d(n1d.x), ff_of_d(n2d.x)), c2unused);
+        tc.e1 = T_s;
+        tc.e2 = T_p;
+        tc.n = n2d;
+        tc.type = r.type & ~RP_REFL_RAY;
+        if (nc)
+            ch[1] = tc;
+        else
+            ch[0] = tc;
         nc++;
     }
     return nc;
@@ -791,13 +862,15 @@ struct Best {
 // specialised path.
 
 // FP64 distance for a face type this kernel does not specialise.
-__device__ __forceinline__ double fallback_dist(const GenArgs &A, const DevScene &S, const rp_face &F, int l,
+__device__ __forceinline__ double fallback_dist(const GenArgs &A, const DevScene &S, const rp_face &F, int f, int l,
                                                 unsigned long long i) {
     const rp_facelist &L = S.lists[l];
     v3 o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
     v3 d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
     v3 pend = addv(o, mulvs(d, A.max_len));
-    return face_isect(S, F, xform(L.inv_trans.m, L.inv_trans.t, o), xform(L.inv_trans.m, L.inv_trans.t, pend), A.err);
+    const v3 p1 = xform(L.inv_trans.m, L.inv_trans.t, o), p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
+    if (distortion_line_misses(S.bounds + 8 * f, p1, p2)) return -1.0;  // cfaces.pyx NO_INTERSECTION
+    return face_isect(S, F, p1, p2, A.err);
 }
 
 // FP32 world normal of a face type this kernel does not specialise, from the
@@ -813,23 +886,23 @@ __device__ __noinline__ f3 fallback_normal(const DevScene &S, const rp_face &F, 
 // waveplate, partial mirror, apertures, ...) through the FP64 path, after the
 // termination filter; *term receives the number of children dropped by it.
 __device__ __noinline__ int fallback_children(const GenArgs &A, const DevScene &S, const rp_face &F,
-                                              const rp_material &Mt, int l, unsigned long long i, double len,
-                                              const double *origin, f3 nrm, ChildCommon *ccd, Child *chd,
+                                              const rp_material &Mt, int l, const RaySoA &Rr, unsigned long long i,
+                                              double len, const double *origin, f3 nrm, ChildCommon *ccd, Child *chd,
                                               unsigned *term) {
     v3 tng = face_tangent(F);
     if (F.invert_normal) tng = negv(tng);
     tng = rotv(S.lists[l].trans.m, tng);
     RayState r;
-    r.o = mkv(A.in.ox[i], A.in.oy[i], A.in.oz[i]);
-    r.d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
-    r.E = mkv(A.in.ex[i], A.in.ey[i], A.in.ez[i]);
-    r.n = A.in.n[i];
-    r.e1 = A.in.e1[i];
-    r.e2 = A.in.e2[i];
+    r.o = mkv(Rr.ox[i], Rr.oy[i], Rr.oz[i]);
+    r.d = mkv(Rr.dx[i], Rr.dy[i], Rr.dz[i]);
+    r.E = mkv(Rr.ex[i], Rr.ey[i], Rr.ez[i]);
+    r.n = Rr.n[i];
+    r.e1 = Rr.e1[i];
+    r.e2 = Rr.e2[i];
     r.len = len;
-    r.opl = A.in.opl[i];
-    r.type = A.in.type[i];
-    r.wl = A.in.wl[i];
+    r.opl = Rr.opl[i];
+    r.type = Rr.type[i];
+    r.wl = Rr.wl[i];
     int nc = eval_children(S, Mt, r, mkv(origin[0], origin[1], origin[2]),
                            mkv(d_of_f(nrm.x), d_of_f(nrm.y), d_of_f(nrm.z)), tng, *ccd, chd, A.err);
     if (A.e2_term > 0.0 && nc > 0) {
@@ -864,23 +937,84 @@ __device__ __forceinline__ void keep_nearest(ff dist, ff t, int f, int l, Best &
     }
 }
 
-// Tests a specialised face (the caller checks face_specialised).
-__device__ __forceinline__ void try_face(const DevScene &S, const MxList *ml, const MxFace *mf, int f, int l,
-                                         int &cur, LRay &R, const ff *O, const ff *D, ff dlen, float tmax,
-                                         unsigned *err, Best &b) {
+// A candidate for the nearest hit from phase one of a face test.
+struct Cand {
+    float d, t;   // FP32 distance along the ray and ray parameter
+    int face, list;
+    bool exact;   // a plane: tx is its float-float parameter already
+    ff tx;
+};
+__device__ __forceinline__ void cand_clear(Cand &c) {
+    c.d = __int_as_float(0x7f800000);
+    c.t = 0.0f;
+    c.face = -1;
+    c.list = -1;
+    c.exact = false;
+    c.tx = ffm(0.0f, 0.0f);
+}
+
+// Phase one of a specialised face test (the caller checks face_specialised):
+// keeps the two nearest candidates by FP32 distance (ties to the lower face
+// record, as the exact comparison does).
+__device__ __forceinline__ void try_face32(const DevScene &S, const MxList *ml, const MxFace *mf, int f, int l,
+                                           int &cur, LRay &R, const ff *O, const ff *D, float dl, float tmax,
+                                           unsigned *err, Cand &c1, Cand &c2) {
     if (l != cur) {
         R = local_ray(ml[l], O, D);
         cur = l;
     }
-    bool fb;
-    // a face whose FP32 root lies beyond the nearest hit so far (with a margin
-    // far above the FP32 root error) cannot win: skip its refinement
-    const float tl = b.face >= 0 ? fminf(tmax, fmaf(b.t.hi, 1.0009765625f, 1e-3f)) : tmax;
-    ff t = face_t(S, S.faces[f], mf[f], R, tl, err, fb);
-    if (t.hi < 0.0f) return;
-    ff dist = ff_mul(t, dlen);
-    if (!(mf[f].tol < dist.hi)) return;
-    keep_nearest(dist, t, f, l, b);
+    bool fb, exact;
+    ff tx;
+    const float t = face_t32(S, S.faces[f], mf[f], R, tmax, err, &tx, &exact, fb);
+    if (!(t >= 0.0f)) return;
+    const float d = t * dl;
+    if (!(mf[f].tol < d)) return;
+    Cand c;
+    c.d = d;
+    c.t = t;
+    c.face = f;
+    c.list = l;
+    c.exact = exact;
+    c.tx = tx;
+    if (d < c1.d || (d == c1.d && f < c1.face)) {
+        c2 = c1;
+        c1 = c;
+    } else if (d < c2.d || (d == c2.d && f < c2.face)) {
+        c2 = c;
+    }
+}
+
+// Phase two for one candidate: its float-float parameter (bounds and the
+// tolerance checked again on the refined value), kept in b when nearer.
+__device__ __forceinline__ void settle(const DevScene &S, const MxList *ml, const MxFace *mf, const Cand &c, int &cur,
+                                       LRay &R, const ff *O, const ff *D, ff dlen, float tmax, Best &b) {
+    if (c.face < 0) return;
+    ff t;
+    if (c.exact) {
+        t = c.tx;
+    } else {
+        if (c.list != cur) {
+            R = local_ray(ml[c.list], O, D);
+            cur = c.list;
+        }
+        t = face_refine(S.faces[c.face], mf[c.face], R, c.t);
+        if (!(t.hi <= tmax) || !(t.hi >= mf[c.face].tmin)) return;
+    }
+    const ff dist = ff_mul(t, dlen);
+    if (!(mf[c.face].tol < dist.hi)) return;
+    keep_nearest(dist, t, c.face, c.list, b);
+}
+
+// The two candidates' refinement: the nearer always; the other when its FP32
+// distance is within the FP32 roots' error of the nearer (so that the exact
+// comparison, not FP32 rounding, decides between close hits) or when the
+// nearer fails its refined checks.
+__device__ __forceinline__ void settle_best(const DevScene &S, const MxList *ml, const MxFace *mf, const Cand &c1,
+                                            const Cand &c2, int &cur, LRay &R, const ff *O, const ff *D, ff dlen,
+                                            float tmax, Best &b) {
+    settle(S, ml, mf, c1, cur, R, O, D, dlen, tmax, b);
+    if (c2.face >= 0 && (b.face < 0 || c2.d <= fmaf(c1.d, 1.000244140625f, 1e-3f)))
+        settle(S, ml, mf, c2, cur, R, O, D, dlen, tmax, b);
 }
 
 // Tests a face through the FP64 path.  Out of line: called only for face types
@@ -888,7 +1022,7 @@ __device__ __forceinline__ void try_face(const DevScene &S, const MxList *ml, co
 __device__ __noinline__ void try_face_fp64(const GenArgs &A, const DevScene &S, int f, int l, unsigned long long i,
                                            ff dlen, Best &b) {
     const rp_face &F = S.faces[f];
-    double dd = fallback_dist(A, S, F, l, i);
+    double dd = fallback_dist(A, S, F, f, l, i);
     if (!(F.tolerance < dd)) return;  // also rejects NO_INTERSECTION (-1)
     ff dist = ff_of_d(dd);
     keep_nearest(dist, ff_div(dist, dlen), f, l, b);
@@ -954,29 +1088,32 @@ __device__ __forceinline__ void cp_async_wait_prev2() { asm volatile("cp.async.w
 
 // Queues the copy of ray i's fields into the lane's slot of `buf` (nothing
 // for i beyond the generation) and closes the thread's copy group.
+// Only origin and direction are copied for a ray traced in place (`full`
+// false): the search kernel then writes just its length and end face.
 __device__ __forceinline__ void prefetch_ray(TileIn *buf, const RaySoA &in, unsigned long long i, unsigned long long n,
-                                             unsigned long long s) {
-    if (i < n) {
+                                             unsigned long long s, bool full) {
+    if (i < n) {  // ray i of the generation; its record is s of `in`
         const unsigned t = threadIdx.x & 31;
         buf->src[t] = (unsigned)s;
-        i = s;
-        cp_async8(&buf->ox[t], &in.ox[i]);
-        cp_async8(&buf->oy[t], &in.oy[i]);
-        cp_async8(&buf->oz[t], &in.oz[i]);
-        cp_async8(&buf->dx[t], &in.dx[i]);
-        cp_async8(&buf->dy[t], &in.dy[i]);
-        cp_async8(&buf->dz[t], &in.dz[i]);
-        cp_async8(&buf->ex[t], &in.ex[i]);
-        cp_async8(&buf->ey[t], &in.ey[i]);
-        cp_async8(&buf->ez[t], &in.ez[i]);
-        cp_async16(&buf->n[t], &in.n[i]);
-        cp_async16(&buf->e1[t], &in.e1[i]);
-        cp_async16(&buf->e2[t], &in.e2[i]);
-        cp_async8(&buf->opl[t], &in.opl[i]);
-        cp_async8(&buf->phase[t], &in.phase[i]);
-        cp_async4(&buf->wl[t], &in.wl[i]);
-        cp_async4(&buf->type[t], &in.type[i]);
-        cp_async4(&buf->ident[t], &in.ident[i]);
+        cp_async8(&buf->ox[t], &in.ox[s]);
+        cp_async8(&buf->oy[t], &in.oy[s]);
+        cp_async8(&buf->oz[t], &in.oz[s]);
+        cp_async8(&buf->dx[t], &in.dx[s]);
+        cp_async8(&buf->dy[t], &in.dy[s]);
+        cp_async8(&buf->dz[t], &in.dz[s]);
+        if (full) {
+            cp_async8(&buf->ex[t], &in.ex[s]);
+            cp_async8(&buf->ey[t], &in.ey[s]);
+            cp_async8(&buf->ez[t], &in.ez[s]);
+            cp_async16(&buf->n[t], &in.n[s]);
+            cp_async16(&buf->e1[t], &in.e1[s]);
+            cp_async16(&buf->e2[t], &in.e2[s]);
+            cp_async8(&buf->opl[t], &in.opl[s]);
+            cp_async8(&buf->phase[t], &in.phase[s]);
+            cp_async4(&buf->wl[t], &in.wl[s]);
+            cp_async4(&buf->type[t], &in.type[s]);
+            cp_async4(&buf->ident[t], &in.ident[s]);
+        }
     }
     cp_async_commit();
 }
@@ -1008,7 +1145,7 @@ __device__ __forceinline__ unsigned map_entry(const GenArgs &A, unsigned tile, u
 
 __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
                                               float iz) {
-    if (b[6] == 0.0f) return 0.0f;
+    if (b[6] != 1.0f) return 0.0f;
     float t1 = (b[0] - ox) * ix, t2 = (b[3] - ox) * ix;
     float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
     t1 = (b[1] - oy) * iy;
@@ -1023,23 +1160,61 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
     return fmaxf(tmin, 0.0f);
 }
 
-// One block stages the tables once; then each of its warps traces sub-tiles
-// of 32 rays taken from a launch-wide counter until none are left, with no
-// barrier between warps, so the staging is paid once per resident block and
-// neither a slow sub-tile nor a slow warp holds up the others.
-// Dynamic shared memory: the plain kernel's tables, the mixed tables at mx_off
-// and, at tb_off, each thread's box-entry distance per culled face.
-// Three blocks (12 warps) per SM: up to 168 registers a thread and no spills;
-// at four blocks (128 registers) the spills cost more than the extra warps
-// hide (5 % slower on the lens-train benchmark).
+
+namespace mx {
+// Position of the r-th (from 0) set bit of m; m has more than r set bits.
+__device__ __forceinline__ unsigned nth_set_bit(unsigned m, unsigned r) {
+    unsigned pos = 0;
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1) {
+        const unsigned low = __popc(m & ((1u << w) - 1u));
+        if (r >= low) {
+            r -= low;
+            m >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
+
+// Whether a hit on face record f goes to the material kernel (its material
+// can produce children).
+__device__ __forceinline__ bool makes_children(const DevScene &S, int f) {
+    const int mat = S.faces[f].material;
+    if (mat < 0) return false;
+    const int t = S.mats[mat].type;
+    return t != RP_MAT_NONE && t != RP_MAT_OPAQUE;
+}
+}  // namespace mx
+
+// Resident blocks per SM the two kernels are compiled for: three (168
+// registers a thread) for both; at four (128 registers) the spills cost more
+// than the extra warps hide (config 2: 20.3 against 19.4 ms per step; the
+// material kernel alone at two blocks: 22.3 ms).
+#define MX_SEARCH_MIN_BLOCKS 3
+#define MX_MAT_MIN_BLOCKS 3
+
+// ---- the search kernel ------------------------------------------------------------
+// One block stages the tables once; then each of its warps takes 32-ray
+// sub-tiles from a launch-wide counter until none are left, with no barrier
+// between warps, so the staging is paid once per resident block and neither
+// a slow sub-tile nor a slow warp holds up the others.  The next sub-tile's
+// fields are copied into the warp's other shared-memory buffer (cp.async)
+// while the current one is searched.  For each ray: the nearest hit (culled
+// nearest-first over the specialised faces, then the FP64 faces), then the
+// ray's final record with its length and end face (gathered input) or just
+// those two fields (in place), and, when the generation keeps children, the
+// hit's ray parameter and face record for the material kernel.
+// Dynamic shared memory: the plain kernel's tables, the mixed tables at
+// mx_off, each thread's box-entry distance per culled face at tb_off, the
+// warps' input buffers at in_off and pass-through buffers at pass_off.
 template <bool FB>
-__global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A, unsigned mx_off, unsigned tb_off,
-                                                                      unsigned in_off, unsigned pass_off) {
+__global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
+    mixed_search_kernel(GenArgs A, unsigned mx_off, unsigned tb_off, unsigned in_off, unsigned pass_off) {
     using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ unsigned s_hits, s_term;
+    __shared__ unsigned s_hits;
     const unsigned lane = threadIdx.x & 31;
-    // this warp's two sub-tile input buffers (double-buffered)
     TileIn *bufs = reinterpret_cast<TileIn *>(smem + in_off) + 2 * (threadIdx.x >> 5);
     PassIn *pass = reinterpret_cast<PassIn *>(smem + pass_off) + (threadIdx.x >> 5);
     unsigned *s_counts;
@@ -1049,24 +1224,16 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
     float *tb = reinterpret_cast<float *>(smem + tb_off) + threadIdx.x;  // tb[f * RP_BLOCK]
     const float max_len = f_of_d(A.max_len);  // exact: max_length is a float
     stage_mixed(A, ml, mf, max_len);
-    if (threadIdx.x == 0) {
-        s_hits = 0;
-        s_term = 0;
-    }
+    if (threadIdx.x == 0) s_hits = 0;
     const unsigned long long n_sub = rp_n_sub(A.n_in);
-    const float e2t = f_of_d(A.e2_term);
-    __syncthreads();  // the staged tables and the counters are ready
+    __syncthreads();  // the staged tables and the counter are ready
 
-    // every warp takes sub-tiles from a launch-wide counter on its own; the
-    // next sub-tile's inputs are copied into the warp's other buffer while
-    // this one is traced (each lane copies and reads only its own slot)
-    // (with a gathered input the map entries of a sub-tile are loaded one
-    // sub-tile before its copies are queued)
     const bool gathered = A.in_map != nullptr;
     unsigned tile = claim_sub_tile(A.tile_next, lane);
     if (tile < n_sub) {
         const unsigned long long i0 = (unsigned long long)tile * RP_SUB + lane;
-        prefetch_ray(&bufs[0], A.in, i0, A.n_in, gathered ? (unsigned long long)map_entry(A, tile, lane, n_sub) : i0);
+        prefetch_ray(&bufs[0], A.in, i0, A.n_in, gathered ? (unsigned long long)map_entry(A, tile, lane, n_sub) : i0,
+                     gathered);
     }
     unsigned next = claim_sub_tile(A.tile_next, lane);
     unsigned next_src = map_entry(A, next, lane, n_sub);
@@ -1085,7 +1252,7 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
         }
         const unsigned long long ni = (unsigned long long)next * RP_SUB + lane;
         if (next < n_sub)
-            prefetch_ray(&bufs[(k + 1) & 1], A.in, ni, A.n_in, gathered ? (unsigned long long)next_src : ni);
+            prefetch_ray(&bufs[(k + 1) & 1], A.in, ni, A.n_in, gathered ? (unsigned long long)next_src : ni, gathered);
         else
             cp_async_commit();
         // this thread's copies for `tile` have landed (the pass-through group
@@ -1096,30 +1263,36 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
             cp_async_wait_prev();
         const unsigned long long src = active && gathered ? (unsigned long long)in.src[t] : i;  // the record in A.in
 
-        Best b;
-        b.len = ffm(max_len, 0.0f);
-        b.t = ffm(0.0f, 0.0f);
-        b.face = -1;
-        b.list = -1;
-        ff O[3], D[3], dlen = ffm(1.0f, 0.0f);
         if (active) {
+            Best b;
+            b.len = ffm(max_len, 0.0f);
+            b.t = ffm(0.0f, 0.0f);
+            b.face = -1;
+            b.list = -1;
+            ff O[3], D[3];
             O[0] = ff_of_d(in.ox[t]);
             O[1] = ff_of_d(in.oy[t]);
             O[2] = ff_of_d(in.oz[t]);
             D[0] = ff_of_d(in.dx[t]);
             D[1] = ff_of_d(in.dy[t]);
             D[2] = ff_of_d(in.dz[t]);
-            dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
+            const ff dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
             int cur = -1;
             LRay R;
             unsigned long long pend = 0;  // culled faces left to the FP64 path
+            Cand c1, c2;                  // the two nearest FP32 candidates of the specialised faces
+            cand_clear(c1);
+            cand_clear(c2);
+            const float dl = dlen.hi;
             if (A.one_list >= 0) {
                 // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
                 const int f = S.lists[A.one_list].first_face + A.one_face;
-                if (face_specialised(S.faces[f].type))
-                    try_face(S, ml, mf, f, A.one_list, cur, R, O, D, dlen, max_len, A.err, b);
-                else if constexpr (FB)
+                if (face_specialised(S.faces[f].type)) {
+                    try_face32(S, ml, mf, f, A.one_list, cur, R, O, D, dl, max_len, A.err, c1, c2);
+                    settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
+                } else if constexpr (FB) {
                     try_face_fp64(A, S, f, A.one_list, src, dlen, b);
+                }
             } else {
                 // culled nearest-first search over the first 64 faces, then the rest in order
                 const float dfx = D[0].hi, dfy = D[1].hi, dfz = D[2].hi;
@@ -1142,13 +1315,15 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
                     int sel = -1;
                     for (unsigned long long m = cand; m; m &= m - 1) {
                         int f = __ffsll((long long)m) - 1;
-                        float t = tb[f * RP_BLOCK];
-                        if (t < tsel) {
-                            tsel = t;
+                        float tf = tb[f * RP_BLOCK];
+                        if (tf < tsel) {
+                            tsel = tf;
                             sel = f;
                         }
                     }
-                    if (sel < 0 || tsel > b.len.hi * 1.000001f + 1e-4f) break;
+                    // boxes entered beyond the nearest FP32 candidate (with a
+                    // margin above the FP32 roots' error) cannot hold a nearer hit
+                    if (sel < 0 || tsel > fmaf(c1.d, 1.000244140625f, 1e-3f)) break;
                     cand &= ~(1ull << sel);
                     int l = S.face_list[sel];
                     if (l < 0 || l >= S.n_lists) {
@@ -1156,20 +1331,22 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
                         break;
                     }
                     if (face_specialised(S.faces[sel].type))
-                        try_face(S, ml, mf, sel, l, cur, R, O, D, dlen, max_len, A.err, b);
+                        try_face32(S, ml, mf, sel, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
                     else
                         pend |= 1ull << sel;
                 }
                 for (int f = nmask; f < nf; f++) {
                     if (!face_specialised(S.faces[f].type)) continue;
-                    if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f) continue;
+                    if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > fmaf(c1.d, 1.000244140625f, 1e-3f))
+                        continue;
                     int l = S.face_list[f];
                     if (l < 0 || l >= S.n_lists) {
                         atomicOr(A.err, ERR_SHAPE_STACK);
                         break;
                     }
-                    try_face(S, ml, mf, f, l, cur, R, O, D, dlen, max_len, A.err, b);
+                    try_face32(S, ml, mf, f, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
                 }
+                settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
                 // the FP64 faces: the nearest hit does not depend on the order of
                 // the tests, and the box bound stays valid against the final length
                 for (int f = 0; FB && f < nf; f++) {
@@ -1197,201 +1374,306 @@ __global__ void __launch_bounds__(RP_BLOCK, 3) generation_mixed_kernel(GenArgs A
                 A.in.len[i] = len64;
                 A.in.endf[i] = endf;
             }
+            if (A.emit) {
+                A.hit_t[i] = make_float2(b.t.hi, b.t.lo);
+                A.hit_face[i] = b.face;
+            }
             if (b.face >= 0) {
                 atomicAdd(&s_counts[b.face], 1u);
                 atomicAdd(&s_hits, 1u);
             }
         }
-        if (!A.emit) {
-            tile = next;
-            next = next2;
-            next_src = next2_src;
-            continue;
-        }
-
-        // ---- material ----
-        int nc = 0;
-        ChildF ch[2];
-        f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);  // unit normal (FP32 copy), E_vector
-        double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
-        bool fp64_children = false;
-        Child chd[2];
-        ChildCommon ccd;
-        if (active && b.face >= 0) {
-            const rp_face &F = S.faces[b.face];
-            const MxFace &M = mf[b.face];
-            const MxList &L = ml[b.list];
-            ff P[3];
-            P[0] = ff_add(O[0], ff_mul(b.t, D[0]));
-            P[1] = ff_add(O[1], ff_mul(b.t, D[1]));
-            P[2] = ff_add(O[2], ff_mul(b.t, D[2]));
-            origin[0] = d_of_ff(P[0]);
-            origin[1] = d_of_ff(P[1]);
-            origin[2] = d_of_ff(P[2]);
-            // the hit in the face list's frame, relative to the face vertex
-            ff lp[3];
-            if (L.ident) {
-                lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
-                lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
-                lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
-            } else {
-                ff_rotate(L, P, lp, true);
-            }
-            ff3 nn;
-            if (face_normal_ff(F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
-                if (F.invert_normal) nn = ff3_neg(nn);
-                if (!L.ident) {
-                    ff v[3] = {nn.x, nn.y, nn.z}, w[3];
-#pragma unroll
-                    for (int rr = 0; rr < 3; rr++)
-                        w[rr] = ff_add(ff_add(ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr), v[0]),
-                                              ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 1), v[1])),
-                                       ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 2), v[2]));
-                    nn = mkff3(w[0], w[1], w[2]);
-                }
-            } else if constexpr (FB) {
-                f3 n32 = fallback_normal(S, F, b.list, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
-                nn = mkff3(ffm(n32.x, 0.0f), ffm(n32.y, 0.0f), ffm(n32.z, 0.0f));
-            }
-            nrm = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
-            if (F.material >= 0) {
-                const rp_material &Mt = S.mats[F.material];
-                const ff lenn = ff_mul(b.len, ff_of_d(in.n[t].x));
-                opl = d_of_ff(ff_add(ff_of_d(in.opl[t]), lenn));
-                if (mat_specialised(Mt.type)) {
-                    RayF r;
-                    r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
-                    r.E = f3_of_d(in.ex[t], in.ey[t], in.ez[t]);
-                    r.e1 = cf_of_d(in.e1[t]);
-                    r.e2 = cf_of_d(in.e2[t]);
-                    r.n = in.n[t];
-                    r.type = in.type[t];
-                    r.wl = in.wl[t];
-                    const ff3 Dff = mkff3(D[0], D[1], D[2]);
-                    const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
-                    nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
-                    if (A.e2_term > 0.0 && nc > 0) {
-                        int w = 0;
-                        for (int k = 0; k < nc; k++) {
-                            if (!(cabs2(ch[k].e1) + cabs2(ch[k].e2) < e2t)) {
-                                if (w != k) ch[w] = ch[k];
-                                w++;
-                            }
-                        }
-                        if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
-                        nc = w;
-                    }
-                } else if constexpr (FB) {
-                    unsigned term = 0;
-                    nc = fallback_children(A, S, F, Mt, b.list, src, d_of_ff(b.len), origin, nrm, &ccd, chd, &term);
-                    fp64_children = true;
-                    if (term) atomicAdd(&s_term, term);
-                }
-            }
-        }
-        // children go to the sub-tile's slot range in parent order: the
-        // exclusive warp scan of the per-ray counts is each ray's first slot
-        unsigned sub_children;
-        const unsigned excl = warp_scan((unsigned)nc, &sub_children);
-        if (nc > 0) {
-            const double phase = in.phase[t];
-            const unsigned wl = in.wl[t], ident = in.ident[t];
-            const unsigned endf = (unsigned)S.faces[b.face].idx;
-            const unsigned long long slot = (unsigned long long)tile * RP_SUB_SLOTS + excl;
-            for (int k = 0; k < nc; k++) {
-                if (FB && fp64_children)
-                    store_child(A.scratch, slot + k, ccd, chd[k], phase, wl, (unsigned)i, endf, ident);
-                else
-                    store_child_f(A.scratch, slot + k, origin, nrm, Eo, opl, ch[k], phase, wl, (unsigned)i, endf,
-                                  ident);
-            }
-        }
-        if (lane == 0) A.tile_counts[tile] = sub_children;
         tile = next;
         next = next2;
         next_src = next2_src;
     }
     flush_counts(A, S, s_counts);
-    if (threadIdx.x == 0) {
-        atomicAdd(&A.stats[0], (unsigned long long)s_hits);
-        if (s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
-    }
+    if (threadIdx.x == 0) atomicAdd(&A.stats[0], (unsigned long long)s_hits);
 }
 
-// Resident blocks for one instantiation and shared-memory size, cached per
-// (device, size) under a lock: several host threads (server lanes) launch.
+// ---- the material kernel ----------------------------------------------------------
+// Each warp takes groups of RP_GROUP rays from a launch-wide counter.  The
+// rays of a group whose hit material can produce children are compacted, in
+// ray order, into chunks of 32 (ballots of the hand-over's face records), so
+// that every lane of a chunk evaluates a hit: misses, absorbing faces and
+// faces without a material never occupy a lane.  Each lane rebuilds its hit
+// point, normal and optical path from the ray's final record and the
+// hand-over's float-float ray parameter, evaluates the material and keeps
+// the children above the |E|^2 threshold; a warp scan of the chunk's child
+// counts plus the group's running count places them in the group's slot
+// range (RP_TILE_SLOTS slots) in parent order, reflected before transmitted,
+// and the group's total goes to tile_counts[group].
 template <bool FB>
-static cudaError_t mixed_grid_blocks(size_t total, int *blocks) {
+__global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS) mixed_material_kernel(GenArgs A, unsigned mx_off) {
+    using namespace mx;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ unsigned s_term;
+    const unsigned lane = threadIdx.x & 31;
+    unsigned *s_counts;
+    DevScene S = stage_tables(A, smem, &s_counts);
+    MxList *ml = reinterpret_cast<MxList *>(smem + mx_off);
+    MxFace *mf = reinterpret_cast<MxFace *>(ml + A.S.n_lists);
+    const float max_len = f_of_d(A.max_len);
+    stage_mixed(A, ml, mf, max_len);
+    if (threadIdx.x == 0) s_term = 0;
+    const float e2t = f_of_d(A.e2_term);
+    const RaySoA Rr = A.in_map ? A.wb : A.in;  // the generation's records, written by the search kernel
+    const unsigned long long n_groups = rp_n_units(A.n_in, RP_GROUP);
+    __syncthreads();
+
+    for (;;) {
+        const unsigned q = claim_sub_tile(A.group_next, lane);
+        if (q >= n_groups) break;
+        const unsigned long long g0 = (unsigned long long)q * RP_GROUP;
+        unsigned mk[RP_GROUP / 32];
+#pragma unroll
+        for (int c = 0; c < RP_GROUP / 32; c++) {
+            const unsigned long long i = g0 + 32 * c + lane;
+            bool m = false;
+            if (i < A.n_in) {
+                const int f = A.hit_face[i];
+                m = f >= 0 && f < S.n_faces && makes_children(S, f);
+            }
+            mk[c] = __ballot_sync(0xffffffffu, m);
+        }
+        const unsigned p1 = __popc(mk[0]), p2 = p1 + __popc(mk[1]), p3 = p2 + __popc(mk[2]), total = p3 + __popc(mk[3]);
+        unsigned carry = 0;
+        for (unsigned k0 = 0; k0 < total; k0 += 32) {
+            const unsigned o = k0 + lane;
+            const bool act = o < total;
+            unsigned long long i = 0;
+            if (act) {
+                unsigned c, base, m;
+                if (o < p1) {
+                    c = 0; base = 0; m = mk[0];
+                } else if (o < p2) {
+                    c = 1; base = p1; m = mk[1];
+                } else if (o < p3) {
+                    c = 2; base = p2; m = mk[2];
+                } else {
+                    c = 3; base = p3; m = mk[3];
+                }
+                i = g0 + 32 * c + nth_set_bit(m, o - base);
+            }
+            int nc = 0;
+            ChildF ch[2];
+            f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);  // unit normal (FP32 copy), E_vector
+            double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
+            bool fp64_children = false;
+            Child chd[2];
+            ChildCommon ccd;
+            int face = -1;
+            if (act) {
+                face = A.hit_face[i];
+                const float2 th = A.hit_t[i];
+                const ff tt = ffm(th.x, th.y);
+                const rp_face &F = S.faces[face];
+                const int l = S.face_list[face];
+                if (l < 0 || l >= S.n_lists) {
+                    atomicOr(A.err, ERR_SHAPE_STACK);
+                } else {
+                    const MxFace &M = mf[face];
+                    const MxList &L = ml[l];
+                    ff O[3], D[3];
+                    O[0] = ff_of_d(Rr.ox[i]);
+                    O[1] = ff_of_d(Rr.oy[i]);
+                    O[2] = ff_of_d(Rr.oz[i]);
+                    D[0] = ff_of_d(Rr.dx[i]);
+                    D[1] = ff_of_d(Rr.dy[i]);
+                    D[2] = ff_of_d(Rr.dz[i]);
+                    const ff dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
+                    const ff lenff = ff_mul(tt, dlen);
+                    ff P[3];
+                    P[0] = ff_add(O[0], ff_mul(tt, D[0]));
+                    P[1] = ff_add(O[1], ff_mul(tt, D[1]));
+                    P[2] = ff_add(O[2], ff_mul(tt, D[2]));
+                    origin[0] = d_of_ff(P[0]);
+                    origin[1] = d_of_ff(P[1]);
+                    origin[2] = d_of_ff(P[2]);
+                    // the hit in the face list's frame, relative to the face vertex
+                    ff lp[3];
+                    if (L.ident) {
+                        lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
+                        lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
+                        lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
+                    } else {
+                        ff_rotate(L, P, lp, true);
+                    }
+                    ff3 nn;
+                    if (face_normal_ff(F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
+                        if (F.invert_normal) nn = ff3_neg(nn);
+                        if (!L.ident) {
+                            ff v[3] = {nn.x, nn.y, nn.z}, w[3];
+#pragma unroll
+                            for (int rr = 0; rr < 3; rr++)
+                                w[rr] = ff_add(ff_add(ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr), v[0]),
+                                                      ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 1), v[1])),
+                                               ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 2), v[2]));
+                            nn = mkff3(w[0], w[1], w[2]);
+                        }
+                    } else if constexpr (FB) {
+                        f3 n32 = fallback_normal(S, F, l, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
+                        nn = mkff3(ffm(n32.x, 0.0f), ffm(n32.y, 0.0f), ffm(n32.z, 0.0f));
+                    }
+                    nrm = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
+                    const rp_material &Mt = S.mats[F.material];
+                    const double2 nin = Rr.n[i];
+                    opl = d_of_ff(ff_add(ff_of_d(Rr.opl[i]), ff_mul(lenff, ff_of_d(nin.x))));
+                    if (mat_specialised(Mt.type)) {
+                        RayF r;
+                        r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
+                        r.E = f3_of_d(Rr.ex[i], Rr.ey[i], Rr.ez[i]);
+                        r.e1 = cf_of_d(Rr.e1[i]);
+                        r.e2 = cf_of_d(Rr.e2[i]);
+                        r.n = nin;
+                        r.type = Rr.type[i];
+                        r.wl = Rr.wl[i];
+                        const ff3 Dff = mkff3(D[0], D[1], D[2]);
+                        const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
+                        nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
+                        if (A.e2_term > 0.0 && nc > 0) {
+                            // the |E|^2 rule, children kept in order (fixed indices: registers)
+                            const bool k0 = !(cabs2(ch[0].e1) + cabs2(ch[0].e2) < e2t);
+                            const bool k1 = nc > 1 && !(cabs2(ch[1].e1) + cabs2(ch[1].e2) < e2t);
+                            if (!k0 && k1) ch[0] = ch[1];
+                            const int w = (int)k0 + (int)k1;
+                            if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
+                            nc = w;
+                        }
+                    } else if constexpr (FB) {
+                        unsigned term = 0;
+                        nc = fallback_children(A, S, F, Mt, l, Rr, i, d_of_ff(lenff), origin, nrm, &ccd, chd, &term);
+                        fp64_children = true;
+                        if (term) atomicAdd(&s_term, term);
+                    }
+                }
+            }
+            // the chunk's children go to the group's slot range in parent
+            // order: the group's running count plus the exclusive warp scan
+            unsigned chunk_children;
+            const unsigned excl = warp_scan((unsigned)nc, &chunk_children);
+            if (nc > 0) {
+                const double phase = Rr.phase[i];
+                const unsigned wl = Rr.wl[i], ident = Rr.ident[i];
+                const unsigned endf = (unsigned)S.faces[face].idx;
+                const unsigned long long slot = (unsigned long long)q * RP_TILE_SLOTS + carry + excl;
+                if (FB && fp64_children) {
+                    for (int kk = 0; kk < nc; kk++)
+                        store_child(A.scratch, slot + kk, ccd, chd[kk], phase, wl, (unsigned)i, endf, ident);
+                } else {
+                    store_child_f(A.scratch, slot, origin, nrm, Eo, opl, ch[0], phase, wl, (unsigned)i, endf, ident);
+                    if (nc > 1)
+                        store_child_f(A.scratch, slot + 1, origin, nrm, Eo, opl, ch[1], phase, wl, (unsigned)i, endf,
+                                      ident);
+                }
+            }
+            carry += chunk_children;
+        }
+        if (lane == 0) A.tile_counts[q] = carry;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
+}
+
+// ---- launches ---------------------------------------------------------------------
+// Resident blocks for one kernel and shared-memory size, cached per (kernel,
+// device, size) under a lock: several host threads (server lanes) launch.
+template <typename K>
+static cudaError_t resident_grid(K kernel, size_t total, int *blocks) {
     static std::mutex mu;
-    static std::map<std::pair<int, size_t>, int> cache;
-    static std::map<int, size_t> limit;  // the kernel's shared-memory limit per device: only ever raised
+    static std::map<std::tuple<const void *, int, size_t>, int> cache;
+    static std::map<std::pair<const void *, int>, size_t> limit;  // shared-memory limit set per (kernel, device)
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    const void *key = reinterpret_cast<const void *>(kernel);
     std::lock_guard<std::mutex> lock(mu);
-    auto it = cache.find({dev, total});
+    auto it = cache.find({key, dev, total});
     if (it != cache.end()) {
         *blocks = it->second;
         return cudaSuccess;
     }
-    if (limit[dev] < total) {
-        e = cudaFuncSetAttribute(generation_mixed_kernel<FB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)total);
+    size_t &lim = limit[{key, dev}];
+    if (lim < total) {
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)total);
         if (e != cudaSuccess) return e;
-        limit[dev] = total;
+        lim = total;
     }
     int sms = 0, per_sm = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, generation_mixed_kernel<FB>, RP_BLOCK, total);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, RP_BLOCK, total);
     if (e != cudaSuccess) return e;
     *blocks = (per_sm > 0 ? per_sm : 1) * sms;
-    cache[{dev, total}] = *blocks;
+    cache[{key, dev, total}] = *blocks;
     return cudaSuccess;
 }
 
-static size_t mixed_smem_total(const GenArgs &a, size_t smem, size_t *mx_off, size_t *tb_off, size_t *in_off,
-                               size_t *pass_off) {
-    *mx_off = (smem + 15) & ~(size_t)15;
-    *tb_off = *mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
+struct MixedLayout {
+    size_t mx_off, tb_off, in_off, pass_off, search_total, mat_total;
+};
+
+static MixedLayout mixed_layout(const GenArgs &a, size_t smem) {
+    MixedLayout L;
+    L.mx_off = (smem + 15) & ~(size_t)15;
+    L.tb_off = L.mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
+    L.mat_total = L.tb_off;
     const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
-    *in_off = (*tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
-    *pass_off = *in_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
-    return *pass_off + (a.in_map ? RP_SUB_PER_BLOCK * sizeof(mx::PassIn) : 0);
+    L.in_off = (L.tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
+    L.pass_off = L.in_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
+    L.search_total = L.pass_off + (a.in_map ? RP_SUB_PER_BLOCK * sizeof(mx::PassIn) : 0);
+    return L;
 }
 
-static cudaError_t mixed_blocks(const GenArgs &a, size_t total, int *blocks) {
-    return a.mixed_fallback ? mixed_grid_blocks<true>(total, blocks) : mixed_grid_blocks<false>(total, blocks);
+static cudaError_t mixed_grids(const GenArgs &a, const MixedLayout &L, int *search_blocks, int *mat_blocks) {
+    cudaError_t e = a.mixed_fallback ? resident_grid(mixed_search_kernel<true>, L.search_total, search_blocks)
+                                     : resident_grid(mixed_search_kernel<false>, L.search_total, search_blocks);
+    if (e != cudaSuccess) return e;
+    return a.mixed_fallback ? resident_grid(mixed_material_kernel<true>, L.mat_total, mat_blocks)
+                            : resident_grid(mixed_material_kernel<false>, L.mat_total, mat_blocks);
 }
 
-// Runs the one-time per-size set-up of the launch (attribute, occupancy) so
-// that a later launch of the same configuration makes no other CUDA call, as
-// stream capture requires.
+// Runs the one-time per-size set-up of the launches (attributes, occupancy)
+// so that a later launch of the same configuration makes no other CUDA call,
+// as stream capture requires.
 cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem) {
-    size_t mx_off, tb_off, in_off, pass_off;
-    const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off, &pass_off);
-    if (total > 220 * 1024) return cudaErrorInvalidConfiguration;
-    int blocks = 0;
-    return mixed_blocks(a, total, &blocks);
+    const MixedLayout L = mixed_layout(a, smem);
+    if (L.search_total > 220 * 1024) return cudaErrorInvalidConfiguration;
+    int sb = 0, mb = 0;
+    return mixed_grids(a, L, &sb, &mb);
 }
 
-// The scene's faces and materials decide the instantiation: without FP64
-// fallbacks the kernel carries no out-of-line calls and their register cost.
-cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st) {
+// The search kernel, then (when the generation keeps children) the material
+// kernel.  The scene's faces and materials decide the instantiation: without
+// FP64 fallbacks the kernels carry no out-of-line calls and their register
+// cost.  The caller has zeroed the tile and group counters.
+cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st, cudaEvent_t mid) {
     if (a.n_in == 0) return cudaSuccess;
-    size_t mx_off, tb_off, in_off, pass_off;
-    const size_t total = mixed_smem_total(a, smem, &mx_off, &tb_off, &in_off, &pass_off);
-    if (total > 220 * 1024) return cudaErrorInvalidConfiguration;  // scene too large for the per-block tables
-    int blocks = 0;
-    cudaError_t e = mixed_blocks(a, total, &blocks);
+    if (a.emit && (!a.hit_t || !a.hit_face || !a.group_next || a.unit_rays != RP_GROUP))
+        return cudaErrorInvalidValue;  // the hand-over and the group unit are set up by the caller
+    const MixedLayout L = mixed_layout(a, smem);
+    if (L.search_total > 220 * 1024) return cudaErrorInvalidConfiguration;  // scene too large for the tables
+    int sb = 0, mb = 0;
+    cudaError_t e = mixed_grids(a, L, &sb, &mb);
     if (e != cudaSuccess) return e;
     const unsigned long long n_tiles = (a.n_in + RP_BLOCK - 1) / RP_BLOCK;
-    const unsigned grid = (unsigned)(n_tiles < (unsigned long long)blocks ? n_tiles : blocks);
-    const unsigned o1 = (unsigned)mx_off, o2 = (unsigned)tb_off, o3 = (unsigned)in_off, o4 = (unsigned)pass_off;
+    const unsigned sgrid = (unsigned)(n_tiles < (unsigned long long)sb ? n_tiles : sb);
+    const unsigned o1 = (unsigned)L.mx_off, o2 = (unsigned)L.tb_off, o3 = (unsigned)L.in_off, o4 = (unsigned)L.pass_off;
     if (a.mixed_fallback)
-        generation_mixed_kernel<true><<<grid, RP_BLOCK, total, st>>>(a, o1, o2, o3, o4);
+        mixed_search_kernel<true><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
     else
-        generation_mixed_kernel<false><<<grid, RP_BLOCK, total, st>>>(a, o1, o2, o3, o4);
+        mixed_search_kernel<false><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && mid) e = cudaEventRecord(mid, st);
+    if (e != cudaSuccess || !a.emit) return e;
+    // one warp per group: RP_SUB_PER_BLOCK groups per block
+    const unsigned long long n_groups = rp_n_units(a.n_in, RP_GROUP);
+    const unsigned long long need = (n_groups + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK;
+    const unsigned mgrid = (unsigned)(need < (unsigned long long)mb ? need : mb);
+    if (a.mixed_fallback)
+        mixed_material_kernel<true><<<mgrid, RP_BLOCK, L.mat_total, st>>>(a, o1);
+    else
+        mixed_material_kernel<false><<<mgrid, RP_BLOCK, L.mat_total, st>>>(a, o1);
     return cudaGetLastError();
 }
 

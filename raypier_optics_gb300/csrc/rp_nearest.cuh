@@ -10,7 +10,7 @@ namespace rp {
 // 0 for faces that are always tested, +inf for a miss.
 __device__ __forceinline__ float box_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
                                            float iz) {
-    if (b[6] == 0.0f) return 0.0f;
+    if (b[6] != 1.0f) return 0.0f;
     float t1 = (b[0] - ox) * ix, t2 = (b[3] - ox) * ix;
     float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
     t1 = (b[1] - oy) * iy;
@@ -79,6 +79,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
             cur_list = l;
         }
         const rp_face &F = S.faces[sel];
+        if (distortion_line_misses(S.bounds + 8 * sel, p1, p2)) continue;
         double dist = face_isect(S, F, p1, p2, err);
         if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && sel < best))) {
             len = dist;
@@ -101,6 +102,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
             cur_list = l;
         }
         const rp_face &F = S.faces[f];
+        if (distortion_line_misses(S.bounds + 8 * f, p1, p2)) continue;
         double dist = face_isect(S, F, p1, p2, err);
         if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && f < best))) {
             len = dist;

@@ -228,7 +228,8 @@ uint64_t job_estimate(const Job *j) {
 int lane_scratch(Lane *L, uint64_t n_tiles) {
     const size_t nb_tally = (size_t)((n_tiles * RP_BLOCK + RP_TALLY_BLOCK - 1) / RP_TALLY_BLOCK);
     const uint64_t n_sub = n_tiles * RP_SUB_PER_BLOCK;  // count entries are per 32-ray sub-tile
-    const size_t need = 64 + align256s(n_sub * 4) + align256s(n_sub * 8) + align256s(nb_tally * RP_TALLY_N * 8);
+    const size_t need = 64 + align256s(n_sub * 4) + align256s(n_sub * 8) + rp_hit_bytes(n_sub * RP_SUB) +
+                        align256s(nb_tally * RP_TALLY_N * 8);
     if (need <= L->scratch_bytes) return RP_OK;
     if (L->scratch) {
         cudaStreamSynchronize(L->ctx->stream);
@@ -284,10 +285,11 @@ int run_generation(Lane *L, rp_scene *sc, rp_rays *in, rp_rays *out, const Job *
     const uint64_t n_sub = n_tiles * RP_SUB_PER_BLOCK;
     a.tile_counts = (unsigned *)(sc0 + 64);
     a.tile_offsets = (unsigned long long *)(sc0 + 64 + align256s(n_sub * 4));
-    double *partials = (double *)(sc0 + 64 + align256s(n_sub * 4) + align256s(n_sub * 8));
+    double *partials = (double *)(sc0 + 64 + align256s(n_sub * 4) + align256s(n_sub * 8) + rp_hit_bytes(n_sub * RP_SUB));
     a.scratch = emit ? L->arena->soa : in->soa;
     a.face_counts = sc->face_counts;
     const bool mixed = (j->flags & RP_TRACE_MIXED) != 0;
+    rp__set_mixed_handover(a, j->flags, sc0, n_sub);
     cudaError_t e = mixed ? prepare_generation_mixed(a, sc->smem) : prepare_generation_plain(a, sc->smem);
     if (e != cudaSuccess) return rp__cuda_fail(e, "generation set-up");
     const unsigned nb_tally = (unsigned)((n + RP_TALLY_BLOCK - 1) / RP_TALLY_BLOCK);
@@ -298,8 +300,8 @@ int run_generation(Lane *L, rp_scene *sc, rp_rays *in, rp_rays *out, const Job *
     if (e != cudaSuccess) return rp__cuda_fail(e, "cudaStreamBeginCapture");
     cudaError_t ce = cudaMemsetAsync(sc0, 0, 64, st);
     if (ce == cudaSuccess) ce = mixed ? launch_generation_mixed(a, sc->smem, st) : launch_generation_plain(a, sc->smem, st);
-    if (ce == cudaSuccess && emit) ce = launch_tile_scan(a, rp_n_sub(n), st);
-    if (ce == cudaSuccess && emit) ce = launch_place_children(a, rp_n_sub(n), st);
+    if (ce == cudaSuccess && emit) ce = launch_tile_scan(a, st);
+    if (ce == cudaSuccess && emit) ce = launch_place_children(a, st);
     if (ce == cudaSuccess && j->detector >= 0) {
         tally_kernel<<<nb_tally, RP_TALLY_BLOCK, 0, st>>>(in->soa, n, (unsigned)j->detector, partials);
         tally_finish_kernel<<<1, 32, 0, st>>>(partials, nb_tally, L->acc);

@@ -259,61 +259,69 @@ cudaError_t launch_count_scan(const unsigned *counts, unsigned long long n, unsi
     return cudaGetLastError();
 }
 
-cudaError_t launch_tile_scan(const GenArgs &a, unsigned long long n_sub, cudaStream_t st) {
-    tile_scan_kernel<<<1, 1024, 0, st>>>(a.tile_counts, n_sub, a.tile_offsets, a.out_count);
+cudaError_t launch_tile_scan(const GenArgs &a, cudaStream_t st) {
+    tile_scan_kernel<<<1, 1024, 0, st>>>(a.tile_counts, rp_n_units(a.n_in, a.unit_rays), a.tile_offsets, a.out_count);
     return cudaGetLastError();
 }
 
-// Moves each sub-tile's children from the front of its slot range to their
-// final place: one warp per sub-tile, a straight coalesced copy of
+// Slots of one child-slot unit (two per ray of the unit).
+__host__ __device__ __forceinline__ unsigned unit_slots(int unit_rays) {
+    return 2u * (unit_rays > 0 ? (unsigned)unit_rays : (unsigned)RP_SUB);
+}
+
+// Moves each unit's children from the front of its slot range to their
+// final place: one warp per unit, a straight coalesced copy of
 // tile_counts[q] records to tile_offsets[q].
-__global__ void __launch_bounds__(RP_BLOCK) place_children_kernel(GenArgs A, unsigned long long n_sub) {
-    const unsigned long long q = sub_tile_of_thread();
-    if (q >= n_sub) return;
+__global__ void __launch_bounds__(RP_BLOCK) place_children_kernel(GenArgs A, unsigned long long n_units) {
+    const unsigned long long q = sub_tile_of_thread();  // one warp per unit
+    if (q >= n_units) return;
     const unsigned lane = threadIdx.x & 31;
+    const unsigned us = unit_slots(A.unit_rays);
     const unsigned count = A.tile_counts[q];
     const unsigned long long base = A.tile_offsets[q];
-    if (count > RP_SUB_SLOTS || base + count > A.out_cap) {
+    if (count > us || base + count > A.out_cap) {
         if (lane == 0) atomicOr(A.err, ERR_OVERFLOW);
         return;
     }
-    const unsigned long long src = q * RP_SUB_SLOTS;
+    const unsigned long long src = q * us;
     for (unsigned j = lane; j < count; j += RP_SUB) copy_ray(A.scratch, src + j, A.out, base + j);
 }
 
-cudaError_t launch_place_children(const GenArgs &a, unsigned long long n_sub, cudaStream_t st) {
-    if (n_sub == 0) return cudaSuccess;
-    const unsigned grid = (unsigned)((n_sub + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK);
-    place_children_kernel<<<grid, RP_BLOCK, 0, st>>>(a, n_sub);
+cudaError_t launch_place_children(const GenArgs &a, cudaStream_t st) {
+    const unsigned long long n_units = rp_n_units(a.n_in, a.unit_rays);
+    if (n_units == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)((n_units + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK);
+    place_children_kernel<<<grid, RP_BLOCK, 0, st>>>(a, n_units);
     return cudaGetLastError();
 }
 
-// The children's gather map instead of their copy: child j of sub-tile q is
+// The children's gather map instead of their copy: child j of unit q is
 // ray tile_offsets[q] + j of the next generation and lives at arena slot
-// q * RP_SUB_SLOTS + j.  4 bytes per child instead of a 188-byte record read
-// and written: the next generation's kernel reads each record through the map
-// and writes it to its final place while tracing it.
+// q * (slots per unit) + j.  4 bytes per child instead of a 188-byte record
+// read and written: the next generation's kernel reads each record through
+// the map and writes it to its final place while tracing it.
 __global__ void __launch_bounds__(RP_BLOCK) child_map_kernel(const unsigned *counts,
                                                              const unsigned long long *offsets,
-                                                             unsigned long long n_sub, unsigned *map,
+                                                             unsigned long long n_units, unsigned us, unsigned *map,
                                                              unsigned long long map_cap, unsigned *err) {
-    const unsigned long long q = sub_tile_of_thread();
-    if (q >= n_sub) return;
+    const unsigned long long q = sub_tile_of_thread();  // one warp per unit
+    if (q >= n_units) return;
     const unsigned lane = threadIdx.x & 31;
     const unsigned count = counts[q];
     const unsigned long long base = offsets[q];
-    if (count > RP_SUB_SLOTS || base + count > map_cap) {
+    if (count > us || base + count > map_cap) {
         if (lane == 0) atomicOr(err, ERR_OVERFLOW);
         return;
     }
-    for (unsigned j = lane; j < count; j += RP_SUB) map[base + j] = (unsigned)(q * RP_SUB_SLOTS + j);
+    for (unsigned j = lane; j < count; j += RP_SUB) map[base + j] = (unsigned)(q * us + j);
 }
 
-cudaError_t launch_child_map(const GenArgs &a, unsigned long long n_sub, unsigned *map, unsigned long long map_cap,
-                             cudaStream_t st) {
-    if (n_sub == 0) return cudaSuccess;
-    const unsigned grid = (unsigned)((n_sub + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK);
-    child_map_kernel<<<grid, RP_BLOCK, 0, st>>>(a.tile_counts, a.tile_offsets, n_sub, map, map_cap, a.err);
+cudaError_t launch_child_map(const GenArgs &a, unsigned *map, unsigned long long map_cap, cudaStream_t st) {
+    const unsigned long long n_units = rp_n_units(a.n_in, a.unit_rays);
+    if (n_units == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)((n_units + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK);
+    child_map_kernel<<<grid, RP_BLOCK, 0, st>>>(a.tile_counts, a.tile_offsets, n_units, unit_slots(a.unit_rays), map,
+                                                map_cap, a.err);
     return cudaGetLastError();
 }
 

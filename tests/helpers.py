@@ -137,3 +137,31 @@ def assert_gausslet_generations(got_gens, exp_gens, exact=False, what=""):
         f"{what}: generation sizes {[len(g) for g in got_gens]} vs {[len(g) for g in exp_gens]}"
     for g, (a, b) in enumerate(zip(got_gens, exp_gens)):
         assert_gausslets(a, b, exact=exact, what=f"{what} gen {g}")
+
+
+def oracle_trace_parallel(tables, wavelengths, records, recursion_limit, max_length, e2_terminate=0.0, chunks=None,
+                          counts=False):
+    """The oracle's trace of `records`, cut into contiguous chunks traced on
+    threads (the oracle is re-entrant and ctypes releases the GIL around each
+    call), merged back into the single-trace order with parent indices
+    rebased.  Returns the generations (and, with counts=True, also the
+    per-face hit counts summed over the chunks).  Every ray's children depend
+    on that ray alone, so the merge equals one trace of all the rays."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    from raypier_optics_gb300 import shard
+    n = len(records)
+    k = chunks or max(1, min(os.cpu_count() or 1, 32, (n + 1023) // 1024))
+    bounds = [shard.shard_bounds(n, k, r) for r in range(k)]
+
+    def one(b):
+        lo, hi = b
+        return oracle.trace_rays(tables, wavelengths, np.ascontiguousarray(records[lo:hi]), recursion_limit,
+                                 max_length, e2_terminate)
+
+    with ThreadPoolExecutor(k) as ex:
+        per = list(ex.map(one, bounds))
+    gens = shard.merge_generations([p[0] for p in per])
+    if counts:
+        return gens, np.sum([np.asarray(p[1], dtype=np.int64) for p in per], axis=0)
+    return gens

@@ -21,6 +21,25 @@ def boxes(tables):
     return out
 
 
+def line_misses(b, p1, u):
+    """The kernels' distortion-face cull restated: the line p1 + s u (local
+    frame) never passes over the rectangle b[0..3] = x0, x1, y0, y1."""
+    x0, x1, y0, y1 = (float(v) for v in b[:4])
+    ux, uy = u[:, 0], u[:, 1]
+    corners = [(x0, y0), (x0, y1), (x1, y0), (x1, y1)]
+    s = np.stack([ux * (cy - p1[:, 1]) - uy * (cx - p1[:, 0]) for cx, cy in corners], axis=1)
+    along_z = (ux == 0) & (uy == 0)
+    outside = (p1[:, 0] < x0) | (p1[:, 0] > x1) | (p1[:, 1] < y0) | (p1[:, 1] > y1)
+    return np.where(along_z, outside, np.all(s > 0, axis=1) | np.all(s < 0, axis=1))
+
+
+def list_of_record(tables, k):
+    for L in tables.lists:
+        if L["first_face"] <= k < L["first_face"] + L["n_faces"]:
+            return L
+    raise KeyError(k)
+
+
 def check_hits_inside(tables, gens):
     b = boxes(tables)
     idx_of = {int(f["idx"]): k for k, f in enumerate(tables.faces[:tables.n_faces])}
@@ -31,6 +50,16 @@ def check_hits_inside(tables, gens):
         recs = np.array([idx_of[int(i)] for i in g["end_face_idx"][hit]], dtype=np.int64)
         for k in np.unique(recs):
             if b[k, 6] == 0:
+                continue
+            if b[k, 6] == 2:
+                # a distortion face: every ray that hit it must pass the line cull
+                L = list_of_record(tables, int(k))
+                m = L["inv_trans"]["m"].reshape(3, 3)
+                sel = np.flatnonzero(hit)[recs == k]
+                p1 = g["origin"][sel] @ m.T + L["inv_trans"]["t"]
+                u = g["direction"][sel] @ m.T
+                assert not line_misses(b[k], p1, u).any(), f"face record {k}: a hit ray would be culled"
+                n_checked += len(sel)
                 continue
             p = pts[recs == k]
             lo, hi = b[k, :3].astype(np.float64), b[k, 3:6].astype(np.float64)
@@ -57,7 +86,7 @@ def test_benchmark_hits_lie_in_face_boxes(config):
         rays, wl = W.subsample(rays, wl, np.arange(0, 1 << 20, 128), per_ray_wavelength=True)
         spec, P = W.config2_spec(), W.CONFIG2
     else:
-        rays, wl = W.config3_rays(ctracer.ray_dtype, 512)
+        rays, wl = W.config3_rays(ctracer.ray_dtype, 2048)
         spec, P = W.config3_spec(), W.CONFIG3
     tables, _, _ = tables_for(spec)
     gens, _ = oracle.trace_rays(tables, wl, rays, P["recursion_limit"], P["max_length"], P["e2_terminate"])

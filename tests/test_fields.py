@@ -162,7 +162,8 @@ def test_gpu_neighbour_index_outside_the_lattice_raises():
 def test_gpu_sphere_projection_matches_the_oracle():
     r = U["rf_rays"].astype(ctracer.ray_dtype)
     c = r["origin"].mean(axis=0) + np.array([0.0, 0.0, 5.0])
-    radius = float(np.max(np.linalg.norm(r["origin"] - c, axis=1))) * 0.9
+    # rays further from the axis than the radius (they run along z) miss the sphere
+    radius = float(np.max(np.linalg.norm(r["origin"][:, :2] - c[:2], axis=1))) * 0.6
     exp = oracle.project_to_sphere(r, c, radius)
     got = fields.project_to_sphere(r, c, radius)
     assert 0 < len(exp) < len(r)

@@ -1,26 +1,35 @@
-"""The mixed FP32/FP64 path against the FP64 oracle.
+"""The mixed FP32 / float-float path against the FP64 oracle.
 
-Directions, normals and the polarisation / Fresnel arithmetic are FP32; ray
-positions, distances (quadratic roots, last asphere Newton step) and the
-optical path stay FP64.  Index fields agree with the oracle except for rays
-that graze an edge, so the checks are statistical: generation sizes within
-0.1 %, index agreement above 99.9 %, and the float error bounds below on the
-rays whose indices agree."""
+The mixed path computes the S/P projection, Fresnel coefficients and
+polarisation amplitudes in FP32, and positions, ray parameters (float-float
+Newton steps whose residuals are evaluated in float-float), directions,
+normals and the optical path in float-float; faces and materials it does not
+specialise run the plain path's FP64 code.  Its accuracy targets on the
+precision workload (configuration 2) are a position error of at most 10 nm
+and an optical-path error of at most 1 nm against the FP64 oracle; they are
+asserted here as MAXIMA over every ray of every generation of a
+65,536-ray sample.  Index fields agree with the oracle except where a ray
+grazes an edge; agreement is asserted on configurations 1 and 2 and
+reported with the number of rays whose indices differ."""
 import numpy as np
 import pytest
 
 import oracle
-from helpers import build, load_case, tables_for, trace_case_names
+from helpers import build, load_case, oracle_trace_parallel, tables_for, trace_case_names
 from raypier_optics_gb300 import ctracer, precision, tracer
 from raypier_optics_gb300 import workloads as W
 from raypier_optics_gb300.ctracer import RayCollection
 
 pytestmark = pytest.mark.gpu
 
-# bounds asserted on the rays whose indices match the FP64 oracle
-POSITION_NM_P99 = 100.0
-OPL_NM_P99 = 10.0
-DIRECTION_RAD_P99 = 1e-5
+# the precision form's targets, asserted as maxima on the configuration-2 sample
+POSITION_NM_MAX = 10.0
+OPL_NM_MAX = 1.0
+DIRECTION_RAD_MAX = 1e-6
+# looser bounds for the face / material zoo, whose scenes put rays at grazing
+# incidence on purpose, and for the FP64-fallback faces of configuration 3
+ZOO_POSITION_NM_P99 = 100.0
+ZOO_OPL_NM_P99 = 10.0
 
 
 def mixed_trace(spec, rays, wl, P):
@@ -32,27 +41,31 @@ def mixed_trace(spec, rays, wl, P):
     return [t.copy_as_array() for t in traced]
 
 
-@pytest.mark.parametrize("config", ["config1", "config2"])
-def test_mixed_path_accuracy_against_oracle(config):
+def _sample(config, n):
     if config == "config1":
         rays, wl = W.config1_rays(ctracer.ray_dtype)
-        spec, P = W.config1_spec(), W.CONFIG1
-    else:
-        rays, wl = W.config2_rays(ctracer.ray_dtype, 1 << 20)
-        rays, wl = W.subsample(rays, wl, np.arange(0, 1 << 20, 256), per_ray_wavelength=True)
-        spec, P = W.config2_spec(), W.CONFIG2
+        return rays, wl, W.config1_spec(), W.CONFIG1
+    rays, wl = W.config2_rays(ctracer.ray_dtype, 1 << 20)
+    idx = np.linspace(0, (1 << 20) - 1, n).astype(np.int64)
+    rays, wl = W.subsample(rays, wl, idx, per_ray_wavelength=True)
+    return rays, wl, W.config2_spec(), W.CONFIG2
+
+
+@pytest.mark.parametrize("config,n", [("config1", 4096), ("config2", 65536)])
+def test_mixed_path_meets_its_accuracy_targets(config, n):
+    """Maximum position, optical-path and direction errors against the FP64
+    oracle over every ray of every generation, with index agreement."""
+    rays, wl, spec, P = _sample(config, n)
     gens = mixed_trace(spec, rays, wl, P)
     tables, _, _ = tables_for(spec)
-    ogens, _ = oracle.trace_rays(tables, wl, rays, P["recursion_limit"], P["max_length"], P["e2_terminate"])
-    sizes, osizes = [len(g) for g in gens], [len(g) for g in ogens]
-    assert len(sizes) == len(osizes)
-    assert all(abs(a - b) <= max(2, 1e-3 * b) for a, b in zip(sizes, osizes)), (sizes, osizes)
+    ogens = oracle_trace_parallel(tables, wl, rays, P["recursion_limit"], P["max_length"], P["e2_terminate"])
     st = precision.compare_traces(gens, ogens)
     print(config, st)
-    assert st["index_agreement"] > 0.999
-    assert st["position_nm"]["p99"] < POSITION_NM_P99
-    assert st["opl_nm"]["p99"] < OPL_NM_P99
-    assert st["direction_rad"]["p99"] < DIRECTION_RAD_P99
+    assert st["generation_sizes_equal"], ([len(g) for g in gens], [len(g) for g in ogens])
+    assert st["index_agreement"] == 1.0, st
+    assert st["position_nm"]["max"] <= POSITION_NM_MAX, st
+    assert st["opl_nm"]["max"] <= OPL_NM_MAX, st
+    assert st["direction_rad"]["max"] <= DIRECTION_RAD_MAX, st
 
 
 def test_mixed_path_config3_runs_and_mostly_agrees():
@@ -67,9 +80,9 @@ def test_mixed_path_config3_runs_and_mostly_agrees():
 
 @pytest.mark.parametrize("name", [n for n in trace_case_names() if n.startswith(("face_", "mat_"))])
 def test_mixed_path_on_every_face_and_material_case(name):
-    """Each face and material type through the mixed kernel (its float-float
-    code where it has one, its FP64 code otherwise) against the reference's
-    golden trace of the same rays."""
+    """Each face and material type through the mixed kernels (their
+    float-float code where they have one, their FP64 code otherwise) against
+    the reference's golden trace of the same rays."""
     c = load_case(name)
     P = dict(c["params"])
     P.setdefault("e2_terminate", 0.0)
@@ -79,5 +92,5 @@ def test_mixed_path_on_every_face_and_material_case(name):
     assert len(sizes) == len(osizes) and all(abs(a - b) <= 2 for a, b in zip(sizes, osizes)), (sizes, osizes)
     assert st["index_agreement"] > 0.97, st
     if st["position_nm"]["p99"] is not None:
-        assert st["position_nm"]["p99"] < POSITION_NM_P99, st
-        assert st["opl_nm"]["p99"] < OPL_NM_P99, st
+        assert st["position_nm"]["p99"] < ZOO_POSITION_NM_P99, st
+        assert st["opl_nm"]["p99"] < ZOO_OPL_NM_P99, st
