@@ -219,6 +219,7 @@ struct MxFace {
     float p[RP_FACE_NPARAM];
     float zv_hi, zv_lo;
     float rq_hi, rq_lo;  // the quadric's Rq as float-float (sphere: -curvature; conic, asphere: -p[0])
+    float ic_hi, ic_lo;  // a sphere's 1 / curvature as float-float (its unit normal is (p - centre) / c)
     float tmin;
     float tol;  // Face.tolerance (a distance) in FP32
 };
@@ -282,6 +283,10 @@ __device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace
         const ff r = ff_of_d(rq);
         o.rq_hi = r.hi;
         o.rq_lo = r.lo;
+        const bool sph = F.type == RP_FACE_SPHERICAL || F.type == RP_FACE_SHAPED_SPHERICAL;
+        const ff ic = sph && rq != 0.0 ? ff_of_d(-1.0 / rq) : ffm(0.0f, 0.0f);
+        o.ic_hi = ic.hi;
+        o.ic_lo = ic.lo;
         o.tmin = f_of_d(F.tolerance) * max_len;
         o.tol = f_of_d(F.tolerance);
     }
@@ -625,11 +630,13 @@ __device__ __forceinline__ bool face_normal_ff(const rp_face &F, const MxFace &M
         case RP_FACE_SHAPED_PLANAR: n = mkff3(zero, zero, ffm(1.0f, 0.0f)); return true;
         case RP_FACE_RECTANGULAR: n = mkff3(zero, zero, ffm(-1.0f, 0.0f)); return true;
         case RP_FACE_SPHERICAL:
-        case RP_FACE_SHAPED_SPHERICAL: {  // cfaces.pyx:485-498, 594-606: (p - centre), flipped for c < 0
-            float c = F.type == RP_FACE_SPHERICAL ? M.p[1] : M.p[0];
-            ff3 q = mkff3(x, y, ff_add_f(z, c));
-            if (c < 0.0f) q = ff3_neg(q);
-            n = ff3_unit(q);
+        case RP_FACE_SHAPED_SPHERICAL: {
+            // cfaces.pyx:485-498, 594-606: (p - centre) normalised, flipped for
+            // c < 0.  At a hit |p - centre| = |c| to float-float accuracy, so
+            // the unit normal is (p - centre) / c: (x, y, z + c) times 1 / c.
+            const ff ic = ffm(M.ic_hi, M.ic_lo);
+            const ff zc = ff_sub(z, ffm(M.rq_hi, M.rq_lo));  // z + c, with c = -Rq
+            n = mkff3(ff_mul(x, ic), ff_mul(y, ic), ff_mul(zc, ic));
             return true;
         }
         case RP_FACE_CONIC: {  // cfaces.pyx:1796-1820
@@ -873,13 +880,13 @@ __device__ __forceinline__ double fallback_dist(const GenArgs &A, const DevScene
     return face_isect(S, F, p1, p2, A.err);
 }
 
-// FP32 world normal of a face type this kernel does not specialise, from the
-// FP64 normal at the local hit point.
-__device__ __noinline__ f3 fallback_normal(const DevScene &S, const rp_face &F, int l, v3 lp, unsigned *err) {
+// World normal of a face type this kernel does not specialise: the FP64
+// normal at the local hit point, rotated, as float-float.
+__device__ __noinline__ ff3 fallback_normal_ff(const DevScene &S, const rp_face &F, int l, v3 lp, unsigned *err) {
     v3 n64 = face_normal(S, F, lp, err);
     if (F.invert_normal) n64 = negv(n64);
     n64 = rotv(S.lists[l].trans.m, n64);
-    return f3_of_d(n64.x, n64.y, n64.z);
+    return mkff3(ff_of_d(n64.x), ff_of_d(n64.y), ff_of_d(n64.z));
 }
 
 // Children of a material this kernel does not specialise (polarisers,
@@ -1085,6 +1092,7 @@ __device__ __forceinline__ void write_back(const TileIn &b, const PassIn &p, uns
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev2() { asm volatile("cp.async.wait_group 2;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Queues the copy of ray i's fields into the lane's slot of `buf` (nothing
 // for i beyond the generation) and closes the thread's copy group.
@@ -1208,7 +1216,12 @@ __device__ __forceinline__ bool makes_children(const DevScene &S, int f) {
 // Dynamic shared memory: the plain kernel's tables, the mixed tables at
 // mx_off, each thread's box-entry distance per culled face at tb_off, the
 // warps' input buffers at in_off and pass-through buffers at pass_off.
-template <bool FB>
+// TB: the box-entry distances of the first 64 faces are kept per thread in
+// shared memory (scenes of up to RP_MX_TB_FACES faces); larger scenes
+// recompute them in the nearest-first selection, so that their blocks are not
+// limited to one per SM by that table.
+#define RP_MX_TB_FACES 16
+template <bool FB, bool TB>
 __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
     mixed_search_kernel(GenArgs A, unsigned mx_off, unsigned tb_off, unsigned in_off, unsigned pass_off) {
     using namespace mx;
@@ -1307,7 +1320,7 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
                 unsigned long long cand = 0;
                 for (int f = 0; f < nmask; f++) {
                     float te = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                    tb[f * RP_BLOCK] = te;
+                    if constexpr (TB) tb[f * RP_BLOCK] = te;
                     if (te <= lim0) cand |= 1ull << f;
                 }
                 while (cand) {
@@ -1315,7 +1328,11 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
                     int sel = -1;
                     for (unsigned long long m = cand; m; m &= m - 1) {
                         int f = __ffsll((long long)m) - 1;
-                        float tf = tb[f * RP_BLOCK];
+                        float tf;
+                        if constexpr (TB)
+                            tf = tb[f * RP_BLOCK];
+                        else
+                            tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
                         if (tf < tsel) {
                             tsel = tf;
                             sel = f;
@@ -1351,7 +1368,13 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
                 // the tests, and the box bound stays valid against the final length
                 for (int f = 0; FB && f < nf; f++) {
                     if (f < nmask) {
-                        if (!((pend >> f) & 1ull) || tb[f * RP_BLOCK] > b.len.hi * 1.000001f + 1e-4f) continue;
+                        if (!((pend >> f) & 1ull)) continue;
+                        float tf;
+                        if constexpr (TB)
+                            tf = tb[f * RP_BLOCK];
+                        else
+                            tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+                        if (tf > b.len.hi * 1.000001f + 1e-4f) continue;
                     } else {
                         if (face_specialised(S.faces[f].type)) continue;
                         if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f)
@@ -1392,23 +1415,127 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
 }
 
 // ---- the material kernel ----------------------------------------------------------
+namespace mx {
+// One chunk's inputs for the material kernel: the fields of up to 32 hit
+// rays (structure of arrays, one slot per lane) with their hand-over.
+struct MatIn {
+    double ox[RP_SUB], oy[RP_SUB], oz[RP_SUB], dx[RP_SUB], dy[RP_SUB], dz[RP_SUB];
+    double ex[RP_SUB], ey[RP_SUB], ez[RP_SUB];
+    double2 n[RP_SUB], e1[RP_SUB], e2[RP_SUB];
+    double opl[RP_SUB], phase[RP_SUB];
+    float2 t[RP_SUB];
+    unsigned wl[RP_SUB], type[RP_SUB], ident[RP_SUB];
+    int face[RP_SUB];
+    unsigned idx[RP_SUB];  // the ray's index in the generation; 0xffffffff for an idle lane
+};
+
+// A group's rays that go to the material kernel: per 32-ray quarter the
+// ballot of hits whose material can produce children, and their prefix counts.
+struct GroupMask {
+    unsigned q;           // the group; n_groups when none is left
+    unsigned m[RP_GROUP / 32];
+    unsigned p1, p2, p3, total;
+};
+
+// Claims groups until one has material rays (a group without any gets its
+// zero child count at once); G.q = n_groups when none is left.
+__device__ __forceinline__ void claim_group(const GenArgs &A, const DevScene &S, unsigned long long n_groups,
+                                            unsigned lane, GroupMask &G) {
+    for (;;) {
+        const unsigned q = claim_sub_tile(A.group_next, lane);
+        G.q = q;
+        G.total = 0;
+        if (q >= n_groups) return;
+        const unsigned long long g0 = (unsigned long long)q * RP_GROUP;
+#pragma unroll
+        for (int c = 0; c < RP_GROUP / 32; c++) {
+            const unsigned long long i = g0 + 32 * c + lane;
+            bool m = false;
+            if (i < A.n_in) {
+                const int f = A.hit_face[i];
+                m = f >= 0 && f < S.n_faces && makes_children(S, f);
+            }
+            G.m[c] = __ballot_sync(0xffffffffu, m);
+        }
+        G.p1 = __popc(G.m[0]);
+        G.p2 = G.p1 + __popc(G.m[1]);
+        G.p3 = G.p2 + __popc(G.m[2]);
+        G.total = G.p3 + __popc(G.m[3]);
+        if (G.total > 0) return;
+        if (lane == 0) A.tile_counts[q] = 0u;
+    }
+}
+
+// The ray of chunk k of group G that this lane evaluates (in ray order), or
+// ~0 when the chunk has fewer rays than lanes.
+__device__ __forceinline__ unsigned long long chunk_ray(const GroupMask &G, unsigned k, unsigned lane) {
+    const unsigned o = 32 * k + lane;
+    if (o >= G.total) return ~0ull;
+    unsigned c, base, m;
+    if (o < G.p1) {
+        c = 0; base = 0; m = G.m[0];
+    } else if (o < G.p2) {
+        c = 1; base = G.p1; m = G.m[1];
+    } else if (o < G.p3) {
+        c = 2; base = G.p2; m = G.m[2];
+    } else {
+        c = 3; base = G.p3; m = G.m[3];
+    }
+    return (unsigned long long)G.q * RP_GROUP + 32 * c + nth_set_bit(m, o - base);
+}
+
+// Queues the copies of ray i's inputs into the lane's slot of B (nothing for
+// i = ~0) and closes the lane's copy group.
+__device__ __forceinline__ void prefetch_mat(MatIn *B, const GenArgs &A, const RaySoA &Rr, unsigned long long i,
+                                             unsigned lane) {
+    B->idx[lane] = i == ~0ull ? 0xffffffffu : (unsigned)i;
+    if (i != ~0ull) {
+        cp_async8(&B->ox[lane], &Rr.ox[i]);
+        cp_async8(&B->oy[lane], &Rr.oy[i]);
+        cp_async8(&B->oz[lane], &Rr.oz[i]);
+        cp_async8(&B->dx[lane], &Rr.dx[i]);
+        cp_async8(&B->dy[lane], &Rr.dy[i]);
+        cp_async8(&B->dz[lane], &Rr.dz[i]);
+        cp_async8(&B->ex[lane], &Rr.ex[i]);
+        cp_async8(&B->ey[lane], &Rr.ey[i]);
+        cp_async8(&B->ez[lane], &Rr.ez[i]);
+        cp_async16(&B->n[lane], &Rr.n[i]);
+        cp_async16(&B->e1[lane], &Rr.e1[i]);
+        cp_async16(&B->e2[lane], &Rr.e2[i]);
+        cp_async8(&B->opl[lane], &Rr.opl[i]);
+        cp_async8(&B->phase[lane], &Rr.phase[i]);
+        cp_async8(&B->t[lane], &A.hit_t[i]);
+        cp_async4(&B->wl[lane], &Rr.wl[i]);
+        cp_async4(&B->type[lane], &Rr.type[i]);
+        cp_async4(&B->ident[lane], &Rr.ident[i]);
+        cp_async4(&B->face[lane], &A.hit_face[i]);
+    }
+    cp_async_commit();
+}
+}  // namespace mx
+
 // Each warp takes groups of RP_GROUP rays from a launch-wide counter.  The
 // rays of a group whose hit material can produce children are compacted, in
 // ray order, into chunks of 32 (ballots of the hand-over's face records), so
 // that every lane of a chunk evaluates a hit: misses, absorbing faces and
-// faces without a material never occupy a lane.  Each lane rebuilds its hit
-// point, normal and optical path from the ray's final record and the
-// hand-over's float-float ray parameter, evaluates the material and keeps
-// the children above the |E|^2 threshold; a warp scan of the chunk's child
-// counts plus the group's running count places them in the group's slot
-// range (RP_TILE_SLOTS slots) in parent order, reflected before transmitted,
-// and the group's total goes to tile_counts[group].
+// faces without a material never occupy a lane.  The next chunk's inputs --
+// scattered records of the group's window -- are copied into the warp's other
+// shared-memory buffer (cp.async) while the current chunk computes, so the
+// loads' latency is hidden behind the arithmetic.  Each lane rebuilds its hit
+// point, normal and optical path from the ray's record and the hand-over's
+// float-float ray parameter, evaluates the material and keeps the children
+// above the |E|^2 threshold; a warp scan of the chunk's child counts plus the
+// group's running count places them in the group's slot range
+// (RP_TILE_SLOTS slots) in parent order, reflected before transmitted, and
+// the group's total goes to tile_counts[group].
 template <bool FB>
-__global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS) mixed_material_kernel(GenArgs A, unsigned mx_off) {
+__global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS) mixed_material_kernel(GenArgs A, unsigned mx_off,
+                                                                                    unsigned buf_off) {
     using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_term;
     const unsigned lane = threadIdx.x & 31;
+    MatIn *bufs = reinterpret_cast<MatIn *>(smem + buf_off) + 2 * (threadIdx.x >> 5);
     unsigned *s_counts;
     DevScene S = stage_tables(A, smem, &s_counts);
     MxList *ml = reinterpret_cast<MxList *>(smem + mx_off);
@@ -1421,156 +1548,149 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS) mixed_material_ke
     const unsigned long long n_groups = rp_n_units(A.n_in, RP_GROUP);
     __syncthreads();
 
-    for (;;) {
-        const unsigned q = claim_sub_tile(A.group_next, lane);
-        if (q >= n_groups) break;
-        const unsigned long long g0 = (unsigned long long)q * RP_GROUP;
-        unsigned mk[RP_GROUP / 32];
-#pragma unroll
-        for (int c = 0; c < RP_GROUP / 32; c++) {
-            const unsigned long long i = g0 + 32 * c + lane;
-            bool m = false;
-            if (i < A.n_in) {
-                const int f = A.hit_face[i];
-                m = f >= 0 && f < S.n_faces && makes_children(S, f);
-            }
-            mk[c] = __ballot_sync(0xffffffffu, m);
+    GroupMask G;
+    claim_group(A, S, n_groups, lane, G);
+    if (G.q < n_groups) prefetch_mat(&bufs[0], A, Rr, chunk_ray(G, 0, lane), lane);
+    unsigned k = 0, carry = 0;
+    for (unsigned step = 0; G.q < n_groups; step++) {
+        // the chunk after this one: the same group's next, or the next group's first
+        GroupMask Gn = G;
+        unsigned kn = k + 1;
+        const bool last_of_group = kn * 32 >= G.total;
+        if (last_of_group) {
+            claim_group(A, S, n_groups, lane, Gn);
+            kn = 0;
         }
-        const unsigned p1 = __popc(mk[0]), p2 = p1 + __popc(mk[1]), p3 = p2 + __popc(mk[2]), total = p3 + __popc(mk[3]);
-        unsigned carry = 0;
-        for (unsigned k0 = 0; k0 < total; k0 += 32) {
-            const unsigned o = k0 + lane;
-            const bool act = o < total;
-            unsigned long long i = 0;
-            if (act) {
-                unsigned c, base, m;
-                if (o < p1) {
-                    c = 0; base = 0; m = mk[0];
-                } else if (o < p2) {
-                    c = 1; base = p1; m = mk[1];
-                } else if (o < p3) {
-                    c = 2; base = p2; m = mk[2];
+        if (Gn.q < n_groups)
+            prefetch_mat(&bufs[(step + 1) & 1], A, Rr, chunk_ray(Gn, kn, lane), lane);
+        else
+            cp_async_commit();
+        cp_async_wait_prev();  // this lane's copies for the current chunk have landed
+        const MatIn &B = bufs[step & 1];
+        const unsigned t = lane;
+        const unsigned ridx = B.idx[t];
+        const bool act = ridx != 0xffffffffu;
+        const unsigned long long i = act ? (unsigned long long)ridx : 0ull;
+
+        int nc = 0;
+        ChildF ch[2];
+        f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);  // unit normal (FP32 copy), E_vector
+        double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
+        bool fp64_children = false;
+        Child chd[2];
+        ChildCommon ccd;
+        int face = -1;
+        if (act) {
+            face = B.face[t];
+            const ff tt = ffm(B.t[t].x, B.t[t].y);
+            const rp_face &F = S.faces[face];
+            const int l = S.face_list[face];
+            if (l < 0 || l >= S.n_lists) {
+                atomicOr(A.err, ERR_SHAPE_STACK);
+            } else {
+                const MxFace &M = mf[face];
+                const MxList &L = ml[l];
+                ff O[3], D[3];
+                O[0] = ff_of_d(B.ox[t]);
+                O[1] = ff_of_d(B.oy[t]);
+                O[2] = ff_of_d(B.oz[t]);
+                D[0] = ff_of_d(B.dx[t]);
+                D[1] = ff_of_d(B.dy[t]);
+                D[2] = ff_of_d(B.dz[t]);
+                const ff dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
+                const ff lenff = ff_mul(tt, dlen);
+                ff P[3];
+                P[0] = ff_add(O[0], ff_mul(tt, D[0]));
+                P[1] = ff_add(O[1], ff_mul(tt, D[1]));
+                P[2] = ff_add(O[2], ff_mul(tt, D[2]));
+                origin[0] = d_of_ff(P[0]);
+                origin[1] = d_of_ff(P[1]);
+                origin[2] = d_of_ff(P[2]);
+                // the hit in the face list's frame, relative to the face vertex
+                ff lp[3];
+                if (L.ident) {
+                    lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
+                    lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
+                    lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
                 } else {
-                    c = 3; base = p3; m = mk[3];
+                    ff_rotate(L, P, lp, true);
                 }
-                i = g0 + 32 * c + nth_set_bit(m, o - base);
-            }
-            int nc = 0;
-            ChildF ch[2];
-            f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);  // unit normal (FP32 copy), E_vector
-            double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
-            bool fp64_children = false;
-            Child chd[2];
-            ChildCommon ccd;
-            int face = -1;
-            if (act) {
-                face = A.hit_face[i];
-                const float2 th = A.hit_t[i];
-                const ff tt = ffm(th.x, th.y);
-                const rp_face &F = S.faces[face];
-                const int l = S.face_list[face];
-                if (l < 0 || l >= S.n_lists) {
-                    atomicOr(A.err, ERR_SHAPE_STACK);
-                } else {
-                    const MxFace &M = mf[face];
-                    const MxList &L = ml[l];
-                    ff O[3], D[3];
-                    O[0] = ff_of_d(Rr.ox[i]);
-                    O[1] = ff_of_d(Rr.oy[i]);
-                    O[2] = ff_of_d(Rr.oz[i]);
-                    D[0] = ff_of_d(Rr.dx[i]);
-                    D[1] = ff_of_d(Rr.dy[i]);
-                    D[2] = ff_of_d(Rr.dz[i]);
-                    const ff dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
-                    const ff lenff = ff_mul(tt, dlen);
-                    ff P[3];
-                    P[0] = ff_add(O[0], ff_mul(tt, D[0]));
-                    P[1] = ff_add(O[1], ff_mul(tt, D[1]));
-                    P[2] = ff_add(O[2], ff_mul(tt, D[2]));
-                    origin[0] = d_of_ff(P[0]);
-                    origin[1] = d_of_ff(P[1]);
-                    origin[2] = d_of_ff(P[2]);
-                    // the hit in the face list's frame, relative to the face vertex
-                    ff lp[3];
-                    if (L.ident) {
-                        lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
-                        lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
-                        lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
-                    } else {
-                        ff_rotate(L, P, lp, true);
-                    }
-                    ff3 nn;
-                    if (face_normal_ff(F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
-                        if (F.invert_normal) nn = ff3_neg(nn);
-                        if (!L.ident) {
-                            ff v[3] = {nn.x, nn.y, nn.z}, w[3];
+                ff3 nn;
+                if (face_normal_ff(F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
+                    if (F.invert_normal) nn = ff3_neg(nn);
+                    if (!L.ident) {
+                        ff v[3] = {nn.x, nn.y, nn.z}, w[3];
 #pragma unroll
-                            for (int rr = 0; rr < 3; rr++)
-                                w[rr] = ff_add(ff_add(ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr), v[0]),
-                                                      ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 1), v[1])),
-                                               ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 2), v[2]));
-                            nn = mkff3(w[0], w[1], w[2]);
-                        }
-                    } else if constexpr (FB) {
-                        f3 n32 = fallback_normal(S, F, l, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
-                        nn = mkff3(ffm(n32.x, 0.0f), ffm(n32.y, 0.0f), ffm(n32.z, 0.0f));
+                        for (int rr = 0; rr < 3; rr++)
+                            w[rr] = ff_add(ff_add(ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr), v[0]),
+                                                  ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 1), v[1])),
+                                           ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 2), v[2]));
+                        nn = mkff3(w[0], w[1], w[2]);
                     }
-                    nrm = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
-                    const rp_material &Mt = S.mats[F.material];
-                    const double2 nin = Rr.n[i];
-                    opl = d_of_ff(ff_add(ff_of_d(Rr.opl[i]), ff_mul(lenff, ff_of_d(nin.x))));
-                    if (mat_specialised(Mt.type)) {
-                        RayF r;
-                        r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
-                        r.E = f3_of_d(Rr.ex[i], Rr.ey[i], Rr.ez[i]);
-                        r.e1 = cf_of_d(Rr.e1[i]);
-                        r.e2 = cf_of_d(Rr.e2[i]);
-                        r.n = nin;
-                        r.type = Rr.type[i];
-                        r.wl = Rr.wl[i];
-                        const ff3 Dff = mkff3(D[0], D[1], D[2]);
-                        const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
-                        nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
-                        if (A.e2_term > 0.0 && nc > 0) {
-                            // the |E|^2 rule, children kept in order (fixed indices: registers)
-                            const bool k0 = !(cabs2(ch[0].e1) + cabs2(ch[0].e2) < e2t);
-                            const bool k1 = nc > 1 && !(cabs2(ch[1].e1) + cabs2(ch[1].e2) < e2t);
-                            if (!k0 && k1) ch[0] = ch[1];
-                            const int w = (int)k0 + (int)k1;
-                            if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
-                            nc = w;
-                        }
-                    } else if constexpr (FB) {
-                        unsigned term = 0;
-                        nc = fallback_children(A, S, F, Mt, l, Rr, i, d_of_ff(lenff), origin, nrm, &ccd, chd, &term);
-                        fp64_children = true;
-                        if (term) atomicAdd(&s_term, term);
+                } else if constexpr (FB) {
+                    nn = fallback_normal_ff(S, F, l, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
+                }
+                nrm = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
+                const rp_material &Mt = S.mats[F.material];
+                const double2 nin = B.n[t];
+                opl = d_of_ff(ff_add(ff_of_d(B.opl[t]), ff_mul(lenff, ff_of_d(nin.x))));
+                if (mat_specialised(Mt.type)) {
+                    RayF r;
+                    r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
+                    r.E = f3_of_d(B.ex[t], B.ey[t], B.ez[t]);
+                    r.e1 = cf_of_d(B.e1[t]);
+                    r.e2 = cf_of_d(B.e2[t]);
+                    r.n = nin;
+                    r.type = B.type[t];
+                    r.wl = B.wl[t];
+                    const ff3 Dff = mkff3(D[0], D[1], D[2]);
+                    const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
+                    nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
+                    if (A.e2_term > 0.0 && nc > 0) {
+                        // the |E|^2 rule, children kept in order (fixed indices: registers)
+                        const bool k0 = !(cabs2(ch[0].e1) + cabs2(ch[0].e2) < e2t);
+                        const bool k1 = nc > 1 && !(cabs2(ch[1].e1) + cabs2(ch[1].e2) < e2t);
+                        if (!k0 && k1) ch[0] = ch[1];
+                        const int w = (int)k0 + (int)k1;
+                        if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
+                        nc = w;
                     }
+                } else if constexpr (FB) {
+                    unsigned term = 0;
+                    nc = fallback_children(A, S, F, Mt, l, Rr, i, d_of_ff(lenff), origin, nrm, &ccd, chd, &term);
+                    fp64_children = true;
+                    if (term) atomicAdd(&s_term, term);
                 }
             }
-            // the chunk's children go to the group's slot range in parent
-            // order: the group's running count plus the exclusive warp scan
-            unsigned chunk_children;
-            const unsigned excl = warp_scan((unsigned)nc, &chunk_children);
-            if (nc > 0) {
-                const double phase = Rr.phase[i];
-                const unsigned wl = Rr.wl[i], ident = Rr.ident[i];
-                const unsigned endf = (unsigned)S.faces[face].idx;
-                const unsigned long long slot = (unsigned long long)q * RP_TILE_SLOTS + carry + excl;
-                if (FB && fp64_children) {
-                    for (int kk = 0; kk < nc; kk++)
-                        store_child(A.scratch, slot + kk, ccd, chd[kk], phase, wl, (unsigned)i, endf, ident);
-                } else {
-                    store_child_f(A.scratch, slot, origin, nrm, Eo, opl, ch[0], phase, wl, (unsigned)i, endf, ident);
-                    if (nc > 1)
-                        store_child_f(A.scratch, slot + 1, origin, nrm, Eo, opl, ch[1], phase, wl, (unsigned)i, endf,
-                                      ident);
-                }
-            }
-            carry += chunk_children;
         }
-        if (lane == 0) A.tile_counts[q] = carry;
+        // the chunk's children go to the group's slot range in parent
+        // order: the group's running count plus the exclusive warp scan
+        unsigned chunk_children;
+        const unsigned excl = warp_scan((unsigned)nc, &chunk_children);
+        if (nc > 0) {
+            const double phase = B.phase[t];
+            const unsigned wl = B.wl[t], ident = B.ident[t];
+            const unsigned endf = (unsigned)S.faces[face].idx;
+            const unsigned long long slot = (unsigned long long)G.q * RP_TILE_SLOTS + carry + excl;
+            if (FB && fp64_children) {
+                for (int kk = 0; kk < nc; kk++)
+                    store_child(A.scratch, slot + kk, ccd, chd[kk], phase, wl, (unsigned)i, endf, ident);
+            } else {
+                store_child_f(A.scratch, slot, origin, nrm, Eo, opl, ch[0], phase, wl, (unsigned)i, endf, ident);
+                if (nc > 1)
+                    store_child_f(A.scratch, slot + 1, origin, nrm, Eo, opl, ch[1], phase, wl, (unsigned)i, endf,
+                                  ident);
+            }
+        }
+        carry += chunk_children;
+        if (last_of_group) {
+            if (lane == 0) A.tile_counts[G.q] = carry;
+            carry = 0;
+        }
+        G = Gn;
+        k = kn;
     }
+    cp_async_wait_all();
     __syncthreads();
     if (threadIdx.x == 0 && s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
 }
@@ -1610,15 +1730,18 @@ static cudaError_t resident_grid(K kernel, size_t total, int *blocks) {
 }
 
 struct MixedLayout {
-    size_t mx_off, tb_off, in_off, pass_off, search_total, mat_total;
+    size_t mx_off, tb_off, in_off, pass_off, search_total, mat_buf_off, mat_total;
+    bool tb;  // the search kernel keeps box entries in shared memory
 };
 
 static MixedLayout mixed_layout(const GenArgs &a, size_t smem) {
     MixedLayout L;
     L.mx_off = (smem + 15) & ~(size_t)15;
     L.tb_off = L.mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
-    L.mat_total = L.tb_off;
-    const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
+    L.mat_buf_off = (L.tb_off + 15) & ~(size_t)15;
+    L.mat_total = L.mat_buf_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::MatIn);
+    L.tb = a.S.n_faces <= RP_MX_TB_FACES;
+    const int nmask = L.tb ? a.S.n_faces : 0;
     L.in_off = (L.tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
     L.pass_off = L.in_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
     L.search_total = L.pass_off + (a.in_map ? RP_SUB_PER_BLOCK * sizeof(mx::PassIn) : 0);
@@ -1626,8 +1749,13 @@ static MixedLayout mixed_layout(const GenArgs &a, size_t smem) {
 }
 
 static cudaError_t mixed_grids(const GenArgs &a, const MixedLayout &L, int *search_blocks, int *mat_blocks) {
-    cudaError_t e = a.mixed_fallback ? resident_grid(mixed_search_kernel<true>, L.search_total, search_blocks)
-                                     : resident_grid(mixed_search_kernel<false>, L.search_total, search_blocks);
+    cudaError_t e;
+    if (L.tb)
+        e = a.mixed_fallback ? resident_grid(mixed_search_kernel<true, true>, L.search_total, search_blocks)
+                             : resident_grid(mixed_search_kernel<false, true>, L.search_total, search_blocks);
+    else
+        e = a.mixed_fallback ? resident_grid(mixed_search_kernel<true, false>, L.search_total, search_blocks)
+                             : resident_grid(mixed_search_kernel<false, false>, L.search_total, search_blocks);
     if (e != cudaSuccess) return e;
     return a.mixed_fallback ? resident_grid(mixed_material_kernel<true>, L.mat_total, mat_blocks)
                             : resident_grid(mixed_material_kernel<false>, L.mat_total, mat_blocks);
@@ -1659,10 +1787,17 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
     const unsigned long long n_tiles = (a.n_in + RP_BLOCK - 1) / RP_BLOCK;
     const unsigned sgrid = (unsigned)(n_tiles < (unsigned long long)sb ? n_tiles : sb);
     const unsigned o1 = (unsigned)L.mx_off, o2 = (unsigned)L.tb_off, o3 = (unsigned)L.in_off, o4 = (unsigned)L.pass_off;
-    if (a.mixed_fallback)
-        mixed_search_kernel<true><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
-    else
-        mixed_search_kernel<false><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+    if (L.tb) {
+        if (a.mixed_fallback)
+            mixed_search_kernel<true, true><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+        else
+            mixed_search_kernel<false, true><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+    } else {
+        if (a.mixed_fallback)
+            mixed_search_kernel<true, false><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+        else
+            mixed_search_kernel<false, false><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+    }
     e = cudaGetLastError();
     if (e == cudaSuccess && mid) e = cudaEventRecord(mid, st);
     if (e != cudaSuccess || !a.emit) return e;
@@ -1670,10 +1805,11 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
     const unsigned long long n_groups = rp_n_units(a.n_in, RP_GROUP);
     const unsigned long long need = (n_groups + RP_SUB_PER_BLOCK - 1) / RP_SUB_PER_BLOCK;
     const unsigned mgrid = (unsigned)(need < (unsigned long long)mb ? need : mb);
+    const unsigned o5 = (unsigned)L.mat_buf_off;
     if (a.mixed_fallback)
-        mixed_material_kernel<true><<<mgrid, RP_BLOCK, L.mat_total, st>>>(a, o1);
+        mixed_material_kernel<true><<<mgrid, RP_BLOCK, L.mat_total, st>>>(a, o1, o5);
     else
-        mixed_material_kernel<false><<<mgrid, RP_BLOCK, L.mat_total, st>>>(a, o1);
+        mixed_material_kernel<false><<<mgrid, RP_BLOCK, L.mat_total, st>>>(a, o1, o5);
     return cudaGetLastError();
 }
 
