@@ -43,21 +43,36 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 METRIC = "ray-segments/s at 1M rays, mixed vs plain FP64 on 1 GB300; p50/p99 job latency"
 UNIT = "ray-segments/s"
-# algorithmic bytes per traced ray (SoA): origin, direction, E_vector (72),
-# n, E1, E2 (48), OPL, phase (16), wavelength_idx, type, ident (12), the
-# per-ray wavelength (8); written back: length, end_face_idx (12)
-BYTES_PER_SEGMENT = 72 + 48 + 16 + 12 + 8 + 12
-BYTES_PER_CHILD = 188
-# a ray of generation > 0 is read through the gather map (4) from its parents'
-# child slots and written to its final record by the kernel that traces it:
-# normal and parent index read (28), the record's other 176 bytes written
-BYTES_PER_GATHERED = 4 + 28 + 176
-# DRAM bytes per input ray of one generation launch (dram__bytes_read.sum +
-# dram__bytes_write.sum from ncu on generation 3 of the 262,144-ray config-2
-# trace, 1,046,875 gathered rays: the launch reads its rays through the gather
-# map and writes their records, 611.9 algorithmic bytes per ray with 1.25
-# children)
-NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 649.2, "generation_mixed_kernel": 616.2}
+# Algorithmic bytes of the generation kernels (structure of arrays; a
+# "gathered" ray is one of generation > 0, read through the gather map from
+# its parents' child slots and written to its final record by the kernel that
+# traces it):
+#   plain generation kernel: per traced ray 168 B (origin, direction,
+#     E_vector 72; n, E1, E2 48; OPL, phase 16; wavelength_idx, type, ident
+#     12; the ray's wavelength 8; length and end face written 12), per
+#     gathered ray 208 B more (map entry 4, normal and parent 28, the other
+#     176 B of its record written), per child 188 B written
+#   mixed search kernel: per traced ray 72 B (origin, direction 48 read;
+#     length, end face 12 and the hand-over's ray parameter and face 12
+#     written), per gathered ray 308 B more (map entry 4, the other 100 B of
+#     its fields and 28 B of pass-through read, the other 176 B of its record
+#     written)
+#   mixed material kernel: per ray 4 B (the hand-over's face), per hit 160 B
+#     (its 148 B of fields and 12 B of hand-over; the hits on absorbing faces
+#     are counted too, so this is an upper bound), per child 188 B written
+BYTES = {"plain": {"segment": 168, "gathered": 208, "child": 188},
+         "search": {"segment": 72, "gathered": 308},
+         "material": {"segment": 4, "hit": 160, "child": 188}}
+# FP64 floating-point operations per segment of the plain kernel (ncu: dadd +
+# dmul + 2 dfma thread instructions, 2,146.6 M over the 2,486,356 rays of
+# generation 5 of the 262,144-ray configuration-2 trace)
+PLAIN_FP64_FLOPS_PER_SEGMENT = 863.4
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per input ray of
+# a launch, from ncu on generation 5 of the 262,144-ray configuration-2 trace
+# (2,486,356 gathered rays): the plain kernel on an earlier capture of
+# generation 3 (1,046,875 rays)
+NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 649.2, "mixed_search_kernel": 364.6,
+                       "mixed_material_kernel": 435.9}
 
 
 def parse():
@@ -76,8 +91,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="rays in the CPU-baseline sample")
     ap.add_argument("--no-serving", action="store_true", help="skip the job-server stream (configuration 5)")
     ap.add_argument("--serving-jobs", type=int, default=10000, help="jobs in the served stream")
-    ap.add_argument("--serving-lanes", type=int, default=4,
-                    help="server lanes (p99 measured 44 / 60 / 108 ms at 4 / 8 / 16 lanes)")
+    ap.add_argument("--serving-lanes", type=int, default=64,
+                    help="jobs the server holds in flight (each step advances all of them by one generation)")
     ap.add_argument("--serving-baseline-jobs", type=int, default=500,
                     help="jobs of the same stream run one at a time through the plain FP64 path")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-lens leg (configuration 4)")
@@ -156,6 +171,58 @@ class ClockSampler:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def pipe_peaks(lib, device):
+    """FP64 / FP32 fused multiply-add and INT32 multiply-add peaks measured on
+    this device by the library (rp_measure_peaks)."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    if lib.rp_measure_peaks(device, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)) != 0:
+        return None
+    return {"fp64_tflops": a.value / 1e12, "fp32_tflops": b.value / 1e12, "int32_tops": c.value / 1e12,
+            "how": "rp_measure_peaks: 8 independent multiply-add chains per thread, 8 waves of resident blocks, "
+                   "best of 3 launches timed with CUDA events"}
+
+
+def kernel_rooflines(flags, st, n_first, hbm_peak, hbm_kind, peaks):
+    """Achieved HBM bandwidth (algorithmic bytes over the kernel's summed
+    launch time) and, for the plain kernel, FP64 throughput, each against its
+    measured peak, for the generation kernels of one path over the timed
+    steps (st: their rp_stats)."""
+    segs, children, hits = float(st.rays_in), float(st.rays_out), float(st.hits)
+    gathered = max(segs - n_first, 0.0)
+    out = []
+
+    def entry(kernel, ms, nbytes, launches, pipe=None):
+        s = ms / 1000.0
+        e = {"kernel": kernel, "ms": ms, "hbm": {"achieved_gbs": nbytes / s / 1e9, "peak_gbs": hbm_peak,
+                                                  "frac": nbytes / s / 1e9 / hbm_peak, "peak_kind": hbm_kind},
+             "algorithmic_bytes": nbytes,
+             "traffic_bytes_per_launch": NCU_TRAFFIC_PER_RAY[kernel] * segs / max(launches, 1)}
+        e["bound"] = "hbm"
+        if pipe:
+            e["pipe"] = pipe
+            if pipe["frac"] > e["hbm"]["frac"]:
+                e["bound"] = pipe["name"]
+        out.append(e)
+
+    gens = max(st.generations, 1)
+    if flags == 0:
+        B = BYTES["plain"]
+        nbytes = segs * B["segment"] + gathered * B["gathered"] + children * B["child"]
+        pipe = None
+        if peaks:
+            f = PLAIN_FP64_FLOPS_PER_SEGMENT * segs / (st.kernel_ms / 1000.0) / 1e12
+            pipe = {"name": "fp64", "achieved_tflops": f, "peak_tflops": peaks["fp64_tflops"],
+                    "frac": f / peaks["fp64_tflops"], "note": "flops per segment from ncu (dadd + dmul + 2 dfma)"}
+        entry("generation_plain_kernel", st.kernel_ms, nbytes, gens, pipe)
+    else:
+        B = BYTES["search"]
+        entry("mixed_search_kernel", st.search_ms, segs * B["segment"] + gathered * B["gathered"], gens)
+        B = BYTES["material"]
+        entry("mixed_material_kernel", st.kernel_ms - st.search_ms,
+              segs * B["segment"] + hits * B["hit"] + children * B["child"], gens)
+    return out
 
 
 def measured_peak_hbm():
@@ -307,12 +374,12 @@ def main():
         mixed_v, plain_v = (ovalue, value) if flags == 0 else (value, ovalue)
         other["speedup_mixed_vs_plain_fp64"] = mixed_v / plain_v
         other["precision_vs_plain_fp64"] = precision_sample(ctx, spec, rays, wl, P, per_ray)
-    # roofline of the generation kernel
-    gathered = max(segs - n * args.steps, 0)  # every generation but the first of each trace
-    alg_bytes = segs * BYTES_PER_SEGMENT + gathered * BYTES_PER_GATHERED + children * BYTES_PER_CHILD
-    kern_s = stats.kernel_ms / 1000.0
-    achieved = alg_bytes / kern_s / 1e9
+    # rooflines of the generation kernels
     peak, peak_kind = measured_peak_hbm()
+    peaks = pipe_peaks(lib, device)
+    krl = kernel_rooflines(flags, stats, n * args.steps, peak, peak_kind, peaks)
+    if other is not None:
+        krl += kernel_rooflines(1 - flags, ost, n * args.steps, peak, peak_kind, peaks)
 
     # ---- end to end through the host-buffer C ABI -----------------------------------------
     e2e_value, d2h, e2e_steps = None, 0, {"steps": 0}
@@ -328,7 +395,7 @@ def main():
         extra["extras"] = extras_leg(ctx)
     if rank == 0:
         emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
-             achieved, peak, peak_kind, flags, stats, clk, cpu, other, extra)
+             krl, peaks, flags, stats, clk, cpu, other, extra)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -411,9 +478,10 @@ def adjoint_leg(ctx, reps=5):
 def serving_leg(args):
     """Configuration 5: a Poisson stream of jobs (systems of 3-39 faces from the
     configuration-2 face mix, log-uniform 1e3-4e6 rays, wavelengths 0.4-1.0 um)
-    replayed in real time against the job server (mixed path, 8 lanes, 120 GB
-    budget); the first jobs of the same stream also run one at a time through
-    the plain FP64 path."""
+    replayed in real time against the job server (mixed path; up to
+    --serving-lanes jobs in flight, advanced together one generation per step;
+    120 GB budget); the first jobs of the same stream also run one at a time
+    through the plain FP64 path."""
     from raypier_optics_gb300 import serve
     from raypier_optics_gb300 import workloads as W
     C = W.CONFIG5
@@ -424,7 +492,8 @@ def serving_leg(args):
                                  e2_terminate=C["e2_terminate"])
     srv.close()
     out = serve.latency_summary(res)
-    out.update({"rate_jobs_per_s": C["rate"], "lanes": args.serving_lanes, "hbm_budget_bytes": C["hbm_budget"],
+    out.update({"rate_jobs_per_s": C["rate"], "jobs_in_flight_max": args.serving_lanes,
+                "hbm_budget_bytes": C["hbm_budget"],
                 "path": "mixed", "wall_s": wall, "p99_over_p50": out["p99_ms"] / out["p50_ms"]})
     nb = min(args.serving_baseline_jobs, len(jobs))
     if nb > 0:
@@ -566,8 +635,9 @@ def precision_sample(ctx, spec, rays, wl, P, per_ray, n_sample=16384):
 
 
 def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2e_value, d2h, e2e_steps,
-         achieved, peak, peak_kind, flags, stats, clk, cpu, other=None, extra=None):
-    kernel = "generation_plain_kernel" if flags == 0 else "generation_mixed_kernel"
+         krl, peaks, flags, stats, clk, cpu, other=None, extra=None):
+    head = krl[:1] if flags == 0 else krl[:2]  # the headline path's kernels
+    dom = max(head, key=lambda k: k["ms"])     # its dominant kernel
     if True:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -584,14 +654,15 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
                      "d2h_bytes_per_step": int(d2h / e2e_steps["steps"]), "steps": e2e_steps["steps"],
                      "api": "rp_trace_rays_host (pinned host records in and out)",
                      "step_ms": {k: e2e_steps[k] for k in ("min", "median", "max")}} if e2e_value else None),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak,
-                         "traffic": NCU_TRAFFIC_PER_RAY[kernel] * stats.rays_in / max(stats.generations, 1),
-                         "kernel": kernel,
-                         "note": f"algorithmic bytes {BYTES_PER_SEGMENT} B/segment + {BYTES_PER_GATHERED} B per "
-                                 f"gathered ray (generations > 0) + {BYTES_PER_CHILD} B/child "
-                                 f"over summed generation-kernel time; peak {peak_kind}; traffic = ncu DRAM "
-                                 f"bytes per input ray x rays per launch (average launch)"},
+            "roofline": {"bound": "hbm", "achieved": dom["hbm"]["achieved_gbs"], "peak": dom["hbm"]["peak_gbs"],
+                         "unit": "GB/s", "frac": dom["hbm"]["frac"], "traffic": dom["traffic_bytes_per_launch"],
+                         "kernel": dom["kernel"],
+                         "note": "the headline path's dominant kernel: algorithmic bytes over its summed launch "
+                                 f"time (CUDA events); peak {dom['hbm']['peak_kind']}; traffic = ncu DRAM bytes "
+                                 "per input ray x rays per launch (average launch); kernel_rooflines has every "
+                                 "generation kernel of both paths with the pipe that bounds it"},
+            "kernel_rooflines": krl,
+            "measured_peaks": peaks,
             "gpu_launches": int(stats.launches),
             "clocks": clk,
         }

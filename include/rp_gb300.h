@@ -539,15 +539,22 @@ int rp_lens_image(const rp_lens *lens, double *xy, uint8_t *valid, uint64_t n);
 
 /* ---- trace-job server ----------------------------------------------------- */
 /* No counterpart in the reference (its traces run one at a time in the caller's
- * thread).  A server owns `lanes` contexts on one device; submitted jobs wait
- * in one FIFO queue and start as soon as a lane is free and the HBM budget
- * admits their estimated footprint, so jobs overlap on the device.  A job is
+ * thread).  A server holds up to `lanes` jobs in flight (at most 64) on one
+ * device; submitted jobs wait in one FIFO queue and are admitted as soon as a
+ * slot is free and the HBM budget holds their estimated footprint.  A job is
  * a whole trace_rays (core/tracer.py:9-47) of rays generated on the device
- * from a source description; each generation runs as one CUDA graph.  The
- * result is the job's counters and the tallies of the rays that ended on its
- * detector face, reduced on the device in a fixed order (the same whether the
- * job runs alone or among others).  Submit and wait may be called from any
- * thread. */
+ * from a source description.  The server advances in steps: each step moves
+ * every admitted job forward by one generation, the RP_TRACE_MIXED jobs
+ * together in one launch of each mixed-path kernel (their rays numbered in
+ * 128-ray groups across the jobs), as one CUDA graph replayed every step, and
+ * the plain FP64 jobs through their own kernels in the same step; one
+ * read-back per step gives every job's next generation size.  Jobs that
+ * arrive while others trace join at the next step.  The result is the job's
+ * counters and the tallies of the rays that ended on its detector face,
+ * reduced on the device in a fixed order within the job (the same whether the
+ * job runs alone or among others).  RP_TRACE_MIXED jobs need scenes of the
+ * faces and materials the mixed kernels specialise (else RP_ERR_UNSUPPORTED
+ * in the result).  Submit and wait may be called from any thread. */
 #define RP_SOURCE_POINT_CONE      1  /* point at `origin`, directions uniform in a cone of `half_angle` about +z */
 #define RP_SOURCE_COLLIMATED_DISC 2  /* directions +z, origins uniform over a disc of `radius` about `origin` */
 typedef struct rp_source_desc {
@@ -595,7 +602,7 @@ int rp_server_submit(rp_server *server, const rp_job_desc *job, uint64_t *job_id
  * them) when face_counts is not NULL.  A job id can be waited for once. */
 int rp_server_wait(rp_server *server, uint64_t job_id, rp_job_result *result, uint32_t *face_counts,
                    int32_t n_faces);
-/* Finishes the queued jobs, then stops the lanes. */
+/* Finishes the queued jobs, then stops the step loop. */
 int rp_server_destroy(rp_server *server);
 
 /* Allocation-free rp_trace_segment.  No counterpart in the reference: this is

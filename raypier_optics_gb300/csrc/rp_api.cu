@@ -334,7 +334,15 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     }
     size_t o_zkoff = o_bnd + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
     size_t o_zkprog = o_zkoff + align256(sizeof(int) * zk_off.size());
-    size_t total = o_zkprog + align256(sizeof(short) * (zk_prog.size() + 1));
+    size_t o_fl = o_zkprog + align256(sizeof(short) * (zk_prog.size() + 1));
+    size_t total = o_fl + align256(sizeof(short) * (size_t)(d->n_faces + 1));
+    // owning list of each traced face (kernels that read the tables from global memory)
+    std::vector<short> face_list((size_t)d->n_faces + 1, (short)-1);
+    for (int l = 0; l < d->n_lists; l++)
+        for (int k = 0; k < d->lists[l].n_faces; k++) {
+            const int f = d->lists[l].first_face + k;
+            if (f >= 0 && f < d->n_faces) face_list[f] = (short)l;
+        }
     int rc = ctx_alloc(ctx, &s->dev_block, total, &s->dev_bytes);
     if (rc) {
         delete s;
@@ -362,6 +370,7 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     UP(o_bnd, bounds.data(), sizeof(float) * 8 * (size_t)d->n_faces);
     UP(o_zkoff, zk_off.data(), sizeof(int) * zk_off.size());
     UP(o_zkprog, zk_prog.data(), sizeof(short) * zk_prog.size());
+    UP(o_fl, face_list.data(), sizeof(short) * (size_t)d->n_faces);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host vectors are pageable and about to go out of scope
 #undef UP
     if (e == cudaSuccess) e = cudaMemsetAsync(b + o_cnt, 0, sizeof(unsigned) * (d->n_face_records + 1), st);
@@ -374,7 +383,7 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     S.aux = (const double *)(b + o_aux);
     S.ntab = (const double2 *)(b + o_ntab);
     S.bounds = (const float *)(b + o_bnd);
-    S.face_list = nullptr;
+    S.face_list = (const short *)(b + o_fl);
     S.zk_off = (const int *)(b + o_zkoff);
     S.zk_prog = (const short *)(b + o_zkprog);
     S.n_wl = n_wl;

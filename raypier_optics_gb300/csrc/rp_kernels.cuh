@@ -80,6 +80,55 @@ struct GenArgs {
     int *hit_face;
     unsigned *group_next;
 };
+// ---- batches of trace jobs (the job server, rp_serve.cu) ----
+// One generation of every job of a batch runs in one launch of each mixed
+// kernel: the jobs' 128-ray groups are numbered consecutively across the
+// batch (job j owns global units [unit_start[j], unit_start[j + 1])), warps
+// take global sub-tiles or groups from the batch's counters, and each item
+// runs with its job's generation arguments and tables, read from global
+// memory.  A job's rays stay in place in its own buffers (no gather map).
+#define RP_BATCH_MAX_JOBS 64
+struct BatchJob {
+    GenArgs a;            // the job's generation: in place (in = wb); its arena, hand-over and count views
+    const void *mx_lists; // its float / float-float list and face tables (mixed kernels)
+    const void *mx_faces;
+    const unsigned long long *own_count;  // plain-path job keeping children: the count of its own tile scan
+    int detector;         // Face.idx whose hits are tallied, -1 for none
+    int mixed;            // 1: traced by the batch kernels; 0: by its own plain-path launches
+    int slot;             // the job's server slot (tally accumulators, results)
+    int first;            // 1 on the job's first generation (its accumulators start from zero)
+};
+struct BatchDev {
+    int n_jobs;
+    unsigned total_units;
+    unsigned unit_start[RP_BATCH_MAX_JOBS + 1];
+    BatchJob jobs[RP_BATCH_MAX_JOBS];
+};
+// counters of a batch step, zeroed before it: [0] next sub-tile, [1] next group, [2] error bits
+#define RP_BATCH_WORDS 8
+// The batch's job owning global unit u (the last job whose first unit is <= u).
+__device__ __forceinline__ int batch_job_of(const BatchDev *B, unsigned u) {
+    int lo = 0, hi = B->n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (B->unit_start[mid] <= u)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+// mixed-path kernels over a batch (rp_mixed.cu); the jobs' scenes use only
+// faces and materials the mixed kernels specialise, and the tables of each job
+// are filled once by launch_batch_tables
+cudaError_t prepare_batch_mixed(size_t *search_smem, size_t *mat_smem, int *search_blocks, int *mat_blocks);
+cudaError_t launch_batch_mixed(const BatchDev *batch, unsigned *ctr, cudaStream_t st);
+size_t batch_tables_bytes(int n_lists, int n_faces);
+cudaError_t launch_batch_tables(const GenArgs &a, void *tables, cudaStream_t st);
+// the unit count scan with the unit count read from device memory
+cudaError_t launch_tile_scan_dev(const unsigned *counts, const unsigned *n_dev, unsigned long long *offsets,
+                                 unsigned long long *total, cudaStream_t st);
+
 // Bytes of per-ray hand-over storage (hit_t, hit_face) the mixed path needs
 // for n rays, each array on a 256-byte boundary.
 __host__ __device__ constexpr unsigned long long rp_hit_bytes(unsigned long long n) {

@@ -1202,6 +1202,130 @@ __device__ __forceinline__ bool makes_children(const DevScene &S, int f) {
 #define MX_SEARCH_MIN_BLOCKS 3
 #define MX_MAT_MIN_BLOCKS 3
 
+// The nearest hit of one ray (origin and direction od[0..5], its record src
+// of A.in for the FP64 faces): culled nearest-first FP32 candidates among the
+// specialised faces, the winner (and a close second) refined in float-float,
+// then the faces left to the FP64 path.  tb is the thread's box-entry table
+// (TB) in shared memory.
+template <bool FB, bool TB>
+__device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene &S, const mx::MxList *ml,
+                                               const mx::MxFace *mf, float *tb, float max_len, const double *od,
+                                               unsigned long long src) {
+    using namespace mx;
+    Best b;
+    b.len = ffm(max_len, 0.0f);
+    b.t = ffm(0.0f, 0.0f);
+    b.face = -1;
+    b.list = -1;
+    ff O[3], D[3];
+    O[0] = ff_of_d(od[0]);
+    O[1] = ff_of_d(od[1]);
+    O[2] = ff_of_d(od[2]);
+    D[0] = ff_of_d(od[3]);
+    D[1] = ff_of_d(od[4]);
+    D[2] = ff_of_d(od[5]);
+    const ff dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
+    int cur = -1;
+    LRay R;
+    unsigned long long pend = 0;  // culled faces left to the FP64 path
+    Cand c1, c2;                  // the two nearest FP32 candidates of the specialised faces
+    cand_clear(c1);
+    cand_clear(c2);
+    const float dl = dlen.hi;
+    if (A.one_list >= 0) {
+        // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
+        const int f = S.lists[A.one_list].first_face + A.one_face;
+        if (face_specialised(S.faces[f].type)) {
+            try_face32(S, ml, mf, f, A.one_list, cur, R, O, D, dl, max_len, A.err, c1, c2);
+            settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
+        } else if constexpr (FB) {
+            try_face_fp64(A, S, f, A.one_list, src, dlen, b);
+        }
+    } else {
+        // culled nearest-first search over the first 64 faces, then the rest in order
+        const float dfx = D[0].hi, dfy = D[1].hi, dfz = D[2].hi;
+        const float il = rsqrtf(dfx * dfx + dfy * dfy + dfz * dfz);
+        const float ix = 1.0f / ((fabsf(dfx * il) < 1e-30f) ? copysignf(1e-30f, dfx) : dfx * il);
+        const float iy = 1.0f / ((fabsf(dfy * il) < 1e-30f) ? copysignf(1e-30f, dfy) : dfy * il);
+        const float iz = 1.0f / ((fabsf(dfz * il) < 1e-30f) ? copysignf(1e-30f, dfz) : dfz * il);
+        const float ox = O[0].hi, oy = O[1].hi, oz = O[2].hi;
+        const int nf = S.n_faces;
+        const int nmask = nf < 64 ? nf : 64;
+        const float lim0 = max_len * 1.000001f + 1e-4f;
+        unsigned long long cand = 0;
+        for (int f = 0; f < nmask; f++) {
+            float te = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+            if constexpr (TB) tb[f * RP_BLOCK] = te;
+            if (te <= lim0) cand |= 1ull << f;
+        }
+        while (cand) {
+            float tsel = __int_as_float(0x7f800000);
+            int sel = -1;
+            for (unsigned long long m = cand; m; m &= m - 1) {
+                int f = __ffsll((long long)m) - 1;
+                float tf;
+                if constexpr (TB)
+                    tf = tb[f * RP_BLOCK];
+                else
+                    tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+                if (tf < tsel) {
+                    tsel = tf;
+                    sel = f;
+                }
+            }
+            // boxes entered beyond the nearest FP32 candidate (with a
+            // margin above the FP32 roots' error) cannot hold a nearer hit
+            if (sel < 0 || tsel > fmaf(c1.d, 1.000244140625f, 1e-3f)) break;
+            cand &= ~(1ull << sel);
+            int l = S.face_list[sel];
+            if (l < 0 || l >= S.n_lists) {
+                atomicOr(A.err, ERR_SHAPE_STACK);
+                break;
+            }
+            if (face_specialised(S.faces[sel].type))
+                try_face32(S, ml, mf, sel, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
+            else
+                pend |= 1ull << sel;
+        }
+        for (int f = nmask; f < nf; f++) {
+            if (!face_specialised(S.faces[f].type)) continue;
+            if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > fmaf(c1.d, 1.000244140625f, 1e-3f))
+                continue;
+            int l = S.face_list[f];
+            if (l < 0 || l >= S.n_lists) {
+                atomicOr(A.err, ERR_SHAPE_STACK);
+                break;
+            }
+            try_face32(S, ml, mf, f, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
+        }
+        settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
+        // the FP64 faces: the nearest hit does not depend on the order of
+        // the tests, and the box bound stays valid against the final length
+        for (int f = 0; FB && f < nf; f++) {
+            if (f < nmask) {
+                if (!((pend >> f) & 1ull)) continue;
+                float tf;
+                if constexpr (TB)
+                    tf = tb[f * RP_BLOCK];
+                else
+                    tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+                if (tf > b.len.hi * 1.000001f + 1e-4f) continue;
+            } else {
+                if (face_specialised(S.faces[f].type)) continue;
+                if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f)
+                    continue;
+            }
+            int l = S.face_list[f];
+            if (l < 0 || l >= S.n_lists) {
+                atomicOr(A.err, ERR_SHAPE_STACK);
+                break;
+            }
+            if constexpr (FB) try_face_fp64(A, S, f, l, src, dlen, b);
+        }
+    }
+    return b;
+}
+
 // ---- the search kernel ------------------------------------------------------------
 // One block stages the tables once; then each of its warps takes 32-ray
 // sub-tiles from a launch-wide counter until none are left, with no barrier
@@ -1277,117 +1401,8 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
         const unsigned long long src = active && gathered ? (unsigned long long)in.src[t] : i;  // the record in A.in
 
         if (active) {
-            Best b;
-            b.len = ffm(max_len, 0.0f);
-            b.t = ffm(0.0f, 0.0f);
-            b.face = -1;
-            b.list = -1;
-            ff O[3], D[3];
-            O[0] = ff_of_d(in.ox[t]);
-            O[1] = ff_of_d(in.oy[t]);
-            O[2] = ff_of_d(in.oz[t]);
-            D[0] = ff_of_d(in.dx[t]);
-            D[1] = ff_of_d(in.dy[t]);
-            D[2] = ff_of_d(in.dz[t]);
-            const ff dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
-            int cur = -1;
-            LRay R;
-            unsigned long long pend = 0;  // culled faces left to the FP64 path
-            Cand c1, c2;                  // the two nearest FP32 candidates of the specialised faces
-            cand_clear(c1);
-            cand_clear(c2);
-            const float dl = dlen.hi;
-            if (A.one_list >= 0) {
-                // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
-                const int f = S.lists[A.one_list].first_face + A.one_face;
-                if (face_specialised(S.faces[f].type)) {
-                    try_face32(S, ml, mf, f, A.one_list, cur, R, O, D, dl, max_len, A.err, c1, c2);
-                    settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
-                } else if constexpr (FB) {
-                    try_face_fp64(A, S, f, A.one_list, src, dlen, b);
-                }
-            } else {
-                // culled nearest-first search over the first 64 faces, then the rest in order
-                const float dfx = D[0].hi, dfy = D[1].hi, dfz = D[2].hi;
-                const float il = rsqrtf(dfx * dfx + dfy * dfy + dfz * dfz);
-                const float ix = 1.0f / ((fabsf(dfx * il) < 1e-30f) ? copysignf(1e-30f, dfx) : dfx * il);
-                const float iy = 1.0f / ((fabsf(dfy * il) < 1e-30f) ? copysignf(1e-30f, dfy) : dfy * il);
-                const float iz = 1.0f / ((fabsf(dfz * il) < 1e-30f) ? copysignf(1e-30f, dfz) : dfz * il);
-                const float ox = O[0].hi, oy = O[1].hi, oz = O[2].hi;
-                const int nf = S.n_faces;
-                const int nmask = nf < 64 ? nf : 64;
-                const float lim0 = max_len * 1.000001f + 1e-4f;
-                unsigned long long cand = 0;
-                for (int f = 0; f < nmask; f++) {
-                    float te = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                    if constexpr (TB) tb[f * RP_BLOCK] = te;
-                    if (te <= lim0) cand |= 1ull << f;
-                }
-                while (cand) {
-                    float tsel = __int_as_float(0x7f800000);
-                    int sel = -1;
-                    for (unsigned long long m = cand; m; m &= m - 1) {
-                        int f = __ffsll((long long)m) - 1;
-                        float tf;
-                        if constexpr (TB)
-                            tf = tb[f * RP_BLOCK];
-                        else
-                            tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                        if (tf < tsel) {
-                            tsel = tf;
-                            sel = f;
-                        }
-                    }
-                    // boxes entered beyond the nearest FP32 candidate (with a
-                    // margin above the FP32 roots' error) cannot hold a nearer hit
-                    if (sel < 0 || tsel > fmaf(c1.d, 1.000244140625f, 1e-3f)) break;
-                    cand &= ~(1ull << sel);
-                    int l = S.face_list[sel];
-                    if (l < 0 || l >= S.n_lists) {
-                        atomicOr(A.err, ERR_SHAPE_STACK);
-                        break;
-                    }
-                    if (face_specialised(S.faces[sel].type))
-                        try_face32(S, ml, mf, sel, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
-                    else
-                        pend |= 1ull << sel;
-                }
-                for (int f = nmask; f < nf; f++) {
-                    if (!face_specialised(S.faces[f].type)) continue;
-                    if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > fmaf(c1.d, 1.000244140625f, 1e-3f))
-                        continue;
-                    int l = S.face_list[f];
-                    if (l < 0 || l >= S.n_lists) {
-                        atomicOr(A.err, ERR_SHAPE_STACK);
-                        break;
-                    }
-                    try_face32(S, ml, mf, f, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
-                }
-                settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
-                // the FP64 faces: the nearest hit does not depend on the order of
-                // the tests, and the box bound stays valid against the final length
-                for (int f = 0; FB && f < nf; f++) {
-                    if (f < nmask) {
-                        if (!((pend >> f) & 1ull)) continue;
-                        float tf;
-                        if constexpr (TB)
-                            tf = tb[f * RP_BLOCK];
-                        else
-                            tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                        if (tf > b.len.hi * 1.000001f + 1e-4f) continue;
-                    } else {
-                        if (face_specialised(S.faces[f].type)) continue;
-                        if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f)
-                            continue;
-                    }
-                    int l = S.face_list[f];
-                    if (l < 0 || l >= S.n_lists) {
-                        atomicOr(A.err, ERR_SHAPE_STACK);
-                        break;
-                    }
-                    if constexpr (FB) try_face_fp64(A, S, f, l, src, dlen, b);
-                }
-            }
+            const double od[6] = {in.ox[t], in.oy[t], in.oz[t], in.dx[t], in.dy[t], in.dz[t]};
+            const Best b = nearest_mx<FB, TB>(A, S, ml, mf, tb, max_len, od, src);
             const double len64 = d_of_ff(b.len);
             const unsigned endf = b.face >= 0 ? (unsigned)S.faces[b.face].idx : 0xFFFFFFFFu;
             if (gathered) {
@@ -1432,37 +1447,68 @@ struct MatIn {
 // A group's rays that go to the material kernel: per 32-ray quarter the
 // ballot of hits whose material can produce children, and their prefix counts.
 struct GroupMask {
-    unsigned q;           // the group; n_groups when none is left
+    unsigned q;           // the group (within its job); n_groups when none is left
     unsigned m[RP_GROUP / 32];
     unsigned p1, p2, p3, total;
+    int job;              // its job in a batch (0 otherwise)
 };
+
+// The masks of group q of the generation A (the rays whose hit material can
+// produce children).
+__device__ __forceinline__ void group_masks(const GenArgs &A, const DevScene &S, unsigned q, unsigned lane,
+                                            GroupMask &G) {
+    const unsigned long long g0 = (unsigned long long)q * RP_GROUP;
+#pragma unroll
+    for (int c = 0; c < RP_GROUP / 32; c++) {
+        const unsigned long long i = g0 + 32 * c + lane;
+        bool m = false;
+        if (i < A.n_in && A.emit) {
+            const int f = A.hit_face[i];
+            m = f >= 0 && f < S.n_faces && makes_children(S, f);
+        }
+        G.m[c] = __ballot_sync(0xffffffffu, m);
+    }
+    G.p1 = __popc(G.m[0]);
+    G.p2 = G.p1 + __popc(G.m[1]);
+    G.p3 = G.p2 + __popc(G.m[2]);
+    G.total = G.p3 + __popc(G.m[3]);
+}
 
 // Claims groups until one has material rays (a group without any gets its
 // zero child count at once); G.q = n_groups when none is left.
 __device__ __forceinline__ void claim_group(const GenArgs &A, const DevScene &S, unsigned long long n_groups,
                                             unsigned lane, GroupMask &G) {
+    G.job = 0;
     for (;;) {
         const unsigned q = claim_sub_tile(A.group_next, lane);
         G.q = q;
         G.total = 0;
         if (q >= n_groups) return;
-        const unsigned long long g0 = (unsigned long long)q * RP_GROUP;
-#pragma unroll
-        for (int c = 0; c < RP_GROUP / 32; c++) {
-            const unsigned long long i = g0 + 32 * c + lane;
-            bool m = false;
-            if (i < A.n_in) {
-                const int f = A.hit_face[i];
-                m = f >= 0 && f < S.n_faces && makes_children(S, f);
-            }
-            G.m[c] = __ballot_sync(0xffffffffu, m);
-        }
-        G.p1 = __popc(G.m[0]);
-        G.p2 = G.p1 + __popc(G.m[1]);
-        G.p3 = G.p2 + __popc(G.m[2]);
-        G.total = G.p3 + __popc(G.m[3]);
+        group_masks(A, S, q, lane, G);
         if (G.total > 0) return;
         if (lane == 0) A.tile_counts[q] = 0u;
+    }
+}
+
+// The same over a batch: global groups taken from the batch's counter, each
+// returned as its job and its group within the job; G.job = -1 when none is
+// left.
+__device__ __forceinline__ void claim_group_batch(const BatchDev *Bt, unsigned *ctr, unsigned lane, GroupMask &G) {
+    for (;;) {
+        const unsigned u = claim_sub_tile(&ctr[1], lane);
+        G.total = 0;
+        if (u >= Bt->total_units) {
+            G.job = -1;
+            G.q = 0;
+            return;
+        }
+        const int j = batch_job_of(Bt, u);
+        const GenArgs &A = Bt->jobs[j].a;
+        G.job = j;
+        G.q = u - Bt->unit_start[j];
+        group_masks(A, A.S, G.q, lane, G);
+        if (G.total > 0) return;
+        if (lane == 0) A.tile_counts[G.q] = 0u;
     }
 }
 
@@ -1513,6 +1559,101 @@ __device__ __forceinline__ void prefetch_mat(MatIn *B, const GenArgs &A, const R
     cp_async_commit();
 }
 }  // namespace mx
+
+// The material evaluation of one hit ray of a chunk (lane t of buffer B, ray
+// i of the generation's records Rr): hit point, normal and optical path
+// rebuilt from the record and the hand-over's ray parameter, then the
+// material's children (FP32 / float-float, or the FP64 path's for materials
+// not specialised here) with the |E|^2 rule applied.
+template <bool FB>
+__device__ __forceinline__ void material_mx(const GenArgs &A, const DevScene &S, const mx::MxList *ml,
+                                            const mx::MxFace *mf, const RaySoA &Rr, const mx::MatIn &B, unsigned t,
+                                            unsigned long long i, float e2t, unsigned *s_term, int &nc,
+                                            mx::ChildF *ch, mx::f3 &nrm, mx::f3 &Eo, double *origin, double &opl,
+                                            bool &fp64_children, Child *chd, ChildCommon &ccd, int &face) {
+    using namespace mx;
+    face = B.face[t];
+    const ff tt = ffm(B.t[t].x, B.t[t].y);
+    const rp_face &F = S.faces[face];
+    const int l = S.face_list[face];
+    if (l < 0 || l >= S.n_lists) {
+        atomicOr(A.err, ERR_SHAPE_STACK);
+    } else {
+        const MxFace &M = mf[face];
+        const MxList &L = ml[l];
+        ff O[3], D[3];
+        O[0] = ff_of_d(B.ox[t]);
+        O[1] = ff_of_d(B.oy[t]);
+        O[2] = ff_of_d(B.oz[t]);
+        D[0] = ff_of_d(B.dx[t]);
+        D[1] = ff_of_d(B.dy[t]);
+        D[2] = ff_of_d(B.dz[t]);
+        const ff dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
+        const ff lenff = ff_mul(tt, dlen);
+        ff P[3];
+        P[0] = ff_add(O[0], ff_mul(tt, D[0]));
+        P[1] = ff_add(O[1], ff_mul(tt, D[1]));
+        P[2] = ff_add(O[2], ff_mul(tt, D[2]));
+        origin[0] = d_of_ff(P[0]);
+        origin[1] = d_of_ff(P[1]);
+        origin[2] = d_of_ff(P[2]);
+        // the hit in the face list's frame, relative to the face vertex
+        ff lp[3];
+        if (L.ident) {
+            lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
+            lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
+            lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
+        } else {
+            ff_rotate(L, P, lp, true);
+        }
+        ff3 nn;
+        if (face_normal_ff(F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
+            if (F.invert_normal) nn = ff3_neg(nn);
+            if (!L.ident) {
+                ff v[3] = {nn.x, nn.y, nn.z}, w[3];
+#pragma unroll
+                for (int rr = 0; rr < 3; rr++)
+                    w[rr] = ff_add(ff_add(ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr), v[0]),
+                                          ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 1), v[1])),
+                                   ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 2), v[2]));
+                nn = mkff3(w[0], w[1], w[2]);
+            }
+        } else if constexpr (FB) {
+            nn = fallback_normal_ff(S, F, l, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
+        }
+        nrm = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
+        const rp_material &Mt = S.mats[F.material];
+        const double2 nin = B.n[t];
+        opl = d_of_ff(ff_add(ff_of_d(B.opl[t]), ff_mul(lenff, ff_of_d(nin.x))));
+        if (mat_specialised(Mt.type)) {
+            RayF r;
+            r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
+            r.E = f3_of_d(B.ex[t], B.ey[t], B.ez[t]);
+            r.e1 = cf_of_d(B.e1[t]);
+            r.e2 = cf_of_d(B.e2[t]);
+            r.n = nin;
+            r.type = B.type[t];
+            r.wl = B.wl[t];
+            const ff3 Dff = mkff3(D[0], D[1], D[2]);
+            const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
+            nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
+            if (A.e2_term > 0.0 && nc > 0) {
+                // the |E|^2 rule, children kept in order (fixed indices: registers)
+                const bool k0 = !(cabs2(ch[0].e1) + cabs2(ch[0].e2) < e2t);
+                const bool k1 = nc > 1 && !(cabs2(ch[1].e1) + cabs2(ch[1].e2) < e2t);
+                if (!k0 && k1) ch[0] = ch[1];
+                const int w = (int)k0 + (int)k1;
+                if (w < nc) atomicAdd(s_term, (unsigned)(nc - w));
+                nc = w;
+            }
+        } else if constexpr (FB) {
+            unsigned term = 0;
+            nc = fallback_children(A, S, F, Mt, l, Rr, i, d_of_ff(lenff), origin, nrm, &ccd, chd, &term);
+            fp64_children = true;
+            if (term) atomicAdd(s_term, term);
+        }
+    }
+}
 
 // Each warp takes groups of RP_GROUP rays from a launch-wide counter.  The
 // rays of a group whose hit material can produce children are compacted, in
@@ -1580,89 +1721,9 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS) mixed_material_ke
         Child chd[2];
         ChildCommon ccd;
         int face = -1;
-        if (act) {
-            face = B.face[t];
-            const ff tt = ffm(B.t[t].x, B.t[t].y);
-            const rp_face &F = S.faces[face];
-            const int l = S.face_list[face];
-            if (l < 0 || l >= S.n_lists) {
-                atomicOr(A.err, ERR_SHAPE_STACK);
-            } else {
-                const MxFace &M = mf[face];
-                const MxList &L = ml[l];
-                ff O[3], D[3];
-                O[0] = ff_of_d(B.ox[t]);
-                O[1] = ff_of_d(B.oy[t]);
-                O[2] = ff_of_d(B.oz[t]);
-                D[0] = ff_of_d(B.dx[t]);
-                D[1] = ff_of_d(B.dy[t]);
-                D[2] = ff_of_d(B.dz[t]);
-                const ff dlen = ff_sqrt(ff_add(ff_add(ff_mul(D[0], D[0]), ff_mul(D[1], D[1])), ff_mul(D[2], D[2])));
-                const ff lenff = ff_mul(tt, dlen);
-                ff P[3];
-                P[0] = ff_add(O[0], ff_mul(tt, D[0]));
-                P[1] = ff_add(O[1], ff_mul(tt, D[1]));
-                P[2] = ff_add(O[2], ff_mul(tt, D[2]));
-                origin[0] = d_of_ff(P[0]);
-                origin[1] = d_of_ff(P[1]);
-                origin[2] = d_of_ff(P[2]);
-                // the hit in the face list's frame, relative to the face vertex
-                ff lp[3];
-                if (L.ident) {
-                    lp[0] = ff_add(P[0], ff_of(L.ti_hi, L.ti_lo, 0));
-                    lp[1] = ff_add(P[1], ff_of(L.ti_hi, L.ti_lo, 1));
-                    lp[2] = ff_add(P[2], ff_of(L.ti_hi, L.ti_lo, 2));
-                } else {
-                    ff_rotate(L, P, lp, true);
-                }
-                ff3 nn;
-                if (face_normal_ff(F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
-                    if (F.invert_normal) nn = ff3_neg(nn);
-                    if (!L.ident) {
-                        ff v[3] = {nn.x, nn.y, nn.z}, w[3];
-#pragma unroll
-                        for (int rr = 0; rr < 3; rr++)
-                            w[rr] = ff_add(ff_add(ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr), v[0]),
-                                                  ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 1), v[1])),
-                                           ff_mul(ff_of(L.r_hi, L.r_lo, 3 * rr + 2), v[2]));
-                        nn = mkff3(w[0], w[1], w[2]);
-                    }
-                } else if constexpr (FB) {
-                    nn = fallback_normal_ff(S, F, l, mkv(d_of_ff(lp[0]), d_of_ff(lp[1]), d_of_ff(lp[2])), A.err);
-                }
-                nrm = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
-                const rp_material &Mt = S.mats[F.material];
-                const double2 nin = B.n[t];
-                opl = d_of_ff(ff_add(ff_of_d(B.opl[t]), ff_mul(lenff, ff_of_d(nin.x))));
-                if (mat_specialised(Mt.type)) {
-                    RayF r;
-                    r.d = mk3(D[0].hi, D[1].hi, D[2].hi);
-                    r.E = f3_of_d(B.ex[t], B.ey[t], B.ez[t]);
-                    r.e1 = cf_of_d(B.e1[t]);
-                    r.e2 = cf_of_d(B.e2[t]);
-                    r.n = nin;
-                    r.type = B.type[t];
-                    r.wl = B.wl[t];
-                    const ff3 Dff = mkff3(D[0], D[1], D[2]);
-                    const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
-                    nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
-                    if (A.e2_term > 0.0 && nc > 0) {
-                        // the |E|^2 rule, children kept in order (fixed indices: registers)
-                        const bool k0 = !(cabs2(ch[0].e1) + cabs2(ch[0].e2) < e2t);
-                        const bool k1 = nc > 1 && !(cabs2(ch[1].e1) + cabs2(ch[1].e2) < e2t);
-                        if (!k0 && k1) ch[0] = ch[1];
-                        const int w = (int)k0 + (int)k1;
-                        if (w < nc) atomicAdd(&s_term, (unsigned)(nc - w));
-                        nc = w;
-                    }
-                } else if constexpr (FB) {
-                    unsigned term = 0;
-                    nc = fallback_children(A, S, F, Mt, l, Rr, i, d_of_ff(lenff), origin, nrm, &ccd, chd, &term);
-                    fp64_children = true;
-                    if (term) atomicAdd(&s_term, term);
-                }
-            }
-        }
+        if (act)
+            material_mx<FB>(A, S, ml, mf, Rr, B, t, i, e2t, &s_term, nc, ch, nrm, Eo, origin, opl, fp64_children, chd,
+                            ccd, face);
         // the chunk's children go to the group's slot range in parent
         // order: the group's running count plus the exclusive warp scan
         unsigned chunk_children;
@@ -1693,6 +1754,165 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS) mixed_material_ke
     cp_async_wait_all();
     __syncthreads();
     if (threadIdx.x == 0 && s_term) atomicAdd(&A.stats[1], (unsigned long long)s_term);
+}
+
+// ---- batches of jobs ---------------------------------------------------------------
+// The search kernel over a batch: warps take global sub-tiles from the
+// batch's counter; each sub-tile belongs to one job (a job's generation
+// starts on a group boundary of the global numbering) and runs with that
+// job's arguments and tables from global memory.  The next sub-tile's origins
+// and directions are prefetched as in the single-job kernel; rays are traced
+// in place (length and end face written to the job's records) and the hit
+// goes to the job's hand-over.  Face hits are added to the job's counters by
+// one atomic per distinct face of a warp.
+__global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
+    mixed_search_batch_kernel(const BatchDev *Bt, unsigned *ctr, unsigned in_off) {
+    using namespace mx;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const unsigned lane = threadIdx.x & 31;
+    TileIn *bufs = reinterpret_cast<TileIn *>(smem + in_off) + 2 * (threadIdx.x >> 5);
+    const unsigned subs = RP_GROUP / RP_SUB;
+    const unsigned long long n_sub = (unsigned long long)Bt->total_units * subs;
+    // global sub-tile -> job and this lane's ray (~0 past the job's rays)
+    auto locate = [&](unsigned tile, int &j, unsigned long long &i) {
+        j = batch_job_of(Bt, tile / subs);
+        const unsigned long long lt = tile - (unsigned long long)Bt->unit_start[j] * subs;
+        i = lt * RP_SUB + lane;
+        if (i >= Bt->jobs[j].a.n_in || !Bt->jobs[j].mixed) i = ~0ull;
+    };
+    unsigned tile = claim_sub_tile(&ctr[0], lane);
+    int j = 0;
+    unsigned long long i = ~0ull;
+    if (tile < n_sub) {
+        locate(tile, j, i);
+        const GenArgs &A = Bt->jobs[j].a;
+        prefetch_ray(&bufs[0], A.in, i, A.n_in, i, false);
+    }
+    for (unsigned k = 0; tile < n_sub; k++) {
+        const unsigned next = claim_sub_tile(&ctr[0], lane);
+        int jn = 0;
+        unsigned long long in_ = ~0ull;
+        if (next < n_sub) {
+            locate(next, jn, in_);
+            const GenArgs &An = Bt->jobs[jn].a;
+            prefetch_ray(&bufs[(k + 1) & 1], An.in, in_, An.n_in, in_, false);
+        } else {
+            cp_async_commit();
+        }
+        cp_async_wait_prev();  // this lane's copies for `tile` have landed
+        const BatchJob &J = Bt->jobs[j];
+        const GenArgs &A = J.a;
+        int face = -1;
+        if (i != ~0ull) {
+            const TileIn &in = bufs[k & 1];
+            const double od[6] = {in.ox[lane], in.oy[lane], in.oz[lane], in.dx[lane], in.dy[lane], in.dz[lane]};
+            const Best b = nearest_mx<false, false>(A, A.S, static_cast<const MxList *>(J.mx_lists),
+                                                    static_cast<const MxFace *>(J.mx_faces), nullptr,
+                                                    f_of_d(A.max_len), od, i);
+            A.in.len[i] = d_of_ff(b.len);
+            A.in.endf[i] = b.face >= 0 ? (unsigned)A.S.faces[b.face].idx : 0xFFFFFFFFu;
+            if (A.emit) {
+                A.hit_t[i] = make_float2(b.t.hi, b.t.lo);
+                A.hit_face[i] = b.face;
+            }
+            face = b.face;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, face);
+        if (face >= 0 && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&A.face_counts[face], (unsigned)__popc(peers));
+        tile = next;
+        j = jn;
+        i = in_;
+    }
+}
+
+// The material kernel over a batch: global groups, each evaluated with its
+// job's arguments and tables; the chunks' inputs are prefetched as in the
+// single-job kernel, and children go to the job's own slot arena at its
+// group's range.
+__global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS)
+    mixed_material_batch_kernel(const BatchDev *Bt, unsigned *ctr, unsigned buf_off) {
+    using namespace mx;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ unsigned s_term;  // not reported per job
+    const unsigned lane = threadIdx.x & 31;
+    MatIn *bufs = reinterpret_cast<MatIn *>(smem + buf_off) + 2 * (threadIdx.x >> 5);
+    if (threadIdx.x == 0) s_term = 0;
+    __syncthreads();
+    GroupMask G;
+    claim_group_batch(Bt, ctr, lane, G);
+    if (G.job >= 0) {
+        const GenArgs &A = Bt->jobs[G.job].a;
+        prefetch_mat(&bufs[0], A, A.in, chunk_ray(G, 0, lane), lane);
+    }
+    unsigned k = 0, carry = 0;
+    for (unsigned step = 0; G.job >= 0; step++) {
+        GroupMask Gn = G;
+        unsigned kn = k + 1;
+        const bool last_of_group = kn * 32 >= G.total;
+        if (last_of_group) {
+            claim_group_batch(Bt, ctr, lane, Gn);
+            kn = 0;
+        }
+        if (Gn.job >= 0) {
+            const GenArgs &An = Bt->jobs[Gn.job].a;
+            prefetch_mat(&bufs[(step + 1) & 1], An, An.in, chunk_ray(Gn, kn, lane), lane);
+        } else {
+            cp_async_commit();
+        }
+        cp_async_wait_prev();
+        const BatchJob &J = Bt->jobs[G.job];
+        const GenArgs &A = J.a;
+        const MatIn &B = bufs[step & 1];
+        const unsigned t = lane;
+        const unsigned ridx = B.idx[t];
+        const bool act = ridx != 0xffffffffu;
+        const unsigned long long i = act ? (unsigned long long)ridx : 0ull;
+        int nc = 0;
+        ChildF ch[2];
+        f3 nrm = mk3(0.0f, 0.0f, 0.0f), Eo = mk3(0.0f, 0.0f, 0.0f);
+        double origin[3] = {0.0, 0.0, 0.0}, opl = 0.0;
+        bool fp64_children = false;
+        Child chd[2];
+        ChildCommon ccd;
+        int face = -1;
+        if (act)
+            material_mx<false>(A, A.S, static_cast<const MxList *>(J.mx_lists), static_cast<const MxFace *>(J.mx_faces),
+                               A.in, B, t, i, f_of_d(A.e2_term), &s_term, nc, ch, nrm, Eo, origin, opl, fp64_children,
+                               chd, ccd, face);
+        unsigned chunk_children;
+        const unsigned excl = warp_scan((unsigned)nc, &chunk_children);
+        if (nc > 0) {
+            const double phase = B.phase[t];
+            const unsigned wl = B.wl[t], ident = B.ident[t];
+            const unsigned endf = (unsigned)A.S.faces[face].idx;
+            const unsigned long long slot = (unsigned long long)G.q * RP_TILE_SLOTS + carry + excl;
+            store_child_f(A.scratch, slot, origin, nrm, Eo, opl, ch[0], phase, wl, (unsigned)i, endf, ident);
+            if (nc > 1)
+                store_child_f(A.scratch, slot + 1, origin, nrm, Eo, opl, ch[1], phase, wl, (unsigned)i, endf, ident);
+        }
+        carry += chunk_children;
+        if (last_of_group) {
+            if (lane == 0) A.tile_counts[G.q] = carry;
+            carry = 0;
+        }
+        G = Gn;
+        k = kn;
+    }
+    cp_async_wait_all();
+}
+
+// One job's float / float-float tables for the batch kernels (the single-job
+// kernels build them in shared memory per block).
+__global__ void batch_tables_kernel(GenArgs a, mx::MxList *ml, mx::MxFace *mf) {
+    mx::stage_mixed(a, ml, mf, mx::f_of_d(a.max_len));
+}
+
+size_t batch_tables_bytes(int n_lists, int n_faces) { return mx::mx_tables_bytes(n_lists, n_faces); }
+
+cudaError_t launch_batch_tables(const GenArgs &a, void *tables, cudaStream_t st) {
+    mx::MxList *ml = static_cast<mx::MxList *>(tables);
+    batch_tables_kernel<<<1, RP_BLOCK, 0, st>>>(a, ml, reinterpret_cast<mx::MxFace *>(ml + a.S.n_lists));
+    return cudaGetLastError();
 }
 
 // ---- launches ---------------------------------------------------------------------
@@ -1810,6 +2030,31 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
         mixed_material_kernel<true><<<mgrid, RP_BLOCK, L.mat_total, st>>>(a, o1, o5);
     else
         mixed_material_kernel<false><<<mgrid, RP_BLOCK, L.mat_total, st>>>(a, o1, o5);
+    return cudaGetLastError();
+}
+
+
+// Shared memory and resident grids of the batch kernels (their tables come
+// from global memory: only the warps' input buffers are in shared memory).
+cudaError_t prepare_batch_mixed(size_t *search_smem, size_t *mat_smem, int *search_blocks, int *mat_blocks) {
+    *search_smem = 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
+    *mat_smem = 2 * RP_SUB_PER_BLOCK * sizeof(mx::MatIn);
+    cudaError_t e = resident_grid(mixed_search_batch_kernel, *search_smem, search_blocks);
+    if (e != cudaSuccess) return e;
+    return resident_grid(mixed_material_batch_kernel, *mat_smem, mat_blocks);
+}
+
+// The two kernels of one batch step, on persistent grids (the same launch
+// for every step: the batch's size is read from device memory).
+cudaError_t launch_batch_mixed(const BatchDev *batch, unsigned *ctr, cudaStream_t st) {
+    size_t ss = 0, ms = 0;
+    int sb = 0, mb = 0;
+    cudaError_t e = prepare_batch_mixed(&ss, &ms, &sb, &mb);
+    if (e != cudaSuccess) return e;
+    mixed_search_batch_kernel<<<sb, RP_BLOCK, ss, st>>>(batch, ctr, 0u);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    mixed_material_batch_kernel<<<mb, RP_BLOCK, ms, st>>>(batch, ctr, 0u);
     return cudaGetLastError();
 }
 

@@ -1,19 +1,22 @@
-// rp_serve.cu -- the trace-job server: continuous batching of whole traces.
+// rp_serve.cu -- the trace-job server: continuous batching of generations.
 //
 // Jobs (a scene, a ray source, trace parameters) are submitted from any host
-// thread.  A fixed set of lanes, each a host thread with its own context
-// (CUDA stream and caching allocator), takes jobs from one FIFO queue as soon
-// as the lane is free and the HBM budget admits the job's estimated footprint;
-// jobs on different lanes run on the device at the same time, so a job that
-// arrives while others are tracing starts as soon as a lane and memory free
-// up.  A lane runs its job generation by generation like rp_trace_rays
-// (core/tracer.py:40-45): the source rays are generated on the device, and
-// each generation is one CUDA graph (generation kernel, tile scan, child
-// placement, detector tally, read-back of the counters) whose launch
-// parameters are updated in the instantiated graph for the next generation.
-// State stays on the device: a job returns its counters and the tallies of
-// the rays that ended on its detector face, reduced on the device in a fixed
-// order, so a job's result does not depend on what else is running.
+// thread and wait in one FIFO queue.  One step loop drives the device: each
+// step first admits waiting jobs while a slot is free and the HBM budget
+// holds their estimated footprint (their scenes and tables are uploaded and
+// their source rays generated on the device), then advances EVERY admitted
+// job by one generation (core/tracer.py:40-45, per job) in one batch: the
+// jobs' rays are numbered in 128-ray groups across the batch, and one launch
+// of the mixed path's search kernel and one of its material kernel drain the
+// batch's (job, group) work items from device counters, so rays of all jobs
+// share each launch.  One scan of the per-group child counts, one placement
+// and one detector tally serve the whole batch; the step is one CUDA graph,
+// captured once and replayed with its parameters in device memory (the
+// batch table is copied in by the graph itself), followed by one read-back
+// of every job's child count and tallies.  A job's rays stay in its own
+// buffers and are reduced in a fixed order within the job, so its result
+// does not depend on what else is in the batch.  Jobs on the plain FP64 path
+// run their own generation kernels inside the same step.
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -25,6 +28,7 @@
 #include <thread>
 
 #include "rp_internal.h"
+#include "rp_nearest.cuh"
 
 namespace rp {
 
@@ -107,47 +111,115 @@ __global__ void source_kernel(SourceArgs A) {
     o.type[i] = 0;
 }
 
-#define RP_TALLY_BLOCK 256
+#define RP_SERVE_WARPS_PER_BLOCK 8
 #define RP_TALLY_N 6  // hits, power, sum x, sum y, sum x^2, sum y^2
 
-// Per block: the tallies of the generation's rays that ended on the detector
-// face (hit point origin + direction * length; power (|E1|^2 + |E2|^2) Re n,
-// ctracer.pyx:1971-1978).
-__global__ void __launch_bounds__(RP_TALLY_BLOCK) tally_kernel(RaySoA in, unsigned long long n, unsigned detector,
-                                                                double *partials) {
-    __shared__ double s[RP_TALLY_N][RP_TALLY_BLOCK / 32];
-    const unsigned long long i = (unsigned long long)blockIdx.x * RP_TALLY_BLOCK + threadIdx.x;
-    double v[RP_TALLY_N] = {0, 0, 0, 0, 0, 0};
-    if (i < n && in.endf[i] == detector) {
-        const double L = in.len[i];
-        const double x = in.ox[i] + in.dx[i] * L, y = in.oy[i] + in.dy[i] * L;
-        const double2 a = in.e1[i], b = in.e2[i];
-        v[0] = 1.0;
-        v[1] = (a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y) * in.n[i].x;
-        v[2] = x;
-        v[3] = y;
-        v[4] = x * x;
-        v[5] = y * y;
-    }
-    for (int k = 0; k < RP_TALLY_N; k++) {
-        double t = v[k];
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        if ((threadIdx.x & 31) == 0) s[k][threadIdx.x >> 5] = t;
-    }
-    __syncthreads();
-    if (threadIdx.x < RP_TALLY_N) {
-        double t = 0.0;
-        for (int w = 0; w < RP_TALLY_BLOCK / 32; w++) t += s[threadIdx.x][w];
-        partials[(size_t)blockIdx.x * RP_TALLY_N + threadIdx.x] = t;
+// Per batch step, written by batch_finish_kernel into mapped host memory.
+struct StepOut {
+    unsigned long long count[RP_BATCH_MAX_JOBS];  // children of each slot's generation
+    double acc[RP_BATCH_MAX_JOBS][RP_TALLY_N];     // each slot's detector tallies so far
+    unsigned err;
+    unsigned pad;
+};
+
+// One warp per global group: the mixed jobs' children move from their slot
+// range to their final place in the job's next generation, at the group's
+// offset within its job.
+__global__ void batch_place_kernel(const BatchDev *B, const unsigned long long *offsets, unsigned *err) {
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    for (unsigned long long u = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+         u < B->total_units; u += warps) {
+        const int j = batch_job_of(B, (unsigned)u);
+        const BatchJob &J = B->jobs[j];
+        if (!J.mixed || !J.a.emit) continue;
+        const unsigned lu = (unsigned)(u - B->unit_start[j]);
+        const unsigned count = J.a.tile_counts[lu];
+        const unsigned long long base = offsets[u] - offsets[B->unit_start[j]];
+        if (count > RP_TILE_SLOTS || base + count > J.a.out_cap) {
+            if (lane == 0) atomicOr(err, ERR_OVERFLOW);
+            continue;
+        }
+        const unsigned long long src = (unsigned long long)lu * RP_TILE_SLOTS;
+        for (unsigned k = lane; k < count; k += 32) copy_ray(J.a.scratch, src + k, J.a.out, base + k);
     }
 }
 
-// Adds the block partials, in block order, to the job's accumulators.
-__global__ void tally_finish_kernel(const double *partials, unsigned nb, double *acc) {
-    if (threadIdx.x >= RP_TALLY_N) return;
-    double t = 0.0;
-    for (unsigned b = 0; b < nb; b++) t += partials[(size_t)b * RP_TALLY_N + threadIdx.x];
-    acc[threadIdx.x] += t;
+// One warp per global group: the tallies of the group's rays that ended on
+// their job's detector face (hit point origin + direction * length; power
+// (|E1|^2 + |E2|^2) Re n, ctracer.pyx:1971-1978), each lane over its four
+// rays in order, then a fixed tree across the warp.
+__global__ void batch_tally_kernel(const BatchDev *B, double *partials) {
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    for (unsigned long long u = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+         u < B->total_units; u += warps) {
+        const int j = batch_job_of(B, (unsigned)u);
+        const BatchJob &J = B->jobs[j];
+        const RaySoA &in = J.a.in;
+        const unsigned long long g0 = (u - B->unit_start[j]) * (unsigned long long)RP_GROUP;
+        double v[RP_TALLY_N] = {0, 0, 0, 0, 0, 0};
+        for (int c = 0; c < RP_GROUP / 32; c++) {
+            const unsigned long long i = g0 + 32 * c + lane;
+            if (i < J.a.n_in && J.detector >= 0 && in.endf[i] == (unsigned)J.detector) {
+                const double L = in.len[i];
+                const double x = in.ox[i] + in.dx[i] * L, y = in.oy[i] + in.dy[i] * L;
+                const double2 a = in.e1[i], b = in.e2[i];
+                v[0] += 1.0;
+                v[1] += (a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y) * in.n[i].x;
+                v[2] += x;
+                v[3] += y;
+                v[4] += x * x;
+                v[5] += y * y;
+            }
+        }
+        for (int k = 0; k < RP_TALLY_N; k++) {
+            double t = v[k];
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            if (lane == 0) partials[u * RP_TALLY_N + k] = t;
+        }
+    }
+}
+
+// One block per job of the batch: its groups' tally partials summed in a
+// fixed order that depends only on the job (thread t adds groups t, t + 256,
+// ... of the job in turn, then a fixed tree over the threads) and added to
+// its slot's accumulators; and its child count (from the batch scan, or a
+// plain-path job's own scan) -- written to mapped host memory.
+#define RP_FINISH_THREADS 256
+__global__ void __launch_bounds__(RP_FINISH_THREADS)
+    batch_finish_kernel(const BatchDev *B, const double *partials, const unsigned long long *offsets,
+                        const unsigned long long *total, double *acc, const unsigned *ctr, StepOut *out) {
+    __shared__ double red[RP_TALLY_N][RP_FINISH_THREADS];
+    const int j = blockIdx.x;
+    if (j >= B->n_jobs) return;
+    const BatchJob &J = B->jobs[j];
+    const unsigned u0 = B->unit_start[j], u1 = B->unit_start[j + 1];
+    double v[RP_TALLY_N] = {0, 0, 0, 0, 0, 0};
+    for (unsigned u = u0 + threadIdx.x; u < u1; u += RP_FINISH_THREADS)
+        for (int k = 0; k < RP_TALLY_N; k++) v[k] += partials[(size_t)u * RP_TALLY_N + k];
+    for (int k = 0; k < RP_TALLY_N; k++) red[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int h = RP_FINISH_THREADS / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int k = 0; k < RP_TALLY_N; k++) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double *a = acc + (size_t)J.slot * RP_TALLY_N;
+        for (int k = 0; k < RP_TALLY_N; k++) {
+            a[k] = J.first ? red[k][0] : a[k] + red[k][0];
+            out->acc[J.slot][k] = a[k];
+        }
+        unsigned long long c = 0;
+        if (J.mixed)
+            c = J.a.emit ? ((j + 1 < B->n_jobs ? offsets[u1] : *total) - offsets[u0]) : 0ull;
+        else
+            c = J.own_count ? *J.own_count : 0ull;  // set only when the plain job keeps children
+        out->count[J.slot] = c;
+        if (j == 0) out->err = ctr[2] | ctr[3];
+        __threadfence_system();
+    }
 }
 
 }  // namespace rp
@@ -156,6 +228,8 @@ __global__ void tally_finish_kernel(const double *partials, unsigned nb, double 
 namespace {
 
 using Clock = std::chrono::steady_clock;
+
+size_t align256s(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct Job {
     uint64_t id = 0;
@@ -176,20 +250,17 @@ struct Job {
     rp_job_result res;
     std::vector<uint32_t> face_counts;
     bool done = false;
-};
-
-struct Lane {
-    int index = 0;
-    rp_ctx *ctx = nullptr;
-    std::thread th;
-    uint64_t reserved = 0;
-    cudaGraphExec_t exec[2] = {nullptr, nullptr};  // [emit]
-    unsigned char *scratch = nullptr;               // header | tile counts | tile offsets | tally partials
-    size_t scratch_bytes = 0;
-    rp_rays *arena = nullptr;
-    double *acc = nullptr;                          // device tally accumulators
-    unsigned long long *h_hdr = nullptr;            // pinned read-back of the header
-    double *h_acc = nullptr;                        // pinned read-back of the tallies
+    // while admitted
+    int slot = -1;
+    int gen = 0;
+    uint64_t segments = 0;
+    bool mixed = true;
+    rp_scene *sc = nullptr;
+    void *mx = nullptr;           // float / float-float tables (mixed)
+    size_t mx_bytes = 0;
+    rp_rays *cur = nullptr, *next = nullptr, *spare = nullptr, *arena = nullptr;  // spare: cur's ping-pong partner
+    unsigned char *hand = nullptr;  // hit hand-over (mixed) or own scan scratch (plain)
+    size_t hand_bytes = 0, hand_cap = 0;
 };
 
 }  // namespace
@@ -197,16 +268,27 @@ struct Lane {
 struct rp_server {
     int device = 0;
     uint64_t budget = 0;
-    std::vector<Lane *> lanes;
+    int max_jobs = 0;
+    rp_ctx *ctx = nullptr;
+    std::thread loop;
     std::mutex mu;
     std::condition_variable cv_pending, cv_done;
     std::deque<Job *> pending;
     std::map<uint64_t, Job *> jobs;
+    std::vector<Job *> slots;  // admitted jobs by slot
     uint64_t next_id = 1;
-    uint64_t reserved_total = 0;
-    int busy = 0;
+    uint64_t reserved = 0;
     bool stop = false;
     Clock::time_point t0;
+    // batch step buffers (device unless noted)
+    BatchDev *h_batch = nullptr, *d_batch = nullptr;  // h_batch: pinned
+    unsigned *d_ctr = nullptr;
+    unsigned *d_counts = nullptr;
+    unsigned long long *d_offsets = nullptr, *d_total = nullptr, *d_dummy = nullptr;
+    double *d_partials = nullptr, *d_acc = nullptr;
+    StepOut *h_out = nullptr, *d_out = nullptr;  // mapped pinned
+    size_t unit_cap = 0;
+    cudaGraphExec_t step_exec = nullptr;
 };
 
 namespace {
@@ -214,8 +296,6 @@ namespace {
 double ms_since(const rp_server *s) {
     return std::chrono::duration<double, std::milli>(Clock::now() - s->t0).count();
 }
-
-size_t align256s(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Device bytes a job is expected to hold: the generation in flight (n), its
 // child buffer (2n), the child-slot arena (2n plus a quarter) and the scene.
@@ -225,141 +305,123 @@ uint64_t job_estimate(const Job *j) {
            (uint64_t)j->wl.size() * 64 + (1u << 20);
 }
 
-int lane_scratch(Lane *L, uint64_t n_tiles) {
-    const size_t nb_tally = (size_t)((n_tiles * RP_BLOCK + RP_TALLY_BLOCK - 1) / RP_TALLY_BLOCK);
-    const uint64_t n_sub = n_tiles * RP_SUB_PER_BLOCK;  // count entries are per 32-ray sub-tile
-    const size_t need = 64 + align256s(n_sub * 4) + align256s(n_sub * 8) + rp_hit_bytes(n_sub * RP_SUB) +
-                        align256s(nb_tally * RP_TALLY_N * 8);
-    if (need <= L->scratch_bytes) return RP_OK;
-    if (L->scratch) {
-        cudaStreamSynchronize(L->ctx->stream);
-        cudaFree(L->scratch);
-        L->scratch = nullptr;
-        L->scratch_bytes = 0;
-    }
-    cudaError_t e = cudaMalloc((void **)&L->scratch, need * 2);
-    if (e != cudaSuccess) return rp__cuda_fail(e, "server scratch");
-    L->scratch_bytes = need * 2;
-    return RP_OK;
+void free_unit_arrays(rp_server *s) {
+    if (s->d_counts) cudaFree(s->d_counts);
+    if (s->d_offsets) cudaFree(s->d_offsets);
+    if (s->d_partials) cudaFree(s->d_partials);
+    s->d_counts = nullptr;
+    s->d_offsets = nullptr;
+    s->d_partials = nullptr;
+    s->unit_cap = 0;
 }
 
-int lane_arena(Lane *L, uint64_t n_tiles) {
-    const uint64_t need = n_tiles * RP_TILE_SLOTS;
-    uint64_t cap = 0;
-    if (L->arena) rp_rays_capacity(L->arena, &cap);
-    if (L->arena && cap >= need) return RP_OK;
-    if (L->arena) {
-        rp_rays_free(L->arena);
-        L->arena = nullptr;
-    }
-    return rp_rays_alloc(L->ctx, need + need / 4, &L->arena);
-}
-
-// Captures one generation into a graph and launches it through the lane's
-// instantiated graph for that shape, updating its parameters in place.
-int run_generation(Lane *L, rp_scene *sc, rp_rays *in, rp_rays *out, const Job *j, int emit) {
-    rp_ctx *ctx = L->ctx;
-    const uint64_t n = in->n, n_tiles = (n + RP_BLOCK - 1) / RP_BLOCK;
-    int rc = lane_scratch(L, n_tiles);
-    if (rc == RP_OK && emit) rc = lane_arena(L, n_tiles);
-    if (rc) return rc;
-    unsigned char *sc0 = L->scratch;
-    GenArgs a;
-    memset(&a, 0, sizeof a);
-    a.in = in->soa;
-    a.out = emit ? out->soa : in->soa;
-    a.n_in = n;
-    a.out_cap = emit ? out->cap : 0;
-    a.max_len = (double)j->max_length;
-    a.e2_term = j->e2;
-    a.emit = emit;
-    a.one_list = -1;
-    a.one_face = -1;
-    a.S = sc->S;
-    a.smem_tables = sc->smem_tables;
-    a.mixed_fallback = sc->mixed_fallback;
-    a.out_count = (unsigned long long *)(sc0 + 0);
-    a.err = (unsigned *)(sc0 + 8);
-    a.stats = (unsigned long long *)(sc0 + 24);
-    a.tile_next = (unsigned *)(sc0 + 40);
-    const uint64_t n_sub = n_tiles * RP_SUB_PER_BLOCK;
-    a.tile_counts = (unsigned *)(sc0 + 64);
-    a.tile_offsets = (unsigned long long *)(sc0 + 64 + align256s(n_sub * 4));
-    double *partials = (double *)(sc0 + 64 + align256s(n_sub * 4) + align256s(n_sub * 8) + rp_hit_bytes(n_sub * RP_SUB));
-    a.scratch = emit ? L->arena->soa : in->soa;
-    a.face_counts = sc->face_counts;
-    const bool mixed = (j->flags & RP_TRACE_MIXED) != 0;
-    rp__set_mixed_handover(a, j->flags, sc0, n_sub);
-    cudaError_t e = mixed ? prepare_generation_mixed(a, sc->smem) : prepare_generation_plain(a, sc->smem);
-    if (e != cudaSuccess) return rp__cuda_fail(e, "generation set-up");
-    const unsigned nb_tally = (unsigned)((n + RP_TALLY_BLOCK - 1) / RP_TALLY_BLOCK);
-
+// The step graph: the batch table's upload, the counters' clear, the mixed
+// jobs' search and material kernels, the scan of every group's child count,
+// the placement, the tallies and the per-job results.  Its pointers are
+// fixed for a unit capacity; a larger batch re-allocates and re-captures it.
+int capture_step(rp_server *s) {
+    rp_ctx *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
-    cudaGraph_t graph = nullptr;
+    if (s->step_exec) {
+        cudaGraphExecDestroy(s->step_exec);
+        s->step_exec = nullptr;
+    }
+    // kernel attributes are set before the capture (set-up calls are not captured)
+    size_t ss = 0, ms = 0;
+    int sb = 0, mb = 0;
+    cudaError_t e = prepare_batch_mixed(&ss, &ms, &sb, &mb);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "batch kernel set-up");
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    const unsigned small_grid = (unsigned)(sms > 0 ? 4 * sms : 512);
+    cudaGraph_t g = nullptr;
     e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return rp__cuda_fail(e, "cudaStreamBeginCapture");
-    cudaError_t ce = cudaMemsetAsync(sc0, 0, 64, st);
-    if (ce == cudaSuccess) ce = mixed ? launch_generation_mixed(a, sc->smem, st) : launch_generation_plain(a, sc->smem, st);
-    if (ce == cudaSuccess && emit) ce = launch_tile_scan(a, st);
-    if (ce == cudaSuccess && emit) ce = launch_place_children(a, st);
-    if (ce == cudaSuccess && j->detector >= 0) {
-        tally_kernel<<<nb_tally, RP_TALLY_BLOCK, 0, st>>>(in->soa, n, (unsigned)j->detector, partials);
-        tally_finish_kernel<<<1, 32, 0, st>>>(partials, nb_tally, L->acc);
+    cudaError_t ce = cudaMemcpyAsync(s->d_batch, s->h_batch, sizeof(BatchDev), cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(s->d_ctr, 0, 3 * sizeof(unsigned), st);  // [3]: the plain jobs' errors
+    if (ce == cudaSuccess) ce = launch_batch_mixed(s->d_batch, s->d_ctr, st);
+    if (ce == cudaSuccess) ce = launch_tile_scan_dev(s->d_counts, &s->d_batch->total_units, s->d_offsets, s->d_total, st);
+    if (ce == cudaSuccess) {
+        batch_place_kernel<<<small_grid, 32 * RP_SERVE_WARPS_PER_BLOCK, 0, st>>>(s->d_batch, s->d_offsets, s->d_ctr + 2);
+        batch_tally_kernel<<<small_grid, 32 * RP_SERVE_WARPS_PER_BLOCK, 0, st>>>(s->d_batch, s->d_partials);
+        batch_finish_kernel<<<RP_BATCH_MAX_JOBS, RP_FINISH_THREADS, 0, st>>>(
+            s->d_batch, s->d_partials, s->d_offsets, s->d_total, s->d_acc, s->d_ctr, s->d_out);
         ce = cudaGetLastError();
     }
-    if (ce == cudaSuccess)
-        ce = cudaMemcpyAsync(L->h_hdr, sc0, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-    e = cudaStreamEndCapture(st, &graph);
+    e = cudaStreamEndCapture(st, &g);
     if (ce != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        return rp__cuda_fail(ce, "generation capture");
+        if (g) cudaGraphDestroy(g);
+        return rp__cuda_fail(ce, "step capture");
     }
     if (e != cudaSuccess) return rp__cuda_fail(e, "cudaStreamEndCapture");
-    cudaGraphExec_t &ex = L->exec[emit ? 1 : 0];
-    bool fresh = ex == nullptr;
-    if (!fresh) {
-        cudaGraphExecUpdateResultInfo info;
-        if (cudaGraphExecUpdate(ex, graph, &info) != cudaSuccess) {
-            cudaGetLastError();
-            cudaGraphExecDestroy(ex);
-            ex = nullptr;
-            fresh = true;
-        }
-    }
-    if (fresh) {
-        e = cudaGraphInstantiate(&ex, graph, 0);
-        if (e != cudaSuccess) {
-            cudaGraphDestroy(graph);
-            ex = nullptr;
-            return rp__cuda_fail(e, "cudaGraphInstantiate");
-        }
-    }
-    cudaGraphDestroy(graph);
-    e = cudaGraphLaunch(ex, st);
-    if (e != cudaSuccess) return rp__cuda_fail(e, "cudaGraphLaunch");
-    e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return rp__cuda_fail(e, "generation");
-    const unsigned err = (unsigned)(L->h_hdr[1] & 0xffffffffu);
-    if (err & (ERR_WAVELENGTH | ERR_ZK_STACK | ERR_SHAPE_STACK | ERR_OVERFLOW)) {
-        rp__set_error("generation error bits 0x%x", err);
-        return RP_ERR_INVALID;
+    e = cudaGraphInstantiate(&s->step_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        s->step_exec = nullptr;
+        return rp__cuda_fail(e, "cudaGraphInstantiate");
     }
     return RP_OK;
 }
 
-void run_job(rp_server *srv, Lane *L, Job *j) {
-    rp_ctx *ctx = L->ctx;
-    j->res.t_start_ms = ms_since(srv);
-    rp_scene *sc = nullptr;
-    rp_rays *g = nullptr;
-    int rc = rp_scene_create(ctx, &j->desc, j->wl.empty() ? nullptr : j->wl.data(), (int64_t)j->wl.size(), &sc);
+int ensure_units(rp_server *s, size_t units) {
+    if (units <= s->unit_cap && s->step_exec) return RP_OK;
+    size_t cap = s->unit_cap ? s->unit_cap : 4096;
+    while (cap < units) cap *= 2;
+    cudaStreamSynchronize(s->ctx->stream);
+    free_unit_arrays(s);
+    cudaError_t e = cudaMalloc((void **)&s->d_counts, (cap + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_offsets, (cap + 1) * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_partials, (cap + 1) * RP_TALLY_N * sizeof(double));
+    if (e != cudaSuccess) {
+        free_unit_arrays(s);
+        return rp__cuda_fail(e, "batch unit arrays");
+    }
+    s->unit_cap = cap;
+    return capture_step(s);
+}
+
+void release_job_buffers(rp_ctx *ctx, Job *j) {
+    if (j->cur) rp_rays_free(j->cur);
+    if (j->next) rp_rays_free(j->next);
+    if (j->spare) rp_rays_free(j->spare);
+    if (j->arena) rp_rays_free(j->arena);
+    j->cur = j->next = j->spare = j->arena = nullptr;
+    if (j->hand) rp__ctx_free(ctx, j->hand, j->hand_bytes);
+    if (j->mx) rp__ctx_free(ctx, j->mx, j->mx_bytes);
+    j->hand = nullptr;
+    j->mx = nullptr;
+    j->hand_cap = 0;
+}
+
+// Admission: the job's scene and tables on the device and its source rays
+// generated into its first generation.
+int admit(rp_server *s, Job *j) {
+    rp_ctx *ctx = s->ctx;
+    j->res.t_start_ms = ms_since(s);
+    j->mixed = (j->flags & RP_TRACE_MIXED) != 0;
+    int rc = rp_scene_create(ctx, &j->desc, j->wl.empty() ? nullptr : j->wl.data(), (int64_t)j->wl.size(), &j->sc);
+    if (rc) return rc;
+    if (j->mixed && j->sc->mixed_fallback) {
+        rp__set_error("the batched mixed path serves scenes of specialised faces and materials only");
+        return RP_ERR_UNSUPPORTED;
+    }
     const uint64_t n0 = j->source.n_rays;
-    if (rc == RP_OK) rc = rp_rays_alloc(ctx, n0 ? n0 : 1, &g);
-    if (rc == RP_OK && cudaMemsetAsync(L->acc, 0, RP_TALLY_N * sizeof(double), ctx->stream) != cudaSuccess)
-        rc = RP_ERR_CUDA;
-    if (rc == RP_OK && n0) {
+    rc = rp_rays_alloc(ctx, n0 ? n0 : 1, &j->cur);
+    if (rc) return rc;
+    if (j->mixed) {
+        j->mx_bytes = batch_tables_bytes(j->sc->S.n_lists, j->sc->S.n_faces);
+        rc = rp__ctx_alloc(ctx, &j->mx, j->mx_bytes, &j->mx_bytes);
+        if (rc) return rc;
+        GenArgs a;
+        memset(&a, 0, sizeof a);
+        a.S = j->sc->S;
+        a.max_len = (double)j->max_length;
+        cudaError_t e = launch_batch_tables(a, j->mx, ctx->stream);
+        if (e != cudaSuccess) return rp__cuda_fail(e, "batch tables");
+    }
+    if (n0) {
         SourceArgs A;
-        A.out = g->soa;
+        A.out = j->cur->soa;
         A.n = n0;
         A.seed = j->source.seed;
         A.type = j->source.type;
@@ -370,105 +432,258 @@ void run_job(rp_server *srv, Lane *L, Job *j) {
         A.radius = j->source.radius;
         A.n_wl = (unsigned)(j->wl.empty() ? 1 : j->wl.size());
         source_kernel<<<(unsigned)((n0 + 255) / 256), 256, 0, ctx->stream>>>(A);
-        if (cudaGetLastError() != cudaSuccess) rc = RP_ERR_CUDA;
-        g->n = n0;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return rp__cuda_fail(e, "source kernel");
     }
-    uint64_t segments = 0;
-    int count = 0;
-    while (rc == RP_OK && g && g->n > 0 && count < j->recursion_limit) {
-        const int last = (count + 1 == j->recursion_limit);
-        rp_rays *out = nullptr;
-        if (!last) rc = rp_rays_alloc(ctx, 2 * g->n, &out);
-        if (rc) break;
-        rc = run_generation(L, sc, g, out, j, last ? 0 : 1);
-        if (rc) {
-            if (out) rp_rays_free(out);
-            break;
-        }
-        segments += g->n;
-        count++;
-        const uint64_t n_child = last ? 0 : L->h_hdr[0];
-        rp_rays_free(g);
-        g = out;
-        if (g) g->n = n_child;
-        if (last || n_child == 0) break;
-    }
-    if (g) rp_rays_free(g);
-    j->res.status = rc;
-    j->res.generations = count;
-    j->res.segments = segments;
-    if (sc) {
+    j->cur->n = n0;
+    j->gen = 0;
+    j->segments = 0;
+    return RP_OK;
+}
+
+void finish_job(rp_server *s, Job *j, int status) {
+    j->res.status = status;
+    j->res.generations = j->gen;
+    j->res.segments = j->segments;
+    if (j->sc) {
         j->face_counts.assign(j->desc.n_faces, 0u);
-        if (rc == RP_OK && j->desc.n_faces)
-            rc = rp_scene_face_counts(sc, j->face_counts.data(), j->desc.n_faces, 0);
-        rp_scene_destroy(sc);
+        if (j->desc.n_faces) {
+            int rc = rp_scene_face_counts(j->sc, j->face_counts.data(), j->desc.n_faces, 0);
+            if (rc && j->res.status == RP_OK) j->res.status = rc;
+        }
     }
-    if (rc == RP_OK) {
-        if (cudaMemcpy(L->h_acc, L->acc, RP_TALLY_N * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
-            rc = RP_ERR_CUDA;
+    if (j->res.status == RP_OK && j->slot >= 0 && j->gen > 0) {
+        const double *a = s->h_out->acc[j->slot];
+        j->res.detector_hits = (uint64_t)a[0];
+        j->res.detector_power = a[1];
+        j->res.sum_x = a[2];
+        j->res.sum_y = a[3];
+        j->res.sum_xx = a[4];
+        j->res.sum_yy = a[5];
     }
-    j->res.status = rc;
-    j->res.detector_hits = rc == RP_OK ? (uint64_t)L->h_acc[0] : 0;
-    j->res.detector_power = rc == RP_OK ? L->h_acc[1] : 0.0;
-    j->res.sum_x = rc == RP_OK ? L->h_acc[2] : 0.0;
-    j->res.sum_y = rc == RP_OK ? L->h_acc[3] : 0.0;
-    j->res.sum_xx = rc == RP_OK ? L->h_acc[4] : 0.0;
-    j->res.sum_yy = rc == RP_OK ? L->h_acc[5] : 0.0;
-    j->res.t_done_ms = ms_since(srv);
+    release_job_buffers(s->ctx, j);
+    if (j->sc) {
+        rp_scene_destroy(j->sc);
+        j->sc = nullptr;
+    }
+    j->res.t_done_ms = ms_since(s);
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (j->slot >= 0) s->slots[j->slot] = nullptr;
+    s->reserved -= j->est_bytes;
+    j->done = true;
+    s->cv_done.notify_all();
 }
 
-uint64_t lane_memory(Lane *L) {
-    uint64_t b = 0;
-    rp_ctx_memory(L->ctx, &b);
-    return b + L->scratch_bytes;
+// Buffer `b` with room for `need` records: kept when it has it, else replaced
+// by one with a quarter more room (a job's generations grow by splitting, so
+// its buffers are re-allocated only a few times in its life).
+int ensure_rays(rp_ctx *ctx, rp_rays **b, uint64_t need) {
+    uint64_t cap = 0;
+    if (*b) rp_rays_capacity(*b, &cap);
+    if (*b && cap >= need) return RP_OK;
+    if (*b) rp_rays_free(*b);
+    *b = nullptr;
+    return rp_rays_alloc(ctx, need + need / 4, b);
 }
 
-void lane_main(rp_server *srv, Lane *L) {
-    cudaSetDevice(srv->device);
+// A job's generation arguments for this step, with buffers grown as needed:
+// the next generation (two children per ray at most) in the partner of the
+// current one, the child-slot arena and the hand-over (mixed), or its own
+// scan scratch (plain).
+int prepare_job(rp_server *s, Job *j, GenArgs &a) {
+    rp_ctx *ctx = s->ctx;
+    const uint64_t n = j->cur->n;
+    const uint64_t units = (n + RP_GROUP - 1) / RP_GROUP;
+    const int emit = j->gen + 1 < j->recursion_limit;
+    int rc = RP_OK;
+    if (emit) {
+        rc = ensure_rays(ctx, &j->spare, 2 * n);
+        if (rc) return rc;
+        j->next = j->spare;
+        j->spare = nullptr;
+        rc = ensure_rays(ctx, &j->arena, units * RP_TILE_SLOTS);
+        if (rc) return rc;
+    }
+    // mixed: hit hand-over for n rays; plain: counters, sub-tile counts and offsets
+    const uint64_t n_sub = rp_n_sub(n);
+    const size_t need = j->mixed ? (size_t)rp_hit_bytes(n ? n : 1)
+                                 : 64 + align256s(n_sub * 4) + align256s(n_sub * 8) + 256;
+    if (need > j->hand_cap) {
+        if (j->hand) rp__ctx_free(ctx, j->hand, j->hand_bytes);
+        j->hand = nullptr;
+        const size_t want = need + need / 4;
+        rc = rp__ctx_alloc(ctx, (void **)&j->hand, want, &j->hand_bytes);
+        if (rc) return rc;
+        j->hand_cap = want;
+    }
+    memset(&a, 0, sizeof a);
+    a.in = j->cur->soa;
+    a.wb = j->cur->soa;
+    a.out = emit ? j->next->soa : j->cur->soa;
+    a.out_cap = emit ? j->next->cap : 0;
+    a.n_in = n;
+    a.max_len = (double)j->max_length;
+    a.e2_term = j->e2;
+    a.emit = emit;
+    a.one_list = -1;
+    a.one_face = -1;
+    a.S = j->sc->S;
+    a.smem_tables = j->sc->smem_tables;
+    a.mixed_fallback = j->sc->mixed_fallback;
+    a.scratch = emit ? j->arena->soa : j->cur->soa;
+    a.face_counts = j->sc->face_counts;
+    a.stats = s->d_dummy;
+    if (j->mixed) {
+        a.err = s->d_ctr + 2;
+        a.unit_rays = RP_GROUP;
+        a.hit_t = (float2 *)j->hand;
+        a.hit_face = (int *)(j->hand + align256s((size_t)(n ? n : 1) * 8));
+    } else {
+        unsigned char *sc = j->hand;
+        a.out_count = (unsigned long long *)sc;
+        a.err = s->d_ctr + 3;
+        a.tile_next = (unsigned *)(sc + 40);
+        a.unit_rays = RP_SUB;
+        a.tile_counts = (unsigned *)(sc + 64);
+        a.tile_offsets = (unsigned long long *)(sc + 64 + align256s(n_sub * 4));
+    }
+    return RP_OK;
+}
+
+// One step: every admitted job advances one generation.
+void run_step(rp_server *s) {
+    rp_ctx *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    std::vector<Job *> act;
+    for (Job *j : s->slots)
+        if (j) act.push_back(j);
+    BatchDev &B = *s->h_batch;
+    std::vector<GenArgs> plain_args;
+    std::vector<Job *> failed;
+    unsigned units = 0;
+    int nj = 0;
+    for (Job *j : act) {
+        GenArgs a;
+        int rc = prepare_job(s, j, a);
+        if (rc) {
+            failed.push_back(j);
+            j->res.status = rc;
+            continue;
+        }
+        BatchJob &J = B.jobs[nj];
+        J.a = a;
+        J.mx_lists = j->mx;
+        // the face table follows the list table (batch_tables_bytes of the lists alone)
+        J.mx_faces = j->mx ? static_cast<const unsigned char *>(j->mx) + batch_tables_bytes(j->sc->S.n_lists, 0)
+                           : nullptr;
+        J.own_count = (!j->mixed && a.emit) ? a.out_count : nullptr;
+        J.detector = j->detector;
+        J.mixed = j->mixed ? 1 : 0;
+        J.slot = j->slot;
+        J.first = j->gen == 0;
+        B.unit_start[nj] = units;
+        const unsigned ju = (unsigned)((a.n_in + RP_GROUP - 1) / RP_GROUP);
+        J.a.tile_counts = nullptr;  // set below, once the unit arrays exist
+        if (!j->mixed) {
+            plain_args.push_back(a);
+            J.a.emit = 0;  // the batch kernels leave a plain job's rays alone
+        }
+        units += ju;
+        nj++;
+        act[nj - 1] = j;
+    }
+    act.resize(nj);
+    for (Job *j : failed) finish_job(s, j, j->res.status);
+    if (nj == 0) return;
+    B.n_jobs = nj;
+    B.total_units = units;
+    B.unit_start[nj] = units;
+    int rc = ensure_units(s, units);
+    if (rc) {
+        for (Job *j : act) finish_job(s, j, rc);
+        return;
+    }
+    for (int k = 0; k < nj; k++) {
+        B.jobs[k].a.tile_counts = s->d_counts + B.unit_start[k];
+        B.jobs[k].a.tile_offsets = s->d_offsets + B.unit_start[k];
+    }
+    // plain-path jobs: their own generation, scan and placement, queued first
+    cudaError_t e = cudaMemsetAsync(s->d_ctr + 3, 0, sizeof(unsigned), st);
+    for (size_t p = 0, k = 0; k < (size_t)nj && e == cudaSuccess; k++) {
+        if (B.jobs[k].mixed) continue;
+        GenArgs &a = plain_args[p++];
+        e = cudaMemsetAsync(a.out_count, 0, 64, st);
+        if (e == cudaSuccess) e = launch_generation_plain(a, act[k]->sc->smem, st);
+        if (e == cudaSuccess && a.emit) e = launch_tile_scan(a, st);
+        if (e == cudaSuccess && a.emit) e = launch_place_children(a, st);
+    }
+    if (e == cudaSuccess) e = cudaGraphLaunch(s->step_exec, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    const unsigned err = e == cudaSuccess ? s->h_out->err : 0u;
+    for (int k = 0; k < nj; k++) {
+        Job *j = act[k];
+        const uint64_t n = j->cur->n;
+        if (e != cudaSuccess) {
+            finish_job(s, j, rp__cuda_fail(e, "batch step"));
+            continue;
+        }
+        if (err & (ERR_WAVELENGTH | ERR_ZK_STACK | ERR_SHAPE_STACK | ERR_OVERFLOW)) {
+            rp__set_error("batch step error bits 0x%x", err);
+            finish_job(s, j, RP_ERR_INVALID);
+            continue;
+        }
+        j->segments += n;
+        j->gen++;
+        const uint64_t count = s->h_out->count[j->slot];
+        if (j->next && count > 0) {
+            j->spare = j->cur;  // reused for the generation after next
+            j->cur = j->next;
+            j->cur->n = count;
+            j->next = nullptr;
+        } else {
+            finish_job(s, j, RP_OK);
+        }
+    }
+}
+
+void step_loop(rp_server *s) {
+    cudaSetDevice(s->device);
     for (;;) {
-        Job *j = nullptr;
+        std::vector<Job *> admitted;
         {
-            std::unique_lock<std::mutex> lk(srv->mu);
+            std::unique_lock<std::mutex> lk(s->mu);
             for (;;) {
-                if (srv->stop && srv->pending.empty()) return;
-                if (!srv->pending.empty()) {
-                    Job *h = srv->pending.front();
-                    const uint64_t mine = lane_memory(L);
-                    const uint64_t need = mine > h->est_bytes ? mine : h->est_bytes;
-                    const uint64_t others = srv->reserved_total - L->reserved;
-                    if (others + need <= srv->budget || srv->busy == 0) {
-                        srv->pending.pop_front();
-                        srv->reserved_total = others + need;
-                        L->reserved = need;
-                        srv->busy++;
-                        j = h;
-                        break;
-                    }
-                    if (mine > 0 && L->reserved == mine) {
-                        // memory pressure: give this idle lane's cached blocks back
-                        lk.unlock();
-                        rp_ctx_trim(L->ctx);
-                        lk.lock();
-                        srv->reserved_total -= L->reserved;
-                        L->reserved = lane_memory(L);
-                        srv->reserved_total += L->reserved;
-                        continue;
-                    }
+                bool any = false;
+                for (Job *j : s->slots) any = any || j;
+                if (any || !s->pending.empty()) break;
+                if (s->stop) return;
+                s->cv_pending.wait(lk);
+            }
+            // admission: FIFO, while a slot is free and the budget holds (one job always runs)
+            while (!s->pending.empty()) {
+                int free_slot = -1, busy = 0;
+                for (int k = 0; k < s->max_jobs; k++) {
+                    if (!s->slots[k] && free_slot < 0) free_slot = k;
+                    if (s->slots[k]) busy++;
                 }
-                srv->cv_pending.wait(lk);
+                Job *h = s->pending.front();
+                if (free_slot < 0 || (busy > 0 && s->reserved + h->est_bytes > s->budget)) break;
+                s->pending.pop_front();
+                h->slot = free_slot;
+                s->slots[free_slot] = h;
+                s->reserved += h->est_bytes;
+                admitted.push_back(h);
             }
         }
-        run_job(srv, L, j);
-        {
-            std::lock_guard<std::mutex> lk(srv->mu);
-            const uint64_t now = lane_memory(L);
-            srv->reserved_total = srv->reserved_total - L->reserved + now;
-            L->reserved = now;
-            srv->busy--;
-            j->done = true;
+        for (Job *j : admitted) {
+            int rc = admit(s, j);
+            if (rc == RP_OK && (j->source.n_rays == 0 || j->recursion_limit <= 0)) {
+                finish_job(s, j, RP_OK);
+            } else if (rc) {
+                finish_job(s, j, rc);
+            }
         }
-        srv->cv_done.notify_all();
-        srv->cv_pending.notify_all();
+        run_step(s);
     }
 }
 
@@ -477,18 +692,16 @@ void copy_table(std::vector<T> &dst, const T *src, int32_t n) {
     dst.assign(src && n > 0 ? src : nullptr, src && n > 0 ? src + n : nullptr);
 }
 
-void destroy_lane(Lane *L) {
-    if (!L) return;
-    cudaSetDevice(L->ctx ? L->ctx->device : 0);
-    for (auto &e : L->exec)
-        if (e) cudaGraphExecDestroy(e);
-    if (L->arena) rp_rays_free(L->arena);
-    if (L->scratch) cudaFree(L->scratch);
-    if (L->acc) cudaFree(L->acc);
-    if (L->h_hdr) cudaFreeHost(L->h_hdr);
-    if (L->h_acc) cudaFreeHost(L->h_acc);
-    if (L->ctx) rp_ctx_destroy(L->ctx);
-    delete L;
+void destroy_buffers(rp_server *s) {
+    if (s->step_exec) cudaGraphExecDestroy(s->step_exec);
+    free_unit_arrays(s);
+    if (s->d_batch) cudaFree(s->d_batch);
+    if (s->d_ctr) cudaFree(s->d_ctr);
+    if (s->d_total) cudaFree(s->d_total);
+    if (s->d_acc) cudaFree(s->d_acc);
+    if (s->h_batch) cudaFreeHost(s->h_batch);
+    if (s->h_out) cudaFreeHost(s->h_out);
+    if (s->ctx) rp_ctx_destroy(s->ctx);
 }
 
 }  // namespace
@@ -520,34 +733,39 @@ int rp_source_generate(rp_ctx *ctx, const rp_source_desc *src, uint32_t n_wl, rp
 }
 
 int rp_server_create(int device, uint64_t hbm_budget, int32_t lanes, rp_server **out) {
-    if (!out || lanes < 1 || lanes > 64) return RP_ERR_INVALID;
+    if (!out || lanes < 1) return RP_ERR_INVALID;
     *out = nullptr;
     rp_server *s = new (std::nothrow) rp_server();
     if (!s) return RP_ERR_NOMEM;
     s->device = device;
     s->budget = hbm_budget ? hbm_budget : ~(uint64_t)0;
+    s->max_jobs = lanes < RP_BATCH_MAX_JOBS ? lanes : RP_BATCH_MAX_JOBS;
+    s->slots.assign(s->max_jobs, nullptr);
     s->t0 = Clock::now();
-    for (int k = 0; k < lanes; k++) {
-        Lane *L = new (std::nothrow) Lane();
-        if (!L) {
-            rp_server_destroy(s);
-            return RP_ERR_NOMEM;
-        }
-        L->index = k;
-        int rc = rp_ctx_create(device, 0, &L->ctx);
-        if (rc == RP_OK && cudaMalloc((void **)&L->acc, RP_TALLY_N * sizeof(double)) != cudaSuccess) rc = RP_ERR_CUDA;
-        if (rc == RP_OK && cudaMallocHost((void **)&L->h_hdr, 8 * sizeof(unsigned long long)) != cudaSuccess)
-            rc = RP_ERR_CUDA;
-        if (rc == RP_OK && cudaMallocHost((void **)&L->h_acc, RP_TALLY_N * sizeof(double)) != cudaSuccess)
-            rc = RP_ERR_CUDA;
-        if (rc) {
-            destroy_lane(L);
-            rp_server_destroy(s);
-            return rc;
-        }
-        s->lanes.push_back(L);
+    int rc = rp_ctx_create(device, 0, &s->ctx);
+    cudaError_t e = cudaSuccess;
+    if (rc == RP_OK) {
+        e = cudaMallocHost((void **)&s->h_batch, sizeof(BatchDev));
+        if (e == cudaSuccess) e = cudaHostAlloc((void **)&s->h_out, sizeof(StepOut), cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&s->d_out, s->h_out, 0);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_batch, sizeof(BatchDev));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_ctr, RP_BATCH_WORDS * sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_total, 4 * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_acc, RP_BATCH_MAX_JOBS * RP_TALLY_N * sizeof(double));
+        if (e != cudaSuccess) rc = rp__cuda_fail(e, "server buffers");
     }
-    for (Lane *L : s->lanes) L->th = std::thread(lane_main, s, L);
+    if (rc == RP_OK) {
+        memset(s->h_batch, 0, sizeof(BatchDev));
+        memset(s->h_out, 0, sizeof(StepOut));
+        s->d_dummy = s->d_total + 2;
+        rc = ensure_units(s, 4096);
+    }
+    if (rc) {
+        destroy_buffers(s);
+        delete s;
+        return rc;
+    }
+    s->loop = std::thread(step_loop, s);
     *out = s;
     return RP_OK;
 }
@@ -624,10 +842,9 @@ int rp_server_destroy(rp_server *s) {
         s->stop = true;
     }
     s->cv_pending.notify_all();
-    for (Lane *L : s->lanes)
-        if (L->th.joinable()) L->th.join();
-    for (Lane *L : s->lanes) destroy_lane(L);
+    if (s->loop.joinable()) s->loop.join();
     for (auto &kv : s->jobs) delete kv.second;
+    destroy_buffers(s);
     delete s;
     return RP_OK;
 }

@@ -184,8 +184,8 @@ cudaError_t prepare_generation_plain(const GenArgs &a, size_t smem) {
 // gives each chunk its start, and the warp then scans its chunk 128 counts at
 // a time with a running carry, writing the offsets with 16-byte stores.
 #define RP_SCAN_SLICE 128  // counts per warp step: 4 per lane
-__global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *counts, unsigned long long n,
-                                                         unsigned long long *offsets, unsigned long long *total) {
+__device__ __forceinline__ void scan_counts(const unsigned *counts, unsigned long long n, unsigned long long *offsets,
+                                            unsigned long long *total) {
     __shared__ unsigned long long s_warp[32];
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool vec = ((reinterpret_cast<uintptr_t>(counts) | reinterpret_cast<uintptr_t>(offsets)) & 15) == 0;
@@ -251,6 +251,24 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *counts,
         carry += __shfl_sync(0xffffffffu, x, 31);
     }
     if (threadIdx.x == 0) *total = s_warp[31];
+}
+
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned *counts, unsigned long long n,
+                                                         unsigned long long *offsets, unsigned long long *total) {
+    scan_counts(counts, n, offsets, total);
+}
+
+// The same with the count read from device memory (a batch step's unit count
+// is known only on the device when its graph is launched).
+__global__ void __launch_bounds__(1024) tile_scan_dev_kernel(const unsigned *counts, const unsigned *n_dev,
+                                                             unsigned long long *offsets, unsigned long long *total) {
+    scan_counts(counts, (unsigned long long)*n_dev, offsets, total);
+}
+
+cudaError_t launch_tile_scan_dev(const unsigned *counts, const unsigned *n_dev, unsigned long long *offsets,
+                                 unsigned long long *total, cudaStream_t st) {
+    tile_scan_dev_kernel<<<1, 1024, 0, st>>>(counts, n_dev, offsets, total);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_count_scan(const unsigned *counts, unsigned long long n, unsigned long long *offsets,

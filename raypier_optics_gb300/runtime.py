@@ -4,7 +4,9 @@ buffers and uploaded scenes.  Thin ctypes wrappers; all work happens in
 from __future__ import annotations
 
 import ctypes
+import hashlib
 import threading
+from collections import OrderedDict
 
 import numpy as np
 
@@ -34,6 +36,8 @@ class Context:
 
     def close(self):
         if getattr(self, "handle", None):
+            for scene in self.__dict__.pop("_scenes", {}).values():
+                scene.free()
             self.lib.rp_ctx_destroy(self.handle)
             self.handle = None
 
@@ -152,6 +156,7 @@ class DeviceScene:
         _native.check(self.lib.rp_scene_create(ctx.handle, ctypes.byref(desc), wl.ctypes.data if wl.size else None,
                                                wl.shape[0], ctypes.byref(h)), "rp_scene_create")
         self.handle = h
+        self.counts_pending = False
 
     def face_counts(self, reset: bool = True) -> np.ndarray:
         n = self.tables.n_faces
@@ -159,6 +164,8 @@ class DeviceScene:
         if n:
             _native.check(self.lib.rp_scene_face_counts(self.handle, out.ctypes.data, n, int(reset)),
                           "rp_scene_face_counts")
+        if reset:
+            self.counts_pending = False
         return out
 
     def free(self):
@@ -171,3 +178,44 @@ class DeviceScene:
             self.free()
         except Exception:
             pass
+
+
+SCENE_CACHE_SIZE = 8
+
+
+def _scene_key(tables, wavelengths) -> bytes:
+    """Digest of everything rp_scene_create reads: every packed table and the
+    wavelengths.  Two face-list states that pack to the same bytes give the
+    same device scene."""
+    h = hashlib.blake2b(digest_size=20)
+    h.update(np.array([tables.n_faces], dtype=np.int64).tobytes())
+    for a in (tables.lists, tables.faces, tables.materials, tables.shape_ops, tables.distortions,
+              tables.dispersions, tables.aux, np.ascontiguousarray(wavelengths, dtype=np.double)):
+        h.update(np.array([a.shape[0]], dtype=np.int64).tobytes())
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.digest()
+
+
+def cached_scene(ctx: Context, tables, wavelengths) -> DeviceScene:
+    """The uploaded scene for `tables` on `ctx`, created once per distinct
+    content and kept in a small per-context LRU.  A caller driving the
+    generation loop itself (trace_segment once per generation) therefore
+    uploads the scene once; changing a face's parameters changes the packed
+    tables and uploads a new scene.  The per-face hit counts of a reused scene
+    are cleared if its previous user did not read them back."""
+    key = _scene_key(tables, wavelengths)
+    with _lock:
+        cache = ctx.__dict__.setdefault("_scenes", OrderedDict())
+        scene = cache.get(key)
+        if scene is not None:
+            cache.move_to_end(key)
+        else:
+            scene = DeviceScene(ctx, tables, wavelengths)
+            ctx.scene_uploads = getattr(ctx, "scene_uploads", 0) + 1
+            cache[key] = scene
+            while len(cache) > SCENE_CACHE_SIZE:
+                cache.popitem(last=False)[1].free()
+    if scene.counts_pending:
+        scene.face_counts(reset=True)
+    scene.counts_pending = True
+    return scene

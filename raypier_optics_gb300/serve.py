@@ -1,8 +1,9 @@
 """Serving: a stream of trace jobs through the library's job server.
 
-``Server`` wraps rp_server (lanes of contexts sharing one device and one HBM
-budget; jobs start as soon as a lane and memory are free and overlap on the
-device).  ``run_stream`` replays a timed job stream (configuration 5: Poisson
+``Server`` wraps rp_server: up to ``lanes`` jobs in flight on one device
+under one HBM budget, admitted as slots and memory free up; every step of
+the server advances all of them by one generation in shared launches of the
+mixed-path kernels (continuous batching of generations).  ``run_stream`` replays a timed job stream (configuration 5: Poisson
 arrivals, systems of 3-39 faces, log-uniform ray counts) against a server and
 returns each job's latency and result.
 """

@@ -60,7 +60,7 @@ def trace_rays(input_rays, face_lists, recursion_limit=100, max_length=100.0, fl
     for fs in face_sets:
         fs.sync_transforms()
     tables = compile_scene(face_sets)
-    scene = runtime.DeviceScene(ctx, tables, wavelengths)
+    scene = runtime.cached_scene(ctx, tables, wavelengths)
     dev0 = input_rays._device(ctx)
     max_gens = max(int(recursion_limit), 1) + 1
     gens = (ctypes.c_void_p * max_gens)()
@@ -99,7 +99,7 @@ def _trace_generation(rays, face_sets, all_faces, max_length, one_face=None, fla
     ctx = ctx or runtime.get_context()
     check_face_indices(face_sets, all_faces)
     tables = compile_scene(face_sets)
-    scene = runtime.DeviceScene(ctx, tables, rays.wavelengths)
+    scene = runtime.cached_scene(ctx, tables, rays.wavelengths)
     dev_in = rays._device(ctx)
     out = runtime.DeviceRays(ctx, 2 * max(rays.n_rays, 1))
     stats = _native.Stats()
@@ -128,7 +128,7 @@ def _trace_gausslet_generation(gc, face_sets, all_faces, max_length, one_face=No
     ctx = ctx or runtime.get_context()
     check_face_indices(face_sets, all_faces)
     tables = compile_scene(face_sets)
-    scene = runtime.DeviceScene(ctx, tables, gc.wavelengths)
+    scene = runtime.cached_scene(ctx, tables, gc.wavelengths)
     n = gc.n_rays
     capture = len(decomp_faces) > 0
     before = gc.copy_as_array() if capture else None

@@ -129,6 +129,40 @@ def test_gpu_trace_segment_mutates_input_and_appends_children_in_order():
     np.testing.assert_array_equal([f.count for f in all_faces], ocounts[:tables.n_faces])
 
 
+def test_gpu_trace_segment_loop_uploads_scene_once():
+    """A caller's own generation loop over trace_segment (the reference's
+    core/tracer.py:36-45 loop) uploads the scene once; a changed face
+    parameter uploads a new one, and every generation still equals the
+    oracle's."""
+    from raypier_optics_gb300 import runtime
+    c = load_case("config2_sub24")
+    lists, all_faces = build(c["spec"])
+    ctx = runtime.get_context()
+
+    def run_loop(n_gens):
+        rc = RayCollection.from_array(c["rays"])
+        rc.wavelengths = c["wl"]
+        tables = scene.compile_scene(lists)
+        host = c["rays"]
+        for g in range(n_gens):
+            if rc.n_rays == 0:
+                break
+            kids = ctracer.trace_segment(rc, lists, all_faces, max_length=1000.0)
+            mutated, okids, _ = oracle.trace_segment(tables, c["wl"], host, 1000.0)
+            assert_records(rc.copy_as_array(), mutated, what=f"generation {g} input")
+            assert_records(kids.copy_as_array(), okids, what=f"generation {g} children")
+            rc, host = kids, okids
+
+    all_faces[0].curvature *= 1.001   # a scene no earlier test uploaded
+    before = getattr(ctx, "scene_uploads", 0)
+    run_loop(4)
+    assert ctx.scene_uploads - before == 1
+    all_faces[0].curvature *= 1.01
+    all_faces[0].update()
+    run_loop(3)
+    assert ctx.scene_uploads - before == 2
+
+
 def test_gpu_trace_one_face_segment_matches_oracle():
     c = load_case("config2_sub24")
     lists, all_faces = build(c["spec"])

@@ -1,6 +1,7 @@
 """The trace-job server (configuration 5): a job's result equals the same
-trace run through rp_trace_rays, is the same alone and among other jobs, and
-the HBM budget holds jobs back."""
+trace run through rp_trace_rays (its generations advanced in batched steps
+with other jobs' rays sharing the kernels' launches), is the same alone and
+among other jobs, and the HBM budget holds jobs back."""
 import ctypes
 
 import numpy as np
@@ -69,14 +70,14 @@ def test_results_are_the_same_alone_and_in_the_mix(stream):
     systems, jobs = stream
     jobs = [dict(j, n_rays=min(j["n_rays"], 300000), system=j["system"] % len(systems)) for j in jobs]
     probe = jobs[:6]
-    # alone: one lane, one job at a time
+    # alone: one job in flight at a time
     srv = serve.Server(lanes=1)
     alone = []
     for j in probe:
         jid = srv.submit(systems[j["system"]], serve.source_desc(j["source"], j["n_rays"], j["seed"]), j["wavelengths"])
         alone.append(srv.wait(jid, systems[j["system"]].n_faces))
     srv.close()
-    # in the mix: eight lanes, the probes interleaved with other jobs, all submitted at once
+    # in the mix: up to eight jobs in flight, the probes among other jobs, all submitted at once
     srv = serve.Server(lanes=8)
     ids = []
     for k, j in enumerate(jobs[:30]):
