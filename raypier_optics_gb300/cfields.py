@@ -52,6 +52,7 @@ class GaussianModes:
         self.ctx = _ctx or runtime.get_context()
         if _handle is not None:
             self.handle = _handle
+            self.ctx.attach()
             return
         recs = rays.copy_as_array() if hasattr(rays, "copy_as_array") else np.ascontiguousarray(rays)
         recs = np.ascontiguousarray(recs)
@@ -65,6 +66,7 @@ class GaussianModes:
                                                    wl.ctypes.data if wl.size else None, wl.shape[0],
                                                    ctypes.byref(h)), "rp_field_create")
         self.handle = h
+        self.ctx.attach()
 
     @classmethod
     def from_gausslets(cls, dev_gausslets, wavelengths, blending=1.0):
@@ -124,6 +126,7 @@ class GaussianModes:
         if getattr(self, "handle", None):
             self.ctx.lib.rp_field_destroy(self.handle)
             self.handle = None
+            self.ctx.detach()
 
     def __del__(self):
         try:

@@ -1253,24 +1253,62 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         const int nmask = nf < 64 ? nf : 64;
         const float lim0 = max_len * 1.000001f + 1e-4f;
         unsigned long long cand = 0;
+        // the three nearest box entries, in order, kept in registers while the
+        // boxes are entered: most rays test one to three faces, so the
+        // selection below rarely has to scan the candidates again
+        const float INF = __int_as_float(0x7f800000);
+        float q0 = INF, q1 = INF, q2 = INF;
+        int f0 = -1, f1 = -1, f2 = -1;
         for (int f = 0; f < nmask; f++) {
-            float te = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+            const float te = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
             if constexpr (TB) tb[f * RP_BLOCK] = te;
-            if (te <= lim0) cand |= 1ull << f;
+            if (te <= lim0) {
+                cand |= 1ull << f;
+                if (te < q2) {
+                    if (te < q1) {
+                        q2 = q1;
+                        f2 = f1;
+                        if (te < q0) {
+                            q1 = q0;
+                            f1 = f0;
+                            q0 = te;
+                            f0 = f;
+                        } else {
+                            q1 = te;
+                            f1 = f;
+                        }
+                    } else {
+                        q2 = te;
+                        f2 = f;
+                    }
+                }
+            }
         }
         while (cand) {
-            float tsel = __int_as_float(0x7f800000);
+            float tsel = INF;
             int sel = -1;
-            for (unsigned long long m = cand; m; m &= m - 1) {
-                int f = __ffsll((long long)m) - 1;
-                float tf;
-                if constexpr (TB)
-                    tf = tb[f * RP_BLOCK];
-                else
-                    tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                if (tf < tsel) {
-                    tsel = tf;
-                    sel = f;
+            if (f0 >= 0) {
+                // the front of the register queue: no candidate left in
+                // `cand` enters its box before it
+                tsel = q0;
+                sel = f0;
+                q0 = q1;
+                f0 = f1;
+                q1 = q2;
+                f1 = f2;
+                f2 = -1;
+            } else {
+                for (unsigned long long m = cand; m; m &= m - 1) {
+                    int f = __ffsll((long long)m) - 1;
+                    float tf;
+                    if constexpr (TB)
+                        tf = tb[f * RP_BLOCK];
+                    else
+                        tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+                    if (tf < tsel) {
+                        tsel = tf;
+                        sel = f;
+                    }
                 }
             }
             // boxes entered beyond the nearest FP32 candidate (with a

@@ -43,6 +43,7 @@ class Lens:
         _native.check(self.lib.rp_lens_create(self.ctx.handle, ctypes.byref(desc), self.n_rays, ctypes.byref(h)),
                       "rp_lens_create")
         self.handle = h
+        self.ctx.attach()
         self.n_params = 5 * self.n_surfaces
 
     def forward(self, params) -> tuple[float, int]:
@@ -74,6 +75,7 @@ class Lens:
         if getattr(self, "handle", None):
             self.lib.rp_lens_destroy(self.handle)
             self.handle = None
+            self.ctx.detach()
         if getattr(self, "rays", None) is not None:
             self.rays.free()
             self.rays = None

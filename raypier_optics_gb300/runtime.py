@@ -17,14 +17,30 @@ _lock = threading.Lock()
 
 
 class Context:
-    """One CUDA device, one stream, one device-memory budget (rp_ctx)."""
+    """One CUDA device, one stream, one device-memory budget (rp_ctx).
+
+    Buffers, scenes, fields and lenses made on a context hold it (``attach``)
+    until they are freed (``detach``).  The native context is destroyed only
+    once none is left: at interpreter exit, objects reachable only from a
+    reference cycle (a script's globals) are finalised in no fixed order, so
+    the context's own finaliser may run before theirs."""
 
     def __init__(self, device: int = 0, hbm_budget: int = 0):
         self.lib = _native.load()
         self.device = device
+        self._live = 0
+        self._close_pending = False
         h = ctypes.c_void_p()
         _native.check(self.lib.rp_ctx_create(device, hbm_budget, ctypes.byref(h)), "rp_ctx_create")
         self.handle = h
+
+    def attach(self):
+        self._live += 1
+
+    def detach(self):
+        self._live -= 1
+        if self._live <= 0 and self._close_pending:
+            self.close()
 
     def synchronize(self):
         _native.check(self.lib.rp_ctx_synchronize(self.handle), "rp_ctx_synchronize")
@@ -35,9 +51,14 @@ class Context:
         return v.value
 
     def close(self):
+        """Destroys the native context, at once if nothing made on it is
+        alive, else when the last such object is freed."""
         if getattr(self, "handle", None):
             for scene in self.__dict__.pop("_scenes", {}).values():
                 scene.free()
+            if self._live > 0:
+                self._close_pending = True
+                return
             self.lib.rp_ctx_destroy(self.handle)
             self.handle = None
 
@@ -67,6 +88,7 @@ class DeviceGausslets:
         h = ctypes.c_void_p()
         _native.check(self.lib.rp_gausslets_alloc(ctx.handle, int(capacity), ctypes.byref(h)), "rp_gausslets_alloc")
         self.handle = h
+        ctx.attach()
 
     def count(self) -> int:
         v = ctypes.c_uint64()
@@ -86,6 +108,7 @@ class DeviceGausslets:
         if getattr(self, "handle", None):
             self.lib.rp_gausslets_free(self.handle)
             self.handle = None
+            self.ctx.detach()
 
     def __del__(self):
         try:
@@ -105,6 +128,7 @@ class DeviceRays:
             _native.check(self.lib.rp_rays_alloc(ctx.handle, int(capacity), ctypes.byref(h)), "rp_rays_alloc")
             handle = h
         self.handle = handle
+        ctx.attach()
 
     def count(self) -> int:
         v = ctypes.c_uint64()
@@ -134,6 +158,7 @@ class DeviceRays:
         if getattr(self, "handle", None):
             self.lib.rp_rays_free(self.handle)
             self.handle = None
+            self.ctx.detach()
 
     def __del__(self):
         try:
@@ -157,6 +182,7 @@ class DeviceScene:
                                                wl.shape[0], ctypes.byref(h)), "rp_scene_create")
         self.handle = h
         self.counts_pending = False
+        ctx.attach()
 
     def face_counts(self, reset: bool = True) -> np.ndarray:
         n = self.tables.n_faces
@@ -172,6 +198,7 @@ class DeviceScene:
         if getattr(self, "handle", None):
             self.lib.rp_scene_destroy(self.handle)
             self.handle = None
+            self.ctx.detach()
 
     def __del__(self):
         try:
