@@ -332,10 +332,29 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
             }
         }
     }
+    // the mixed path's FP32 tables of the distortions whose programs replay
+    // on polynomials (rp_zkprog.h)
+    std::vector<int> zk32_off((size_t)d->n_distortions + 1, -1);
+    std::vector<double> zk64;
+    std::vector<zkp::Table> ztab((size_t)d->n_distortions);
+    for (int q = 0; q < d->n_distortions; q++) {
+        const rp_distortion &dq = d->distortions[q];
+        if (zk_off[2 * q] < 0 || zk_off[2 * q + 1] < 0) continue;
+        const short *pz = zk_prog.data() + zk_off[2 * q], *pg = zk_prog.data() + zk_off[2 * q + 1];
+        const std::vector<short> vz(pz, pz + 3 + pz[0] * RP_ZKOP_WORDS + pz[2]);
+        const std::vector<short> vg(pg, pg + 3 + pg[0] * RP_ZKOP_WORDS + pg[2]);
+        if (!zkp::build(dq.n_coefs, dq.unit_radius, d->aux + dq.aux, vz, vg, ztab[(size_t)q])) continue;
+        zk32_off[(size_t)q] = (int)zk64.size();
+        zkp::pack(ztab[(size_t)q], zk64);
+    }
+    const std::vector<float> zk32(zk64.begin(), zk64.end());
     size_t o_zkoff = o_bnd + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
     size_t o_zkprog = o_zkoff + align256(sizeof(int) * zk_off.size());
     size_t o_fl = o_zkprog + align256(sizeof(short) * (zk_prog.size() + 1));
-    size_t total = o_fl + align256(sizeof(short) * (size_t)(d->n_faces + 1));
+    size_t o_zk32off = o_fl + align256(sizeof(short) * (size_t)(d->n_faces + 1));
+    size_t o_zk32 = o_zk32off + align256(sizeof(int) * zk32_off.size());
+    size_t o_zk64 = o_zk32 + align256(sizeof(float) * (zk32.size() + 1));
+    size_t total = o_zk64 + align256(sizeof(double) * (zk64.size() + 1));
     // owning list of each traced face (kernels that read the tables from global memory)
     std::vector<short> face_list((size_t)d->n_faces + 1, (short)-1);
     for (int l = 0; l < d->n_lists; l++)
@@ -368,6 +387,9 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
             face_world_box(d, d->lists[l], d->faces[f], &bounds[(size_t)f * 8]);
         }
     UP(o_bnd, bounds.data(), sizeof(float) * 8 * (size_t)d->n_faces);
+    UP(o_zk32off, zk32_off.data(), sizeof(int) * zk32_off.size());
+    UP(o_zk32, zk32.data(), sizeof(float) * zk32.size());
+    UP(o_zk64, zk64.data(), sizeof(double) * zk64.size());
     UP(o_zkoff, zk_off.data(), sizeof(int) * zk_off.size());
     UP(o_zkprog, zk_prog.data(), sizeof(short) * zk_prog.size());
     UP(o_fl, face_list.data(), sizeof(short) * (size_t)d->n_faces);
@@ -386,6 +408,9 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     S.face_list = (const short *)(b + o_fl);
     S.zk_off = (const int *)(b + o_zkoff);
     S.zk_prog = (const short *)(b + o_zkprog);
+    S.zk32_off = (const int *)(b + o_zk32off);
+    S.zk32 = (const float *)(b + o_zk32);
+    S.zk64 = (const double *)(b + o_zk64);
     S.n_wl = n_wl;
     S.wl = (const double *)(b + o_wl);
     S.n_lists = d->n_lists;

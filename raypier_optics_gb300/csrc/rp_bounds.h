@@ -290,6 +290,8 @@ inline bool face_local_box(const rp_scene_desc *d, const rp_face &f, double lo[3
 // list's frame, converged or not (cfaces.pyx:2372-2407) -- has local (x, y)
 // inside the shape, so a ray whose line never passes over that rectangle
 // cannot hit it (distortion_line_misses).
+inline void world_from_local(const rp_facelist &L, const double lo[3], const double hi[3], float out[8]);
+
 inline void face_world_box(const rp_scene_desc *d, const rp_facelist &L, const rp_face &f, float out[8]) {
     double lo[3], hi[3];
     out[6] = 0.0f;
@@ -311,6 +313,12 @@ inline void face_world_box(const rp_scene_desc *d, const rp_facelist &L, const r
         return;
     }
     if (!face_local_box(d, f, lo, hi)) return;
+    world_from_local(L, lo, hi, out);
+}
+
+// The world box of a local box (its eight corners through the list's
+// transform), padded as above, with out[6] = 1.
+inline void world_from_local(const rp_facelist &L, const double lo[3], const double hi[3], float out[8]) {
     double w0[3] = {INFINITY, INFINITY, INFINITY}, w1[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int c = 0; c < 8; c++) {
         double q[3] = {(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]};

@@ -25,6 +25,9 @@ struct DevScene {
     const short *face_list;  // [n_faces]: owning face list of each traced face
     const short *zk_prog;    // compiled Zernike programs (rp_zkprog.h), or null
     const int *zk_off;       // [n_dists][2]: offsets of the z and z-gradient programs in zk_prog, -1 for none
+    const float *zk32;       // the mixed path's polynomial tables of the distortions (rp_zkprog.h, zkp), FP32
+    const double *zk64;      // the same tables in FP64, at the same word offsets
+    const int *zk32_off;     // [n_dists]: offset of a distortion's table in zk32 / zk64, -1 for none
     long long n_wl;
     int n_lists, n_faces, n_recs, n_mats, n_shapes, n_dists;
 };

@@ -221,7 +221,9 @@ struct MxFace {
     float rq_hi, rq_lo;  // the quadric's Rq as float-float (sphere: -curvature; conic, asphere: -p[0])
     float ic_hi, ic_lo;  // a sphere's 1 / curvature as float-float (its unit normal is (p - centre) / c)
     float tmin;
-    float tol;  // Face.tolerance (a distance) in FP32
+    float tol;   // Face.tolerance (a distance) in FP32
+    float btol;  // DistortionFace: its base face's tolerance (a fraction of the segment)
+    int spec;    // 1: the face is tested here (face_t32), 0: by the FP64 path
 };
 
 __host__ __device__ __forceinline__ size_t mx_tables_bytes(int n_lists, int n_faces) {
@@ -244,6 +246,131 @@ __device__ __forceinline__ int vertex_param(int type) {
 
 // Fills the tables from the FP64 tables in global memory (the shared copies of
 // those are not complete until the caller's next barrier).
+// A DistortionFace the mixed path tests itself: a ShapedPlanarFace base and a
+// distortion with an FP32 table (or the closed-form J7 test distortion); the
+// scene set-up makes the same test when it boxes the face for this path.
+__device__ __forceinline__ bool mx_distortion_ok(const DevScene &S, const rp_face &F) {
+    if (F.base < 0 || F.base >= S.n_recs || F.distortion < 0 || F.distortion >= S.n_dists) return false;
+    if (S.faces[F.base].type != RP_FACE_SHAPED_PLANAR) return false;
+    const rp_distortion &D = S.dists[F.distortion];
+    return D.type == RP_DIST_SIMPLE_J7 || (S.zk32_off && S.zk32_off[F.distortion] >= 0);
+}
+
+__device__ __forceinline__ float zk_horner(const float *c, int n, float r) {
+    float v = c[n - 1];
+    for (int k = n - 2; k >= 0; k--) v = fmaf(v, r, c[k]);
+    return v;
+}
+
+// A distortion at local (x, y) in FP32: z as ZernikeDistortion.z_offset_c
+// (cdistortions.pyx:416-450), or with grad (dz/dx, dz/dy, z) as
+// z_offset_and_gradient_c (456-514); SimpleTestZernikeJ7 in closed form
+// (48-81).  Zernike distortions use their polynomial table (the groups in
+// ascending |m|: cos / sin of m theta step up by the Chebyshev recurrence).
+// The distortion is a small height (N(0, 0.5 um) coefficients on the
+// clutter workload), so FP32 resolves it to far below a picometre.
+__device__ __noinline__ void zk_eval32(const DevScene &S, int dist, float x, float y, bool grad, float &zx, float &zy,
+                                       float &z) {
+    const rp_distortion &D = S.dists[dist];
+    zx = 0.0f;
+    zy = 0.0f;
+    z = 0.0f;
+    if (D.type == RP_DIST_SIMPLE_J7) {
+        const float R = f_of_d(D.unit_radius), a = 2.8284271247461903f * f_of_d(D.amplitude);  // sqrt(8) A
+        x /= R;
+        y /= R;
+        z = a * (3.0f * (x * x + y * y) - 2.0f) * y;
+        zx = a * 6.0f * x * y / R;
+        zy = a * (3.0f * x * x + 9.0f * y * y - 2.0f) / R;
+        return;
+    }
+    const float *T = S.zk32 + S.zk32_off[dist];
+    const int ng = (int)T[0], st = (int)T[1];
+    const float iur = T[3];
+    x *= iur;
+    y *= iur;
+    const float r = sqrtf(x * x + y * y);
+    float ct, sn;
+    if (r > 0.0f) {
+        ct = x / r;
+        sn = y / r;
+    } else {
+        sincosf(atan2f(y, x), &sn, &ct);  // the reference's atan2 of signed zeros
+    }
+    float cp = ct, sp = -sn, cc = 1.0f, sc = 0.0f;  // cos / sin of (k - 1) theta and k theta
+    int k = 0;
+    const float *g = T + 4;
+    for (int i = 0; i < ng; i++, g += 4 + 4 * st) {
+        const int m = (int)g[0], kind = (int)g[1];
+        for (; k < m; k++) {
+            const float cn = 2.0f * ct * cc - cp, sn2 = 2.0f * ct * sc - sp;
+            cp = cc;
+            sp = sc;
+            cc = cn;
+            sc = sn2;
+        }
+        const float A = kind ? sc : cc;                            // cos(m theta) or sin(|m| theta)
+        const float Ad = kind ? (float)m * cc : -(float)m * sc;   // its derivative in theta
+        const float *P = g + 4;
+        if (!grad) {
+            z = fmaf(zk_horner(P, st, r), A, z);
+            continue;
+        }
+        const float G = zk_horner(P + st, st, r), Q = zk_horner(P + 2 * st, st, r), W = zk_horner(P + 3 * st, st, r);
+        z = fmaf(G, A, z);
+        zx += Q * ct * A - W * sn * Ad;
+        zy += Q * sn * A + W * ct * Ad;
+    }
+    zx *= iur;
+    zy *= iur;
+}
+
+// zk_eval32 in FP64 over the FP64 tables (Zernike distortions with a table).
+__device__ void zk_eval64(const DevScene &S, int dist, double x, double y, bool grad, double &zx, double &zy,
+                          double &z) {
+    zx = 0.0;
+    zy = 0.0;
+    z = 0.0;
+    const double *T = S.zk64 + S.zk32_off[dist];
+    const int ng = (int)T[0], st = (int)T[1];
+    const double iur = T[3];
+    x *= iur;
+    y *= iur;
+    const double r = sqrt(x * x + y * y);
+    double ct, sn;
+    polar_cs(x, y, r, ct, sn);
+    double cp = ct, sp = -sn, cc = 1.0, sc = 0.0;
+    int k = 0;
+    const double *g = T + 4;
+    for (int i = 0; i < ng; i++, g += 4 + 4 * st) {
+        const int m = (int)g[0], kind = (int)g[1];
+        for (; k < m; k++) {
+            const double cn = 2.0 * ct * cc - cp, sn2 = 2.0 * ct * sc - sp;
+            cp = cc;
+            sp = sc;
+            cc = cn;
+            sc = sn2;
+        }
+        const double A = kind ? sc : cc, Ad = kind ? (double)m * cc : -(double)m * sc;
+        const double *P = g + 4;
+        auto horner = [&](const double *c) {
+            double v = c[st - 1];
+            for (int q = st - 2; q >= 0; q--) v = fma(v, r, c[q]);
+            return v;
+        };
+        if (!grad) {
+            z += horner(P) * A;
+            continue;
+        }
+        const double G = horner(P + st), Q = horner(P + 2 * st), W = horner(P + 3 * st);
+        z += G * A;
+        zx += Q * ct * A - W * sn * Ad;
+        zy += Q * sn * A + W * ct * Ad;
+    }
+    zx *= iur;
+    zy *= iur;
+}
+
 __device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace *mf, float max_len) {
     for (int l = threadIdx.x; l < A.S.n_lists; l += blockDim.x) {
         const rp_facelist &L = A.S.lists[l];
@@ -274,6 +401,14 @@ __device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace
         for (int k = 0; k < RP_FACE_NPARAM; k++) o.p[k] = f_of_d(F.p[k]);
         int vp = vertex_param(F.type);
         ff z = vp >= 0 ? ff_of_d(F.p[vp]) : ffm(0.0f, 0.0f);
+        o.spec = vp >= 0 ? 1 : 0;
+        o.btol = 0.0f;
+        if (F.type == RP_FACE_DISTORTION && mx_distortion_ok(A.S, F)) {
+            const rp_face &Bf = A.S.faces[F.base];
+            z = ff_of_d(Bf.p[0]);  // the ShapedPlanarFace base's z_height
+            o.btol = f_of_d(Bf.tolerance);
+            o.spec = 1;
+        }
         o.zv_hi = z.hi;
         o.zv_lo = z.lo;
         double rq = 0.0;
@@ -467,12 +602,106 @@ __device__ __forceinline__ float asph_residual_ff(const MxFace &M, ff Rq, float 
     return ff_sub(ff_add_f(conic, poly), Z).hi;
 }
 
+// DistortionFace.intersect_c (cfaces.pyx:2341-2407) over a ShapedPlanarFace
+// base z = zb, after the plain path's exact cull of lines that never pass
+// over the shape (box: the face's entry in S.bounds).  The base plane's hit
+// is exact in float-float (tb, distance ab); the points the reference visits
+// lie on the ray a distance del from it -- for a hit on the surface a small
+// one, the distortion's height over the slope -- so the iteration runs in
+// FP32 on del: the first estimate from the tangent plane at the distorted
+// point above the base hit, then per step the base hit of the ray shifted
+// down by z_offset, the tangent plane there and its ray distance, until two
+// estimates agree within the face's accuracy, the reference's sequence of
+// points and tests.  The hit is tb + del / |D| in float-float (*exact set).
+// A shifted ray that misses the base, 20 steps without agreement, or an
+// agreement away from the surface set fb: the FP64 path then decides.
+__device__ __noinline__ float distortion_t32(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R, float tmax,
+                                float dl, const float *box, unsigned *err, ff *tff, bool *exact, bool &fb) {
+    // the exact cull of the plain path (distortion_line_misses), in FP32 on
+    // its padded rectangle: a line that never passes over it cannot hit
+    if (box[6] == 2.0f) {
+        const float px = R.px.hi, py = R.py.hi, vx = R.dx.hi, vy = R.dy.hi;
+        if (vx == 0.0f && vy == 0.0f) {
+            if (px < box[0] || px > box[1] || py < box[2] || py > box[3]) return MX_MISS_T;
+        } else {
+            const float s00 = vx * (box[2] - py) - vy * (box[0] - px), s01 = vx * (box[3] - py) - vy * (box[0] - px);
+            const float s10 = vx * (box[2] - py) - vy * (box[1] - px), s11 = vx * (box[3] - py) - vy * (box[1] - px);
+            if ((s00 > 0.0f && s01 > 0.0f && s10 > 0.0f && s11 > 0.0f) ||
+                (s00 < 0.0f && s01 < 0.0f && s10 < 0.0f && s11 < 0.0f))
+                return MX_MISS_T;
+        }
+    }
+    const ff zb = ffm(M.zv_hi, M.zv_lo);
+    // ShapedPlanarFace.intersect_c, is_base_ray 0 (cfaces.pyx:213-221): h in [tolerance, 1]
+    const ff tb = ff_div(ff_sub(zb, R.pz), R.dz);
+    const float h = tb.hi / tmax;
+    if (!(h >= M.btol) || h > 1.0f) return MX_MISS_T;
+    const float seg = tmax * dl;  // the segment's length (h of intersect_c)
+    const float ab = tb.hi * dl;  // a2: the base hit's distance
+    if (ab > seg || ab < M.tol) return MX_MISS_T;  // cfaces.pyx:2355
+    const float ux = R.dx.hi / dl, uy = R.dy.hi / dl, uz = R.dz.hi / dl;
+    const float xb = ff_add(R.px, ff_mul(tb, R.dx)).hi, yb = ff_add(R.py, ff_mul(tb, R.dy)).hi;
+    float gx, gy, gz;
+    zk_eval32(S, F.distortion, xb, yb, true, gx, gy, gz);
+    // the tangent plane at the distorted point, normal (-gx, -gy, 1): a1 - ab
+    float del = gz / (uz - gx * ux - gy * uy);
+    if (ab + del < fabsf(gz)) return MX_MISS_T;  // cfaces.pyx:2375-2377
+    const float acc = M.p[0];                    // DistortionFace.accuracy
+    float dprev = 0.0f, x = xb, y = yb;
+    bool conv = false;
+    for (int it = 0; it < 20; it++) {
+        x = fmaf(ux, del, xb);  // the ray point at a1
+        y = fmaf(uy, del, yb);
+        if (fabsf(del - dprev) < acc) {
+            conv = true;
+            break;
+        }
+        float zs, wx, wy;
+        zk_eval32(S, F.distortion, x, y, false, wx, wy, zs);
+        const float d2 = zs / uz;  // the base hit of the ray shifted by -z_offset
+        const float h2 = (ab + d2) / seg;
+        if (!(h2 >= M.btol) || h2 > 1.0f) {
+            fb = true;
+            return MX_MISS_T;
+        }
+        x = fmaf(ux, d2, xb);
+        y = fmaf(uy, d2, yb);
+        zk_eval32(S, F.distortion, x, y, true, gx, gy, gz);
+        const float dnew = (gz - d2 * (gx * ux + gy * uy)) / (uz - gx * ux - gy * uy);
+        dprev = del;
+        del = dnew;
+    }
+    if (!conv || !isfinite(del)) {
+        fb = true;
+        return MX_MISS_T;
+    }
+    // A converged estimate lies on the distorted surface.  The reference's
+    // iteration can also settle where no surface is: a base hit far outside
+    // the face, where the polynomials are large, whose tangent plane meets
+    // the ray far from the plane; FP32 cannot follow it there (del is then
+    // tens of millimetres), so the FP64 path decides such a ray.
+    {
+        float zs, wx, wy;
+        zk_eval32(S, F.distortion, x, y, false, wx, wy, zs);
+        if (!(fabsf(uz * del - zs) < 1e-3f)) {
+            fb = true;
+            return MX_MISS_T;
+        }
+    }
+    if (!shape_in_f(S, F.shape, x, y, err)) return MX_MISS_T;  // cfaces.pyx:2402
+    const ff t = ff_add_f(tb, del / dl);
+    *tff = t;
+    *exact = true;
+    return t.hi;
+}
+
 // Phase one of a face test: the FP32 ray parameter of face F's hit (hit =
 // P + t Dl), with bounds and aperture tested at the FP32 hit point, or
 // MX_MISS_T; `fb` is set for face types left to the FP64 path.  A plane's
 // parameter costs one float-float division, so it is returned exactly in *tff
 // (*exact set); curved faces are refined by face_refine only if they win.
-__device__ float face_t32(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R, float tmax,
+template <bool DIST>
+__device__ float face_t32(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R, float tmax, float dl,
                           unsigned *err, ff *tff, bool *exact, bool &fb) {
     fb = false;
     *exact = false;
@@ -588,6 +817,12 @@ __device__ float face_t32(const DevScene &S, const rp_face &F, const MxFace &M, 
             if (!shape_in_f(S, F.shape, fmaf(t, dx, px), fmaf(t, dy, py), err)) return MX_MISS_T;
             return t;
         }
+        case RP_FACE_DISTORTION:  // (only scenes that also carry the FP64 path specialise it)
+            if constexpr (DIST)
+                if (M.spec) return distortion_t32(S, F, M, R, tmax, dl, S.bounds + 8 * (&F - S.faces), err, tff,
+                                                  exact, fb);
+            fb = true;
+            return MX_MISS_T;
         default: fb = true; return MX_MISS_T;
     }
 }
@@ -623,7 +858,9 @@ __device__ __forceinline__ ff face_refine(const rp_face &F, const MxFace &M, con
 // Unit normal of a specialised face in float-float at a hit given in vertex
 // coordinates (x, y and z relative to the vertex); false for faces left to the
 // FP64 path.  Face parameters are the FP32 copies.
-__device__ __forceinline__ bool face_normal_ff(const rp_face &F, const MxFace &M, ff x, ff y, ff z, ff3 &n) {
+template <bool DIST>
+__device__ __forceinline__ bool face_normal_ff(const DevScene &S, const rp_face &F, const MxFace &M, ff x, ff y, ff z,
+                                               ff3 &n) {
     const ff zero = ffm(0.0f, 0.0f);
     switch (F.type) {
         case RP_FACE_CIRCULAR: n = mkff3(zero, zero, ffm(F.invert_normals ? 1.0f : -1.0f, 0.0f)); return true;
@@ -660,6 +897,16 @@ __device__ __forceinline__ bool face_normal_ff(const rp_face &F, const MxFace &M
             df += 2.0f * inv + beta * r2 * inv * inv / (Rq * root);
             n = ff3_unit(mkff3(ff_mul_f(x, -df * sign), ff_mul_f(y, -df * sign), ffm(sign, 0.0f)));
             return true;
+        }
+        case RP_FACE_DISTORTION: {  // cfaces.pyx:2409-2422 over a plane: (-dz/dx, -dz/dy, 1) normalised
+            if constexpr (DIST) {
+                if (!M.spec) return false;
+                float gx, gy, gz;
+                zk_eval32(S, F.distortion, x.hi, y.hi, true, gx, gy, gz);
+                n = ff3_unit(mkff3(ffm(-gx, 0.0f), ffm(-gy, 0.0f), ffm(1.0f, 0.0f)));
+                return true;
+            }
+            return false;
         }
         default: return false;
     }
@@ -868,7 +1115,57 @@ struct Best {
 // kept out of line so that their registers and stack do not weigh on the
 // specialised path.
 
-// FP64 distance for a face type this kernel does not specialise.
+// DistortionFace.intersect_c in FP64 (distortion_isect, the same iteration
+// step for step) with the distortion from its FP64 polynomial table instead
+// of the reference's recursion: for the rays the FP32 iteration hands over
+// (those that wander where the polynomials are large), which then need no
+// workspace in local memory.
+__device__ __noinline__ double distortion_t64(const DevScene &S, const rp_face &f, v3 p1, v3 p2, unsigned *err) {
+    const rp_face &face = S.faces[f.base];
+    double a1, a2, h = sepv(p2, p1);
+    const double tolerance = f.p[0];
+    a2 = face_isect_base(S, face, p1, p2, 0, err);
+    if (a2 > h || a2 < f.tolerance) return RP_MISS;
+    const v3 d = subv(p2, p1);
+    v3 pt1 = addv(p1, mulvs(d, a2 / h));
+    double gx, gy, gz;
+    zk_eval64(S, f.distortion, pt1.x, pt1.y, true, gx, gy, gz);
+    v3 n = face_normal_base(S, face, pt1);
+    pt1.z += gz;
+    n.x /= n.z;
+    n.y /= n.z;
+    n.x -= gx;
+    n.y -= gy;
+    v3 o = subv(p1, pt1);
+    a1 = -h * dotv(o, n) / dotv(d, n);
+    if (a1 < fabs(gz)) return RP_MISS;
+    for (int i = 0; i < 20; i++) {
+        pt1 = addv(p1, mulvs(d, a1 / h));
+        if (fabs(a1 - a2) < tolerance) break;
+        double zs, wx, wy;
+        zk_eval64(S, f.distortion, pt1.x, pt1.y, false, wx, wy, zs);
+        v3 q1 = p1, q2 = p2;
+        q1.z -= zs;
+        q2.z -= zs;
+        a2 = face_isect_base(S, face, q1, q2, 0, err);
+        pt1 = addv(q1, mulvs(d, a2 / h));
+        n = face_normal_base(S, face, pt1);
+        zk_eval64(S, f.distortion, pt1.x, pt1.y, true, gx, gy, gz);
+        pt1.z += gz;
+        n.x /= n.z;
+        n.y /= n.z;
+        n.x -= gx;
+        n.y -= gy;
+        o = subv(p1, pt1);
+        a2 = a1;
+        a1 = -h * dotv(o, n) / dotv(d, n);
+    }
+    if (!shape_inside(S, f.shape, pt1.x, pt1.y, err)) return RP_MISS;
+    return a1;
+}
+
+// FP64 distance for a face type this kernel does not specialise (and for a
+// DistortionFace its FP32 iteration handed over).
 __device__ __forceinline__ double fallback_dist(const GenArgs &A, const DevScene &S, const rp_face &F, int f, int l,
                                                 unsigned long long i) {
     const rp_facelist &L = S.lists[l];
@@ -877,6 +1174,8 @@ __device__ __forceinline__ double fallback_dist(const GenArgs &A, const DevScene
     v3 pend = addv(o, mulvs(d, A.max_len));
     const v3 p1 = xform(L.inv_trans.m, L.inv_trans.t, o), p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
     if (distortion_line_misses(S.bounds + 8 * f, p1, p2)) return -1.0;  // cfaces.pyx NO_INTERSECTION
+    if (F.type == RP_FACE_DISTORTION && mx_distortion_ok(S, F) && S.dists[F.distortion].type == RP_DIST_ZERNIKE)
+        return distortion_t64(S, F, p1, p2, A.err);
     return face_isect(S, F, p1, p2, A.err);
 }
 
@@ -926,12 +1225,6 @@ __device__ __noinline__ int fallback_children(const GenArgs &A, const DevScene &
     return nc;
 }
 
-// Face types the specialised path handles (the rest go through the FP64 path).
-__device__ __forceinline__ bool face_specialised(int type) {
-    return type == RP_FACE_CIRCULAR || type == RP_FACE_RECTANGULAR || type == RP_FACE_SHAPED_PLANAR ||
-           type == RP_FACE_SPHERICAL || type == RP_FACE_SHAPED_SPHERICAL || type == RP_FACE_CONIC ||
-           type == RP_FACE_ASPHERIC;
-}
 
 // Keeps the hit if it is nearer than b (the reference's strict `dist < length`,
 // ties to the lower face index as in the oracle's order of evaluation).
@@ -960,10 +1253,12 @@ __device__ __forceinline__ void cand_clear(Cand &c) {
     c.tx = ffm(0.0f, 0.0f);
 }
 
-// Phase one of a specialised face test (the caller checks face_specialised):
+// Phase one of a specialised face test (the caller checks MxFace.spec):
 // keeps the two nearest candidates by FP32 distance (ties to the lower face
-// record, as the exact comparison does).
-__device__ __forceinline__ void try_face32(const DevScene &S, const MxList *ml, const MxFace *mf, int f, int l,
+// record, as the exact comparison does).  True when the face's FP32 test
+// could not decide (a DistortionFace's iteration that the FP64 path must run).
+template <bool DIST>
+__device__ __forceinline__ bool try_face32(const DevScene &S, const MxList *ml, const MxFace *mf, int f, int l,
                                            int &cur, LRay &R, const ff *O, const ff *D, float dl, float tmax,
                                            unsigned *err, Cand &c1, Cand &c2) {
     if (l != cur) {
@@ -972,10 +1267,11 @@ __device__ __forceinline__ void try_face32(const DevScene &S, const MxList *ml, 
     }
     bool fb, exact;
     ff tx;
-    const float t = face_t32(S, S.faces[f], mf[f], R, tmax, err, &tx, &exact, fb);
-    if (!(t >= 0.0f)) return;
+    const float t = face_t32<DIST>(S, S.faces[f], mf[f], R, tmax, dl, err, &tx, &exact, fb);
+    if (fb) return true;
+    if (!(t >= 0.0f)) return false;
     const float d = t * dl;
-    if (!(mf[f].tol < d)) return;
+    if (!(mf[f].tol < d)) return false;
     Cand c;
     c.d = d;
     c.t = t;
@@ -989,6 +1285,7 @@ __device__ __forceinline__ void try_face32(const DevScene &S, const MxList *ml, 
     } else if (d < c2.d || (d == c2.d && f < c2.face)) {
         c2 = c;
     }
+    return false;
 }
 
 // Phase two for one candidate: its float-float parameter (bounds and the
@@ -1235,12 +1532,13 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
     if (A.one_list >= 0) {
         // sequential trace: one face of one list (FaceList.intersect_one_face_c, ctracer.pyx:1861-1879)
         const int f = S.lists[A.one_list].first_face + A.one_face;
-        if (face_specialised(S.faces[f].type)) {
-            try_face32(S, ml, mf, f, A.one_list, cur, R, O, D, dl, max_len, A.err, c1, c2);
+        bool fp64 = !mf[f].spec;
+        if (!fp64) {
+            fp64 = try_face32<FB>(S, ml, mf, f, A.one_list, cur, R, O, D, dl, max_len, A.err, c1, c2);
             settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
-        } else if constexpr (FB) {
-            try_face_fp64(A, S, f, A.one_list, src, dlen, b);
         }
+        if constexpr (FB)
+            if (fp64) try_face_fp64(A, S, f, A.one_list, src, dlen, b);
     } else {
         // culled nearest-first search over the first 64 faces, then the rest in order
         const float dfx = D[0].hi, dfy = D[1].hi, dfz = D[2].hi;
@@ -1320,13 +1618,17 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
                 atomicOr(A.err, ERR_SHAPE_STACK);
                 break;
             }
-            if (face_specialised(S.faces[sel].type))
-                try_face32(S, ml, mf, sel, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
-            else
-                pend |= 1ull << sel;
+            // a face the FP32 test cannot decide goes to the FP64 faces below
+            // (a scene without FP64 faces has only faces the FP32 test decides)
+            if constexpr (FB) {
+                if (!mf[sel].spec || try_face32<FB>(S, ml, mf, sel, l, cur, R, O, D, dl, max_len, A.err, c1, c2))
+                    pend |= 1ull << sel;
+            } else {
+                try_face32<FB>(S, ml, mf, sel, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
+            }
         }
         for (int f = nmask; f < nf; f++) {
-            if (!face_specialised(S.faces[f].type)) continue;
+            if (!mf[f].spec) continue;
             if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > fmaf(c1.d, 1.000244140625f, 1e-3f))
                 continue;
             int l = S.face_list[f];
@@ -1334,7 +1636,9 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
                 atomicOr(A.err, ERR_SHAPE_STACK);
                 break;
             }
-            try_face32(S, ml, mf, f, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
+            const bool fp64 = try_face32<FB>(S, ml, mf, f, l, cur, R, O, D, dl, max_len, A.err, c1, c2);
+            if constexpr (FB)
+                if (fp64) try_face_fp64(A, S, f, l, src, dlen, b);
         }
         settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
         // the FP64 faces: the nearest hit does not depend on the order of
@@ -1349,7 +1653,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
                     tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
                 if (tf > b.len.hi * 1.000001f + 1e-4f) continue;
             } else {
-                if (face_specialised(S.faces[f].type)) continue;
+                if (mf[f].spec) continue;
                 if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f)
                     continue;
             }
@@ -1645,7 +1949,7 @@ __device__ __forceinline__ void material_mx(const GenArgs &A, const DevScene &S,
             ff_rotate(L, P, lp, true);
         }
         ff3 nn;
-        if (face_normal_ff(F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
+        if (face_normal_ff<FB>(S, F, M, lp[0], lp[1], ff_sub(lp[2], ffm(M.zv_hi, M.zv_lo)), nn)) {
             if (F.invert_normal) nn = ff3_neg(nn);
             if (!L.ident) {
                 ff v[3] = {nn.x, nn.y, nn.z}, w[3];
