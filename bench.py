@@ -96,6 +96,9 @@ def parse():
     ap.add_argument("--serving-baseline-jobs", type=int, default=500,
                     help="jobs of the same stream run one at a time through the plain FP64 path")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-lens leg (configuration 4)")
+    ap.add_argument("--no-clutter", action="store_true",
+                    help="skip the clutter-scene leg (configuration 3: mixed and plain FP64 on 1M rays)")
+    ap.add_argument("--clutter-rays", type=int, default=1 << 20, help="rays of the clutter-scene leg")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the Gausslet, sequential and E-field legs")
     return ap.parse_args()
@@ -389,6 +392,8 @@ def main():
     extra = {}
     if rank == 0 and world == 1 and not args.no_adjoint:
         extra["adjoint"] = adjoint_leg(ctx)
+    if rank == 0 and world == 1 and not args.no_clutter and args.workload != "config3":
+        extra["clutter"] = clutter_leg(ctx, args)
     if rank == 0 and world == 1 and not args.no_serving:
         extra["serving"] = serving_leg(args)
     if rank == 0 and world == 1 and not args.no_extras:
@@ -504,6 +509,63 @@ def serving_leg(args):
         b = serve.latency_summary(bres)
         b.update({"path": "plain FP64, one job at a time", "wall_s": bwall})
         out["plain_one_at_a_time_fp64"] = b
+    return out
+
+
+def clutter_leg(ctx, args):
+    """The 64-face clutter scene (configuration 3: Zernike-distorted planes,
+    polynomial faces, prisms, spheres, conic mirrors; 12 generations) on
+    args.clutter_rays rays, device-resident: the mixed and the plain FP64
+    path, one warm-up and two timed steps each (CUDA events on the library
+    stream), their index agreement and errors on a 4096-ray sample, and the
+    reference's own CPU code on a 2048-ray sample of the same rays."""
+    import types
+
+    import cpu_bench
+    from raypier_optics_gb300 import _native, cdistortions, cfaces, cmaterials, cshapes, ctracer, runtime, scene
+    from raypier_optics_gb300 import workloads as W
+    ns = types.SimpleNamespace(ctracer=ctracer, cfaces=cfaces, cmaterials=cmaterials, cshapes=cshapes,
+                               cdistortions=cdistortions)
+    lib = ctx.lib
+    P = W.CONFIG3
+    n = args.clutter_rays
+    rays, wl = W.config3_rays(ctracer.ray_dtype, n)
+    lists = W.build_scene(W.config3_spec(), ns)
+    for i, f in enumerate([f for fl in lists for f in fl.faces]):
+        f.idx = i
+        f.update()
+    ds = runtime.DeviceScene(ctx, scene.compile_scene(lists), wl)
+    g0 = runtime.DeviceRays(ctx, n)
+    g0.upload(np.ascontiguousarray(rays))
+    rl = P["recursion_limit"]
+    max_gens = rl + 1
+
+    def step(st, fl):
+        gens = (ctypes.c_void_p * max_gens)()
+        gens[0] = g0.handle
+        ng = ctypes.c_int32(0)
+        _native.check(lib.rp_trace_rays(ctx.handle, ds.handle, gens, max_gens, rl, ctypes.c_float(P["max_length"]),
+                                        fl, P["e2_terminate"], ctypes.byref(ng), ctypes.byref(st)), "rp_trace_rays")
+        for g in range(1, max_gens):
+            if gens[g]:
+                lib.rp_rays_free(ctypes.c_void_p(gens[g]))
+
+    out = {"workload": f"config3: {n} rays, 64 faces, {rl} generations, |E|^2<{P['e2_terminate']} termination",
+           "timing": "CUDA events on the library stream, 1 warm-up + 2 timed steps per path"}
+    for fl, name in ((1, "mixed"), (0, "plain_fp64")):
+        step(_native.Stats(), fl)
+        st = _native.Stats()
+        for _ in range(2):
+            step(st, fl)
+        out[name] = {"value": st.rays_in / (st.device_ms / 1000.0), "unit": UNIT, "ms_per_step": st.device_ms / 2,
+                     "segments_per_step": st.rays_in / 2}
+    out["speedup_mixed_vs_plain_fp64"] = out["mixed"]["value"] / out["plain_fp64"]["value"]
+    g0.free()
+    ds.free()
+    out["precision_mixed_vs_plain_fp64"] = precision_sample(ctx, W.config3_spec(), rays, wl, P, False, 4096)
+    idx = np.linspace(0, n - 1, min(2048, n)).astype(np.int64)
+    out["cpu_reference"] = cpu_bench.time_cpu("config3", rays[idx], wl, False)
+    out["cpu_reference"]["sample"] = f"{len(idx)} rays spread over the {n}-ray workload, all generations"
     return out
 
 

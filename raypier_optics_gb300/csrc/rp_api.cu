@@ -299,7 +299,7 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
         int t = d->faces[f].type;
         if (t != RP_FACE_CIRCULAR && t != RP_FACE_RECTANGULAR && t != RP_FACE_SHAPED_PLANAR &&
             t != RP_FACE_SPHERICAL && t != RP_FACE_SHAPED_SPHERICAL && t != RP_FACE_CONIC && t != RP_FACE_ASPHERIC)
-            s->mixed_fallback = 1;
+            s->mixed_fallback = 1;  // (DistortionFace and ExtendedPolynomialFace run in that form's FP32 code)
     }
     for (int m = 0; m < d->n_materials; m++) {
         int t = d->materials[m].type;
@@ -348,13 +348,26 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
         zkp::pack(ztab[(size_t)q], zk64);
     }
     const std::vector<float> zk32(zk64.begin(), zk64.end());
+    // FP32 copies of the ExtendedPolynomialFace coefficient matrices
+    std::vector<int> ep32_off((size_t)d->n_face_records + 1, -1);
+    std::vector<float> ep32;
+    for (int r = 0; r < d->n_face_records; r++) {
+        const rp_face &F = d->faces[r];
+        if (F.type != RP_FACE_EXTPOLY) continue;
+        ep32_off[(size_t)r] = (int)ep32.size();
+        ep32.push_back((float)F.n_aux0);
+        ep32.push_back((float)F.n_aux1);
+        for (int k = 0; k < F.n_aux0 * F.n_aux1; k++) ep32.push_back((float)d->aux[F.aux + k]);
+    }
     size_t o_zkoff = o_bnd + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
     size_t o_zkprog = o_zkoff + align256(sizeof(int) * zk_off.size());
     size_t o_fl = o_zkprog + align256(sizeof(short) * (zk_prog.size() + 1));
     size_t o_zk32off = o_fl + align256(sizeof(short) * (size_t)(d->n_faces + 1));
     size_t o_zk32 = o_zk32off + align256(sizeof(int) * zk32_off.size());
     size_t o_zk64 = o_zk32 + align256(sizeof(float) * (zk32.size() + 1));
-    size_t total = o_zk64 + align256(sizeof(double) * (zk64.size() + 1));
+    size_t o_ep32off = o_zk64 + align256(sizeof(double) * (zk64.size() + 1));
+    size_t o_ep32 = o_ep32off + align256(sizeof(int) * ep32_off.size());
+    size_t total = o_ep32 + align256(sizeof(float) * (ep32.size() + 1));
     // owning list of each traced face (kernels that read the tables from global memory)
     std::vector<short> face_list((size_t)d->n_faces + 1, (short)-1);
     for (int l = 0; l < d->n_lists; l++)
@@ -390,6 +403,8 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     UP(o_zk32off, zk32_off.data(), sizeof(int) * zk32_off.size());
     UP(o_zk32, zk32.data(), sizeof(float) * zk32.size());
     UP(o_zk64, zk64.data(), sizeof(double) * zk64.size());
+    UP(o_ep32off, ep32_off.data(), sizeof(int) * ep32_off.size());
+    UP(o_ep32, ep32.data(), sizeof(float) * ep32.size());
     UP(o_zkoff, zk_off.data(), sizeof(int) * zk_off.size());
     UP(o_zkprog, zk_prog.data(), sizeof(short) * zk_prog.size());
     UP(o_fl, face_list.data(), sizeof(short) * (size_t)d->n_faces);
@@ -411,6 +426,8 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     S.zk32_off = (const int *)(b + o_zk32off);
     S.zk32 = (const float *)(b + o_zk32);
     S.zk64 = (const double *)(b + o_zk64);
+    S.ep32_off = (const int *)(b + o_ep32off);
+    S.ep32 = (const float *)(b + o_ep32);
     S.n_wl = n_wl;
     S.wl = (const double *)(b + o_wl);
     S.n_lists = d->n_lists;

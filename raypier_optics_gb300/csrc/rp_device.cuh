@@ -28,6 +28,8 @@ struct DevScene {
     const float *zk32;       // the mixed path's polynomial tables of the distortions (rp_zkprog.h, zkp), FP32
     const double *zk64;      // the same tables in FP64, at the same word offsets
     const int *zk32_off;     // [n_dists]: offset of a distortion's table in zk32 / zk64, -1 for none
+    const float *ep32;       // the mixed path's FP32 copies of the ExtendedPolynomialFace coefficient matrices
+    const int *ep32_off;     // [n_recs]: offset of a face record's matrix ([Nx, Ny, E...]) in ep32, -1 for none
     long long n_wl;
     int n_lists, n_faces, n_recs, n_mats, n_shapes, n_dists;
 };

@@ -240,12 +240,11 @@ __device__ __forceinline__ int vertex_param(int type) {
         case RP_FACE_SHAPED_SPHERICAL: return 1;
         case RP_FACE_CONIC: return 1;
         case RP_FACE_ASPHERIC: return 1;
+        case RP_FACE_EXTPOLY: return 3;
         default: return -1;
     }
 }
 
-// Fills the tables from the FP64 tables in global memory (the shared copies of
-// those are not complete until the caller's next barrier).
 // A DistortionFace the mixed path tests itself: a ShapedPlanarFace base and a
 // distortion with an FP32 table (or the closed-form J7 test distortion); the
 // scene set-up makes the same test when it boxes the face for this path.
@@ -371,6 +370,8 @@ __device__ void zk_eval64(const DevScene &S, int dist, double x, double y, bool 
     zy *= iur;
 }
 
+// Fills the tables from the FP64 tables in global memory (the shared copies of
+// those are not complete until the caller's next barrier).
 __device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace *mf, float max_len) {
     for (int l = threadIdx.x; l < A.S.n_lists; l += blockDim.x) {
         const rp_facelist &L = A.S.lists[l];
@@ -415,6 +416,7 @@ __device__ __forceinline__ void stage_mixed(const GenArgs &A, MxList *ml, MxFace
         if (F.type == RP_FACE_SPHERICAL) rq = -F.p[1];
         else if (F.type == RP_FACE_SHAPED_SPHERICAL) rq = -F.p[0];
         else if (F.type == RP_FACE_CONIC || F.type == RP_FACE_ASPHERIC) rq = -F.p[0];
+        else if (F.type == RP_FACE_EXTPOLY) rq = F.p[0];  // extpoly_t.R (cfaces.pyx:2030)
         const ff r = ff_of_d(rq);
         o.rq_hi = r.hi;
         o.rq_lo = r.lo;
@@ -602,6 +604,112 @@ __device__ __forceinline__ float asph_residual_ff(const MxFace &M, ff Rq, float 
     return ff_sub(ff_add_f(conic, poly), Z).hi;
 }
 
+// intersect_conic (cfaces.pyx:1695-1747) in vertex coordinates, FP32: the
+// ray parameter (units of the direction d) of the quadric of vertex radius Rq
+// and beta = 1 + conic constant, the reference's choice of root by the sign
+// of Rq beta d_z; -tmax (its -1, a fraction of the segment) without a root.
+__device__ __forceinline__ float conic_root32(float Rq, float beta, float px, float py, float pz, float dx, float dy,
+                                              float dz, float tmax) {
+    const float b2 = beta * beta;
+    float A = b2 * dz * dz + beta * (dx * dx + dy * dy);
+    float B = -2.0f * Rq * beta * dz + 2.0f * beta * (px * dx + py * dy) + 2.0f * pz * b2 * dz;
+    float C = -2.0f * Rq * pz * beta + beta * (px * px + py * py) + pz * pz * b2;
+    float disc = B * B - 4.0f * A * C;
+    if (disc < 0.0f) return -tmax;
+    float sd = sqrtf(disc);
+    bool plus = Rq * beta * dz <= 0.0f;
+    if (A == 0.0f) return plus ? (-B + sd) / (2.0f * A) : (-B - sd) / (2.0f * A);
+    if (plus) return (B > 0.0f) ? (2.0f * C) / (-B - sd) : (-B + sd) / (2.0f * A);
+    return (B < 0.0f) ? (2.0f * C) / (-B + sd) : (-B - sd) / (2.0f * A);
+}
+
+// The 2D polynomial of an ExtendedPolynomialFace at normalised (xs, ys)
+// (cfaces.pyx:2066-2068) and its derivatives in xs and ys (2092-2100), in
+// FP32 from the face's table E = [Nx, Ny, E[0][0], E[0][1], ...].
+__device__ __forceinline__ void ep_eval32(const float *E, float xs, float ys, float &P, float &Px, float &Py) {
+    const int nx = (int)E[0], ny = (int)E[1];
+    const float *c = E + 2;
+    P = 0.0f;
+    Px = 0.0f;
+    Py = 0.0f;
+    for (int i = nx - 1; i >= 0; i--) {
+        // row i at ys and its derivative in ys
+        float q = 0.0f, qd = 0.0f;
+        for (int j = ny - 1; j >= 0; j--) {
+            qd = fmaf(qd, ys, q);
+            q = fmaf(q, ys, c[i * ny + j]);
+        }
+        Px = fmaf(Px, xs, P);
+        P = fmaf(P, xs, q);
+        Py = fmaf(Py, xs, qd);
+    }
+}
+
+// The extended polynomial's residual conic(r^2) + P(x, y) - z at a
+// float-float point in vertex coordinates (eval_extpoly_impf,
+// cfaces.pyx:2043-2070, relative to z_height): the conic part in
+// float-float, the polynomial part (a small height) in FP32; and its FP32
+// derivative along the ray direction d (eval_extpoly_grad, 2073-2104).
+__device__ __forceinline__ float ep_residual_ff(const float *E, ff Rq, float beta, float irho, ff X, ff Y, ff Z) {
+    const ff r2 = ff_add(ff_sqr(X), ff_sqr(Y));
+    const float k = beta / (Rq.hi * Rq.hi);
+    const ff root = ff_sqrt(ff_add_f(ff_neg(ff_mul_f(r2, k)), 1.0f));
+    const ff conic = ff_div(r2, ff_mul(Rq, ff_add_f(root, 1.0f)));
+    float P, Px, Py;
+    ep_eval32(E, X.hi * irho, Y.hi * irho, P, Px, Py);
+    return ff_sub(ff_add_f(conic, P), Z).hi;
+}
+__device__ __forceinline__ void ep_fg32(const float *E, float Rq, float beta, float irho, f3 u, float dx, float dy,
+                                        float dz, float &fv, float &g) {
+    const float r2 = u.x * u.x + u.y * u.y;
+    const float rt = sqrtf(1.0f - beta * r2 / (Rq * Rq));
+    const float denom = Rq * (rt + 1.0f);
+    const float nom = 2.0f * (dx * u.x + dy * u.y);
+    float P, Px, Py;
+    ep_eval32(E, u.x * irho, u.y * irho, P, Px, Py);
+    fv = r2 / denom + P - u.z;
+    g = nom / denom + beta * nom * r2 / (2.0f * Rq * rt * denom * denom) + (Px * dx + Py * dy) * irho - dz;
+}
+
+// ExtendedPolynomialFace.intersect_c (cfaces.pyx:2182-2234): the conic root,
+// then Newton on the residual in FP32 (in vertex coordinates), a miss when it
+// stops converging above the FP32 rounding of the residual or takes 100
+// steps; the winner is refined in float-float (face_refine).  Out of line, so
+// that scenes without such faces do not carry its registers.
+__device__ __noinline__ float extpoly_t32(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R,
+                                          float tmax, unsigned *err, bool &fb) {
+    const ff zv = ffm(M.zv_hi, M.zv_lo);
+    if (!S.ep32_off || S.ep32_off[&F - S.faces] < 0) {
+        fb = true;
+        return MX_MISS_T;
+    }
+    const float *E = S.ep32 + S.ep32_off[&F - S.faces];
+    const float Rq = M.p[0], beta = M.p[1], irho = 1.0f / M.p[2];
+    const float px = R.px.hi, py = R.py.hi, pz = ff_sub(R.pz, zv).hi;
+    const float dx = R.dx.hi, dy = R.dy.hi, dz = R.dz.hi;
+    float tf = conic_root32(Rq, beta, px, py, pz, dx, dy, dz, tmax);
+    float fv, g;
+    ep_fg32(E, Rq, beta, irho, mk3(fmaf(tf, dx, px), fmaf(tf, dy, py), fmaf(tf, dz, pz)), dx, dy, dz, fv, g);
+    float f_last = fv, step = -fv / g;
+    bool conv = false;
+    for (int it = 0; it < 100; it++) {
+        tf += step;
+        if (fabsf(step) <= 1e-5f * (1.0f + fabsf(tf))) {
+            conv = true;
+            break;
+        }
+        const f3 u = mk3(fmaf(tf, dx, px), fmaf(tf, dy, py), fmaf(tf, dz, pz));
+        ep_fg32(E, Rq, beta, irho, u, dx, dy, dz, fv, g);
+        if (fabsf(fv) > fabsf(f_last) && fabsf(fv) > 1e-6f * (1.0f + fabsf(u.z))) return MX_MISS_T;
+        f_last = fv;
+        step = -fv / g;
+    }
+    if (!conv || !isfinite(tf)) return MX_MISS_T;
+    if (!shape_in_f(S, F.shape, fmaf(tf, dx, px), fmaf(tf, dy, py), err)) return MX_MISS_T;
+    if (!(tf <= tmax) || !(tf >= M.tmin)) return MX_MISS_T;  // a1 > 1 or a1 < tolerance
+    return tf;
+}
+
 // DistortionFace.intersect_c (cfaces.pyx:2341-2407) over a ShapedPlanarFace
 // base z = zb, after the plain path's exact cull of lines that never pass
 // over the shape (box: the face's entry in S.bounds).  The base plane's hit
@@ -768,27 +876,11 @@ __device__ float face_t32(const DevScene &S, const rp_face &F, const MxFace &M, 
         }
         case RP_FACE_CONIC:
         case RP_FACE_ASPHERIC: {
-            // intersect_conic (cfaces.pyx:1695-1747) in vertex coordinates, the
-            // reference's choice of root by the sign of R beta d_z
             const float Rq = -M.p[0], beta = 1.0f + M.p[2];
             const float px = R.px.hi, py = R.py.hi;
             const float pz = ff_sub(R.pz, zv).hi;
             const float dx = R.dx.hi, dy = R.dy.hi, dz = R.dz.hi;
-            const float b2 = beta * beta;
-            float A = b2 * dz * dz + beta * (dx * dx + dy * dy);
-            float B = -2.0f * Rq * beta * dz + 2.0f * beta * (px * dx + py * dy) + 2.0f * pz * b2 * dz;
-            float C = -2.0f * Rq * pz * beta + beta * (px * px + py * py) + pz * pz * b2;
-            float disc = B * B - 4.0f * A * C;
-            float t;
-            if (disc < 0.0f) {
-                t = -tmax;  // intersect_conic's -1 (a fraction of the segment): the asphere starts from there
-            } else {
-                float sd = sqrtf(disc);
-                bool plus = Rq * beta * dz <= 0.0f;
-                if (A == 0.0f) t = plus ? (-B + sd) / (2.0f * A) : (-B - sd) / (2.0f * A);
-                else if (plus) t = (B > 0.0f) ? (2.0f * C) / (-B - sd) : (-B + sd) / (2.0f * A);
-                else t = (B < 0.0f) ? (2.0f * C) / (-B + sd) : (-B - sd) / (2.0f * A);
-            }
+            float t = conic_root32(Rq, beta, px, py, pz, dx, dy, dz, tmax);
             if (F.type == RP_FACE_CONIC) {
                 if (!(t <= tmax) || !(t >= M.tmin)) return MX_MISS_T;  // D < 0 gives -1: a miss
             } else {
@@ -817,6 +909,10 @@ __device__ float face_t32(const DevScene &S, const rp_face &F, const MxFace &M, 
             if (!shape_in_f(S, F.shape, fmaf(t, dx, px), fmaf(t, dy, py), err)) return MX_MISS_T;
             return t;
         }
+        case RP_FACE_EXTPOLY:  // (as the DistortionFace: scenes that have one carry the FP64 path)
+            if constexpr (DIST) return extpoly_t32(S, F, M, R, tmax, err, fb);
+            fb = true;
+            return MX_MISS_T;
         case RP_FACE_DISTORTION:  // (only scenes that also carry the FP64 path specialise it)
             if constexpr (DIST)
                 if (M.spec) return distortion_t32(S, F, M, R, tmax, dl, S.bounds + 8 * (&F - S.faces), err, tff,
@@ -827,16 +923,44 @@ __device__ float face_t32(const DevScene &S, const rp_face &F, const MxFace &M, 
     }
 }
 
+// An ExtendedPolynomialFace hit in float-float from its FP32 ray parameter:
+// Newton steps on the residual in float-float (ep_residual_ff).
+__device__ __noinline__ ff extpoly_refine(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R,
+                                          float t32) {
+    const ff zv = ffm(M.zv_hi, M.zv_lo);
+    const ff Rq = ffm(M.rq_hi, M.rq_lo);
+    const float *E = S.ep32 + S.ep32_off[&F - S.faces];
+    const float beta = M.p[1], irho = 1.0f / M.p[2];
+    ff tt = ffm(t32, 0.0f);
+    const float dx = R.dx.hi, dy = R.dy.hi, dz = R.dz.hi;
+    for (int it = 0; it < 2; it++) {
+        ff X, Y, Z;
+        vertex_point_ff(R, zv, tt, X, Y, Z);
+        float fv, g;
+        ep_fg32(E, Rq.hi, beta, irho, mk3(X.hi, Y.hi, Z.hi), dx, dy, dz, fv, g);
+        fv = ep_residual_ff(E, Rq, beta, irho, X, Y, Z);
+        const float step = -fv / g;
+        if (!isfinite(step)) break;
+        tt = ff_add_f(tt, step);
+        if (fabsf(step) <= 1e-3f) break;
+    }
+    return tt;
+}
+
 // Phase two, for a face that may be the nearest: its ray parameter in
 // float-float from the FP32 one, by Newton steps whose residuals are
 // evaluated in float-float (refine_quadric; the asphere's sag residual by
 // asph_residual_ff, its derivative in FP32).  The FP32 root is within
 // ~1e-5 mm, so one step suffices unless it moved the root by more than a
 // micrometre.
-__device__ __forceinline__ ff face_refine(const rp_face &F, const MxFace &M, const LRay &R, float t32) {
+template <bool DIST>
+__device__ __forceinline__ ff face_refine(const DevScene &S, const rp_face &F, const MxFace &M, const LRay &R,
+                                          float t32) {
     const ff zv = ffm(M.zv_hi, M.zv_lo);
     const ff Rq = ffm(M.rq_hi, M.rq_lo);
     if (F.type == RP_FACE_SPHERICAL || F.type == RP_FACE_SHAPED_SPHERICAL) return refine_quadric(R, zv, t32, 1.0f, Rq);
+    if constexpr (DIST)
+        if (F.type == RP_FACE_EXTPOLY) return extpoly_refine(S, F, M, R, t32);
     const float beta = 1.0f + M.p[2];
     if (F.type == RP_FACE_CONIC) return refine_quadric(R, zv, t32, beta, Rq);
     ff tt = ffm(t32, 0.0f);
@@ -896,6 +1020,24 @@ __device__ __forceinline__ bool face_normal_ff(const DevScene &S, const rp_face 
             float inv = 1.0f / (Rq * (1.0f + root));
             df += 2.0f * inv + beta * r2 * inv * inv / (Rq * root);
             n = ff3_unit(mkff3(ff_mul_f(x, -df * sign), ff_mul_f(y, -df * sign), ffm(sign, 0.0f)));
+            return true;
+        }
+        case RP_FACE_EXTPOLY: {  // cfaces.pyx:2236-2293: the conic's unit normal, then the polynomial's gradient
+            if constexpr (!DIST) return false;
+            if (!S.ep32_off || S.ep32_off[&F - S.faces] < 0) return false;
+            const float *E = S.ep32 + S.ep32_off[&F - S.faces];
+            const float Rq = M.p[0], beta = M.p[1], irho = 1.0f / M.p[2];
+            float sign = F.invert_normals ? -1.0f : 1.0f;
+            if (Rq * beta < 0.0f) sign = -sign;
+            ff3 g = mkff3(ff_mul_f(x, -2.0f * beta * sign), ff_mul_f(y, -2.0f * beta * sign),
+                          ff_mul_f(ff_add_f(ff_mul_f(z, -beta), Rq), 2.0f * beta * sign));
+            g = ff3_unit(g);
+            float P, Px, Py;
+            ep_eval32(E, x.hi * irho, y.hi * irho, P, Px, Py);
+            const float s2 = F.invert_normals ? irho : -irho;  // added with invert_normals, else subtracted
+            g.x = ff_add_f(g.x, s2 * Px);
+            g.y = ff_add_f(g.y, s2 * Py);
+            n = ff3_unit(g);
             return true;
         }
         case RP_FACE_DISTORTION: {  // cfaces.pyx:2409-2422 over a plane: (-dz/dx, -dz/dy, 1) normalised
@@ -1290,6 +1432,7 @@ __device__ __forceinline__ bool try_face32(const DevScene &S, const MxList *ml, 
 
 // Phase two for one candidate: its float-float parameter (bounds and the
 // tolerance checked again on the refined value), kept in b when nearer.
+template <bool DIST>
 __device__ __forceinline__ void settle(const DevScene &S, const MxList *ml, const MxFace *mf, const Cand &c, int &cur,
                                        LRay &R, const ff *O, const ff *D, ff dlen, float tmax, Best &b) {
     if (c.face < 0) return;
@@ -1301,7 +1444,7 @@ __device__ __forceinline__ void settle(const DevScene &S, const MxList *ml, cons
             R = local_ray(ml[c.list], O, D);
             cur = c.list;
         }
-        t = face_refine(S.faces[c.face], mf[c.face], R, c.t);
+        t = face_refine<DIST>(S, S.faces[c.face], mf[c.face], R, c.t);
         if (!(t.hi <= tmax) || !(t.hi >= mf[c.face].tmin)) return;
     }
     const ff dist = ff_mul(t, dlen);
@@ -1313,12 +1456,13 @@ __device__ __forceinline__ void settle(const DevScene &S, const MxList *ml, cons
 // distance is within the FP32 roots' error of the nearer (so that the exact
 // comparison, not FP32 rounding, decides between close hits) or when the
 // nearer fails its refined checks.
+template <bool DIST>
 __device__ __forceinline__ void settle_best(const DevScene &S, const MxList *ml, const MxFace *mf, const Cand &c1,
                                             const Cand &c2, int &cur, LRay &R, const ff *O, const ff *D, ff dlen,
                                             float tmax, Best &b) {
-    settle(S, ml, mf, c1, cur, R, O, D, dlen, tmax, b);
+    settle<DIST>(S, ml, mf, c1, cur, R, O, D, dlen, tmax, b);
     if (c2.face >= 0 && (b.face < 0 || c2.d <= fmaf(c1.d, 1.000244140625f, 1e-3f)))
-        settle(S, ml, mf, c2, cur, R, O, D, dlen, tmax, b);
+        settle<DIST>(S, ml, mf, c2, cur, R, O, D, dlen, tmax, b);
 }
 
 // Tests a face through the FP64 path.  Out of line: called only for face types
@@ -1535,7 +1679,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         bool fp64 = !mf[f].spec;
         if (!fp64) {
             fp64 = try_face32<FB>(S, ml, mf, f, A.one_list, cur, R, O, D, dl, max_len, A.err, c1, c2);
-            settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
+            settle_best<FB>(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
         }
         if constexpr (FB)
             if (fp64) try_face_fp64(A, S, f, A.one_list, src, dlen, b);
@@ -1640,7 +1784,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
             if constexpr (FB)
                 if (fp64) try_face_fp64(A, S, f, l, src, dlen, b);
         }
-        settle_best(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
+        settle_best<FB>(S, ml, mf, c1, c2, cur, R, O, D, dlen, max_len, b);
         // the FP64 faces: the nearest hit does not depend on the order of
         // the tests, and the box bound stays valid against the final length
         for (int f = 0; FB && f < nf; f++) {
