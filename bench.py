@@ -67,12 +67,12 @@ BYTES = {"plain": {"segment": 168, "gathered": 208, "child": 188},
 # dmul + 2 dfma thread instructions, 2,146.6 M over the 2,486,356 rays of
 # generation 5 of the 262,144-ray configuration-2 trace)
 PLAIN_FP64_FLOPS_PER_SEGMENT = 863.4
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per input ray of
-# a launch, from ncu on generation 5 of the 262,144-ray configuration-2 trace
-# (2,486,356 gathered rays): the plain kernel on an earlier capture of
-# generation 3 (1,046,875 rays)
-NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 649.2, "mixed_search_kernel": 364.6,
-                       "mixed_material_kernel": 435.9}
+# DRAM bytes per input ray of a launch, from ncu on generation 3 of the
+# 262,144-ray configuration-2 trace (1,046,875 gathered rays), this build:
+# dram__bytes_read.sum + dram__bytes_write.sum of the search and material
+# kernels, dram__bytes.sum.per_second x duration of the plain kernel
+NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 805.1, "mixed_search_kernel": 331.0,
+                       "mixed_material_kernel": 426.5}
 
 
 def parse():
