@@ -481,7 +481,7 @@ def adjoint_leg(ctx, reps=5):
 
 
 def serving_leg(args):
-    """Configuration 5: a Poisson stream of jobs (systems of 3-39 faces from the
+    """Configuration 5: a Poisson stream of jobs (systems of 2-40 faces from the
     configuration-2 face mix, log-uniform 1e3-4e6 rays, wavelengths 0.4-1.0 um)
     replayed in real time against the job server (mixed path; up to
     --serving-lanes jobs in flight, advanced together one generation per step;

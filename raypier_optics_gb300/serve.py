@@ -4,7 +4,7 @@
 under one HBM budget, admitted as slots and memory free up; every step of
 the server advances all of them by one generation in shared launches of the
 mixed-path kernels (continuous batching of generations).  ``run_stream`` replays a timed job stream (configuration 5: Poisson
-arrivals, systems of 3-39 faces, log-uniform ray counts) against a server and
+arrivals, systems of 2-40 faces, log-uniform ray counts) against a server and
 returns each job's latency and result.
 """
 from __future__ import annotations

@@ -479,13 +479,15 @@ CONFIG5 = {"n_jobs": 10000, "rate": 200.0, "seed": 5, "min_rays": 1000, "max_ray
            "recursion_limit": 8, "max_length": 1000.0, "e2_terminate": 1e-6}
 
 
-def config5_system(rng, n_elements):
+def config5_system(rng, n_elements, entrance=False):
     """A random coaxial system of `n_elements` singlets (2 faces each) drawn
     from configuration 2's face mix (spherical, conic, aspheric, plane), crown
     or flint with Sellmeier dispersion and the materials' default Fresnel
-    thresholds, followed by a detector: 2 n_elements + 1 faces.  Every face's
-    normal points to +z at its vertex, so a face's material has the medium in
-    front as `inside` (DielectricMaterial's out-to-in test is normal . d < 0)."""
+    thresholds, then (`entrance`) one more air-to-glass surface whose glass
+    runs on to the detector, then the detector: 2 n_elements + 1 (+ 1) faces.
+    Every face's normal points to +z at its vertex, so a face's material has
+    the medium in front as `inside` (DielectricMaterial's out-to-in test is
+    normal . d < 0)."""
     mats = {"detector": {"type": "OpaqueMaterial"}}
     for g in ("crown", "flint"):
         mats[f"in_{g}"] = {"type": "FullDielectricDispersiveMaterial",
@@ -519,6 +521,9 @@ def config5_system(rng, n_elements):
         z += float(rng.uniform(4.0, 8.0))
         faces.append(surface(z, f"out_{g}"))
         z += float(rng.uniform(3.0, 10.0))
+    if entrance:
+        faces.append(surface(z, "in_crown" if rng.uniform() < 0.5 else "in_flint"))
+        z += float(rng.uniform(3.0, 10.0))
     faces.append({"type": "CircularFace", "kw": {"z_plane": z + 20.0}, "owner": {"diameter": 400.0, "offset": 0.0},
                   "material": "detector"})
     return {"curves": {"crown": CROWN, "flint": FLINT, "air": AIR}, "materials": mats,
@@ -528,12 +533,15 @@ def config5_system(rng, n_elements):
 def config5_jobs(n_jobs=None, seed=None):
     """The seeded job stream: (arrival time s, system index, n_rays, source seed,
     source type, wavelengths), with `CONFIG5["n_systems"]` distinct systems
-    of 3-39 faces that jobs draw from, arrivals Poisson at CONFIG5["rate"]/s and
-    ray counts log-uniform over [1e3, 4e6]."""
+    of 2-40 faces (uniform) that jobs draw from, arrivals Poisson at
+    CONFIG5["rate"]/s and ray counts log-uniform over [1e3, 4e6]."""
     C = CONFIG5
     n_jobs = C["n_jobs"] if n_jobs is None else n_jobs
     rng = np.random.Generator(np.random.PCG64(C["seed"] if seed is None else seed))
-    systems = [config5_system(rng, int(rng.integers(1, 20))) for _ in range(C["n_systems"])]
+    systems = []
+    for _ in range(C["n_systems"]):
+        lens_faces = int(rng.integers(2, 41)) - 1  # 2-40 faces with the detector
+        systems.append(config5_system(rng, lens_faces // 2, entrance=lens_faces % 2 == 1))
     t = np.cumsum(rng.exponential(1.0 / C["rate"], n_jobs))
     sys_idx = rng.integers(0, len(systems), n_jobs)
     n_rays = np.exp(rng.uniform(math.log(C["min_rays"]), math.log(C["max_rays"]), n_jobs)).astype(np.int64)
