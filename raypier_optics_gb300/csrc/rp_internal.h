@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdarg>
+#include <mutex>
 #include <vector>
 
 #include "../../include/rp_gb300.h"
@@ -24,6 +25,7 @@ struct rp_ctx {
     uint64_t in_use;                 // bytes of live allocations
     std::vector<PoolBlock> pool;     // freed blocks kept for reuse
     uint64_t pooled;                 // bytes in `pool`
+    std::mutex pool_mu;              // the pool and the byte counts (a buffer may be freed from another thread)
     std::vector<cudaEvent_t> gen_ev; // per-generation kernel events (pairs)
     struct rp_rays *arena;           // child slots of the generation being traced
     struct rp_rays *arena2;          // trace_rays: the other arena (one is read while the other is written)

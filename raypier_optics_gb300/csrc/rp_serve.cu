@@ -261,6 +261,7 @@ struct Job {
     rp_rays *cur = nullptr, *next = nullptr, *spare = nullptr, *arena = nullptr;  // spare: cur's ping-pong partner
     unsigned char *hand = nullptr;  // hit hand-over (mixed) or own scan scratch (plain)
     size_t hand_bytes = 0, hand_cap = 0;
+    bool active = false;            // admitted and taking part in the steps
 };
 
 }  // namespace
@@ -269,11 +270,14 @@ struct rp_server {
     int device = 0;
     uint64_t budget = 0;
     int max_jobs = 0;
-    rp_ctx *ctx = nullptr;
-    std::thread loop;
+    rp_ctx *ctx = nullptr;   // the steps' stream and buffers
+    rp_ctx *actx = nullptr;  // admission: scenes, tables and source rays, on its own stream
+    std::thread loop, admit_th;
     std::mutex mu;
-    std::condition_variable cv_pending, cv_done;
+    std::condition_variable cv_pending, cv_step, cv_done;
     std::deque<Job *> pending;
+    std::deque<Job *> ready;  // admitted, joining at the next step
+    int admitting = 0;        // jobs in admission
     std::map<uint64_t, Job *> jobs;
     std::vector<Job *> slots;  // admitted jobs by slot
     uint64_t next_id = 1;
@@ -380,23 +384,26 @@ int ensure_units(rp_server *s, size_t units) {
     return capture_step(s);
 }
 
-void release_job_buffers(rp_ctx *ctx, Job *j) {
+// (Ray buffers return to the pool of the context that made them; the
+// hand-over was made by the steps' context, the tables by admission's.)
+void release_job_buffers(rp_server *s, Job *j) {
     if (j->cur) rp_rays_free(j->cur);
     if (j->next) rp_rays_free(j->next);
     if (j->spare) rp_rays_free(j->spare);
     if (j->arena) rp_rays_free(j->arena);
     j->cur = j->next = j->spare = j->arena = nullptr;
-    if (j->hand) rp__ctx_free(ctx, j->hand, j->hand_bytes);
-    if (j->mx) rp__ctx_free(ctx, j->mx, j->mx_bytes);
+    if (j->hand) rp__ctx_free(s->ctx, j->hand, j->hand_bytes);
+    if (j->mx) rp__ctx_free(s->actx, j->mx, j->mx_bytes);
     j->hand = nullptr;
     j->mx = nullptr;
     j->hand_cap = 0;
 }
 
-// Admission: the job's scene and tables on the device and its source rays
-// generated into its first generation.
+// Admission, on the admission context's stream while the steps run: the
+// job's scene and tables on the device and its source rays generated into
+// its first generation; done when the stream has finished them.
 int admit(rp_server *s, Job *j) {
-    rp_ctx *ctx = s->ctx;
+    rp_ctx *ctx = s->actx;
     j->res.t_start_ms = ms_since(s);
     j->mixed = (j->flags & RP_TRACE_MIXED) != 0;
     int rc = rp_scene_create(ctx, &j->desc, j->wl.empty() ? nullptr : j->wl.data(), (int64_t)j->wl.size(), &j->sc);
@@ -438,6 +445,8 @@ int admit(rp_server *s, Job *j) {
     j->cur->n = n0;
     j->gen = 0;
     j->segments = 0;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "admission");
     return RP_OK;
 }
 
@@ -461,17 +470,20 @@ void finish_job(rp_server *s, Job *j, int status) {
         j->res.sum_xx = a[4];
         j->res.sum_yy = a[5];
     }
-    release_job_buffers(s->ctx, j);
+    release_job_buffers(s, j);
     if (j->sc) {
         rp_scene_destroy(j->sc);
         j->sc = nullptr;
     }
     j->res.t_done_ms = ms_since(s);
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (j->slot >= 0) s->slots[j->slot] = nullptr;
-    s->reserved -= j->est_bytes;
-    j->done = true;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (j->slot >= 0) s->slots[j->slot] = nullptr;
+        s->reserved -= j->est_bytes;
+        j->done = true;
+    }
     s->cv_done.notify_all();
+    s->cv_pending.notify_all();  // a slot and budget are free for admission
 }
 
 // Buffer `b` with room for `need` records: kept when it has it, else replaced
@@ -550,13 +562,10 @@ int prepare_job(rp_server *s, Job *j, GenArgs &a) {
     return RP_OK;
 }
 
-// One step: every admitted job advances one generation.
-void run_step(rp_server *s) {
+// One step: every active job advances one generation.
+void run_step(rp_server *s, std::vector<Job *> act) {
     rp_ctx *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
-    std::vector<Job *> act;
-    for (Job *j : s->slots)
-        if (j) act.push_back(j);
     BatchDev &B = *s->h_batch;
     std::vector<GenArgs> plain_args;
     std::vector<Job *> failed;
@@ -646,44 +655,68 @@ void run_step(rp_server *s) {
     }
 }
 
+// The steps: the jobs admitted since the last step join, then every active
+// job advances one generation; waits while none is active.
 void step_loop(rp_server *s) {
     cudaSetDevice(s->device);
     for (;;) {
-        std::vector<Job *> admitted;
+        std::vector<Job *> act;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             for (;;) {
-                bool any = false;
-                for (Job *j : s->slots) any = any || j;
-                if (any || !s->pending.empty()) break;
-                if (s->stop) return;
+                for (Job *j : s->ready) j->active = true;
+                s->ready.clear();
+                for (Job *j : s->slots)
+                    if (j && j->active) act.push_back(j);
+                if (!act.empty()) break;
+                if (s->stop && s->pending.empty() && s->admitting == 0) return;
+                s->cv_step.wait(lk);
+            }
+        }
+        run_step(s, act);
+    }
+}
+
+// Admission: FIFO, while a slot is free and the budget holds (one job is
+// always admitted when none is in flight), each job prepared on the
+// admission stream and handed to the steps when ready.
+void admit_loop(rp_server *s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        Job *h = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            for (;;) {
+                if (!s->pending.empty()) {
+                    int free_slot = -1, busy = 0;
+                    for (int k = 0; k < s->max_jobs; k++) {
+                        if (!s->slots[k] && free_slot < 0) free_slot = k;
+                        if (s->slots[k]) busy++;
+                    }
+                    Job *p = s->pending.front();
+                    if (free_slot >= 0 && (busy == 0 || s->reserved + p->est_bytes <= s->budget)) {
+                        s->pending.pop_front();
+                        p->slot = free_slot;
+                        s->slots[free_slot] = p;
+                        s->reserved += p->est_bytes;
+                        s->admitting++;
+                        h = p;
+                        break;
+                    }
+                }
+                if (s->stop && s->pending.empty()) return;
                 s->cv_pending.wait(lk);
             }
-            // admission: FIFO, while a slot is free and the budget holds (one job always runs)
-            while (!s->pending.empty()) {
-                int free_slot = -1, busy = 0;
-                for (int k = 0; k < s->max_jobs; k++) {
-                    if (!s->slots[k] && free_slot < 0) free_slot = k;
-                    if (s->slots[k]) busy++;
-                }
-                Job *h = s->pending.front();
-                if (free_slot < 0 || (busy > 0 && s->reserved + h->est_bytes > s->budget)) break;
-                s->pending.pop_front();
-                h->slot = free_slot;
-                s->slots[free_slot] = h;
-                s->reserved += h->est_bytes;
-                admitted.push_back(h);
-            }
         }
-        for (Job *j : admitted) {
-            int rc = admit(s, j);
-            if (rc == RP_OK && (j->source.n_rays == 0 || j->recursion_limit <= 0)) {
-                finish_job(s, j, RP_OK);
-            } else if (rc) {
-                finish_job(s, j, rc);
-            }
+        const int rc = admit(s, h);
+        const bool done = rc != RP_OK || h->source.n_rays == 0 || h->recursion_limit <= 0;
+        if (done) finish_job(s, h, rc);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->admitting--;
+            if (!done) s->ready.push_back(h);
         }
-        run_step(s);
+        s->cv_step.notify_all();
     }
 }
 
@@ -702,6 +735,7 @@ void destroy_buffers(rp_server *s) {
     if (s->h_batch) cudaFreeHost(s->h_batch);
     if (s->h_out) cudaFreeHost(s->h_out);
     if (s->ctx) rp_ctx_destroy(s->ctx);
+    if (s->actx) rp_ctx_destroy(s->actx);
 }
 
 }  // namespace
@@ -743,6 +777,7 @@ int rp_server_create(int device, uint64_t hbm_budget, int32_t lanes, rp_server *
     s->slots.assign(s->max_jobs, nullptr);
     s->t0 = Clock::now();
     int rc = rp_ctx_create(device, 0, &s->ctx);
+    if (rc == RP_OK) rc = rp_ctx_create(device, 0, &s->actx);
     cudaError_t e = cudaSuccess;
     if (rc == RP_OK) {
         e = cudaMallocHost((void **)&s->h_batch, sizeof(BatchDev));
@@ -766,6 +801,7 @@ int rp_server_create(int device, uint64_t hbm_budget, int32_t lanes, rp_server *
         return rc;
     }
     s->loop = std::thread(step_loop, s);
+    s->admit_th = std::thread(admit_loop, s);
     *out = s;
     return RP_OK;
 }
@@ -842,6 +878,8 @@ int rp_server_destroy(rp_server *s) {
         s->stop = true;
     }
     s->cv_pending.notify_all();
+    if (s->admit_th.joinable()) s->admit_th.join();
+    s->cv_step.notify_all();
     if (s->loop.joinable()) s->loop.join();
     for (auto &kv : s->jobs) delete kv.second;
     destroy_buffers(s);
