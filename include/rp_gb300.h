@@ -510,8 +510,8 @@ int rp_measure_peaks(int device, double *fp64_flops, double *fp32_flops, double 
  * (CircularFace); the loss is the RMS spot radius of the rays that reach it.
  * The forward runs the plain path's FP64 face and material arithmetic, so it
  * equals rp_trace_rays on the same faces bit for bit; the backward is a
- * hand-written adjoint that recomputes each surface from the ray states the
- * forward kept.
+ * hand-written adjoint that re-traces each ray from its input up to every
+ * surface (no per-surface state is kept between the passes).
  * params[5 * n_surfaces]: curvature[n] (raypier sign, R = -curvature),
  * conic[n], A4[n], A6[n], thickness[n] (vertex to next vertex; the last one
  * from the last vertex to the image plane).  Surface 0's vertex is at z0. */

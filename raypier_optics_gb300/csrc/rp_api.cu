@@ -1623,7 +1623,7 @@ static size_t lens_layout(int n_surf, uint64_t cap, size_t off[8]) {
     off[0] = o; o += align256(sizeof(rp_face) * (n_surf + 1));                   // faces
     off[1] = o; o += align256(sizeof(double) * (n_surf + 1));                    // indices
     off[2] = o; o += align256(sizeof(rp_shape_op) * 2 * n_surf);                 // apertures
-    off[3] = o; o += align256(sizeof(double) * 6 * (n_surf + 1) * (cap ? cap : 1));  // states
+    off[3] = o;                                                                   // (no per-surface states)
     off[4] = o; o += align256(sizeof(double) * 2 * (cap ? cap : 1));             // image points
     off[5] = o; o += align256(cap ? cap : 1);                                    // valid flags
     off[6] = o; o += align256(sizeof(double) * 3 * nb);                          // partial sums
@@ -1708,7 +1708,6 @@ int rp_lens_create(rp_ctx *ctx, const rp_lens_desc *d, uint64_t max_rays, rp_len
     L->a.S.shapes = (const rp_shape_op *)(b + off[2]);
     L->a.S.n_shapes = 2 * L->n_surf;
     L->a.max_len = L->max_len;
-    L->a.state = (double *)(b + off[3]);
     L->a.img = (double *)(b + off[4]);
     L->a.valid = b + off[5];
     L->a.part = (double *)(b + off[6]);

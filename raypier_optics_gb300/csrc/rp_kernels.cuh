@@ -207,7 +207,6 @@ struct LensArgs {
     double max_len;             // segment length of the intersection tests
     RaySoA in;                  // input rays (origin, direction)
     unsigned long long n;
-    double *state;              // [(n_surf + 1) * 6 * n] p, d in front of each surface and the image plane
     double *img;                // [2 n] image-plane x, y
     unsigned char *valid;       // [n] ray reached the image
     double *part;               // per-block partial sums

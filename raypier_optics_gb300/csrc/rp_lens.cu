@@ -14,10 +14,12 @@
 // Loss: the RMS spot radius on the image plane, sqrt(mean |x - xbar|^2) over
 // the surviving rays.
 //
-// Adjoint: the ray state in front of every surface is kept from the forward
-// (the generations of the trace); the backward pass walks the surfaces in
-// reverse, recomputes that surface's hit, normal and refraction from the kept
-// state, and applies the chain rule:
+// Adjoint: nothing of the forward is kept but each ray's image point and
+// reached flag.  The backward pass walks the surfaces in reverse and, for
+// each, re-traces the ray from its input through the surfaces before it (the
+// forward per generation, recomputed: O(n^2) surface evaluations for n
+// surfaces, no per-surface state in memory), recomputes that surface's hit,
+// normal and refraction, and applies the chain rule:
 //   hit     h = p + t d with F(h) = z - z_k - s(x^2 + y^2) = 0, so
 //           dt = (ds - dz_k - G.dp - t G.dd) / (G.d) with G = grad F
 //   normal  n = m / |m|, m = (-2 s' x, -2 s' y, 1)
@@ -42,10 +44,6 @@ __device__ __forceinline__ double lens_block_sum(double v, double *s_red) {
     if (threadIdx.x == 0)
         for (int w = 0; w < RP_LENS_BLOCK / 32; w++) t += s_red[w];
     return t;
-}
-
-__device__ __forceinline__ double *lens_state(const LensArgs &L, int k, int c) {
-    return L.state + ((size_t)k * 6 + c) * L.n;
 }
 
 // One surface of the forward trace (shared by the forward and the adjoint so
@@ -83,14 +81,8 @@ __global__ void __launch_bounds__(RP_LENS_BLOCK) lens_forward_kernel(LensArgs L)
         v3 p = mkv(L.in.ox[i], L.in.oy[i], L.in.oz[i]);
         v3 d = mkv(L.in.dx[i], L.in.dy[i], L.in.dz[i]);
         bool ok = true;
-        for (int k = 0; k <= L.n_surf; k++) {
-            lens_state(L, k, 0)[i] = p.x;
-            lens_state(L, k, 1)[i] = p.y;
-            lens_state(L, k, 2)[i] = p.z;
-            lens_state(L, k, 3)[i] = d.x;
-            lens_state(L, k, 4)[i] = d.y;
-            lens_state(L, k, 5)[i] = d.z;
-            if (!ok || k == L.n_surf) continue;
+        for (int k = 0; k < L.n_surf; k++) {
+            if (!ok) continue;
             v3 h, dn;
             double t;
             ok = lens_surface(L, k, p, d, h, dn, t, L.err);
@@ -165,6 +157,22 @@ __device__ __forceinline__ SagD sag_derivs(double u, double R, double beta, doub
     return g;
 }
 
+// The ray i in front of surface k (k = n_surf: in front of the image plane):
+// its input re-traced through surfaces 0 .. k-1 with the forward's arithmetic.
+// Only called for rays the forward kept, which pass every surface again.
+__device__ __forceinline__ void lens_prefix(const LensArgs &L, unsigned long long i, int k, v3 &p, v3 &d) {
+    p = mkv(L.in.ox[i], L.in.oy[i], L.in.oz[i]);
+    d = mkv(L.in.dx[i], L.in.dy[i], L.in.dz[i]);
+    for (int j = 0; j < k; j++) {
+        v3 h, dn;
+        double t;
+        if (lens_surface(L, j, p, d, h, dn, t, L.err)) {
+            p = h;
+            d = dn;
+        }
+    }
+}
+
 // Per ray: the adjoint of the loss through the image plane and every surface
 // in reverse.  gpart[block][5 * k + j] receives the block's sum of dL/dR,
 // dL/dbeta, dL/dA4, dL/dA6, dL/dz_k for surface k, and gpart[block][5 n] dL/dz_image.
@@ -179,8 +187,8 @@ __global__ void __launch_bounds__(RP_LENS_BLOCK) lens_backward_kernel(LensArgs L
     if (ok) {
         // image plane z = z_img: h = p + t d, t = (z_img - p_z) / d_z
         const int k = L.n_surf;
-        v3 p = mkv(lens_state(L, k, 0)[i], lens_state(L, k, 1)[i], lens_state(L, k, 2)[i]);
-        v3 d = mkv(lens_state(L, k, 3)[i], lens_state(L, k, 4)[i], lens_state(L, k, 5)[i]);
+        v3 p, d;
+        lens_prefix(L, i, k, p, d);
         const double zi = L.faces[k].p[2];
         const double t = (zi - p.z) / d.z;
         v3 h = addv(p, mulvs(d, t));
@@ -195,8 +203,8 @@ __global__ void __launch_bounds__(RP_LENS_BLOCK) lens_backward_kernel(LensArgs L
     for (int k = L.n_surf - 1; k >= 0; k--) {
         double gR = 0.0, gB = 0.0, gA4 = 0.0, gA6 = 0.0, gZ = 0.0;
         if (ok) {
-            v3 p = mkv(lens_state(L, k, 0)[i], lens_state(L, k, 1)[i], lens_state(L, k, 2)[i]);
-            v3 d = mkv(lens_state(L, k, 3)[i], lens_state(L, k, 4)[i], lens_state(L, k, 5)[i]);
+            v3 p, d;
+            lens_prefix(L, i, k, p, d);
             v3 h, dn;
             double t = 0.0;
             lens_surface(L, k, p, d, h, dn, t, L.err);  // the forward kept this ray, so it hits again

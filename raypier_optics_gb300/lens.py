@@ -4,9 +4,10 @@ A stack of even aspheres (raypier's AsphericFace with a circular aperture,
 refracting as DielectricMaterial) traced in order onto an image plane.  The
 forward is the plain FP64 path's arithmetic (the same image points as
 ``tracer.trace_rays`` on ``workloads.config4_spec(params)``); the gradient is
-the library's hand-written adjoint (``rp_lens_backward``), which recomputes
-each surface from the ray states the forward kept.  PyTorch is used only for
-the ``torch.autograd.Function`` wrapper.
+the library's hand-written adjoint (``rp_lens_backward``), which re-traces
+every ray from its input up to each surface in turn instead of keeping the
+forward's ray states.  PyTorch is used only for the
+``torch.autograd.Function`` wrapper.
 
 Parameters (``5 * n_surfaces`` doubles): curvature (raypier sign, R =
 -curvature), conic constant, A4, A6 and thickness (vertex to next vertex; the
