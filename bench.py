@@ -372,7 +372,7 @@ def main():
     if not args.no_mixed:
         ost, odev_s, _, _, _, ovalue = timed(1 - flags, False)
         other = {"value": ovalue, "unit": UNIT, "ms_per_step": 1000.0 * odev_s / args.steps,
-                 "kernel": "generation_mixed_kernel" if flags == 0 else "generation_plain_kernel",
+                 "kernel": "mixed_search_kernel + mixed_material_kernel" if flags == 0 else "generation_plain_kernel",
                  "kernel_ms_per_step": ost.kernel_ms / args.steps}
         mixed_v, plain_v = (ovalue, value) if flags == 0 else (value, ovalue)
         other["speedup_mixed_vs_plain_fp64"] = mixed_v / plain_v
