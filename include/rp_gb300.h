@@ -602,6 +602,12 @@ int rp_server_submit(rp_server *server, const rp_job_desc *job, uint64_t *job_id
  * them) when face_counts is not NULL.  A job id can be waited for once. */
 int rp_server_wait(rp_server *server, uint64_t job_id, rp_job_result *result, uint32_t *face_counts,
                    int32_t n_faces);
+/* The work of a step: a mixed job's generation of more than `groups` 128-ray
+ * groups (what is left of the step's budget after the smaller generations,
+ * and at least `min_chunk` groups) is traced over several steps, so that
+ * small jobs' steps stay short; results do not depend on it.  Defaults
+ * 32768 and 1024. */
+int rp_server_set_step_groups(rp_server *server, uint32_t groups, uint32_t min_chunk);
 /* Finishes the queued jobs, then stops the step loop. */
 int rp_server_destroy(rp_server *server);
 

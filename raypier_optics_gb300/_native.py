@@ -248,6 +248,7 @@ _SIGS = {
     "rp_server_create": (_I, [_I, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(_P)]),
     "rp_server_submit": (_I, [_P, ctypes.POINTER(JobDesc), ctypes.POINTER(ctypes.c_uint64)]),
     "rp_server_wait": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(JobResult), _P, ctypes.c_int32]),
+    "rp_server_set_step_groups": (_I, [_P, ctypes.c_uint32, ctypes.c_uint32]),
     "rp_server_destroy": (_I, [_P]),
     "rp_face_intersect": (_I, [_P, ctypes.c_int32, _P, _P, ctypes.c_uint64, _I, _P]),
     "rp_face_normal": (_I, [_P, ctypes.c_int32, _P, ctypes.c_uint64, _P]),

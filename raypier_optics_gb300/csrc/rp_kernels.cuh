@@ -79,6 +79,10 @@ struct GenArgs {
     float2 *hit_t;
     int *hit_face;
     unsigned *group_next;
+    // Added to the children's parent index: the first ray of the part of a
+    // generation these arguments cover (the job server traces a large
+    // generation in chunks); 0 otherwise.
+    unsigned long long parent_base;
 };
 // ---- batches of trace jobs (the job server, rp_serve.cu) ----
 // One generation of every job of a batch runs in one launch of each mixed
@@ -97,6 +101,14 @@ struct BatchJob {
     int mixed;            // 1: traced by the batch kernels; 0: by its own plain-path launches
     int slot;             // the job's server slot (tally accumulators, results)
     int first;            // 1 on the job's first generation (its accumulators start from zero)
+    // Detector tallies: per unit of the job's whole generation (part_gen,
+    // gen_units units); `part` is the entry of the step's first unit.  The
+    // step that completes the generation (gen_done) sums them in a fixed
+    // order, however the generation was split into steps.
+    double *part;
+    const double *part_gen;
+    unsigned long long gen_units;
+    int gen_done;
 };
 struct BatchDev {
     int n_jobs;

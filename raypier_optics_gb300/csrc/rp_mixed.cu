@@ -2372,9 +2372,10 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS)
             const unsigned wl = B.wl[t], ident = B.ident[t];
             const unsigned endf = (unsigned)A.S.faces[face].idx;
             const unsigned long long slot = (unsigned long long)G.q * RP_TILE_SLOTS + carry + excl;
-            store_child_f(A.scratch, slot, origin, nrm, Eo, opl, ch[0], phase, wl, (unsigned)i, endf, ident);
+            const unsigned parent = (unsigned)(i + A.parent_base);  // within the job's generation
+            store_child_f(A.scratch, slot, origin, nrm, Eo, opl, ch[0], phase, wl, parent, endf, ident);
             if (nc > 1)
-                store_child_f(A.scratch, slot + 1, origin, nrm, Eo, opl, ch[1], phase, wl, (unsigned)i, endf, ident);
+                store_child_f(A.scratch, slot + 1, origin, nrm, Eo, opl, ch[1], phase, wl, parent, endf, ident);
         }
         carry += chunk_children;
         if (last_of_group) {

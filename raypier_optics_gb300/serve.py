@@ -80,6 +80,13 @@ class Server:
         _native.check(self.lib.rp_server_submit(self.handle, ctypes.byref(jd), ctypes.byref(jid)), "rp_server_submit")
         return jid.value
 
+    def set_step_groups(self, groups, min_chunk):
+        """Bounds a step's work: a mixed job's generation of more than
+        `groups` 128-ray groups is traced over several steps (at least
+        `min_chunk` groups each); results do not depend on it."""
+        _native.check(self.lib.rp_server_set_step_groups(self.handle, int(groups), int(min_chunk)),
+                      "rp_server_set_step_groups")
+
     def wait(self, job_id, n_faces=0):
         r = _native.JobResult()
         counts = np.zeros(max(n_faces, 1), dtype=np.uint32)

@@ -45,14 +45,20 @@ def trace_reference(system, src, wl, flags):
             "face_counts": np.array([f.count for f in faces], dtype=np.uint32)}
 
 
-@pytest.mark.parametrize("flags", [0, 1], ids=["plain_fp64", "mixed"])
-def test_job_matches_trace_rays(flags):
+@pytest.mark.parametrize("flags,step_groups", [(0, None), (1, None), (1, 24)],
+                         ids=["plain_fp64", "mixed", "mixed_in_chunks"])
+def test_job_matches_trace_rays(flags, step_groups):
+    """A job through the server against the same rays through trace_rays; in
+    chunks: every generation of more than 24 groups (3,072 rays) traced over
+    several steps of at most 24 groups (at least 8)."""
     spec = W.config5_system(np.random.Generator(np.random.PCG64(3)), 4)
     system = serve.CompiledSystem(spec)
     system.spec = spec
     wl = np.linspace(0.45, 0.95, 32)
     src = serve.source_desc(serve.RP_SOURCE_POINT_CONE, 20000, 1234)
     srv = serve.Server(lanes=1)
+    if step_groups:
+        srv.set_step_groups(step_groups, 8)
     jid = srv.submit(system, src, wl, flags=flags)
     got = srv.wait(jid, system.n_faces)
     srv.close()
