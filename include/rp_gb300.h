@@ -608,6 +608,17 @@ int rp_server_wait(rp_server *server, uint64_t job_id, rp_job_result *result, ui
  * small jobs' steps stay short; results do not depend on it.  Defaults
  * 32768 and 1024. */
 int rp_server_set_step_groups(rp_server *server, uint32_t groups, uint32_t min_chunk);
+/* Counters of the step loop since the server was created: how busy the GPU
+ * was while jobs were in the steps (step_gpu_ms / step_wall_ms) and what the
+ * host adds per step. */
+typedef struct rp_server_stats {
+    uint64_t steps;               /* batch steps run */
+    uint64_t step_jobs;           /* sum over the steps of the jobs in each */
+    double step_gpu_ms;           /* device time of the steps' work (CUDA events on the step stream) */
+    double step_wall_ms;          /* host time inside the steps: preparation, launch, wait, bookkeeping */
+    double idle_wall_ms;          /* host time between steps while jobs were in flight */
+} rp_server_stats;
+int rp_server_get_stats(rp_server *server, rp_server_stats *out);
 /* Finishes the queued jobs, then stops the step loop. */
 int rp_server_destroy(rp_server *server);
 

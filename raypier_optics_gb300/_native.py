@@ -162,6 +162,11 @@ class JobResult(ctypes.Structure):
                 ("t_done_ms", ctypes.c_double)]
 
 
+class ServerStats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint64), ("step_jobs", ctypes.c_uint64), ("step_gpu_ms", ctypes.c_double),
+                ("step_wall_ms", ctypes.c_double), ("idle_wall_ms", ctypes.c_double)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("rays_in", ctypes.c_uint64), ("rays_out", ctypes.c_uint64),
                 ("hits", ctypes.c_uint64), ("terminated", ctypes.c_uint64),
@@ -249,6 +254,7 @@ _SIGS = {
     "rp_server_submit": (_I, [_P, ctypes.POINTER(JobDesc), ctypes.POINTER(ctypes.c_uint64)]),
     "rp_server_wait": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(JobResult), _P, ctypes.c_int32]),
     "rp_server_set_step_groups": (_I, [_P, ctypes.c_uint32, ctypes.c_uint32]),
+    "rp_server_get_stats": (_I, [_P, ctypes.POINTER(ServerStats)]),
     "rp_server_destroy": (_I, [_P]),
     "rp_face_intersect": (_I, [_P, ctypes.c_int32, _P, _P, ctypes.c_uint64, _I, _P]),
     "rp_face_normal": (_I, [_P, ctypes.c_int32, _P, ctypes.c_uint64, _P]),

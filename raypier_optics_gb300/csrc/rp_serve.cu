@@ -305,6 +305,8 @@ struct rp_server {
     StepOut *h_out = nullptr, *d_out = nullptr;  // mapped pinned
     size_t unit_cap = 0;
     cudaGraphExec_t step_exec = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_end = nullptr;  // around each step's device work
+    rp_server_stats stats{};                           // under mu
 };
 
 namespace {
@@ -624,6 +626,7 @@ int prepare_job(rp_server *s, Job *j, GenArgs &a) {
 
 // One step: every active job advances one generation.
 void run_step(rp_server *s, std::vector<Job *> act) {
+    const Clock::time_point t_enter = Clock::now();
     rp_ctx *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     BatchDev &B = *s->h_batch;
@@ -718,7 +721,8 @@ void run_step(rp_server *s, std::vector<Job *> act) {
         B.jobs[k].a.tile_offsets = s->d_offsets + B.unit_start[k];
     }
     // plain-path jobs: their own generation, scan and placement, queued first
-    cudaError_t e = cudaMemsetAsync(s->d_ctr + 3, 0, sizeof(unsigned), st);
+    cudaError_t e = cudaEventRecord(s->ev_start, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_ctr + 3, 0, sizeof(unsigned), st);
     for (size_t p = 0, k = 0; k < (size_t)nj && e == cudaSuccess; k++) {
         if (B.jobs[k].mixed) continue;
         GenArgs &a = plain_args[p++];
@@ -728,7 +732,10 @@ void run_step(rp_server *s, std::vector<Job *> act) {
         if (e == cudaSuccess && a.emit) e = launch_place_children(a, st);
     }
     if (e == cudaSuccess) e = cudaGraphLaunch(s->step_exec, st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev_end, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    float gpu_ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&gpu_ms, s->ev_start, s->ev_end);
     const unsigned err = e == cudaSuccess ? s->h_out->err : 0u;
     for (int k = 0; k < nj; k++) {
         Job *j = act[k];
@@ -763,16 +770,27 @@ void run_step(rp_server *s, std::vector<Job *> act) {
             finish_job(s, j, RP_OK);
         }
     }
+    const double wall = std::chrono::duration<double, std::milli>(Clock::now() - t_enter).count();
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stats.steps++;
+    s->stats.step_jobs += (uint64_t)nj;
+    s->stats.step_gpu_ms += gpu_ms;
+    s->stats.step_wall_ms += wall;
 }
 
 // The steps: the jobs admitted since the last step join, then every active
 // job advances one generation; waits while none is active.
 void step_loop(rp_server *s) {
     cudaSetDevice(s->device);
+    Clock::time_point t_last = Clock::now();
+    bool after_step = false;  // the previous pass ran a step
     for (;;) {
         std::vector<Job *> act;
         {
             std::unique_lock<std::mutex> lk(s->mu);
+            // time between the previous step and this one, unless the loop waited for jobs
+            if (after_step)
+                s->stats.idle_wall_ms += std::chrono::duration<double, std::milli>(Clock::now() - t_last).count();
             for (;;) {
                 for (Job *j : s->ready) j->active = true;
                 s->ready.clear();
@@ -784,6 +802,8 @@ void step_loop(rp_server *s) {
             }
         }
         run_step(s, act);
+        t_last = Clock::now();
+        after_step = true;
     }
 }
 
@@ -837,6 +857,8 @@ void copy_table(std::vector<T> &dst, const T *src, int32_t n) {
 
 void destroy_buffers(rp_server *s) {
     if (s->step_exec) cudaGraphExecDestroy(s->step_exec);
+    if (s->ev_start) cudaEventDestroy(s->ev_start);
+    if (s->ev_end) cudaEventDestroy(s->ev_end);
     free_unit_arrays(s);
     if (s->d_batch) cudaFree(s->d_batch);
     if (s->d_ctr) cudaFree(s->d_ctr);
@@ -899,6 +921,8 @@ int rp_server_create(int device, uint64_t hbm_budget, int32_t lanes, rp_server *
         if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_ctr, RP_BATCH_WORDS * sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_total, 4 * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_acc, RP_BATCH_MAX_JOBS * RP_TALLY_N * sizeof(double));
+        if (e == cudaSuccess) e = cudaEventCreate(&s->ev_start);
+        if (e == cudaSuccess) e = cudaEventCreate(&s->ev_end);
         if (e != cudaSuccess) rc = rp__cuda_fail(e, "server buffers");
     }
     if (rc == RP_OK) {
@@ -970,6 +994,13 @@ int rp_server_set_step_groups(rp_server *s, uint32_t groups, uint32_t min_chunk)
     std::lock_guard<std::mutex> lk(s->mu);
     s->step_groups = groups;
     s->min_chunk = min_chunk;
+    return RP_OK;
+}
+
+int rp_server_get_stats(rp_server *s, rp_server_stats *out) {
+    if (!s || !out) return RP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
     return RP_OK;
 }
 

@@ -87,6 +87,14 @@ class Server:
         _native.check(self.lib.rp_server_set_step_groups(self.handle, int(groups), int(min_chunk)),
                       "rp_server_set_step_groups")
 
+    def stats(self) -> dict:
+        """The step loop's counters since creation: steps, jobs summed over
+        the steps, the steps' device time, host time inside the steps and
+        host time between steps while jobs were in flight (ms)."""
+        st = _native.ServerStats()
+        _native.check(self.lib.rp_server_get_stats(self.handle, ctypes.byref(st)), "rp_server_get_stats")
+        return {k: getattr(st, k) for k, _ in _native.ServerStats._fields_}
+
     def wait(self, job_id, n_faces=0):
         r = _native.JobResult()
         counts = np.zeros(max(n_faces, 1), dtype=np.uint32)

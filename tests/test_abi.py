@@ -62,8 +62,9 @@ def test_struct_layouts_match_the_header():
              sizeof(rp_material), sizeof(rp_dispersion), sizeof(rp_scene_desc), sizeof(rp_stats));
       printf("%zu %zu %zu %zu\n", offsetof(rp_ray, refractive_index), offsetof(rp_ray, length),
              offsetof(rp_ray, wavelength_idx), offsetof(rp_face, p));
-      printf("%zu %zu %zu %zu %zu %zu\n", sizeof(rp_lens_desc), sizeof(rp_source_desc), sizeof(rp_job_desc),
-             sizeof(rp_job_result), offsetof(rp_job_desc, source), offsetof(rp_job_result, t_submit_ms));
+      printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(rp_lens_desc), sizeof(rp_source_desc), sizeof(rp_job_desc),
+             sizeof(rp_job_result), offsetof(rp_job_desc, source), offsetof(rp_job_result, t_submit_ms),
+             sizeof(rp_server_stats), offsetof(rp_server_stats, idle_wall_ms));
       return 0; }
     '''
     with tempfile.TemporaryDirectory() as d:
@@ -95,3 +96,5 @@ def test_struct_layouts_match_the_header():
     assert more[3] == ctypes.sizeof(_native.JobResult)
     assert more[4] == _native.JobDesc.source.offset
     assert more[5] == _native.JobResult.t_submit_ms.offset
+    assert more[6] == ctypes.sizeof(_native.ServerStats)
+    assert more[7] == _native.ServerStats.idle_wall_ms.offset
