@@ -190,6 +190,29 @@ def pipe_peaks(lib, device):
                    "best of 3 launches timed with CUDA events"}
 
 
+def host_link(lib, device):
+    """The host link's D2H / H2D copy rates measured on this device by the
+    library (rp_measure_host_link), the bound of the e2e leg."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    if lib.rp_measure_host_link(device, ctypes.byref(a), ctypes.byref(b)) != 0:
+        return None
+    return {"d2h_gbs": a.value / 1e9, "h2d_gbs": b.value / 1e9,
+            "how": "rp_measure_host_link: one 256 MB cudaMemcpyAsync each way with page-locked host memory, "
+                   "best of 3 after a warm-up, CUDA events"}
+
+
+def e2e_link(h2d_bytes, d2h_bytes, step_ms, peaks):
+    """The e2e step's bound by the host link: its input's upload and its
+    generations' download at the measured copy rates (the downloads overlap
+    the trace, the upload precedes it), against the fastest timed step."""
+    link = (peaks or {}).get("host_link")
+    if not link or not link["d2h_gbs"] or not link["h2d_gbs"]:
+        return None
+    bound_ms = h2d_bytes / (link["h2d_gbs"] * 1e6) + d2h_bytes / (link["d2h_gbs"] * 1e6)
+    return {"bound_ms": bound_ms, "min_step_ms": step_ms, "frac": bound_ms / step_ms,
+            "d2h_gbs": link["d2h_gbs"], "h2d_gbs": link["h2d_gbs"]}
+
+
 def kernel_rooflines(flags, st, n_first, hbm_peak, hbm_kind, peaks):
     """Achieved HBM bandwidth (algorithmic bytes over the kernel's summed
     launch time) and, for the plain kernel, FP64 throughput, each against its
@@ -383,6 +406,8 @@ def main():
     # rooflines of the generation kernels
     peak, peak_kind = measured_peak_hbm()
     peaks = pipe_peaks(lib, device)
+    if peaks is not None:
+        peaks["host_link"] = host_link(lib, device)
     krl = kernel_rooflines(flags, stats, n * args.steps, peak, peak_kind, peaks)
     if other is not None:
         krl += kernel_rooflines(1 - flags, ost, n * args.steps, peak, peak_kind, peaks)
@@ -754,7 +779,9 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
             "e2e": ({"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 188,
                      "d2h_bytes_per_step": int(d2h / e2e_steps["steps"]), "steps": e2e_steps["steps"],
                      "api": "rp_trace_rays_host (pinned host records in and out)",
-                     "step_ms": {k: e2e_steps[k] for k in ("min", "median", "max")}} if e2e_value else None),
+                     "step_ms": {k: e2e_steps[k] for k in ("min", "median", "max")},
+                     "host_link": e2e_link(n * 188, d2h / e2e_steps["steps"], e2e_steps["min"], peaks)}
+                    if e2e_value else None),
             "roofline": {"bound": "hbm", "achieved": dom["hbm"]["achieved_gbs"], "peak": dom["hbm"]["peak_gbs"],
                          "unit": "GB/s", "frac": dom["hbm"]["frac"], "traffic": dom["traffic_bytes_per_launch"],
                          "kernel": dom["kernel"],

@@ -501,6 +501,11 @@ int rp_rays_project_to_sphere(rp_rays *rays, const double *centre, double radius
  * from many independent chains per thread timed with CUDA events (best of
  * three launches after a warm-up).  Takes about a tenth of a second. */
 int rp_measure_peaks(int device, double *fp64_flops, double *fp32_flops, double *int32_ops);
+/* The host link's copy rates in bytes per second, device to page-locked host
+ * memory and back (one 256 MB cudaMemcpyAsync each way, best of three after a
+ * warm-up, CUDA events): the bound of the host-buffer entry points, which
+ * move every generation over it. */
+int rp_measure_host_link(int device, double *d2h_bytes_per_s, double *h2d_bytes_per_s);
 
 /* ---- differentiable sequential lens ------------------------------------- */
 /* No counterpart in the reference: raypier has no gradients.  A stack of even

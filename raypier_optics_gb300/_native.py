@@ -225,6 +225,7 @@ _SIGS = {
     "rp_gausslets_total_power": (_I, [_P, ctypes.POINTER(ctypes.c_double)]),
     "rp_measure_peaks": (_I, [_I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                               ctypes.POINTER(ctypes.c_double)]),
+    "rp_measure_host_link": (_I, [_I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "rp_select_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
     "rp_select_gausslet_intersections": (_I, [_P, _P, ctypes.c_int32, _P, _P, ctypes.c_uint32]),
     "rp_trace_gausslet_segment": (_I, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _P,

@@ -104,3 +104,47 @@ extern "C" int rp_measure_peaks(int device, double *fp64_flops, double *fp32_flo
     *int32_ops = ri;
     return RP_OK;
 }
+
+// Host-link copy rates: one cudaMemcpyAsync of RP_LINK_BYTES between device
+// memory and page-locked host memory each way, best of three after a warm-up,
+// timed with CUDA events.  The end-to-end entry points move every generation
+// over this link, so its rate bounds them.
+#define RP_LINK_BYTES ((size_t)256 << 20)
+
+extern "C" int rp_measure_host_link(int device, double *d2h_bytes_per_s, double *h2d_bytes_per_s) {
+    if (!d2h_bytes_per_s || !h2d_bytes_per_s) return RP_ERR_INVALID;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "cudaSetDevice");
+    void *d = nullptr, *h = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    e = cudaMalloc(&d, RP_LINK_BYTES);
+    if (e == cudaSuccess) e = cudaHostAlloc(&h, RP_LINK_BYTES, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMemset(d, 0, RP_LINK_BYTES);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float best[2] = {0.0f, 0.0f};
+    for (int dir = 0; dir < 2 && e == cudaSuccess; dir++) {
+        for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {  // the first copy is the warm-up
+            e = cudaEventRecord(e0, st);
+            if (e == cudaSuccess)
+                e = dir == 0 ? cudaMemcpyAsync(h, d, RP_LINK_BYTES, cudaMemcpyDeviceToHost, st)
+                             : cudaMemcpyAsync(d, h, RP_LINK_BYTES, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e == cudaSuccess && rep > 0 && (best[dir] == 0.0f || ms < best[dir])) best[dir] = ms;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    if (h) cudaFreeHost(h);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return rp__cuda_fail(e, "host link copies");
+    *d2h_bytes_per_s = best[0] > 0.0f ? RP_LINK_BYTES / (best[0] * 1e-3) : 0.0;
+    *h2d_bytes_per_s = best[1] > 0.0f ? RP_LINK_BYTES / (best[1] * 1e-3) : 0.0;
+    return RP_OK;
+}
