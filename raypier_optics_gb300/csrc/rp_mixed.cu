@@ -26,6 +26,7 @@
 // The TU is compiled with FMA contraction on.  Index fields agree with the
 // FP64 oracle except for rays that graze an aperture edge or a face, which is
 // why parity for this path is statistical (see the precision report).
+#include <cuda_fp16.h>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -1635,6 +1636,15 @@ __device__ __forceinline__ void queue_insert(float te, int f, float &q0, float &
     }
 }
 
+// A thread's box-entry table in shared memory: face f's entry at
+// tb[f * RP_BLOCK], as FP32, or as FP16 rounded down (a lower bound: the
+// nearest-first order and its stopping test stay valid) for tables of more
+// than 32 faces, which then still take 16 KB a block at most.
+__device__ __forceinline__ void tb_put(float *tb, int f, float te) { tb[f * RP_BLOCK] = te; }
+__device__ __forceinline__ void tb_put(__half *tb, int f, float te) { tb[f * RP_BLOCK] = __float2half_rd(te); }
+__device__ __forceinline__ float tb_get(const float *tb, int f) { return tb[f * RP_BLOCK]; }
+__device__ __forceinline__ float tb_get(const __half *tb, int f) { return __half2float(tb[f * RP_BLOCK]); }
+
 // Position of the r-th (from 0) set bit of m; m has more than r set bits.
 __device__ __forceinline__ unsigned nth_set_bit(unsigned m, unsigned r) {
     unsigned pos = 0;
@@ -1670,11 +1680,11 @@ __device__ __forceinline__ bool makes_children(const DevScene &S, int f) {
 // The nearest hit of one ray (origin and direction od[0..5], its record src
 // of A.in for the FP64 faces): culled nearest-first FP32 candidates among the
 // specialised faces, the winner (and a close second) refined in float-float,
-// then the faces left to the FP64 path.  tb is the thread's box-entry table
-// (TB) in shared memory.
-template <bool FB, bool TB>
+// then the faces left to the FP64 path.  tb is the thread's table of the box
+// entries of the first 64 faces in shared memory (tb_put / tb_get).
+template <bool FB, typename TbT>
 __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene &S, const mx::MxList *ml,
-                                               const mx::MxFace *mf, float *tb, float max_len, const double *od,
+                                               const mx::MxFace *mf, TbT *tb, float max_len, const double *od,
                                                unsigned long long src) {
     using namespace mx;
     Best b;
@@ -1727,7 +1737,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         int f0 = -1, f1 = -1, f2 = -1;
         for (int f = 0; f < nmask; f++) {
             const float te = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-            if constexpr (TB) tb[f * RP_BLOCK] = te;
+            tb_put(tb, f, te);
             if (te <= lim0) {
                 cand |= 1ull << f;
                 queue_insert(te, f, q0, q1, q2, f0, f1, f2);
@@ -1741,12 +1751,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
                 f1 = f2 = -1;
                 for (unsigned long long m = cand; m; m &= m - 1) {
                     const int f = __ffsll((long long)m) - 1;
-                    float tf;
-                    if constexpr (TB)
-                        tf = tb[f * RP_BLOCK];
-                    else
-                        tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                    queue_insert(tf, f, q0, q1, q2, f0, f1, f2);
+                    queue_insert(tb_get(tb, f), f, q0, q1, q2, f0, f1, f2);
                 }
             }
             // the front of the register queue: no candidate left in `cand`
@@ -1795,12 +1800,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         for (int f = 0; FB && f < nf; f++) {
             if (f < nmask) {
                 if (!((pend >> f) & 1ull)) continue;
-                float tf;
-                if constexpr (TB)
-                    tf = tb[f * RP_BLOCK];
-                else
-                    tf = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
-                if (tf > b.len.hi * 1.000001f + 1e-4f) continue;
+                if (tb_get(tb, f) > b.len.hi * 1.000001f + 1e-4f) continue;
             } else {
                 if (mf[f].spec) continue;
                 if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f)
@@ -1831,14 +1831,14 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
 // Dynamic shared memory: the plain kernel's tables, the mixed tables at
 // mx_off, each thread's box-entry distance per culled face at tb_off, the
 // warps' input buffers at in_off and pass-through buffers at pass_off.
-// TB: the box-entry distances are kept per thread in shared memory (scenes of
-// up to RP_MX_TB_FACES faces: 16 KB a block, three blocks still fit an SM);
-// larger scenes recompute them when the queue of nearest entries is refilled,
-// so that their blocks are not limited to two per SM by that table (a 41-face
-// system, 1M rays: search 4.04 ms recomputing against 4.19 ms with a 64-face
-// table; a 21-face one: 2.83 ms with the table against 3.10 recomputing).
-#define RP_MX_TB_FACES 32
-template <bool FB, bool TB>
+// TbT: the type of the box-entry table (tb_put), which the refills of the
+// queue of nearest entries read instead of entering the boxes again: FP32
+// for scenes of up to RP_MX_TB_F32_FACES faces, FP16 above (the first 64
+// faces; 16 KB a block, so three blocks still fit an SM).  The FP16 table's
+// conversions cost about 2 % of the search on an 11-face scene; a 41-face
+// scene's search takes 15 % less with it than re-entering the boxes.
+#define RP_MX_TB_F32_FACES 32
+template <bool FB, typename TbT>
 __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
     mixed_search_kernel(GenArgs A, unsigned mx_off, unsigned tb_off, unsigned in_off, unsigned pass_off) {
     using namespace mx;
@@ -1851,7 +1851,7 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
     DevScene S = stage_tables(A, smem, &s_counts);
     MxList *ml = reinterpret_cast<MxList *>(smem + mx_off);
     MxFace *mf = reinterpret_cast<MxFace *>(ml + A.S.n_lists);
-    float *tb = reinterpret_cast<float *>(smem + tb_off) + threadIdx.x;  // tb[f * RP_BLOCK]
+    TbT *tb = reinterpret_cast<TbT *>(smem + tb_off) + threadIdx.x;  // tb[f * RP_BLOCK]
     const float max_len = f_of_d(A.max_len);  // exact: max_length is a float
     stage_mixed(A, ml, mf, max_len);
     if (threadIdx.x == 0) s_hits = 0;
@@ -1895,7 +1895,7 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
 
         if (active) {
             const double od[6] = {in.ox[t], in.oy[t], in.oz[t], in.dx[t], in.dy[t], in.dz[t]};
-            const Best b = nearest_mx<FB, TB>(A, S, ml, mf, tb, max_len, od, src);
+            const Best b = nearest_mx<FB, TbT>(A, S, ml, mf, tb, max_len, od, src);
             const double len64 = d_of_ff(b.len);
             const unsigned endf = b.face >= 0 ? (unsigned)S.faces[b.face].idx : 0xFFFFFFFFu;
             if (gathered) {
@@ -2264,6 +2264,8 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
     extern __shared__ __align__(16) unsigned char smem[];
     const unsigned lane = threadIdx.x & 31;
     TileIn *bufs = reinterpret_cast<TileIn *>(smem + in_off) + 2 * (threadIdx.x >> 5);
+    // each thread's box entries of the first 64 faces of its ray's job, after the input buffers
+    __half *tb = reinterpret_cast<__half *>(smem + in_off + 2 * RP_SUB_PER_BLOCK * sizeof(TileIn)) + threadIdx.x;
     const unsigned subs = RP_GROUP / RP_SUB;
     const unsigned long long n_sub = (unsigned long long)Bt->total_units * subs;
     // global sub-tile -> job and this lane's ray (~0 past the job's rays)
@@ -2299,9 +2301,9 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
         if (i != ~0ull) {
             const TileIn &in = bufs[k & 1];
             const double od[6] = {in.ox[lane], in.oy[lane], in.oz[lane], in.dx[lane], in.dy[lane], in.dz[lane]};
-            const Best b = nearest_mx<false, false>(A, A.S, static_cast<const MxList *>(J.mx_lists),
-                                                    static_cast<const MxFace *>(J.mx_faces), nullptr,
-                                                    f_of_d(A.max_len), od, i);
+            const Best b = nearest_mx<false, __half>(A, A.S, static_cast<const MxList *>(J.mx_lists),
+                                                     static_cast<const MxFace *>(J.mx_faces), tb, f_of_d(A.max_len),
+                                                     od, i);
             A.in.len[i] = d_of_ff(b.len);
             A.in.endf[i] = b.face >= 0 ? (unsigned)A.S.faces[b.face].idx : 0xFFFFFFFFu;
             if (A.emit) {
@@ -2445,7 +2447,7 @@ static cudaError_t resident_grid(K kernel, size_t total, int *blocks) {
 
 struct MixedLayout {
     size_t mx_off, tb_off, in_off, pass_off, search_total, mat_buf_off, mat_total;
-    bool tb;  // the search kernel keeps box entries in shared memory
+    bool tb;  // the search kernel's box-entry table is FP32 (else FP16)
 };
 
 static MixedLayout mixed_layout(const GenArgs &a, size_t smem) {
@@ -2454,9 +2456,9 @@ static MixedLayout mixed_layout(const GenArgs &a, size_t smem) {
     L.tb_off = L.mx_off + mx::mx_tables_bytes(a.S.n_lists, a.S.n_faces);
     L.mat_buf_off = (L.tb_off + 15) & ~(size_t)15;
     L.mat_total = L.mat_buf_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::MatIn);
-    L.tb = a.S.n_faces <= RP_MX_TB_FACES;
-    const int nmask = L.tb ? a.S.n_faces : 0;
-    L.in_off = (L.tb_off + (size_t)nmask * RP_BLOCK * sizeof(float) + 15) & ~(size_t)15;
+    L.tb = a.S.n_faces <= RP_MX_TB_F32_FACES;  // an FP32 table (else FP16)
+    const int nmask = a.S.n_faces < 64 ? a.S.n_faces : 64;
+    L.in_off = (L.tb_off + (size_t)nmask * RP_BLOCK * (L.tb ? sizeof(float) : sizeof(__half)) + 15) & ~(size_t)15;
     L.pass_off = L.in_off + 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
     L.search_total = L.pass_off + (a.in_map ? RP_SUB_PER_BLOCK * sizeof(mx::PassIn) : 0);
     return L;
@@ -2465,11 +2467,11 @@ static MixedLayout mixed_layout(const GenArgs &a, size_t smem) {
 static cudaError_t mixed_grids(const GenArgs &a, const MixedLayout &L, int *search_blocks, int *mat_blocks) {
     cudaError_t e;
     if (L.tb)
-        e = a.mixed_fallback ? resident_grid(mixed_search_kernel<true, true>, L.search_total, search_blocks)
-                             : resident_grid(mixed_search_kernel<false, true>, L.search_total, search_blocks);
+        e = a.mixed_fallback ? resident_grid(mixed_search_kernel<true, float>, L.search_total, search_blocks)
+                             : resident_grid(mixed_search_kernel<false, float>, L.search_total, search_blocks);
     else
-        e = a.mixed_fallback ? resident_grid(mixed_search_kernel<true, false>, L.search_total, search_blocks)
-                             : resident_grid(mixed_search_kernel<false, false>, L.search_total, search_blocks);
+        e = a.mixed_fallback ? resident_grid(mixed_search_kernel<true, __half>, L.search_total, search_blocks)
+                             : resident_grid(mixed_search_kernel<false, __half>, L.search_total, search_blocks);
     if (e != cudaSuccess) return e;
     return a.mixed_fallback ? resident_grid(mixed_material_kernel<true>, L.mat_total, mat_blocks)
                             : resident_grid(mixed_material_kernel<false>, L.mat_total, mat_blocks);
@@ -2503,14 +2505,14 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
     const unsigned o1 = (unsigned)L.mx_off, o2 = (unsigned)L.tb_off, o3 = (unsigned)L.in_off, o4 = (unsigned)L.pass_off;
     if (L.tb) {
         if (a.mixed_fallback)
-            mixed_search_kernel<true, true><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+            mixed_search_kernel<true, float><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
         else
-            mixed_search_kernel<false, true><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+            mixed_search_kernel<false, float><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
     } else {
         if (a.mixed_fallback)
-            mixed_search_kernel<true, false><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+            mixed_search_kernel<true, __half><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
         else
-            mixed_search_kernel<false, false><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
+            mixed_search_kernel<false, __half><<<sgrid, RP_BLOCK, L.search_total, st>>>(a, o1, o2, o3, o4);
     }
     e = cudaGetLastError();
     if (e == cudaSuccess && mid) e = cudaEventRecord(mid, st);
@@ -2529,9 +2531,10 @@ cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t 
 
 
 // Shared memory and resident grids of the batch kernels (their tables come
-// from global memory: only the warps' input buffers are in shared memory).
+// from global memory: the warps' input buffers and, for the search, each
+// thread's box entries of up to 64 faces are in shared memory).
 cudaError_t prepare_batch_mixed(size_t *search_smem, size_t *mat_smem, int *search_blocks, int *mat_blocks) {
-    *search_smem = 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn);
+    *search_smem = 2 * RP_SUB_PER_BLOCK * sizeof(mx::TileIn) + 64 * RP_BLOCK * sizeof(__half);
     *mat_smem = 2 * RP_SUB_PER_BLOCK * sizeof(mx::MatIn);
     cudaError_t e = resident_grid(mixed_search_batch_kernel, *search_smem, search_blocks);
     if (e != cudaSuccess) return e;
