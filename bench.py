@@ -86,6 +86,7 @@ def parse():
     ap.add_argument("--rays", type=int, default=0, help="override the ray count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--e2e-steps", type=int, default=30, help="timed steps of the end-to-end leg (at least --steps)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the second path's leg (plain FP64 when the "
                     "headline is mixed, mixed when it is plain) and the precision sample")
     ap.add_argument("--cpu-sample", type=int, default=0, help="rays in the CPU-baseline sample")
@@ -436,6 +437,10 @@ def main():
 
 
 def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, seg_per_step, dist, world):
+    """rp_trace_rays_host on pinned host records, --e2e-steps timed calls (at
+    least --steps): each step's ~11 GB of generations cross the host link,
+    which other work on the machine can hold up for a few hundred ms, so
+    more steps keep one such stall from setting the mean."""
     from raypier_optics_gb300 import _native
     # output capacity: the measured segment count of a step plus headroom
     out_cap = int(seg_per_step * 1.05) + n
@@ -445,7 +450,7 @@ def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, s
     _native.check(lib.rp_host_alloc(out_cap * 188, ctypes.byref(pin_out)), "rp_host_alloc")
     ctypes.memmove(pin_in, np.ascontiguousarray(rays).ctypes.data, n * 188)
     offs = (ctypes.c_uint64 * (max_gens + 1))()
-    e2e_steps = max(1, args.steps)
+    e2e_steps = max(1, args.steps, args.e2e_steps)
 
     def e2e_step(st):
         ng = ctypes.c_int32(0)
