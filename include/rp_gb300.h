@@ -295,6 +295,12 @@ int rp_scene_face_counts(rp_scene *scene, uint32_t *counts, int32_t n_faces, int
  * reference, which tests every face).  out[8*f .. 8*f+5] = lo xyz, hi xyz,
  * out[8*f+6] = 1 if face f may be skipped, 0 if it is always tested. */
 int rp_scene_bounds(const rp_scene_desc *desc, float *out, int32_t n_faces);
+/* Host-only: the boxes of the mixed path's search, 16 floats per face:
+ * out[16*f .. 16*f+7] as rp_scene_bounds and, for a ConicRevolutionFace, the
+ * boxes of its two sheets' parts over the aperture in out[16*f .. +7] and
+ * out[16*f+8 .. +15] (out[16*f+6] = 3 when the two boxes are set; a ray
+ * that may hit the face enters one of them). */
+int rp_scene_mixed_bounds(const rp_scene_desc *desc, float *out, int32_t n_faces);
 
 /* ---- device ray buffers (structure-of-arrays) ---------------------------- */
 int rp_rays_alloc(rp_ctx *ctx, uint64_t capacity, rp_rays **out);

@@ -116,6 +116,28 @@ inline bool conic_z_range(double R, double beta, double rmax, double &z0, double
     return true;
 }
 
+// The same z values by sheet: [a0, a1] for the sheet through the vertex
+// (z = 0 at r = 0) and [b0, b1] for the other one, whose points the reference
+// also returns when its choice of root falls on them.  Each root is monotonic
+// in r^2, so its range lies between its values at r = 0 and r = rmax.  False
+// for a paraboloid (one sheet) or a non-finite input.
+inline bool conic_sheet_ranges(double R, double beta, double rmax, double &a0, double &a1, double &b0,
+                               double &b1) {
+    if (!(std::isfinite(R) && std::isfinite(beta) && std::isfinite(rmax)) || beta == 0.0 || R == 0.0) return false;
+    double r2max = rmax * rmax;
+    if (beta > 0) r2max = std::min(r2max, R * R / beta);
+    const double d0 = std::fabs(R), d1 = std::sqrt(std::max(R * R - beta * r2max, 0.0));
+    // the vertex sheet takes the root R - sign(R) sqrt(disc): 0 at r = 0
+    const double s = R > 0 ? -1.0 : 1.0;
+    const double va0 = (R + s * d0) / beta, va1 = (R + s * d1) / beta;
+    const double vb0 = (R - s * d0) / beta, vb1 = (R - s * d1) / beta;
+    a0 = std::min(va0, va1);
+    a1 = std::max(va0, va1);
+    b0 = std::min(vb0, vb1);
+    b1 = std::max(vb0, vb1);
+    return std::isfinite(a0) && std::isfinite(a1) && std::isfinite(b0) && std::isfinite(b1);
+}
+
 // Local-frame box of face record `f`; returns false if the face is not bounded.
 inline bool face_local_box(const rp_scene_desc *d, const rp_face &f, double lo[3], double hi[3]) {
     const double *p = f.p;
@@ -338,6 +360,33 @@ inline void world_from_local(const rp_facelist &L, const double lo[3], const dou
         out[3 + k] = (float)(w1[k] + pad);
     }
     out[6] = 1.0f;
+}
+
+// The boxes of the mixed path's search: out[0..7] as face_world_box and, for a
+// ConicRevolutionFace, out[0..7] and out[8..15] the world boxes of its two
+// sheets' parts over the aperture (out[6] = 3 when the two boxes are set):
+// each a thin slab where the union of both can span hundreds of millimetres,
+// so a ray that starts between the sheets enters neither.  A face's entry
+// distance is the nearer of its boxes' entries.
+inline void face_world_boxes(const rp_scene_desc *d, const rp_facelist &L, const rp_face &f, float out[16]) {
+    for (int k = 0; k < 16; k++) out[k] = 0.0f;
+    face_world_box(d, L, f, out);
+    if (f.type != RP_FACE_CONIC || out[6] != 1.0f) return;
+    const Box2 b = shape_box(d, f.shape);
+    double a0, a1, b0, b1;
+    if (!b.bounded || !conic_sheet_ranges(-f.p[0], 1 + f.p[2], b.rmax, a0, a1, b0, b1)) return;
+    float wa[8] = {0}, wb[8] = {0};
+    double lo[3] = {b.x0, b.y0, a0 + f.p[1]}, hi[3] = {b.x1, b.y1, a1 + f.p[1]};
+    world_from_local(L, lo, hi, wa);
+    lo[2] = b0 + f.p[1];
+    hi[2] = b1 + f.p[1];
+    world_from_local(L, lo, hi, wb);
+    if (wa[6] != 1.0f || wb[6] != 1.0f) return;  // keep the single box
+    for (int k = 0; k < 8; k++) {
+        out[k] = wa[k];
+        out[8 + k] = wb[k];
+    }
+    out[6] = 3.0f;
 }
 
 }  // namespace rp

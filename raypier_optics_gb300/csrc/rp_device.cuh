@@ -30,6 +30,12 @@ struct DevScene {
     const int *zk32_off;     // [n_dists]: offset of a distortion's table in zk32 / zk64, -1 for none
     const float *ep32;       // the mixed path's FP32 copies of the ExtendedPolynomialFace coefficient matrices
     const int *ep32_off;     // [n_recs]: offset of a face record's matrix ([Nx, Ny, E...]) in ep32, -1 for none
+    // The mixed path's search boxes (rp_bounds.h face_world_boxes), [n_faces][8]
+    // each: mxbounds as `bounds` but a ConicRevolutionFace's first sheet with
+    // flag 3, whose second sheet's box is in mxbox2; the mixed kernels are
+    // launched with bounds = mxbounds.
+    const float *mxbounds;
+    const float *mxbox2;
     long long n_wl;
     int n_lists, n_faces, n_recs, n_mats, n_shapes, n_dists;
 };

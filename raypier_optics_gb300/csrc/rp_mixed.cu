@@ -1593,9 +1593,11 @@ __device__ __forceinline__ unsigned map_entry(const GenArgs &A, unsigned tile, u
 
 }  // namespace mx
 
+// A ray's entry distance into a padded world box b (lo xyz, hi xyz;
+// rp_bounds.h): the FP32 slab test with the inverse direction (ix, iy, iz),
+// infinity when the ray misses the box or it lies behind.
 __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
                                               float iz) {
-    if (b[6] != 1.0f) return 0.0f;
     float t1 = (b[0] - ox) * ix, t2 = (b[3] - ox) * ix;
     float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
     t1 = (b[1] - oy) * iy;
@@ -1608,6 +1610,19 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
     tmax = fminf(tmax, fmaxf(t1, t2));
     if (!(tmax >= tmin) || tmax < 0.0f) return __int_as_float(0x7f800000);
     return fmaxf(tmin, 0.0f);
+}
+
+// A face's entry distance in the mixed search.  b: its box in the mixed
+// kernels' box table (DevScene::mxbounds, staged as S.bounds); b[6] = 1, that
+// box's entry; 3, the nearer entry of it and the face's second box b2
+// (DevScene::mxbox2); otherwise 0 (a face without a box is always tested).
+__device__ __forceinline__ float mx_face_enter(const float *b, const float *b2, float ox, float oy, float oz,
+                                               float ix, float iy, float iz) {
+    if (b[6] != 1.0f) {
+        if (b[6] != 3.0f) return 0.0f;
+        return fminf(mx_box_enter(b, ox, oy, oz, ix, iy, iz), mx_box_enter(b2, ox, oy, oz, ix, iy, iz));
+    }
+    return mx_box_enter(b, ox, oy, oz, ix, iy, iz);
 }
 
 
@@ -1736,7 +1751,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         float q0 = INF, q1 = INF, q2 = INF;
         int f0 = -1, f1 = -1, f2 = -1;
         for (int f = 0; f < nmask; f++) {
-            const float te = mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+            const float te = mx_face_enter(S.bounds + 8 * f, S.mxbox2 + 8 * f, ox, oy, oz, ix, iy, iz);
             tb_put(tb, f, te);
             if (te <= lim0) {
                 cand |= 1ull << f;
@@ -1783,8 +1798,8 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         }
         for (int f = nmask; f < nf; f++) {
             if (!mf[f].spec) continue;
-            if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > fmaf(c1.d, 1.000244140625f, 1e-3f))
-                continue;
+            const float te = mx_face_enter(S.bounds + 8 * f, S.mxbox2 + 8 * f, ox, oy, oz, ix, iy, iz);
+            if (te > fmaf(c1.d, 1.000244140625f, 1e-3f)) continue;
             int l = S.face_list[f];
             if (l < 0 || l >= S.n_lists) {
                 atomicOr(A.err, ERR_SHAPE_STACK);
@@ -1803,8 +1818,8 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
                 if (tb_get(tb, f) > b.len.hi * 1.000001f + 1e-4f) continue;
             } else {
                 if (mf[f].spec) continue;
-                if (mx_box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > b.len.hi * 1.000001f + 1e-4f)
-                    continue;
+                const float te = mx_face_enter(S.bounds + 8 * f, S.mxbox2 + 8 * f, ox, oy, oz, ix, iy, iz);
+                if (te > b.len.hi * 1.000001f + 1e-4f) continue;
             }
             int l = S.face_list[f];
             if (l < 0 || l >= S.n_lists) {
@@ -2491,8 +2506,10 @@ cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem) {
 // kernel.  The scene's faces and materials decide the instantiation: without
 // FP64 fallbacks the kernels carry no out-of-line calls and their register
 // cost.  The caller has zeroed the tile and group counters.
-cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st, cudaEvent_t mid) {
-    if (a.n_in == 0) return cudaSuccess;
+cudaError_t launch_generation_mixed(const GenArgs &args, size_t smem, cudaStream_t st, cudaEvent_t mid) {
+    if (args.n_in == 0) return cudaSuccess;
+    GenArgs a = args;
+    if (a.S.mxbounds) a.S.bounds = a.S.mxbounds;  // the search's boxes (DevScene::mxbounds)
     if (a.emit && (!a.hit_t || !a.hit_face || !a.group_next || a.unit_rays != RP_GROUP))
         return cudaErrorInvalidValue;  // the hand-over and the group unit are set up by the caller
     const MixedLayout L = mixed_layout(a, smem);

@@ -21,6 +21,36 @@ def boxes(tables):
     return out
 
 
+def mixed_boxes(tables):
+    lib = _native.load()
+    out = np.zeros((tables.n_faces, 16), dtype=np.float32)
+    d = tables.desc()
+    assert lib.rp_scene_mixed_bounds(ctypes.byref(d), out.ctypes.data, tables.n_faces) == 0
+    return out
+
+
+def check_hits_inside_mixed(tables, gens):
+    """Every hit on a face with search boxes lies in one of them (the mixed
+    path's search enters a face at the nearer of its boxes; flag 3: two)."""
+    b = mixed_boxes(tables)
+    idx_of = {int(f["idx"]): k for k, f in enumerate(tables.faces[:tables.n_faces])}
+    n_checked = 0
+    for g in gens:
+        hit = g["end_face_idx"] != 0xFFFFFFFF
+        pts = g["origin"][hit] + g["direction"][hit] * g["length"][hit][:, None]
+        recs = np.array([idx_of[int(i)] for i in g["end_face_idx"][hit]], dtype=np.int64)
+        for k in np.unique(recs):
+            if b[k, 6] not in (1, 3):
+                continue
+            p = pts[recs == k]
+            inside = np.all((p >= b[k, 0:3].astype(np.float64)) & (p <= b[k, 3:6].astype(np.float64)), axis=1)
+            if b[k, 6] == 3:
+                inside |= np.all((p >= b[k, 8:11].astype(np.float64)) & (p <= b[k, 11:14].astype(np.float64)), axis=1)
+            assert inside.all(), f"face record {k}: {np.count_nonzero(~inside)} hits outside its search boxes"
+            n_checked += len(p)
+    return n_checked
+
+
 def line_misses(b, p1, u):
     """The kernels' distortion-face cull restated: the line p1 + s u (local
     frame) never passes over the rectangle b[0..3] = x0, x1, y0, y1."""
@@ -74,6 +104,7 @@ def test_golden_hits_lie_in_face_boxes(name):
     c = load_case(name)
     tables, _, _ = tables_for(c["spec"])
     check_hits_inside(tables, c["gens"])
+    check_hits_inside_mixed(tables, c["gens"])
 
 
 @pytest.mark.parametrize("config", ["config1", "config2", "config3"])
@@ -91,6 +122,7 @@ def test_benchmark_hits_lie_in_face_boxes(config):
     tables, _, _ = tables_for(spec)
     gens, _ = oracle.trace_rays(tables, wl, rays, P["recursion_limit"], P["max_length"], P["e2_terminate"])
     assert check_hits_inside(tables, gens) > 0
+    assert check_hits_inside_mixed(tables, gens) > 0
 
 
 def test_boxes_are_tight_for_axis_aligned_faces():
@@ -124,3 +156,68 @@ def test_curved_face_boxes_hold_on_dense_samples(name):
     assert boxes(tables)[0, 6] == 1
     gens, _ = oracle.trace_rays(tables, np.array([0.55]), rays, 4, 200.0, 0.0)
     assert check_hits_inside(tables, gens) > 100
+
+
+def dense_rays(n, seed, spread=16.0, z_below=-10.0, z_above=45.0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    th = rng.uniform(0.0, 0.6, n)
+    ph = rng.uniform(0.0, 2 * np.pi, n)
+    up = rng.uniform(size=n) < 0.5
+    d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.where(up, 1.0, -1.0) * np.cos(th)], axis=1)
+    o = np.stack([rng.uniform(-spread, spread, n), rng.uniform(-spread, spread, n), np.where(up, z_below, z_above)],
+                 axis=1)
+    e = np.cross(np.array([0.0, 1.0, 0.0]), d)
+    e /= np.linalg.norm(e, axis=1)[:, None]
+    return W.fill_rays(np.zeros(n, dtype=ctracer.ray_dtype), o, d, e)
+
+
+@pytest.mark.parametrize("name", ["conic_mirror", "conic_inv"])
+def test_conic_sheet_boxes_hold_on_dense_samples(name):
+    """A conic face's two sheet boxes: 4096 seeded rays from both sides and
+    from between the sheets; every hit the oracle reports lies in one of the
+    face's boxes, and the boxes are split (each far thinner than their union)."""
+    from helpers import load_face_specs
+    spec = load_face_specs()[name]
+    tables, _, _ = tables_for(spec)
+    mb, ub = mixed_boxes(tables), boxes(tables)
+    assert mb[0, 6] == 3
+    union_dz = ub[0, 5] - ub[0, 2]
+    assert mb[0, 5] - mb[0, 2] < 0.5 * union_dz and mb[0, 13] - mb[0, 10] < 0.5 * union_dz
+    n_checked = 0
+    for seed, zb, za in ((5, -10.0, 45.0), (6, float(ub[0, 2]) - 5.0, float(ub[0, 5]) + 5.0),
+                         (7, 0.5 * float(ub[0, 2] + ub[0, 5]), 0.5 * float(ub[0, 2] + ub[0, 5]))):
+        rays = dense_rays(4096, seed, z_below=zb, z_above=za)
+        gens, _ = oracle.trace_rays(tables, np.array([0.55]), rays, 4, 5000.0, 0.0)
+        n_checked += check_hits_inside_mixed(tables, gens)
+    assert n_checked > 100
+
+
+def test_conic_sheet_ranges_cover_the_quadric():
+    """The sheet ranges of conic faces of the served mix and the clutter scene
+    (k in [-2, 0.5], |R| 20-400 mm): every point of the quadric over the
+    aperture, sampled densely on both roots, lies in its sheet's box."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    n_split = 0
+    for _ in range(64):
+        R = float(rng.uniform(20.0, 400.0)) * (1.0 if rng.uniform() < 0.5 else -1.0)
+        k = float(rng.uniform(-2.0, 0.5))
+        spec = {"materials": {"m": {"type": "PECMaterial"}},
+                "lists": [{"faces": [{"type": "ConicRevolutionFace",
+                                      "kw": {"curvature": R, "z_height": 0.0, "conic_const": k},
+                                      "shape": {"type": "CircleShape", "kw": {"radius": 12.5}},
+                                      "material": "m"}]}]}
+        tables, _, _ = tables_for(spec)
+        mb = mixed_boxes(tables)[0]
+        if mb[6] != 3:
+            continue
+        n_split += 1
+        beta, Rq = 1.0 + k, -R  # the face's quadric: beta z^2 - 2 Rq z + r^2 = 0 (rp_bounds.h)
+        r = np.linspace(0.0, 12.5, 2001)
+        disc = Rq * Rq - beta * r * r
+        ok = disc >= 0
+        for sign in (1.0, -1.0):
+            z = (Rq + sign * np.sqrt(disc[ok])) / beta
+            in_a = (z >= mb[2]) & (z <= mb[5])
+            in_b = (z >= mb[10]) & (z <= mb[13])
+            assert np.all(in_a | in_b), (R, k, sign)
+    assert n_split > 48
