@@ -290,17 +290,20 @@ int rp_scene_destroy(rp_scene *scene);
  * ctracer.pyx:2108). counts has n_faces entries. */
 int rp_scene_face_counts(rp_scene *scene, uint32_t *counts, int32_t n_faces, int reset);
 
-/* Host-only: the world-space boxes the nearest-hit search uses to skip faces a
- * ray cannot reach before its current nearest hit (no counterpart in the
- * reference, which tests every face).  out[8*f .. 8*f+5] = lo xyz, hi xyz,
- * out[8*f+6] = 1 if face f may be skipped, 0 if it is always tested. */
+/* Host-only: one world-space box per face that holds every point where the
+ * face can report a hit (no counterpart in the reference, which tests every
+ * face): out[8*f .. 8*f+5] = lo xyz, hi xyz, out[8*f+6] = 1 if face f may be
+ * skipped, 0 if it is always tested (2: a distortion face's local rectangle).
+ * For a conic face it spans both sheets; the searches use
+ * rp_scene_search_bounds. */
 int rp_scene_bounds(const rp_scene_desc *desc, float *out, int32_t n_faces);
-/* Host-only: the boxes of the mixed path's search, 16 floats per face:
- * out[16*f .. 16*f+7] as rp_scene_bounds and, for a ConicRevolutionFace, the
- * boxes of its two sheets' parts over the aperture in out[16*f .. +7] and
- * out[16*f+8 .. +15] (out[16*f+6] = 3 when the two boxes are set; a ray
- * that may hit the face enters one of them). */
-int rp_scene_mixed_bounds(const rp_scene_desc *desc, float *out, int32_t n_faces);
+/* Host-only: the boxes the nearest-hit searches use to skip faces a ray cannot
+ * reach before its current nearest hit, 16 floats per face: out[16*f ..
+ * 16*f+7] as rp_scene_bounds and, for a ConicRevolutionFace, the boxes of its
+ * two sheets' parts over the aperture in out[16*f .. +7] and out[16*f+8 ..
+ * +15] (out[16*f+6] = 3 when the two boxes are set; a ray that may hit the
+ * face enters one of them). */
+int rp_scene_search_bounds(const rp_scene_desc *desc, float *out, int32_t n_faces);
 
 /* ---- device ray buffers (structure-of-arrays) ---------------------------- */
 int rp_rays_alloc(rp_ctx *ctx, uint64_t capacity, rp_rays **out);

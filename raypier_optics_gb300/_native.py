@@ -191,7 +191,7 @@ _SIGS = {
     "rp_scene_create": (_I, [_P, ctypes.POINTER(SceneDesc), _P, ctypes.c_int64, ctypes.POINTER(_P)]),
     "rp_scene_destroy": (_I, [_P]),
     "rp_scene_bounds": (_I, [ctypes.POINTER(SceneDesc), _P, ctypes.c_int32]),
-    "rp_scene_mixed_bounds": (_I, [ctypes.POINTER(SceneDesc), _P, ctypes.c_int32]),
+    "rp_scene_search_bounds": (_I, [ctypes.POINTER(SceneDesc), _P, ctypes.c_int32]),
     "rp_scene_face_counts": (_I, [_P, _P, ctypes.c_int32, _I]),
     "rp_rays_alloc": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(_P)]),
     "rp_rays_free": (_I, [_P]),

@@ -367,7 +367,7 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
         ep32.push_back((float)F.n_aux1);
         for (int k = 0; k < F.n_aux0 * F.n_aux1; k++) ep32.push_back((float)d->aux[F.aux + k]);
     }
-    size_t o_zkoff = o_bnd + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
+    size_t o_zkoff = o_bnd + align256(sizeof(float) * 16 * (size_t)(d->n_faces + 1));
     size_t o_zkprog = o_zkoff + align256(sizeof(int) * zk_off.size());
     size_t o_fl = o_zkprog + align256(sizeof(short) * (zk_prog.size() + 1));
     size_t o_zk32off = o_fl + align256(sizeof(short) * (size_t)(d->n_faces + 1));
@@ -375,9 +375,7 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     size_t o_zk64 = o_zk32 + align256(sizeof(float) * (zk32.size() + 1));
     size_t o_ep32off = o_zk64 + align256(sizeof(double) * (zk64.size() + 1));
     size_t o_ep32 = o_ep32off + align256(sizeof(int) * ep32_off.size());
-    size_t o_mxa = o_ep32 + align256(sizeof(float) * (ep32.size() + 1));
-    size_t o_mxb = o_mxa + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
-    size_t total = o_mxb + align256(sizeof(float) * 8 * (size_t)(d->n_faces + 1));
+    size_t total = o_ep32 + align256(sizeof(float) * (ep32.size() + 1));
     // owning list of each traced face (kernels that read the tables from global memory)
     std::vector<short> face_list((size_t)d->n_faces + 1, (short)-1);
     for (int l = 0; l < d->n_lists; l++)
@@ -403,24 +401,14 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     UP(o_disp, d->dispersions, sizeof(rp_dispersion) * d->n_dispersions);
     UP(o_aux, d->aux, sizeof(double) * d->n_aux);
     UP(o_wl, wavelengths, sizeof(double) * (size_t)n_wl);
-    std::vector<float> bounds((size_t)d->n_faces * 8 + 8, 0.0f);
+    // the searches' boxes: a face's box, or a conic face's two sheet boxes (rp_bounds.h)
+    std::vector<float> bounds((size_t)d->n_faces * 16 + 16, 0.0f);
     for (int l = 0; l < d->n_lists; l++)
         for (int k = 0; k < d->lists[l].n_faces; k++) {
             int f = d->lists[l].first_face + k;
-            face_world_box(d, d->lists[l], d->faces[f], &bounds[(size_t)f * 8]);
+            face_world_boxes(d, d->lists[l], d->faces[f], &bounds[(size_t)f * 16]);
         }
-    UP(o_bnd, bounds.data(), sizeof(float) * 8 * (size_t)d->n_faces);
-    std::vector<float> mxa((size_t)d->n_faces * 8 + 8, 0.0f), mxb((size_t)d->n_faces * 8 + 8, 0.0f);
-    for (int l = 0; l < d->n_lists; l++)
-        for (int k = 0; k < d->lists[l].n_faces; k++) {
-            int f = d->lists[l].first_face + k;
-            float two[16];
-            face_world_boxes(d, d->lists[l], d->faces[f], two);
-            std::copy(two, two + 8, &mxa[(size_t)f * 8]);
-            std::copy(two + 8, two + 16, &mxb[(size_t)f * 8]);
-        }
-    UP(o_mxa, mxa.data(), sizeof(float) * 8 * (size_t)d->n_faces);
-    UP(o_mxb, mxb.data(), sizeof(float) * 8 * (size_t)d->n_faces);
+    UP(o_bnd, bounds.data(), sizeof(float) * 16 * (size_t)d->n_faces);
     UP(o_zk32off, zk32_off.data(), sizeof(int) * zk32_off.size());
     UP(o_zk32, zk32.data(), sizeof(float) * zk32.size());
     UP(o_zk64, zk64.data(), sizeof(double) * zk64.size());
@@ -449,8 +437,6 @@ int rp_scene_create(rp_ctx *ctx, const rp_scene_desc *d, const double *wavelengt
     S.zk64 = (const double *)(b + o_zk64);
     S.ep32_off = (const int *)(b + o_ep32off);
     S.ep32 = (const float *)(b + o_ep32);
-    S.mxbounds = (const float *)(b + o_mxa);
-    S.mxbox2 = (const float *)(b + o_mxb);
     S.n_wl = n_wl;
     S.wl = (const double *)(b + o_wl);
     S.n_lists = d->n_lists;
@@ -499,7 +485,7 @@ int rp_scene_bounds(const rp_scene_desc *d, float *out, int32_t n_faces) {
     return RP_OK;
 }
 
-int rp_scene_mixed_bounds(const rp_scene_desc *d, float *out, int32_t n_faces) {
+int rp_scene_search_bounds(const rp_scene_desc *d, float *out, int32_t n_faces) {
     if (!d || !out || n_faces != d->n_faces) return RP_ERR_INVALID;
     int v = validate_scene(d);
     if (v != RP_OK) return v;

@@ -21,7 +21,7 @@ struct DevScene {
     const double *aux;
     const double2 *ntab;  // [n_dispersions][n_wl] complex index per curve and wavelength
     const double *wl;     // [n_wl] the wavelengths (um)
-    const float *bounds;  // [n_faces][8]: world box lo[3], hi[3], skippable flag (rp_bounds.h)
+    const float *bounds;  // [n_faces][16]: world box lo[3], hi[3], flag, -, and a second box (flag 3; rp_bounds.h)
     const short *face_list;  // [n_faces]: owning face list of each traced face
     const short *zk_prog;    // compiled Zernike programs (rp_zkprog.h), or null
     const int *zk_off;       // [n_dists][2]: offsets of the z and z-gradient programs in zk_prog, -1 for none
@@ -30,12 +30,6 @@ struct DevScene {
     const int *zk32_off;     // [n_dists]: offset of a distortion's table in zk32 / zk64, -1 for none
     const float *ep32;       // the mixed path's FP32 copies of the ExtendedPolynomialFace coefficient matrices
     const int *ep32_off;     // [n_recs]: offset of a face record's matrix ([Nx, Ny, E...]) in ep32, -1 for none
-    // The mixed path's search boxes (rp_bounds.h face_world_boxes), [n_faces][8]
-    // each: mxbounds as `bounds` but a ConicRevolutionFace's first sheet with
-    // flag 3, whose second sheet's box is in mxbox2; the mixed kernels are
-    // launched with bounds = mxbounds.
-    const float *mxbounds;
-    const float *mxbox2;
     long long n_wl;
     int n_lists, n_faces, n_recs, n_mats, n_shapes, n_dists;
 };

@@ -37,10 +37,10 @@ __device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char
         S.mats = reinterpret_cast<const rp_material *>(dst + nl + nf);
     }
     double *tail = A.smem_tables ? dst + nl + nf + nm : dst;
-    // per-face world boxes (8 floats each), then the face -> list map, then hit counters
+    // per-face world boxes (16 floats each), then the face -> list map, then hit counters
     float *bnd = reinterpret_cast<float *>(tail);
-    for (int k = threadIdx.x; k < S.n_faces * 8; k += blockDim.x) bnd[k] = A.S.bounds[k];
-    short *fl = reinterpret_cast<short *>(bnd + S.n_faces * 8);
+    for (int k = threadIdx.x; k < S.n_faces * 16; k += blockDim.x) bnd[k] = A.S.bounds[k];
+    short *fl = reinterpret_cast<short *>(bnd + S.n_faces * 16);
     // the list ranges are read from global memory: the shared copy above is
     // not complete until the block's next barrier
     for (int l = 0; l < S.n_lists; l++) {
@@ -48,7 +48,7 @@ __device__ __forceinline__ DevScene stage_tables(const GenArgs &A, unsigned char
         for (int k = threadIdx.x; k < n; k += blockDim.x)
             if (f0 + k < S.n_faces) fl[f0 + k] = (short)l;
     }
-    unsigned *cnt = reinterpret_cast<unsigned *>(tail + (S.n_faces * 8 * 4 + S.n_faces * 2 + 7) / 8);
+    unsigned *cnt = reinterpret_cast<unsigned *>(tail + (S.n_faces * 16 * 4 + S.n_faces * 2 + 7) / 8);
     for (int k = threadIdx.x; k < S.n_faces; k += blockDim.x) cnt[k] = 0;
     S.bounds = bnd;
     S.face_list = fl;

@@ -916,7 +916,7 @@ __device__ float face_t32(const DevScene &S, const rp_face &F, const MxFace &M, 
             return MX_MISS_T;
         case RP_FACE_DISTORTION:  // (only scenes that also carry the FP64 path specialise it)
             if constexpr (DIST)
-                if (M.spec) return distortion_t32(S, F, M, R, tmax, dl, S.bounds + 8 * (&F - S.faces), err, tff,
+                if (M.spec) return distortion_t32(S, F, M, R, tmax, dl, S.bounds + 16 * (&F - S.faces), err, tff,
                                                   exact, fb);
             fb = true;
             return MX_MISS_T;
@@ -1316,7 +1316,7 @@ __device__ __forceinline__ double fallback_dist(const GenArgs &A, const DevScene
     v3 d = mkv(A.in.dx[i], A.in.dy[i], A.in.dz[i]);
     v3 pend = addv(o, mulvs(d, A.max_len));
     const v3 p1 = xform(L.inv_trans.m, L.inv_trans.t, o), p2 = xform(L.inv_trans.m, L.inv_trans.t, pend);
-    if (distortion_line_misses(S.bounds + 8 * f, p1, p2)) return -1.0;  // cfaces.pyx NO_INTERSECTION
+    if (distortion_line_misses(S.bounds + 16 * f, p1, p2)) return -1.0;  // cfaces.pyx NO_INTERSECTION
     if (F.type == RP_FACE_DISTORTION && mx_distortion_ok(S, F) && S.dists[F.distortion].type == RP_DIST_ZERNIKE)
         return distortion_t64(S, F, p1, p2, A.err);
     return face_isect(S, F, p1, p2, A.err);
@@ -1612,15 +1612,14 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
     return fmaxf(tmin, 0.0f);
 }
 
-// A face's entry distance in the mixed search.  b: its box in the mixed
-// kernels' box table (DevScene::mxbounds, staged as S.bounds); b[6] = 1, that
-// box's entry; 3, the nearer entry of it and the face's second box b2
-// (DevScene::mxbox2); otherwise 0 (a face without a box is always tested).
-__device__ __forceinline__ float mx_face_enter(const float *b, const float *b2, float ox, float oy, float oz,
-                                               float ix, float iy, float iz) {
+// A face's entry distance in the mixed search.  b: its 16 floats of
+// S.bounds; b[6] = 1, its box's entry; 3, the nearer entry of its two boxes
+// (b[0..7], b[8..15]); otherwise 0 (a face without a box is always tested).
+__device__ __forceinline__ float mx_face_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
+                                               float iz) {
     if (b[6] != 1.0f) {
         if (b[6] != 3.0f) return 0.0f;
-        return fminf(mx_box_enter(b, ox, oy, oz, ix, iy, iz), mx_box_enter(b2, ox, oy, oz, ix, iy, iz));
+        return fminf(mx_box_enter(b, ox, oy, oz, ix, iy, iz), mx_box_enter(b + 8, ox, oy, oz, ix, iy, iz));
     }
     return mx_box_enter(b, ox, oy, oz, ix, iy, iz);
 }
@@ -1751,7 +1750,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         float q0 = INF, q1 = INF, q2 = INF;
         int f0 = -1, f1 = -1, f2 = -1;
         for (int f = 0; f < nmask; f++) {
-            const float te = mx_face_enter(S.bounds + 8 * f, S.mxbox2 + 8 * f, ox, oy, oz, ix, iy, iz);
+            const float te = mx_face_enter(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz);
             tb_put(tb, f, te);
             if (te <= lim0) {
                 cand |= 1ull << f;
@@ -1798,7 +1797,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         }
         for (int f = nmask; f < nf; f++) {
             if (!mf[f].spec) continue;
-            const float te = mx_face_enter(S.bounds + 8 * f, S.mxbox2 + 8 * f, ox, oy, oz, ix, iy, iz);
+            const float te = mx_face_enter(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz);
             if (te > fmaf(c1.d, 1.000244140625f, 1e-3f)) continue;
             int l = S.face_list[f];
             if (l < 0 || l >= S.n_lists) {
@@ -1818,7 +1817,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
                 if (tb_get(tb, f) > b.len.hi * 1.000001f + 1e-4f) continue;
             } else {
                 if (mf[f].spec) continue;
-                const float te = mx_face_enter(S.bounds + 8 * f, S.mxbox2 + 8 * f, ox, oy, oz, ix, iy, iz);
+                const float te = mx_face_enter(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz);
                 if (te > b.len.hi * 1.000001f + 1e-4f) continue;
             }
             int l = S.face_list[f];
@@ -2506,10 +2505,8 @@ cudaError_t prepare_generation_mixed(const GenArgs &a, size_t smem) {
 // kernel.  The scene's faces and materials decide the instantiation: without
 // FP64 fallbacks the kernels carry no out-of-line calls and their register
 // cost.  The caller has zeroed the tile and group counters.
-cudaError_t launch_generation_mixed(const GenArgs &args, size_t smem, cudaStream_t st, cudaEvent_t mid) {
-    if (args.n_in == 0) return cudaSuccess;
-    GenArgs a = args;
-    if (a.S.mxbounds) a.S.bounds = a.S.mxbounds;  // the search's boxes (DevScene::mxbounds)
+cudaError_t launch_generation_mixed(const GenArgs &a, size_t smem, cudaStream_t st, cudaEvent_t mid) {
+    if (a.n_in == 0) return cudaSuccess;
     if (a.emit && (!a.hit_t || !a.hit_face || !a.group_next || a.unit_rays != RP_GROUP))
         return cudaErrorInvalidValue;  // the hand-over and the group unit are set up by the caller
     const MixedLayout L = mixed_layout(a, smem);

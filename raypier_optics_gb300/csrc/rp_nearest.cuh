@@ -6,11 +6,10 @@
 
 namespace rp {
 
-// Entry distance of the ray (FP32, unit direction) into face f's world box;
-// 0 for faces that are always tested, +inf for a miss.
-__device__ __forceinline__ float box_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
-                                           float iz) {
-    if (b[6] != 1.0f) return 0.0f;
+// Entry distance of the ray (FP32, unit direction) into a padded world box
+// (lo xyz, hi xyz), +inf for a miss.
+__device__ __forceinline__ float slab_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
+                                            float iz) {
     float t1 = (b[0] - ox) * ix, t2 = (b[3] - ox) * ix;
     float tmin = fminf(t1, t2), tmax = fmaxf(t1, t2);
     t1 = (b[1] - oy) * iy;
@@ -23,6 +22,19 @@ __device__ __forceinline__ float box_enter(const float *b, float ox, float oy, f
     tmax = fminf(tmax, fmaxf(t1, t2));
     if (!(tmax >= tmin) || tmax < 0.0f) return __int_as_float(0x7f800000);
     return fmaxf(tmin, 0.0f);
+}
+
+// Entry distance of the ray into face f's boxes (rp_bounds.h
+// face_world_boxes): flag 1, its box; 3, the nearer of its box and its second
+// box (a conic face's two sheets); 0 for faces that are always tested.
+__device__ __forceinline__ float box_enter(const DevScene &S, int f, float ox, float oy, float oz, float ix, float iy,
+                                           float iz) {
+    const float *b = S.bounds + 16 * f;
+    if (b[6] != 1.0f) {
+        if (b[6] != 3.0f) return 0.0f;
+        return fminf(slab_enter(b, ox, oy, oz, ix, iy, iz), slab_enter(b + 8, ox, oy, oz, ix, iy, iz));
+    }
+    return slab_enter(b, ox, oy, oz, ix, iy, iz);
 }
 
 __device__ __forceinline__ float inv_dir(float v) {
@@ -51,7 +63,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
     const float lim0 = (float)max_len * 1.000001f + 1e-4f;
     unsigned long long cand = 0;
     for (int f = 0; f < nmask; f++)
-        if (box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) <= lim0) cand |= 1ull << f;
+        if (box_enter(S, f, ox, oy, oz, ix, iy, iz) <= lim0) cand |= 1ull << f;
     int cur_list = -1;
     v3 p1 = o, p2 = pend;
     while (cand) {
@@ -59,7 +71,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
         int sel = -1;
         for (unsigned long long m = cand; m; m &= m - 1) {
             int f = __ffsll((long long)m) - 1;
-            float t = box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz);
+            float t = box_enter(S, f, ox, oy, oz, ix, iy, iz);
             if (t < tsel) {
                 tsel = t;
                 sel = f;
@@ -79,7 +91,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
             cur_list = l;
         }
         const rp_face &F = S.faces[sel];
-        if (distortion_line_misses(S.bounds + 8 * sel, p1, p2)) continue;
+        if (distortion_line_misses(S.bounds + 16 * sel, p1, p2)) continue;
         double dist = face_isect(S, F, p1, p2, err);
         if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && sel < best))) {
             len = dist;
@@ -89,7 +101,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
     }
     // faces beyond the first 64 records: list order with the same skip test
     for (int f = nmask; f < nf; f++) {
-        if (box_enter(S.bounds + 8 * f, ox, oy, oz, ix, iy, iz) > (float)len * 1.000001f + 1e-4f) continue;
+        if (box_enter(S, f, ox, oy, oz, ix, iy, iz) > (float)len * 1.000001f + 1e-4f) continue;
         int l = S.face_list[f];
         if (l < 0 || l >= S.n_lists) {
             atomicOr(err, ERR_SHAPE_STACK);
@@ -102,7 +114,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
             cur_list = l;
         }
         const rp_face &F = S.faces[f];
-        if (distortion_line_misses(S.bounds + 8 * f, p1, p2)) continue;
+        if (distortion_line_misses(S.bounds + 16 * f, p1, p2)) continue;
         double dist = face_isect(S, F, p1, p2, err);
         if (F.tolerance < dist && (dist < len || (dist == len && best >= 0 && f < best))) {
             len = dist;

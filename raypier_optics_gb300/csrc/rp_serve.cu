@@ -687,7 +687,6 @@ void run_step(rp_server *s, std::vector<Job *> act) {
         J.own_count = (!j->mixed && a.emit) ? a.out_count : nullptr;
         J.detector = j->detector;
         J.mixed = j->mixed ? 1 : 0;
-        if (j->mixed && J.a.S.mxbounds) J.a.S.bounds = J.a.S.mxbounds;  // the mixed search's boxes
         J.slot = j->slot;
         J.first = j->gen == 0;
         const uint64_t gen_units = (j->cur->n + RP_GROUP - 1) / RP_GROUP;

@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(RP_BLOCK) generation_plain_kernel(GenArgs A) {
 
 size_t generation_smem_bytes(int n_lists, int n_recs, int n_mats, int n_faces) {
     // tables (when staged) + boxes + face->list map (padded to 8 bytes) + hit counters
-    size_t tail = ((size_t)n_faces * 8 * 4 + (size_t)n_faces * 2 + 7) / 8 * 8 + (size_t)n_faces * sizeof(unsigned);
+    size_t tail = ((size_t)n_faces * 16 * 4 + (size_t)n_faces * 2 + 7) / 8 * 8 + (size_t)n_faces * sizeof(unsigned);
     return (size_t)n_lists * sizeof(rp_facelist) + (size_t)n_recs * sizeof(rp_face) +
            (size_t)n_mats * sizeof(rp_material) + tail;
 }

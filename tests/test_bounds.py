@@ -21,18 +21,18 @@ def boxes(tables):
     return out
 
 
-def mixed_boxes(tables):
+def search_boxes(tables):
     lib = _native.load()
     out = np.zeros((tables.n_faces, 16), dtype=np.float32)
     d = tables.desc()
-    assert lib.rp_scene_mixed_bounds(ctypes.byref(d), out.ctypes.data, tables.n_faces) == 0
+    assert lib.rp_scene_search_bounds(ctypes.byref(d), out.ctypes.data, tables.n_faces) == 0
     return out
 
 
-def check_hits_inside_mixed(tables, gens):
-    """Every hit on a face with search boxes lies in one of them (the mixed
-    path's search enters a face at the nearer of its boxes; flag 3: two)."""
-    b = mixed_boxes(tables)
+def check_hits_inside_search(tables, gens):
+    """Every hit on a face with search boxes lies in one of them (the
+    searches enter a face at the nearer of its boxes; flag 3: two)."""
+    b = search_boxes(tables)
     idx_of = {int(f["idx"]): k for k, f in enumerate(tables.faces[:tables.n_faces])}
     n_checked = 0
     for g in gens:
@@ -104,7 +104,7 @@ def test_golden_hits_lie_in_face_boxes(name):
     c = load_case(name)
     tables, _, _ = tables_for(c["spec"])
     check_hits_inside(tables, c["gens"])
-    check_hits_inside_mixed(tables, c["gens"])
+    check_hits_inside_search(tables, c["gens"])
 
 
 @pytest.mark.parametrize("config", ["config1", "config2", "config3"])
@@ -122,7 +122,7 @@ def test_benchmark_hits_lie_in_face_boxes(config):
     tables, _, _ = tables_for(spec)
     gens, _ = oracle.trace_rays(tables, wl, rays, P["recursion_limit"], P["max_length"], P["e2_terminate"])
     assert check_hits_inside(tables, gens) > 0
-    assert check_hits_inside_mixed(tables, gens) > 0
+    assert check_hits_inside_search(tables, gens) > 0
 
 
 def test_boxes_are_tight_for_axis_aligned_faces():
@@ -179,7 +179,7 @@ def test_conic_sheet_boxes_hold_on_dense_samples(name):
     from helpers import load_face_specs
     spec = load_face_specs()[name]
     tables, _, _ = tables_for(spec)
-    mb, ub = mixed_boxes(tables), boxes(tables)
+    mb, ub = search_boxes(tables), boxes(tables)
     assert mb[0, 6] == 3
     union_dz = ub[0, 5] - ub[0, 2]
     assert mb[0, 5] - mb[0, 2] < 0.5 * union_dz and mb[0, 13] - mb[0, 10] < 0.5 * union_dz
@@ -188,7 +188,7 @@ def test_conic_sheet_boxes_hold_on_dense_samples(name):
                          (7, 0.5 * float(ub[0, 2] + ub[0, 5]), 0.5 * float(ub[0, 2] + ub[0, 5]))):
         rays = dense_rays(4096, seed, z_below=zb, z_above=za)
         gens, _ = oracle.trace_rays(tables, np.array([0.55]), rays, 4, 5000.0, 0.0)
-        n_checked += check_hits_inside_mixed(tables, gens)
+        n_checked += check_hits_inside_search(tables, gens)
     assert n_checked > 100
 
 
@@ -207,7 +207,7 @@ def test_conic_sheet_ranges_cover_the_quadric():
                                       "shape": {"type": "CircleShape", "kw": {"radius": 12.5}},
                                       "material": "m"}]}]}
         tables, _, _ = tables_for(spec)
-        mb = mixed_boxes(tables)[0]
+        mb = search_boxes(tables)[0]
         if mb[6] != 3:
             continue
         n_split += 1
