@@ -1102,9 +1102,10 @@ __device__ __forceinline__ bool mat_specialised(int type) {
 // float-float from the float-float ray direction D, its unit vector ind and
 // the unit normal nn; the S/P projection, Fresnel coefficients and amplitudes
 // are FP32.  Eo receives the children's shared E_vector; returns the number of
-// children.
+// children.  nt_in / nt_out: a dispersive material's complex indices inside
+// and outside at the ray's wavelength (loaded by the caller ahead of use).
 __device__ int eval_f(const DevScene &S, const rp_material &m, const RayF &r, const ff3 &D, const ff3 &ind,
-                      const ff3 &nn, f3 &Eo, ChildF *ch, unsigned *err) {
+                      const ff3 &nn, f3 &Eo, ChildF *ch, unsigned *err, double2 nt_in, double2 nt_out) {
     if (m.type == RP_MAT_NONE || m.type == RP_MAT_OPAQUE) return 0;
     const f3 normal = mk3(nn.x.hi, nn.y.hi, nn.z.hi);
     cf E1, E2;
@@ -1170,13 +1171,12 @@ __device__ int eval_f(const DevScene &S, const rp_material &m, const RayF &r, co
         n1d = out_to_in ? no : ni;
         n2d = out_to_in ? ni : no;
     } else {
-        long long w = (long long)r.wl;
-        if (w >= S.n_wl) {
+        if ((long long)r.wl >= S.n_wl) {
             atomicOr(err, ERR_WAVELENGTH);
             return 0;
         }
-        n1d = S.ntab[(long long)(out_to_in ? m.curve_outside : m.curve_inside) * S.n_wl + w];
-        n2d = S.ntab[(long long)(out_to_in ? m.curve_inside : m.curve_outside) * S.n_wl + w];
+        n1d = out_to_in ? nt_out : nt_in;
+        n2d = out_to_in ? nt_in : nt_out;
     }
     const cf n1 = cf_of_d(n1d), n2 = cf_of_d(n2d);
     const float sin1 = sqrtf(fabsf(1.0f - cos1 * cos1));
@@ -2083,6 +2083,18 @@ __device__ __forceinline__ void material_mx(const GenArgs &A, const DevScene &S,
     const ff tt = ffm(B.t[t].x, B.t[t].y);
     const rp_face &F = S.faces[face];
     const int l = S.face_list[face];
+    // a dispersive material's indices at the ray's wavelength: scattered
+    // loads, issued here so that they land while the hit point and normal
+    // are computed
+    double2 nt_in = make_double2(0.0, 0.0), nt_out = make_double2(0.0, 0.0);
+    {
+        const rp_material &Mn = S.mats[F.material];
+        const long long w = (long long)B.wl[t];
+        if (Mn.type == RP_MAT_FULL_DIELECTRIC_DISPERSIVE && w < S.n_wl) {
+            nt_in = S.ntab[(long long)Mn.curve_inside * S.n_wl + w];
+            nt_out = S.ntab[(long long)Mn.curve_outside * S.n_wl + w];
+        }
+    }
     if (l < 0 || l >= S.n_lists) {
         atomicOr(A.err, ERR_SHAPE_STACK);
     } else {
@@ -2143,7 +2155,7 @@ __device__ __forceinline__ void material_mx(const GenArgs &A, const DevScene &S,
             r.wl = B.wl[t];
             const ff3 Dff = mkff3(D[0], D[1], D[2]);
             const ff idl = ff_div(ffm(1.0f, 0.0f), dlen);
-            nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err);
+            nc = eval_f(S, Mt, r, Dff, ff3_scale(Dff, idl), nn, Eo, ch, A.err, nt_in, nt_out);
             if (A.e2_term > 0.0 && nc > 0) {
                 // the |E|^2 rule, children kept in order (fixed indices: registers)
                 const bool k0 = !(cabs2(ch[0].e1) + cabs2(ch[0].e2) < e2t);
