@@ -483,7 +483,7 @@ def run_e2e(args, ctx, lib, dscene, rays, n, rl, max_len, flags, e2, max_gens, s
     lib.rp_host_free(pin_out)
     step_ms = [1000.0 * t for t in step_s]
     return e2e_value, d2h, {"steps": e2e_steps, "min": min(step_ms), "median": statistics.median(step_ms),
-                            "max": max(step_ms)}
+                            "max": max(step_ms), "all": [round(t, 2) for t in step_ms]}
 
 
 def adjoint_leg(ctx, reps=5):
@@ -784,7 +784,7 @@ def emit(args, world, value, dev_s, wall, ng, n, faces, rl, e2, seg_per_step, e2
             "e2e": ({"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 188,
                      "d2h_bytes_per_step": int(d2h / e2e_steps["steps"]), "steps": e2e_steps["steps"],
                      "api": "rp_trace_rays_host (pinned host records in and out)",
-                     "step_ms": {k: e2e_steps[k] for k in ("min", "median", "max")},
+                     "step_ms": {k: e2e_steps[k] for k in ("min", "median", "max", "all")},
                      "host_link": e2e_link(n * 188, d2h / e2e_steps["steps"], e2e_steps["min"], peaks)}
                     if e2e_value else None),
             "roofline": {"bound": "hbm", "achieved": dom["hbm"]["achieved_gbs"], "peak": dom["hbm"]["peak_gbs"],

@@ -1960,60 +1960,101 @@ struct GroupMask {
     int job;              // its job in a batch (0 otherwise)
 };
 
-// The masks of group q of the generation A (the rays whose hit material can
-// produce children).
-__device__ __forceinline__ void group_masks(const GenArgs &A, const DevScene &S, unsigned q, unsigned lane,
-                                            GroupMask &G) {
-    const unsigned long long g0 = (unsigned long long)q * RP_GROUP;
+// A group claimed a group ahead of its use: its index and this lane's four
+// hit-face records, loaded when it is claimed so that the loads (and the
+// claim's atomic) complete while the warp evaluates the current group.
+struct GroupAhead {
+    unsigned q;
+    int hf[RP_GROUP / 32];
+};
+
+__device__ __forceinline__ void claim_ahead(const GenArgs &A, unsigned long long n_groups, unsigned lane,
+                                            GroupAhead &H) {
+    H.q = claim_sub_tile(A.group_next, lane);
+    const unsigned long long g0 = (unsigned long long)H.q * RP_GROUP;
 #pragma unroll
     for (int c = 0; c < RP_GROUP / 32; c++) {
         const unsigned long long i = g0 + 32 * c + lane;
-        bool m = false;
-        if (i < A.n_in && A.emit) {
-            const int f = A.hit_face[i];
-            m = f >= 0 && f < S.n_faces && makes_children(S, f);
-        }
-        G.m[c] = __ballot_sync(0xffffffffu, m);
+        H.hf[c] = (H.q < n_groups && i < A.n_in) ? A.hit_face[i] : -1;
     }
-    G.p1 = __popc(G.m[0]);
-    G.p2 = G.p1 + __popc(G.m[1]);
-    G.p3 = G.p2 + __popc(G.m[2]);
-    G.total = G.p3 + __popc(G.m[3]);
 }
 
-// Claims groups until one has material rays (a group without any gets its
-// zero child count at once); G.q = n_groups when none is left.
-__device__ __forceinline__ void claim_group(const GenArgs &A, const DevScene &S, unsigned long long n_groups,
-                                            unsigned lane, GroupMask &G) {
+// Takes the group claimed ahead in H (claiming the next one into H at once)
+// until one has material rays (a group without any gets its zero child count
+// at once); G.q = n_groups when none is left.
+__device__ __forceinline__ void next_group(const GenArgs &A, const DevScene &S, unsigned long long n_groups,
+                                           unsigned lane, GroupAhead &H, GroupMask &G) {
     G.job = 0;
     for (;;) {
-        const unsigned q = claim_sub_tile(A.group_next, lane);
-        G.q = q;
+        const GroupAhead cur = H;
+        G.q = cur.q;
         G.total = 0;
-        if (q >= n_groups) return;
-        group_masks(A, S, q, lane, G);
+        if (cur.q >= n_groups) return;
+        claim_ahead(A, n_groups, lane, H);
+#pragma unroll
+        for (int c = 0; c < RP_GROUP / 32; c++) {
+            const int f = cur.hf[c];
+            G.m[c] = __ballot_sync(0xffffffffu, f >= 0 && f < S.n_faces && makes_children(S, f));
+        }
+        G.p1 = __popc(G.m[0]);
+        G.p2 = G.p1 + __popc(G.m[1]);
+        G.p3 = G.p2 + __popc(G.m[2]);
+        G.total = G.p3 + __popc(G.m[3]);
         if (G.total > 0) return;
-        if (lane == 0) A.tile_counts[q] = 0u;
+        if (lane == 0) A.tile_counts[cur.q] = 0u;
     }
 }
 
 // The same over a batch: global groups taken from the batch's counter, each
 // returned as its job and its group within the job; G.job = -1 when none is
 // left.
-__device__ __forceinline__ void claim_group_batch(const BatchDev *Bt, unsigned *ctr, unsigned lane, GroupMask &G) {
+// (claimed ahead as in the single-job kernel: the global group, its job and
+// this lane's four hit-face records)
+struct BatchAhead {
+    unsigned u;
+    int j;
+    int hf[RP_GROUP / 32];
+};
+
+__device__ __forceinline__ void claim_ahead_batch(const BatchDev *Bt, unsigned *ctr, unsigned lane, BatchAhead &H) {
+    H.u = claim_sub_tile(&ctr[1], lane);
+    H.j = -1;
+#pragma unroll
+    for (int c = 0; c < RP_GROUP / 32; c++) H.hf[c] = -1;
+    if (H.u >= Bt->total_units) return;
+    H.j = batch_job_of(Bt, H.u);
+    const GenArgs &A = Bt->jobs[H.j].a;
+    const unsigned long long g0 = (unsigned long long)(H.u - Bt->unit_start[H.j]) * RP_GROUP;
+#pragma unroll
+    for (int c = 0; c < RP_GROUP / 32; c++) {
+        const unsigned long long i = g0 + 32 * c + lane;
+        if (i < A.n_in && A.emit) H.hf[c] = A.hit_face[i];
+    }
+}
+
+__device__ __forceinline__ void next_group_batch(const BatchDev *Bt, unsigned *ctr, unsigned lane, BatchAhead &H,
+                                                 GroupMask &G) {
     for (;;) {
-        const unsigned u = claim_sub_tile(&ctr[1], lane);
+        const BatchAhead cur = H;
         G.total = 0;
-        if (u >= Bt->total_units) {
+        if (cur.u >= Bt->total_units) {
             G.job = -1;
             G.q = 0;
             return;
         }
-        const int j = batch_job_of(Bt, u);
-        const GenArgs &A = Bt->jobs[j].a;
-        G.job = j;
-        G.q = u - Bt->unit_start[j];
-        group_masks(A, A.S, G.q, lane, G);
+        claim_ahead_batch(Bt, ctr, lane, H);
+        const GenArgs &A = Bt->jobs[cur.j].a;
+        G.job = cur.j;
+        G.q = cur.u - Bt->unit_start[cur.j];
+#pragma unroll
+        for (int c = 0; c < RP_GROUP / 32; c++) {
+            const int f = cur.hf[c];
+            G.m[c] = __ballot_sync(0xffffffffu, f >= 0 && f < A.S.n_faces && makes_children(A.S, f));
+        }
+        G.p1 = __popc(G.m[0]);
+        G.p2 = G.p1 + __popc(G.m[1]);
+        G.p3 = G.p2 + __popc(G.m[2]);
+        G.total = G.p3 + __popc(G.m[3]);
         if (G.total > 0) return;
         if (lane == 0) A.tile_counts[G.q] = 0u;
     }
@@ -2209,7 +2250,9 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS) mixed_material_ke
     __syncthreads();
 
     GroupMask G;
-    claim_group(A, S, n_groups, lane, G);
+    GroupAhead H;
+    claim_ahead(A, n_groups, lane, H);
+    next_group(A, S, n_groups, lane, H, G);
     if (G.q < n_groups) prefetch_mat(&bufs[0], A, Rr, chunk_ray(G, 0, lane), lane);
     unsigned k = 0, carry = 0;
     for (unsigned step = 0; G.q < n_groups; step++) {
@@ -2218,7 +2261,7 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS) mixed_material_ke
         unsigned kn = k + 1;
         const bool last_of_group = kn * 32 >= G.total;
         if (last_of_group) {
-            claim_group(A, S, n_groups, lane, Gn);
+            next_group(A, S, n_groups, lane, H, Gn);
             kn = 0;
         }
         if (Gn.q < n_groups)
@@ -2360,7 +2403,9 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS)
     if (threadIdx.x == 0) s_term = 0;
     __syncthreads();
     GroupMask G;
-    claim_group_batch(Bt, ctr, lane, G);
+    BatchAhead H;
+    claim_ahead_batch(Bt, ctr, lane, H);
+    next_group_batch(Bt, ctr, lane, H, G);
     if (G.job >= 0) {
         const GenArgs &A = Bt->jobs[G.job].a;
         prefetch_mat(&bufs[0], A, A.in, chunk_ray(G, 0, lane), lane);
@@ -2371,7 +2416,7 @@ __global__ void __launch_bounds__(RP_BLOCK, MX_MAT_MIN_BLOCKS)
         unsigned kn = k + 1;
         const bool last_of_group = kn * 32 >= G.total;
         if (last_of_group) {
-            claim_group_batch(Bt, ctr, lane, Gn);
+            next_group_batch(Bt, ctr, lane, H, Gn);
             kn = 0;
         }
         if (Gn.job >= 0) {
