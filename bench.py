@@ -71,8 +71,8 @@ PLAIN_FP64_FLOPS_PER_SEGMENT = 863.4
 # 262,144-ray configuration-2 trace (1,046,875 gathered rays), this build:
 # dram__bytes_read.sum + dram__bytes_write.sum of the search and material
 # kernels, dram__bytes.sum.per_second x duration of the plain kernel
-NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 805.1, "mixed_search_kernel": 331.4,
-                       "mixed_material_kernel": 426.5}
+NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 805.1, "mixed_search_kernel": 331.2,
+                       "mixed_material_kernel": 425.4}
 
 
 def parse():
