@@ -64,14 +64,13 @@ BYTES = {"plain": {"segment": 168, "gathered": 208, "child": 188},
          "search": {"segment": 72, "gathered": 308},
          "material": {"segment": 4, "hit": 160, "child": 188}}
 # FP64 floating-point operations per segment of the plain kernel (ncu: dadd +
-# dmul + 2 dfma thread instructions, 2,146.6 M over the 2,486,356 rays of
-# generation 5 of the 262,144-ray configuration-2 trace)
-PLAIN_FP64_FLOPS_PER_SEGMENT = 863.4
+# dmul + 2 dfma thread instructions, 859.7 M over the 1,046,875 rays of
+# generation 3 of the 262,144-ray configuration-2 trace, this build)
+PLAIN_FP64_FLOPS_PER_SEGMENT = 821.2
 # DRAM bytes per input ray of a launch, from ncu on generation 3 of the
 # 262,144-ray configuration-2 trace (1,046,875 gathered rays), this build:
-# dram__bytes_read.sum + dram__bytes_write.sum of the search and material
-# kernels, dram__bytes.sum.per_second x duration of the plain kernel
-NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 805.1, "mixed_search_kernel": 331.2,
+# dram__bytes_read.sum + dram__bytes_write.sum of each kernel
+NCU_TRAFFIC_PER_RAY = {"generation_plain_kernel": 811.6, "mixed_search_kernel": 331.2,
                        "mixed_material_kernel": 425.4}
 
 
