@@ -29,7 +29,7 @@ def _emit(capsys, e2e_value=9.0e8):
     stats = _stats()
     krl = bench.kernel_rooflines(1, stats, 10 << 20, 6778.0, "measured", PEAKS) + \
         bench.kernel_rooflines(0, _stats(0.0, 1548.0), 10 << 20, 6778.0, "measured", PEAKS)
-    e2e_steps = {"steps": 10, "min": 56.4, "median": 56.5, "max": 120.0}
+    e2e_steps = {"steps": 10, "min": 56.4, "median": 56.5, "max": 120.0, "all": [56.4] * 8 + [56.5, 120.0]}
     cpu = {"value": 3.3e6, "cores": 16, "kind": "reference", "sample": "16384 rays"}
     clk = {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []}
     bench.emit(args, 1, 2.3e9, 0.2413, 0.2415, 8, 1 << 20, list(range(11)), 8, 1e-6, 5.63e7, e2e_value,
@@ -67,7 +67,8 @@ def test_derived_fields(capsys):
     assert line["measured_peaks"] == PEAKS
     e = line["e2e"]
     assert e["d2h_bytes_per_step"] == 10_592_222_680 and e["h2d_bytes_per_step"] == (1 << 20) * 188
-    assert e["step_ms"] == {"min": 56.4, "median": 56.5, "max": 120.0} and e["steps"] == 10
+    assert e["step_ms"] == {"min": 56.4, "median": 56.5, "max": 120.0, "all": [56.4] * 8 + [56.5, 120.0]}
+    assert e["steps"] == 10
     assert line["cpu_baseline"]["cores"] == 16 and line["gpu_launches"] == 380
 
 
