@@ -89,6 +89,12 @@ def check_hits_inside(tables, gens):
                 p1 = g["origin"][sel] @ m.T + L["inv_trans"]["t"]
                 u = g["direction"][sel] @ m.T
                 assert not line_misses(b[k], p1, u).any(), f"face record {k}: a hit ray would be culled"
+                # and its hit point's local (x, y) lies in the padded rectangle: the
+                # searches enter the face at the ray's entry into the prism over it
+                q = pts[recs == k] @ m.T + L["inv_trans"]["t"]
+                x0, x1, y0, y1 = (float(v) for v in b[k, :4])
+                inside = (q[:, 0] >= x0) & (q[:, 0] <= x1) & (q[:, 1] >= y0) & (q[:, 1] <= y1)
+                assert inside.all(), f"face record {k}: {np.count_nonzero(~inside)} hits outside its prism"
                 n_checked += len(sel)
                 continue
             p = pts[recs == k]
