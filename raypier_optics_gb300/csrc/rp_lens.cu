@@ -16,9 +16,11 @@
 //
 // Adjoint: nothing of the forward is kept but each ray's image point and
 // reached flag.  The backward pass walks the surfaces in reverse and, for
-// each, re-traces the ray from its input through the surfaces before it (the
-// forward per generation, recomputed: O(n^2) surface evaluations for n
-// surfaces, no per-surface state in memory), recomputes that surface's hit,
+// each, re-traces the ray through the surfaces before it (the forward per
+// generation, recomputed; no per-surface state in memory): from a checkpoint
+// in registers, the ray in front of the middle surface, for the later
+// surfaces, from its input for the earlier ones (n^2/4 + n surface
+// evaluations for n surfaces instead of n^2/2), recomputes that surface's hit,
 // normal and refraction, and applies the chain rule:
 //   hit     h = p + t d with F(h) = z - z_k - s(x^2 + y^2) = 0, so
 //           dt = (ds - dz_k - G.dp - t G.dd) / (G.d) with G = grad F
@@ -160,6 +162,18 @@ __device__ __forceinline__ SagD sag_derivs(double u, double R, double beta, doub
 // The ray i in front of surface k (k = n_surf: in front of the image plane):
 // its input re-traced through surfaces 0 .. k-1 with the forward's arithmetic.
 // Only called for rays the forward kept, which pass every surface again.
+// From surface j0 with the ray (p, d) in front of it (j0 = 0: the input).
+__device__ __forceinline__ void lens_prefix_from(const LensArgs &L, int j0, int k, v3 &p, v3 &d) {
+    for (int j = j0; j < k; j++) {
+        v3 h, dn;
+        double t;
+        if (lens_surface(L, j, p, d, h, dn, t, L.err)) {
+            p = h;
+            d = dn;
+        }
+    }
+}
+
 __device__ __forceinline__ void lens_prefix(const LensArgs &L, unsigned long long i, int k, v3 &p, v3 &d) {
     p = mkv(L.in.ox[i], L.in.oy[i], L.in.oz[i]);
     d = mkv(L.in.dx[i], L.in.dy[i], L.in.dz[i]);
@@ -184,11 +198,18 @@ __global__ void __launch_bounds__(RP_LENS_BLOCK) lens_backward_kernel(LensArgs L
     const bool ok = i < L.n && L.valid[i];
     v3 hb = mkv(0, 0, 0), db = mkv(0, 0, 0);
     double zimg_b = 0.0;
+    // one checkpoint, in registers: the ray in front of the middle surface,
+    // from which the prefixes of the later surfaces are re-traced (the same
+    // arithmetic as from the input, so the same states); the earlier ones
+    // start from the input
+    const int km = L.n_surf / 2;
+    v3 pm = mkv(0, 0, 0), dm = mkv(0, 0, 1);
+    if (ok) lens_prefix(L, i, km, pm, dm);
     if (ok) {
         // image plane z = z_img: h = p + t d, t = (z_img - p_z) / d_z
         const int k = L.n_surf;
-        v3 p, d;
-        lens_prefix(L, i, k, p, d);
+        v3 p = pm, d = dm;
+        lens_prefix_from(L, km, k, p, d);
         const double zi = L.faces[k].p[2];
         const double t = (zi - p.z) / d.z;
         v3 h = addv(p, mulvs(d, t));
@@ -204,7 +225,13 @@ __global__ void __launch_bounds__(RP_LENS_BLOCK) lens_backward_kernel(LensArgs L
         double gR = 0.0, gB = 0.0, gA4 = 0.0, gA6 = 0.0, gZ = 0.0;
         if (ok) {
             v3 p, d;
-            lens_prefix(L, i, k, p, d);
+            if (k >= km) {
+                p = pm;
+                d = dm;
+                lens_prefix_from(L, km, k, p, d);
+            } else {
+                lens_prefix(L, i, k, p, d);
+            }
             v3 h, dn;
             double t = 0.0;
             lens_surface(L, k, p, d, h, dn, t, L.err);  // the forward kept this ray, so it hits again
