@@ -362,15 +362,25 @@ inline void world_from_local(const rp_facelist &L, const double lo[3], const dou
     out[6] = 1.0f;
 }
 
-// The boxes of the mixed path's search: out[0..7] as face_world_box and, for a
-// ConicRevolutionFace, out[0..7] and out[8..15] the world boxes of its two
-// sheets' parts over the aperture (out[6] = 3 when the two boxes are set):
+// The boxes of the searches: out[0..7] as face_world_box; for a distortion
+// face (flag 2) out[8..15] the x and y rows of its list's world-to-list map;
+// for a ConicRevolutionFace, out[0..7] and out[8..15] the world boxes of its
+// two sheets' parts over the aperture (out[6] = 3 when the two boxes are set):
 // each a thin slab where the union of both can span hundreds of millimetres,
 // so a ray that starts between the sheets enters neither.  A face's entry
 // distance is the nearer of its boxes' entries.
 inline void face_world_boxes(const rp_scene_desc *d, const rp_facelist &L, const rp_face &f, float out[16]) {
     for (int k = 0; k < 16; k++) out[k] = 0.0f;
     face_world_box(d, L, f, out);
+    if (out[6] == 2.0f) {
+        // a distortion face: rows x and y of its list's world-to-list map
+        // (m[0..2], t[0]; m[3..5], t[1]) for the searches' prism entry
+        for (int r = 0; r < 2; r++) {
+            for (int c = 0; c < 3; c++) out[8 + 4 * r + c] = (float)L.inv_trans.m[3 * r + c];
+            out[8 + 4 * r + 3] = (float)L.inv_trans.t[r];
+        }
+        return;
+    }
     if (f.type != RP_FACE_CONIC || out[6] != 1.0f) return;
     const Box2 b = shape_box(d, f.shape);
     double a0, a1, b0, b1;

@@ -70,6 +70,44 @@ __device__ __forceinline__ bool distortion_line_misses(const float *b, v3 p1, v3
     return (s00 > 0.0 && s01 > 0.0 && s10 > 0.0 && s11 > 0.0) || (s00 < 0.0 && s01 < 0.0 && s10 < 0.0 && s11 < 0.0);
 }
 
+// A DistortionFace's entry distance for the searches' culling (its box record
+// b, flag 2: b[0..3] its shape's padded rectangle x0, x1, y0, y1 in the face
+// list's frame, b[8..15] the x and y rows of the world-to-list map).  The
+// reference accepts only a point of the ray's line whose local (x, y) lies
+// inside the shape (cfaces.pyx:2402), converged or not, so no hit lies before
+// the ray enters the prism over that rectangle.  The ray (world origin o, unit
+// direction u) goes to the list's frame in FP32, with a margin above that
+// rounding; the parameter along the ray is its world distance in both
+// frames.  Infinity when the prism lies behind the ray or the line misses it.
+static __device__ __noinline__ float prism_enter(const float *b, float ox, float oy, float oz, float ux, float uy,
+                                                 float uz) {
+    const float *r0 = b + 8, *r1 = b + 12;
+    const float qx = fmaf(r0[0], ox, fmaf(r0[1], oy, fmaf(r0[2], oz, r0[3])));
+    const float qy = fmaf(r1[0], ox, fmaf(r1[1], oy, fmaf(r1[2], oz, r1[3])));
+    const float vx = fmaf(r0[0], ux, fmaf(r0[1], uy, r0[2] * uz));
+    const float vy = fmaf(r1[0], ux, fmaf(r1[1], uy, r1[2] * uz));
+    // FP32 rounding of the map: a few units of 6e-8 of the terms' magnitudes
+    const float m = 1e-6f * (fabsf(ox) + fabsf(oy) + fabsf(oz) + fabsf(r0[3]) + fabsf(r1[3]) + 1.0f);
+    const float INF = __int_as_float(0x7f800000);
+    float t0 = 0.0f, t1 = INF;
+    const float lo[2] = {b[0] - m, b[2] - m}, hi[2] = {b[1] + m, b[3] + m}, q[2] = {qx, qy}, v[2] = {vx, vy};
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        if (fabsf(v[k]) < 1e-20f) {
+            if (q[k] < lo[k] || q[k] > hi[k]) return INF;
+        } else {
+            const float iv = 1.0f / v[k];
+            const float a = (lo[k] - q[k]) * iv, c = (hi[k] - q[k]) * iv;
+            t0 = fmaxf(t0, fminf(a, c));
+            t1 = fminf(t1, fmaxf(a, c));
+        }
+    }
+    // (the padded bounds cover the position's rounding; the relative margin
+    // the direction's)
+    if (!(t1 + 1e-4f * fabsf(t1) + m >= t0)) return INF;
+    return fmaxf(t0 - 1e-4f * fabsf(t0) - m, 0.0f);
+}
+
 // Exclusive scan of `c` over the block; *total_out gets the block total.
 // Must be called by all threads of the block.
 __device__ __forceinline__ unsigned block_scan(unsigned c, unsigned *total_out) {

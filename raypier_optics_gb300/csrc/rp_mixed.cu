@@ -1612,57 +1612,19 @@ __device__ __forceinline__ float mx_box_enter(const float *b, float ox, float oy
     return fmaxf(tmin, 0.0f);
 }
 
-// A DistortionFace's entry distance (flag 2: b[0..3] = its shape's padded
-// rectangle x0, x1, y0, y1 in the face list's frame): the reference accepts
-// only a point of the ray's line whose local (x, y) lies inside the shape
-// (cfaces.pyx:2402), converged or not, so no hit lies before the ray enters
-// the prism over that rectangle.  The ray (world origin o, unit direction u)
-// goes to the list's frame in FP32 (rows x and y of the world-to-list map,
-// L's ri / ti), with a margin above that rounding; the parameter along the
-// ray is its world distance in both frames.  Infinity when the prism lies
-// behind the ray or the line misses it.
-__device__ __noinline__ float mx_prism_enter(const mx::MxList &L, const float *b, float ox, float oy, float oz,
-                                             float ux, float uy, float uz) {
-    const float qx = fmaf(L.ri_hi[0], ox, fmaf(L.ri_hi[1], oy, fmaf(L.ri_hi[2], oz, L.ti_hi[0])));
-    const float qy = fmaf(L.ri_hi[3], ox, fmaf(L.ri_hi[4], oy, fmaf(L.ri_hi[5], oz, L.ti_hi[1])));
-    const float vx = fmaf(L.ri_hi[0], ux, fmaf(L.ri_hi[1], uy, L.ri_hi[2] * uz));
-    const float vy = fmaf(L.ri_hi[3], ux, fmaf(L.ri_hi[4], uy, L.ri_hi[5] * uz));
-    // FP32 rounding of the map: a few units of 6e-8 of the terms' magnitudes
-    const float m = 1e-6f * (fabsf(ox) + fabsf(oy) + fabsf(oz) + fabsf(L.ti_hi[0]) + fabsf(L.ti_hi[1]) + 1.0f);
-    const float INF = __int_as_float(0x7f800000);
-    float t0 = 0.0f, t1 = INF;
-    const float lo[2] = {b[0] - m, b[2] - m}, hi[2] = {b[1] + m, b[3] + m}, q[2] = {qx, qy}, v[2] = {vx, vy};
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        if (fabsf(v[k]) < 1e-20f) {
-            if (q[k] < lo[k] || q[k] > hi[k]) return INF;
-        } else {
-            const float iv = 1.0f / v[k];
-            const float a = (lo[k] - q[k]) * iv, c = (hi[k] - q[k]) * iv;
-            t0 = fmaxf(t0, fminf(a, c));
-            t1 = fminf(t1, fmaxf(a, c));
-        }
-    }
-    // (the padded bounds cover the position's rounding; the relative margin
-    // the direction's)
-    if (!(t1 + 1e-4f * fabsf(t1) + m >= t0)) return INF;
-    return fmaxf(t0 - 1e-4f * fabsf(t0) - m, 0.0f);
-}
-
 // A face's entry distance in the mixed search.  b: its 16 floats of
 // S.bounds; b[6] = 1, its box's entry; 3, the nearer entry of its two boxes
 // (b[0..7], b[8..15]); 2 (a DistortionFace, in the form of the kernels that
-// carry its code), its prism's entry (mx_prism_enter: L its face list, u the
-// ray's unit direction); otherwise 0 (a face without a box is always tested).
+// carry its code), its prism's entry (prism_enter, u the ray's unit
+// direction); otherwise 0 (a face without a box is always tested).
 template <bool FB>
 __device__ __forceinline__ float mx_face_enter(const float *b, float ox, float oy, float oz, float ix, float iy,
-                                               float iz, const mx::MxList *ml, const short *face_list, int f,
-                                               float ux, float uy, float uz) {
+                                               float iz, float ux, float uy, float uz) {
     if (b[6] != 1.0f) {
         if (b[6] == 3.0f)
             return fminf(mx_box_enter(b, ox, oy, oz, ix, iy, iz), mx_box_enter(b + 8, ox, oy, oz, ix, iy, iz));
         if constexpr (FB)
-            if (b[6] == 2.0f) return mx_prism_enter(ml[face_list[f]], b, ox, oy, oz, ux, uy, uz);
+            if (b[6] == 2.0f) return prism_enter(b, ox, oy, oz, ux, uy, uz);
         return 0.0f;
     }
     return mx_box_enter(b, ox, oy, oz, ix, iy, iz);
@@ -1795,8 +1757,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         float q0 = INF, q1 = INF, q2 = INF;
         int f0 = -1, f1 = -1, f2 = -1;
         for (int f = 0; f < nmask; f++) {
-            const float te = mx_face_enter<FB>(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz, ml, S.face_list, f,
-                                                              ux, uy, uz);
+            const float te = mx_face_enter<FB>(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz, ux, uy, uz);
             tb_put(tb, f, te);
             if (te <= lim0) {
                 cand |= 1ull << f;
@@ -1843,8 +1804,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
         }
         for (int f = nmask; f < nf; f++) {
             if (!mf[f].spec) continue;
-            const float te = mx_face_enter<FB>(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz, ml, S.face_list, f,
-                                                              ux, uy, uz);
+            const float te = mx_face_enter<FB>(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz, ux, uy, uz);
             if (te > fmaf(c1.d, 1.000244140625f, 1e-3f)) continue;
             int l = S.face_list[f];
             if (l < 0 || l >= S.n_lists) {
@@ -1864,8 +1824,7 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
                 if (tb_get(tb, f) > b.len.hi * 1.000001f + 1e-4f) continue;
             } else {
                 if (mf[f].spec) continue;
-                const float te = mx_face_enter<FB>(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz, ml, S.face_list, f,
-                                                              ux, uy, uz);
+                const float te = mx_face_enter<FB>(S.bounds + 16 * f, ox, oy, oz, ix, iy, iz, ux, uy, uz);
                 if (te > b.len.hi * 1.000001f + 1e-4f) continue;
             }
             int l = S.face_list[f];

@@ -24,15 +24,18 @@ __device__ __forceinline__ float slab_enter(const float *b, float ox, float oy, 
     return fmaxf(tmin, 0.0f);
 }
 
-// Entry distance of the ray into face f's boxes (rp_bounds.h
-// face_world_boxes): flag 1, its box; 3, the nearer of its box and its second
-// box (a conic face's two sheets); 0 for faces that are always tested.
+// Entry distance of the ray (unit direction u, its inverse i) into face f's
+// boxes (rp_bounds.h face_world_boxes): flag 1, its box; 3, the nearer of
+// its box and its second box (a conic face's two sheets); 2, a distortion
+// face's prism (prism_enter); 0 for faces that are always tested.
 __device__ __forceinline__ float box_enter(const DevScene &S, int f, float ox, float oy, float oz, float ix, float iy,
-                                           float iz) {
+                                           float iz, float ux, float uy, float uz) {
     const float *b = S.bounds + 16 * f;
     if (b[6] != 1.0f) {
-        if (b[6] != 3.0f) return 0.0f;
-        return fminf(slab_enter(b, ox, oy, oz, ix, iy, iz), slab_enter(b + 8, ox, oy, oz, ix, iy, iz));
+        if (b[6] == 3.0f)
+            return fminf(slab_enter(b, ox, oy, oz, ix, iy, iz), slab_enter(b + 8, ox, oy, oz, ix, iy, iz));
+        if (b[6] == 2.0f) return prism_enter(b, ox, oy, oz, ux, uy, uz);
+        return 0.0f;
     }
     return slab_enter(b, ox, oy, oz, ix, iy, iz);
 }
@@ -57,13 +60,14 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
     float dx = (float)d.x, dy = (float)d.y, dz = (float)d.z;
     float il = 1.0f / sqrtf(dx * dx + dy * dy + dz * dz);
     float ix = inv_dir(dx * il), iy = inv_dir(dy * il), iz = inv_dir(dz * il);
+    const float ux = dx * il, uy = dy * il, uz = dz * il;
     // distances along the ray are Euclidean in the reference (h * |p2 - p1|)
     const int nf = S.n_faces;
     const int nmask = nf < 64 ? nf : 64;
     const float lim0 = (float)max_len * 1.000001f + 1e-4f;
     unsigned long long cand = 0;
     for (int f = 0; f < nmask; f++)
-        if (box_enter(S, f, ox, oy, oz, ix, iy, iz) <= lim0) cand |= 1ull << f;
+        if (box_enter(S, f, ox, oy, oz, ix, iy, iz, ux, uy, uz) <= lim0) cand |= 1ull << f;
     int cur_list = -1;
     v3 p1 = o, p2 = pend;
     while (cand) {
@@ -71,7 +75,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
         int sel = -1;
         for (unsigned long long m = cand; m; m &= m - 1) {
             int f = __ffsll((long long)m) - 1;
-            float t = box_enter(S, f, ox, oy, oz, ix, iy, iz);
+            float t = box_enter(S, f, ox, oy, oz, ix, iy, iz, ux, uy, uz);
             if (t < tsel) {
                 tsel = t;
                 sel = f;
@@ -101,7 +105,7 @@ __device__ __forceinline__ void nearest_hit(const DevScene &S, v3 o, v3 d, v3 pe
     }
     // faces beyond the first 64 records: list order with the same skip test
     for (int f = nmask; f < nf; f++) {
-        if (box_enter(S, f, ox, oy, oz, ix, iy, iz) > (float)len * 1.000001f + 1e-4f) continue;
+        if (box_enter(S, f, ox, oy, oz, ix, iy, iz, ux, uy, uz) > (float)len * 1.000001f + 1e-4f) continue;
         int l = S.face_list[f];
         if (l < 0 || l >= S.n_lists) {
             atomicOr(err, ERR_SHAPE_STACK);
