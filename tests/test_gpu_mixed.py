@@ -108,3 +108,38 @@ def test_mixed_path_on_every_face_and_material_case(name):
     if st["position_nm"]["p99"] is not None:
         assert st["position_nm"]["p99"] < ZOO_POSITION_NM_P99, st
         assert st["opl_nm"]["p99"] < ZOO_OPL_NM_P99, st
+
+
+def _served_mix_rays(n, seed):
+    """A point source 200 mm before a served-mix system (directions uniform
+    in a 0.05 rad cone, three wavelengths), as the job server's sources."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    th = 0.05 * np.sqrt(rng.uniform(size=n))
+    ph = rng.uniform(0.0, 2.0 * np.pi, n)
+    d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], axis=1)
+    e = np.cross(np.array([0.0, 1.0, 0.0]), d)
+    e /= np.linalg.norm(e, axis=1)[:, None]
+    rays = W.fill_rays(np.zeros(n, dtype=ctracer.ray_dtype), np.tile([0.0, 0.0, -200.0], (n, 1)), d, e)
+    rays["wavelength_idx"] = rng.integers(0, 3, n)
+    return rays, np.array([0.45, 0.6, 0.9])
+
+
+@pytest.mark.parametrize("n_elements", [10, 20])
+def test_mixed_path_on_served_mix_lens_trains(n_elements):
+    """Lens trains of the served mix (21 and 41 faces: spherical, conic,
+    aspheric and plane surfaces; above 32 faces the search keeps FP16 box
+    entries, and conic faces enter at the nearer of their two sheet boxes)
+    against the FP64 oracle: every hit face, parent and generation size equal,
+    positions and optical paths within the precision form's bounds."""
+    spec = W.config5_system(np.random.Generator(np.random.PCG64(100 + n_elements)), n_elements)
+    rays, wl = _served_mix_rays(4096, 7 + n_elements)
+    P = {"recursion_limit": 8, "max_length": 1000.0, "e2_terminate": 1e-6}
+    gens = mixed_trace(spec, rays, wl, P)
+    tables, _, _ = tables_for(spec)
+    ogens = oracle_trace_parallel(tables, wl, rays, P["recursion_limit"], P["max_length"], P["e2_terminate"])
+    st = precision.compare_traces(gens, ogens)
+    print("served mix", n_elements, st)
+    assert st["generation_sizes_equal"], ([len(g) for g in gens], [len(g) for g in ogens])
+    assert st["index_agreement"] == 1.0, st
+    assert st["position_nm"]["max"] <= POSITION_NM_MAX, st
+    assert st["opl_nm"]["max"] <= OPL_NM_MAX, st
