@@ -1859,8 +1859,12 @@ __device__ __forceinline__ mx::Best nearest_mx(const GenArgs &A, const DevScene 
 // conversions cost about 2 % of the search on an 11-face scene; a 41-face
 // scene's search takes 15 % less with it than re-entering the boxes.
 #define RP_MX_TB_F32_FACES 32
+// (The form with the FP64 fallback is compiled for two blocks per SM: the
+// scenes that need it hold two by shared memory already -- the 64-face clutter
+// scene, 109 KB a block -- and at 255 registers it spills 0.3 instead of 1.4 KB
+// a thread: 797 against 834 ms per 1M-ray clutter step.)
 template <bool FB, typename TbT>
-__global__ void __launch_bounds__(RP_BLOCK, MX_SEARCH_MIN_BLOCKS)
+__global__ void __launch_bounds__(RP_BLOCK, FB ? 2 : MX_SEARCH_MIN_BLOCKS)
     mixed_search_kernel(GenArgs A, unsigned mx_off, unsigned tb_off, unsigned in_off, unsigned pass_off) {
     using namespace mx;
     extern __shared__ __align__(16) unsigned char smem[];
